@@ -1,0 +1,144 @@
+"""ctypes binding of libbx.so (declarations mirror ``include/bx.h``).
+
+The library is the only compute path: if it is missing or fails to load, every
+entry point raises ``BxLibraryError`` -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libbx.so')
+
+MAX_IONS = 8
+BX_OK = 0
+BX_EINVAL = -22
+BX_ENOMEM = -12
+BX_ECUDA = -5
+BX_EUNSTABLE = -1001
+BX_ESTATE = -1002
+PLAIN_FP64 = 0
+SPLIT_FP32 = 1
+
+_dp = ct.POINTER(ct.c_double)
+_ip = ct.POINTER(ct.c_int32)
+_u8p = ct.POINTER(ct.c_uint8)
+
+
+class BxLibraryError(RuntimeError):
+    """libbx.so is missing, failed to load or a call failed."""
+
+
+class BxGeom(ct.Structure):
+    _fields_ = [('n_cells', ct.c_int32), ('n_mems', ct.c_int32),
+                ('grid_ny', ct.c_int32), ('grid_nx', ct.c_int32),
+                ('cell_mem_ptr', _ip), ('nn_i', _ip), ('bflag', _u8p),
+                ('map_mem2ecm', _ip), ('mem_sa', _dp), ('mem_nx', _dp),
+                ('mem_ny', _dp), ('gj_weight', _dp),
+                ('smooth_weight_mem', _dp), ('smooth_weight_o', _dp),
+                ('cell_vol', _dp), ('cell_sa', _dp), ('diviterm', _dp),
+                ('mem_sa_per_env', _dp), ('gj_len', ct.c_double),
+                ('delta', ct.c_double)]
+
+
+class BxParams(ct.Structure):
+    _fields_ = [('n_ions', ct.c_int32), ('iNa', ct.c_int32), ('iK', ct.c_int32),
+                ('is_ecm', ct.c_int32)] + \
+        [(n, ct.c_double) for n in (
+            'F', 'R', 'T', 'dt', 'cm', 'tm', 'gj_surface', 'gj_block',
+            'nakatp_block', 'alpha_NaK', 'KmNK_Na', 'KmNK_K', 'KmNK_ATP', 'cATP',
+            'cADP', 'cPi', 'deltaGATP', 'vol_env', 'cell_height', 'q', 'kb', 'eo',
+            'er', 'sharpness', 'cell_radius', 'true_cell_size', 'ko_env', 'sigma',
+            'mu')] + \
+        [('zs', ct.c_double * MAX_IONS), ('D_free', ct.c_double * MAX_IONS),
+         ('D_gj', ct.c_double * MAX_IONS), ('c_env_bound', ct.c_double * MAX_IONS)]
+
+
+class BxState(ct.Structure):
+    _fields_ = [('vm', _dp), ('cc_cells', _dp), ('cc_at_mem', _dp),
+                ('cc_env', _dp), ('E_env_x', _dp), ('E_env_y', _dp)]
+
+
+OUTPUT_FIELDS = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn',
+                 'I_mem', 'J_cell_x', 'J_cell_y', 'Jc', 'vm_ave', 'dvm',
+                 'E_cell_x', 'E_cell_y', 'Emc', 'E_gj_x', 'E_gj_y', 'gjopen',
+                 'sigma_cell', 'fluxes_env_x', 'fluxes_env_y', 'rho_env', 'v_env']
+
+
+class BxOutputs(ct.Structure):
+    _fields_ = [(n, _dp) for n in OUTPUT_FIELDS]
+
+
+class BxStepStatus(ct.Structure):
+    _fields_ = [('steps_done', ct.c_int64), ('nan_vm', ct.c_int32),
+                ('nan_conc', ct.c_int32), ('neg_clamped', ct.c_int64),
+                ('unstable', ct.c_int32), ('precision', ct.c_int32)]
+
+
+# every symbol include/bx.h declares: name -> (restype, argtypes)
+SIGNATURES = {
+    'bx_cluster_create': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_int,
+                                     ct.POINTER(ct.c_void_p)]),
+    'bx_destroy': (None, [ct.c_void_p]),
+    'bx_set_membrane_diffusivity': (ct.c_int, [ct.c_void_p, _dp]),
+    'bx_set_env_diffusivity': (ct.c_int, [ct.c_void_p, _dp]),
+    'bx_set_boundary_potential': (ct.c_int, [ct.c_void_p, _dp]),
+    'bx_set_params': (ct.c_int, [ct.c_void_p, ct.POINTER(BxParams)]),
+    'bx_state_upload': (ct.c_int, [ct.c_void_p, ct.POINTER(BxState)]),
+    'bx_state_download': (ct.c_int, [ct.c_void_p, ct.POINTER(BxState)]),
+    'bx_step': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p]),
+    'bx_outputs_download': (ct.c_int, [ct.c_void_p, ct.POINTER(BxOutputs)]),
+    'bx_status': (ct.c_int, [ct.c_void_p, ct.POINTER(BxStepStatus)]),
+    'bx_env_fields': (ct.c_int, [ct.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    'bx_dense_apply_f64': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int,
+                                      ct.c_int, ct.c_void_p]),
+    'bx_abi_version': (ct.c_int, []),
+    'bx_last_error': (ct.c_char_p, []),
+    'bx_launch_count': (ct.c_int64, [ct.c_void_p]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libbx.so (once) and declare its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise BxLibraryError(
+            f'{path} is missing: build it with betse_gb300.build.build() '
+            '(there is no CPU fallback for the step)')
+    try:
+        lib = ct.CDLL(path)
+    except OSError as e:
+        raise BxLibraryError(f'cannot load {path}: {e}') from e
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc != BX_OK:
+        msg = load().bx_last_error()
+        msg = msg.decode() if msg else ''
+        raise BxLibraryError(f'{what} failed ({rc}): {msg}')
+
+
+def dptr(a):
+    """double* of a C-contiguous float64 numpy array (or None)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_ip)
+
+
+def u8ptr(a):
+    return a.ctypes.data_as(_u8p)

@@ -1,0 +1,232 @@
+// bx_env.cuh -- environment-grid kernels (extracellular spaces and fields).
+//
+// The grid is row-major (ny, nx), k = i*nx + j, as FiniteDiffSolver.cell_grid
+// lays it out (betse/science/math/finitediff.py:158-250).  Each kernel is one
+// thread per grid cell; the work is a few hundred bytes per cell, HBM- or
+// launch-bound, and runs inside the step's CUDA graph.
+#pragma once
+#include "bx_kernels.cuh"
+
+namespace bx {
+
+struct EnvConst {
+  int I, ny, nx, G;
+  double delta, inv_delta, inv_2delta, dt, sharpness;
+  double np_alpha[kMaxIons];   // z q / (kb T)  (times D_env per cell)
+  double zF[kMaxIons];
+  double c_bound[kMaxIons];
+  double surf_scale;           // cell_height delta^2 / mean(memSa_per_envSquare[map])
+  double inv_koeoer;           // 1 / (ko_env eo er)
+  double screen;               // (2/(ko_env delta)) (cell_radius/true_cell_size)
+  double inv_h_d2;             // 1 / (cell_height delta^2)
+  double gw[9];                // Gaussian taps, sigma 1, radius 4
+};
+
+__device__ __forceinline__ bool on_edge(int i, int j, int ny, int nx) {
+  return i == 0 || j == 0 || i == ny - 1 || j == nx - 1;
+}
+
+// Boundary-set concentration (update_ecm sets the four edges, sim.py:2214-2217)
+__device__ __forceinline__ double cb_at(const double* c, const EnvConst& e, int ion, int i, int j) {
+  return on_edge(i, j, e.ny, e.nx) ? e.c_bound[ion] : c[(size_t)ion * e.G + i * e.nx + j];
+}
+
+// Nernst-Planck flux on the grid (update_ecm, sim.py:2219-2242;
+// stb.nernst_planck_flux, sim_toolbox.py:385-413) with fd.gradient
+// (finitediff.py:1236-1266).  E_env is the previous update_V's field.
+__global__ void k_env_np_flux(const double* __restrict__ cenv, const double* __restrict__ Denv,
+                              const double* __restrict__ Ex, const double* __restrict__ Ey,
+                              double* fx, double* fy, EnvConst e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e.G) return;
+  const int i = k / e.nx, j = k - i * e.nx;
+  for (int ion = 0; ion < e.I; ++ion) {
+    const double c0 = cb_at(cenv, e, ion, i, j);
+    double gcx, gcy;
+    if (j == 0) gcx = (cb_at(cenv, e, ion, i, 1) - c0) / e.delta;
+    else if (j == e.nx - 1) gcx = (c0 - cb_at(cenv, e, ion, i, j - 1)) / e.delta;
+    else gcx = -(cb_at(cenv, e, ion, i, j - 1) - cb_at(cenv, e, ion, i, j + 1)) / (2 * e.delta);
+    if (i == 0) gcy = (cb_at(cenv, e, ion, 1, j) - c0) / e.delta;
+    else if (i == e.ny - 1) gcy = (c0 - cb_at(cenv, e, ion, i - 1, j)) / e.delta;
+    else gcy = -(cb_at(cenv, e, ion, i - 1, j) - cb_at(cenv, e, ion, i + 1, j)) / (2 * e.delta);
+    const double D = Denv[(size_t)ion * e.G + k];
+    const double alpha = D * e.np_alpha[ion];
+    const double gvx = -Ex[k], gvy = -Ey[k];
+    fx[(size_t)ion * e.G + k] = -D * gcx - alpha * gvx * c0;
+    fy[(size_t)ion * e.G + k] = -D * gcy - alpha * gvy * c0;
+  }
+}
+
+// fd.diff with the reference's flipped one-sided edge signs (finitediff.py:1268-1303)
+__device__ __forceinline__ double ddx_neg(const double* f, const EnvConst& e, int i, int j) {
+  // diff(-f, axis=0)
+  const double* r = f + i * e.nx;
+  if (j == 0) return ((-r[0]) - (-r[1])) / e.delta;
+  if (j == e.nx - 1) return ((-r[j - 1]) - (-r[j])) / e.delta;
+  return -((-r[j - 1]) - (-r[j + 1])) / (2 * e.delta);
+}
+__device__ __forceinline__ double ddy_neg(const double* f, const EnvConst& e, int i, int j) {
+  // diff(-f, axis=1)
+  const int nx = e.nx;
+  if (i == 0) return -((-f[nx + j]) - (-f[j])) / e.delta;
+  if (i == e.ny - 1) return -((-f[i * nx + j]) - (-f[(i - 1) * nx + j])) / e.delta;
+  return -((-f[(i - 1) * nx + j]) - (-f[(i + 1) * nx + j])) / (2 * e.delta);
+}
+
+// c <- cb + div(-f) dt  [+ membrane exchange if FUSE_SCATTER]
+// (update_ecm sim.py:2247-2254, then update_Co's ECM term sim_toolbox.py:1189-1195
+//  with div_env = M_divmap_mem2ecm @ (-flux) / (cell_height delta^2), :1229-1232)
+template <bool FUSE_SCATTER>
+__global__ void k_env_update(double* cenv, double* tmp, const double* __restrict__ fx,
+                             const double* __restrict__ fy, const int* __restrict__ env_ptr,
+                             const int* __restrict__ env_mem, const double* __restrict__ mem_flux_sa,
+                             int M, EnvConst e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e.G) return;
+  const int i = k / e.nx, j = k - i * e.nx;
+  for (int ion = 0; ion < e.I; ++ion) {
+    const double* fxi = fx + (size_t)ion * e.G;
+    const double* fyi = fy + (size_t)ion * e.G;
+    const double div = ddx_neg(fxi, e, i, j) + ddy_neg(fyi, e, i, j);
+    double c = cb_at(cenv, e, ion, i, j) + div * e.dt;
+    if (FUSE_SCATTER) {
+      double s = 0.0;
+      for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
+      c = c + (s * e.inv_h_d2) * e.dt;
+      cenv[(size_t)ion * e.G + k] = c;
+    } else {
+      tmp[(size_t)ion * e.G + k] = c;
+    }
+  }
+}
+
+// fd.integrator (finitediff.py:1479-1512) when sharpness < 1, then the membrane exchange.
+__global__ void k_env_integrate_scatter(double* cenv, const double* __restrict__ tmp,
+                                        const int* __restrict__ env_ptr, const int* __restrict__ env_mem,
+                                        const double* __restrict__ mem_flux_sa, int M, EnvConst e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e.G) return;
+  const int i = k / e.nx, j = k - i * e.nx;
+  const double sides = (1 - e.sharpness) / 4;
+  for (int ion = 0; ion < e.I; ++ion) {
+    const double* P = tmp + (size_t)ion * e.G;
+    double F;
+    if (on_edge(i, j, e.ny, e.nx)) {
+      F = P[k];
+    } else {
+      F = e.sharpness * P[k];
+      F += sides * P[k + e.nx];
+      F += sides * P[k - e.nx];
+      F += sides * P[k + 1];
+      F += sides * P[k - 1];
+    }
+    double s = 0.0;
+    for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
+    cenv[(size_t)ion * e.G + k] = F + (s * e.inv_h_d2) * e.dt;
+  }
+}
+
+// get_current ECM branch (ion_current.py:79-110): environment charge on the
+// membrane-touched grid cells -> v, then the axis-0 pass of a sigma=1 Gaussian
+// with zero padding (scipy mode='constant').
+__global__ void k_env_charge_gauss_y(const double* __restrict__ cenv, const uint8_t* __restrict__ touched,
+                                     double* rho_env, double* tmp, EnvConst e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e.G) return;
+  const int i = k / e.nx, j = k - i * e.nx;
+  double acc = 0.0;
+  for (int q = -4; q <= 4; ++q) {
+    const int ii = i + q;
+    if (ii < 0 || ii >= e.ny) continue;
+    const int kk = ii * e.nx + j;
+    double v = 0.0;
+    if (touched[kk]) {
+      double rho = 0.0;
+      for (int ion = 0; ion < e.I; ++ion) rho += e.zF[ion] * cenv[(size_t)ion * e.G + kk];
+      v = (rho * e.surf_scale) * e.inv_koeoer;
+    }
+    acc += e.gw[q + 4] * v;
+  }
+  tmp[k] = acc;
+  if (rho_env) {
+    double rho = 0.0;
+    for (int ion = 0; ion < e.I; ++ion) rho += e.zF[ion] * cenv[(size_t)ion * e.G + k];
+    rho_env[k] = rho;
+  }
+}
+
+// axis-1 pass of the Gaussian (+ Phi_b) -> v_env
+__global__ void k_env_gauss_x(const double* __restrict__ tmp, const double* __restrict__ phib,
+                              double* venv, EnvConst e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e.G) return;
+  const int i = k / e.nx, j = k - i * e.nx;
+  double acc = 0.0;
+  for (int q = -4; q <= 4; ++q) {
+    const int jj = j + q;
+    if (jj < 0 || jj >= e.nx) continue;
+    acc += e.gw[q + 4] * tmp[i * e.nx + jj];
+  }
+  venv[k] = acc + (phib ? phib[k] : 0.0);
+}
+
+// E = -gradient(scale * F)  (fd.gradient, finitediff.py:1236-1266)
+__global__ void k_env_neg_grad(const double* __restrict__ F, double scale, double* Ex, double* Ey,
+                               EnvConst e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e.G) return;
+  const int i = k / e.nx, j = k - i * e.nx;
+  const int nx = e.nx;
+  auto f = [&](int a, int bb) { return scale * F[a * nx + bb]; };
+  double gx, gy;
+  if (j == 0) gx = (f(i, 1) - f(i, 0)) / e.delta;
+  else if (j == nx - 1) gx = (f(i, j) - f(i, j - 1)) / e.delta;
+  else gx = -(f(i, j - 1) - f(i, j + 1)) / (2 * e.delta);
+  if (i == 0) gy = (f(1, j) - f(0, j)) / e.delta;
+  else if (i == e.ny - 1) gy = (f(i, j) - f(i - 1, j)) / e.delta;
+  else gy = -(f(i - 1, j) - f(i + 1, j)) / (2 * e.delta);
+  Ex[k] = -gx;
+  Ey[k] = -gy;
+}
+
+// ---------------------------------------------------------------------------
+// Dense FP64 products Y[n x R] = A[n x n] X[n x R], R <= 4 (row-major).
+// One warp per row; the row streams from HBM with 16-byte loads, X is
+// L2-resident.  The HBM-bound form of np.dot(lapENVinv, .).
+// ---------------------------------------------------------------------------
+template <int R>
+__global__ void __launch_bounds__(256) k_dense_rows(const double* __restrict__ A, const double* __restrict__ X,
+                                                    double* __restrict__ Y, int n) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* row = A + (size_t)warp * n;
+  double acc[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) acc[r] = 0.0;
+  const bool al16 = ((reinterpret_cast<uintptr_t>(row) & 15) == 0);
+  int k0 = 0;
+  if (al16) {
+    const int n2 = n >> 1;
+    const double2* row2 = reinterpret_cast<const double2*>(row);
+    for (int q = lane; q < n2; q += 32) {
+      const double2 a = __ldcs(row2 + q);
+      const int kk = 2 * q;
+#pragma unroll
+      for (int r = 0; r < R; ++r) acc[r] += a.x * X[(size_t)kk * R + r] + a.y * X[(size_t)(kk + 1) * R + r];
+    }
+    k0 = 2 * n2;
+  }
+  for (int kk = k0 + lane; kk < n; kk += 32) {
+    const double a = row[kk];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] += a * X[(size_t)kk * R + r];
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const double s = warp_sum(acc[r]);
+    if (lane == 0) Y[(size_t)warp * R + r] = s;
+  }
+}
+
+}  // namespace bx

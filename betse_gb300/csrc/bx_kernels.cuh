@@ -1,0 +1,392 @@
+// bx_kernels.cuh -- sm_103a kernels of the cell-network electrodiffusion step.
+//
+// Data layout in HBM (structure of arrays, row = ion):
+//   per membrane : Dm[I][M] (FP64 or FP32), vm[2][M] FP64 ping-pong,
+//                  m2c, nn, nn_cell, map_env (int32), bflag (u8),
+//                  mem_sa, gj_w (FP64 or FP32)
+//   per cell     : cc_cells[I][C] FP64 (post-GJ, clamped; owned by one CTA),
+//                  cc_mem[2][I][C] FP64 ping-pong (the value BETSE broadcasts
+//                  to cc_at_mem: cells + membrane term, before the GJ term),
+//                  cell_vol, diviterm (FP64), cell_mem_ptr (int32)
+//   per CTA      : blk_cell[nblk+1] (host-built partition of whole cells with
+//                  at most TPB membranes), env partial sums [nblk][I]
+//
+// One CTA owns a contiguous run of whole cells, so every segment sum over a
+// cell's membranes (BETSE's dense M_sum_mems products) is a fixed-order sum in
+// shared memory: deterministic, no atomics.  Gap-junction partners are read
+// from the previous step's ping-pong buffers, so CTAs never wait on each other.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bx {
+
+constexpr int kMaxIons = 8;
+constexpr double kNonce = 1.0e-25;   // sim_toolbox.py:52
+
+struct DevGeom {
+  int C, M, I, G, ny, nx;
+  const int* cell_ptr;    // [C+1]
+  const int* m2c;         // [M]
+  const int* nn;          // [M]
+  const int* nn_cell;     // [M] = m2c[nn]
+  const uint8_t* bflag;   // [M]
+  const int* map_env;     // [M]
+  const double* mem_sa;   // [M] FP64 copy
+  const float* mem_sa_f;  // [M] FP32 copy (split form)
+  const double* gj_w;     // [M]
+  const float* gj_w_f;    // [M]
+  const double* mem_nx;   // [M]
+  const double* mem_ny;   // [M]
+  const double* sw_mem;   // [M]
+  const double* sw_o;     // [M]
+  const double* cell_vol; // [C]
+  const double* cell_sa;  // [C]
+  const double* diviterm; // [C]
+  const int* blk_cell;    // [nblk+1]
+};
+
+// Per-step constants (kernel parameter, passed by value).
+struct StepConst {
+  int I, iNa, iK;
+  int zcode[kMaxIons];     // +1,-1,+2,-2 fast paths; 0 = generic z
+  double z[kMaxIons];
+  double zF[kMaxIons];     // z*F
+  double sig_coef[kMaxIons]; // z^2 F^2 D_free 0.1 / (R T)
+  double dgj_gs[kMaxIons]; // D_gj * gj_surface
+  double F_RT;             // F / (R T)
+  double dt, inv_cm, tm, gj_len;
+  double gj_block;
+  double pump_coef;        // -3 * block * alpha_NaK
+  double inv_KmNa, inv_KmK, atp_term; // 1/Km, (cATP/KmATP)
+  double atp_den;          // 1 + cATP/KmATP
+  double qnum_c;           // (cADP*1e-3)*(cPi*1e-3)
+  double qden_c;           // cATP*1e-3
+  double K0;               // exp(-deltaGATP / (R T))
+  double pump_on;          // alpha_NaK > 0
+  double env_scale;        // dt / (vol_env * M): no-ECM well-mixed update
+  double inv_h_d2_dt;      // dt / (cell_height * delta^2): ECM membrane->grid
+};
+
+struct StepPtrs {
+  const double* vm_in;  double* vm_out;
+  const double* ccm_in; double* ccm_out;   // [I][C] membrane-side concentrations
+  double* cc;                              // [I][C] cell concentrations (in place)
+  const double* Dm;                        // [I][M] FP64 (plain form)
+  const float* Dm_f;                       // [I][M] FP32 (split form)
+  const double* cenv;                      // [I] (no ECM) or [I][G] (ECM)
+  const double* phib;                      // [G] or nullptr
+  double* env_part;                        // [nblk][I] partial sums (no ECM)
+  double* mem_flux_sa;                     // [I][M] f_mem*sa (ECM scatter input)
+  unsigned long long* status;              // [4]: nan_vm, nan_conc, neg clamps, spare
+  // outputs (OUT variant)
+  double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_Jn;
+  double* o_Imem; double* o_Jcx; double* o_Jcy; double* o_Jc; double* o_vmave;
+  double* o_dvm; double* o_Ecx; double* o_Ecy; double* o_Emc; double* o_Egjx;
+  double* o_Egjy; double* o_gjopen; double* o_sigma;
+};
+
+// ---------------------------------------------------------------------------
+// math helpers
+// ---------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T bx_expm1(T x);
+template <> __device__ __forceinline__ double bx_expm1<double>(double x) { return expm1(x); }
+template <> __device__ __forceinline__ float bx_expm1<float>(float x) { return expm1f(x); }
+template <typename T> __device__ __forceinline__ T bx_exp(T x);
+template <> __device__ __forceinline__ double bx_exp<double>(double x) { return exp(x); }
+template <> __device__ __forceinline__ float bx_exp<float>(float x) { return expf(x); }
+
+// Shared exponentials of one GHK voltage: alpha1 = (v + nonce) F/(RT) for a
+// unit charge; every |z| in {1,2} flux is derived from expm1(-alpha1).
+template <typename T>
+struct GhkShared {
+  T a1, em1, e1, r, q2;
+  __device__ __forceinline__ void init(double v_nonce, double F_RT) {
+    a1 = (T)(v_nonce * F_RT);
+    em1 = bx_expm1<T>(-a1);         // expm1(-alpha1)
+    e1 = (T)1 + em1;                // exp(-alpha1)
+    r = (T)1 / em1;
+    q2 = (T)1 / ((T)2 + em1);
+  }
+};
+
+// GHK flux of sim_toolbox.electroflux (sim_toolbox.py:18-69) for charge z,
+// written in terms of the shared exponentials:
+//   f = -(Dc*alpha/d) * (cB - cA*exp(-alpha)) / (-expm1(-alpha)),
+//   alpha = z*alpha1.  Exact identities give, with e1 = exp(-alpha1),
+//   em1 = expm1(-alpha1):
+//   z=+1: (Dc a1/d)(cB - cA e1)/em1          z=-1: (Dc a1/d)(cB e1 - cA)/em1
+//   z=+2: 2(Dc a1/d)(cB - cA e1^2)/(em1(2+em1))
+//   z=-2: 2(Dc a1/d)(cB e1^2 - cA)/(em1(2+em1))
+template <typename T>
+__device__ __forceinline__ T ghk_flux(const GhkShared<T>& s, int zcode, double zval,
+                                      double v_nonce, double F_RT, T cA, T cB, T Dc, T inv_d) {
+  const T k = Dc * s.a1 * inv_d;
+  switch (zcode) {
+    case 1:  return k * (cB - cA * s.e1) * s.r;
+    case -1: return k * (cB * s.e1 - cA) * s.r;
+    case 2:  { T e2 = s.e1 * s.e1; return (T)2 * k * (cB - cA * e2) * s.r * s.q2; }
+    case -2: { T e2 = s.e1 * s.e1; return (T)2 * k * (cB * e2 - cA) * s.r * s.q2; }
+    default: {
+      // generic charge: ((z + nonce) * vBA * F) / (R T), then the formula as is
+      T a = (T)(((zval + kNonce) * v_nonce) * F_RT);
+      T ea = bx_exp<T>(-a);
+      T den = -bx_expm1<T>(-a);
+      return -((Dc * a) * inv_d) * ((cB - cA * ea) / den);
+    }
+  }
+}
+
+// Na/K-ATPase (sim_toolbox.pumpNaKATP, sim_toolbox.py:71-122), rearranged to
+// one division: f_Na = -3 block alpha fwd (1 - Q/Keq) with Keq = K0/e1,
+// e1 = exp(-F V/(R T)) shared with the GHK fluxes.
+template <typename T>
+__device__ __forceinline__ T pump_fna(const StepConst& k, T e1, T cNai, T cNao, T cKi, T cKo) {
+  const T nai = cNai * (T)1e-3, nao = cNao * (T)1e-3, ki = cKi * (T)1e-3, ko = cKo * (T)1e-3;
+  const T qnum = (T)k.qnum_c * (nao * nao * nao) * (ki * ki);
+  T qden = (T)k.qden_c * (nai * nai * nai) * (ko * ko);
+  if (qden == (T)0) qden = (T)1.0e-15;
+  const T xna = cNai * (T)k.inv_KmNa, xk = cKo * (T)k.inv_KmK;
+  const T na3 = xna * xna * xna, k2 = xk * xk;
+  const T num_e = na3 * k2 * (T)k.atp_term;
+  const T den_e = ((T)1 + na3) * ((T)1 + k2) * (T)k.atp_den;
+  // fwd * (1 - Q/Keq) = num_e (qden K0 - qnum e1) / (den_e qden K0)
+  const T K0 = (T)k.K0;
+  return (T)k.pump_coef * num_e * (qden * K0 - qnum * e1) / (den_e * qden * K0);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// The fused cell step.  TPB threads = TPB membrane slots of one CTA.
+//   T   : arithmetic type of fluxes and pumps (double: plain, float: split)
+//   ECM : extracellular grid on (env gathered per membrane, f*sa exported)
+//   OUT : also compute the step outputs BETSE stores
+//   PHIB: subtract the boundary potential Phi_b[map_mem2ecm]
+// ---------------------------------------------------------------------------
+template <typename T, int TPB, bool ECM, bool OUT, bool PHIB>
+__global__ void __launch_bounds__(TPB)
+k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
+  extern __shared__ double smem[];
+  const int I = k.I;
+  double* sA = smem;                    // [I][TPB] f_mem*sa
+  double* sB = sA + I * TPB;            // [I][TPB] -f_gj*sa
+  double* sV = sB + I * TPB;            // [TPB]   per-cell Vmem (by local cell)
+  double* sX = sV + TPB;                // [4][TPB] output scratch
+
+  const int b = blockIdx.x;
+  const int c0 = g.blk_cell[b], c1 = g.blk_cell[b + 1];
+  const int m0 = g.cell_ptr[c0], m1 = g.cell_ptr[c1];
+  const int t = threadIdx.x;
+  const int m = m0 + t;
+  const bool active = m < m1;
+  const T inv_tm = (T)(1.0 / k.tm);
+  const T inv_gjl = (T)(1.0 / k.gj_len);
+
+  double env_acc[kMaxIons];
+#pragma unroll
+  for (int i = 0; i < kMaxIons; ++i) env_acc[i] = 0.0;
+
+  double v = 0.0, vgj = 0.0;
+  int c = 0, lc = 0;
+  T fmem_o[kMaxIons], fgj_o[kMaxIons];
+  T rate_o = (T)0;
+  if (active) {
+    v = p.vm_in[m];
+    c = g.m2c[m];
+    lc = c - c0;
+    const int nn = g.nn[m];
+    const int cn = g.nn_cell[m];
+    const double vn = p.vm_in[nn];
+    const bool bnd = g.bflag[m] != 0;
+    // BETSE adds 1e-25 to vm in place in each electroflux call (sim_toolbox.py:54);
+    // for |vm| > 1e-8 V the addition is below one ulp, so every ion sees v1.
+    const double v1 = v + kNonce;
+    vgj = (vn + kNonce) - v1;                   // update_gj, sim.py:2166
+    const double vgj1 = vgj + kNonce;
+    GhkShared<T> sm, sg;
+    sm.init(v1, k.F_RT);
+    sg.init(vgj1, k.F_RT);
+    double msa;
+    T msa_t, gjw_t;
+    if constexpr (sizeof(T) == 8) { msa = g.mem_sa[m]; msa_t = (T)msa; gjw_t = (T)g.gj_w[m]; }
+    else { msa_t = (T)g.mem_sa_f[m]; msa = (double)msa_t; gjw_t = (T)g.gj_w_f[m]; }
+    const int ge = ECM ? g.map_env[m] : 0;
+
+    // Na/K-ATPase first, on the start-of-step concentrations (sim.py:1196-1234)
+    T fNa = (T)0;
+    if (k.pump_on != 0.0) {
+      const T cNai = (T)p.ccm_in[k.iNa * g.C + c];
+      const T cKi = (T)p.ccm_in[k.iK * g.C + c];
+      const T cNao = (T)(ECM ? p.cenv[k.iNa * g.G + ge] : p.cenv[k.iNa]);
+      const T cKo = (T)(ECM ? p.cenv[k.iK * g.G + ge] : p.cenv[k.iK]);
+      // the pump sees vm before any nonce (it runs before the ion loop);
+      // e1 of v1 equals exp(-F vm/(R T)) for |vm| > 1e-8 V
+      fNa = pump_fna<T>(k, sm.e1, cNai, cNao, cKi, cKo);
+    }
+    rate_o = -fNa;
+    for (int i = 0; i < I; ++i) {
+      const T cin = (T)p.ccm_in[i * g.C + c];
+      const T cout = (T)(ECM ? p.cenv[i * g.G + ge] : p.cenv[i]);
+      T dm;
+      if constexpr (sizeof(T) == 8) dm = (T)p.Dm[(size_t)i * g.M + m];
+      else dm = p.Dm_f[(size_t)i * g.M + m];
+      T f = ghk_flux<T>(sm, k.zcode[i], k.z[i], v1, k.F_RT, cout, cin, dm, inv_tm);
+      if (i == k.iNa) f = fNa + f;
+      else if (i == k.iK) f = (T)(-(2.0 / 3.0)) * fNa + f;
+      // gap junction (sim.py:2189-2206): from this membrane's cell into the partner's
+      const T cn_i = (T)p.ccm_in[i * g.C + cn];
+      const T dgj = (T)k.dgj_gs[i] * (gjw_t * (T)k.gj_block);
+      T fg = ghk_flux<T>(sg, k.zcode[i], k.z[i], vgj1, k.F_RT, cin, cn_i, dgj, inv_gjl);
+      if (bnd) fg = (T)0;
+      const double a = (double)(f * msa_t);
+      sA[i * TPB + t] = a;
+      sB[i * TPB + t] = (double)(-fg * msa_t);
+      if (ECM) p.mem_flux_sa[(size_t)i * g.M + m] = a;
+      else env_acc[i] = a;
+      if (OUT) { fmem_o[i] = f; fgj_o[i] = fg; }
+    }
+    (void)msa;
+  } else {
+    for (int i = 0; i < I; ++i) { sA[i * TPB + t] = 0.0; sB[i * TPB + t] = 0.0; }
+  }
+
+  // no-ECM well-mixed environment: per-CTA partial sums of f_mem*sa per ion
+  if (!ECM) {
+    __shared__ double red[kMaxIons][TPB / 32];
+    for (int i = 0; i < I; ++i) {
+      double s = warp_sum(env_acc[i]);
+      if ((t & 31) == 0) red[i][t >> 5] = s;
+    }
+    __syncthreads();
+    if (t < I) {
+      double s = 0.0;
+      for (int w = 0; w < TPB / 32; ++w) s += red[t][w];
+      p.env_part[(size_t)b * I + t] = s;
+    }
+  }
+  __syncthreads();
+
+  // ---- cell phase: one thread per cell of this CTA (update_all_concs, update_V)
+  const int ncell = c1 - c0;
+  int bad_conc = 0, neg = 0;
+  if (t < ncell) {
+    const int cc = c0 + t;
+    const int a0 = g.cell_ptr[cc] - m0, a1 = g.cell_ptr[cc + 1] - m0;
+    const double vol = g.cell_vol[cc];
+    double rho = 0.0, sig = 0.0;
+    for (int i = 0; i < I; ++i) {
+      double s1 = 0.0, s2 = 0.0;
+      for (int j = a0; j < a1; ++j) { s1 += sA[i * TPB + j]; s2 += sB[i * TPB + j]; }
+      double x = p.cc[i * g.C + cc] + (s1 / vol) * k.dt;     // update_Co, sim_toolbox.py:1182-1183
+      p.ccm_out[i * g.C + cc] = x;                            // cc_at_mem = cX_cell[mem_to_cells]
+      x = x + k.dt * (s2 / vol);                              // gap-junction term, sim.py:2105-2108
+      if (x != x) bad_conc++;
+      if (x < 0.0) { x = 0.0; neg++; }                        // no_negs
+      p.cc[i * g.C + cc] = x;
+      rho += k.zF[i] * x;                                     // rho_cells, ion_current.py:19
+      if (OUT) sig += k.sig_coef[i] * x;
+    }
+    const double vcell = k.inv_cm * (rho * g.diviterm[cc]);   // sim.py:2027-2029
+    sV[t] = vcell;
+    if (OUT) { p.o_rho[cc] = rho; p.o_sigma[cc] = sig / (double)I; }
+  }
+  if (bad_conc) atomicAdd(&p.status[1], (unsigned long long)bad_conc);
+  if (neg) atomicAdd(&p.status[2], (unsigned long long)neg);
+  __syncthreads();
+
+  // ---- membrane phase 2: new Vmem
+  double vnew = 0.0;
+  if (active) {
+    vnew = sV[lc];
+    if (PHIB) vnew -= p.phib[g.map_env[m]];
+    p.vm_out[m] = vnew;
+    if (vnew != vnew) atomicAdd(&p.status[0], 1ull);
+  }
+
+  if constexpr (OUT) {
+    // fluxes, rate, Jn smoothing and cell currents (ion_current.py:19-47, sim.py:2031-2083)
+    double Jraw = 0.0;
+    if (active) {
+      for (int i = 0; i < I; ++i) {
+        p.o_fmem[(size_t)i * g.M + m] = (double)fmem_o[i];
+        p.o_fgj[(size_t)i * g.M + m] = (double)fgj_o[i];
+      }
+      double Jmem = 0.0, Jgj = 0.0;
+      for (int i = 0; i < I; ++i) { Jmem += k.zF[i] * (double)fmem_o[i]; Jgj += k.zF[i] * (double)fgj_o[i]; }
+      Jraw = -Jmem + Jgj;
+      p.o_rate[m] = (double)rate_o;
+      const double Egj = -vgj / k.gj_len;
+      p.o_Egjx[m] = Egj * g.mem_nx[m];
+      p.o_Egjy[m] = Egj * g.mem_ny[m];
+      p.o_gjopen[m] = k.gj_block * g.gj_w[m];
+      sX[t] = Jraw * g.mem_sa[m];
+      sX[TPB + t] = vnew;
+    } else { sX[t] = 0.0; sX[TPB + t] = 0.0; }
+    __syncthreads();
+    if (t < ncell) {
+      const int cc = c0 + t;
+      const int a0 = g.cell_ptr[cc] - m0, a1 = g.cell_ptr[cc + 1] - m0;
+      double s = 0.0, sv = 0.0;
+      for (int j = a0; j < a1; ++j) { s += sX[j]; sv += sX[TPB + j]; }
+      sV[t] = s / g.cell_sa[cc];              // Jn_ave
+      p.o_vmave[cc] = sv / (double)(a1 - a0);
+    }
+    __syncthreads();
+    double Jn = 0.0;
+    if (active) {
+      Jn = g.sw_mem[m] * Jraw + sV[lc] * g.sw_o[m];
+      p.o_Jn[m] = Jn;
+      p.o_Imem[m] = -Jn * g.mem_sa[m];
+      sX[2 * TPB + t] = Jn * g.mem_nx[m] * g.mem_sa[m];
+      sX[3 * TPB + t] = Jn * g.mem_ny[m] * g.mem_sa[m];
+      double vmo = v;
+      for (int i = 0; i < I; ++i) vmo += kNonce;
+      p.o_dvm[m] = (vnew - vmo) / k.dt;
+    } else { sX[2 * TPB + t] = 0.0; sX[3 * TPB + t] = 0.0; }
+    __syncthreads();
+    if (t < ncell) {
+      const int cc = c0 + t;
+      const int a0 = g.cell_ptr[cc] - m0, a1 = g.cell_ptr[cc + 1] - m0;
+      double sx = 0.0, sy = 0.0;
+      for (int j = a0; j < a1; ++j) { sx += sX[2 * TPB + j]; sy += sX[3 * TPB + j]; }
+      const double jx = sx / g.cell_sa[cc], jy = sy / g.cell_sa[cc];
+      p.o_Jcx[cc] = jx; p.o_Jcy[cc] = jy;
+      const double sg = p.o_sigma[cc];
+      p.o_Ecx[cc] = jx / sg; p.o_Ecy[cc] = jy / sg;
+      sA[t] = jx; sA[TPB + t] = jy; sB[t] = jx / sg; sB[TPB + t] = jy / sg;
+    }
+    __syncthreads();
+    if (active) {
+      const double nx = g.mem_nx[m], ny = g.mem_ny[m];
+      p.o_Jc[m] = sA[lc] * nx + sA[TPB + lc] * ny;
+      p.o_Emc[m] = sB[lc] * nx + sB[TPB + lc] * ny;
+    }
+  }
+}
+
+// No-ECM environment: the well-mixed value per ion (sim_toolbox.py:1196-1205)
+// c_env <- mean_m(c_env - f_m sa_m / vol_env * dt); fixed-order reduction.
+static __global__ void k_env_mix(const double* __restrict__ part, int nblk, int I,
+                          double* cenv, double env_scale) {
+  __shared__ double red[32];
+  for (int i = 0; i < I; ++i) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[(size_t)b * I + i];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+      cenv[i] = cenv[i] - tot * env_scale;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace bx

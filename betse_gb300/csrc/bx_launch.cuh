@@ -1,0 +1,36 @@
+// bx_launch.cuh -- host-side launchers of the templated step kernels; the
+// instantiations live in bx_step_f64.cu (plain form) and bx_step_f32.cu
+// (split form) so the two compile in parallel.
+#pragma once
+#include "bx_kernels.cuh"
+
+namespace bx {
+
+inline size_t cell_step_smem(int I, int tpb, bool out) {
+  return sizeof(double) * (size_t)tpb * (2 * (size_t)I + 1 + (out ? 4 : 0));
+}
+
+template <typename T, int TPB>
+cudaError_t launch_cell_step(bool ecm, bool out, bool phib, int nblk, cudaStream_t s,
+                             const DevGeom& g, const StepPtrs& p, const StepConst& k);
+
+#define BX_DEFINE_CELL_STEP_LAUNCHER(T, TPB)                                                    \
+  template <>                                                                                   \
+  cudaError_t launch_cell_step<T, TPB>(bool ecm, bool out, bool phib, int nblk, cudaStream_t s, \
+                                       const DevGeom& g, const StepPtrs& p, const StepConst& k) { \
+    const size_t sm = cell_step_smem(k.I, TPB, out);                                            \
+    const int code = (ecm ? 4 : 0) | (out ? 2 : 0) | (phib ? 1 : 0);                            \
+    switch (code) {                                                                             \
+      case 0: k_cell_step<T, TPB, false, false, false><<<nblk, TPB, sm, s>>>(g, p, k); break;  \
+      case 1: k_cell_step<T, TPB, false, false, true><<<nblk, TPB, sm, s>>>(g, p, k); break;   \
+      case 2: k_cell_step<T, TPB, false, true, false><<<nblk, TPB, sm, s>>>(g, p, k); break;   \
+      case 3: k_cell_step<T, TPB, false, true, true><<<nblk, TPB, sm, s>>>(g, p, k); break;    \
+      case 4: k_cell_step<T, TPB, true, false, false><<<nblk, TPB, sm, s>>>(g, p, k); break;   \
+      case 5: k_cell_step<T, TPB, true, false, true><<<nblk, TPB, sm, s>>>(g, p, k); break;    \
+      case 6: k_cell_step<T, TPB, true, true, false><<<nblk, TPB, sm, s>>>(g, p, k); break;    \
+      default: k_cell_step<T, TPB, true, true, true><<<nblk, TPB, sm, s>>>(g, p, k); break;    \
+    }                                                                                           \
+    return cudaGetLastError();                                                                  \
+  }
+
+}  // namespace bx

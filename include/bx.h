@@ -1,0 +1,216 @@
+/*
+ * bx.h -- C ABI of the GB300-native electrodiffusion step (libbx.so).
+ *
+ * One handle ("cluster") owns device copies of a cell cluster's index maps and
+ * geometry, its per-membrane channel diffusivities and its evolving state, and
+ * advances BETSE's full-solver time step on the GPU.  Every entry point
+ * returns 0 on success or a negative errno-style code (BX_E*); no C++
+ * exception crosses this boundary.  bx_last_error() gives a message for the
+ * last failure on the calling thread.  A handle is not thread-safe: drive each
+ * handle from one host thread.  All host pointers are plain arrays in the
+ * layouts documented below; none is retained after the call returns.
+ *
+ * Reference interfaces each entry point replaces (BETSE, pure Python):
+ *   bx_cluster_create   Cells index maps / geometry consumed by the step:
+ *                       cells.py:1126-1146 (mem_to_cells, cell_to_mems),
+ *                       cells.py:1498-1533 (nn_i), cells.py:1446 (bflags_mems),
+ *                       cells.py:1385-1390 (cell_vol, diviterm),
+ *                       cells.py:1150-1155 (cell_sa), cells.py:1758
+ *                       (map_mem2ecm), and Simulator.init_core/init_dynamics
+ *                       constants, sim.py:452-1012.
+ *   bx_set_membrane_diffusivity   sim.Dm_cells written by
+ *                       TissueHandler.init_profiles (tishandler.py:363-452).
+ *   bx_set_env_diffusivity        sim.D_env from Simulator.initDenv
+ *                       (sim.py:2347-2400).
+ *   bx_set_boundary_potential     sim.Phi_b = lapENVinv @ (-div_Jb)
+ *                       (physics/ion_current.py:100-102,164-169).
+ *   bx_state_upload / bx_state_download   the Simulator attributes vm,
+ *                       cc_cells, cc_at_mem, cc_env (sim.py:452-755).
+ *   bx_step             Simulator._run_sim_core_loop body, sim.py:1169-1363
+ *                       (pumpNaKATP, electroflux, update_gj, update_ecm,
+ *                       update_all_concs, update_V, check_v).
+ *   bx_outputs_download the per-step attributes write2storage reads
+ *                       (sim.py:1789-1884): fluxes_mem, fluxes_gj,
+ *                       rate_NaKATP, rho_cells, Jn, I_mem, J_cell_x/y, Jc,
+ *                       vm_ave, dvm, E_cell_x/y, Emc, E_gj_x/y, gjopen,
+ *                       sigma_cell.
+ *   bx_status           stb.check_v (sim_toolbox.py:332-344) and stb.no_negs
+ *                       (sim_toolbox.py:475-503): NaN and clamp counters.
+ *   bx_env_fields       get_current's environment branches
+ *                       (physics/ion_current.py:50-171): v_env, E_env_x/y,
+ *                       J_env_x/y, B_field with dense lapENVinv products.
+ *   bx_dense_apply      np.dot(cells.lapENVinv, .) / np.dot(cells.lapGJinv, .)
+ *                       (ion_current.py:90,170; sim_toolbox.py:1263,1284;
+ *                       physics/pressures.py:59).
+ */
+#ifndef BX_H
+#define BX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BX_ABI_VERSION 1
+#define BX_MAX_IONS 8
+#define BX_MAX_MEMS_PER_CELL 256
+
+/* error codes */
+#define BX_OK 0
+#define BX_EINVAL (-22)      /* bad argument or inconsistent geometry */
+#define BX_ENOMEM (-12)      /* device or host allocation failed */
+#define BX_ECUDA (-5)        /* a CUDA runtime call failed */
+#define BX_EUNSTABLE (-1001) /* NaN in Vmem or a concentration (check_v) */
+#define BX_ESTATE (-1002)    /* call out of order (e.g. step before upload) */
+
+/* precision forms of the step */
+#define BX_PLAIN_FP64 0 /* every flux, pump and sum in FP64 */
+#define BX_SPLIT_FP32 1 /* fluxes/pumps in FP32; sums, concentrations, Vmem FP64 */
+
+typedef struct bx_cluster* bx_handle;
+
+/* Cluster geometry and index maps.  Membranes of cell c are the contiguous
+ * range [cell_mem_ptr[c], cell_mem_ptr[c+1]) -- the CSR form of BETSE's
+ * cell_to_mems / mem_to_cells.  Arrays are host pointers, copied at create. */
+typedef struct bx_geom {
+    int32_t n_cells;
+    int32_t n_mems;
+    int32_t grid_ny, grid_nx;   /* environment grid (cells.X.shape); >= 3 each */
+    const int32_t* cell_mem_ptr; /* [n_cells+1] */
+    const int32_t* nn_i;         /* [n_mems] gap-junction partner (self at boundary) */
+    const uint8_t* bflag;        /* [n_mems] 1 = outer-boundary membrane */
+    const int32_t* map_mem2ecm;  /* [n_mems] environment grid index of each membrane */
+    const double* mem_sa;        /* [n_mems] membrane surface area (m^2) */
+    const double* mem_nx;        /* [n_mems] outward normal x (mem_vects_flat[:,2]) */
+    const double* mem_ny;        /* [n_mems] outward normal y (mem_vects_flat[:,3]) */
+    const double* gj_weight;     /* [n_mems] static gap-junction open fraction */
+    const double* smooth_weight_mem; /* [n_mems] Jn smoothing weights (sim.py:783-786) */
+    const double* smooth_weight_o;   /* [n_mems] */
+    const double* cell_vol;      /* [n_cells] */
+    const double* cell_sa;       /* [n_cells] */
+    const double* diviterm;      /* [n_cells] cell_vol / cell_sa */
+    const double* mem_sa_per_env; /* [grid] cells.memSa_per_envSquare (ECM only; may be NULL) */
+    double gj_len;               /* cells.gj_len (= p.cell_space) */
+    double delta;                /* environment grid spacing (cells.delta) */
+} bx_geom;
+
+/* Scalar parameters and per-ion constants (Parameters + Simulator fields). */
+typedef struct bx_params {
+    int32_t n_ions;
+    int32_t iNa, iK;             /* ion rows of Na+ and K+ */
+    int32_t is_ecm;              /* 1 = extracellular spaces on */
+    double F, R, T, dt, cm, tm;
+    double gj_surface, gj_block, nakatp_block;
+    double alpha_NaK, KmNK_Na, KmNK_K, KmNK_ATP, cATP, cADP, cPi, deltaGATP;
+    double vol_env;              /* well-mixed environment volume (no ECM) */
+    double cell_height, q, kb, eo, er, sharpness, cell_radius, true_cell_size;
+    double ko_env;               /* inverse Debye length of the environment (ECM) */
+    double sigma;                /* mean environment conductivity (no-ECM fields) */
+    double mu;                   /* magnetic permeability (B_field output) */
+    double zs[BX_MAX_IONS];
+    double D_free[BX_MAX_IONS];
+    double D_gj[BX_MAX_IONS];
+    double c_env_bound[BX_MAX_IONS]; /* Dirichlet value on the grid edge (ECM) */
+} bx_params;
+
+/* Host views of the evolving state, BETSE layouts (row = ion).
+ * cc_env is [n_ions] without ECM (one well-mixed value per ion; BETSE keeps a
+ * uniform vector of length n_mems) and [n_ions * grid] with ECM.
+ * cc_at_mem is [n_ions * n_mems]; it is constant over each cell's membranes
+ * in BETSE, and upload checks that.  E_env_x/y ([grid], ECM only) are the
+ * environment field from the previous update_V. */
+typedef struct bx_state {
+    double* vm;
+    double* cc_cells;
+    double* cc_at_mem;
+    double* cc_env;
+    double* E_env_x;
+    double* E_env_y;
+} bx_state;
+
+/* Host destinations for one step's outputs; any pointer may be NULL. */
+typedef struct bx_outputs {
+    double* fluxes_mem;   /* [n_ions * n_mems] */
+    double* fluxes_gj;    /* [n_ions * n_mems] */
+    double* rate_NaKATP;  /* [n_mems] */
+    double* rho_cells;    /* [n_cells] */
+    double* Jn;           /* [n_mems] */
+    double* I_mem;        /* [n_mems] */
+    double* J_cell_x;     /* [n_cells] */
+    double* J_cell_y;     /* [n_cells] */
+    double* Jc;           /* [n_mems] */
+    double* vm_ave;       /* [n_cells] */
+    double* dvm;          /* [n_mems] */
+    double* E_cell_x;     /* [n_cells] */
+    double* E_cell_y;     /* [n_cells] */
+    double* Emc;          /* [n_mems] */
+    double* E_gj_x;       /* [n_mems] */
+    double* E_gj_y;       /* [n_mems] */
+    double* gjopen;       /* [n_mems] */
+    double* sigma_cell;   /* [n_cells] */
+    double* fluxes_env_x; /* [n_ions * grid] (ECM) */
+    double* fluxes_env_y; /* [n_ions * grid] (ECM) */
+    double* rho_env;      /* [grid] (ECM) */
+    double* v_env;        /* [grid] (ECM) */
+} bx_outputs;
+
+typedef struct bx_step_status {
+    int64_t steps_done;
+    int32_t nan_vm;        /* membranes whose Vmem became NaN (last failing step) */
+    int32_t nan_conc;      /* cell concentrations that became NaN */
+    int64_t neg_clamped;   /* negative cell concentrations set to 0 (no_negs), cumulative */
+    int32_t unstable;      /* 1 once a NaN was seen; further steps are refused */
+    int32_t precision;
+} bx_step_status;
+
+/* Create a handle; copies geometry to the device of the current CUDA context.
+ * precision is BX_PLAIN_FP64 or BX_SPLIT_FP32. */
+int bx_cluster_create(const bx_geom* g, const bx_params* p, int precision,
+                      bx_handle* out);
+void bx_destroy(bx_handle h);
+
+/* Per-membrane channel diffusivities Dm[n_ions * n_mems] (sim.Dm_cells). */
+int bx_set_membrane_diffusivity(bx_handle h, const double* Dm);
+/* Environment diffusivities D_env[n_ions * grid] (ECM; sim.D_env). */
+int bx_set_env_diffusivity(bx_handle h, const double* D_env);
+/* Boundary potential Phi_b[grid]; NULL resets it to zero. */
+int bx_set_boundary_potential(bx_handle h, const double* Phi_b);
+/* Replace the scalar parameters (e.g. dt between phases). */
+int bx_set_params(bx_handle h, const bx_params* p);
+
+/* Copy state in / out (synchronous on the handle's stream). */
+int bx_state_upload(bx_handle h, const bx_state* s);
+int bx_state_download(bx_handle h, bx_state* s);
+
+/* Advance n_steps time steps on `stream` (a cudaStream_t; NULL = the handle's
+ * own stream).  If want_outputs != 0 the last step also computes the step
+ * outputs.  Asynchronous: returns after enqueueing; bx_status synchronises. */
+int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream);
+int bx_outputs_download(bx_handle h, bx_outputs* o);
+int bx_status(bx_handle h, bx_step_status* st);
+
+/* Environment fields of get_current for the current state (outputs only
+ * except E_env with ECM): v_env, E_env_x/y, J_env_x/y, B_field [grid].
+ * lap_env_inv is the dense [grid x grid] row-major lapENVinv, copied to the
+ * device on first use (pass NULL afterwards to reuse it). */
+int bx_env_fields(bx_handle h, const double* lap_env_inv, double* v_env,
+                  double* E_env_x, double* E_env_y, double* J_env_x,
+                  double* J_env_y, double* B_field);
+
+/* Dense products y[n x nrhs] = A[n x n] @ x[n x nrhs] (row-major, FP64) on the
+ * GPU, device pointers; the kernel BETSE's lapENVinv / lapGJinv matvecs use. */
+int bx_dense_apply_f64(const double* A, const double* x, double* y, int n,
+                       int nrhs, void* stream);
+
+/* Version / diagnostics. */
+int bx_abi_version(void);
+const char* bx_last_error(void);
+/* Number of kernel launches this handle has enqueued (cumulative). */
+int64_t bx_launch_count(bx_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BX_H */

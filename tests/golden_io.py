@@ -1,0 +1,115 @@
+"""Load the committed golden fixtures into (geometry, params, state) records.
+
+The fixtures were written by ``tests/golden/make_golden.py`` from BETSE's own
+``Cells``/``Simulator`` objects; field names follow BETSE's attributes.
+"""
+from __future__ import annotations
+
+import os
+from types import SimpleNamespace
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
+CASES = ['noecm_r80_s1', 'noecm_r50_s7', 'ecm_r50_s3', 'noecm_r20_s2']
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN, name + '.npz')))
+
+
+def geometry(d):
+    g = SimpleNamespace()
+    for k, v in d.items():
+        if k.startswith('geom_'):
+            setattr(g, k[5:], v)
+    M = len(g.mem_to_cells)
+    C = len(g.cell_vol)
+    g.n_mems, g.n_cells = M, C
+    g.cell_mem_ptr = np.concatenate([[0], np.cumsum(np.bincount(g.mem_to_cells, minlength=C))]).astype(np.int64)
+    g.bflag = np.zeros(M, bool)
+    g.bflag[g.bflags_mems] = True
+    g.mem_nx = np.ascontiguousarray(g.mem_vects_flat[:, 2])
+    g.mem_ny = np.ascontiguousarray(g.mem_vects_flat[:, 3])
+    g.gj_weight = g.gj_default_weights
+    g.grid_shape = tuple(int(x) for x in g.grid_shape)
+    g.delta = float(g.delta)
+    g.gj_len = float(g.gj_len)
+    g.smooth_weight_mem = d['par_smooth_weight_mem']
+    g.smooth_weight_o = d['par_smooth_weight_o']
+    g.sigma = float(d['par_sigma'])
+    g.D_env_weight = g.D_env_weight.ravel()
+    if hasattr(g, 'ko_env'):
+        g.ko_env = float(g.ko_env)
+    return g
+
+
+def params(d):
+    p = SimpleNamespace()
+    for k, v in d.items():
+        if k.startswith('par_') and np.ndim(v) == 0 and v.dtype.kind == 'f':
+            setattr(p, k[4:], float(v))
+    p.zs = d['par_zs']
+    p.D_free = d['par_D_free']
+    p.D_gj = d['par_D_gj']
+    p.Dm = d['par_Dm_cells']
+    names = [str(x) for x in d['par_ion_names']]
+    p.ion_names = names
+    p.iNa, p.iK = names.index('Na'), names.index('K')
+    p.is_ecm = bool(p.is_ecm)
+    p.nakatp_block = 1.0
+    p.gj_block = 1.0
+    if 'geom_c_env_bound' in d:
+        p.c_env_bound = d['geom_c_env_bound']
+    return p
+
+
+def state(d, prefix='init'):
+    from oracle import OracleState
+    g = geometry(d)
+    G = int(np.prod(g.grid_shape))
+    s = OracleState(vm=d[prefix + '_vm'].copy(),
+                    cc_cells=d[prefix + '_cc_cells'].copy(),
+                    cc_at_mem=d[prefix + '_cc_at_mem'].copy(),
+                    cc_env=d[prefix + '_cc_env'].copy(),
+                    Phi_b=np.zeros(G))
+    if bool(d['par_is_ecm']):
+        s.E_env_x = np.zeros(g.grid_shape)
+        s.E_env_y = np.zeros(g.grid_shape)
+        from oracle import init_fields
+        init_fields(g, params(d), s)
+    return s
+
+
+def rel_err(a, b):
+    """max |a-b| / max |b| (0 when both vanish)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.max(np.abs(b)) if b.size else 0.0
+    num = np.max(np.abs(a - b)) if b.size else 0.0
+    return 0.0 if num == 0.0 else num / (den if den > 0 else 1.0)
+
+
+def engine_inputs(d):
+    """(ClusterGeometry, StepParams, Dm, state kwargs, D_env) for ClusterEngine."""
+    from betse_gb300.cluster import ClusterGeometry, StepParams
+    g = geometry(d)
+    p = params(d)
+    cg = ClusterGeometry.from_cells(g, sim=SimpleNamespace(
+        smooth_weight_mem=g.smooth_weight_mem, smooth_weight_o=g.smooth_weight_o,
+        D_env_weight=g.D_env_weight))
+    kw = {k: getattr(p, k) for k in ('F', 'R', 'T', 'dt', 'cm', 'tm', 'gj_surface',
+                                     'alpha_NaK', 'KmNK_Na', 'KmNK_K', 'KmNK_ATP', 'cATP',
+                                     'cADP', 'cPi', 'deltaGATP', 'vol_env', 'cell_height',
+                                     'q', 'kb', 'eo', 'er', 'mu', 'sharpness',
+                                     'cell_radius', 'true_cell_size')}
+    sp = StepParams(zs=p.zs, D_free=p.D_free, D_gj=p.D_gj, iNa=p.iNa, iK=p.iK,
+                    is_ecm=p.is_ecm, ko_env=getattr(g, 'ko_env', 0.0), sigma=g.sigma,
+                    c_env_bound=getattr(p, 'c_env_bound', None), ion_names=p.ion_names,
+                    **kw)
+    s = state(d)
+    st = dict(vm=s.vm, cc_cells=s.cc_cells, cc_at_mem=s.cc_at_mem, cc_env=s.cc_env)
+    if p.is_ecm:
+        st.update(E_env_x=s.E_env_x, E_env_y=s.E_env_y)
+    D_env = getattr(g, 'D_env', None)
+    return cg, sp, p.Dm, st, D_env

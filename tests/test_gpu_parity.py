@@ -1,0 +1,135 @@
+"""GPU parity: the CUDA step (through the C ABI) against BETSE's own results.
+
+Golden fixtures hold BETSE's state after selected step counts on seeded
+clusters (``tests/golden/make_golden.py``). Tolerances:
+
+* plain FP64 form: Vmem and concentrations within 1e-10 relative
+  (max|a-b| / max|b|), the bar BETSE's run_sim_core sets for this form;
+* FP32/FP64-split form: |Vmem - Vmem_ref| < 1e-6 V.
+"""
+import numpy as np
+import pytest
+
+import golden_io as gi
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-10
+TOL_SPLIT_V = 1e-6
+
+
+def _engine(d, precision):
+    from betse_gb300.engine import ClusterEngine
+    cg, sp, Dm, st, D_env = gi.engine_inputs(d)
+    eng = ClusterEngine(cg, sp, precision)
+    eng.set_membrane_diffusivity(Dm)
+    if sp.is_ecm:
+        eng.set_env_diffusivity(D_env)
+    eng.upload(**st)
+    return eng
+
+
+def _cmp_env(eng_env, ref_env, ecm):
+    if ecm:
+        return gi.rel_err(eng_env, ref_env)
+    return gi.rel_err(eng_env, ref_env[:, 0])
+
+
+@pytest.mark.parametrize('name', gi.CASES)
+def test_state_fp64_matches_betse(name):
+    d = gi.load(name)
+    ecm = bool(d['par_is_ecm'])
+    with _engine(d, 'fp64') as eng:
+        done = 0
+        for cp in d['meta_checkpoints']:
+            eng.step(int(cp - done))
+            done = int(cp)
+            st = eng.check_stable()
+            s = eng.download()
+            e_vm = gi.rel_err(s['vm'], d[f's{cp}_vm'])
+            e_cc = gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells'])
+            e_cm = gi.rel_err(s['cc_at_mem'], d[f's{cp}_cc_at_mem'])
+            e_env = _cmp_env(s['cc_env'], d[f's{cp}_cc_env'], ecm)
+            assert e_vm < TOL_FP64, (cp, e_vm)
+            assert e_cc < TOL_FP64, (cp, e_cc)
+            assert e_cm < TOL_FP64, (cp, e_cm)
+            assert e_env < TOL_FP64, (cp, e_env)
+            assert st['steps_done'] == done
+
+
+@pytest.mark.parametrize('name', gi.CASES)
+def test_outputs_fp64_match_betse(name):
+    d = gi.load(name)
+    cp = int(d['meta_checkpoints'][1])
+    ecm = bool(d['par_is_ecm'])
+    with _engine(d, 'fp64') as eng:
+        eng.step(cp, outputs=True)
+        o = eng.outputs()
+    keys = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn', 'I_mem', 'J_cell_x',
+            'J_cell_y', 'Jc', 'vm_ave', 'dvm', 'E_cell_x', 'E_cell_y', 'Emc', 'E_gj_x',
+            'E_gj_y', 'gjopen', 'sigma_cell']
+    for k in keys:
+        ref = d[f's{cp}_{k}']
+        got = o[k]
+        # rho_cells is a cancellation of ~1e7 C/m3 terms into ~1e2: absolute
+        # agreement at 1e-16 of the terms is the FP64 bar there
+        tol = 1e-9 if k in ('rho_cells', 'dvm') else TOL_FP64
+        assert gi.rel_err(got, ref) < tol, (k, gi.rel_err(got, ref))
+    if ecm:
+        for k in ('v_env',):
+            assert gi.rel_err(o[k], d[f's{cp}_{k}']) < 1e-9, k
+
+
+@pytest.mark.parametrize('name', ['noecm_r80_s1', 'ecm_r50_s3'])
+def test_split_precision_vmem_error(name):
+    d = gi.load(name)
+    with _engine(d, 'split') as eng:
+        done = 0
+        for cp in d['meta_checkpoints']:
+            eng.step(int(cp - done))
+            done = int(cp)
+            eng.check_stable()
+            s = eng.download()
+            err = np.max(np.abs(s['vm'] - d[f's{cp}_vm']))
+            assert err < TOL_SPLIT_V, (cp, err)
+            assert gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells']) < 1e-5
+
+
+def test_graph_chunks_equal_eager_steps():
+    """CUDA-graph-replayed steps give bit-identical state to eager steps."""
+    d = gi.load('noecm_r50_s7')
+    with _engine(d, 'fp64') as a, _engine(d, 'fp64') as b:
+        a.step(70)                 # graph chunks of 32 + eager tail
+        for _ in range(70):
+            b.step(1)              # eager only
+        sa, sb = a.download(), b.download()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_deterministic_repeat():
+    d = gi.load('noecm_r80_s1')
+    res = []
+    for _ in range(2):
+        with _engine(d, 'fp64') as e:
+            e.step(100)
+            res.append(e.download())
+    for k in res[0]:
+        assert np.array_equal(res[0][k], res[1][k]), k
+
+
+def test_nan_input_raises_unstable():
+    from betse_gb300.exceptions import BetseSimUnstableException
+    d = gi.load('noecm_r20_s2')
+    cg, sp, Dm, st, _ = gi.engine_inputs(d)
+    from betse_gb300.engine import ClusterEngine
+    with ClusterEngine(cg, sp, 'fp64') as eng:
+        eng.set_membrane_diffusivity(Dm)
+        st = dict(st)
+        cc = st['cc_cells'].copy()
+        cc[0, 3] = np.nan            # poisoned host input, not a device fault
+        st['cc_cells'] = cc
+        eng.upload(**st)
+        eng.step(2)
+        with pytest.raises(BetseSimUnstableException):
+            eng.check_stable()
