@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 electrodiffusion step (one JSON line on rank 0).
+
+Metric: membrane-updates/s (membranes x time steps / second) of BETSE's full
+solver step, FP32/FP64-split form against the plain FP64 GPU form at Vmem
+error below 1e-6 V.
+
+Default workload (``--workload cluster100k``): one jittered-hex Voronoi cluster
+of ~100k cells (~600k membranes), no extracellular spaces, diffusivities
+log-uniform in [1e-19, 1e-16] m^2/s, dt 1e-2 s. One bench step is one run of
+1000 time steps of that cluster (the run length of the workload); W warm-up
+runs, then K timed runs bracketed by synchronisation, with the L2 flushed
+(a 256 MiB write) before every run. The plain FP64 form is timed on the same
+cluster and its Vmem after the same steps is the error reference of the split
+form.
+
+``value``: device-resident throughput of the split form. ``e2e``: the same
+metric through the C ABI with host buffers: every run uploads the state from
+pinned host memory, steps, and downloads the state.
+
+``--impl reference`` times the CPU restatement of BETSE's step (the oracle,
+NumPy) on the host cores on a bounded sample of the same cluster.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'membrane-updates/s vs plain FP64 GPU at Vmem err<1e-6 V; init time-to-steady'
+UNIT = 'membrane-updates/s'
+
+WORKLOADS = {
+    # configs of the benchmark: radius (m) of the disc the hex lattice is clipped to
+    'cluster100k': dict(radius=1450e-6, seed=3, is_ecm=False, dt=1e-2, dm=(1e-19, 1e-16),
+                        time_steps=1000, grid_size=20,
+                        desc='precision variant: ~100k-cell jittered-hex Voronoi cluster '
+                             '(~600k membranes), no ECM, Dm log-uniform [1e-19,1e-16], '
+                             'dt 1e-2 s, 1000 steps per run; split step vs plain FP64'),
+    'plain250': dict(radius=80e-6, seed=1, is_ecm=False, dt=1e-2, dm=(1e-19, 1e-17),
+                     time_steps=2000, grid_size=20,
+                     desc='plain FP64 reference step, ~250 cells, no ECM, 2000 steps'),
+}
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def peaks():
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        self.p = None
+        self.idx = gpu_index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', '-i', str(self.idx), f'--query-gpu={self.Q}',
+                                       '--format=csv,noheader,nounits', '-lms', '200'],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(',') for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == 'active':
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': smax, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def build_workload(name):
+    from betse_gb300 import generator as gen
+    w = WORKLOADS[name]
+    g, p, Dm, st, D_env = gen.workload(w['radius'], w['seed'], is_ecm=w['is_ecm'], dt=w['dt'],
+                                       dm_range=w['dm'], grid_size=w['grid_size'])
+    return w, g, p, Dm, st, D_env
+
+
+def cpu_baseline(g, p, Dm, st, budget_s=12.0):
+    """Oracle (NumPy restatement of BETSE's step) on a bounded sample: whole
+    cluster, as many time steps as fit in about budget_s seconds."""
+    import oracle
+    from types import SimpleNamespace
+    geo = SimpleNamespace(**{k: getattr(g, k) for k in (
+        'mem_to_cells', 'nn_i', 'map_mem2ecm', 'mem_sa', 'mem_nx', 'mem_ny', 'cell_vol',
+        'cell_sa', 'diviterm', 'num_mems', 'smooth_weight_mem', 'smooth_weight_o', 'delta',
+        'gj_len', 'cell_mem_ptr')})
+    geo.bflag = g.bflag.astype(bool)
+    geo.gj_weight = g.gj_weight
+    geo.grid_shape = tuple(g.grid_shape)
+    geo.mem_to_cells = g.mem_to_cells.astype(np.int64)
+    geo.nn_i = g.nn_i.astype(np.int64)
+    par = SimpleNamespace(**{k: getattr(p, k) for k in (
+        'F', 'R', 'T', 'dt', 'cm', 'tm', 'gj_surface', 'alpha_NaK', 'KmNK_Na', 'KmNK_K',
+        'KmNK_ATP', 'cATP', 'cADP', 'cPi', 'deltaGATP', 'vol_env', 'zs', 'D_free', 'D_gj',
+        'iNa', 'iK', 'is_ecm', 'gj_block', 'nakatp_block')})
+    par.Dm = Dm
+    I, M = Dm.shape
+    ce = np.repeat(np.asarray(st['cc_env'], np.float64)[:, None], M, axis=1)
+    s = oracle.OracleState(vm=st['vm'].copy(), cc_cells=st['cc_cells'].copy(),
+                           cc_at_mem=st['cc_at_mem'].copy(), cc_env=ce,
+                           Phi_b=np.zeros(g.n_grid))
+    t0 = time.perf_counter()
+    oracle.step(geo, par, s)
+    one = time.perf_counter() - t0
+    n = max(1, int(budget_s / max(one, 1e-3)) - 1)
+    t0 = time.perf_counter()
+    for _ in range(n):
+        oracle.step(geo, par, s)
+    dt = time.perf_counter() - t0
+    return {'value': g.n_mems * n / dt, 'unit': UNIT, 'cores': 1, 'kind': 'port',
+            'sample': f'{n} time steps of the full {g.n_cells}-cell / {g.n_mems}-membrane '
+                      f'cluster ({dt:.1f} s), NumPy oracle, one thread'}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU restatement of BETSE's step on the host cores."""
+    if rank != 0:
+        return
+    w, g, p, Dm, st, _ = build_workload(args.workload)
+    budget = float(os.environ.get('BX_REF_BUDGET_S', '6'))
+    samples = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(g, p, Dm, st, budget_s=budget)
+        if k >= args.warmup:
+            samples.append(r['value'])
+    v = statistics.mean(samples)
+    line = {'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1e3 * g.n_mems / v,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic', 'impl': 'reference',
+            'config': {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems},
+            'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': 1, 'kind': 'port',
+                             'sample': r['sample']},
+            'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--workload', default='cluster100k', choices=sorted(WORKLOADS))
+    ap.add_argument('--time-steps', type=int, default=None)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    args = ap.parse_args()
+    world = _env_int('WORLD_SIZE', 1)
+    rank = _env_int('RANK', 0)
+    local = _env_int('LOCAL_RANK', 0)
+    if args.impl == 'reference':
+        return run_reference(args, rank, world)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    else:
+        torch.cuda.set_device(0)
+    from betse_gb300.build import build
+    build()
+    from betse_gb300.engine import ClusterEngine
+
+    w, g, p, Dm, st, D_env = build_workload(args.workload)
+    T = args.time_steps or w['time_steps']
+    dev = torch.device('cuda', torch.cuda.current_device())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    # a non-default stream: bx_step launches on it and the events bracket exactly it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def make(prec):
+        e = ClusterEngine(g, p, prec)
+        e.set_membrane_diffusivity(Dm)
+        e.upload(**st)
+        return e
+
+    split = make('split')
+    plain = make('fp64')
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def timed_runs(eng, n_runs, runs_warm):
+        for _ in range(runs_warm):
+            flush.fill_(1)
+            eng.step(T, stream=stream.cuda_stream)
+        barrier()
+        ev = []
+        l0 = eng.launch_count()
+        for _ in range(n_runs):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.step(T, stream=stream.cuda_stream)
+            b.record(stream)
+            ev.append((a, b))
+        barrier()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        return ms, eng.launch_count() - l0
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_split, launches = timed_runs(split, args.steps, args.warmup)
+    clk = clocks.stop()
+    ms_plain, _ = timed_runs(plain, max(1, min(args.steps, 2)), 1)
+    split.check_stable()
+    plain.check_stable()
+
+    tot_ms = sum(ms_split)
+    t_local = tot_ms / 1e3
+    if dist is not None:
+        t = torch.tensor([t_local], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    else:
+        t_max = t_local
+    units = g.n_mems * T * args.steps * world
+    value = units / t_max
+    plain_value = g.n_mems * T * len(ms_plain) / (sum(ms_plain) / 1e3)
+
+    # ---- error at equal step counts: fresh engines, same number of steps
+    e_s, e_p = make('split'), make('fp64')
+    e_s.step(T)
+    e_p.step(T)
+    vm_err = float(np.max(np.abs(e_s.download()['vm'] - e_p.download()['vm'])))
+
+    # ---- roofline of the dominant kernel (fused cell step), events on its stream
+    e_s.upload(**st)
+    kern_ms = e_s.time_cell_kernel(50)
+    kbytes = e_s.cell_kernel_bytes()
+    hbm, src = peaks()
+    achieved = kbytes / (kern_ms / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, 'profiles', 'cell_step_split_100k.traffic.json')
+    if os.path.exists(tp):
+        tj = json.load(open(tp))
+        traffic = int(tj['dram_bytes_per_launch'] * g.n_mems / tj['membranes'])
+
+    # ---- end to end through the C ABI with host buffers (pinned)
+    pin = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy()
+           for k, v in st.items()}
+    h2d = sum(v.nbytes for v in pin.values())
+    e_s.upload(**pin)
+    e_s.step(T)
+    torch.cuda.synchronize()
+    d2h = 0
+    t_e2e = []
+    for k in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_s.upload(**pin)
+        e_s.step(T)
+        out = e_s.download()
+        t1 = time.perf_counter()
+        d2h = sum(v.nbytes for v in out.values())
+        if k >= args.warmup:
+            t_e2e.append(t1 - t0)
+    e2e_val = g.n_mems * T * len(t_e2e) * world / sum(t_e2e)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(g, p, Dm, st)
+
+    if rank == 0:
+        line = {
+            'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_max * 1e3 / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32 fluxes / f64 concentrations+Vmem', 'data': 'synthetic',
+            'config': {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems,
+                       'time_steps_per_step': T, 'precision': 'split',
+                       'l2': 'flushed (256 MiB write) before every timed run',
+                       'parallelism': f'replicas x{world}'},
+            'plain_fp64': {'value': plain_value, 'unit': UNIT,
+                           'ms_per_step': sum(ms_plain) / len(ms_plain),
+                           'speedup_split_vs_plain': value / world / plain_value,
+                           'vm_max_abs_err_V': vm_err, 'vm_err_after_steps': T},
+            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
+                         'frac': achieved / hbm, 'traffic': traffic,
+                         'kernel': 'k_cell_step<float> (fused membrane flux + cell update)',
+                         'algorithmic_bytes_per_launch': kbytes, 'launch_ms': kern_ms,
+                         'peak_source': src},
+            'cpu_baseline': cpu,
+            'e2e': {'value': e2e_val, 'unit': UNIT, 'h2d_bytes_per_step': int(h2d),
+                    'd2h_bytes_per_step': int(d2h)},
+            'gpu_launches': int(launches),
+            'clocks': clk,
+        }
+        print(json.dumps(line), flush=True)
+    for e in (split, plain, e_s, e_p):
+        e.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -633,6 +633,51 @@ int bx_outputs_download(bx_handle hh, bx_outputs* o) {
   return BX_OK;
 }
 
+int bx_time_cell_kernel(bx_handle hh, int n, double* ms_per_launch) {
+  if (!hh || !ms_per_launch || n <= 0) return fail(BX_EINVAL, "bad arguments");
+  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+  if (!h->have_state || !h->have_dm) return fail(BX_ESTATE, "upload state and Dm first");
+  bx::DevGeom g = dev_geom(h);
+  bx::StepConst k = make_step_const(h);
+  k.gj_len = h->gj_len;
+  cudaEvent_t e0, e1;
+  BX_CU(cudaEventCreate(&e0));
+  BX_CU(cudaEventCreate(&e1));
+  double tot = 0.0;
+  const bool split = h->precision == BX_SPLIT_FP32;
+  for (int q = 0; q < n; ++q) {
+    bx::StepPtrs p = step_ptrs(h, h->parity);
+    BX_CU(cudaEventRecord(e0, h->stream));
+    cudaError_t e = split ? bx::launch_cell_step<float, 256>(h->ecm, false, h->phib_nonzero, h->nblk, h->stream, g, p, k)
+                          : bx::launch_cell_step<double, 256>(h->ecm, false, h->phib_nonzero, h->nblk, h->stream, g, p, k);
+    if (e != cudaSuccess) return fail(BX_ECUDA, cudaGetErrorString(e));
+    BX_CU(cudaEventRecord(e1, h->stream));
+    BX_CU(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    BX_CU(cudaEventElapsedTime(&ms, e0, e1));
+    tot += ms;
+    h->parity ^= 1;
+    h->launches++;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_per_launch = tot / n;
+  return BX_OK;
+}
+
+int64_t bx_cell_kernel_bytes(bx_handle hh) {
+  if (!hh) return -1;
+  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+  const int64_t M = h->M, C = h->C, I = h->I;
+  const int64_t w = (h->precision == BX_SPLIT_FP32) ? 4 : 8;   // Dm, mem_sa, gj_w width
+  // per membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env with ECM,
+  // + f*sa export with ECM); per cell: cc in+out, cc_mem in+out, cell_vol, diviterm, ptr
+  int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0);
+  int64_t cell = 4 * I * 8 + 16 + 4;
+  int64_t blk = h->ecm ? 0 : (int64_t)h->nblk * I * 8;
+  return M * mem + C * cell + blk;
+}
+
 int64_t bx_launch_count(bx_handle hh) {
   if (!hh) return -1;
   return static_cast<bx_cluster_ext*>(hh)->launches;

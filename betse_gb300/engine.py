@@ -138,5 +138,15 @@ class ClusterEngine:
                 'reduce gap junction radius, and/or reduce rate coefficients.')
         return st
 
+    def time_cell_kernel(self, n=20) -> float:
+        """Mean ms of one fused-cell-kernel launch (CUDA events, handle stream).
+        Advances the state; re-upload afterwards."""
+        ms = ct.c_double()
+        _lib.check(self.lib.bx_time_cell_kernel(self.h, int(n), ct.byref(ms)), 'bx_time_cell_kernel')
+        return ms.value
+
+    def cell_kernel_bytes(self) -> int:
+        return int(self.lib.bx_cell_kernel_bytes(self.h))
+
     def launch_count(self) -> int:
         return int(self.lib.bx_launch_count(self.h))

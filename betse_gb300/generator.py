@@ -1,0 +1,273 @@
+"""Synthetic cell clusters with BETSE's conventions, at any size.
+
+BETSE seeds a cluster with ``Cells.make_world`` (``betse/science/cells.py:414``):
+a jittered hexagonal lattice (``_make_cell_lattice``, cells.py:742-801), a DEC
+mesh whose Voronoi vertices are triangle centroids (``DECMesh(use_centroids=
+True)``, math/mesh.py:86) clipped to the tissue shape, then per-cell membranes
+(``cellVerts``, cells.py:978-1175), volumes (``cell_vols``, :1358-1390), gap
+junction pairs (``mem_processing``/``near_neigh``, :1392-1573) and the
+environment grid maps (``makeECM``/``environment``, :1576-1843). Its O(N^2)
+Python loops and dense ``pinv`` limit it to a few thousand cells.
+
+This module builds the same data in vectorised NumPy/SciPy:
+
+* the lattice recipe is BETSE's (linspace rows, legacy ``np.random`` jitter
+  ``disorder * d_cell * (rand - 0.5)``);
+* cells are the Delaunay duals with centroid vertices of every seed whose
+  distance to the lattice centre is below ``radius`` and whose triangle fan is
+  closed; membranes are the polygon edges scaled in by ``scale_cell`` about the
+  centroid, listed counter-clockwise per cell exactly as ``cellVerts`` does;
+* gap-junction partners come from the shared Delaunay edge (BETSE finds the
+  same pairs by a radius search on membrane midpoints); a membrane with no
+  partner in the cluster is a boundary membrane, paired with itself;
+* cells are ordered along a Z-order curve so that gap-junction partners sit
+  close in memory.
+
+The result is a ``ClusterGeometry`` plus the initial-state helpers the step
+needs; clip-edge refinement of the reference mesh is not reproduced (boundary
+cells are whole Voronoi cells).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .cluster import ClusterGeometry, StepParams
+
+ION_NAMES = ['Na', 'K', 'Cl', 'Ca', 'P', 'M']
+# workload ion set: Na/K/Cl/Ca/P inside and outside (mM); M balances charge
+CELL_CONC = {'Na': 8.0, 'K': 125.0, 'Cl': 10.0, 'Ca': 1e-4, 'P': 100.0}
+ENV_CONC = {'Na': 145.0, 'K': 5.0, 'Cl': 105.0, 'Ca': 1.0, 'P': 10.0}
+Z = {'Na': 1, 'K': 1, 'Cl': -1, 'Ca': 2, 'P': -1, 'M': -1}
+D_FREE = {'Na': 1.33e-9, 'K': 1.96e-9, 'Cl': 2.03e-9, 'Ca': 1.0e-10, 'P': 0.0, 'M': 1.0e-9}
+
+
+def hex_lattice(wsx, wsy, d_cell, disorder, rs):
+    """BETSE's hexagonal seed lattice (cells.py:742-801) with jitter from ``rs``."""
+    r = d_cell / 2
+    a_hex = np.sqrt(3) * r
+    b_hex = 3 * r
+    bx = np.linspace(0, wsy, int(wsy / b_hex))
+    by = np.linspace(a_hex / 2, wsx - a_hex / 2, int((wsx - a_hex) / a_hex))
+    rx = np.linspace(b_hex / 2, wsy - b_hex / 2, int((wsy - b_hex) / b_hex))
+    ry = np.linspace(0, wsx, int(wsx / a_hex))
+    xb, yb = np.meshgrid(bx, by)
+    xr, yr = np.meshgrid(rx, ry)
+    x = np.hstack((xb.ravel(), xr.ravel()))
+    y = np.hstack((yb.ravel(), yr.ravel()))
+    x = x + disorder * d_cell * (rs.rand(len(x)) - 0.5)
+    y = y + disorder * d_cell * (rs.rand(len(y)) - 0.5)
+    return np.column_stack((x, y))
+
+
+def _zorder(xy, bits=16):
+    lo = xy.min(axis=0)
+    span = np.maximum(xy.max(axis=0) - lo, 1e-30)
+    q = ((xy - lo) / span * (2 ** bits - 1)).astype(np.uint64)
+    key = np.zeros(len(xy), np.uint64)
+    for b in range(bits):
+        key |= ((q[:, 0] >> np.uint64(b)) & np.uint64(1)) << np.uint64(2 * b)
+        key |= ((q[:, 1] >> np.uint64(b)) & np.uint64(1)) << np.uint64(2 * b + 1)
+    return key
+
+
+@dataclass
+class GeneratedCluster:
+    geom: ClusterGeometry
+    cell_centres: np.ndarray
+    mem_mids: np.ndarray
+    xmin: float
+    xmax: float
+    ymin: float
+    ymax: float
+    world: float       # side of the square world (p.wsx after the disorder margin)
+
+
+def make_cluster(radius, seed, d_cell=10e-6, disorder=0.4, cell_height=1e-5,
+                 cell_space=26e-9, scale_cell=0.99, grid_size=20, smooth_cells=2.0):
+    """A jittered-hex Voronoi cluster clipped to a disc of ``radius`` (m)."""
+    from scipy.spatial import Delaunay
+
+    cell_radius = d_cell / 2
+    world = 2 * radius + 20e-6
+    wsx = wsy = world + 5 * disorder * d_cell
+    rs = np.random.RandomState(seed)
+    pts = hex_lattice(wsx, wsy, d_cell, disorder, rs)
+    centre = pts.mean(axis=0)
+    xmin, ymin = pts.min(axis=0) - cell_radius
+    xmax, ymax = pts.max(axis=0) + cell_radius
+
+    tri = Delaunay(pts)
+    simp = tri.simplices
+    tcent = pts[simp].mean(axis=1)                # centroid Voronoi vertices
+    n = len(pts)
+    # triangles around each seed, ordered by angle (counter-clockwise)
+    owner = simp.ravel()
+    tid = np.repeat(np.arange(len(simp)), 3)
+    ang = np.arctan2(tcent[tid, 1] - pts[owner, 1], tcent[tid, 0] - pts[owner, 0])
+    order = np.lexsort((ang, owner))
+    owner, tid = owner[order], tid[order]
+    fan_ptr = np.concatenate([[0], np.cumsum(np.bincount(owner, minlength=n))])
+    # closed fan: seeds not on the hull
+    hull = np.zeros(n, bool)
+    hull[np.unique(tri.convex_hull.ravel())] = True
+    keep = (~hull) & (np.hypot(pts[:, 0] - centre[0], pts[:, 1] - centre[1]) < radius)
+    keep &= np.diff(fan_ptr) >= 3
+    seeds = np.nonzero(keep)[0]
+    # polygon of each kept seed, then cell order along a Z curve of the centroid
+    polys = [tcent[tid[fan_ptr[s]:fan_ptr[s + 1]]] for s in seeds]
+    cents = np.array([p.mean(axis=0) for p in polys])
+    zo = np.argsort(_zorder(cents), kind='stable')
+    seeds = seeds[zo]
+    polys = [polys[i] for i in zo]
+    C = len(seeds)
+    seed_to_cell = -np.ones(n, np.int64)
+    seed_to_cell[seeds] = np.arange(C)
+
+    counts = np.array([len(p) for p in polys])
+    M = int(counts.sum())
+    ptr = np.concatenate([[0], np.cumsum(counts)])
+    m2c = np.repeat(np.arange(C), counts)
+    # vertices scaled toward the centroid (cellVerts: p.scale_cell)
+    poly_c = np.array([p.mean(axis=0) for p in polys])
+    V = np.concatenate(polys)
+    V = scale_cell * (V - poly_c[m2c]) + poly_c[m2c]
+    # membrane k of a cell joins vertex k-1 and vertex k (cellVerts' loop)
+    prev = np.arange(M) - 1
+    prev[ptr[:-1]] = ptr[1:] - 1
+    p1, p2 = V[prev], V[np.arange(M)]
+    mids = (p1 + p2) / 2
+    tang = p2 - p1
+    length = np.hypot(tang[:, 0], tang[:, 1])
+    tang = tang / length[:, None]
+    nx, ny = tang[:, 1], -tang[:, 0]
+    mem_sa = length * cell_height
+    # cell centre: BETSE's cell_centres are polygon centroids of the unscaled cells
+    rad = mids - poly_c[m2c]
+    R_rads = np.hypot(rad[:, 0], rad[:, 1])
+    mem_vol = 0.5 * R_rads * mem_sa
+    cell_vol = np.bincount(m2c, weights=mem_vol, minlength=C)
+    cell_sa = np.bincount(m2c, weights=mem_sa, minlength=C)
+    diviterm = cell_vol / cell_sa
+
+    # gap junction partners: the edge between triangles (t_prev, t) around seed s is
+    # the Voronoi edge dual to the Delaunay edge (s, other); pair by that edge.
+    t_prev = tid[np.concatenate([fan_ptr[s] + (np.arange(c) - 1) % c for s, c in
+                                 zip(seeds, counts)])] if C else np.zeros(0, np.int64)
+    t_cur = tid[np.concatenate([fan_ptr[s] + np.arange(c) for s, c in zip(seeds, counts)])]
+    own_seed = seeds[m2c]
+    a, b = simp[t_prev], simp[t_cur]
+    # the shared vertex of the two triangles that is not the owner seed
+    other = np.full(M, -1, np.int64)
+    for ka in range(3):
+        for kb in range(3):
+            same = (a[:, ka] == b[:, kb]) & (a[:, ka] != own_seed)
+            other = np.where(same & (other < 0), a[:, ka], other)
+    key_lo = np.minimum(own_seed, other)
+    key_hi = np.maximum(own_seed, other)
+    nn = np.arange(M)
+    valid = (other >= 0) & (seed_to_cell[np.maximum(other, 0)] >= 0)
+    idx = np.nonzero(valid)[0]
+    keys = key_lo[idx] * (n + 1) + key_hi[idx]
+    o = np.argsort(keys, kind='stable')
+    ks, ix = keys[o], idx[o]
+    pair = np.nonzero(ks[1:] == ks[:-1])[0]
+    nn[ix[pair]] = ix[pair + 1]
+    nn[ix[pair + 1]] = ix[pair]
+    bflags = np.nonzero(nn == np.arange(M))[0]
+
+    # environment grid (makeECM / FiniteDiffSolver.cell_grid, environment)
+    delta = (xmax - xmin) / grid_size
+    gnx = int((xmax - xmin) / delta)
+    gny = int((ymax - ymin) / delta)
+    xv = np.linspace(xmin, xmax, gnx + 1)
+    yv = np.linspace(ymin, ymax, gny + 1)
+    cx = (xv[:-1] + xv[1:]) / 2
+    cy = (yv[:-1] + yv[1:]) / 2
+    jx = np.clip(np.searchsorted(cx, mids[:, 0]), 1, gnx - 1)
+    jx = np.where(np.abs(cx[jx - 1] - mids[:, 0]) <= np.abs(cx[jx] - mids[:, 0]), jx - 1, jx)
+    iy = np.clip(np.searchsorted(cy, mids[:, 1]), 1, gny - 1)
+    iy = np.where(np.abs(cy[iy - 1] - mids[:, 1]) <= np.abs(cy[iy] - mids[:, 1]), iy - 1, iy)
+    map_env = iy * gnx + jx
+    msa_env = np.bincount(map_env, weights=mem_sa, minlength=gnx * gny)
+
+    # cell adjacency (near_neigh's cell_nn) for the warm-start network
+    part = nn != np.arange(M)
+    src, dst = m2c[part], m2c[nn[part]]
+    oo = np.lexsort((dst, src))
+    src, dst = src[oo], dst[oo]
+    cnn_ptr = np.concatenate([[0], np.cumsum(np.bincount(src, minlength=C))])
+
+    geom = ClusterGeometry.from_arrays(
+        mem_to_cells=m2c, nn_i=nn, bflags_mems=bflags, map_mem2ecm=map_env,
+        mem_sa=mem_sa, mem_nx=nx, mem_ny=ny, gj_weight=np.ones(M), cell_vol=cell_vol,
+        cell_sa=cell_sa, diviterm=diviterm, grid_shape=(gny, gnx), delta=delta,
+        gj_len=cell_space, smooth_cells=smooth_cells, mem_sa_per_env=msa_env,
+        D_env_weight=np.ones(gnx * gny), cell_nn_ptr=cnn_ptr, cell_nn=dst)
+    return GeneratedCluster(geom=geom, cell_centres=poly_c, mem_mids=mids,
+                            xmin=xmin, xmax=xmax, ymin=ymin, ymax=ymax, world=wsx)
+
+
+def charge_balanced(conc):
+    c = dict(conc)
+    q = sum(c[k] * Z[k] for k in c)
+    assert q >= 0, 'the balancing ion M must be an anion'
+    c['M'] = q
+    return c
+
+
+def workload(radius, seed, is_ecm=False, dt=1e-2, dm_range=(1e-19, 1e-17),
+             grid_size=20, cell_space=26e-9, alpha_NaK=5e-8, gj_range=(0.5, 1.0),
+             na_k_dm_mult=1.0, pump_mult=1.0):
+    """Cluster + parameters + initial state of the seeded synthetic workload.
+
+    Returns (geom, params, Dm, state dict, D_env). Diffusivities are
+    log-uniform in ``dm_range`` per membrane and ion (Dm_P = 0), gap-junction
+    weights uniform in ``gj_range`` per membrane pair; draws come from
+    ``np.random.default_rng(seed + 1)``, the lattice from ``RandomState(seed)``.
+    """
+    gc = make_cluster(radius, seed, grid_size=grid_size, cell_space=cell_space)
+    g = gc.geom
+    M, C, G = g.n_mems, g.n_cells, g.n_grid
+    rng = np.random.default_rng(seed + 1)
+    Dm = np.exp(rng.uniform(np.log(dm_range[0]), np.log(dm_range[1]), size=(6, M)))
+    Dm[ION_NAMES.index('P')] = 0.0
+    Dm[ION_NAMES.index('Na')] *= na_k_dm_mult
+    Dm[ION_NAMES.index('K')] *= na_k_dm_mult
+    w = rng.uniform(gj_range[0], gj_range[1], size=M)
+    w = w[np.minimum(np.arange(M), g.nn_i)]
+    g.gj_weight = np.ascontiguousarray(w)
+    cell = charge_balanced(CELL_CONC)
+    env = charge_balanced(ENV_CONC)
+    zs = np.array([Z[k] for k in ION_NAMES], np.float64)
+    D_free = np.array([D_FREE[k] for k in ION_NAMES])
+    cc_cells = np.array([[cell[k]] * C for k in ION_NAMES], np.float64)
+    env_v = np.array([env[k] for k in ION_NAMES], np.float64)
+    T = 310.15
+    F, R, q, kb, eo, er, NAv = 96485.0, 8.314, 1.602e-19, 1.3806e-23, 8.854e-12, 80.0, 6.022e23
+    cell_height = 1e-5
+    vol_env = gc.world * gc.world * cell_height      # parameters.py:540, multiplier 1
+    ko_env = float(np.sqrt(np.dot((NAv * q ** 2 * zs ** 2) / (er * eo * kb * T), env_v)))
+    sigma = float((((zs ** 2) * q * F * cell_conc_vec(cell) * D_free) / (kb * T)).sum())
+    p = StepParams(zs=zs, D_free=D_free, D_gj=D_free.copy(), iNa=0, iK=1, is_ecm=is_ecm,
+                   T=T, dt=dt, cm=0.022, alpha_NaK=alpha_NaK * pump_mult, vol_env=vol_env,
+                   cell_height=cell_height, ko_env=ko_env, sigma=sigma,
+                   c_env_bound=env_v.copy(), ion_names=list(ION_NAMES))
+    if is_ecm:
+        cc_env = np.repeat(env_v[:, None], G, axis=1)
+    else:
+        cc_env = env_v.copy()
+    cc_at_mem = cc_cells[:, g.mem_to_cells].copy()
+    rho = np.dot(zs * F, cc_cells)
+    vm = (1 / p.cm) * (rho * g.diviterm)[g.mem_to_cells]
+    state = dict(vm=vm, cc_cells=cc_cells, cc_at_mem=cc_at_mem, cc_env=cc_env)
+    if is_ecm:
+        # uniform, charge-balanced environment: zero initial field
+        state.update(E_env_x=np.zeros(g.grid_shape), E_env_y=np.zeros(g.grid_shape))
+    D_env = np.repeat(D_free[:, None], G, axis=1) if is_ecm else None
+    return g, p, Dm, state, D_env
+
+
+def cell_conc_vec(cell):
+    return np.array([cell[k] for k in ION_NAMES], np.float64)

@@ -204,6 +204,16 @@ int bx_env_fields(bx_handle h, const double* lap_env_inv, double* v_env,
 int bx_dense_apply_f64(const double* A, const double* x, double* y, int n,
                        int nrhs, void* stream);
 
+/* Diagnostics: launch the fused cell kernel alone n times on the handle's
+ * stream (state ping-pongs as in bx_step) and return the mean duration of one
+ * launch in *ms_per_launch, measured with CUDA events around each launch.
+ * Intended for roofline measurement; it advances the state by n steps
+ * without the environment update, so re-upload the state afterwards. */
+int bx_time_cell_kernel(bx_handle h, int n, double* ms_per_launch);
+/* Algorithmic bytes one launch of the fused cell kernel moves (each array
+ * counted once at its stored width; reads plus writes). */
+int64_t bx_cell_kernel_bytes(bx_handle h);
+
 /* Version / diagnostics. */
 int bx_abi_version(void);
 const char* bx_last_error(void);

@@ -113,3 +113,21 @@ def engine_inputs(d):
         st.update(E_env_x=s.E_env_x, E_env_y=s.E_env_y)
     D_env = getattr(g, 'D_env', None)
     return cg, sp, p.Dm, st, D_env
+
+
+def vm_floor(d, cc_cells, ulps=4.0):
+    """FP64 cancellation floor of Vmem (volts).
+
+    Vmem = (sum_i z_i F c_i) * diviterm / cm is a small difference of charges of
+    ~1e7 C/m3 (betse/science/sim.py:2027-2029); any two summation orders of that
+    sum differ by a few ulp of the largest term, mapped to volts here."""
+    zF = np.abs(d['par_zs'] * d['par_F'])
+    charge = (zF[:, None] * np.abs(cc_cells)).sum(axis=0)
+    div = d['geom_diviterm']
+    return ulps * np.finfo(np.float64).eps * np.max(charge * div) / float(d['par_cm'])
+
+
+def vm_err_ok(d, vm, vm_ref, cc_ref, rel=1e-10):
+    err = np.max(np.abs(vm - vm_ref))
+    bound = rel * np.max(np.abs(vm_ref)) + vm_floor(d, cc_ref)
+    return err <= bound, err, bound
