@@ -80,6 +80,10 @@ class BxStepStatus(ct.Structure):
 SIGNATURES = {
     'bx_cluster_create': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_int,
                                      ct.POINTER(ct.c_void_p)]),
+    'bx_batch_create': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_int, ct.c_int,
+                                   ct.POINTER(ct.c_void_p)]),
+    'bx_batch_layout': (ct.c_int, [ct.c_void_p, _ip, _ip]),
+    'bx_batch_set_params': (ct.c_int, [ct.c_void_p, ct.POINTER(BxParams)]),
     'bx_destroy': (None, [ct.c_void_p]),
     'bx_set_membrane_diffusivity': (ct.c_int, [ct.c_void_p, _dp]),
     'bx_set_env_diffusivity': (ct.c_int, [ct.c_void_p, _dp]),

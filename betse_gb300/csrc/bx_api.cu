@@ -1,6 +1,17 @@
 // bx_api.cu -- the C ABI (include/bx.h): handle lifetime, validation of the
 // CSR index maps, host<->device state transfer, CUDA-graph-captured stepping
 // and the environment / dense-product entry points.
+//
+// A handle holds one cluster or a batch of clusters (a parameter sweep).  The
+// clusters' cells and membranes are concatenated; CTAs never straddle two
+// clusters, so per-cluster quantities (the well-mixed environment, the pump
+// rate) are looked up by CTA.
+//
+// Three step paths:
+//   plain      BX_PLAIN_FP64: k_cell_step<double> (bx_kernels.cuh)
+//   split      BX_SPLIT_FP32 without ECM: k_split_step (bx_split.cuh), no FP64
+//              arithmetic per step
+//   split+ECM  BX_SPLIT_FP32 with ECM: k_cell_step<float> + the FP64 grid
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -13,6 +24,7 @@
 #include "../../include/bx.h"
 #include "bx_env.cuh"
 #include "bx_launch.cuh"
+#include "bx_split.cuh"
 
 namespace {
 
@@ -23,11 +35,11 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
-#define BX_CU(call)                                                                   \
-  do {                                                                                \
-    cudaError_t e_ = (call);                                                          \
-    if (e_ != cudaSuccess)                                                            \
-      return fail(BX_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));     \
+#define BX_CU(call)                                                               \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return fail(BX_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
 template <typename P>
@@ -37,72 +49,86 @@ cudaError_t dalloc(P** p, size_t n) {
   return cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(P));
 }
 
-constexpr int kGraphChunk = 32;   // steps per captured graph (even: ping-pong parity returns)
+template <typename P>
+cudaError_t h2d(P* dst, const P* src, size_t n) {
+  return cudaMemcpy(dst, src, n * sizeof(P), cudaMemcpyHostToDevice);
+}
+
+constexpr int kGraphChunk = 32;  // steps per captured graph (even: ping-pong parity returns)
 constexpr int kEnvTPB = 256;
+constexpr int kTPB = 256;        // membrane slots per CTA of the cell kernels
+
+enum Mode { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SPLIT_ECM = 2 };
 
 }  // namespace
 
 struct bx_cluster {
   int dev = 0;
   cudaStream_t stream = nullptr;
+  int ncl = 1;
   int C = 0, M = 0, I = 0, G = 0, ny = 0, nx = 0;
   int precision = BX_PLAIN_FP64;
-  int tpb = 256;
+  int mode = MODE_PLAIN;
   int nblk = 0;
   bool ecm = false;
-  bx_params par{};
-  // geometry
+  bx_params par{};                 // parameters of cluster 0 (the shared ones)
+  std::vector<bx_params> cl_par;   // per-cluster parameters
+  std::vector<int> cl_cell, cl_mem, cl_blk;   // offsets [ncl+1]
+  double gj_len = 0.0, delta = 0.0, env_surf_scale = 0.0;
+  // ---- geometry (device)
   int *d_cell_ptr = nullptr, *d_m2c = nullptr, *d_nn = nullptr, *d_nn_cell = nullptr,
-      *d_map_env = nullptr, *d_blk = nullptr, *d_env_ptr = nullptr, *d_env_mem = nullptr;
-  uint8_t *d_bflag = nullptr, *d_touched = nullptr;
-  double *d_mem_sa = nullptr, *d_gj_w = nullptr, *d_nx = nullptr, *d_ny = nullptr,
-         *d_swm = nullptr, *d_swo = nullptr, *d_cell_vol = nullptr, *d_cell_sa = nullptr,
-         *d_diviterm = nullptr;
-  float *d_mem_sa_f = nullptr, *d_gj_w_f = nullptr, *d_Dm_f = nullptr;
+      *d_map_env = nullptr, *d_blk = nullptr, *d_blk_cl = nullptr, *d_cl_blk = nullptr,
+      *d_env_ptr = nullptr, *d_env_mem = nullptr;
+  uint8_t *d_bflag = nullptr, *d_touched = nullptr, *d_lcell = nullptr;
+  double *d_mem_sa = nullptr, *d_gj_w = nullptr, *d_nx = nullptr, *d_ny = nullptr, *d_swm = nullptr,
+         *d_swo = nullptr, *d_cell_vol = nullptr, *d_cell_sa = nullptr, *d_diviterm = nullptr;
+  float *d_mem_sa_f = nullptr, *d_gj_w_f = nullptr, *d_gjw0_f = nullptr, *d_dtv = nullptr,
+        *d_dvc = nullptr;
+  // ---- per-membrane channel data
   double* d_Dm = nullptr;
-  // state
-  double *d_vm[2] = {nullptr, nullptr}, *d_ccm[2] = {nullptr, nullptr};
-  double *d_cc = nullptr, *d_cenv = nullptr, *d_phib = nullptr, *d_env_part = nullptr,
-         *d_mem_flux_sa = nullptr;
+  float* d_Dm_f = nullptr;
+  // ---- state: plain / split+ECM
+  double *d_vm[2] = {nullptr, nullptr}, *d_ccm[2] = {nullptr, nullptr}, *d_cc = nullptr;
+  // ---- state: split
+  float2* s_cc2 = nullptr;
+  float *s_ccm[2] = {nullptr, nullptr}, *s_vc[2] = {nullptr, nullptr};
+  float *s_cenv_f = nullptr, *s_pump = nullptr, *s_part = nullptr, *s_phib = nullptr;
+  // ---- environment
+  double *d_cenv = nullptr, *d_phib = nullptr, *d_env_part = nullptr, *d_mem_flux_sa = nullptr,
+         *d_pump = nullptr, *d_env_scale = nullptr;
   double *d_Denv = nullptr, *d_Ex = nullptr, *d_Ey = nullptr, *d_fx = nullptr, *d_fy = nullptr,
          *d_tmp = nullptr, *d_tmp2 = nullptr, *d_venv = nullptr, *d_rho_env = nullptr;
   unsigned long long* d_status = nullptr;
-  // outputs
-  double *o_fmem = nullptr, *o_fgj = nullptr, *o_rate = nullptr, *o_rho = nullptr,
-         *o_Jn = nullptr, *o_Imem = nullptr, *o_Jcx = nullptr, *o_Jcy = nullptr,
-         *o_Jc = nullptr, *o_vmave = nullptr, *o_dvm = nullptr, *o_Ecx = nullptr,
-         *o_Ecy = nullptr, *o_Emc = nullptr, *o_Egjx = nullptr, *o_Egjy = nullptr,
-         *o_gjopen = nullptr, *o_sigma = nullptr;
-  // field outputs
-  double *d_lap = nullptr, *d_fld = nullptr;
+  // ---- outputs
+  double *o_fmem = nullptr, *o_fgj = nullptr, *o_rate = nullptr, *o_rho = nullptr, *o_Jn = nullptr,
+         *o_Imem = nullptr, *o_Jcx = nullptr, *o_Jcy = nullptr, *o_Jc = nullptr, *o_vmave = nullptr,
+         *o_dvm = nullptr, *o_Ecx = nullptr, *o_Ecy = nullptr, *o_Emc = nullptr, *o_Egjx = nullptr,
+         *o_Egjy = nullptr, *o_gjopen = nullptr, *o_sigma = nullptr, *o_vmc = nullptr,
+         *o_vm_mem = nullptr;
   int parity = 0;
   bool have_state = false, have_dm = false, have_denv = false, have_outputs = false;
   bool phib_nonzero = false;
   int64_t steps_done = 0, launches = 0;
   cudaGraphExec_t graph = nullptr;
   bool graph_valid = false;
-  int64_t neg_seen = 0;
-  std::vector<int> h_cell_ptr;
-  std::vector<int> h_m2c;
-  double env_surf_scale = 0.0;
-  double gj_len = 0.0, delta = 0.0;
+  std::vector<int> h_cell_ptr, h_m2c, h_map_env;
+  std::vector<double> h_phib;
 };
-
-using bx_cluster_ext = bx_cluster;
 
 namespace {
 
 void free_all(bx_cluster* h) {
-  void* ptrs[] = {h->d_cell_ptr, h->d_m2c, h->d_nn, h->d_nn_cell, h->d_map_env, h->d_blk,
-                  h->d_env_ptr, h->d_env_mem, h->d_bflag, h->d_touched, h->d_mem_sa, h->d_gj_w,
-                  h->d_nx, h->d_ny, h->d_swm, h->d_swo, h->d_cell_vol, h->d_cell_sa,
-                  h->d_diviterm, h->d_mem_sa_f, h->d_gj_w_f, h->d_Dm_f, h->d_Dm, h->d_vm[0],
-                  h->d_vm[1], h->d_ccm[0], h->d_ccm[1], h->d_cc, h->d_cenv, h->d_phib,
-                  h->d_env_part, h->d_mem_flux_sa, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy,
-                  h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_status, h->o_fmem, h->o_fgj,
-                  h->o_rate, h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc,
-                  h->o_vmave, h->o_dvm, h->o_Ecx, h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy,
-                  h->o_gjopen, h->o_sigma, h->d_lap, h->d_fld};
+  void* ptrs[] = {
+      h->d_cell_ptr, h->d_m2c, h->d_nn, h->d_nn_cell, h->d_map_env, h->d_blk, h->d_blk_cl, h->d_cl_blk,
+      h->d_env_ptr, h->d_env_mem, h->d_bflag, h->d_touched, h->d_lcell, h->d_mem_sa, h->d_gj_w, h->d_nx,
+      h->d_ny, h->d_swm, h->d_swo, h->d_cell_vol, h->d_cell_sa, h->d_diviterm, h->d_mem_sa_f,
+      h->d_gj_w_f, h->d_gjw0_f, h->d_dtv, h->d_dvc, h->d_Dm, h->d_Dm_f, h->d_vm[0], h->d_vm[1],
+      h->d_ccm[0], h->d_ccm[1], h->d_cc, h->s_cc2, h->s_ccm[0], h->s_ccm[1], h->s_vc[0], h->s_vc[1],
+      h->s_cenv_f, h->s_pump, h->s_part, h->s_phib, h->d_cenv, h->d_phib, h->d_env_part,
+      h->d_mem_flux_sa, h->d_pump, h->d_env_scale, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy,
+      h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
+      h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
+      h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->graph) cudaGraphExecDestroy(h->graph);
@@ -135,9 +161,8 @@ bx::StepConst make_step_const(const bx_cluster* h) {
   k.dt = p.dt;
   k.inv_cm = 1.0 / p.cm;
   k.tm = p.tm;
-  k.gj_len = 0.0;  // set by caller (geometry)
+  k.gj_len = h->gj_len;
   k.gj_block = p.gj_block;
-  k.pump_coef = -3.0 * p.nakatp_block * p.alpha_NaK;
   k.inv_KmNa = 1.0 / p.KmNK_Na;
   k.inv_KmK = 1.0 / p.KmNK_K;
   k.atp_term = p.cATP / p.KmNK_ATP;
@@ -145,21 +170,46 @@ bx::StepConst make_step_const(const bx_cluster* h) {
   k.qnum_c = (p.cADP * 1e-3) * (p.cPi * 1e-3);
   k.qden_c = p.cATP * 1e-3;
   k.K0 = std::exp(-(p.deltaGATP / RT));
-  k.pump_on = p.alpha_NaK > 0.0 ? 1.0 : 0.0;
-  k.env_scale = p.dt / (p.vol_env * (double)h->M);
   return k;
 }
 
-bx::EnvConst make_env_const(const bx_cluster* h, double delta) {
+bx::SplitConst make_split_const(const bx_cluster* h) {
+  const bx::StepConst d = make_step_const(h);
+  bx::SplitConst k{};
+  k.I = d.I;
+  k.iNa = d.iNa;
+  k.iK = d.iK;
+  for (int i = 0; i < d.I; ++i) {
+    k.zcode[i] = d.zcode[i];
+    k.z[i] = (float)d.z[i];
+    k.zF_hi[i] = (float)d.zF[i];
+    k.zF_lo[i] = (float)(d.zF[i] - (double)k.zF_hi[i]);
+    k.dgj_gs[i] = (float)d.dgj_gs[i];
+  }
+  k.F_RT = (float)d.F_RT;
+  k.inv_tm = (float)(1.0 / d.tm);
+  k.inv_gjl = (float)(1.0 / d.gj_len);
+  k.gj_block = (float)d.gj_block;
+  k.inv_KmNa = (float)d.inv_KmNa;
+  k.inv_KmK = (float)d.inv_KmK;
+  k.atp_term = (float)d.atp_term;
+  k.atp_den = (float)d.atp_den;
+  k.qnum_c = (float)d.qnum_c;
+  k.qden_c = (float)d.qden_c;
+  k.K0 = (float)d.K0;
+  return k;
+}
+
+bx::EnvConst make_env_const(const bx_cluster* h) {
   const bx_params& p = h->par;
   bx::EnvConst e{};
   e.I = h->I;
   e.ny = h->ny;
   e.nx = h->nx;
   e.G = h->G;
-  e.delta = delta;
-  e.inv_delta = 1.0 / delta;
-  e.inv_2delta = 1.0 / (2.0 * delta);
+  e.delta = h->delta;
+  e.inv_delta = 1.0 / h->delta;
+  e.inv_2delta = 1.0 / (2.0 * h->delta);
   e.dt = p.dt;
   e.sharpness = p.sharpness;
   for (int i = 0; i < h->I; ++i) {
@@ -169,35 +219,34 @@ bx::EnvConst make_env_const(const bx_cluster* h, double delta) {
   }
   e.surf_scale = h->env_surf_scale;
   e.inv_koeoer = (p.ko_env != 0.0) ? 1.0 / (p.ko_env * p.eo * p.er) : 0.0;
-  e.screen = (p.ko_env != 0.0) ? (2.0 / (p.ko_env * delta)) * (p.cell_radius / p.true_cell_size) : 0.0;
-  e.inv_h_d2 = 1.0 / (p.cell_height * delta * delta);
+  e.screen = (p.ko_env != 0.0) ? (2.0 / (p.ko_env * h->delta)) * (p.cell_radius / p.true_cell_size) : 0.0;
+  e.inv_h_d2 = 1.0 / (p.cell_height * h->delta * h->delta);
   // sigma = 1, truncate = 4: the taps scipy.ndimage.gaussian_filter uses
   double w[9], s = 0.0;
-  for (int q = -4; q <= 4; ++q) { w[q + 4] = std::exp(-0.5 * (double)(q * q)); s += w[q + 4]; }
+  for (int q = -4; q <= 4; ++q) {
+    w[q + 4] = std::exp(-0.5 * (double)(q * q));
+    s += w[q + 4];
+  }
   for (int q = 0; q < 9; ++q) e.gw[q] = w[q] / s;
   return e;
 }
 
-}  // namespace
-
-namespace {
-
-bx::DevGeom dev_geom(const bx_cluster_ext* h) {
+bx::DevGeom dev_geom(const bx_cluster* h) {
   bx::DevGeom g{};
   g.C = h->C; g.M = h->M; g.I = h->I; g.G = h->G; g.ny = h->ny; g.nx = h->nx;
   g.cell_ptr = h->d_cell_ptr; g.m2c = h->d_m2c; g.nn = h->d_nn; g.nn_cell = h->d_nn_cell;
   g.bflag = h->d_bflag; g.map_env = h->d_map_env; g.mem_sa = h->d_mem_sa; g.mem_sa_f = h->d_mem_sa_f;
   g.gj_w = h->d_gj_w; g.gj_w_f = h->d_gj_w_f; g.mem_nx = h->d_nx; g.mem_ny = h->d_ny;
   g.sw_mem = h->d_swm; g.sw_o = h->d_swo; g.cell_vol = h->d_cell_vol; g.cell_sa = h->d_cell_sa;
-  g.diviterm = h->d_diviterm; g.blk_cell = h->d_blk;
+  g.diviterm = h->d_diviterm; g.blk_cell = h->d_blk; g.blk_cluster = h->d_blk_cl;
   return g;
 }
 
-bx::StepPtrs step_ptrs(bx_cluster_ext* h, int parity) {
+bx::StepPtrs step_ptrs(bx_cluster* h, int parity) {
   bx::StepPtrs p{};
   p.vm_in = h->d_vm[parity]; p.vm_out = h->d_vm[parity ^ 1];
   p.ccm_in = h->d_ccm[parity]; p.ccm_out = h->d_ccm[parity ^ 1];
-  p.cc = h->d_cc; p.Dm = h->d_Dm; p.Dm_f = h->d_Dm_f; p.cenv = h->d_cenv;
+  p.cc = h->d_cc; p.Dm = h->d_Dm; p.Dm_f = h->d_Dm_f; p.cenv = h->d_cenv; p.pump_coef = h->d_pump;
   p.phib = h->d_phib; p.env_part = h->d_env_part; p.mem_flux_sa = h->d_mem_flux_sa;
   p.status = h->d_status;
   p.o_fmem = h->o_fmem; p.o_fgj = h->o_fgj; p.o_rate = h->o_rate; p.o_rho = h->o_rho;
@@ -208,31 +257,89 @@ bx::StepPtrs step_ptrs(bx_cluster_ext* h, int parity) {
   return p;
 }
 
+bx::SplitGeom split_geom(const bx_cluster* h) {
+  bx::SplitGeom g{};
+  g.C = h->C; g.M = h->M; g.I = h->I; g.G = h->G;
+  g.cell_ptr = h->d_cell_ptr; g.nn_cell = h->d_nn_cell; g.lcell = h->d_lcell;
+  g.mem_sa = h->d_mem_sa_f; g.gjw = h->d_gjw0_f; g.dtv = h->d_dtv; g.dvc = h->d_dvc;
+  g.blk_cell = h->d_blk; g.blk_cluster = h->d_blk_cl; g.map_env = h->d_map_env; g.nn = h->d_nn;
+  return g;
+}
+
+bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
+  bx::SplitPtrs p{};
+  p.vc_in = h->s_vc[parity]; p.vc_out = h->s_vc[parity ^ 1];
+  p.ccm_in = h->s_ccm[parity]; p.ccm_out = h->s_ccm[parity ^ 1];
+  p.cc2 = h->s_cc2; p.Dm = h->d_Dm_f; p.cenv_f = h->s_cenv_f; p.pump_coef = h->s_pump;
+  p.phib = h->s_phib; p.env_part = h->s_part; p.status = h->d_status;
+  p.o_fmem = h->o_fmem; p.o_fgj = h->o_fgj; p.o_rate = h->o_rate; p.o_rho = h->o_rho;
+  p.o_vmem = h->o_vmc;
+  return p;
+}
+
 inline int env_grid(int G) { return (G + kEnvTPB - 1) / kEnvTPB; }
 
-// Enqueue one time step (reads parity, writes parity^1).
-cudaError_t enqueue_step(bx_cluster_ext* h, int parity, bool out, cudaStream_t s) {
+cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
+  bx::SplitGeom g = split_geom(h);
+  bx::SplitPtrs p = split_ptrs(h, parity);
+  bx::SplitConst k = make_split_const(h);
+  const int code = (out ? 2 : 0) | (h->phib_nonzero ? 1 : 0);
+  switch (code) {
+    case 0: bx::k_split_step<kTPB, false, false><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+    case 1: bx::k_split_step<kTPB, false, true><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+    case 2: bx::k_split_step<kTPB, true, false><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+    default: bx::k_split_step<kTPB, true, true><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   bx::DevGeom g = dev_geom(h);
   bx::StepConst k = make_step_const(h);
-  k.gj_len = h->gj_len;
   bx::StepPtrs p = step_ptrs(h, parity);
+  if (h->mode == MODE_SPLIT_ECM)
+    return bx::launch_cell_step<float, kTPB>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+  return bx::launch_cell_step<double, kTPB>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+}
+
+// Enqueue one time step (reads parity, writes parity^1).
+cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   cudaError_t e;
-  const bool split = h->precision == BX_SPLIT_FP32;
-  if (split) {
-    e = (h->tpb == 128) ? bx::launch_cell_step<float, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k)
-                        : bx::launch_cell_step<float, 256>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
-  } else {
-    e = (h->tpb == 128) ? bx::launch_cell_step<double, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k)
-                        : bx::launch_cell_step<double, 256>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+  if (h->mode == MODE_SPLIT) {
+    e = launch_split(h, parity, out, s);
+    if (e != cudaSuccess) return e;
+    bx::k_split_env_mix<<<h->ncl, 256, 0, s>>>(h->s_part, h->d_cl_blk, h->I, h->d_cenv, h->s_cenv_f,
+                                              h->d_env_scale);
+    h->launches += 2;
+    if (out) {
+      bx::SplitOutGeom og{h->C, h->M, h->I, h->d_cell_ptr, h->d_blk, h->d_nn, h->d_map_env,
+                          h->d_mem_sa, h->d_nx, h->d_ny, h->d_swm, h->d_swo, h->d_cell_sa,
+                          h->d_gj_w, h->d_bflag};
+      bx::SplitOutPtrs op{h->o_fmem, h->o_fgj, h->s_vc[parity ^ 1], h->s_vc[parity], h->s_cc2,
+                          h->phib_nonzero ? h->s_phib : nullptr, h->o_Jn, h->o_Imem, h->o_Jcx,
+                          h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx, h->o_Ecy, h->o_Emc,
+                          h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vm_mem};
+      bx::SplitOutConst oc{};
+      const bx::StepConst d = make_step_const(h);
+      oc.I = h->I;
+      for (int i = 0; i < h->I; ++i) { oc.zF[i] = d.zF[i]; oc.sig_coef[i] = d.sig_coef[i]; }
+      oc.dt = d.dt; oc.gj_len = h->gj_len; oc.gj_block = d.gj_block;
+      bx::k_split_outputs<kTPB><<<h->nblk, kTPB, 0, s>>>(og, op, oc);
+      bx::k_split_egj<<<(h->M + 255) / 256, 256, 0, s>>>(h->M, h->d_nn, h->o_vm_mem, h->d_nx, h->d_ny,
+                                                         h->gj_len, h->o_Egjx, h->o_Egjy);
+      h->launches += 2;
+    }
+    return cudaGetLastError();
   }
+  e = launch_cell(h, parity, out, s);
   if (e != cudaSuccess) return e;
   h->launches++;
   if (!h->ecm) {
-    bx::k_env_mix<<<1, 256, 0, s>>>(h->d_env_part, h->nblk, h->I, h->d_cenv, k.env_scale);
+    bx::k_env_mix<<<h->ncl, 256, 0, s>>>(h->d_env_part, h->d_cl_blk, h->I, h->d_cenv, h->d_env_scale);
     h->launches++;
     return cudaGetLastError();
   }
-  bx::EnvConst ec = make_env_const(h, h->delta);
+  bx::EnvConst ec = make_env_const(h);
   const int gg = env_grid(h->G);
   bx::k_env_np_flux<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
   if (h->par.sharpness < 1.0) {
@@ -240,18 +347,278 @@ cudaError_t enqueue_step(bx_cluster_ext* h, int parity, bool out, cudaStream_t s
                                                   h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
     bx::k_env_integrate_scatter<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_env_ptr, h->d_env_mem,
                                                       h->d_mem_flux_sa, h->M, ec);
-    h->launches += 2;
+    h->launches += 3;
   } else {
     bx::k_env_update<true><<<gg, kEnvTPB, 0, s>>>(h->d_cenv, nullptr, h->d_fx, h->d_fy, h->d_env_ptr,
                                                  h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
-    h->launches += 1;
+    h->launches += 2;
   }
   bx::k_env_charge_gauss_y<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_touched, out ? h->d_rho_env : nullptr,
                                                  h->d_tmp, ec);
   bx::k_env_gauss_x<<<gg, kEnvTPB, 0, s>>>(h->d_tmp, h->phib_nonzero ? h->d_phib : nullptr, h->d_venv, ec);
   bx::k_env_neg_grad<<<gg, kEnvTPB, 0, s>>>(h->d_venv, ec.screen, h->d_Ex, h->d_Ey, ec);
-  h->launches += 4;
+  h->launches += 3;
   return cudaGetLastError();
+}
+
+int launches_per_step(const bx_cluster* h) {
+  if (h->mode == MODE_SPLIT) return 2;
+  if (!h->ecm) return 2;
+  return h->par.sharpness < 1.0 ? 7 : 6;
+}
+
+// per-cluster constants that depend on the parameters (dt, cm, alpha_NaK, vol_env)
+int upload_param_arrays(bx_cluster* h) {
+  std::vector<double> pump(h->ncl), escale(h->ncl);
+  std::vector<float> pump_f(h->ncl);
+  for (int c = 0; c < h->ncl; ++c) {
+    const bx_params& p = h->cl_par[c];
+    pump[c] = -3.0 * p.nakatp_block * p.alpha_NaK;
+    pump_f[c] = (float)pump[c];
+    const int Mc = h->cl_mem[c + 1] - h->cl_mem[c];
+    escale[c] = p.dt / (p.vol_env * (double)Mc);
+  }
+  BX_CU(h2d(h->d_pump, pump.data(), h->ncl));
+  BX_CU(h2d(h->d_env_scale, escale.data(), h->ncl));
+  if (h->mode == MODE_SPLIT) {
+    BX_CU(h2d(h->s_pump, pump_f.data(), h->ncl));
+    std::vector<double> vol(h->C), div(h->C);
+    BX_CU(cudaMemcpy(vol.data(), h->d_cell_vol, h->C * sizeof(double), cudaMemcpyDeviceToHost));
+    BX_CU(cudaMemcpy(div.data(), h->d_diviterm, h->C * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<float> dtv(h->C), dvc(h->C);
+    for (int c = 0; c < h->C; ++c) {
+      dtv[c] = (float)(h->par.dt / vol[c]);
+      dvc[c] = (float)(div[c] / h->par.cm);
+    }
+    BX_CU(h2d(h->d_dtv, dtv.data(), h->C));
+    BX_CU(h2d(h->d_dvc, dvc.data(), h->C));
+  }
+  return BX_OK;
+}
+
+bool same_shared_params(const bx_params& a, const bx_params& b) {
+  if (a.n_ions != b.n_ions || a.iNa != b.iNa || a.iK != b.iK || a.is_ecm != b.is_ecm) return false;
+  const double sa[] = {a.F, a.R, a.T, a.dt, a.cm, a.tm, a.gj_surface, a.gj_block, a.KmNK_Na, a.KmNK_K,
+                       a.KmNK_ATP, a.cATP, a.cADP, a.cPi, a.deltaGATP};
+  const double sb[] = {b.F, b.R, b.T, b.dt, b.cm, b.tm, b.gj_surface, b.gj_block, b.KmNK_Na, b.KmNK_K,
+                       b.KmNK_ATP, b.cATP, b.cADP, b.cPi, b.deltaGATP};
+  for (size_t q = 0; q < sizeof(sa) / sizeof(sa[0]); ++q)
+    if (sa[q] != sb[q]) return false;
+  for (int i = 0; i < a.n_ions; ++i)
+    if (a.zs[i] != b.zs[i] || a.D_gj[i] != b.D_gj[i] || a.D_free[i] != b.D_free[i]) return false;
+  return true;
+}
+
+int check_geom(const bx_geom* g, const bx_params* p) {
+  const int C = g->n_cells, M = g->n_mems;
+  if (C <= 0 || M <= 0) return fail(BX_EINVAL, "empty cluster (n_cells and n_mems must be > 0)");
+  if (g->grid_ny < 3 || g->grid_nx < 3) return fail(BX_EINVAL, "environment grid must be at least 3x3");
+  if (!g->cell_mem_ptr || !g->nn_i || !g->bflag || !g->map_mem2ecm || !g->mem_sa || !g->gj_weight ||
+      !g->cell_vol || !g->cell_sa || !g->diviterm || !g->mem_nx || !g->mem_ny || !g->smooth_weight_mem ||
+      !g->smooth_weight_o)
+    return fail(BX_EINVAL, "missing geometry array");
+  if (!(g->gj_len > 0.0) || !(g->delta > 0.0)) return fail(BX_EINVAL, "gj_len and delta must be > 0");
+  const int G = g->grid_ny * g->grid_nx;
+  // the CSR map (the bit-exact form of mem_to_cells / cell_to_mems)
+  if (g->cell_mem_ptr[0] != 0 || g->cell_mem_ptr[C] != M)
+    return fail(BX_EINVAL, "cell_mem_ptr must start at 0 and end at n_mems");
+  for (int c = 0; c < C; ++c) {
+    const int a = g->cell_mem_ptr[c], b = g->cell_mem_ptr[c + 1];
+    if (b <= a) return fail(BX_EINVAL, "cell_mem_ptr must be increasing (every cell needs a membrane)");
+    if (b - a > BX_MAX_MEMS_PER_CELL) return fail(BX_EINVAL, "a cell has more than 256 membranes");
+    if (!(g->cell_vol[c] > 0.0) || !(g->cell_sa[c] > 0.0))
+      return fail(BX_EINVAL, "cell_vol and cell_sa must be > 0");
+  }
+  for (int m = 0; m < M; ++m) {
+    if (g->nn_i[m] < 0 || g->nn_i[m] >= M) return fail(BX_EINVAL, "nn_i out of range");
+    if (g->map_mem2ecm[m] < 0 || g->map_mem2ecm[m] >= G) return fail(BX_EINVAL, "map_mem2ecm out of range");
+  }
+  if (p->is_ecm && !g->mem_sa_per_env) return fail(BX_EINVAL, "ECM needs mem_sa_per_env");
+  return BX_OK;
+}
+
+int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, bx_handle* out) {
+  if (!gs || !ps || !out || ncl <= 0) return fail(BX_EINVAL, "null argument");
+  *out = nullptr;
+  if (precision != BX_PLAIN_FP64 && precision != BX_SPLIT_FP32)
+    return fail(BX_EINVAL, "precision must be BX_PLAIN_FP64 or BX_SPLIT_FP32");
+  const bx_params& p0 = ps[0];
+  const int I = p0.n_ions;
+  if (I <= 0 || I > BX_MAX_IONS) return fail(BX_EINVAL, "n_ions must be in [1, 8]");
+  if (p0.iNa < 0 || p0.iNa >= I || p0.iK < 0 || p0.iK >= I || p0.iNa == p0.iK)
+    return fail(BX_EINVAL, "iNa/iK out of range");
+  if (ncl > 1 && p0.is_ecm) return fail(BX_EINVAL, "batches of clusters need is_ecm == 0");
+  long long Ctot = 0, Mtot = 0;
+  for (int c = 0; c < ncl; ++c) {
+    int rc = check_geom(&gs[c], &ps[c]);
+    if (rc != BX_OK) return rc;
+    if (!same_shared_params(p0, ps[c]))
+      return fail(BX_EINVAL, "clusters of a batch may differ only in alpha_NaK, nakatp_block, vol_env");
+    if (gs[c].gj_len != gs[0].gj_len) return fail(BX_EINVAL, "clusters of a batch need one gj_len");
+    Ctot += gs[c].n_cells;
+    Mtot += gs[c].n_mems;
+  }
+  if (Mtot > 0x7fffffffLL / 8) return fail(BX_EINVAL, "batch too large for int32 indexing");
+  const int C = (int)Ctot, M = (int)Mtot;
+
+  bx_cluster* h = new (std::nothrow) bx_cluster();
+  if (!h) return fail(BX_ENOMEM, "host allocation failed");
+  auto bail = [&](int code, const std::string& msg) {
+    free_all(h);
+    delete h;
+    return fail(code, msg);
+  };
+  h->ncl = ncl; h->C = C; h->M = M; h->I = I;
+  h->ny = gs[0].grid_ny; h->nx = gs[0].grid_nx; h->G = h->ny * h->nx;
+  h->precision = precision; h->par = p0; h->ecm = p0.is_ecm != 0;
+  h->cl_par.assign(ps, ps + ncl);
+  h->mode = (precision == BX_PLAIN_FP64) ? MODE_PLAIN : (h->ecm ? MODE_SPLIT_ECM : MODE_SPLIT);
+  h->gj_len = gs[0].gj_len; h->delta = gs[0].delta;
+  const int G = h->G;
+
+  // ---- concatenate the clusters
+  std::vector<int> ptr(C + 1), nn(M), m2c(M), nn_cell(M), map_env(M), blk{0}, blk_cl;
+  std::vector<uint8_t> bflag(M), lcell(M);
+  std::vector<double> msa(M), mnx(M), mny(M), gjw(M), swm(M), swo(M), vol(C), csa(C), div(C);
+  h->cl_cell.assign(ncl + 1, 0); h->cl_mem.assign(ncl + 1, 0); h->cl_blk.assign(ncl + 1, 0);
+  int coff = 0, moff = 0;
+  ptr[0] = 0;
+  for (int cl = 0; cl < ncl; ++cl) {
+    const bx_geom& g = gs[cl];
+    for (int c = 0; c < g.n_cells; ++c) {
+      ptr[coff + c + 1] = moff + g.cell_mem_ptr[c + 1];
+      vol[coff + c] = g.cell_vol[c]; csa[coff + c] = g.cell_sa[c]; div[coff + c] = g.diviterm[c];
+      for (int m = g.cell_mem_ptr[c]; m < g.cell_mem_ptr[c + 1]; ++m) m2c[moff + m] = coff + c;
+    }
+    for (int m = 0; m < g.n_mems; ++m) {
+      nn[moff + m] = moff + g.nn_i[m];
+      bflag[moff + m] = g.bflag[m] ? 1 : 0;
+      map_env[moff + m] = g.map_mem2ecm[m];
+      msa[moff + m] = g.mem_sa[m]; mnx[moff + m] = g.mem_nx[m]; mny[moff + m] = g.mem_ny[m];
+      gjw[moff + m] = g.gj_weight[m]; swm[moff + m] = g.smooth_weight_mem[m]; swo[moff + m] = g.smooth_weight_o[m];
+    }
+    // CTA partition of this cluster: whole cells, at most kTPB membranes
+    int acc = 0;
+    for (int c = 0; c < g.n_cells; ++c) {
+      const int n = g.cell_mem_ptr[c + 1] - g.cell_mem_ptr[c];
+      if (acc + n > kTPB) { blk.push_back(coff + c); blk_cl.push_back(cl); acc = 0; }
+      acc += n;
+    }
+    blk.push_back(coff + g.n_cells);
+    blk_cl.push_back(cl);
+    coff += g.n_cells;
+    moff += g.n_mems;
+    h->cl_cell[cl + 1] = coff;
+    h->cl_mem[cl + 1] = moff;
+    h->cl_blk[cl + 1] = (int)blk.size() - 1;
+  }
+  h->nblk = (int)blk.size() - 1;
+  for (int m = 0; m < M; ++m) nn_cell[m] = m2c[nn[m]];
+  for (int b = 0; b < h->nblk; ++b)
+    for (int c = blk[b]; c < blk[b + 1]; ++c)
+      for (int m = ptr[c]; m < ptr[c + 1]; ++m) lcell[m] = (uint8_t)(c - blk[b]);
+  h->h_cell_ptr = ptr; h->h_m2c = m2c; h->h_map_env = map_env;
+  h->h_phib.assign(G, 0.0);
+
+  // environment CSR (grid cell -> its membranes, ascending) for the ECM scatter
+  std::vector<int> env_ptr(G + 1, 0), env_mem(M);
+  std::vector<uint8_t> touched(G, 0);
+  if (h->ecm) {
+    for (int m = 0; m < M; ++m) env_ptr[map_env[m] + 1]++;
+    for (int k = 0; k < G; ++k) env_ptr[k + 1] += env_ptr[k];
+    std::vector<int> fill(env_ptr.begin(), env_ptr.end() - 1);
+    for (int m = 0; m < M; ++m) env_mem[fill[map_env[m]]++] = m;
+    for (int k = 0; k < G; ++k) touched[k] = env_ptr[k + 1] > env_ptr[k];
+    double s = 0.0;
+    for (int m = 0; m < M; ++m) s += gs[0].mem_sa_per_env[map_env[m]];
+    h->env_surf_scale = (p0.cell_height * h->delta * h->delta) / (s / (double)M);
+  }
+
+  if (cudaGetDevice(&h->dev) != cudaSuccess) return bail(BX_ECUDA, "no CUDA device");
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(BX_ECUDA, "cudaStreamCreate failed");
+
+#define ALLOC(ptr, n) \
+  if (dalloc(&(ptr), (size_t)(n)) != cudaSuccess) return bail(BX_ENOMEM, "cudaMalloc " #ptr)
+#define H2D(dst, src, n) \
+  if (h2d((dst), (src), (size_t)(n)) != cudaSuccess) return bail(BX_ECUDA, "copy " #dst)
+  ALLOC(h->d_cell_ptr, C + 1); H2D(h->d_cell_ptr, ptr.data(), C + 1);
+  ALLOC(h->d_m2c, M); H2D(h->d_m2c, m2c.data(), M);
+  ALLOC(h->d_nn, M); H2D(h->d_nn, nn.data(), M);
+  ALLOC(h->d_nn_cell, M); H2D(h->d_nn_cell, nn_cell.data(), M);
+  ALLOC(h->d_map_env, M); H2D(h->d_map_env, map_env.data(), M);
+  ALLOC(h->d_blk, blk.size()); H2D(h->d_blk, blk.data(), blk.size());
+  ALLOC(h->d_blk_cl, blk_cl.size()); H2D(h->d_blk_cl, blk_cl.data(), blk_cl.size());
+  ALLOC(h->d_cl_blk, ncl + 1); H2D(h->d_cl_blk, h->cl_blk.data(), ncl + 1);
+  ALLOC(h->d_bflag, M); H2D(h->d_bflag, bflag.data(), M);
+  ALLOC(h->d_mem_sa, M); H2D(h->d_mem_sa, msa.data(), M);
+  ALLOC(h->d_gj_w, M); H2D(h->d_gj_w, gjw.data(), M);
+  ALLOC(h->d_nx, M); H2D(h->d_nx, mnx.data(), M);
+  ALLOC(h->d_ny, M); H2D(h->d_ny, mny.data(), M);
+  ALLOC(h->d_swm, M); H2D(h->d_swm, swm.data(), M);
+  ALLOC(h->d_swo, M); H2D(h->d_swo, swo.data(), M);
+  ALLOC(h->d_cell_vol, C); H2D(h->d_cell_vol, vol.data(), C);
+  ALLOC(h->d_cell_sa, C); H2D(h->d_cell_sa, csa.data(), C);
+  ALLOC(h->d_diviterm, C); H2D(h->d_diviterm, div.data(), C);
+  ALLOC(h->d_pump, ncl); ALLOC(h->d_env_scale, ncl);
+  ALLOC(h->d_phib, G);
+  ALLOC(h->d_status, 4);
+  if (cudaMemset(h->d_status, 0, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(h->d_phib, 0, (size_t)G * sizeof(double)) != cudaSuccess)
+    return bail(BX_ECUDA, "cudaMemset");
+  if (h->mode == MODE_SPLIT) {
+    std::vector<float> fsa(M), gw0(M);
+    for (int m = 0; m < M; ++m) { fsa[m] = (float)msa[m]; gw0[m] = bflag[m] ? 0.0f : (float)gjw[m]; }
+    ALLOC(h->d_lcell, M); H2D(h->d_lcell, lcell.data(), M);
+    ALLOC(h->d_mem_sa_f, M); H2D(h->d_mem_sa_f, fsa.data(), M);
+    ALLOC(h->d_gjw0_f, M); H2D(h->d_gjw0_f, gw0.data(), M);
+    ALLOC(h->d_dtv, C); ALLOC(h->d_dvc, C);
+    ALLOC(h->d_Dm_f, (size_t)I * M);
+    ALLOC(h->s_cc2, (size_t)I * C);
+    ALLOC(h->s_ccm[0], (size_t)I * C); ALLOC(h->s_ccm[1], (size_t)I * C);
+    ALLOC(h->s_vc[0], C); ALLOC(h->s_vc[1], C);
+    ALLOC(h->s_cenv_f, (size_t)ncl * I); ALLOC(h->d_cenv, (size_t)ncl * I);
+    ALLOC(h->s_pump, ncl);
+    ALLOC(h->s_part, (size_t)h->nblk * I);
+    ALLOC(h->s_phib, G);
+    if (cudaMemset(h->s_phib, 0, (size_t)G * sizeof(float)) != cudaSuccess) return bail(BX_ECUDA, "cudaMemset");
+    ALLOC(h->o_vmc, C); ALLOC(h->o_vm_mem, M);
+  } else {
+    std::vector<float> fsa(M), fgw(M);
+    for (int m = 0; m < M; ++m) { fsa[m] = (float)msa[m]; fgw[m] = (float)gjw[m]; }
+    ALLOC(h->d_mem_sa_f, M); H2D(h->d_mem_sa_f, fsa.data(), M);
+    ALLOC(h->d_gj_w_f, M); H2D(h->d_gj_w_f, fgw.data(), M);
+    if (h->mode == MODE_SPLIT_ECM) { ALLOC(h->d_Dm_f, (size_t)I * M); } else { ALLOC(h->d_Dm, (size_t)I * M); }
+    ALLOC(h->d_vm[0], M); ALLOC(h->d_vm[1], M);
+    ALLOC(h->d_ccm[0], (size_t)I * C); ALLOC(h->d_ccm[1], (size_t)I * C);
+    ALLOC(h->d_cc, (size_t)I * C);
+    ALLOC(h->d_cenv, h->ecm ? (size_t)I * G : (size_t)ncl * I);
+    ALLOC(h->d_env_part, (size_t)h->nblk * I);
+  }
+  if (h->ecm) {
+    ALLOC(h->d_env_ptr, G + 1); H2D(h->d_env_ptr, env_ptr.data(), G + 1);
+    ALLOC(h->d_env_mem, M); H2D(h->d_env_mem, env_mem.data(), M);
+    ALLOC(h->d_touched, G); H2D(h->d_touched, touched.data(), G);
+    ALLOC(h->d_mem_flux_sa, (size_t)I * M);
+    ALLOC(h->d_Denv, (size_t)I * G);
+    ALLOC(h->d_Ex, G); ALLOC(h->d_Ey, G);
+    ALLOC(h->d_fx, (size_t)I * G); ALLOC(h->d_fy, (size_t)I * G);
+    ALLOC(h->d_tmp, G); ALLOC(h->d_tmp2, (size_t)I * G);
+    ALLOC(h->d_venv, G); ALLOC(h->d_rho_env, G);
+  }
+  ALLOC(h->o_fmem, (size_t)I * M); ALLOC(h->o_fgj, (size_t)I * M);
+  ALLOC(h->o_rate, M); ALLOC(h->o_rho, C); ALLOC(h->o_Jn, M); ALLOC(h->o_Imem, M);
+  ALLOC(h->o_Jcx, C); ALLOC(h->o_Jcy, C); ALLOC(h->o_Jc, M); ALLOC(h->o_vmave, C);
+  ALLOC(h->o_dvm, M); ALLOC(h->o_Ecx, C); ALLOC(h->o_Ecy, C); ALLOC(h->o_Emc, M);
+  ALLOC(h->o_Egjx, M); ALLOC(h->o_Egjy, M); ALLOC(h->o_gjopen, M); ALLOC(h->o_sigma, C);
+#undef ALLOC
+#undef H2D
+  if (upload_param_arrays(h) != BX_OK) {
+    std::string msg = g_err;
+    return bail(BX_ECUDA, msg);
+  }
+  *out = h;
+  return BX_OK;
 }
 
 }  // namespace
@@ -262,318 +629,242 @@ int bx_abi_version(void) { return BX_ABI_VERSION; }
 const char* bx_last_error(void) { return g_err.c_str(); }
 
 int bx_cluster_create(const bx_geom* g, const bx_params* p, int precision, bx_handle* out) {
-  if (!g || !p || !out) return fail(BX_EINVAL, "null argument");
-  *out = nullptr;
-  if (precision != BX_PLAIN_FP64 && precision != BX_SPLIT_FP32)
-    return fail(BX_EINVAL, "precision must be BX_PLAIN_FP64 or BX_SPLIT_FP32");
-  const int C = g->n_cells, M = g->n_mems, I = p->n_ions;
-  if (C <= 0 || M <= 0) return fail(BX_EINVAL, "empty cluster (n_cells and n_mems must be > 0)");
-  if (I <= 0 || I > BX_MAX_IONS) return fail(BX_EINVAL, "n_ions must be in [1, 8]");
-  if (p->iNa < 0 || p->iNa >= I || p->iK < 0 || p->iK >= I || p->iNa == p->iK)
-    return fail(BX_EINVAL, "iNa/iK out of range");
-  if (g->grid_ny < 3 || g->grid_nx < 3) return fail(BX_EINVAL, "environment grid must be at least 3x3");
-  if (!g->cell_mem_ptr || !g->nn_i || !g->bflag || !g->map_mem2ecm || !g->mem_sa || !g->gj_weight ||
-      !g->cell_vol || !g->cell_sa || !g->diviterm || !g->mem_nx || !g->mem_ny ||
-      !g->smooth_weight_mem || !g->smooth_weight_o)
-    return fail(BX_EINVAL, "missing geometry array");
-  if (!(g->gj_len > 0.0) || !(g->delta > 0.0)) return fail(BX_EINVAL, "gj_len and delta must be > 0");
-  const int G = g->grid_ny * g->grid_nx;
-  // ---- validate the CSR map (the bit-exact form of mem_to_cells / cell_to_mems)
-  if (g->cell_mem_ptr[0] != 0 || g->cell_mem_ptr[C] != M)
-    return fail(BX_EINVAL, "cell_mem_ptr must start at 0 and end at n_mems");
-  std::vector<int> m2c(M);
-  for (int c = 0; c < C; ++c) {
-    const int a = g->cell_mem_ptr[c], b = g->cell_mem_ptr[c + 1];
-    if (b < a) return fail(BX_EINVAL, "cell_mem_ptr must be non-decreasing");
-    if (b - a > BX_MAX_MEMS_PER_CELL) return fail(BX_EINVAL, "a cell has more than 256 membranes");
-    for (int m = a; m < b; ++m) m2c[m] = c;
-  }
-  std::vector<int> nn_cell(M);
-  for (int m = 0; m < M; ++m) {
-    const int n = g->nn_i[m];
-    if (n < 0 || n >= M) return fail(BX_EINVAL, "nn_i out of range");
-    nn_cell[m] = m2c[n];
-    const int e = g->map_mem2ecm[m];
-    if (e < 0 || e >= G) return fail(BX_EINVAL, "map_mem2ecm out of range");
-  }
-  for (int c = 0; c < C; ++c)
-    if (!(g->cell_vol[c] > 0.0) || !(g->cell_sa[c] > 0.0))
-      return fail(BX_EINVAL, "cell_vol and cell_sa must be > 0");
-  if (p->is_ecm && !g->mem_sa_per_env) return fail(BX_EINVAL, "ECM needs mem_sa_per_env");
+  return create_impl(g, p, 1, precision, out);
+}
 
-  bx_cluster_ext* h = new (std::nothrow) bx_cluster_ext();
-  if (!h) return fail(BX_ENOMEM, "host allocation failed");
-  h->C = C; h->M = M; h->I = I; h->G = G; h->ny = g->grid_ny; h->nx = g->grid_nx;
-  h->precision = precision; h->par = *p; h->ecm = p->is_ecm != 0;
-  h->gj_len = g->gj_len; h->delta = g->delta;
-  h->h_cell_ptr.assign(g->cell_mem_ptr, g->cell_mem_ptr + C + 1);
-  h->h_m2c = m2c;
-  int rc = BX_OK;
-  auto bail = [&](int code, const std::string& msg) {
-    free_all(h);
-    delete h;
-    return fail(code, msg);
-  };
-  if (cudaGetDevice(&h->dev) != cudaSuccess) return bail(BX_ECUDA, "no CUDA device");
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
-    return bail(BX_ECUDA, "cudaStreamCreate failed");
+int bx_batch_create(const bx_geom* g, const bx_params* p, int n_clusters, int precision, bx_handle* out) {
+  return create_impl(g, p, n_clusters, precision, out);
+}
 
-  // ---- CTA partition: whole cells, at most tpb membranes each
-  h->tpb = 256;
-  std::vector<int> blk{0};
-  {
-    int acc = 0;
-    for (int c = 0; c < C; ++c) {
-      const int n = g->cell_mem_ptr[c + 1] - g->cell_mem_ptr[c];
-      if (acc + n > h->tpb && acc > 0) { blk.push_back(c); acc = 0; }
-      acc += n;
-    }
-    blk.push_back(C);
+int bx_batch_layout(bx_handle h, int32_t* cell_offsets, int32_t* mem_offsets) {
+  if (!h || !cell_offsets || !mem_offsets) return fail(BX_EINVAL, "null argument");
+  for (int c = 0; c <= h->ncl; ++c) {
+    cell_offsets[c] = h->cl_cell[c];
+    mem_offsets[c] = h->cl_mem[c];
   }
-  h->nblk = (int)blk.size() - 1;
-
-  // ---- environment CSR (grid cell -> its membranes, ascending) for the ECM scatter
-  std::vector<int> env_ptr(G + 1, 0), env_mem(M);
-  std::vector<uint8_t> touched(G, 0);
-  for (int m = 0; m < M; ++m) env_ptr[g->map_mem2ecm[m] + 1]++;
-  for (int k = 0; k < G; ++k) env_ptr[k + 1] += env_ptr[k];
-  {
-    std::vector<int> fill(env_ptr.begin(), env_ptr.end() - 1);
-    for (int m = 0; m < M; ++m) env_mem[fill[g->map_mem2ecm[m]]++] = m;
-  }
-  for (int k = 0; k < G; ++k) touched[k] = env_ptr[k + 1] > env_ptr[k];
-  if (h->ecm) {
-    double s = 0.0;
-    for (int m = 0; m < M; ++m) s += g->mem_sa_per_env[g->map_mem2ecm[m]];
-    const double mean = s / (double)M;  // memSa_per_envSquare[map_mem2ecm].mean()
-    h->env_surf_scale = (p->cell_height * g->delta * g->delta) / mean;
-  }
-
-  std::vector<float> fsa(M), fgw(M);
-  for (int m = 0; m < M; ++m) { fsa[m] = (float)g->mem_sa[m]; fgw[m] = (float)g->gj_weight[m]; }
-  std::vector<double> gjw(g->gj_weight, g->gj_weight + M);
-
-#define ALLOC(ptr, n) if (dalloc(&(ptr), (size_t)(n)) != cudaSuccess) return bail(BX_ENOMEM, "cudaMalloc " #ptr)
-#define H2D(dst, src, n) if (cudaMemcpy((dst), (src), sizeof(*(dst)) * (size_t)(n), cudaMemcpyHostToDevice) != cudaSuccess) return bail(BX_ECUDA, "copy " #dst)
-  ALLOC(h->d_cell_ptr, C + 1); H2D(h->d_cell_ptr, g->cell_mem_ptr, C + 1);
-  ALLOC(h->d_m2c, M); H2D(h->d_m2c, m2c.data(), M);
-  ALLOC(h->d_nn, M); H2D(h->d_nn, g->nn_i, M);
-  ALLOC(h->d_nn_cell, M); H2D(h->d_nn_cell, nn_cell.data(), M);
-  ALLOC(h->d_map_env, M); H2D(h->d_map_env, g->map_mem2ecm, M);
-  ALLOC(h->d_blk, blk.size()); H2D(h->d_blk, blk.data(), blk.size());
-  ALLOC(h->d_env_ptr, G + 1); H2D(h->d_env_ptr, env_ptr.data(), G + 1);
-  ALLOC(h->d_env_mem, M); H2D(h->d_env_mem, env_mem.data(), M);
-  ALLOC(h->d_touched, G); H2D(h->d_touched, touched.data(), G);
-  ALLOC(h->d_bflag, M); H2D(h->d_bflag, g->bflag, M);
-  ALLOC(h->d_mem_sa, M); H2D(h->d_mem_sa, g->mem_sa, M);
-  ALLOC(h->d_mem_sa_f, M); H2D(h->d_mem_sa_f, fsa.data(), M);
-  ALLOC(h->d_gj_w, M); H2D(h->d_gj_w, gjw.data(), M);
-  ALLOC(h->d_gj_w_f, M); H2D(h->d_gj_w_f, fgw.data(), M);
-  ALLOC(h->d_nx, M); H2D(h->d_nx, g->mem_nx, M);
-  ALLOC(h->d_ny, M); H2D(h->d_ny, g->mem_ny, M);
-  ALLOC(h->d_swm, M); H2D(h->d_swm, g->smooth_weight_mem, M);
-  ALLOC(h->d_swo, M); H2D(h->d_swo, g->smooth_weight_o, M);
-  ALLOC(h->d_cell_vol, C); H2D(h->d_cell_vol, g->cell_vol, C);
-  ALLOC(h->d_cell_sa, C); H2D(h->d_cell_sa, g->cell_sa, C);
-  ALLOC(h->d_diviterm, C); H2D(h->d_diviterm, g->diviterm, C);
-  if (precision == BX_SPLIT_FP32) { ALLOC(h->d_Dm_f, (size_t)I * M); }
-  else { ALLOC(h->d_Dm, (size_t)I * M); }
-  ALLOC(h->d_vm[0], M); ALLOC(h->d_vm[1], M);
-  ALLOC(h->d_ccm[0], (size_t)I * C); ALLOC(h->d_ccm[1], (size_t)I * C);
-  ALLOC(h->d_cc, (size_t)I * C);
-  ALLOC(h->d_cenv, h->ecm ? (size_t)I * G : (size_t)I);
-  ALLOC(h->d_phib, G);
-  ALLOC(h->d_env_part, (size_t)h->nblk * I);
-  ALLOC(h->d_status, 4);
-  if (cudaMemset(h->d_status, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) return bail(BX_ECUDA, "memset");
-  if (cudaMemset(h->d_phib, 0, G * sizeof(double)) != cudaSuccess) return bail(BX_ECUDA, "memset");
-  if (h->ecm) {
-    ALLOC(h->d_mem_flux_sa, (size_t)I * M);
-    ALLOC(h->d_Denv, (size_t)I * G);
-    ALLOC(h->d_Ex, G); ALLOC(h->d_Ey, G);
-    ALLOC(h->d_fx, (size_t)I * G); ALLOC(h->d_fy, (size_t)I * G);
-    ALLOC(h->d_tmp, G); ALLOC(h->d_tmp2, (size_t)I * G);
-    ALLOC(h->d_venv, G); ALLOC(h->d_rho_env, G);
-  }
-  // outputs
-  ALLOC(h->o_fmem, (size_t)I * M); ALLOC(h->o_fgj, (size_t)I * M);
-  ALLOC(h->o_rate, M); ALLOC(h->o_rho, C); ALLOC(h->o_Jn, M); ALLOC(h->o_Imem, M);
-  ALLOC(h->o_Jcx, C); ALLOC(h->o_Jcy, C); ALLOC(h->o_Jc, M); ALLOC(h->o_vmave, C);
-  ALLOC(h->o_dvm, M); ALLOC(h->o_Ecx, C); ALLOC(h->o_Ecy, C); ALLOC(h->o_Emc, M);
-  ALLOC(h->o_Egjx, M); ALLOC(h->o_Egjy, M); ALLOC(h->o_gjopen, M); ALLOC(h->o_sigma, C);
-#undef ALLOC
-#undef H2D
-  (void)rc;
-  *out = h;
   return BX_OK;
 }
 
-void bx_destroy(bx_handle hh) {
-  if (!hh) return;
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+void bx_destroy(bx_handle h) {
+  if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_all(h);
   delete h;
 }
 
-int bx_set_params(bx_handle hh, const bx_params* p) {
-  if (!hh || !p) return fail(BX_EINVAL, "null argument");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_set_params(bx_handle h, const bx_params* p) {
+  if (!h || !p) return fail(BX_EINVAL, "null argument");
   if (p->n_ions != h->I || (p->is_ecm != 0) != h->ecm)
     return fail(BX_EINVAL, "n_ions / is_ecm cannot change after create");
+  if (h->ncl > 1) return fail(BX_EINVAL, "use bx_batch_set_params for a batch");
   h->par = *p;
+  h->cl_par[0] = *p;
   h->graph_valid = false;
-  return BX_OK;
+  return upload_param_arrays(h);
 }
 
-int bx_set_membrane_diffusivity(bx_handle hh, const double* Dm) {
-  if (!hh || !Dm) return fail(BX_EINVAL, "null argument");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_batch_set_params(bx_handle h, const bx_params* p) {
+  if (!h || !p) return fail(BX_EINVAL, "null argument");
+  for (int c = 0; c < h->ncl; ++c)
+    if (!same_shared_params(p[0], p[c]) || p[c].n_ions != h->I || (p[c].is_ecm != 0) != h->ecm)
+      return fail(BX_EINVAL, "clusters of a batch may differ only in alpha_NaK, nakatp_block, vol_env");
+  h->par = p[0];
+  h->cl_par.assign(p, p + h->ncl);
+  h->graph_valid = false;
+  return upload_param_arrays(h);
+}
+
+int bx_set_membrane_diffusivity(bx_handle h, const double* Dm) {
+  if (!h || !Dm) return fail(BX_EINVAL, "null argument");
   const size_t n = (size_t)h->I * h->M;
   for (size_t q = 0; q < n; ++q)
-    if (!(Dm[q] >= 0.0)) return fail(BX_EINVAL, "Dm must be finite and >= 0");
-  if (h->precision == BX_SPLIT_FP32) {
+    if (!(Dm[q] >= 0.0) || Dm[q] == INFINITY) return fail(BX_EINVAL, "Dm must be finite and >= 0");
+  BX_CU(cudaStreamSynchronize(h->stream));
+  if (h->d_Dm_f) {
     std::vector<float> f(n);
     for (size_t q = 0; q < n; ++q) f[q] = (float)Dm[q];
-    BX_CU(cudaMemcpyAsync(h->d_Dm_f, f.data(), n * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-    BX_CU(cudaStreamSynchronize(h->stream));
+    BX_CU(cudaMemcpy(h->d_Dm_f, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
   } else {
-    BX_CU(cudaMemcpyAsync(h->d_Dm, Dm, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    BX_CU(cudaStreamSynchronize(h->stream));
+    BX_CU(cudaMemcpy(h->d_Dm, Dm, n * sizeof(double), cudaMemcpyHostToDevice));
   }
   h->have_dm = true;
   return BX_OK;
 }
 
-int bx_set_env_diffusivity(bx_handle hh, const double* D_env) {
-  if (!hh || !D_env) return fail(BX_EINVAL, "null argument");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_set_env_diffusivity(bx_handle h, const double* D_env) {
+  if (!h || !D_env) return fail(BX_EINVAL, "null argument");
   if (!h->ecm) return fail(BX_EINVAL, "environment diffusivity needs is_ecm");
-  BX_CU(cudaMemcpyAsync(h->d_Denv, D_env, (size_t)h->I * h->G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   BX_CU(cudaStreamSynchronize(h->stream));
+  BX_CU(cudaMemcpy(h->d_Denv, D_env, (size_t)h->I * h->G * sizeof(double), cudaMemcpyHostToDevice));
   h->have_denv = true;
   return BX_OK;
 }
 
-int bx_set_boundary_potential(bx_handle hh, const double* Phi_b) {
-  if (!hh) return fail(BX_EINVAL, "null handle");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_set_boundary_potential(bx_handle h, const double* Phi_b) {
+  if (!h) return fail(BX_EINVAL, "null handle");
   bool nz = false;
-  if (Phi_b) for (int k = 0; k < h->G; ++k) nz |= (Phi_b[k] != 0.0);
-  if (nz) {
-    BX_CU(cudaMemcpyAsync(h->d_phib, Phi_b, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  } else {
-    BX_CU(cudaMemsetAsync(h->d_phib, 0, (size_t)h->G * sizeof(double), h->stream));
-  }
+  if (Phi_b)
+    for (int k = 0; k < h->G; ++k) nz |= (Phi_b[k] != 0.0);
+  if (nz && h->ncl > 1) return fail(BX_EINVAL, "a boundary potential needs a single cluster");
   BX_CU(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < h->G; ++k) h->h_phib[k] = nz ? Phi_b[k] : 0.0;
+  BX_CU(cudaMemcpy(h->d_phib, h->h_phib.data(), (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice));
+  if (h->s_phib) {
+    std::vector<float> f(h->G);
+    for (int k = 0; k < h->G; ++k) f[k] = (float)h->h_phib[k];
+    BX_CU(cudaMemcpy(h->s_phib, f.data(), (size_t)h->G * sizeof(float), cudaMemcpyHostToDevice));
+  }
   if (nz != h->phib_nonzero) h->graph_valid = false;
   h->phib_nonzero = nz;
   return BX_OK;
 }
 
-int bx_state_upload(bx_handle hh, const bx_state* s) {
-  if (!hh || !s || !s->vm || !s->cc_cells || !s->cc_at_mem || !s->cc_env)
+int bx_state_upload(bx_handle h, const bx_state* s) {
+  if (!h || !s || !s->vm || !s->cc_cells || !s->cc_at_mem || !s->cc_env)
     return fail(BX_EINVAL, "null argument");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
   const int C = h->C, M = h->M, I = h->I;
+  const std::vector<int>& ptr = h->h_cell_ptr;
   std::vector<double> ccm((size_t)I * C);
   for (int i = 0; i < I; ++i)
     for (int c = 0; c < C; ++c) {
-      const int a = h->h_cell_ptr[c], b = h->h_cell_ptr[c + 1];
-      const double v = (b > a) ? s->cc_at_mem[(size_t)i * M + a] : s->cc_cells[(size_t)i * C + c];
-      for (int m = a + 1; m < b; ++m)
+      const double v = s->cc_at_mem[(size_t)i * M + ptr[c]];
+      for (int m = ptr[c] + 1; m < ptr[c + 1]; ++m)
         if (s->cc_at_mem[(size_t)i * M + m] != v)
           return fail(BX_EINVAL, "cc_at_mem must be constant over each cell's membranes");
       ccm[(size_t)i * C + c] = v;
     }
   if (h->ecm && (!s->E_env_x || !s->E_env_y)) return fail(BX_EINVAL, "ECM state needs E_env_x/E_env_y");
-  h->parity = 0;
-  BX_CU(cudaMemcpyAsync(h->d_vm[0], s->vm, (size_t)M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  BX_CU(cudaMemcpyAsync(h->d_cc, s->cc_cells, (size_t)I * C * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  BX_CU(cudaMemcpyAsync(h->d_ccm[0], ccm.data(), (size_t)I * C * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  BX_CU(cudaMemcpyAsync(h->d_cenv, s->cc_env, (h->ecm ? (size_t)I * h->G : (size_t)I) * sizeof(double),
-                        cudaMemcpyHostToDevice, h->stream));
-  if (h->ecm) {
-    BX_CU(cudaMemcpyAsync(h->d_Ex, s->E_env_x, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    BX_CU(cudaMemcpyAsync(h->d_Ey, s->E_env_y, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  }
   BX_CU(cudaStreamSynchronize(h->stream));
+  h->parity = 0;
+  const size_t nenv = h->ecm ? (size_t)I * h->G : (size_t)h->ncl * I;
+  if (h->mode == MODE_SPLIT) {
+    // Vmem is constant per cell (minus Phi_b per membrane) in BETSE's full
+    // solver with cell_polarizability == 0 (sim.py:2027-2029)
+    std::vector<float> vc(C), ccmf((size_t)I * C);
+    std::vector<float2> cc2((size_t)I * C);
+    for (int c = 0; c < C; ++c) {
+      const double v0 = s->vm[ptr[c]] + h->h_phib[h->h_map_env[ptr[c]]];
+      for (int m = ptr[c] + 1; m < ptr[c + 1]; ++m) {
+        const double v = s->vm[m] + h->h_phib[h->h_map_env[m]];
+        if (std::fabs(v - v0) > 1e-12 * std::fabs(v0) + 1e-18)
+          return fail(BX_EINVAL, "split form: vm must be uniform over each cell's membranes");
+      }
+      vc[c] = (float)v0;
+    }
+    for (size_t q = 0; q < (size_t)I * C; ++q) {
+      const double x = s->cc_cells[q];
+      const float hi = (float)x;
+      cc2[q] = make_float2(hi, (float)(x - (double)hi));
+      ccmf[q] = (float)ccm[q];
+    }
+    std::vector<float> cef(nenv);
+    for (size_t q = 0; q < nenv; ++q) cef[q] = (float)s->cc_env[q];
+    BX_CU(h2d(h->s_vc[0], vc.data(), C));
+    BX_CU(h2d(h->s_cc2, cc2.data(), cc2.size()));
+    BX_CU(h2d(h->s_ccm[0], ccmf.data(), ccmf.size()));
+    BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
+    BX_CU(h2d(h->s_cenv_f, cef.data(), nenv));
+  } else {
+    BX_CU(h2d(h->d_vm[0], s->vm, M));
+    BX_CU(h2d(h->d_cc, s->cc_cells, (size_t)I * C));
+    BX_CU(h2d(h->d_ccm[0], ccm.data(), ccm.size()));
+    BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
+    if (h->ecm) {
+      BX_CU(h2d(h->d_Ex, s->E_env_x, h->G));
+      BX_CU(h2d(h->d_Ey, s->E_env_y, h->G));
+    }
+  }
   h->have_state = true;
   h->have_outputs = false;
   return BX_OK;
 }
 
-int bx_state_download(bx_handle hh, bx_state* s) {
-  if (!hh || !s) return fail(BX_EINVAL, "null argument");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_state_download(bx_handle h, bx_state* s) {
+  if (!h || !s) return fail(BX_EINVAL, "null argument");
   if (!h->have_state) return fail(BX_ESTATE, "no state uploaded");
   const int C = h->C, M = h->M, I = h->I;
   BX_CU(cudaStreamSynchronize(h->stream));
-  if (s->vm) BX_CU(cudaMemcpy(s->vm, h->d_vm[h->parity], (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
-  if (s->cc_cells) BX_CU(cudaMemcpy(s->cc_cells, h->d_cc, (size_t)I * C * sizeof(double), cudaMemcpyDeviceToHost));
-  if (s->cc_at_mem) {
-    std::vector<double> ccm((size_t)I * C);
+  const size_t nenv = h->ecm ? (size_t)I * h->G : (size_t)h->ncl * I;
+  std::vector<double> ccm((size_t)I * C);
+  if (h->mode == MODE_SPLIT) {
+    std::vector<float> vc(C), ccmf((size_t)I * C);
+    std::vector<float2> cc2((size_t)I * C);
+    BX_CU(cudaMemcpy(vc.data(), h->s_vc[h->parity], C * sizeof(float), cudaMemcpyDeviceToHost));
+    BX_CU(cudaMemcpy(cc2.data(), h->s_cc2, cc2.size() * sizeof(float2), cudaMemcpyDeviceToHost));
+    BX_CU(cudaMemcpy(ccmf.data(), h->s_ccm[h->parity], ccmf.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    if (s->vm)
+      for (int m = 0; m < M; ++m) s->vm[m] = (double)vc[h->h_m2c[m]] - h->h_phib[h->h_map_env[m]];
+    if (s->cc_cells)
+      for (size_t q = 0; q < cc2.size(); ++q) s->cc_cells[q] = (double)cc2[q].x + (double)cc2[q].y;
+    for (size_t q = 0; q < ccm.size(); ++q) ccm[q] = (double)ccmf[q];
+  } else {
+    if (s->vm) BX_CU(cudaMemcpy(s->vm, h->d_vm[h->parity], (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
+    if (s->cc_cells)
+      BX_CU(cudaMemcpy(s->cc_cells, h->d_cc, (size_t)I * C * sizeof(double), cudaMemcpyDeviceToHost));
     BX_CU(cudaMemcpy(ccm.data(), h->d_ccm[h->parity], ccm.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (h->ecm) {
+      if (s->E_env_x) BX_CU(cudaMemcpy(s->E_env_x, h->d_Ex, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
+      if (s->E_env_y) BX_CU(cudaMemcpy(s->E_env_y, h->d_Ey, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+  }
+  if (s->cc_at_mem)
     for (int i = 0; i < I; ++i)
       for (int m = 0; m < M; ++m) s->cc_at_mem[(size_t)i * M + m] = ccm[(size_t)i * C + h->h_m2c[m]];
-  }
-  if (s->cc_env)
-    BX_CU(cudaMemcpy(s->cc_env, h->d_cenv, (h->ecm ? (size_t)I * h->G : (size_t)I) * sizeof(double),
-                     cudaMemcpyDeviceToHost));
-  if (h->ecm) {
-    if (s->E_env_x) BX_CU(cudaMemcpy(s->E_env_x, h->d_Ex, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
-    if (s->E_env_y) BX_CU(cudaMemcpy(s->E_env_y, h->d_Ey, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
-  }
+  if (s->cc_env) BX_CU(cudaMemcpy(s->cc_env, h->d_cenv, nenv * sizeof(double), cudaMemcpyDeviceToHost));
   return BX_OK;
 }
 
-int bx_step(bx_handle hh, int n_steps, int want_outputs, void* stream) {
-  if (!hh) return fail(BX_EINVAL, "null handle");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream) {
+  if (!h) return fail(BX_EINVAL, "null handle");
   if (n_steps < 0) return fail(BX_EINVAL, "n_steps must be >= 0");
   if (!h->have_state) return fail(BX_ESTATE, "bx_step before bx_state_upload");
   if (!h->have_dm) return fail(BX_ESTATE, "bx_step before bx_set_membrane_diffusivity");
   if (h->ecm && !h->have_denv) return fail(BX_ESTATE, "ECM step before bx_set_env_diffusivity");
   if (n_steps == 0) return BX_OK;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  cudaEvent_t ev = nullptr;
   if (s != h->stream) {
-    // order the caller's stream after the handle's pending work
-    cudaEvent_t ev;
+    // the caller's stream runs after the handle's pending work
     BX_CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     BX_CU(cudaEventRecord(ev, h->stream));
     BX_CU(cudaStreamWaitEvent(s, ev, 0));
-    cudaEventDestroy(ev);
   }
   int left = n_steps;
   const int tail_out = want_outputs ? 1 : 0;
-  // graph-captured chunks of kGraphChunk steps from parity 0
   if (left - tail_out >= kGraphChunk) {
     if (h->parity != 0) {
-      if (enqueue_step(h, h->parity, false, s) != cudaSuccess) return fail(BX_ECUDA, cudaGetErrorString(cudaGetLastError()));
-      h->parity ^= 1; --left;
+      cudaError_t e = enqueue_step(h, h->parity, false, s);
+      if (e != cudaSuccess) return fail(BX_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
+      h->parity ^= 1;
+      --left;
     }
     if (!h->graph_valid) {
-      if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+      if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+      }
       cudaStream_t cs;
       BX_CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       cudaGraph_t graph;
       const int64_t l0 = h->launches;
       BX_CU(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
       int par = 0;
-      for (int q = 0; q < kGraphChunk; ++q) { enqueue_step(h, par, false, cs); par ^= 1; }
+      for (int q = 0; q < kGraphChunk; ++q) {
+        enqueue_step(h, par, false, cs);
+        par ^= 1;
+      }
       cudaError_t ce = cudaStreamEndCapture(cs, &graph);
       cudaStreamDestroy(cs);
-      h->launches = l0;  // captured launches are counted on replay
+      h->launches = l0;  // captured launches are counted when the graph replays
       if (ce != cudaSuccess) return fail(BX_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
       ce = cudaGraphInstantiate(&h->graph, graph, 0);
       cudaGraphDestroy(graph);
       if (ce != cudaSuccess) return fail(BX_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
       h->graph_valid = true;
     }
-    const int per_step_launches = h->ecm ? ((h->par.sharpness < 1.0) ? 7 : 6) : 2;
     while (left - tail_out >= kGraphChunk) {
       BX_CU(cudaGraphLaunch(h->graph, s));
-      h->launches += (int64_t)kGraphChunk * per_step_launches;
+      h->launches += (int64_t)kGraphChunk * launches_per_step(h);
       left -= kGraphChunk;
     }
   }
@@ -587,8 +878,6 @@ int bx_step(bx_handle hh, int n_steps, int want_outputs, void* stream) {
   h->steps_done += n_steps;
   if (want_outputs) h->have_outputs = true;
   if (s != h->stream) {
-    cudaEvent_t ev;
-    BX_CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     BX_CU(cudaEventRecord(ev, s));
     BX_CU(cudaStreamWaitEvent(h->stream, ev, 0));
     cudaEventDestroy(ev);
@@ -596,9 +885,8 @@ int bx_step(bx_handle hh, int n_steps, int want_outputs, void* stream) {
   return BX_OK;
 }
 
-int bx_status(bx_handle hh, bx_step_status* st) {
-  if (!hh || !st) return fail(BX_EINVAL, "null argument");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_status(bx_handle h, bx_step_status* st) {
+  if (!h || !st) return fail(BX_EINVAL, "null argument");
   unsigned long long v[4];
   BX_CU(cudaStreamSynchronize(h->stream));
   BX_CU(cudaMemcpy(v, h->d_status, sizeof(v), cudaMemcpyDeviceToHost));
@@ -611,13 +899,16 @@ int bx_status(bx_handle hh, bx_step_status* st) {
   return BX_OK;
 }
 
-int bx_outputs_download(bx_handle hh, bx_outputs* o) {
-  if (!hh || !o) return fail(BX_EINVAL, "null argument");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_outputs_download(bx_handle h, bx_outputs* o) {
+  if (!h || !o) return fail(BX_EINVAL, "null argument");
   if (!h->have_outputs) return fail(BX_ESTATE, "no step with want_outputs has run");
   BX_CU(cudaStreamSynchronize(h->stream));
   const size_t M = h->M, C = h->C, I = h->I, G = h->G;
-  struct Pair { double* dst; const double* src; size_t n; };
+  struct Pair {
+    double* dst;
+    const double* src;
+    size_t n;
+  };
   Pair pairs[] = {
       {o->fluxes_mem, h->o_fmem, I * M}, {o->fluxes_gj, h->o_fgj, I * M}, {o->rate_NaKATP, h->o_rate, M},
       {o->rho_cells, h->o_rho, C}, {o->Jn, h->o_Jn, M}, {o->I_mem, h->o_Imem, M},
@@ -625,31 +916,27 @@ int bx_outputs_download(bx_handle hh, bx_outputs* o) {
       {o->vm_ave, h->o_vmave, C}, {o->dvm, h->o_dvm, M}, {o->E_cell_x, h->o_Ecx, C},
       {o->E_cell_y, h->o_Ecy, C}, {o->Emc, h->o_Emc, M}, {o->E_gj_x, h->o_Egjx, M},
       {o->E_gj_y, h->o_Egjy, M}, {o->gjopen, h->o_gjopen, M}, {o->sigma_cell, h->o_sigma, C},
-      {o->fluxes_env_x, h->ecm ? h->d_fx : nullptr, I * G}, {o->fluxes_env_y, h->ecm ? h->d_fy : nullptr, I * G},
-      {o->rho_env, h->ecm ? h->d_rho_env : nullptr, G}, {o->v_env, h->ecm ? h->d_venv : nullptr, G},
+      {o->fluxes_env_x, h->ecm ? h->d_fx : nullptr, I * G},
+      {o->fluxes_env_y, h->ecm ? h->d_fy : nullptr, I * G},
+      {o->rho_env, h->ecm ? h->d_rho_env : nullptr, G},
+      {o->v_env, h->ecm ? h->d_venv : nullptr, G},
   };
   for (const Pair& p : pairs)
     if (p.dst && p.src) BX_CU(cudaMemcpy(p.dst, p.src, p.n * sizeof(double), cudaMemcpyDeviceToHost));
   return BX_OK;
 }
 
-int bx_time_cell_kernel(bx_handle hh, int n, double* ms_per_launch) {
-  if (!hh || !ms_per_launch || n <= 0) return fail(BX_EINVAL, "bad arguments");
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
+int bx_time_cell_kernel(bx_handle h, int n, double* ms_per_launch) {
+  if (!h || !ms_per_launch || n <= 0) return fail(BX_EINVAL, "bad arguments");
   if (!h->have_state || !h->have_dm) return fail(BX_ESTATE, "upload state and Dm first");
-  bx::DevGeom g = dev_geom(h);
-  bx::StepConst k = make_step_const(h);
-  k.gj_len = h->gj_len;
   cudaEvent_t e0, e1;
   BX_CU(cudaEventCreate(&e0));
   BX_CU(cudaEventCreate(&e1));
   double tot = 0.0;
-  const bool split = h->precision == BX_SPLIT_FP32;
   for (int q = 0; q < n; ++q) {
-    bx::StepPtrs p = step_ptrs(h, h->parity);
     BX_CU(cudaEventRecord(e0, h->stream));
-    cudaError_t e = split ? bx::launch_cell_step<float, 256>(h->ecm, false, h->phib_nonzero, h->nblk, h->stream, g, p, k)
-                          : bx::launch_cell_step<double, 256>(h->ecm, false, h->phib_nonzero, h->nblk, h->stream, g, p, k);
+    cudaError_t e = (h->mode == MODE_SPLIT) ? launch_split(h, h->parity, false, h->stream)
+                                            : launch_cell(h, h->parity, false, h->stream);
     if (e != cudaSuccess) return fail(BX_ECUDA, cudaGetErrorString(e));
     BX_CU(cudaEventRecord(e1, h->stream));
     BX_CU(cudaEventSynchronize(e1));
@@ -665,23 +952,24 @@ int bx_time_cell_kernel(bx_handle hh, int n, double* ms_per_launch) {
   return BX_OK;
 }
 
-int64_t bx_cell_kernel_bytes(bx_handle hh) {
-  if (!hh) return -1;
-  bx_cluster_ext* h = static_cast<bx_cluster_ext*>(hh);
-  const int64_t M = h->M, C = h->C, I = h->I;
-  const int64_t w = (h->precision == BX_SPLIT_FP32) ? 4 : 8;   // Dm, mem_sa, gj_w width
-  // per membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env with ECM,
-  // + f*sa export with ECM); per cell: cc in+out, cc_mem in+out, cell_vol, diviterm, ptr
-  int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0);
-  int64_t cell = 4 * I * 8 + 16 + 4;
-  int64_t blk = h->ecm ? 0 : (int64_t)h->nblk * I * 8;
-  return M * mem + C * cell + blk;
+int64_t bx_cell_kernel_bytes(bx_handle h) {
+  if (!h) return -1;
+  const int64_t M = h->M, C = h->C, I = h->I, B = h->nblk;
+  if (h->mode == MODE_SPLIT) {
+    // membrane: Dm (4I), nn_cell 4, lcell 1, mem_sa 4, gjw 4
+    // cell: cc2 in+out 16I, ccm in+out 8I, Vmem in+out 8, dt/vol 4, diviterm/cm 4, ptr 4
+    // CTA: partial sums 4I, partition and cluster id 12
+    return M * (4 * I + 13) + C * (24 * I + 20) + B * (4 * I + 12);
+  }
+  const int64_t w = (h->mode == MODE_SPLIT_ECM) ? 4 : 8;  // Dm, mem_sa, gj_w width
+  // membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env and the f*sa
+  // export with ECM); cell: cc in+out, cc_mem in+out, cell_vol, diviterm, ptr
+  const int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0);
+  const int64_t cell = 4 * I * 8 + 16 + 4;
+  return M * mem + C * cell + (h->ecm ? 0 : B * I * 8);
 }
 
-int64_t bx_launch_count(bx_handle hh) {
-  if (!hh) return -1;
-  return static_cast<bx_cluster_ext*>(hh)->launches;
-}
+int64_t bx_launch_count(bx_handle h) { return h ? h->launches : -1; }
 
 int bx_dense_apply_f64(const double* A, const double* x, double* y, int n, int nrhs, void* stream) {
   if (!A || !x || !y || n <= 0 || nrhs <= 0 || nrhs > 4) return fail(BX_EINVAL, "bad dense_apply arguments");
@@ -698,10 +986,10 @@ int bx_dense_apply_f64(const double* A, const double* x, double* y, int n, int n
   return BX_OK;
 }
 
-int bx_env_fields(bx_handle hh, const double* lap_env_inv, double* v_env, double* E_env_x,
-                  double* E_env_y, double* J_env_x, double* J_env_y, double* B_field) {
+int bx_env_fields(bx_handle h, const double* lap_env_inv, double* v_env, double* E_env_x, double* E_env_y,
+                  double* J_env_x, double* J_env_y, double* B_field) {
   (void)lap_env_inv; (void)v_env; (void)E_env_x; (void)E_env_y; (void)J_env_x; (void)J_env_y; (void)B_field;
-  if (!hh) return fail(BX_EINVAL, "null handle");
+  if (!h) return fail(BX_EINVAL, "null handle");
   return fail(BX_EINVAL, "bx_env_fields: not available in this build");
 }
 

@@ -44,6 +44,7 @@ struct DevGeom {
   const double* cell_sa;  // [C]
   const double* diviterm; // [C]
   const int* blk_cell;    // [nblk+1]
+  const int* blk_cluster; // [nblk] cluster of each CTA (batched sweeps)
 };
 
 // Per-step constants (kernel parameter, passed by value).
@@ -57,15 +58,11 @@ struct StepConst {
   double F_RT;             // F / (R T)
   double dt, inv_cm, tm, gj_len;
   double gj_block;
-  double pump_coef;        // -3 * block * alpha_NaK
   double inv_KmNa, inv_KmK, atp_term; // 1/Km, (cATP/KmATP)
   double atp_den;          // 1 + cATP/KmATP
   double qnum_c;           // (cADP*1e-3)*(cPi*1e-3)
   double qden_c;           // cATP*1e-3
   double K0;               // exp(-deltaGATP / (R T))
-  double pump_on;          // alpha_NaK > 0
-  double env_scale;        // dt / (vol_env * M): no-ECM well-mixed update
-  double inv_h_d2_dt;      // dt / (cell_height * delta^2): ECM membrane->grid
 };
 
 struct StepPtrs {
@@ -74,7 +71,8 @@ struct StepPtrs {
   double* cc;                              // [I][C] cell concentrations (in place)
   const double* Dm;                        // [I][M] FP64 (plain form)
   const float* Dm_f;                       // [I][M] FP32 (split form)
-  const double* cenv;                      // [I] (no ECM) or [I][G] (ECM)
+  const double* cenv;                      // [ncl][I] (no ECM) or [I][G] (ECM)
+  const double* pump_coef;                 // [ncl] -3 block alpha_NaK (0 = pump off)
   const double* phib;                      // [G] or nullptr
   double* env_part;                        // [nblk][I] partial sums (no ECM)
   double* mem_flux_sa;                     // [I][M] f_mem*sa (ECM scatter input)
@@ -141,7 +139,7 @@ __device__ __forceinline__ T ghk_flux(const GhkShared<T>& s, int zcode, double z
 // one division: f_Na = -3 block alpha fwd (1 - Q/Keq) with Keq = K0/e1,
 // e1 = exp(-F V/(R T)) shared with the GHK fluxes.
 template <typename T>
-__device__ __forceinline__ T pump_fna(const StepConst& k, T e1, T cNai, T cNao, T cKi, T cKo) {
+__device__ __forceinline__ T pump_fna(const StepConst& k, T pcoef, T e1, T cNai, T cNao, T cKi, T cKo) {
   const T nai = cNai * (T)1e-3, nao = cNao * (T)1e-3, ki = cKi * (T)1e-3, ko = cKo * (T)1e-3;
   const T qnum = (T)k.qnum_c * (nao * nao * nao) * (ki * ki);
   T qden = (T)k.qden_c * (nai * nai * nai) * (ko * ko);
@@ -152,7 +150,7 @@ __device__ __forceinline__ T pump_fna(const StepConst& k, T e1, T cNai, T cNao, 
   const T den_e = ((T)1 + na3) * ((T)1 + k2) * (T)k.atp_den;
   // fwd * (1 - Q/Keq) = num_e (qden K0 - qnum e1) / (den_e qden K0)
   const T K0 = (T)k.K0;
-  return (T)k.pump_coef * num_e * (qden * K0 - qnum * e1) / (den_e * qden * K0);
+  return pcoef * num_e * (qden * K0 - qnum * e1) / (den_e * qden * K0);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -180,6 +178,8 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
 
   const int b = blockIdx.x;
   const int c0 = g.blk_cell[b], c1 = g.blk_cell[b + 1];
+  const int cl = g.blk_cluster[b];
+  const double* cenv_cl = ECM ? p.cenv : p.cenv + (size_t)cl * I;
   const int m0 = g.cell_ptr[c0], m1 = g.cell_ptr[c1];
   const int t = threadIdx.x;
   const int m = m0 + t;
@@ -219,19 +219,20 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
 
     // Na/K-ATPase first, on the start-of-step concentrations (sim.py:1196-1234)
     T fNa = (T)0;
-    if (k.pump_on != 0.0) {
+    const double pcoef = p.pump_coef[cl];
+    if (pcoef != 0.0) {
       const T cNai = (T)p.ccm_in[k.iNa * g.C + c];
       const T cKi = (T)p.ccm_in[k.iK * g.C + c];
-      const T cNao = (T)(ECM ? p.cenv[k.iNa * g.G + ge] : p.cenv[k.iNa]);
-      const T cKo = (T)(ECM ? p.cenv[k.iK * g.G + ge] : p.cenv[k.iK]);
+      const T cNao = (T)(ECM ? cenv_cl[k.iNa * g.G + ge] : cenv_cl[k.iNa]);
+      const T cKo = (T)(ECM ? cenv_cl[k.iK * g.G + ge] : cenv_cl[k.iK]);
       // the pump sees vm before any nonce (it runs before the ion loop);
       // e1 of v1 equals exp(-F vm/(R T)) for |vm| > 1e-8 V
-      fNa = pump_fna<T>(k, sm.e1, cNai, cNao, cKi, cKo);
+      fNa = pump_fna<T>(k, (T)pcoef, sm.e1, cNai, cNao, cKi, cKo);
     }
     rate_o = -fNa;
     for (int i = 0; i < I; ++i) {
       const T cin = (T)p.ccm_in[i * g.C + c];
-      const T cout = (T)(ECM ? p.cenv[i * g.G + ge] : p.cenv[i]);
+      const T cout = (T)(ECM ? cenv_cl[i * g.G + ge] : cenv_cl[i]);
       T dm;
       if constexpr (sizeof(T) == 8) dm = (T)p.Dm[(size_t)i * g.M + m];
       else dm = p.Dm_f[(size_t)i * g.M + m];
@@ -369,21 +370,24 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
   }
 }
 
-// No-ECM environment: the well-mixed value per ion (sim_toolbox.py:1196-1205)
-// c_env <- mean_m(c_env - f_m sa_m / vol_env * dt); fixed-order reduction.
-static __global__ void k_env_mix(const double* __restrict__ part, int nblk, int I,
-                          double* cenv, double env_scale) {
+// No-ECM environment: the well-mixed value per cluster and ion
+// (sim_toolbox.py:1196-1205) c_env <- mean_m(c_env - f_m sa_m / vol_env * dt);
+// one CTA per cluster reduces its CTAs' partial sums in a fixed order.
+static __global__ void k_env_mix(const double* __restrict__ part, const int* __restrict__ cl_blk, int I,
+                                 double* cenv, const double* __restrict__ env_scale) {
   __shared__ double red[32];
+  const int cl = blockIdx.x;
+  const int b0 = cl_blk[cl], b1 = cl_blk[cl + 1];
   for (int i = 0; i < I; ++i) {
     double s = 0.0;
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[(size_t)b * I + i];
+    for (int b = b0 + (int)threadIdx.x; b < b1; b += blockDim.x) s += part[(size_t)b * I + i];
     s = warp_sum(s);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
       double tot = 0.0;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
-      cenv[i] = cenv[i] - tot * env_scale;
+      cenv[(size_t)cl * I + i] = cenv[(size_t)cl * I + i] - tot * env_scale[cl];
     }
     __syncthreads();
   }

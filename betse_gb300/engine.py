@@ -150,3 +150,69 @@ class ClusterEngine:
 
     def launch_count(self) -> int:
         return int(self.lib.bx_launch_count(self.h))
+
+
+class BatchEngine(ClusterEngine):
+    """Many independent clusters stepped together (a parameter sweep).
+
+    Arrays are the clusters' arrays concatenated in order; ``layout`` gives
+    each cluster's cell and membrane offsets. Clusters may differ in geometry,
+    ``alpha_NaK``, ``nakatp_block`` and ``vol_env``.
+    """
+
+    def __init__(self, geoms, params, precision='split'):
+        self.lib = _lib.load()
+        self.geoms = list(geoms)
+        self.params_list = list(params)
+        self.params = self.params_list[0]
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        n = len(self.geoms)
+        self._cgs = (_lib.BxGeom * n)(*[g.to_c() for g in self.geoms])
+        self._cps = (_lib.BxParams * n)(*[p.to_c() for p in self.params_list])
+        h = ct.c_void_p()
+        _lib.check(self.lib.bx_batch_create(self._cgs, self._cps, n, self.precision, ct.byref(h)),
+                   'bx_batch_create')
+        self.h = h
+        self.n_clusters = n
+        self.I = self.params.n_ions
+        self.C = sum(g.n_cells for g in self.geoms)
+        self.M = sum(g.n_mems for g in self.geoms)
+        self.G = self.geoms[0].n_grid
+        self.ecm = False
+        co = np.zeros(n + 1, np.int32)
+        mo = np.zeros(n + 1, np.int32)
+        _lib.check(self.lib.bx_batch_layout(self.h, _lib.iptr(co), _lib.iptr(mo)), 'bx_batch_layout')
+        self.cell_offsets, self.mem_offsets = co, mo
+
+    def set_membrane_diffusivity(self, Dm_list):
+        Dm = np.concatenate([_c(d) for d in Dm_list], axis=1) if isinstance(Dm_list, (list, tuple)) else _c(Dm_list)
+        super().set_membrane_diffusivity(Dm)
+
+    def upload_states(self, states):
+        """Upload a list of per-cluster state dicts (as ``ClusterEngine.upload``)."""
+        cat = lambda k, ax: np.concatenate([_c(s[k]) for s in states], axis=ax)  # noqa: E731
+        ce = []
+        for s in states:
+            e = _c(s['cc_env'])
+            if e.ndim == 2:
+                if not np.all(e == e[:, :1]):
+                    raise ValueError('without ECM, cc_env must be uniform over membranes')
+                e = e[:, 0]
+            ce.append(e)
+        vm, cc, cam, cenv = cat('vm', 0), cat('cc_cells', 1), cat('cc_at_mem', 1), _c(np.stack(ce))
+        st = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(cenv), None, None)
+        _lib.check(self.lib.bx_state_upload(self.h, ct.byref(st)), 'bx_state_upload')
+
+    def download_states(self):
+        I = self.I
+        vm, cc, cam = np.empty(self.M), np.empty((I, self.C)), np.empty((I, self.M))
+        cenv = np.empty((self.n_clusters, I))
+        st = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(cenv), None, None)
+        _lib.check(self.lib.bx_state_download(self.h, ct.byref(st)), 'bx_state_download')
+        out = []
+        for k in range(self.n_clusters):
+            c0, c1 = self.cell_offsets[k], self.cell_offsets[k + 1]
+            m0, m1 = self.mem_offsets[k], self.mem_offsets[k + 1]
+            out.append(dict(vm=vm[m0:m1].copy(), cc_cells=cc[:, c0:c1].copy(),
+                            cc_at_mem=cam[:, m0:m1].copy(), cc_env=cenv[k].copy()))
+        return out

@@ -169,6 +169,20 @@ typedef struct bx_step_status {
  * precision is BX_PLAIN_FP64 or BX_SPLIT_FP32. */
 int bx_cluster_create(const bx_geom* g, const bx_params* p, int precision,
                       bx_handle* out);
+/* A batch of independent clusters stepped together (a parameter sweep; no
+ * reference counterpart beyond running Simulator once per cluster).  g[k] and
+ * p[k] describe cluster k; the clusters may differ in size, geometry,
+ * alpha_NaK, nakatp_block and vol_env, and share every other parameter.  The
+ * handle's arrays are the clusters' arrays concatenated in order (state rows
+ * still ion-major: cc_cells is [n_ions][sum n_cells]); without ECM cc_env is
+ * [n_clusters][n_ions].  Batches need is_ecm == 0. */
+int bx_batch_create(const bx_geom* g, const bx_params* p, int n_clusters, int precision,
+                    bx_handle* out);
+/* Offsets of each cluster's cells and membranes in the concatenation
+ * ([n_clusters+1] each). */
+int bx_batch_layout(bx_handle h, int32_t* cell_offsets, int32_t* mem_offsets);
+/* Replace every cluster's parameters (p[n_clusters]). */
+int bx_batch_set_params(bx_handle h, const bx_params* p);
 void bx_destroy(bx_handle h);
 
 /* Per-membrane channel diffusivities Dm[n_ions * n_mems] (sim.Dm_cells). */

@@ -131,3 +131,25 @@ def vm_err_ok(d, vm, vm_ref, cc_ref, rel=1e-10):
     err = np.max(np.abs(vm - vm_ref))
     bound = rel * np.max(np.abs(vm_ref)) + vm_floor(d, cc_ref)
     return err <= bound, err, bound
+
+
+def output_floors(d, cc, o):
+    """Absolute FP64 cancellation floors of the step outputs (see vm_floor).
+
+    * rho_cells, vm_ave, dvm: the charge sum (~1e7 C/m3 terms);
+    * fluxes_gj and what is built from it (Jn, I_mem, J_cell, Jc, E_cell, Emc):
+      the gap-junction GHK numerator cB - cA*exp(-alpha) cancels between two
+      nearly equal neighbour concentrations; its floor is a few ulp of one term,
+      (D_gj * gj_surface / gj_len) * max c, per ion."""
+    eps = np.finfo(np.float64).eps
+    zF = np.abs(d['par_zs'] * d['par_F'])
+    rho_floor = 4 * eps * np.max((zF[:, None] * cc).sum(axis=0))
+    vfl = vm_floor(d, cc)
+    gj_term = (d['par_D_gj'] * d['par_gj_surface'] / d['geom_gj_len'])[:, None] * np.abs(cc)
+    f_gj = 8 * eps * np.max(gj_term)
+    j_floor = 8 * eps * np.max((zF[:, None] * gj_term).sum(axis=0))
+    sig = np.min(np.abs(o['sigma_cell'])) if 'sigma_cell' in o else 1.0
+    return {'rho_cells': rho_floor, 'vm_ave': vfl, 'dvm': 2 * vfl / float(d['par_dt']),
+            'fluxes_gj': f_gj, 'Jn': j_floor, 'I_mem': j_floor * np.max(d['geom_mem_sa']),
+            'J_cell_x': j_floor, 'J_cell_y': j_floor, 'Jc': j_floor,
+            'E_cell_x': j_floor / sig, 'E_cell_y': j_floor / sig, 'Emc': j_floor / sig}

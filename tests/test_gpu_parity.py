@@ -71,17 +71,12 @@ def test_outputs_fp64_match_betse(name):
     keys = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn', 'I_mem', 'J_cell_x',
             'J_cell_y', 'Jc', 'vm_ave', 'dvm', 'E_cell_x', 'E_cell_y', 'Emc', 'E_gj_x',
             'E_gj_y', 'gjopen', 'sigma_cell']
-    cc = d[f's{cp}_cc_cells']
-    vfl = gi.vm_floor(d, cc)
-    zF = np.abs(d['par_zs'] * d['par_F'])
-    rho_floor = 4 * np.finfo(float).eps * np.max((zF[:, None] * cc).sum(axis=0))
+    floors = gi.output_floors(d, d[f's{cp}_cc_cells'], o)
     for k in keys:
         ref = d[f's{cp}_{k}']
         got = o[k]
         err = np.max(np.abs(got - ref))
-        # rho_cells, Vmem and dVm/dt carry the cancellation floor of the charge sum
-        floor = {'rho_cells': rho_floor, 'vm_ave': vfl,
-                 'dvm': 2 * vfl / float(d['par_dt'])}.get(k, 0.0)
+        floor = floors.get(k, 0.0)
         assert err <= TOL_FP64 * np.max(np.abs(ref)) + floor, (k, err, floor)
     if ecm:
         for k in ('v_env',):
