@@ -57,6 +57,7 @@ cudaError_t h2d(P* dst, const P* src, size_t n) {
 constexpr int kGraphChunk = 32;  // steps per captured graph (even: ping-pong parity returns)
 constexpr int kEnvTPB = 256;
 constexpr int kTPB = 256;        // membrane slots per CTA of the cell kernels
+constexpr int kRec = 8;          // floats per cell record of the split form (<= 7 ions + Vmem)
 
 enum Mode { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SPLIT_ECM = 2 };
 
@@ -91,8 +92,9 @@ struct bx_cluster {
   double *d_vm[2] = {nullptr, nullptr}, *d_ccm[2] = {nullptr, nullptr}, *d_cc = nullptr;
   // ---- state: split
   float2* s_cc2 = nullptr;
-  float *s_ccm[2] = {nullptr, nullptr}, *s_vc[2] = {nullptr, nullptr};
+  float* s_rec[2] = {nullptr, nullptr};   // [C][kRec]: membrane-side concentrations + Vmem
   float *s_cenv_f = nullptr, *s_pump = nullptr, *s_part = nullptr, *s_phib = nullptr;
+  unsigned int* s_count = nullptr;
   // ---- environment
   double *d_cenv = nullptr, *d_phib = nullptr, *d_env_part = nullptr, *d_mem_flux_sa = nullptr,
          *d_pump = nullptr, *d_env_scale = nullptr;
@@ -123,7 +125,7 @@ void free_all(bx_cluster* h) {
       h->d_env_ptr, h->d_env_mem, h->d_bflag, h->d_touched, h->d_lcell, h->d_mem_sa, h->d_gj_w, h->d_nx,
       h->d_ny, h->d_swm, h->d_swo, h->d_cell_vol, h->d_cell_sa, h->d_diviterm, h->d_mem_sa_f,
       h->d_gj_w_f, h->d_gjw0_f, h->d_dtv, h->d_dvc, h->d_Dm, h->d_Dm_f, h->d_vm[0], h->d_vm[1],
-      h->d_ccm[0], h->d_ccm[1], h->d_cc, h->s_cc2, h->s_ccm[0], h->s_ccm[1], h->s_vc[0], h->s_vc[1],
+      h->d_ccm[0], h->d_ccm[1], h->d_cc, h->s_cc2, h->s_rec[0], h->s_rec[1], h->s_count,
       h->s_cenv_f, h->s_pump, h->s_part, h->s_phib, h->d_cenv, h->d_phib, h->d_env_part,
       h->d_mem_flux_sa, h->d_pump, h->d_env_scale, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy,
       h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
@@ -262,16 +264,17 @@ bx::SplitGeom split_geom(const bx_cluster* h) {
   g.C = h->C; g.M = h->M; g.I = h->I; g.G = h->G;
   g.cell_ptr = h->d_cell_ptr; g.nn_cell = h->d_nn_cell; g.lcell = h->d_lcell;
   g.mem_sa = h->d_mem_sa_f; g.gjw = h->d_gjw0_f; g.dtv = h->d_dtv; g.dvc = h->d_dvc;
-  g.blk_cell = h->d_blk; g.blk_cluster = h->d_blk_cl; g.map_env = h->d_map_env; g.nn = h->d_nn;
+  g.blk_cell = h->d_blk; g.blk_cluster = h->d_blk_cl; g.cl_blk = h->d_cl_blk;
+  g.map_env = h->d_map_env; g.nn = h->d_nn;
   return g;
 }
 
 bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
   bx::SplitPtrs p{};
-  p.vc_in = h->s_vc[parity]; p.vc_out = h->s_vc[parity ^ 1];
-  p.ccm_in = h->s_ccm[parity]; p.ccm_out = h->s_ccm[parity ^ 1];
-  p.cc2 = h->s_cc2; p.Dm = h->d_Dm_f; p.cenv_f = h->s_cenv_f; p.pump_coef = h->s_pump;
-  p.phib = h->s_phib; p.env_part = h->s_part; p.status = h->d_status;
+  p.rec_in = h->s_rec[parity]; p.rec_out = h->s_rec[parity ^ 1];
+  p.cc2 = h->s_cc2; p.Dm = h->d_Dm_f; p.cenv_f = h->s_cenv_f; p.cenv64 = h->d_cenv;
+  p.env_scale = h->d_env_scale; p.pump_coef = h->s_pump; p.phib = h->s_phib;
+  p.env_part = h->s_part; p.cl_count = h->s_count; p.status = h->d_status;
   p.o_fmem = h->o_fmem; p.o_fgj = h->o_fgj; p.o_rate = h->o_rate; p.o_rho = h->o_rho;
   p.o_vmem = h->o_vmc;
   return p;
@@ -285,10 +288,10 @@ cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   bx::SplitConst k = make_split_const(h);
   const int code = (out ? 2 : 0) | (h->phib_nonzero ? 1 : 0);
   switch (code) {
-    case 0: bx::k_split_step<kTPB, false, false><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
-    case 1: bx::k_split_step<kTPB, false, true><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
-    case 2: bx::k_split_step<kTPB, true, false><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
-    default: bx::k_split_step<kTPB, true, true><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+    case 0: bx::k_split_step<kTPB, kRec, false, false><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+    case 1: bx::k_split_step<kTPB, kRec, false, true><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+    case 2: bx::k_split_step<kTPB, kRec, true, false><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+    default: bx::k_split_step<kTPB, kRec, true, true><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
   }
   return cudaGetLastError();
 }
@@ -308,14 +311,12 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   if (h->mode == MODE_SPLIT) {
     e = launch_split(h, parity, out, s);
     if (e != cudaSuccess) return e;
-    bx::k_split_env_mix<<<h->ncl, 256, 0, s>>>(h->s_part, h->d_cl_blk, h->I, h->d_cenv, h->s_cenv_f,
-                                              h->d_env_scale);
-    h->launches += 2;
+    h->launches += 1;
     if (out) {
       bx::SplitOutGeom og{h->C, h->M, h->I, h->d_cell_ptr, h->d_blk, h->d_nn, h->d_map_env,
                           h->d_mem_sa, h->d_nx, h->d_ny, h->d_swm, h->d_swo, h->d_cell_sa,
                           h->d_gj_w, h->d_bflag};
-      bx::SplitOutPtrs op{h->o_fmem, h->o_fgj, h->s_vc[parity ^ 1], h->s_vc[parity], h->s_cc2,
+      bx::SplitOutPtrs op{h->o_fmem, h->o_fgj, h->s_rec[parity ^ 1], h->s_rec[parity], kRec, h->s_cc2,
                           h->phib_nonzero ? h->s_phib : nullptr, h->o_Jn, h->o_Imem, h->o_Jcx,
                           h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx, h->o_Ecy, h->o_Emc,
                           h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vm_mem};
@@ -362,7 +363,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
 }
 
 int launches_per_step(const bx_cluster* h) {
-  if (h->mode == MODE_SPLIT) return 2;
+  if (h->mode == MODE_SPLIT) return 1;
   if (!h->ecm) return 2;
   return h->par.sharpness < 1.0 ? 7 : 6;
 }
@@ -473,6 +474,10 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   h->precision = precision; h->par = p0; h->ecm = p0.is_ecm != 0;
   h->cl_par.assign(ps, ps + ncl);
   h->mode = (precision == BX_PLAIN_FP64) ? MODE_PLAIN : (h->ecm ? MODE_SPLIT_ECM : MODE_SPLIT);
+  if (h->mode == MODE_SPLIT && I > kRec - 1) {
+    delete h;
+    return fail(BX_EINVAL, "the split form holds at most 7 ions (BETSE's full ion set)");
+  }
   h->gj_len = gs[0].gj_len; h->delta = gs[0].delta;
   const int G = h->G;
 
@@ -575,8 +580,10 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     ALLOC(h->d_dtv, C); ALLOC(h->d_dvc, C);
     ALLOC(h->d_Dm_f, (size_t)I * M);
     ALLOC(h->s_cc2, (size_t)I * C);
-    ALLOC(h->s_ccm[0], (size_t)I * C); ALLOC(h->s_ccm[1], (size_t)I * C);
-    ALLOC(h->s_vc[0], C); ALLOC(h->s_vc[1], C);
+    ALLOC(h->s_rec[0], (size_t)kRec * C); ALLOC(h->s_rec[1], (size_t)kRec * C);
+    ALLOC(h->s_count, ncl);
+    if (cudaMemset(h->s_count, 0, (size_t)ncl * sizeof(unsigned int)) != cudaSuccess)
+      return bail(BX_ECUDA, "cudaMemset");
     ALLOC(h->s_cenv_f, (size_t)ncl * I); ALLOC(h->d_cenv, (size_t)ncl * I);
     ALLOC(h->s_pump, ncl);
     ALLOC(h->s_part, (size_t)h->nblk * I);
@@ -740,7 +747,7 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
   if (h->mode == MODE_SPLIT) {
     // Vmem is constant per cell (minus Phi_b per membrane) in BETSE's full
     // solver with cell_polarizability == 0 (sim.py:2027-2029)
-    std::vector<float> vc(C), ccmf((size_t)I * C);
+    std::vector<float> rec((size_t)kRec * C, 0.0f);
     std::vector<float2> cc2((size_t)I * C);
     for (int c = 0; c < C; ++c) {
       const double v0 = s->vm[ptr[c]] + h->h_phib[h->h_map_env[ptr[c]]];
@@ -749,19 +756,19 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
         if (std::fabs(v - v0) > 1e-12 * std::fabs(v0) + 1e-18)
           return fail(BX_EINVAL, "split form: vm must be uniform over each cell's membranes");
       }
-      vc[c] = (float)v0;
+      rec[(size_t)c * kRec + kRec - 1] = (float)v0;
+      for (int i = 0; i < I; ++i) rec[(size_t)c * kRec + i] = (float)ccm[(size_t)i * C + c];
     }
     for (size_t q = 0; q < (size_t)I * C; ++q) {
       const double x = s->cc_cells[q];
       const float hi = (float)x;
       cc2[q] = make_float2(hi, (float)(x - (double)hi));
-      ccmf[q] = (float)ccm[q];
     }
     std::vector<float> cef(nenv);
     for (size_t q = 0; q < nenv; ++q) cef[q] = (float)s->cc_env[q];
-    BX_CU(h2d(h->s_vc[0], vc.data(), C));
+    BX_CU(h2d(h->s_rec[0], rec.data(), rec.size()));
     BX_CU(h2d(h->s_cc2, cc2.data(), cc2.size()));
-    BX_CU(h2d(h->s_ccm[0], ccmf.data(), ccmf.size()));
+    BX_CU(cudaMemset(h->s_count, 0, (size_t)h->ncl * sizeof(unsigned int)));
     BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
     BX_CU(h2d(h->s_cenv_f, cef.data(), nenv));
   } else {
@@ -787,16 +794,17 @@ int bx_state_download(bx_handle h, bx_state* s) {
   const size_t nenv = h->ecm ? (size_t)I * h->G : (size_t)h->ncl * I;
   std::vector<double> ccm((size_t)I * C);
   if (h->mode == MODE_SPLIT) {
-    std::vector<float> vc(C), ccmf((size_t)I * C);
+    std::vector<float> rec((size_t)kRec * C);
     std::vector<float2> cc2((size_t)I * C);
-    BX_CU(cudaMemcpy(vc.data(), h->s_vc[h->parity], C * sizeof(float), cudaMemcpyDeviceToHost));
+    BX_CU(cudaMemcpy(rec.data(), h->s_rec[h->parity], rec.size() * sizeof(float), cudaMemcpyDeviceToHost));
     BX_CU(cudaMemcpy(cc2.data(), h->s_cc2, cc2.size() * sizeof(float2), cudaMemcpyDeviceToHost));
-    BX_CU(cudaMemcpy(ccmf.data(), h->s_ccm[h->parity], ccmf.size() * sizeof(float), cudaMemcpyDeviceToHost));
     if (s->vm)
-      for (int m = 0; m < M; ++m) s->vm[m] = (double)vc[h->h_m2c[m]] - h->h_phib[h->h_map_env[m]];
+      for (int m = 0; m < M; ++m)
+        s->vm[m] = (double)rec[(size_t)h->h_m2c[m] * kRec + kRec - 1] - h->h_phib[h->h_map_env[m]];
     if (s->cc_cells)
       for (size_t q = 0; q < cc2.size(); ++q) s->cc_cells[q] = (double)cc2[q].x + (double)cc2[q].y;
-    for (size_t q = 0; q < ccm.size(); ++q) ccm[q] = (double)ccmf[q];
+    for (int i = 0; i < I; ++i)
+      for (int c = 0; c < C; ++c) ccm[(size_t)i * C + c] = (double)rec[(size_t)c * kRec + i];
   } else {
     if (s->vm) BX_CU(cudaMemcpy(s->vm, h->d_vm[h->parity], (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
     if (s->cc_cells)
@@ -957,9 +965,9 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
   const int64_t M = h->M, C = h->C, I = h->I, B = h->nblk;
   if (h->mode == MODE_SPLIT) {
     // membrane: Dm (4I), nn_cell 4, lcell 1, mem_sa 4, gjw 4
-    // cell: cc2 in+out 16I, ccm in+out 8I, Vmem in+out 8, dt/vol 4, diviterm/cm 4, ptr 4
+    // cell: cc2 in+out 16I, record in+out 2*4*kRec, dt/vol 4, diviterm/cm 4, ptr 4
     // CTA: partial sums 4I, partition and cluster id 12
-    return M * (4 * I + 13) + C * (24 * I + 20) + B * (4 * I + 12);
+    return M * (4 * I + 13) + C * (16 * I + 8 * kRec + 12) + B * (4 * I + 12);
   }
   const int64_t w = (h->mode == MODE_SPLIT_ECM) ? 4 : 8;  // Dm, mem_sa, gj_w width
   // membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env and the f*sa

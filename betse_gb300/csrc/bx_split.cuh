@@ -76,17 +76,18 @@ __device__ __forceinline__ float ghk_flux_f(const GhkShared<float>& s, int zcode
 
 struct SplitGeom {
   int C, M, I, G;
-  const int* cell_ptr;      // [C+1]
-  const int* nn_cell;       // [M]
-  const uint8_t* lcell;     // [M]
-  const float* mem_sa;      // [M]
-  const float* gjw;         // [M]  (0 on boundary membranes)
-  const float* dtv;         // [C]  dt / cell_vol
-  const float* dvc;         // [C]  diviterm / cm
-  const int* blk_cell;      // [nblk+1]
-  const int* blk_cluster;   // [nblk]
-  const int* map_env;       // [M]  (PHIB only)
-  const int* nn;            // [M]  (PHIB only)
+  const int* __restrict__ cell_ptr;      // [C+1]
+  const int* __restrict__ nn_cell;       // [M]
+  const uint8_t* __restrict__ lcell;     // [M]
+  const float* __restrict__ mem_sa;      // [M]
+  const float* __restrict__ gjw;         // [M]  (0 on boundary membranes)
+  const float* __restrict__ dtv;         // [C]  dt / cell_vol
+  const float* __restrict__ dvc;         // [C]  diviterm / cm
+  const int* __restrict__ blk_cell;      // [nblk+1]
+  const int* __restrict__ blk_cluster;   // [nblk]
+  const int* __restrict__ cl_blk;        // [ncl+1] CTA range of each cluster
+  const int* __restrict__ map_env;       // [M]  (PHIB only)
+  const int* __restrict__ nn;            // [M]  (PHIB only)
 };
 
 struct SplitConst {
@@ -101,26 +102,86 @@ struct SplitConst {
   float inv_KmNa, inv_KmK, atp_term, atp_den, qnum_c, qden_c, K0;
 };
 
+// Per-cell record, REC floats, 16-byte aligned: slots [0, I) hold the
+// membrane-side concentration of each ion (BETSE's cc_at_mem), slot REC-1
+// the cell's Vmem.  A membrane reads its own and its partner's record with
+// REC/4 vector loads.
 struct SplitPtrs {
-  const float* vc_in; float* vc_out;    // [C]
-  const float* ccm_in; float* ccm_out;  // [I][C]
-  float2* cc2;                          // [I][C]
-  const float* Dm;                      // [I][M]
-  const float* cenv_f;                  // [ncl][I] FP32 copy of the environment
-  const float* pump_coef;               // [ncl] -3 block alpha_NaK (0 = pump off)
-  const float* phib;                    // [G] (PHIB)
-  float* env_part;                      // [nblk][I]
-  unsigned long long* status;           // nan_vm, nan_conc, neg clamps
+  const float* __restrict__ rec_in; float* __restrict__ rec_out;   // [C][REC]
+  float2* __restrict__ cc2;                // [I][C]
+  const float* __restrict__ Dm;            // [I][M]
+  float* cenv_f;                           // [ncl][I] FP32 copy of the environment
+  double* cenv64;                          // [ncl][I] FP64 master copy
+  const double* __restrict__ env_scale;    // [ncl] dt / (vol_env * M_cluster)
+  const float* __restrict__ pump_coef;     // [ncl] -3 block alpha_NaK (0 = pump off)
+  const float* __restrict__ phib;          // [G] (PHIB)
+  float* env_part;                         // [nblk][I] per-CTA partial sums
+  unsigned int* cl_count;                  // [ncl] CTAs of the cluster done this step
+  unsigned long long* status;              // nan_vm, nan_conc, neg clamps
   // outputs (OUT)
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_vmem;
 };
 
-template <int TPB, bool OUT, bool PHIB>
+template <int REC>
+__device__ __forceinline__ void load_rec(const float* __restrict__ rec, int c, float (&v)[REC]) {
+  const float4* r4 = reinterpret_cast<const float4*>(rec + (size_t)c * REC);
+#pragma unroll
+  for (int q = 0; q < REC / 4; ++q) {
+    const float4 x = r4[q];
+    v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
+  }
+}
+
+// Well-mixed environment of cluster cl (sim_toolbox.py:1196-1205), done by the
+// last CTA of the cluster to finish: it sums the cluster's per-CTA partials in
+// a fixed order (double-float), so the result does not depend on which CTA is
+// last.  No CTA waits for another.
+template <int TPB>
+__device__ void finalize_env(const SplitGeom& g, const SplitPtrs& p, int I, int cl) {
+  __shared__ float2 fin[kMaxIons][TPB / 32];
+  const int t = threadIdx.x;
+  const int b0 = g.cl_blk[cl], b1 = g.cl_blk[cl + 1];
+  df acc[kMaxIons];
+#pragma unroll
+  for (int i = 0; i < kMaxIons; ++i) acc[i] = df{0.f, 0.f};
+  for (int b = b0 + t; b < b1; b += TPB) {
+    const float* pp = p.env_part + (size_t)b * I;
+#pragma unroll
+    for (int i = 0; i < kMaxIons; ++i)
+      if (i < I) acc[i] = df_add_f(acc[i], __ldcg(pp + i));
+  }
+#pragma unroll
+  for (int i = 0; i < kMaxIons; ++i) {
+    if (i >= I) break;
+    df a = acc[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      df other{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
+      a = df_add(a, other);
+    }
+    if ((t & 31) == 0) fin[i][t >> 5] = make_float2(a.hi, a.lo);
+  }
+  __syncthreads();
+  if (t < I) {
+    df a{0.f, 0.f};
+    for (int w = 0; w < TPB / 32; ++w) a = df_add(a, df{fin[t][w].x, fin[t][w].y});
+    const double tot = (double)a.hi + (double)a.lo;
+    const double v = p.cenv64[(size_t)cl * I + t] - tot * p.env_scale[cl];
+    p.cenv64[(size_t)cl * I + t] = v;
+    p.cenv_f[(size_t)cl * I + t] = (float)v;
+  }
+  if (t == 0) p.cl_count[cl] = 0u;   // ready for the next step
+}
+
+template <int TPB, int REC, bool OUT, bool PHIB>
 __global__ void __launch_bounds__(TPB)
 k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   __shared__ float sA[kMaxIons][TPB];
   __shared__ float sB[kMaxIons][TPB];
   __shared__ float red[kMaxIons][TPB / 32];
+  __shared__ float sRec[TPB][REC];          // new records of the CTA's cells
+  __shared__ float2 sQ[kMaxIons][TPB];      // z F c per (ion, cell), double-float
+  __shared__ int sLast;
   const int I = k.I;
   const int b = blockIdx.x;
   const int c0 = g.blk_cell[b], c1 = g.blk_cell[b + 1];
@@ -136,8 +197,14 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   if (active) {
     const int c = c0 + g.lcell[m];
     const int cn = g.nn_cell[m];
-    float v = p.vc_in[c];
-    float vn = p.vc_in[cn];
+    float own[REC], nbr[REC];
+    load_rec<REC>(p.rec_in, c, own);
+    load_rec<REC>(p.rec_in, cn, nbr);
+    float dmv[kMaxIons];
+#pragma unroll
+    for (int i = 0; i < kMaxIons; ++i) dmv[i] = (i < I) ? p.Dm[(size_t)i * g.M + m] : 0.f;
+    float v = own[REC - 1];
+    float vn = nbr[REC - 1];
     if (PHIB) { v -= p.phib[g.map_env[m]]; vn -= p.phib[g.map_env[g.nn[m]]]; }
     // BETSE's 1e-25 nonces (sim_toolbox.py:52-56) keep alpha != 0 at zero volts
     const float v1 = v + 1.0e-25f;
@@ -154,7 +221,9 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     const float pc = p.pump_coef[cl];
     if (pc != 0.f) {
       // pumpNaKATP (sim_toolbox.py:71-122), one division
-      const float cNai = p.ccm_in[k.iNa * g.C + c], cKi = p.ccm_in[k.iK * g.C + c];
+      float cNai = 0.f, cKi = 0.f;
+#pragma unroll
+      for (int i = 0; i < REC - 1; ++i) { if (i == k.iNa) cNai = own[i]; if (i == k.iK) cKi = own[i]; }
       const float cNao = ce[k.iNa], cKo = ce[k.iK];
       const float nai = cNai * 1e-3f, nao = cNao * 1e-3f, ki = cKi * 1e-3f, ko = cKo * 1e-3f;
       const float qnum = k.qnum_c * (nao * nao * nao) * (ki * ki);
@@ -167,15 +236,13 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
       fNa = pc * num_e * (qden * k.K0 - qnum * sm.e1) / (den_e * qden * k.K0);
     }
 #pragma unroll
-    for (int i = 0; i < kMaxIons; ++i) {
+    for (int i = 0; i < REC - 1; ++i) {
       if (i >= I) break;
-      const float cin = p.ccm_in[i * g.C + c];
-      const float dm = p.Dm[(size_t)i * g.M + m];
-      float f = ghk_flux_f(sm, k.zcode[i], k.z[i], v1, k.F_RT, ce[i], cin, dm, k.inv_tm);
+      const float cin = own[i];
+      float f = ghk_flux_f(sm, k.zcode[i], k.z[i], v1, k.F_RT, ce[i], cin, dmv[i], k.inv_tm);
       if (i == k.iNa) f = fNa + f;
       else if (i == k.iK) f = (-(2.f / 3.f)) * fNa + f;
-      const float cn_i = p.ccm_in[i * g.C + cn];
-      const float fg = ghk_flux_f(sg, k.zcode[i], k.z[i], vgj1, k.F_RT, cin, cn_i,
+      const float fg = ghk_flux_f(sg, k.zcode[i], k.z[i], vgj1, k.F_RT, cin, nbr[i],
                                   k.dgj_gs[i] * gw, k.inv_gjl);
       const float a = f * sa;
       sA[i][t] = a;
@@ -204,61 +271,59 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     float s = 0.f;
     for (int w = 0; w < TPB / 32; ++w) s += red[t][w];
     p.env_part[(size_t)b * I + t] = s;
+    __threadfence();   // visible device-wide before this CTA is counted done
   }
 
-  // cell phase: update_all_concs + update_V for the CTA's cells
+  // cell phase 1: one thread per (ion, cell) -- update_all_concs
   const int ncell = c1 - c0;
+  int bad = 0, neg = 0;
+  for (int q = t; q < I * ncell; q += TPB) {
+    const int i = q / ncell, lc = q - i * ncell;
+    const int c = c0 + lc;
+    const int a0 = g.cell_ptr[c] - m0, a1 = g.cell_ptr[c + 1] - m0;
+    float s1 = 0.f, s2 = 0.f;
+    for (int j = a0; j < a1; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
+    const float dtv = g.dtv[c];
+    const float2 x2 = p.cc2[(size_t)i * g.C + c];
+    df x{x2.x, x2.y};
+    x = df_add_f(x, s1 * dtv);                         // update_Co
+    sRec[lc][i] = x.hi + x.lo;                         // cc_at_mem (before the GJ term)
+    x = df_add_f(x, s2 * dtv);                         // gap-junction term
+    if (x.hi != x.hi) bad++;
+    if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg++; }   // no_negs
+    p.cc2[(size_t)i * g.C + c] = make_float2(x.hi, x.lo);
+    const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
+    sQ[i][lc] = make_float2(qz.hi, qz.lo);
+  }
+  __syncthreads();
+  // cell phase 2: charge sum -> Vmem, write the record (update_V, sim.py:2027-2029)
   if (t < ncell) {
     const int c = c0 + t;
-    const int a0 = g.cell_ptr[c] - m0, a1 = g.cell_ptr[c + 1] - m0;
-    const float dtv = g.dtv[c];
     df rho{0.f, 0.f};
-    int bad = 0, neg = 0;
-    for (int i = 0; i < I; ++i) {
-      float s1 = 0.f, s2 = 0.f;
-      for (int j = a0; j < a1; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
-      const float2 x2 = p.cc2[i * g.C + c];
-      df x{x2.x, x2.y};
-      x = df_add_f(x, s1 * dtv);                         // update_Co
-      p.ccm_out[i * g.C + c] = x.hi + x.lo;              // cc_at_mem (pre-GJ)
-      x = df_add_f(x, s2 * dtv);                         // gap-junction term
-      if (x.hi != x.hi) bad++;
-      if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg++; }   // no_negs
-      p.cc2[i * g.C + c] = make_float2(x.hi, x.lo);
-      rho = df_add(rho, df_mul(x, k.zF_hi[i], k.zF_lo[i]));   // rho_cells = sum z F c
-    }
-    const float vc = (rho.hi + rho.lo) * g.dvc[c];      // vm = rho diviterm / cm
-    p.vc_out[c] = vc;
+    for (int i = 0; i < I; ++i) rho = df_add(rho, df{sQ[i][t].x, sQ[i][t].y});
+    const float vc = (rho.hi + rho.lo) * g.dvc[c];
+    sRec[t][REC - 1] = vc;
+    for (int i = I; i < REC - 1; ++i) sRec[t][i] = 0.f;
+    float4* out4 = reinterpret_cast<float4*>(p.rec_out + (size_t)c * REC);
+#pragma unroll
+    for (int q = 0; q < REC / 4; ++q)
+      out4[q] = make_float4(sRec[t][4 * q], sRec[t][4 * q + 1], sRec[t][4 * q + 2], sRec[t][4 * q + 3]);
     if (vc != vc) atomicAdd(&p.status[0], 1ull);
-    if (bad) atomicAdd(&p.status[1], (unsigned long long)bad);
-    if (neg) atomicAdd(&p.status[2], (unsigned long long)neg);
     if (OUT) { p.o_rho[c] = (double)rho.hi + (double)rho.lo; p.o_vmem[c] = (double)vc; }
   }
-}
+  if (bad) atomicAdd(&p.status[1], (unsigned long long)bad);
+  if (neg) atomicAdd(&p.status[2], (unsigned long long)neg);
 
-// Well-mixed environment per cluster (sim_toolbox.py:1196-1205): one CTA per
-// cluster reduces its CTAs' partial sums in a fixed order; FP64 master copy,
-// FP32 copy for the flux kernel.
-static __global__ void k_split_env_mix(const float* __restrict__ part, const int* __restrict__ cl_blk,
-                                       int I, double* cenv64, float* cenv_f,
-                                       const double* __restrict__ env_scale) {
-  __shared__ double red[32];
-  const int cl = blockIdx.x;
-  const int b0 = cl_blk[cl], b1 = cl_blk[cl + 1];
-  for (int i = 0; i < I; ++i) {
-    double s = 0.0;
-    for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) s += (double)part[(size_t)b * I + i];
-    s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double tot = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
-      const double v = cenv64[(size_t)cl * I + i] - tot * env_scale[cl];
-      cenv64[(size_t)cl * I + i] = v;
-      cenv_f[(size_t)cl * I + i] = (float)v;
-    }
-    __syncthreads();
+  // last CTA of the cluster: the well-mixed environment update
+  if (t == 0) {
+    __threadfence();
+    const unsigned int done = atomicAdd(&p.cl_count[cl], 1u);
+    sLast = (done == (unsigned int)(g.cl_blk[cl + 1] - g.cl_blk[cl] - 1));
+  }
+  __syncthreads();
+  if (sLast) {
+    __threadfence();
+    finalize_env<TPB>(g, p, I, cl);
   }
 }
 
@@ -273,7 +338,7 @@ struct SplitOutGeom {
   const double* sw_o; const double* cell_sa; const double* gj_w; const uint8_t* bflag;
 };
 struct SplitOutPtrs {
-  const double* fmem; const double* fgj; const float* vc_new; const float* vc_old;
+  const double* fmem; const double* fgj; const float* rec_new; const float* rec_old; int rec;
   const float2* cc2; const float* phib;
   double* Jn; double* Imem; double* Jcx; double* Jcy; double* Jc; double* vmave; double* dvm;
   double* Ecx; double* Ecy; double* Emc; double* Egjx; double* Egjy; double* gjopen; double* sigma;
@@ -304,7 +369,7 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
     for (int i = 0; i < k.I; ++i) { Jm += k.zF[i] * p.fmem[(size_t)i * g.M + m]; Jg += k.zF[i] * p.fgj[(size_t)i * g.M + m]; }
     Jraw = -Jm + Jg;
     const double ph = p.phib ? (double)p.phib[g.map_env[m]] : 0.0;
-    vm = (double)p.vc_new[c] - ph;
+    vm = (double)p.rec_new[(size_t)c * p.rec + p.rec - 1] - ph;
     p.vm_mem[m] = vm;
     sX[0][t] = Jraw * g.mem_sa[m];
     sX[1][t] = vm;
@@ -331,7 +396,7 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
     sX[2][t] = Jn * g.nx[m] * g.mem_sa[m];
     sX[3][t] = Jn * g.ny[m] * g.mem_sa[m];
     const int c = c0 + lc;
-    double vmo = (double)p.vc_old[c] - (p.phib ? (double)p.phib[g.map_env[m]] : 0.0);
+    double vmo = (double)p.rec_old[(size_t)c * p.rec + p.rec - 1] - (p.phib ? (double)p.phib[g.map_env[m]] : 0.0);
     for (int i = 0; i < k.I; ++i) vmo += kNonce;
     p.dvm[m] = (vm - vmo) / k.dt;
   } else { sX[2][t] = 0.0; sX[3][t] = 0.0; }

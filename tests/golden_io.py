@@ -137,19 +137,28 @@ def output_floors(d, cc, o):
     """Absolute FP64 cancellation floors of the step outputs (see vm_floor).
 
     * rho_cells, vm_ave, dvm: the charge sum (~1e7 C/m3 terms);
-    * fluxes_gj and what is built from it (Jn, I_mem, J_cell, Jc, E_cell, Emc):
-      the gap-junction GHK numerator cB - cA*exp(-alpha) cancels between two
-      nearly equal neighbour concentrations; its floor is a few ulp of one term,
-      (D_gj * gj_surface / gj_len) * max c, per ion."""
+    * fluxes: the GHK numerator cB - cA*exp(-alpha) cancels near equilibrium and
+      between nearly equal neighbour cells (a few ulp of one term), and alpha =
+      z F V/(R T) carries the Vmem floor (for gap junctions twice, through
+      vm[nn] - vm[m]); the currents built from the fluxes (Jn, I_mem, J_cell,
+      Jc, E_cell, Emc) carry the same floors times |z| F."""
     eps = np.finfo(np.float64).eps
     zF = np.abs(d['par_zs'] * d['par_F'])
     rho_floor = 4 * eps * np.max((zF[:, None] * cc).sum(axis=0))
     vfl = vm_floor(d, cc)
-    gj_term = (d['par_D_gj'] * d['par_gj_surface'] / d['geom_gj_len'])[:, None] * np.abs(cc)
-    f_gj = 8 * eps * np.max(gj_term)
-    j_floor = 8 * eps * np.max((zF[:, None] * gj_term).sum(axis=0))
+    F_RT = float(d['par_F']) / (float(d['par_R']) * float(d['par_T']))
+    cmax = np.max(np.abs(cc), axis=1)
+    env = np.asarray(d['init_cc_env'])
+    cenv = np.max(np.abs(env), axis=1) if env.ndim == 2 else np.abs(env)
+    mem_term = np.max(d['par_Dm_cells'], axis=1) / float(d['par_tm']) * np.maximum(cmax, cenv)
+    gj_term = d['par_D_gj'] * float(d['par_gj_surface']) / float(d['geom_gj_len']) * cmax
+    f_mem = 8 * eps * mem_term + mem_term * F_RT * 2 * vfl
+    f_gj = 8 * eps * gj_term + gj_term * F_RT * 4 * vfl
+    j_floor = float(np.sum(zF * (f_mem + f_gj)))
     sig = np.min(np.abs(o['sigma_cell'])) if 'sigma_cell' in o else 1.0
     return {'rho_cells': rho_floor, 'vm_ave': vfl, 'dvm': 2 * vfl / float(d['par_dt']),
-            'fluxes_gj': f_gj, 'Jn': j_floor, 'I_mem': j_floor * np.max(d['geom_mem_sa']),
+            'fluxes_mem': float(np.max(f_mem)), 'fluxes_gj': float(np.max(f_gj)),
+            'rate_NaKATP': float(np.max(f_mem)), 'Jn': j_floor,
+            'I_mem': j_floor * np.max(d['geom_mem_sa']),
             'J_cell_x': j_floor, 'J_cell_y': j_floor, 'Jc': j_floor,
             'E_cell_x': j_floor / sig, 'E_cell_y': j_floor / sig, 'Emc': j_floor / sig}

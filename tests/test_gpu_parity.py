@@ -83,7 +83,7 @@ def test_outputs_fp64_match_betse(name):
             assert gi.rel_err(o[k], d[f's{cp}_{k}']) < 1e-9, k
 
 
-@pytest.mark.parametrize('name', ['noecm_r80_s1', 'ecm_r50_s3'])
+@pytest.mark.parametrize('name', gi.CASES)
 def test_split_precision_vmem_error(name):
     d = gi.load(name)
     with _engine(d, 'split') as eng:
@@ -98,10 +98,11 @@ def test_split_precision_vmem_error(name):
             assert gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells']) < 1e-5
 
 
-def test_graph_chunks_equal_eager_steps():
+@pytest.mark.parametrize('precision', ['fp64', 'split'])
+def test_graph_chunks_equal_eager_steps(precision):
     """CUDA-graph-replayed steps give bit-identical state to eager steps."""
     d = gi.load('noecm_r50_s7')
-    with _engine(d, 'fp64') as a, _engine(d, 'fp64') as b:
+    with _engine(d, precision) as a, _engine(d, precision) as b:
         a.step(70)                 # graph chunks of 32 + eager tail
         for _ in range(70):
             b.step(1)              # eager only
@@ -110,23 +111,25 @@ def test_graph_chunks_equal_eager_steps():
         assert np.array_equal(sa[k], sb[k]), k
 
 
-def test_deterministic_repeat():
+@pytest.mark.parametrize('precision', ['fp64', 'split'])
+def test_deterministic_repeat(precision):
     d = gi.load('noecm_r80_s1')
     res = []
     for _ in range(2):
-        with _engine(d, 'fp64') as e:
+        with _engine(d, precision) as e:
             e.step(100)
             res.append(e.download())
     for k in res[0]:
         assert np.array_equal(res[0][k], res[1][k]), k
 
 
-def test_nan_input_raises_unstable():
+@pytest.mark.parametrize('precision', ['fp64', 'split'])
+def test_nan_input_raises_unstable(precision):
     from betse_gb300.exceptions import BetseSimUnstableException
     d = gi.load('noecm_r20_s2')
     cg, sp, Dm, st, _ = gi.engine_inputs(d)
     from betse_gb300.engine import ClusterEngine
-    with ClusterEngine(cg, sp, 'fp64') as eng:
+    with ClusterEngine(cg, sp, precision) as eng:
         eng.set_membrane_diffusivity(Dm)
         st = dict(st)
         cc = st['cc_cells'].copy()
@@ -136,3 +139,16 @@ def test_nan_input_raises_unstable():
         eng.step(2)
         with pytest.raises(BetseSimUnstableException):
             eng.check_stable()
+
+
+def test_split_outputs_close_to_betse():
+    """The split form's sampled-step outputs (FP32 fluxes) against BETSE's FP64."""
+    d = gi.load('noecm_r80_s1')
+    cp = int(d['meta_checkpoints'][1])
+    with _engine(d, 'split') as eng:
+        eng.step(cp, outputs=True)
+        o = eng.outputs()
+    for k in ('fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'Jn', 'I_mem', 'J_cell_x', 'J_cell_y',
+              'vm_ave', 'sigma_cell', 'E_gj_x', 'E_gj_y', 'gjopen'):
+        ref = d[f's{cp}_{k}']
+        assert np.max(np.abs(o[k] - ref)) <= 2e-3 * np.max(np.abs(ref)) + 1e-30, k
