@@ -232,6 +232,8 @@ def main():
 
     split = make('split')
     plain = make('fp64')
+    tune_split = split.autotune(20)
+    tune_plain = plain.autotune(5)
 
     def barrier():
         torch.cuda.synchronize()
@@ -279,6 +281,7 @@ def main():
 
     # ---- error at equal step counts: fresh engines, same number of steps
     e_s, e_p = make('split'), make('fp64')
+    e_s.autotune(10)
     e_s.step(T)
     e_p.step(T)
     vm_err = float(np.max(np.abs(e_s.download()['vm'] - e_p.download()['vm'])))
@@ -330,7 +333,8 @@ def main():
             'config': {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems,
                        'time_steps_per_step': T, 'precision': 'split',
                        'l2': 'flushed (256 MiB write) before every timed run',
-                       'parallelism': f'replicas x{world}'},
+                       'parallelism': f'replicas x{world}',
+                       'autotuned_cta_threads': {'split': tune_split[0], 'plain_fp64': tune_plain[0]}},
             'plain_fp64': {'value': plain_value, 'unit': UNIT,
                            'ms_per_step': sum(ms_plain) / len(ms_plain),
                            'speedup_split_vs_plain': value / world / plain_value,

@@ -102,6 +102,7 @@ SIGNATURES = {
     'bx_launch_count': (ct.c_int64, [ct.c_void_p]),
     'bx_time_cell_kernel': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_double)]),
     'bx_cell_kernel_bytes': (ct.c_int64, [ct.c_void_p]),
+    'bx_autotune': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int), ct.POINTER(ct.c_double)]),
 }
 
 _lib = None

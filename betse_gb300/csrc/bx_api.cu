@@ -71,6 +71,7 @@ struct bx_cluster {
   int precision = BX_PLAIN_FP64;
   int mode = MODE_PLAIN;
   int nblk = 0;
+  int tpb = kTPB;                  // membrane slots per CTA (autotuned: 128 or 256)
   bool ecm = false;
   bx_params par{};                 // parameters of cluster 0 (the shared ones)
   std::vector<bx_params> cl_par;   // per-cluster parameters
@@ -282,18 +283,38 @@ bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
 
 inline int env_grid(int G) { return (G + kEnvTPB - 1) / kEnvTPB; }
 
-cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
+template <int TPB, bool OUT, bool PHIB>
+cudaError_t launch_split_t(bx_cluster* h, int parity, cudaStream_t s) {
   bx::SplitGeom g = split_geom(h);
   bx::SplitPtrs p = split_ptrs(h, parity);
   bx::SplitConst k = make_split_const(h);
-  const int code = (out ? 2 : 0) | (h->phib_nonzero ? 1 : 0);
+  // programmatic dependent launch: the kernel's geometry prologue overlaps the
+  // previous step; cudaGridDependencySynchronize orders the state accesses
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)h->nblk);
+  cfg.blockDim = dim3(TPB);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, bx::k_split_step<TPB, kRec, OUT, PHIB>, g, p, k);
+}
+
+cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
+  const int code = (h->tpb == 128 ? 4 : 0) | (out ? 2 : 0) | (h->phib_nonzero ? 1 : 0);
   switch (code) {
-    case 0: bx::k_split_step<kTPB, kRec, false, false><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
-    case 1: bx::k_split_step<kTPB, kRec, false, true><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
-    case 2: bx::k_split_step<kTPB, kRec, true, false><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
-    default: bx::k_split_step<kTPB, kRec, true, true><<<h->nblk, kTPB, 0, s>>>(g, p, k); break;
+    case 0: return launch_split_t<256, false, false>(h, parity, s);
+    case 1: return launch_split_t<256, false, true>(h, parity, s);
+    case 2: return launch_split_t<256, true, false>(h, parity, s);
+    case 3: return launch_split_t<256, true, true>(h, parity, s);
+    case 4: return launch_split_t<128, false, false>(h, parity, s);
+    case 5: return launch_split_t<128, false, true>(h, parity, s);
+    case 6: return launch_split_t<128, true, false>(h, parity, s);
+    default: return launch_split_t<128, true, true>(h, parity, s);
   }
-  return cudaGetLastError();
 }
 
 cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
@@ -301,8 +322,10 @@ cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   bx::StepConst k = make_step_const(h);
   bx::StepPtrs p = step_ptrs(h, parity);
   if (h->mode == MODE_SPLIT_ECM)
-    return bx::launch_cell_step<float, kTPB>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
-  return bx::launch_cell_step<double, kTPB>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+    return h->tpb == 128 ? bx::launch_cell_step<float, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k)
+                         : bx::launch_cell_step<float, 256>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+  return h->tpb == 128 ? bx::launch_cell_step<double, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k)
+                       : bx::launch_cell_step<double, 256>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
 }
 
 // Enqueue one time step (reads parity, writes parity^1).
@@ -325,7 +348,8 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
       oc.I = h->I;
       for (int i = 0; i < h->I; ++i) { oc.zF[i] = d.zF[i]; oc.sig_coef[i] = d.sig_coef[i]; }
       oc.dt = d.dt; oc.gj_len = h->gj_len; oc.gj_block = d.gj_block;
-      bx::k_split_outputs<kTPB><<<h->nblk, kTPB, 0, s>>>(og, op, oc);
+      if (h->tpb == 128) bx::k_split_outputs<128><<<h->nblk, 128, 0, s>>>(og, op, oc);
+      else bx::k_split_outputs<256><<<h->nblk, 256, 0, s>>>(og, op, oc);
       bx::k_split_egj<<<(h->M + 255) / 256, 256, 0, s>>>(h->M, h->d_nn, h->o_vm_mem, h->d_nx, h->d_ny,
                                                          h->gj_len, h->o_Egjx, h->o_Egjy);
       h->launches += 2;
@@ -438,6 +462,65 @@ int check_geom(const bx_geom* g, const bx_params* p) {
   return BX_OK;
 }
 
+// CTA partition for `tpb` membrane slots: runs of whole cells of one cluster
+// with at most tpb membranes and at most 3*tpb/I cells (the (ion, cell) phase
+// gives each thread at most three pairs).  Rebuilt by the autotuner.
+int build_partition(bx_cluster* h, int tpb) {
+  const std::vector<int>& ptr = h->h_cell_ptr;
+  const int max_cells = std::max(1, (3 * tpb) / h->I);
+  std::vector<int> blk{0}, blk_cl;
+  std::vector<int> cl_blk(h->ncl + 1, 0);
+  for (int cl = 0; cl < h->ncl; ++cl) {
+    int acc = 0, nc = 0;
+    for (int c = h->cl_cell[cl]; c < h->cl_cell[cl + 1]; ++c) {
+      const int n = ptr[c + 1] - ptr[c];
+      if (n > tpb) return fail(BX_EINVAL, "a cell has more membranes than a CTA has threads");
+      if ((acc + n > tpb || nc + 1 > max_cells) && acc > 0) {
+        blk.push_back(c);
+        blk_cl.push_back(cl);
+        acc = 0;
+        nc = 0;
+      }
+      acc += n;
+      ++nc;
+    }
+    blk.push_back(h->cl_cell[cl + 1]);
+    blk_cl.push_back(cl);
+    cl_blk[cl + 1] = (int)blk.size() - 1;
+  }
+  const int nblk = (int)blk.size() - 1;
+  std::vector<uint8_t> lcell(h->M);
+  for (int b = 0; b < nblk; ++b)
+    for (int c = blk[b]; c < blk[b + 1]; ++c)
+      for (int m = ptr[c]; m < ptr[c + 1]; ++m) lcell[m] = (uint8_t)(c - blk[b]);
+  BX_CU(cudaStreamSynchronize(h->stream));
+  void* old[] = {h->d_blk, h->d_blk_cl, h->d_cl_blk, h->d_lcell, h->s_part, h->d_env_part};
+  for (void* q : old)
+    if (q) cudaFree(q);
+  h->d_blk = h->d_blk_cl = h->d_cl_blk = nullptr;
+  h->d_lcell = nullptr;
+  h->s_part = nullptr;
+  h->d_env_part = nullptr;
+  BX_CU(dalloc(&h->d_blk, blk.size()));
+  BX_CU(h2d(h->d_blk, blk.data(), blk.size()));
+  BX_CU(dalloc(&h->d_blk_cl, blk_cl.size()));
+  BX_CU(h2d(h->d_blk_cl, blk_cl.data(), blk_cl.size()));
+  BX_CU(dalloc(&h->d_cl_blk, cl_blk.size()));
+  BX_CU(h2d(h->d_cl_blk, cl_blk.data(), cl_blk.size()));
+  if (h->mode == MODE_SPLIT) {
+    BX_CU(dalloc(&h->d_lcell, h->M));
+    BX_CU(h2d(h->d_lcell, lcell.data(), lcell.size()));
+    BX_CU(dalloc(&h->s_part, (size_t)nblk * h->I));
+  } else {
+    BX_CU(dalloc(&h->d_env_part, (size_t)nblk * h->I));
+  }
+  h->cl_blk = cl_blk;
+  h->nblk = nblk;
+  h->tpb = tpb;
+  h->graph_valid = false;
+  return BX_OK;
+}
+
 int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, bx_handle* out) {
   if (!gs || !ps || !out || ncl <= 0) return fail(BX_EINVAL, "null argument");
   *out = nullptr;
@@ -482,10 +565,10 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   const int G = h->G;
 
   // ---- concatenate the clusters
-  std::vector<int> ptr(C + 1), nn(M), m2c(M), nn_cell(M), map_env(M), blk{0}, blk_cl;
-  std::vector<uint8_t> bflag(M), lcell(M);
+  std::vector<int> ptr(C + 1), nn(M), m2c(M), nn_cell(M), map_env(M);
+  std::vector<uint8_t> bflag(M);
   std::vector<double> msa(M), mnx(M), mny(M), gjw(M), swm(M), swo(M), vol(C), csa(C), div(C);
-  h->cl_cell.assign(ncl + 1, 0); h->cl_mem.assign(ncl + 1, 0); h->cl_blk.assign(ncl + 1, 0);
+  h->cl_cell.assign(ncl + 1, 0); h->cl_mem.assign(ncl + 1, 0);
   int coff = 0, moff = 0;
   ptr[0] = 0;
   for (int cl = 0; cl < ncl; ++cl) {
@@ -502,26 +585,12 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
       msa[moff + m] = g.mem_sa[m]; mnx[moff + m] = g.mem_nx[m]; mny[moff + m] = g.mem_ny[m];
       gjw[moff + m] = g.gj_weight[m]; swm[moff + m] = g.smooth_weight_mem[m]; swo[moff + m] = g.smooth_weight_o[m];
     }
-    // CTA partition of this cluster: whole cells, at most kTPB membranes
-    int acc = 0;
-    for (int c = 0; c < g.n_cells; ++c) {
-      const int n = g.cell_mem_ptr[c + 1] - g.cell_mem_ptr[c];
-      if (acc + n > kTPB) { blk.push_back(coff + c); blk_cl.push_back(cl); acc = 0; }
-      acc += n;
-    }
-    blk.push_back(coff + g.n_cells);
-    blk_cl.push_back(cl);
     coff += g.n_cells;
     moff += g.n_mems;
     h->cl_cell[cl + 1] = coff;
     h->cl_mem[cl + 1] = moff;
-    h->cl_blk[cl + 1] = (int)blk.size() - 1;
   }
-  h->nblk = (int)blk.size() - 1;
   for (int m = 0; m < M; ++m) nn_cell[m] = m2c[nn[m]];
-  for (int b = 0; b < h->nblk; ++b)
-    for (int c = blk[b]; c < blk[b + 1]; ++c)
-      for (int m = ptr[c]; m < ptr[c + 1]; ++m) lcell[m] = (uint8_t)(c - blk[b]);
   h->h_cell_ptr = ptr; h->h_m2c = m2c; h->h_map_env = map_env;
   h->h_phib.assign(G, 0.0);
 
@@ -552,9 +621,6 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   ALLOC(h->d_nn, M); H2D(h->d_nn, nn.data(), M);
   ALLOC(h->d_nn_cell, M); H2D(h->d_nn_cell, nn_cell.data(), M);
   ALLOC(h->d_map_env, M); H2D(h->d_map_env, map_env.data(), M);
-  ALLOC(h->d_blk, blk.size()); H2D(h->d_blk, blk.data(), blk.size());
-  ALLOC(h->d_blk_cl, blk_cl.size()); H2D(h->d_blk_cl, blk_cl.data(), blk_cl.size());
-  ALLOC(h->d_cl_blk, ncl + 1); H2D(h->d_cl_blk, h->cl_blk.data(), ncl + 1);
   ALLOC(h->d_bflag, M); H2D(h->d_bflag, bflag.data(), M);
   ALLOC(h->d_mem_sa, M); H2D(h->d_mem_sa, msa.data(), M);
   ALLOC(h->d_gj_w, M); H2D(h->d_gj_w, gjw.data(), M);
@@ -574,7 +640,6 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   if (h->mode == MODE_SPLIT) {
     std::vector<float> fsa(M), gw0(M);
     for (int m = 0; m < M; ++m) { fsa[m] = (float)msa[m]; gw0[m] = bflag[m] ? 0.0f : (float)gjw[m]; }
-    ALLOC(h->d_lcell, M); H2D(h->d_lcell, lcell.data(), M);
     ALLOC(h->d_mem_sa_f, M); H2D(h->d_mem_sa_f, fsa.data(), M);
     ALLOC(h->d_gjw0_f, M); H2D(h->d_gjw0_f, gw0.data(), M);
     ALLOC(h->d_dtv, C); ALLOC(h->d_dvc, C);
@@ -586,7 +651,6 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
       return bail(BX_ECUDA, "cudaMemset");
     ALLOC(h->s_cenv_f, (size_t)ncl * I); ALLOC(h->d_cenv, (size_t)ncl * I);
     ALLOC(h->s_pump, ncl);
-    ALLOC(h->s_part, (size_t)h->nblk * I);
     ALLOC(h->s_phib, G);
     if (cudaMemset(h->s_phib, 0, (size_t)G * sizeof(float)) != cudaSuccess) return bail(BX_ECUDA, "cudaMemset");
     ALLOC(h->o_vmc, C); ALLOC(h->o_vm_mem, M);
@@ -600,7 +664,6 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     ALLOC(h->d_ccm[0], (size_t)I * C); ALLOC(h->d_ccm[1], (size_t)I * C);
     ALLOC(h->d_cc, (size_t)I * C);
     ALLOC(h->d_cenv, h->ecm ? (size_t)I * G : (size_t)ncl * I);
-    ALLOC(h->d_env_part, (size_t)h->nblk * I);
   }
   if (h->ecm) {
     ALLOC(h->d_env_ptr, G + 1); H2D(h->d_env_ptr, env_ptr.data(), G + 1);
@@ -620,7 +683,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   ALLOC(h->o_Egjx, M); ALLOC(h->o_Egjy, M); ALLOC(h->o_gjopen, M); ALLOC(h->o_sigma, C);
 #undef ALLOC
 #undef H2D
-  if (upload_param_arrays(h) != BX_OK) {
+  if (upload_param_arrays(h) != BX_OK || build_partition(h, kTPB) != BX_OK) {
     std::string msg = g_err;
     return bail(BX_ECUDA, msg);
   }
@@ -978,6 +1041,67 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
 }
 
 int64_t bx_launch_count(bx_handle h) { return h ? h->launches : -1; }
+
+// Autotuner: time `n_steps` eager steps for each CTA size, keep the fastest.
+// The state is saved before the trials and restored after, so tuning does not
+// advance the simulation.
+int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out) {
+  if (!h || n_steps <= 0) return fail(BX_EINVAL, "bad arguments");
+  if (!h->have_state || !h->have_dm) return fail(BX_ESTATE, "upload state and Dm first");
+  BX_CU(cudaStreamSynchronize(h->stream));
+  struct Buf { void* p; size_t bytes; std::vector<char> save; };
+  const size_t C = h->C, I = h->I, M = h->M;
+  const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
+  std::vector<Buf> bufs;
+  if (h->mode == MODE_SPLIT) {
+    bufs = {{h->s_rec[h->parity], C * kRec * 4, {}}, {h->s_cc2, C * I * 8, {}},
+            {h->d_cenv, nenv * 8, {}}, {h->s_cenv_f, nenv * 4, {}}};
+  } else {
+    bufs = {{h->d_vm[h->parity], M * 8, {}}, {h->d_ccm[h->parity], C * I * 8, {}}, {h->d_cc, C * I * 8, {}},
+            {h->d_cenv, nenv * 8, {}}};
+    if (h->ecm) { bufs.push_back({h->d_Ex, (size_t)h->G * 8, {}}); bufs.push_back({h->d_Ey, (size_t)h->G * 8, {}}); }
+  }
+  bufs.push_back({h->d_status, 4 * sizeof(unsigned long long), {}});
+  for (Buf& b : bufs) {
+    b.save.resize(b.bytes);
+    BX_CU(cudaMemcpy(b.save.data(), b.p, b.bytes, cudaMemcpyDeviceToHost));
+  }
+  const int parity0 = h->parity;
+  const int64_t launches0 = h->launches;
+  const int cands[2] = {256, 128};
+  double best = 1e300;
+  int best_tpb = h->tpb;
+  cudaEvent_t e0, e1;
+  BX_CU(cudaEventCreate(&e0));
+  BX_CU(cudaEventCreate(&e1));
+  for (int tpb : cands) {
+    if (build_partition(h, tpb) != BX_OK) continue;
+    if (h->mode == MODE_SPLIT) BX_CU(cudaMemset(h->s_count, 0, (size_t)h->ncl * sizeof(unsigned int)));
+    h->parity = parity0;
+    for (int w = 0; w < 2; ++w) { enqueue_step(h, h->parity, false, h->stream); h->parity ^= 1; }
+    BX_CU(cudaEventRecord(e0, h->stream));
+    for (int q = 0; q < n_steps; ++q) { enqueue_step(h, h->parity, false, h->stream); h->parity ^= 1; }
+    BX_CU(cudaEventRecord(e1, h->stream));
+    BX_CU(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    BX_CU(cudaEventElapsedTime(&ms, e0, e1));
+    const double per = ms / n_steps;
+    if (per < best) { best = per; best_tpb = tpb; }
+    // restore the state for the next candidate / the caller
+    h->parity = parity0;
+    for (Buf& b : bufs) BX_CU(cudaMemcpy(b.p, b.save.data(), b.bytes, cudaMemcpyHostToDevice));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int rc = build_partition(h, best_tpb);
+  if (rc != BX_OK) return rc;
+  if (h->mode == MODE_SPLIT) BX_CU(cudaMemset(h->s_count, 0, (size_t)h->ncl * sizeof(unsigned int)));
+  h->launches = launches0;
+  h->parity = parity0;
+  if (tpb_out) *tpb_out = best_tpb;
+  if (ms_per_step_out) *ms_per_step_out = best;
+  return BX_OK;
+}
 
 int bx_dense_apply_f64(const double* A, const double* x, double* y, int n, int nrhs, void* stream) {
   if (!A || !x || !y || n <= 0 || nrhs <= 0 || nrhs > 4) return fail(BX_EINVAL, "bad dense_apply arguments");

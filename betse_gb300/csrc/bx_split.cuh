@@ -174,7 +174,7 @@ __device__ void finalize_env(const SplitGeom& g, const SplitPtrs& p, int I, int 
 }
 
 template <int TPB, int REC, bool OUT, bool PHIB>
-__global__ void __launch_bounds__(TPB)
+__global__ void __launch_bounds__(TPB, 2048 / TPB / 2)
 k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   __shared__ float sA[kMaxIons][TPB];
   __shared__ float sB[kMaxIons][TPB];
@@ -184,25 +184,76 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   __shared__ int sLast;
   const int I = k.I;
   const int b = blockIdx.x;
+  const int t = threadIdx.x;
+
+  // ---- prologue: read-only geometry and channel data.  With programmatic
+  // dependent launch this overlaps the previous step's tail; the next step
+  // may be scheduled as soon as every CTA of this one is resident.
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
+  cudaTriggerProgrammaticLaunchCompletion();
+#endif
   const int c0 = g.blk_cell[b], c1 = g.blk_cell[b + 1];
   const int cl = g.blk_cluster[b];
   const int m0 = g.cell_ptr[c0], m1 = g.cell_ptr[c1];
-  const int t = threadIdx.x;
+  const int ncell = c1 - c0;
   const int m = m0 + t;
   const bool active = m < m1;
+  int c = 0, cn = 0;
+  float sa = 0.f, gw = 0.f;
+  float dmv[kMaxIons];
+#pragma unroll
+  for (int i = 0; i < kMaxIons; ++i) dmv[i] = 0.f;
+  if (active) {
+    c = c0 + g.lcell[m];
+    cn = g.nn_cell[m];
+    sa = g.mem_sa[m];
+    gw = g.gjw[m] * k.gj_block;
+#pragma unroll
+    for (int i = 0; i < kMaxIons; ++i)
+      if (i < I) dmv[i] = p.Dm[(size_t)i * g.M + m];
+  }
+  // operands of the (ion, cell) phase; at most three (ion, cell) pairs per
+  // thread because every cell has at least three membranes
+  constexpr int QPT = 3;
+  int q_a0[QPT], q_a1[QPT];
+  float q_dtv[QPT];
+#pragma unroll
+  for (int r = 0; r < QPT; ++r) {
+    const int q = t + r * TPB;
+    q_a0[r] = q_a1[r] = 0;
+    q_dtv[r] = 0.f;
+    if (q < I * ncell) {
+      const int lc = q % ncell;
+      q_a0[r] = g.cell_ptr[c0 + lc] - m0;
+      q_a1[r] = g.cell_ptr[c0 + lc + 1] - m0;
+      q_dtv[r] = g.dtv[c0 + lc];
+    }
+  }
+  const float dvc = (t < ncell) ? g.dvc[c0 + t] : 0.f;
+
+  // ---- wait for the previous step's state
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
+  cudaGridDependencySynchronize();
+#endif
+
+  float2 q_x[QPT];
+#pragma unroll
+  for (int r = 0; r < QPT; ++r) {
+    const int q = t + r * TPB;
+    q_x[r] = make_float2(0.f, 0.f);
+    if (q < I * ncell) {
+      const int i = q / ncell, lc = q - i * ncell;
+      q_x[r] = p.cc2[(size_t)i * g.C + c0 + lc];
+    }
+  }
   float env_acc[kMaxIons];
 #pragma unroll
   for (int i = 0; i < kMaxIons; ++i) env_acc[i] = 0.f;
 
   if (active) {
-    const int c = c0 + g.lcell[m];
-    const int cn = g.nn_cell[m];
     float own[REC], nbr[REC];
     load_rec<REC>(p.rec_in, c, own);
     load_rec<REC>(p.rec_in, cn, nbr);
-    float dmv[kMaxIons];
-#pragma unroll
-    for (int i = 0; i < kMaxIons; ++i) dmv[i] = (i < I) ? p.Dm[(size_t)i * g.M + m] : 0.f;
     float v = own[REC - 1];
     float vn = nbr[REC - 1];
     if (PHIB) { v -= p.phib[g.map_env[m]]; vn -= p.phib[g.map_env[g.nn[m]]]; }
@@ -214,8 +265,6 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     sm.em1 = expm1f(-sm.a1); sm.e1 = 1.f + sm.em1; sm.r = 1.f / sm.em1; sm.q2 = 1.f / (2.f + sm.em1);
     sg.a1 = vgj1 * k.F_RT;
     sg.em1 = expm1f(-sg.a1); sg.e1 = 1.f + sg.em1; sg.r = 1.f / sg.em1; sg.q2 = 1.f / (2.f + sg.em1);
-    const float sa = g.mem_sa[m];
-    const float gw = g.gjw[m] * k.gj_block;
     const float* ce = p.cenv_f + (size_t)cl * I;
     float fNa = 0.f;
     const float pc = p.pump_coef[cl];
@@ -275,41 +324,40 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   }
 
   // cell phase 1: one thread per (ion, cell) -- update_all_concs
-  const int ncell = c1 - c0;
   int bad = 0, neg = 0;
-  for (int q = t; q < I * ncell; q += TPB) {
-    const int i = q / ncell, lc = q - i * ncell;
-    const int c = c0 + lc;
-    const int a0 = g.cell_ptr[c] - m0, a1 = g.cell_ptr[c + 1] - m0;
-    float s1 = 0.f, s2 = 0.f;
-    for (int j = a0; j < a1; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
-    const float dtv = g.dtv[c];
-    const float2 x2 = p.cc2[(size_t)i * g.C + c];
-    df x{x2.x, x2.y};
-    x = df_add_f(x, s1 * dtv);                         // update_Co
-    sRec[lc][i] = x.hi + x.lo;                         // cc_at_mem (before the GJ term)
-    x = df_add_f(x, s2 * dtv);                         // gap-junction term
-    if (x.hi != x.hi) bad++;
-    if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg++; }   // no_negs
-    p.cc2[(size_t)i * g.C + c] = make_float2(x.hi, x.lo);
-    const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
-    sQ[i][lc] = make_float2(qz.hi, qz.lo);
+#pragma unroll
+  for (int r = 0; r < QPT; ++r) {
+    const int q = t + r * TPB;
+    if (q < I * ncell) {
+      const int i = q / ncell, lc = q - i * ncell;
+      float s1 = 0.f, s2 = 0.f;
+      for (int j = q_a0[r]; j < q_a1[r]; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
+      df x{q_x[r].x, q_x[r].y};
+      x = df_add_f(x, s1 * q_dtv[r]);                  // update_Co
+      sRec[lc][i] = x.hi + x.lo;                       // cc_at_mem (before the GJ term)
+      x = df_add_f(x, s2 * q_dtv[r]);                  // gap-junction term
+      if (x.hi != x.hi) bad++;
+      if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg++; }   // no_negs
+      p.cc2[(size_t)i * g.C + c0 + lc] = make_float2(x.hi, x.lo);
+      const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
+      sQ[i][lc] = make_float2(qz.hi, qz.lo);
+    }
   }
   __syncthreads();
   // cell phase 2: charge sum -> Vmem, write the record (update_V, sim.py:2027-2029)
   if (t < ncell) {
-    const int c = c0 + t;
+    const int cc = c0 + t;
     df rho{0.f, 0.f};
     for (int i = 0; i < I; ++i) rho = df_add(rho, df{sQ[i][t].x, sQ[i][t].y});
-    const float vc = (rho.hi + rho.lo) * g.dvc[c];
+    const float vc = (rho.hi + rho.lo) * dvc;
     sRec[t][REC - 1] = vc;
     for (int i = I; i < REC - 1; ++i) sRec[t][i] = 0.f;
-    float4* out4 = reinterpret_cast<float4*>(p.rec_out + (size_t)c * REC);
+    float4* out4 = reinterpret_cast<float4*>(p.rec_out + (size_t)cc * REC);
 #pragma unroll
     for (int q = 0; q < REC / 4; ++q)
       out4[q] = make_float4(sRec[t][4 * q], sRec[t][4 * q + 1], sRec[t][4 * q + 2], sRec[t][4 * q + 3]);
     if (vc != vc) atomicAdd(&p.status[0], 1ull);
-    if (OUT) { p.o_rho[c] = (double)rho.hi + (double)rho.lo; p.o_vmem[c] = (double)vc; }
+    if (OUT) { p.o_rho[cc] = (double)rho.hi + (double)rho.lo; p.o_vmem[cc] = (double)vc; }
   }
   if (bad) atomicAdd(&p.status[1], (unsigned long long)bad);
   if (neg) atomicAdd(&p.status[2], (unsigned long long)neg);
@@ -342,7 +390,7 @@ struct SplitOutPtrs {
   const float2* cc2; const float* phib;
   double* Jn; double* Imem; double* Jcx; double* Jcy; double* Jc; double* vmave; double* dvm;
   double* Ecx; double* Ecy; double* Emc; double* Egjx; double* Egjy; double* gjopen; double* sigma;
-  double* vm_mem;
+  double* vm_mem;      // [M] start-of-step Vmem per membrane (update_gj reads it)
 };
 struct SplitOutConst {
   int I; double zF[kMaxIons]; double sig_coef[kMaxIons]; double dt; double gj_len; double gj_block;
@@ -370,7 +418,7 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
     Jraw = -Jm + Jg;
     const double ph = p.phib ? (double)p.phib[g.map_env[m]] : 0.0;
     vm = (double)p.rec_new[(size_t)c * p.rec + p.rec - 1] - ph;
-    p.vm_mem[m] = vm;
+    p.vm_mem[m] = (double)p.rec_old[(size_t)c * p.rec + p.rec - 1] - ph;
     sX[0][t] = Jraw * g.mem_sa[m];
     sX[1][t] = vm;
   } else { sX[0][t] = 0.0; sX[1][t] = 0.0; }
@@ -422,7 +470,8 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
   }
 }
 
-// E_gj needs the partner's Vmem: a separate pass over membranes.
+// E_gj needs the partner's start-of-step Vmem (update_gj runs before
+// update_V, sim.py:2166-2174): a separate pass over membranes.
 __global__ void k_split_egj(int M, const int* __restrict__ nn, const double* __restrict__ vm_mem,
                             const double* __restrict__ nx, const double* __restrict__ ny,
                             double gj_len, double* Egjx, double* Egjy) {

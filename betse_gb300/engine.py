@@ -145,6 +145,14 @@ class ClusterEngine:
         _lib.check(self.lib.bx_time_cell_kernel(self.h, int(n), ct.byref(ms)), 'bx_time_cell_kernel')
         return ms.value
 
+    def autotune(self, n_steps=20):
+        """Pick the fastest CTA size for this cluster; the state is unchanged.
+        Returns (threads per CTA, ms per step)."""
+        tpb = ct.c_int()
+        ms = ct.c_double()
+        _lib.check(self.lib.bx_autotune(self.h, int(n_steps), ct.byref(tpb), ct.byref(ms)), 'bx_autotune')
+        return tpb.value, ms.value
+
     def cell_kernel_bytes(self) -> int:
         return int(self.lib.bx_cell_kernel_bytes(self.h))
 

@@ -228,6 +228,12 @@ int bx_time_cell_kernel(bx_handle h, int n, double* ms_per_launch);
  * counted once at its stored width; reads plus writes). */
 int64_t bx_cell_kernel_bytes(bx_handle h);
 
+/* Autotuner: times n_steps steps for each supported CTA size (128 and 256
+ * membrane slots) on the uploaded state, keeps the fastest, and restores the
+ * state so the simulation does not advance.  Reports the choice and its
+ * ms per step (either pointer may be NULL). */
+int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out);
+
 /* Version / diagnostics. */
 int bx_abi_version(void);
 const char* bx_last_error(void);

@@ -161,4 +161,6 @@ def output_floors(d, cc, o):
             'rate_NaKATP': float(np.max(f_mem)), 'Jn': j_floor,
             'I_mem': j_floor * np.max(d['geom_mem_sa']),
             'J_cell_x': j_floor, 'J_cell_y': j_floor, 'Jc': j_floor,
-            'E_cell_x': j_floor / sig, 'E_cell_y': j_floor / sig, 'Emc': j_floor / sig}
+            'E_cell_x': j_floor / sig, 'E_cell_y': j_floor / sig, 'Emc': j_floor / sig,
+            # E_gj = -(vm[nn] - vm[m]) / gj_len: two Vmem floors over 26 nm
+            'E_gj_x': 2 * vfl / float(d['geom_gj_len']), 'E_gj_y': 2 * vfl / float(d['geom_gj_len'])}

@@ -152,3 +152,21 @@ def test_split_outputs_close_to_betse():
               'vm_ave', 'sigma_cell', 'E_gj_x', 'E_gj_y', 'gjopen'):
         ref = d[f's{cp}_{k}']
         assert np.max(np.abs(o[k] - ref)) <= 2e-3 * np.max(np.abs(ref)) + 1e-30, k
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split'])
+def test_autotune_keeps_state_and_results(precision):
+    """Autotuning changes the CTA partition, not the simulation: the state is
+    restored and the result after stepping matches an untuned engine."""
+    d = gi.load('noecm_r80_s1')
+    with _engine(d, precision) as a, _engine(d, precision) as b:
+        tpb, ms = a.autotune(5)
+        assert tpb in (128, 256) and ms > 0
+        s0 = a.download()
+        assert np.array_equal(s0['vm'], b.download()['vm'])
+        a.step(40)
+        b.step(40)
+        sa, sb = a.download(), b.download()
+    tol = 0.0 if precision == 'fp64' else 1e-12
+    for k in sa:
+        assert gi.rel_err(sa[k], sb[k]) <= tol, k
