@@ -273,9 +273,9 @@ bx::SplitGeom split_geom(const bx_cluster* h) {
 bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
   bx::SplitPtrs p{};
   p.rec_in = h->s_rec[parity]; p.rec_out = h->s_rec[parity ^ 1];
-  p.cc2 = h->s_cc2; p.Dm = h->d_Dm_f; p.cenv_f = h->s_cenv_f; p.cenv64 = h->d_cenv;
-  p.env_scale = h->d_env_scale; p.pump_coef = h->s_pump; p.phib = h->s_phib;
-  p.env_part = h->s_part; p.cl_count = h->s_count; p.status = h->d_status;
+  p.cc2 = h->s_cc2; p.Dm = h->d_Dm_f; p.cenv_f = h->s_cenv_f;
+  p.pump_coef = h->s_pump; p.phib = h->s_phib;
+  p.env_part = h->s_part; p.status = h->d_status;
   p.o_fmem = h->o_fmem; p.o_fgj = h->o_fgj; p.o_rate = h->o_rate; p.o_rho = h->o_rho;
   p.o_vmem = h->o_vmc;
   return p;
@@ -283,16 +283,13 @@ bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
 
 inline int env_grid(int G) { return (G + kEnvTPB - 1) / kEnvTPB; }
 
-template <int TPB, bool OUT, bool PHIB>
-cudaError_t launch_split_t(bx_cluster* h, int parity, cudaStream_t s) {
-  bx::SplitGeom g = split_geom(h);
-  bx::SplitPtrs p = split_ptrs(h, parity);
-  bx::SplitConst k = make_split_const(h);
-  // programmatic dependent launch: the kernel's geometry prologue overlaps the
-  // previous step; cudaGridDependencySynchronize orders the state accesses
+// launch with programmatic dependent launch: the kernel's prologue overlaps
+// the previous kernel; cudaGridDependencySynchronize orders the state accesses
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)h->nblk);
-  cfg.blockDim = dim3(TPB);
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -300,21 +297,32 @@ cudaError_t launch_split_t(bx_cluster* h, int parity, cudaStream_t s) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, bx::k_split_step<TPB, kRec, OUT, PHIB>, g, p, k);
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+template <int TPB, bool OUT, bool PHIB>
+cudaError_t launch_split_t(bx_cluster* h, int parity, cudaStream_t s) {
+  return launch_pdl(bx::k_split_step<TPB, kRec, OUT, PHIB>, (unsigned)h->nblk, TPB, s, split_geom(h),
+                    split_ptrs(h, parity), make_split_const(h));
 }
 
 cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
-  const int code = (h->tpb == 128 ? 4 : 0) | (out ? 2 : 0) | (h->phib_nonzero ? 1 : 0);
+  const int code = (h->tpb == 192 ? 4 : 0) | (out ? 2 : 0) | (h->phib_nonzero ? 1 : 0);
   switch (code) {
     case 0: return launch_split_t<256, false, false>(h, parity, s);
     case 1: return launch_split_t<256, false, true>(h, parity, s);
     case 2: return launch_split_t<256, true, false>(h, parity, s);
     case 3: return launch_split_t<256, true, true>(h, parity, s);
-    case 4: return launch_split_t<128, false, false>(h, parity, s);
-    case 5: return launch_split_t<128, false, true>(h, parity, s);
-    case 6: return launch_split_t<128, true, false>(h, parity, s);
-    default: return launch_split_t<128, true, true>(h, parity, s);
+    case 4: return launch_split_t<192, false, false>(h, parity, s);
+    case 5: return launch_split_t<192, false, true>(h, parity, s);
+    case 6: return launch_split_t<192, true, false>(h, parity, s);
+    default: return launch_split_t<192, true, true>(h, parity, s);
   }
+}
+
+cudaError_t launch_split_env(bx_cluster* h, cudaStream_t s) {
+  return launch_pdl(bx::k_split_env<512>, (unsigned)h->ncl, 512, s, (const float*)h->s_part,
+                    (const int*)h->d_cl_blk, h->I, h->d_cenv, h->s_cenv_f, (const double*)h->d_env_scale);
 }
 
 cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
@@ -334,7 +342,9 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   if (h->mode == MODE_SPLIT) {
     e = launch_split(h, parity, out, s);
     if (e != cudaSuccess) return e;
-    h->launches += 1;
+    e = launch_split_env(h, s);
+    if (e != cudaSuccess) return e;
+    h->launches += 2;
     if (out) {
       bx::SplitOutGeom og{h->C, h->M, h->I, h->d_cell_ptr, h->d_blk, h->d_nn, h->d_map_env,
                           h->d_mem_sa, h->d_nx, h->d_ny, h->d_swm, h->d_swo, h->d_cell_sa,
@@ -348,7 +358,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
       oc.I = h->I;
       for (int i = 0; i < h->I; ++i) { oc.zF[i] = d.zF[i]; oc.sig_coef[i] = d.sig_coef[i]; }
       oc.dt = d.dt; oc.gj_len = h->gj_len; oc.gj_block = d.gj_block;
-      if (h->tpb == 128) bx::k_split_outputs<128><<<h->nblk, 128, 0, s>>>(og, op, oc);
+      if (h->tpb == 192) bx::k_split_outputs<192><<<h->nblk, 192, 0, s>>>(og, op, oc);
       else bx::k_split_outputs<256><<<h->nblk, 256, 0, s>>>(og, op, oc);
       bx::k_split_egj<<<(h->M + 255) / 256, 256, 0, s>>>(h->M, h->d_nn, h->o_vm_mem, h->d_nx, h->d_ny,
                                                          h->gj_len, h->o_Egjx, h->o_Egjy);
@@ -387,7 +397,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
 }
 
 int launches_per_step(const bx_cluster* h) {
-  if (h->mode == MODE_SPLIT) return 1;
+  if (h->mode == MODE_SPLIT) return 2;
   if (!h->ecm) return 2;
   return h->par.sharpness < 1.0 ? 7 : 6;
 }
@@ -463,11 +473,13 @@ int check_geom(const bx_geom* g, const bx_params* p) {
 }
 
 // CTA partition for `tpb` membrane slots: runs of whole cells of one cluster
-// with at most tpb membranes and at most 3*tpb/I cells (the (ion, cell) phase
-// gives each thread at most three pairs).  Rebuilt by the autotuner.
+// with at most tpb membranes; the split form also caps a tile at 32 cells
+// (its (ion, cell) phase maps ion -> warp, cell -> lane).  Rebuilt by the
+// autotuner.
 int build_partition(bx_cluster* h, int tpb) {
   const std::vector<int>& ptr = h->h_cell_ptr;
-  const int max_cells = std::max(1, (3 * tpb) / h->I);
+  if (h->mode == MODE_SPLIT && h->I > tpb / 32) return fail(BX_EINVAL, "CTA too small for the ion count");
+  const int max_cells = (h->mode == MODE_SPLIT) ? bx::kCellsPerCta : tpb;
   std::vector<int> blk{0}, blk_cl;
   std::vector<int> cl_blk(h->ncl + 1, 0);
   for (int cl = 0; cl < h->ncl; ++cl) {
@@ -646,9 +658,6 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     ALLOC(h->d_Dm_f, (size_t)I * M);
     ALLOC(h->s_cc2, (size_t)I * C);
     ALLOC(h->s_rec[0], (size_t)kRec * C); ALLOC(h->s_rec[1], (size_t)kRec * C);
-    ALLOC(h->s_count, ncl);
-    if (cudaMemset(h->s_count, 0, (size_t)ncl * sizeof(unsigned int)) != cudaSuccess)
-      return bail(BX_ECUDA, "cudaMemset");
     ALLOC(h->s_cenv_f, (size_t)ncl * I); ALLOC(h->d_cenv, (size_t)ncl * I);
     ALLOC(h->s_pump, ncl);
     ALLOC(h->s_phib, G);
@@ -831,7 +840,6 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
     for (size_t q = 0; q < nenv; ++q) cef[q] = (float)s->cc_env[q];
     BX_CU(h2d(h->s_rec[0], rec.data(), rec.size()));
     BX_CU(h2d(h->s_cc2, cc2.data(), cc2.size()));
-    BX_CU(cudaMemset(h->s_count, 0, (size_t)h->ncl * sizeof(unsigned int)));
     BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
     BX_CU(h2d(h->s_cenv_f, cef.data(), nenv));
   } else {
@@ -1068,7 +1076,7 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   }
   const int parity0 = h->parity;
   const int64_t launches0 = h->launches;
-  const int cands[2] = {256, 128};
+  const int cands[2] = {256, (h->mode == MODE_SPLIT) ? 192 : 128};
   double best = 1e300;
   int best_tpb = h->tpb;
   cudaEvent_t e0, e1;
@@ -1076,7 +1084,6 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   BX_CU(cudaEventCreate(&e1));
   for (int tpb : cands) {
     if (build_partition(h, tpb) != BX_OK) continue;
-    if (h->mode == MODE_SPLIT) BX_CU(cudaMemset(h->s_count, 0, (size_t)h->ncl * sizeof(unsigned int)));
     h->parity = parity0;
     for (int w = 0; w < 2; ++w) { enqueue_step(h, h->parity, false, h->stream); h->parity ^= 1; }
     BX_CU(cudaEventRecord(e0, h->stream));
@@ -1095,7 +1102,6 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   cudaEventDestroy(e1);
   int rc = build_partition(h, best_tpb);
   if (rc != BX_OK) return rc;
-  if (h->mode == MODE_SPLIT) BX_CU(cudaMemset(h->s_count, 0, (size_t)h->ncl * sizeof(unsigned int)));
   h->launches = launches0;
   h->parity = parity0;
   if (tpb_out) *tpb_out = best_tpb;

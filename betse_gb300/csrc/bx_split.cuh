@@ -110,13 +110,10 @@ struct SplitPtrs {
   const float* __restrict__ rec_in; float* __restrict__ rec_out;   // [C][REC]
   float2* __restrict__ cc2;                // [I][C]
   const float* __restrict__ Dm;            // [I][M]
-  float* cenv_f;                           // [ncl][I] FP32 copy of the environment
-  double* cenv64;                          // [ncl][I] FP64 master copy
-  const double* __restrict__ env_scale;    // [ncl] dt / (vol_env * M_cluster)
+  const float* __restrict__ cenv_f;        // [ncl][I] FP32 copy of the environment
   const float* __restrict__ pump_coef;     // [ncl] -3 block alpha_NaK (0 = pump off)
   const float* __restrict__ phib;          // [G] (PHIB)
-  float* env_part;                         // [nblk][I] per-CTA partial sums
-  unsigned int* cl_count;                  // [ncl] CTAs of the cluster done this step
+  float* __restrict__ env_part;            // [nblk][I] per-CTA partial sums
   unsigned long long* status;              // nan_vm, nan_conc, neg clamps
   // outputs (OUT)
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_vmem;
@@ -132,63 +129,36 @@ __device__ __forceinline__ void load_rec(const float* __restrict__ rec, int c, f
   }
 }
 
-// Well-mixed environment of cluster cl (sim_toolbox.py:1196-1205), done by the
-// last CTA of the cluster to finish: it sums the cluster's per-CTA partials in
-// a fixed order (double-float), so the result does not depend on which CTA is
-// last.  No CTA waits for another.
-template <int TPB>
-__device__ void finalize_env(const SplitGeom& g, const SplitPtrs& p, int I, int cl) {
-  __shared__ float2 fin[kMaxIons][TPB / 32];
-  const int t = threadIdx.x;
-  const int b0 = g.cl_blk[cl], b1 = g.cl_blk[cl + 1];
-  df acc[kMaxIons];
-#pragma unroll
-  for (int i = 0; i < kMaxIons; ++i) acc[i] = df{0.f, 0.f};
-  for (int b = b0 + t; b < b1; b += TPB) {
-    const float* pp = p.env_part + (size_t)b * I;
-#pragma unroll
-    for (int i = 0; i < kMaxIons; ++i)
-      if (i < I) acc[i] = df_add_f(acc[i], __ldcg(pp + i));
-  }
-#pragma unroll
-  for (int i = 0; i < kMaxIons; ++i) {
-    if (i >= I) break;
-    df a = acc[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      df other{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
-      a = df_add(a, other);
-    }
-    if ((t & 31) == 0) fin[i][t >> 5] = make_float2(a.hi, a.lo);
-  }
-  __syncthreads();
-  if (t < I) {
-    df a{0.f, 0.f};
-    for (int w = 0; w < TPB / 32; ++w) a = df_add(a, df{fin[t][w].x, fin[t][w].y});
-    const double tot = (double)a.hi + (double)a.lo;
-    const double v = p.cenv64[(size_t)cl * I + t] - tot * p.env_scale[cl];
-    p.cenv64[(size_t)cl * I + t] = v;
-    p.cenv_f[(size_t)cl * I + t] = (float)v;
-  }
-  if (t == 0) p.cl_count[cl] = 0u;   // ready for the next step
-}
+// 2-ulp FP32 reciprocal (MUFU-based); operands here are far from the
+// denormal range except at exactly zero volts, where BETSE's 1e-25 nonce keeps
+// them above 1e-24.
+__device__ __forceinline__ float rcp_fast(float x) { return __fdividef(1.f, x); }
 
+constexpr int kCellsPerCta = 32;   // cells per CTA tile: (ion, cell) phase maps ion -> warp, cell -> lane
+
+// One time step of the split form for one CTA tile of at most 32 whole cells
+// (and at most TPB membranes).  Phases:
+//   prologue  read-only geometry, Dm                 (overlaps the previous step)
+//   wait      cudaGridDependencySynchronize
+//   membranes GHK + pump + gap-junction fluxes (FP32), per-ion f*sa into smem
+//   cells     warp i = ion i, lane = cell: update_all_concs in double-float
+//   charge    warp 0: rho = sum_i z_i F c_i (double-float) -> Vmem record
 template <int TPB, int REC, bool OUT, bool PHIB>
 __global__ void __launch_bounds__(TPB, 2048 / TPB / 2)
 k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   __shared__ float sA[kMaxIons][TPB];
   __shared__ float sB[kMaxIons][TPB];
   __shared__ float red[kMaxIons][TPB / 32];
-  __shared__ float sRec[TPB][REC];          // new records of the CTA's cells
-  __shared__ float2 sQ[kMaxIons][TPB];      // z F c per (ion, cell), double-float
-  __shared__ int sLast;
+  __shared__ float sRec[kCellsPerCta][REC];
+  __shared__ float2 sQ[kMaxIons][kCellsPerCta];
   const int I = k.I;
   const int b = blockIdx.x;
   const int t = threadIdx.x;
+  const int lane = t & 31, wid = t >> 5;
 
   // ---- prologue: read-only geometry and channel data.  With programmatic
-  // dependent launch this overlaps the previous step's tail; the next step
-  // may be scheduled as soon as every CTA of this one is resident.
+  // dependent launch this overlaps the previous kernel; the next kernel may
+  // be scheduled as soon as every CTA of this one is resident.
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
   cudaTriggerProgrammaticLaunchCompletion();
 #endif
@@ -212,40 +182,23 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     for (int i = 0; i < kMaxIons; ++i)
       if (i < I) dmv[i] = p.Dm[(size_t)i * g.M + m];
   }
-  // operands of the (ion, cell) phase; at most three (ion, cell) pairs per
-  // thread because every cell has at least three membranes
-  constexpr int QPT = 3;
-  int q_a0[QPT], q_a1[QPT];
-  float q_dtv[QPT];
-#pragma unroll
-  for (int r = 0; r < QPT; ++r) {
-    const int q = t + r * TPB;
-    q_a0[r] = q_a1[r] = 0;
-    q_dtv[r] = 0.f;
-    if (q < I * ncell) {
-      const int lc = q % ncell;
-      q_a0[r] = g.cell_ptr[c0 + lc] - m0;
-      q_a1[r] = g.cell_ptr[c0 + lc + 1] - m0;
-      q_dtv[r] = g.dtv[c0 + lc];
-    }
+  // (ion, cell) operands: warp wid handles ion wid, lane handles cell c0+lane
+  const bool cell_thr = (wid < I) && (lane < ncell);
+  int a0 = 0, a1 = 0;
+  float dtv = 0.f, dvc = 0.f;
+  if (cell_thr) {
+    a0 = g.cell_ptr[c0 + lane] - m0;
+    a1 = g.cell_ptr[c0 + lane + 1] - m0;
+    dtv = g.dtv[c0 + lane];
   }
-  const float dvc = (t < ncell) ? g.dvc[c0 + t] : 0.f;
+  if (t < ncell) dvc = g.dvc[c0 + t];
 
   // ---- wait for the previous step's state
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
   cudaGridDependencySynchronize();
 #endif
-
-  float2 q_x[QPT];
-#pragma unroll
-  for (int r = 0; r < QPT; ++r) {
-    const int q = t + r * TPB;
-    q_x[r] = make_float2(0.f, 0.f);
-    if (q < I * ncell) {
-      const int i = q / ncell, lc = q - i * ncell;
-      q_x[r] = p.cc2[(size_t)i * g.C + c0 + lc];
-    }
-  }
+  float2 x2 = make_float2(0.f, 0.f);
+  if (cell_thr) x2 = p.cc2[(size_t)wid * g.C + c0 + lane];
   float env_acc[kMaxIons];
 #pragma unroll
   for (int i = 0; i < kMaxIons; ++i) env_acc[i] = 0.f;
@@ -262,9 +215,9 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     const float vgj1 = ((vn + 1.0e-25f) - v1) + 1.0e-25f;
     GhkShared<float> sm, sg;
     sm.a1 = v1 * k.F_RT;
-    sm.em1 = expm1f(-sm.a1); sm.e1 = 1.f + sm.em1; sm.r = 1.f / sm.em1; sm.q2 = 1.f / (2.f + sm.em1);
+    sm.em1 = expm1f(-sm.a1); sm.e1 = 1.f + sm.em1; sm.r = rcp_fast(sm.em1); sm.q2 = rcp_fast(2.f + sm.em1);
     sg.a1 = vgj1 * k.F_RT;
-    sg.em1 = expm1f(-sg.a1); sg.e1 = 1.f + sg.em1; sg.r = 1.f / sg.em1; sg.q2 = 1.f / (2.f + sg.em1);
+    sg.em1 = expm1f(-sg.a1); sg.e1 = 1.f + sg.em1; sg.r = rcp_fast(sg.em1); sg.q2 = rcp_fast(2.f + sg.em1);
     const float* ce = p.cenv_f + (size_t)cl * I;
     float fNa = 0.f;
     const float pc = p.pump_coef[cl];
@@ -282,7 +235,7 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
       const float na3 = xna * xna * xna, k2 = xk * xk;
       const float num_e = na3 * k2 * k.atp_term;
       const float den_e = (1.f + na3) * (1.f + k2) * k.atp_den;
-      fNa = pc * num_e * (qden * k.K0 - qnum * sm.e1) / (den_e * qden * k.K0);
+      fNa = pc * num_e * (qden * k.K0 - qnum * sm.e1) * rcp_fast(den_e * qden * k.K0);
     }
 #pragma unroll
     for (int i = 0; i < REC - 1; ++i) {
@@ -306,72 +259,106 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   } else {
     for (int i = 0; i < I; ++i) { sA[i][t] = 0.f; sB[i][t] = 0.f; }
   }
-  // per-CTA partial sums of f_mem*sa per ion for the well-mixed environment
+  // per-CTA partial sums of f_mem*sa per ion (the finalize kernel reduces them)
 #pragma unroll
   for (int i = 0; i < kMaxIons; ++i) {
     if (i >= I) break;
     float s = env_acc[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((t & 31) == 0) red[i][t >> 5] = s;
+    if (lane == 0) red[i][wid] = s;
   }
   __syncthreads();
   if (t < I) {
     float s = 0.f;
     for (int w = 0; w < TPB / 32; ++w) s += red[t][w];
     p.env_part[(size_t)b * I + t] = s;
-    __threadfence();   // visible device-wide before this CTA is counted done
   }
 
-  // cell phase 1: one thread per (ion, cell) -- update_all_concs
+  // ---- cells: warp = ion, lane = cell -- update_all_concs (sim.py:2086-2111)
   int bad = 0, neg = 0;
-#pragma unroll
-  for (int r = 0; r < QPT; ++r) {
-    const int q = t + r * TPB;
-    if (q < I * ncell) {
-      const int i = q / ncell, lc = q - i * ncell;
-      float s1 = 0.f, s2 = 0.f;
-      for (int j = q_a0[r]; j < q_a1[r]; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
-      df x{q_x[r].x, q_x[r].y};
-      x = df_add_f(x, s1 * q_dtv[r]);                  // update_Co
-      sRec[lc][i] = x.hi + x.lo;                       // cc_at_mem (before the GJ term)
-      x = df_add_f(x, s2 * q_dtv[r]);                  // gap-junction term
-      if (x.hi != x.hi) bad++;
-      if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg++; }   // no_negs
-      p.cc2[(size_t)i * g.C + c0 + lc] = make_float2(x.hi, x.lo);
-      const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
-      sQ[i][lc] = make_float2(qz.hi, qz.lo);
-    }
+  if (cell_thr) {
+    const int i = wid;
+    float s1 = 0.f, s2 = 0.f;
+    for (int j = a0; j < a1; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
+    df x{x2.x, x2.y};
+    x = df_add_f(x, s1 * dtv);                         // update_Co
+    sRec[lane][i] = x.hi + x.lo;                       // cc_at_mem (before the GJ term)
+    x = df_add_f(x, s2 * dtv);                         // gap-junction term
+    if (x.hi != x.hi) bad = 1;
+    if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg = 1; }   // no_negs
+    p.cc2[(size_t)i * g.C + c0 + lane] = make_float2(x.hi, x.lo);
+    const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
+    sQ[i][lane] = make_float2(qz.hi, qz.lo);
   }
-  __syncthreads();
-  // cell phase 2: charge sum -> Vmem, write the record (update_V, sim.py:2027-2029)
+  const int n_bad = __syncthreads_count(bad);
+  const int n_neg = __syncthreads_count(neg);
+  // ---- charge -> Vmem (update_V, sim.py:2027-2029), one lane per cell
   if (t < ncell) {
     const int cc = c0 + t;
     df rho{0.f, 0.f};
     for (int i = 0; i < I; ++i) rho = df_add(rho, df{sQ[i][t].x, sQ[i][t].y});
     const float vc = (rho.hi + rho.lo) * dvc;
-    sRec[t][REC - 1] = vc;
-    for (int i = I; i < REC - 1; ++i) sRec[t][i] = 0.f;
+    float o[REC];
+#pragma unroll
+    for (int i = 0; i < REC - 1; ++i) o[i] = (i < I) ? sRec[t][i] : 0.f;
+    o[REC - 1] = vc;
     float4* out4 = reinterpret_cast<float4*>(p.rec_out + (size_t)cc * REC);
 #pragma unroll
-    for (int q = 0; q < REC / 4; ++q)
-      out4[q] = make_float4(sRec[t][4 * q], sRec[t][4 * q + 1], sRec[t][4 * q + 2], sRec[t][4 * q + 3]);
+    for (int q = 0; q < REC / 4; ++q) out4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
     if (vc != vc) atomicAdd(&p.status[0], 1ull);
     if (OUT) { p.o_rho[cc] = (double)rho.hi + (double)rho.lo; p.o_vmem[cc] = (double)vc; }
   }
-  if (bad) atomicAdd(&p.status[1], (unsigned long long)bad);
-  if (neg) atomicAdd(&p.status[2], (unsigned long long)neg);
-
-  // last CTA of the cluster: the well-mixed environment update
   if (t == 0) {
-    __threadfence();
-    const unsigned int done = atomicAdd(&p.cl_count[cl], 1u);
-    sLast = (done == (unsigned int)(g.cl_blk[cl + 1] - g.cl_blk[cl] - 1));
+    if (n_bad) atomicAdd(&p.status[1], (unsigned long long)n_bad);
+    if (n_neg) atomicAdd(&p.status[2], (unsigned long long)n_neg);
+  }
+}
+
+// Well-mixed environment per cluster (sim_toolbox.py:1196-1205):
+// c_env <- mean_m(c_env - f_m sa_m / vol_env * dt).  One CTA per cluster sums
+// the cluster's per-CTA partials in a fixed order (double-float), so the
+// result is deterministic.  Launched after the step kernel with programmatic
+// dependent launch.
+template <int NT>
+__global__ void __launch_bounds__(NT)
+k_split_env(const float* __restrict__ part, const int* __restrict__ cl_blk, int I,
+            double* cenv64, float* cenv_f, const double* __restrict__ env_scale) {
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
+  cudaTriggerProgrammaticLaunchCompletion();
+  cudaGridDependencySynchronize();
+#endif
+  __shared__ float2 fin[kMaxIons][NT / 32];
+  const int cl = blockIdx.x, t = threadIdx.x;
+  const int b0 = cl_blk[cl], b1 = cl_blk[cl + 1];
+  df acc[kMaxIons];
+#pragma unroll
+  for (int i = 0; i < kMaxIons; ++i) acc[i] = df{0.f, 0.f};
+  for (int b = b0 + t; b < b1; b += NT) {
+    const float* pp = part + (size_t)b * I;
+#pragma unroll
+    for (int i = 0; i < kMaxIons; ++i)
+      if (i < I) acc[i] = df_add_f(acc[i], pp[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < kMaxIons; ++i) {
+    if (i >= I) break;
+    df a = acc[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      df other{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
+      a = df_add(a, other);
+    }
+    if ((t & 31) == 0) fin[i][t >> 5] = make_float2(a.hi, a.lo);
   }
   __syncthreads();
-  if (sLast) {
-    __threadfence();
-    finalize_env<TPB>(g, p, I, cl);
+  if (t < I) {
+    df a{0.f, 0.f};
+    for (int w = 0; w < NT / 32; ++w) a = df_add(a, df{fin[t][w].x, fin[t][w].y});
+    const double tot = (double)a.hi + (double)a.lo;
+    const double v = cenv64[(size_t)cl * I + t] - tot * env_scale[cl];
+    cenv64[(size_t)cl * I + t] = v;
+    cenv_f[(size_t)cl * I + t] = (float)v;
   }
 }
 

@@ -161,7 +161,7 @@ def test_autotune_keeps_state_and_results(precision):
     d = gi.load('noecm_r80_s1')
     with _engine(d, precision) as a, _engine(d, precision) as b:
         tpb, ms = a.autotune(5)
-        assert tpb in (128, 256) and ms > 0
+        assert tpb in (128, 192, 256) and ms > 0
         s0 = a.download()
         assert np.array_equal(s0['vm'], b.download()['vm'])
         a.step(40)
