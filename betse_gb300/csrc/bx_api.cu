@@ -702,6 +702,9 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
 
 }  // namespace
 
+// shared with the other translation units of the library
+void bx_record_error(const char* msg) { g_err = msg; }
+
 extern "C" {
 
 int bx_abi_version(void) { return BX_ABI_VERSION; }

@@ -1,0 +1,221 @@
+// bx_noalloc.cu -- the plain FP64 step on caller-owned device memory, with no
+// allocation of any kind.
+//
+// Who needs it: code that must not allocate device memory while it steps --
+// a caller whose device memory is owned by another framework's pool, or one
+// that steps from a context where cudaMalloc is forbidden or too slow (a
+// real-time loop, an allocator-free embedding).  bx_cluster_create allocates
+// every buffer a handle needs; this entry point instead takes the caller's
+// device buffers and keeps the step's scratch (derived index maps, the CTA
+// tiling and the per-CTA partial sums of the well-mixed environment) in one
+// file-scope __device__ array of fixed size.
+//
+// Limits (checked before any work; BX_EINVAL beyond them):
+//   n_cells <= 16384, n_mems <= 131072, n_ions <= 8, and every run of 16
+//   consecutive cells has at most 256 membranes.
+// The array lives on every GPU that loads the library until the process
+// exits: 140,297 doubles, about 1.1 MB (kScratchDoubles).
+//
+// Sharing: every call uses the same array and leaves the last call's contents
+// in it; each call rebuilds what it reads before it reads it.  Calls that
+// overlap on the GPU (two streams, or two host threads) race on the array and
+// corrupt each other's results: serialise them.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <string>
+
+#include "../../include/bx.h"
+#include "bx_launch.cuh"
+
+namespace {
+
+constexpr int kMaxCells = 16384;
+constexpr int kMaxMems = 131072;
+constexpr int kTileCells = 16;
+constexpr int kTileThreads = 256;
+constexpr int kMaxTiles = kMaxCells / kTileCells;
+// layout of the scratch, in 8-byte words
+constexpr size_t kOffM2c = 0;                                   // int32 [kMaxMems]
+constexpr size_t kOffNnCell = kOffM2c + kMaxMems / 2;           // int32 [kMaxMems]
+constexpr size_t kOffBlk = kOffNnCell + kMaxMems / 2;           // int32 [kMaxTiles + 1]
+constexpr size_t kOffBlkCl = kOffBlk + (kMaxTiles + 2) / 2;     // int32 [kMaxTiles]
+constexpr size_t kOffClBlk = kOffBlkCl + kMaxTiles / 2;         // int32 [2]
+constexpr size_t kOffPart = kOffClBlk + 1;                      // double [kMaxTiles * 8]
+constexpr size_t kOffPump = kOffPart + (size_t)kMaxTiles * BX_MAX_IONS;  // double [1]
+constexpr size_t kOffEscale = kOffPump + 1;                     // double [1]
+constexpr size_t kOffStatus = kOffEscale + 1;                   // u64 [4]
+constexpr size_t kOffFlag = kOffStatus + 4;                     // int32 [2]: tile overflow flag
+constexpr size_t kScratchDoubles = kOffFlag + 1;
+
+static __device__ __align__(256) double g_scratch[kScratchDoubles];
+
+}  // namespace
+
+// error text for bx_last_error (defined with the other entry points)
+void bx_record_error(const char* msg);
+
+namespace {
+
+int na_fail(int code, const char* msg) {
+  bx_record_error(msg);
+  return code;
+}
+
+// set-up, once per device, with that device current: the device address of
+// the scratch array (its name in host code is only a host-side stand-in)
+double* scratch_address(int* rc) {
+  static double* addr[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    *rc = na_fail(BX_ECUDA, "bx_step_fp64_noalloc: no current CUDA device");
+    return nullptr;
+  }
+  if (!addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) {
+      *rc = na_fail(BX_ECUDA, "bx_step_fp64_noalloc: cudaGetSymbolAddress failed");
+      return nullptr;
+    }
+    addr[dev] = static_cast<double*>(p);
+  }
+  *rc = BX_OK;
+  return addr[dev];
+}
+
+// Rebuild the derived maps in the scratch: mem_to_cells, the partner's cell,
+// the fixed 16-cell tiling, the per-cluster constants; clear the counters and
+// raise the flag if a tile holds more than 256 membranes.
+__global__ void k_noalloc_prep(const int* __restrict__ ptr, const int* __restrict__ nn, int C, int M,
+                               double* scratch, double pump, double escale) {
+  int* m2c = reinterpret_cast<int*>(scratch + kOffM2c);
+  int* nn_cell = reinterpret_cast<int*>(scratch + kOffNnCell);
+  int* blk = reinterpret_cast<int*>(scratch + kOffBlk);
+  int* blk_cl = reinterpret_cast<int*>(scratch + kOffBlkCl);
+  int* cl_blk = reinterpret_cast<int*>(scratch + kOffClBlk);
+  int* flag = reinterpret_cast<int*>(scratch + kOffFlag);
+  const int ntile = (C + kTileCells - 1) / kTileCells;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  for (int c = tid; c < C; c += stride)
+    for (int m = ptr[c]; m < ptr[c + 1]; ++m) m2c[m] = c;
+  for (int b = tid; b <= ntile; b += stride) {
+    const int cb = min(b * kTileCells, C);
+    blk[b] = cb;
+    if (b < ntile) {
+      blk_cl[b] = 0;
+      const int ce = min(cb + kTileCells, C);
+      if (ptr[ce] - ptr[cb] > kTileThreads) atomicExch(flag, 1);
+    }
+  }
+  if (tid == 0) {
+    cl_blk[0] = 0;
+    cl_blk[1] = ntile;
+    scratch[kOffPump] = pump;
+    scratch[kOffEscale] = escale;
+    unsigned long long* st = reinterpret_cast<unsigned long long*>(scratch + kOffStatus);
+    st[0] = st[1] = st[2] = st[3] = 0ull;
+  }
+}
+
+__global__ void k_noalloc_nn_cell(const int* __restrict__ nn, int M, double* scratch) {
+  const int* m2c = reinterpret_cast<const int*>(scratch + kOffM2c);
+  int* nn_cell = reinterpret_cast<int*>(scratch + kOffNnCell);
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x)
+    nn_cell[m] = m2c[nn[m]];
+}
+
+__global__ void k_noalloc_clear_flag(double* scratch) {
+  reinterpret_cast<int*>(scratch + kOffFlag)[0] = 0;
+}
+
+int zc(double z) { return z == 1.0 ? 1 : z == -1.0 ? -1 : z == 2.0 ? 2 : z == -2.0 ? -2 : 0; }
+
+}  // namespace
+
+extern "C" int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
+                                    double* vm, double* vm_work, double* cc_cells, double* cc_mem,
+                                    double* cc_mem_work, double* cc_env, int n_steps, void* stream) {
+  if (!g || !p || !Dm || !vm || !vm_work || !cc_cells || !cc_mem || !cc_mem_work || !cc_env)
+    return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: null argument");
+  const int C = g->n_cells, M = g->n_mems, I = p->n_ions;
+  if (C <= 0 || M <= 0 || n_steps < 0) return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: bad sizes");
+  if (C > kMaxCells || M > kMaxMems)
+    return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: at most 16384 cells and 131072 membranes");
+  if (I <= 0 || I > BX_MAX_IONS || p->iNa < 0 || p->iNa >= I || p->iK < 0 || p->iK >= I)
+    return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: bad ion indices");
+  if (p->is_ecm) return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs is_ecm == 0");
+  if (!g->cell_mem_ptr || !g->nn_i || !g->bflag || !g->map_mem2ecm || !g->mem_sa || !g->gj_weight ||
+      !g->cell_vol || !g->diviterm)
+    return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: missing geometry array");
+  int rc = BX_OK;
+  double* scratch = scratch_address(&rc);
+  if (!scratch) return rc;
+  if (n_steps == 0) return BX_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int ntile = (C + kTileCells - 1) / kTileCells;
+  const double pump = -3.0 * p->nakatp_block * p->alpha_NaK;
+  const double escale = p->dt / (p->vol_env * (double)M);
+
+  k_noalloc_clear_flag<<<1, 1, 0, s>>>(scratch);
+  k_noalloc_prep<<<64, 256, 0, s>>>(g->cell_mem_ptr, g->nn_i, C, M, scratch, pump, escale);
+  k_noalloc_nn_cell<<<64, 256, 0, s>>>(g->nn_i, M, scratch);
+  int flag = 0;
+  if (cudaMemcpyAsync(&flag, scratch + kOffFlag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: set-up kernels failed");
+  if (flag) return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: 16 consecutive cells hold more than 256 membranes");
+
+  bx::DevGeom dg{};
+  dg.C = C; dg.M = M; dg.I = I; dg.G = g->grid_ny * g->grid_nx; dg.ny = g->grid_ny; dg.nx = g->grid_nx;
+  dg.cell_ptr = g->cell_mem_ptr;
+  dg.m2c = reinterpret_cast<const int*>(scratch + kOffM2c);
+  dg.nn = g->nn_i;
+  dg.nn_cell = reinterpret_cast<const int*>(scratch + kOffNnCell);
+  dg.bflag = g->bflag; dg.map_env = g->map_mem2ecm; dg.mem_sa = g->mem_sa; dg.gj_w = g->gj_weight;
+  dg.mem_nx = g->mem_nx; dg.mem_ny = g->mem_ny; dg.sw_mem = g->smooth_weight_mem; dg.sw_o = g->smooth_weight_o;
+  dg.cell_vol = g->cell_vol; dg.cell_sa = g->cell_sa; dg.diviterm = g->diviterm;
+  dg.blk_cell = reinterpret_cast<const int*>(scratch + kOffBlk);
+  dg.blk_cluster = reinterpret_cast<const int*>(scratch + kOffBlkCl);
+
+  bx::StepConst k{};
+  k.I = I; k.iNa = p->iNa; k.iK = p->iK;
+  const double RT = p->R * p->T;
+  for (int i = 0; i < I; ++i) {
+    k.z[i] = p->zs[i]; k.zcode[i] = zc(p->zs[i]); k.zF[i] = p->zs[i] * p->F;
+    k.sig_coef[i] = ((p->zs[i] * p->zs[i]) * (p->F * p->F) * p->D_free[i] * 0.1) / RT;
+    k.dgj_gs[i] = p->D_gj[i] * p->gj_surface;
+  }
+  k.F_RT = p->F / RT; k.dt = p->dt; k.inv_cm = 1.0 / p->cm; k.tm = p->tm; k.gj_len = g->gj_len;
+  k.gj_block = p->gj_block; k.inv_KmNa = 1.0 / p->KmNK_Na; k.inv_KmK = 1.0 / p->KmNK_K;
+  k.atp_term = p->cATP / p->KmNK_ATP; k.atp_den = 1.0 + p->cATP / p->KmNK_ATP;
+  k.qnum_c = (p->cADP * 1e-3) * (p->cPi * 1e-3); k.qden_c = p->cATP * 1e-3;
+  k.K0 = std::exp(-(p->deltaGATP / RT));
+
+  double* vbuf[2] = {vm, vm_work};
+  double* cbuf[2] = {cc_mem, cc_mem_work};
+  int par = 0;
+  for (int q = 0; q < n_steps; ++q) {
+    bx::StepPtrs sp{};
+    sp.vm_in = vbuf[par]; sp.vm_out = vbuf[par ^ 1];
+    sp.ccm_in = cbuf[par]; sp.ccm_out = cbuf[par ^ 1];
+    sp.cc = cc_cells; sp.Dm = Dm; sp.cenv = cc_env;
+    sp.pump_coef = scratch + kOffPump;
+    sp.phib = nullptr;
+    sp.env_part = scratch + kOffPart;
+    sp.status = reinterpret_cast<unsigned long long*>(scratch + kOffStatus);
+    if (bx::launch_cell_step<double, kTileThreads>(false, false, false, ntile, s, dg, sp, k) != cudaSuccess)
+      return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: step launch failed");
+    bx::k_env_mix<<<1, 256, 0, s>>>(scratch + kOffPart, reinterpret_cast<const int*>(scratch + kOffClBlk), I,
+                                    cc_env, scratch + kOffEscale);
+    par ^= 1;
+  }
+  if (par == 1) {   // the result sits in the work buffers: move it to the caller's primaries
+    if (cudaMemcpyAsync(vm, vm_work, (size_t)M * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(cc_mem, cc_mem_work, (size_t)I * C * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: copy-back failed");
+  }
+  if (cudaGetLastError() != cudaSuccess) return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: launch failed");
+  return BX_OK;
+}

@@ -228,6 +228,30 @@ int bx_time_cell_kernel(bx_handle h, int n, double* ms_per_launch);
  * counted once at its stored width; reads plus writes). */
 int64_t bx_cell_kernel_bytes(bx_handle h);
 
+/* No-allocation step.  No counterpart in the reference (BETSE has no device
+ * memory); it serves callers that cannot allocate GPU memory while they step,
+ * e.g. a host framework that owns every device buffer through its own pool,
+ * or a loop where cudaMalloc is forbidden.  It advances n_steps plain FP64
+ * steps of one cluster without ECM on the caller's device buffers and calls
+ * no cudaMalloc/cudaFree: its scratch is a fixed file-scope device array of
+ * about 1.1 MB, present on every GPU that loads the library until exit.
+ *   g      bx_geom whose array pointers are DEVICE pointers (cell_mem_ptr,
+ *          nn_i, bflag, map_mem2ecm, mem_sa, gj_weight, cell_vol, diviterm)
+ *   Dm     [n_ions * n_mems] device, read only
+ *   vm, cc_mem, cc_cells, cc_env   device state in BETSE layouts: vm [n_mems],
+ *          cc_mem [n_ions * n_cells] (cc_at_mem, one value per cell),
+ *          cc_cells [n_ions * n_cells], cc_env [n_ions] (well mixed); updated
+ *   vm_work [n_mems], cc_mem_work [n_ions * n_cells]   device work buffers
+ * Limits (BX_EINVAL beyond them): n_cells <= 16384, n_mems <= 131072, and at
+ * most 256 membranes in any 16 consecutive cells.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress).  Every call
+ * shares the array and leaves the last call's contents in it; calls that
+ * overlap on the GPU race on it, so serialise them.  Synchronises `stream`
+ * once per call to check the limits. */
+int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm, double* vm,
+                         double* vm_work, double* cc_cells, double* cc_mem, double* cc_mem_work,
+                         double* cc_env, int n_steps, void* stream);
+
 /* Autotuner: times n_steps steps for each supported CTA size (128 and 256
  * membrane slots) on the uploaded state, keeps the fastest, and restores the
  * state so the simulation does not advance.  Reports the choice and its
