@@ -51,6 +51,11 @@ WORKLOADS = {
     'plain250': dict(radius=80e-6, seed=1, is_ecm=False, dt=1e-2, dm=(1e-19, 1e-17),
                      time_steps=2000, grid_size=20,
                      desc='plain FP64 reference step, ~250 cells, no ECM, 2000 steps'),
+    'sweep512': dict(sweep=True, n_clusters=512, seed=7, dt=5e-3, dm=(1e-19, 1e-17),
+                     time_steps=1000,
+                     desc='batched sweep: 512 independent clusters, cells log-uniform [200,5000], '
+                          'per-cluster Na/K Dm and pump multipliers log-uniform [0.1,10], '
+                          'Dm log-uniform [1e-19,1e-17], dt 5e-3 s, 1000 steps per run, split step'),
 }
 
 
@@ -123,9 +128,42 @@ class ClockSampler:
 def build_workload(name):
     from betse_gb300 import generator as gen
     w = WORKLOADS[name]
+    if w.get('sweep'):
+        gs, ps, Dms, sts = gen.sweep_workload(w['n_clusters'], w['seed'], dt=w['dt'],
+                                              dm_range=w['dm'])
+        return w, gs, ps, Dms, sts, None
     g, p, Dm, st, D_env = gen.workload(w['radius'], w['seed'], is_ecm=w['is_ecm'], dt=w['dt'],
                                        dm_range=w['dm'], grid_size=w['grid_size'])
     return w, g, p, Dm, st, D_env
+
+
+class Sweep:
+    """Adapter giving a batch the single-cluster calls bench.py uses."""
+
+    def __init__(self, gs, ps, Dms, sts, precision):
+        from betse_gb300.engine import BatchEngine
+        self.e = BatchEngine(gs, ps, precision)
+        self.e.set_membrane_diffusivity(Dms)
+        self.sts = sts
+        self.e.upload_states(sts)
+        self.n_mems = self.e.M
+        self.n_cells = self.e.C
+
+    def __getattr__(self, k):
+        return getattr(self.e, k)
+
+    def upload(self, **_):
+        self.e.upload_states(self.sts)
+
+    def upload_pinned(self, pin_states):
+        self.e.upload_states(pin_states)
+
+    def download(self):
+        d = self.e.download_states()
+        return {'vm': np.concatenate([x['vm'] for x in d]),
+                'cc_cells': np.concatenate([x['cc_cells'] for x in d], axis=1),
+                'cc_at_mem': np.concatenate([x['cc_at_mem'] for x in d], axis=1),
+                'cc_env': np.concatenate([x['cc_env'] for x in d])}
 
 
 def cpu_baseline(g, p, Dm, st, budget_s=12.0):
@@ -171,6 +209,10 @@ def run_reference(args, rank, world):
         return
     w, g, p, Dm, st, _ = build_workload(args.workload)
     budget = float(os.environ.get('BX_REF_BUDGET_S', '6'))
+    n_cells, n_mems = (sum(x.n_cells for x in g), sum(x.n_mems for x in g)) if w.get('sweep') \
+        else (g.n_cells, g.n_mems)
+    if w.get('sweep'):      # a bounded sample of the sweep: its first cluster
+        g, p, Dm, st = g[0], p[0], Dm[0], st[0]
     samples = []
     for k in range(args.warmup + args.steps):
         r = cpu_baseline(g, p, Dm, st, budget_s=budget)
@@ -181,7 +223,7 @@ def run_reference(args, rank, world):
             'warmup': args.warmup, 'ms_per_step': 1e3 * g.n_mems / v,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
             'data': 'synthetic', 'impl': 'reference',
-            'config': {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems},
+            'config': {'workload': w['desc'], 'cells': n_cells, 'membranes': n_mems},
             'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': 1, 'kind': 'port',
                              'sample': r['sample']},
             'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
@@ -204,6 +246,8 @@ def main():
     if args.impl == 'reference':
         return run_reference(args, rank, world)
 
+    w, g, p, Dm, st, D_env = build_workload(args.workload)
+    sweep = bool(w.get('sweep'))
     import torch
     dist = None
     if world > 1:
@@ -216,7 +260,6 @@ def main():
     build()
     from betse_gb300.engine import ClusterEngine
 
-    w, g, p, Dm, st, D_env = build_workload(args.workload)
     T = args.time_steps or w['time_steps']
     dev = torch.device('cuda', torch.cuda.current_device())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -225,6 +268,8 @@ def main():
     torch.cuda.set_stream(stream)
 
     def make(prec):
+        if sweep:
+            return Sweep(g, p, Dm, st, prec)
         e = ClusterEngine(g, p, prec)
         e.set_membrane_diffusivity(Dm)
         e.upload(**st)
@@ -232,8 +277,10 @@ def main():
 
     split = make('split')
     plain = make('fp64')
+    n_mems = split.n_mems if sweep else g.n_mems
+    n_cells = split.n_cells if sweep else g.n_cells
     tune_split = split.autotune(20)
-    tune_plain = plain.autotune(5)
+    tune_plain = plain.autotune(3)
 
     def barrier():
         torch.cuda.synchronize()
@@ -263,46 +310,55 @@ def main():
     clocks.start()
     ms_split, launches = timed_runs(split, args.steps, args.warmup)
     clk = clocks.stop()
-    ms_plain, _ = timed_runs(plain, max(1, min(args.steps, 2)), 1)
+    ms_plain, _ = timed_runs(plain, 1, 1)
     split.check_stable()
     plain.check_stable()
 
-    tot_ms = sum(ms_split)
-    t_local = tot_ms / 1e3
+    t_local = sum(ms_split) / 1e3
     if dist is not None:
-        t = torch.tensor([t_local], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+        tt = torch.tensor([t_local], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
     else:
         t_max = t_local
-    units = g.n_mems * T * args.steps * world
-    value = units / t_max
-    plain_value = g.n_mems * T * len(ms_plain) / (sum(ms_plain) / 1e3)
+    value = n_mems * T * args.steps * world / t_max
+    plain_value = n_mems * T * len(ms_plain) / (sum(ms_plain) / 1e3)
 
-    # ---- error at equal step counts: fresh engines, same number of steps
+    # ---- Vmem error of the split form against the plain FP64 form, equal steps
     e_s, e_p = make('split'), make('fp64')
-    e_s.autotune(10)
     e_s.step(T)
     e_p.step(T)
     vm_err = float(np.max(np.abs(e_s.download()['vm'] - e_p.download()['vm'])))
+    e_p.close()
 
-    # ---- roofline of the dominant kernel (fused cell step), events on its stream
-    e_s.upload(**st)
+    # ---- roofline of the dominant kernel (the fused cell step), events on its stream
+    e_s.upload(**({} if sweep else st))
+    e_s.autotune(10)
     kern_ms = e_s.time_cell_kernel(50)
     kbytes = e_s.cell_kernel_bytes()
     hbm, src = peaks()
     achieved = kbytes / (kern_ms / 1e3) / 1e9
     traffic = None
-    tp = os.path.join(ROOT, 'profiles', 'cell_step_split_100k.traffic.json')
+    tp = os.path.join(ROOT, 'profiles', f'k_split_step_{args.workload}.traffic.json')
     if os.path.exists(tp):
         tj = json.load(open(tp))
-        traffic = int(tj['dram_bytes_per_launch'] * g.n_mems / tj['membranes'])
+        traffic = int(tj['dram_bytes_per_launch'] * n_mems / tj['membranes'])
 
     # ---- end to end through the C ABI with host buffers (pinned)
-    pin = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy()
-           for k, v in st.items()}
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    if sweep:
+        cat = {'vm': np.concatenate([s_['vm'] for s_ in st]),
+               'cc_cells': np.concatenate([s_['cc_cells'] for s_ in st], axis=1),
+               'cc_at_mem': np.concatenate([s_['cc_at_mem'] for s_ in st], axis=1),
+               'cc_env': np.stack([np.asarray(s_['cc_env']) for s_ in st])}
+        pin = {k: pinned(v) for k, v in cat.items()}
+        up = lambda: e_s.e.upload_concat(**pin)  # noqa: E731
+    else:
+        pin = {k: pinned(v) for k, v in st.items()}
+        up = lambda: e_s.upload(**pin)  # noqa: E731
     h2d = sum(v.nbytes for v in pin.values())
-    e_s.upload(**pin)
+    up()
     e_s.step(T)
     torch.cuda.synchronize()
     d2h = 0
@@ -311,18 +367,22 @@ def main():
         flush.fill_(1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        e_s.upload(**pin)
+        up()
         e_s.step(T)
-        out = e_s.download()
+        out = e_s.e.download_concat() if sweep else e_s.download()
         t1 = time.perf_counter()
         d2h = sum(v.nbytes for v in out.values())
         if k >= args.warmup:
             t_e2e.append(t1 - t0)
-    e2e_val = g.n_mems * T * len(t_e2e) * world / sum(t_e2e)
+    e2e_val = n_mems * T * len(t_e2e) * world / sum(t_e2e)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(g, p, Dm, st)
+        if sweep:
+            cpu = cpu_baseline(g[0], p[0], Dm[0], st[0])
+            cpu['sample'] += ' (cluster 0 of the sweep)'
+        else:
+            cpu = cpu_baseline(g, p, Dm, st)
 
     if rank == 0:
         line = {
@@ -330,7 +390,7 @@ def main():
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_max * 1e3 / args.steps,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f32 fluxes / f64 concentrations+Vmem', 'data': 'synthetic',
-            'config': {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems,
+            'config': {'workload': w['desc'], 'cells': n_cells, 'membranes': n_mems,
                        'time_steps_per_step': T, 'precision': 'split',
                        'l2': 'flushed (256 MiB write) before every timed run',
                        'parallelism': f'replicas x{world}',
@@ -341,7 +401,7 @@ def main():
                            'vm_max_abs_err_V': vm_err, 'vm_err_after_steps': T},
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
                          'frac': achieved / hbm, 'traffic': traffic,
-                         'kernel': 'k_cell_step<float> (fused membrane flux + cell update)',
+                         'kernel': 'k_split_step (fused membrane fluxes + cell update, split form)',
                          'algorithmic_bytes_per_launch': kbytes, 'launch_ms': kern_ms,
                          'peak_source': src},
             'cpu_baseline': cpu,
@@ -351,7 +411,7 @@ def main():
             'clocks': clk,
         }
         print(json.dumps(line), flush=True)
-    for e in (split, plain, e_s, e_p):
+    for e in (split, plain, e_s):
         e.close()
     if dist is not None:
         dist.destroy_process_group()

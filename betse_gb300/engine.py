@@ -211,6 +211,21 @@ class BatchEngine(ClusterEngine):
         st = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(cenv), None, None)
         _lib.check(self.lib.bx_state_upload(self.h, ct.byref(st)), 'bx_state_upload')
 
+    def upload_concat(self, vm, cc_cells, cc_at_mem, cc_env):
+        """Upload the concatenated state directly (cc_env is [n_clusters, n_ions]);
+        the arrays are passed to the C ABI as they are (e.g. pinned views)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (vm, cc_cells, cc_at_mem, cc_env)]
+        st = _lib.BxState(*[_lib.dptr(a) for a in arrs], None, None)
+        _lib.check(self.lib.bx_state_upload(self.h, ct.byref(st)), 'bx_state_upload')
+
+    def download_concat(self):
+        I = self.I
+        out = dict(vm=np.empty(self.M), cc_cells=np.empty((I, self.C)), cc_at_mem=np.empty((I, self.M)),
+                   cc_env=np.empty((self.n_clusters, I)))
+        st = _lib.BxState(*[_lib.dptr(out[k]) for k in ('vm', 'cc_cells', 'cc_at_mem', 'cc_env')], None, None)
+        _lib.check(self.lib.bx_state_download(self.h, ct.byref(st)), 'bx_state_download')
+        return out
+
     def download_states(self):
         I = self.I
         vm, cc, cam = np.empty(self.M), np.empty((I, self.C)), np.empty((I, self.M))

@@ -271,3 +271,41 @@ def workload(radius, seed, is_ecm=False, dt=1e-2, dm_range=(1e-19, 1e-17),
 
 def cell_conc_vec(cell):
     return np.array([cell[k] for k in ION_NAMES], np.float64)
+
+
+def _sweep_member(args):
+    k, n_cells, seed, na_k_mult, pump_mult, dt, dm_range = args
+    R = np.sqrt(n_cells / 0.0456) * 1e-6       # cells ~ 0.0456 (R / 1 um)^2 for this lattice
+    g, p, Dm, st, _ = workload(R, seed, dt=dt, dm_range=dm_range, na_k_dm_mult=na_k_mult,
+                               pump_mult=pump_mult)
+    return k, g, p, Dm, st
+
+
+def sweep_workload(n_clusters=512, seed=7, cells_range=(200, 5000), mult_range=(0.1, 10.0),
+                   dt=5e-3, dm_range=(1e-19, 1e-17), workers=None):
+    """A parameter sweep: ``n_clusters`` independent clusters with cell counts
+    log-uniform in ``cells_range`` and per-cluster Na/K diffusivity and pump
+    multipliers log-uniform in ``mult_range``. Clusters are generated in a
+    spawn-started process pool. Returns lists (geoms, params, Dms, states)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import os
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(cells_range[0]), np.log(cells_range[1])
+    counts = np.exp(rng.uniform(lo, hi, n_clusters))
+    ml, mh = np.log(mult_range[0]), np.log(mult_range[1])
+    dmm = np.exp(rng.uniform(ml, mh, n_clusters))
+    pmm = np.exp(rng.uniform(ml, mh, n_clusters))
+    jobs = [(k, float(counts[k]), seed * 1000 + k, float(dmm[k]), float(pmm[k]), dt, dm_range)
+            for k in range(n_clusters)]
+    workers = workers or min(16, os.cpu_count() or 1)
+    out = [None] * n_clusters
+    if workers > 1:
+        with cf.ProcessPoolExecutor(workers, mp_context=mp.get_context('spawn')) as ex:
+            for k, g, p, Dm, st in ex.map(_sweep_member, jobs, chunksize=8):
+                out[k] = (g, p, Dm, st)
+    else:
+        for j in jobs:
+            k, g, p, Dm, st = _sweep_member(j)
+            out[k] = (g, p, Dm, st)
+    return ([o[0] for o in out], [o[1] for o in out], [o[2] for o in out], [o[3] for o in out])
