@@ -230,6 +230,24 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def profile_run(args):
+    """A short, deterministic launch sequence for ncu captures."""
+    from betse_gb300.build import build
+    build()
+    w, g, p, Dm, st, _ = build_workload(args.workload)
+    if w.get('sweep'):
+        e = Sweep(g, p, Dm, st, args.precision)
+    else:
+        from betse_gb300.engine import ClusterEngine
+        e = ClusterEngine(g, p, args.precision)
+        e.set_membrane_diffusivity(Dm)
+        e.upload(**st)
+    e.step(4)
+    e.check_stable()
+    e.close()
+    print('profile run done:', args.workload, args.precision)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -239,8 +257,13 @@ def main():
     ap.add_argument('--workload', default='cluster100k', choices=sorted(WORKLOADS))
     ap.add_argument('--time-steps', type=int, default=None)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--profile-run', action='store_true',
+                    help='for ncu: build the workload, upload it, run 4 eager steps, exit')
+    ap.add_argument('--precision', default='split', choices=['split', 'fp64'])
     args = ap.parse_args()
     world = _env_int('WORLD_SIZE', 1)
+    if args.profile_run:
+        return profile_run(args)
     rank = _env_int('RANK', 0)
     local = _env_int('LOCAL_RANK', 0)
     if args.impl == 'reference':
