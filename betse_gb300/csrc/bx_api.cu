@@ -91,9 +91,19 @@ struct bx_cluster {
   float* d_Dm_f = nullptr;
   // ---- state: plain / split+ECM
   double *d_vm[2] = {nullptr, nullptr}, *d_ccm[2] = {nullptr, nullptr}, *d_cc = nullptr;
-  // ---- state: split
-  float2* s_cc2 = nullptr;
-  float* s_rec[2] = {nullptr, nullptr};   // [C][kRec]: membrane-side concentrations + Vmem
+  // ---- split form: tile-major slots (Q membrane slots, S cell slots)
+  int Q = 0, S = 0;
+  uint8_t* t_lcell = nullptr;
+  int *t_nn = nullptr, *t_map_env = nullptr, *t_nn_env = nullptr, *t_c0 = nullptr, *t_m0 = nullptr,
+      *t_slot_of_cell = nullptr;
+  float *t_sa = nullptr, *t_gw = nullptr, *t_dtv = nullptr, *t_dvc = nullptr;
+  short2* t_rng = nullptr;
+  std::vector<int> h_slot_of_cell, h_slot_of_mem;
+  std::vector<double> h_Dm, h_msa, h_gjw, h_vol, h_div;
+  std::vector<uint8_t> h_bflag;
+  std::vector<int> h_nn;
+  float2* s_cc2 = nullptr;                  // [I][S]
+  float* s_rec[2] = {nullptr, nullptr};     // [S][kRec]: membrane-side concentrations + Vmem
   float *s_cenv_f = nullptr, *s_pump = nullptr, *s_part = nullptr, *s_phib = nullptr;
   unsigned int* s_count = nullptr;
   // ---- environment
@@ -127,6 +137,8 @@ void free_all(bx_cluster* h) {
       h->d_ny, h->d_swm, h->d_swo, h->d_cell_vol, h->d_cell_sa, h->d_diviterm, h->d_mem_sa_f,
       h->d_gj_w_f, h->d_gjw0_f, h->d_dtv, h->d_dvc, h->d_Dm, h->d_Dm_f, h->d_vm[0], h->d_vm[1],
       h->d_ccm[0], h->d_ccm[1], h->d_cc, h->s_cc2, h->s_rec[0], h->s_rec[1], h->s_count,
+      h->t_lcell, h->t_nn, h->t_map_env, h->t_nn_env, h->t_c0, h->t_m0, h->t_slot_of_cell, h->t_sa,
+      h->t_gw, h->t_dtv, h->t_dvc, h->t_rng,
       h->s_cenv_f, h->s_pump, h->s_part, h->s_phib, h->d_cenv, h->d_phib, h->d_env_part,
       h->d_mem_flux_sa, h->d_pump, h->d_env_scale, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy,
       h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
@@ -262,11 +274,10 @@ bx::StepPtrs step_ptrs(bx_cluster* h, int parity) {
 
 bx::SplitGeom split_geom(const bx_cluster* h) {
   bx::SplitGeom g{};
-  g.C = h->C; g.M = h->M; g.I = h->I; g.G = h->G;
-  g.cell_ptr = h->d_cell_ptr; g.nn_cell = h->d_nn_cell; g.lcell = h->d_lcell;
-  g.mem_sa = h->d_mem_sa_f; g.gjw = h->d_gjw0_f; g.dtv = h->d_dtv; g.dvc = h->d_dvc;
-  g.blk_cell = h->d_blk; g.blk_cluster = h->d_blk_cl; g.cl_blk = h->d_cl_blk;
-  g.map_env = h->d_map_env; g.nn = h->d_nn;
+  g.C = h->C; g.M = h->M; g.I = h->I; g.G = h->G; g.Q = h->Q; g.S = h->S;
+  g.lcell = h->t_lcell; g.nn_slot = h->t_nn; g.mem_sa = h->t_sa; g.gjw = h->t_gw;
+  g.cell_rng = h->t_rng; g.dtv = h->t_dtv; g.dvc = h->t_dvc; g.blk_cluster = h->d_blk_cl;
+  g.tile_c0 = h->t_c0; g.tile_m0 = h->t_m0; g.map_env = h->t_map_env; g.nn_env = h->t_nn_env;
   return g;
 }
 
@@ -279,6 +290,15 @@ bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
   p.o_fmem = h->o_fmem; p.o_fgj = h->o_fgj; p.o_rate = h->o_rate; p.o_rho = h->o_rho;
   p.o_vmem = h->o_vmc;
   return p;
+}
+
+// BETSE's six-ion set compiled as constants (bx_split.cuh IonSet<1>)
+bool is_betse_six_ions(const bx_cluster* h) {
+  const double z6[6] = {1, 1, -1, 2, -1, -1};
+  if (h->I != 6 || h->par.iNa != 0 || h->par.iK != 1) return false;
+  for (int i = 0; i < 6; ++i)
+    if (h->par.zs[i] != z6[i]) return false;
+  return true;
 }
 
 inline int env_grid(int G) { return (G + kEnvTPB - 1) / kEnvTPB; }
@@ -302,7 +322,10 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), unsigned grid, unsigned block, cu
 
 template <int TPB, bool OUT, bool PHIB>
 cudaError_t launch_split_t(bx_cluster* h, int parity, cudaStream_t s) {
-  return launch_pdl(bx::k_split_step<TPB, kRec, OUT, PHIB>, (unsigned)h->nblk, TPB, s, split_geom(h),
+  if (is_betse_six_ions(h))
+    return launch_pdl(bx::k_split_step<TPB, kRec, 1, OUT, PHIB>, (unsigned)h->nblk, TPB, s, split_geom(h),
+                      split_ptrs(h, parity), make_split_const(h));
+  return launch_pdl(bx::k_split_step<TPB, kRec, 0, OUT, PHIB>, (unsigned)h->nblk, TPB, s, split_geom(h),
                     split_ptrs(h, parity), make_split_const(h));
 }
 
@@ -350,6 +373,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
                           h->d_mem_sa, h->d_nx, h->d_ny, h->d_swm, h->d_swo, h->d_cell_sa,
                           h->d_gj_w, h->d_bflag};
       bx::SplitOutPtrs op{h->o_fmem, h->o_fgj, h->s_rec[parity ^ 1], h->s_rec[parity], kRec, h->s_cc2,
+                          h->S, h->t_slot_of_cell,
                           h->phib_nonzero ? h->s_phib : nullptr, h->o_Jn, h->o_Imem, h->o_Jcx,
                           h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx, h->o_Ecy, h->o_Emc,
                           h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vm_mem};
@@ -417,16 +441,16 @@ int upload_param_arrays(bx_cluster* h) {
   BX_CU(h2d(h->d_env_scale, escale.data(), h->ncl));
   if (h->mode == MODE_SPLIT) {
     BX_CU(h2d(h->s_pump, pump_f.data(), h->ncl));
-    std::vector<double> vol(h->C), div(h->C);
-    BX_CU(cudaMemcpy(vol.data(), h->d_cell_vol, h->C * sizeof(double), cudaMemcpyDeviceToHost));
-    BX_CU(cudaMemcpy(div.data(), h->d_diviterm, h->C * sizeof(double), cudaMemcpyDeviceToHost));
-    std::vector<float> dtv(h->C), dvc(h->C);
-    for (int c = 0; c < h->C; ++c) {
-      dtv[c] = (float)(h->par.dt / vol[c]);
-      dvc[c] = (float)(div[c] / h->par.cm);
+    if (h->t_dtv) {
+      std::vector<float> dtv(h->S, 0.f), dvc(h->S, 0.f);
+      for (int c = 0; c < h->C; ++c) {
+        const int s = h->h_slot_of_cell[c];
+        dtv[s] = (float)(h->par.dt / h->h_vol[c]);
+        dvc[s] = (float)(h->h_div[c] / h->par.cm);
+      }
+      BX_CU(h2d(h->t_dtv, dtv.data(), h->S));
+      BX_CU(h2d(h->t_dvc, dvc.data(), h->S));
     }
-    BX_CU(h2d(h->d_dtv, dtv.data(), h->C));
-    BX_CU(h2d(h->d_dvc, dvc.data(), h->C));
   }
   return BX_OK;
 }
@@ -472,6 +496,82 @@ int check_geom(const bx_geom* g, const bx_params* p) {
   return BX_OK;
 }
 
+// Tile-major slot layout of the split form for the partition `blk`: tile b
+// owns membrane slots [b*tpb, (b+1)*tpb) and cell slots [32b, 32b+32).
+// Geometry and Dm are re-laid out; the state buffers are reallocated and
+// must be uploaded again.
+int build_split_layout(bx_cluster* h, const std::vector<int>& blk) {
+  const int nblk = h->nblk, tpb = h->tpb, C = h->C, M = h->M, I = h->I;
+  const int Q = tpb * nblk, S = bx::kCellsPerCta * nblk;
+  const std::vector<int>& ptr = h->h_cell_ptr;
+  std::vector<uint8_t> lcell(Q, 255);
+  std::vector<int> nn_slot(Q), map_env(Q, 0), nn_env(Q, 0), t_c0(nblk), t_m0(nblk);
+  std::vector<float> sa(Q, 0.f), gw(Q, 0.f);
+  std::vector<short2> rng(S, make_short2(0, 0));
+  h->h_slot_of_cell.assign(C, 0);
+  h->h_slot_of_mem.assign(M, 0);
+  for (int b = 0; b < nblk; ++b) {
+    const int c0 = blk[b], c1 = blk[b + 1], m0 = ptr[c0];
+    t_c0[b] = c0;
+    t_m0[b] = m0;
+    for (int qq = tpb * b; qq < tpb * (b + 1); ++qq) nn_slot[qq] = bx::kCellsPerCta * b;
+    for (int c = c0; c < c1; ++c) {
+      const int s = bx::kCellsPerCta * b + (c - c0);
+      h->h_slot_of_cell[c] = s;
+      rng[s] = make_short2((short)(ptr[c] - m0), (short)(ptr[c + 1] - m0));
+      for (int m = ptr[c]; m < ptr[c + 1]; ++m) {
+        const int qq = tpb * b + (m - m0);
+        h->h_slot_of_mem[m] = qq;
+        lcell[qq] = (uint8_t)(c - c0);
+        sa[qq] = (float)h->h_msa[m];
+        gw[qq] = h->h_bflag[m] ? 0.f : (float)h->h_gjw[m];
+        map_env[qq] = h->h_map_env[m];
+      }
+    }
+  }
+  for (int m = 0; m < M; ++m) {
+    const int qq = h->h_slot_of_mem[m];
+    nn_slot[qq] = h->h_slot_of_cell[h->h_m2c[h->h_nn[m]]];
+    nn_env[qq] = h->h_map_env[h->h_nn[m]];
+  }
+  void* old[] = {h->t_lcell, h->t_nn, h->t_map_env, h->t_nn_env, h->t_c0, h->t_m0, h->t_slot_of_cell,
+                 h->t_sa, h->t_gw, h->t_dtv, h->t_dvc, h->t_rng, h->d_Dm_f, h->s_cc2, h->s_rec[0], h->s_rec[1]};
+  for (void* q : old)
+    if (q) cudaFree(q);
+  h->t_lcell = nullptr; h->t_nn = h->t_map_env = h->t_nn_env = h->t_c0 = h->t_m0 = h->t_slot_of_cell = nullptr;
+  h->t_sa = h->t_gw = h->t_dtv = h->t_dvc = nullptr; h->t_rng = nullptr; h->d_Dm_f = nullptr;
+  h->s_cc2 = nullptr; h->s_rec[0] = h->s_rec[1] = nullptr;
+  h->Q = Q;
+  h->S = S;
+  BX_CU(dalloc(&h->t_lcell, Q)); BX_CU(h2d(h->t_lcell, lcell.data(), Q));
+  BX_CU(dalloc(&h->t_nn, Q)); BX_CU(h2d(h->t_nn, nn_slot.data(), Q));
+  BX_CU(dalloc(&h->t_map_env, Q)); BX_CU(h2d(h->t_map_env, map_env.data(), Q));
+  BX_CU(dalloc(&h->t_nn_env, Q)); BX_CU(h2d(h->t_nn_env, nn_env.data(), Q));
+  BX_CU(dalloc(&h->t_c0, nblk)); BX_CU(h2d(h->t_c0, t_c0.data(), nblk));
+  BX_CU(dalloc(&h->t_m0, nblk)); BX_CU(h2d(h->t_m0, t_m0.data(), nblk));
+  BX_CU(dalloc(&h->t_slot_of_cell, C)); BX_CU(h2d(h->t_slot_of_cell, h->h_slot_of_cell.data(), C));
+  BX_CU(dalloc(&h->t_sa, Q)); BX_CU(h2d(h->t_sa, sa.data(), Q));
+  BX_CU(dalloc(&h->t_gw, Q)); BX_CU(h2d(h->t_gw, gw.data(), Q));
+  BX_CU(dalloc(&h->t_rng, S)); BX_CU(h2d(h->t_rng, rng.data(), S));
+  BX_CU(dalloc(&h->t_dtv, S)); BX_CU(dalloc(&h->t_dvc, S));
+  BX_CU(dalloc(&h->d_Dm_f, (size_t)I * Q));
+  BX_CU(cudaMemset(h->d_Dm_f, 0, (size_t)I * Q * sizeof(float)));
+  if (!h->h_Dm.empty()) {
+    std::vector<float> f((size_t)I * Q, 0.f);
+    for (int i = 0; i < I; ++i)
+      for (int m = 0; m < M; ++m) f[(size_t)i * Q + h->h_slot_of_mem[m]] = (float)h->h_Dm[(size_t)i * M + m];
+    BX_CU(h2d(h->d_Dm_f, f.data(), f.size()));
+  }
+  BX_CU(dalloc(&h->s_cc2, (size_t)I * S));
+  BX_CU(cudaMemset(h->s_cc2, 0, (size_t)I * S * sizeof(float2)));
+  BX_CU(dalloc(&h->s_rec[0], (size_t)kRec * S));
+  BX_CU(dalloc(&h->s_rec[1], (size_t)kRec * S));
+  BX_CU(cudaMemset(h->s_rec[0], 0, (size_t)kRec * S * sizeof(float)));
+  BX_CU(cudaMemset(h->s_rec[1], 0, (size_t)kRec * S * sizeof(float)));
+  h->have_state = false;
+  return upload_param_arrays(h);
+}
+
 // CTA partition for `tpb` membrane slots: runs of whole cells of one cluster
 // with at most tpb membranes; the split form also caps a tile at 32 cells
 // (its (ion, cell) phase maps ion -> warp, cell -> lane).  Rebuilt by the
@@ -501,10 +601,6 @@ int build_partition(bx_cluster* h, int tpb) {
     cl_blk[cl + 1] = (int)blk.size() - 1;
   }
   const int nblk = (int)blk.size() - 1;
-  std::vector<uint8_t> lcell(h->M);
-  for (int b = 0; b < nblk; ++b)
-    for (int c = blk[b]; c < blk[b + 1]; ++c)
-      for (int m = ptr[c]; m < ptr[c + 1]; ++m) lcell[m] = (uint8_t)(c - blk[b]);
   BX_CU(cudaStreamSynchronize(h->stream));
   void* old[] = {h->d_blk, h->d_blk_cl, h->d_cl_blk, h->d_lcell, h->s_part, h->d_env_part};
   for (void* q : old)
@@ -520,8 +616,6 @@ int build_partition(bx_cluster* h, int tpb) {
   BX_CU(dalloc(&h->d_cl_blk, cl_blk.size()));
   BX_CU(h2d(h->d_cl_blk, cl_blk.data(), cl_blk.size()));
   if (h->mode == MODE_SPLIT) {
-    BX_CU(dalloc(&h->d_lcell, h->M));
-    BX_CU(h2d(h->d_lcell, lcell.data(), lcell.size()));
     BX_CU(dalloc(&h->s_part, (size_t)nblk * h->I));
   } else {
     BX_CU(dalloc(&h->d_env_part, (size_t)nblk * h->I));
@@ -530,6 +624,7 @@ int build_partition(bx_cluster* h, int tpb) {
   h->nblk = nblk;
   h->tpb = tpb;
   h->graph_valid = false;
+  if (h->mode == MODE_SPLIT) return build_split_layout(h, blk);
   return BX_OK;
 }
 
@@ -650,14 +745,8 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
       cudaMemset(h->d_phib, 0, (size_t)G * sizeof(double)) != cudaSuccess)
     return bail(BX_ECUDA, "cudaMemset");
   if (h->mode == MODE_SPLIT) {
-    std::vector<float> fsa(M), gw0(M);
-    for (int m = 0; m < M; ++m) { fsa[m] = (float)msa[m]; gw0[m] = bflag[m] ? 0.0f : (float)gjw[m]; }
-    ALLOC(h->d_mem_sa_f, M); H2D(h->d_mem_sa_f, fsa.data(), M);
-    ALLOC(h->d_gjw0_f, M); H2D(h->d_gjw0_f, gw0.data(), M);
-    ALLOC(h->d_dtv, C); ALLOC(h->d_dvc, C);
-    ALLOC(h->d_Dm_f, (size_t)I * M);
-    ALLOC(h->s_cc2, (size_t)I * C);
-    ALLOC(h->s_rec[0], (size_t)kRec * C); ALLOC(h->s_rec[1], (size_t)kRec * C);
+    // host copies for the tile-major relayout (build_split_layout)
+    h->h_msa = msa; h->h_gjw = gjw; h->h_bflag = bflag; h->h_nn = nn; h->h_vol = vol; h->h_div = div;
     ALLOC(h->s_cenv_f, (size_t)ncl * I); ALLOC(h->d_cenv, (size_t)ncl * I);
     ALLOC(h->s_pump, ncl);
     ALLOC(h->s_phib, G);
@@ -762,7 +851,13 @@ int bx_set_membrane_diffusivity(bx_handle h, const double* Dm) {
   for (size_t q = 0; q < n; ++q)
     if (!(Dm[q] >= 0.0) || Dm[q] == INFINITY) return fail(BX_EINVAL, "Dm must be finite and >= 0");
   BX_CU(cudaStreamSynchronize(h->stream));
-  if (h->d_Dm_f) {
+  if (h->mode == MODE_SPLIT) {
+    h->h_Dm.assign(Dm, Dm + n);
+    std::vector<float> f((size_t)h->I * h->Q, 0.f);
+    for (int i = 0; i < h->I; ++i)
+      for (int m = 0; m < h->M; ++m) f[(size_t)i * h->Q + h->h_slot_of_mem[m]] = (float)Dm[(size_t)i * h->M + m];
+    BX_CU(cudaMemcpy(h->d_Dm_f, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+  } else if (h->d_Dm_f) {
     std::vector<float> f(n);
     for (size_t q = 0; q < n; ++q) f[q] = (float)Dm[q];
     BX_CU(cudaMemcpy(h->d_Dm_f, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
@@ -822,8 +917,9 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
   if (h->mode == MODE_SPLIT) {
     // Vmem is constant per cell (minus Phi_b per membrane) in BETSE's full
     // solver with cell_polarizability == 0 (sim.py:2027-2029)
-    std::vector<float> rec((size_t)kRec * C, 0.0f);
-    std::vector<float2> cc2((size_t)I * C);
+    const int S = h->S;
+    std::vector<float> rec((size_t)kRec * S, 0.0f);
+    std::vector<float2> cc2((size_t)I * S, make_float2(0.f, 0.f));
     for (int c = 0; c < C; ++c) {
       const double v0 = s->vm[ptr[c]] + h->h_phib[h->h_map_env[ptr[c]]];
       for (int m = ptr[c] + 1; m < ptr[c + 1]; ++m) {
@@ -831,13 +927,14 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
         if (std::fabs(v - v0) > 1e-12 * std::fabs(v0) + 1e-18)
           return fail(BX_EINVAL, "split form: vm must be uniform over each cell's membranes");
       }
-      rec[(size_t)c * kRec + kRec - 1] = (float)v0;
-      for (int i = 0; i < I; ++i) rec[(size_t)c * kRec + i] = (float)ccm[(size_t)i * C + c];
-    }
-    for (size_t q = 0; q < (size_t)I * C; ++q) {
-      const double x = s->cc_cells[q];
-      const float hi = (float)x;
-      cc2[q] = make_float2(hi, (float)(x - (double)hi));
+      const int sc = h->h_slot_of_cell[c];
+      rec[(size_t)sc * kRec + kRec - 1] = (float)v0;
+      for (int i = 0; i < I; ++i) {
+        rec[(size_t)sc * kRec + i] = (float)ccm[(size_t)i * C + c];
+        const double x = s->cc_cells[(size_t)i * C + c];
+        const float hi = (float)x;
+        cc2[(size_t)i * S + sc] = make_float2(hi, (float)(x - (double)hi));
+      }
     }
     std::vector<float> cef(nenv);
     for (size_t q = 0; q < nenv; ++q) cef[q] = (float)s->cc_env[q];
@@ -868,17 +965,25 @@ int bx_state_download(bx_handle h, bx_state* s) {
   const size_t nenv = h->ecm ? (size_t)I * h->G : (size_t)h->ncl * I;
   std::vector<double> ccm((size_t)I * C);
   if (h->mode == MODE_SPLIT) {
-    std::vector<float> rec((size_t)kRec * C);
-    std::vector<float2> cc2((size_t)I * C);
+    const int S = h->S;
+    std::vector<float> rec((size_t)kRec * S);
+    std::vector<float2> cc2((size_t)I * S);
     BX_CU(cudaMemcpy(rec.data(), h->s_rec[h->parity], rec.size() * sizeof(float), cudaMemcpyDeviceToHost));
     BX_CU(cudaMemcpy(cc2.data(), h->s_cc2, cc2.size() * sizeof(float2), cudaMemcpyDeviceToHost));
     if (s->vm)
       for (int m = 0; m < M; ++m)
-        s->vm[m] = (double)rec[(size_t)h->h_m2c[m] * kRec + kRec - 1] - h->h_phib[h->h_map_env[m]];
-    if (s->cc_cells)
-      for (size_t q = 0; q < cc2.size(); ++q) s->cc_cells[q] = (double)cc2[q].x + (double)cc2[q].y;
-    for (int i = 0; i < I; ++i)
-      for (int c = 0; c < C; ++c) ccm[(size_t)i * C + c] = (double)rec[(size_t)c * kRec + i];
+        s->vm[m] = (double)rec[(size_t)h->h_slot_of_cell[h->h_m2c[m]] * kRec + kRec - 1] -
+                   h->h_phib[h->h_map_env[m]];
+    for (int c = 0; c < C; ++c) {
+      const int sc = h->h_slot_of_cell[c];
+      for (int i = 0; i < I; ++i) {
+        if (s->cc_cells) {
+          const float2 x = cc2[(size_t)i * S + sc];
+          s->cc_cells[(size_t)i * C + c] = (double)x.x + (double)x.y;
+        }
+        ccm[(size_t)i * C + c] = (double)rec[(size_t)sc * kRec + i];
+      }
+    }
   } else {
     if (s->vm) BX_CU(cudaMemcpy(s->vm, h->d_vm[h->parity], (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
     if (s->cc_cells)
@@ -1038,10 +1143,10 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
   if (!h) return -1;
   const int64_t M = h->M, C = h->C, I = h->I, B = h->nblk;
   if (h->mode == MODE_SPLIT) {
-    // membrane: Dm (4I), nn_cell 4, lcell 1, mem_sa 4, gjw 4
-    // cell: cc2 in+out 16I, record in+out 2*4*kRec, dt/vol 4, diviterm/cm 4, ptr 4
-    // CTA: partial sums 4I, partition and cluster id 12
-    return M * (4 * I + 13) + C * (16 * I + 8 * kRec + 12) + B * (4 * I + 12);
+    // membrane: Dm (4I), nn_slot 4, lcell 1, mem_sa 4, gjw 4
+    // cell: cc2 in+out 16I, record in+out 2*4*kRec, dt/vol 4, diviterm/cm 4, range 4
+    // tile: partial sums 4I, cluster id 4
+    return M * (4 * I + 13) + C * (16 * I + 8 * kRec + 12) + B * (4 * I + 4);
   }
   const int64_t w = (h->mode == MODE_SPLIT_ECM) ? 4 : 8;  // Dm, mem_sa, gj_w width
   // membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env and the f*sa
@@ -1054,30 +1159,21 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
 int64_t bx_launch_count(bx_handle h) { return h ? h->launches : -1; }
 
 // Autotuner: time `n_steps` eager steps for each CTA size, keep the fastest.
-// The state is saved before the trials and restored after, so tuning does not
-// advance the simulation.
+// The state is downloaded before the trials and uploaded again after each
+// one (the split form's tile-major layout changes with the CTA size), so
+// tuning does not advance the simulation.
 int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out) {
   if (!h || n_steps <= 0) return fail(BX_EINVAL, "bad arguments");
   if (!h->have_state || !h->have_dm) return fail(BX_ESTATE, "upload state and Dm first");
-  BX_CU(cudaStreamSynchronize(h->stream));
-  struct Buf { void* p; size_t bytes; std::vector<char> save; };
   const size_t C = h->C, I = h->I, M = h->M;
   const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
-  std::vector<Buf> bufs;
-  if (h->mode == MODE_SPLIT) {
-    bufs = {{h->s_rec[h->parity], C * kRec * 4, {}}, {h->s_cc2, C * I * 8, {}},
-            {h->d_cenv, nenv * 8, {}}, {h->s_cenv_f, nenv * 4, {}}};
-  } else {
-    bufs = {{h->d_vm[h->parity], M * 8, {}}, {h->d_ccm[h->parity], C * I * 8, {}}, {h->d_cc, C * I * 8, {}},
-            {h->d_cenv, nenv * 8, {}}};
-    if (h->ecm) { bufs.push_back({h->d_Ex, (size_t)h->G * 8, {}}); bufs.push_back({h->d_Ey, (size_t)h->G * 8, {}}); }
-  }
-  bufs.push_back({h->d_status, 4 * sizeof(unsigned long long), {}});
-  for (Buf& b : bufs) {
-    b.save.resize(b.bytes);
-    BX_CU(cudaMemcpy(b.save.data(), b.p, b.bytes, cudaMemcpyDeviceToHost));
-  }
-  const int parity0 = h->parity;
+  std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1);
+  bx_state sv{vm.data(), cc.data(), cam.data(), cenv.data(), h->ecm ? ex.data() : nullptr,
+              h->ecm ? ey.data() : nullptr};
+  int rc = bx_state_download(h, &sv);
+  if (rc != BX_OK) return rc;
+  unsigned long long status[4];
+  BX_CU(cudaMemcpy(status, h->d_status, sizeof(status), cudaMemcpyDeviceToHost));
   const int64_t launches0 = h->launches;
   const int cands[2] = {256, (h->mode == MODE_SPLIT) ? 192 : 128};
   double best = 1e300;
@@ -1087,7 +1183,7 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   BX_CU(cudaEventCreate(&e1));
   for (int tpb : cands) {
     if (build_partition(h, tpb) != BX_OK) continue;
-    h->parity = parity0;
+    if ((rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
     for (int w = 0; w < 2; ++w) { enqueue_step(h, h->parity, false, h->stream); h->parity ^= 1; }
     BX_CU(cudaEventRecord(e0, h->stream));
     for (int q = 0; q < n_steps; ++q) { enqueue_step(h, h->parity, false, h->stream); h->parity ^= 1; }
@@ -1097,16 +1193,13 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
     BX_CU(cudaEventElapsedTime(&ms, e0, e1));
     const double per = ms / n_steps;
     if (per < best) { best = per; best_tpb = tpb; }
-    // restore the state for the next candidate / the caller
-    h->parity = parity0;
-    for (Buf& b : bufs) BX_CU(cudaMemcpy(b.p, b.save.data(), b.bytes, cudaMemcpyHostToDevice));
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  int rc = build_partition(h, best_tpb);
-  if (rc != BX_OK) return rc;
+  if ((rc = build_partition(h, best_tpb)) != BX_OK) return rc;
+  if ((rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
+  BX_CU(cudaMemcpy(h->d_status, status, sizeof(status), cudaMemcpyHostToDevice));
   h->launches = launches0;
-  h->parity = parity0;
   if (tpb_out) *tpb_out = best_tpb;
   if (ms_per_step_out) *ms_per_step_out = best;
   return BX_OK;

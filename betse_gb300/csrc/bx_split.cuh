@@ -74,20 +74,27 @@ __device__ __forceinline__ float ghk_flux_f(const GhkShared<float>& s, int zcode
   }
 }
 
+// Tile-major layout of the split form.  Tile b (a run of at most 32 whole
+// cells of one cluster holding at most TPB membranes) owns membrane slots
+// [b*TPB, (b+1)*TPB) and cell slots [32b, 32b+32); unused slots are padding.
+// Every address a CTA needs follows from blockIdx, so the loads of a step
+// form two independent waves: geometry before the grid dependency wait, and
+// all state (own record, partner record, concentrations) right after it.
 struct SplitGeom {
   int C, M, I, G;
-  const int* __restrict__ cell_ptr;      // [C+1]
-  const int* __restrict__ nn_cell;       // [M]
-  const uint8_t* __restrict__ lcell;     // [M]
-  const float* __restrict__ mem_sa;      // [M]
-  const float* __restrict__ gjw;         // [M]  (0 on boundary membranes)
-  const float* __restrict__ dtv;         // [C]  dt / cell_vol
-  const float* __restrict__ dvc;         // [C]  diviterm / cm
-  const int* __restrict__ blk_cell;      // [nblk+1]
-  const int* __restrict__ blk_cluster;   // [nblk]
-  const int* __restrict__ cl_blk;        // [ncl+1] CTA range of each cluster
-  const int* __restrict__ map_env;       // [M]  (PHIB only)
-  const int* __restrict__ nn;            // [M]  (PHIB only)
+  int Q, S;                                // membrane slots (TPB*nblk), cell slots (32*nblk)
+  const uint8_t* __restrict__ lcell;       // [Q] cell of the slot within its tile, 255 = padding
+  const int* __restrict__ nn_slot;         // [Q] cell slot of the gap-junction partner
+  const float* __restrict__ mem_sa;        // [Q]
+  const float* __restrict__ gjw;           // [Q] (0 on boundary membranes and padding)
+  const short2* __restrict__ cell_rng;     // [S] local membrane range [x, y) of the cell slot
+  const float* __restrict__ dtv;           // [S] dt / cell_vol
+  const float* __restrict__ dvc;           // [S] diviterm / cm
+  const int* __restrict__ blk_cluster;     // [nblk]
+  const int* __restrict__ tile_c0;         // [nblk] first cell (natural order) of the tile
+  const int* __restrict__ tile_m0;         // [nblk] first membrane (natural order) of the tile
+  const int* __restrict__ map_env;         // [Q]  (PHIB only)
+  const int* __restrict__ nn_env;          // [Q]  map_mem2ecm of the partner membrane (PHIB only)
 };
 
 struct SplitConst {
@@ -104,18 +111,17 @@ struct SplitConst {
 
 // Per-cell record, REC floats, 16-byte aligned: slots [0, I) hold the
 // membrane-side concentration of each ion (BETSE's cc_at_mem), slot REC-1
-// the cell's Vmem.  A membrane reads its own and its partner's record with
-// REC/4 vector loads.
+// the cell's Vmem.
 struct SplitPtrs {
-  const float* __restrict__ rec_in; float* __restrict__ rec_out;   // [C][REC]
-  float2* __restrict__ cc2;                // [I][C]
-  const float* __restrict__ Dm;            // [I][M]
+  const float* __restrict__ rec_in; float* __restrict__ rec_out;   // [S][REC]
+  float2* __restrict__ cc2;                // [I][S]
+  const float* __restrict__ Dm;            // [I][Q]
   const float* __restrict__ cenv_f;        // [ncl][I] FP32 copy of the environment
   const float* __restrict__ pump_coef;     // [ncl] -3 block alpha_NaK (0 = pump off)
   const float* __restrict__ phib;          // [G] (PHIB)
-  float* __restrict__ env_part;            // [nblk][I] per-CTA partial sums
+  float* __restrict__ env_part;            // [nblk][I] per-tile partial sums
   unsigned long long* status;              // nan_vm, nan_conc, neg clamps
-  // outputs (OUT)
+  // outputs (OUT), natural order
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_vmem;
 };
 
@@ -134,82 +140,100 @@ __device__ __forceinline__ void load_rec(const float* __restrict__ rec, int c, f
 // them above 1e-24.
 __device__ __forceinline__ float rcp_fast(float x) { return __fdividef(1.f, x); }
 
-constexpr int kCellsPerCta = 32;   // cells per CTA tile: (ion, cell) phase maps ion -> warp, cell -> lane
+constexpr int kCellsPerCta = 32;   // cells per tile: the (ion, cell) phase maps ion -> warp, cell -> lane
 
-// One time step of the split form for one CTA tile of at most 32 whole cells
-// (and at most TPB membranes).  Phases:
-//   prologue  read-only geometry, Dm                 (overlaps the previous step)
+// Charge patterns compiled as constants.  ZP = 0: any ion set, charges read
+// at run time.  ZP = 1: BETSE's six-ion set (ion profiles 'mammal' and
+// 'amphibian': Na, K, Cl, Ca, P, M with z = +1, +1, -1, +2, -1, -1; Na row 0,
+// K row 1).
+template <int ZP> struct IonSet {
+  static constexpr int NI = kMaxIons;
+  __device__ static int zc(const SplitConst& k, int i) { return k.zcode[i]; }
+  __device__ static int n(const SplitConst& k) { return k.I; }
+  __device__ static int iNa(const SplitConst& k) { return k.iNa; }
+  __device__ static int iK(const SplitConst& k) { return k.iK; }
+};
+template <> struct IonSet<1> {
+  static constexpr int NI = 6;
+  __device__ static constexpr int zc(const SplitConst&, int i) {
+    return i == 0 ? 1 : i == 1 ? 1 : i == 2 ? -1 : i == 3 ? 2 : -1;
+  }
+  __device__ static constexpr int n(const SplitConst&) { return 6; }
+  __device__ static constexpr int iNa(const SplitConst&) { return 0; }
+  __device__ static constexpr int iK(const SplitConst&) { return 1; }
+};
+
+// One time step of the split form for one tile.
+//   prologue  geometry and Dm of the tile's slots (overlaps the previous kernel)
 //   wait      cudaGridDependencySynchronize
+//   loads     own record, partner record, cc2, environment -- one wave
 //   membranes GHK + pump + gap-junction fluxes (FP32), per-ion f*sa into smem
 //   cells     warp i = ion i, lane = cell: update_all_concs in double-float
 //   charge    warp 0: rho = sum_i z_i F c_i (double-float) -> Vmem record
-template <int TPB, int REC, bool OUT, bool PHIB>
+template <int TPB, int REC, int ZP, bool OUT, bool PHIB>
 __global__ void __launch_bounds__(TPB, 2048 / TPB / 2)
 k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
-  __shared__ float sA[kMaxIons][TPB];
-  __shared__ float sB[kMaxIons][TPB];
-  __shared__ float red[kMaxIons][TPB / 32];
+  using IS = IonSet<ZP>;
+  constexpr int NI = IS::NI;
+  __shared__ float sA[NI][TPB];
+  __shared__ float sB[NI][TPB];
+  __shared__ float red[NI][TPB / 32];
   __shared__ float sRec[kCellsPerCta][REC];
-  __shared__ float2 sQ[kMaxIons][kCellsPerCta];
-  const int I = k.I;
+  __shared__ float2 sQ[NI][kCellsPerCta];
+  const int I = IS::n(k);
   const int b = blockIdx.x;
   const int t = threadIdx.x;
   const int lane = t & 31, wid = t >> 5;
+  const int q = b * TPB + t;                 // membrane slot
+  const int s0 = b * kCellsPerCta;           // first cell slot of the tile
 
-  // ---- prologue: read-only geometry and channel data.  With programmatic
-  // dependent launch this overlaps the previous kernel; the next kernel may
-  // be scheduled as soon as every CTA of this one is resident.
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
   cudaTriggerProgrammaticLaunchCompletion();
 #endif
-  const int c0 = g.blk_cell[b], c1 = g.blk_cell[b + 1];
-  const int cl = g.blk_cluster[b];
-  const int m0 = g.cell_ptr[c0], m1 = g.cell_ptr[c1];
-  const int ncell = c1 - c0;
-  const int m = m0 + t;
-  const bool active = m < m1;
-  int c = 0, cn = 0;
+  // ---- prologue: geometry and channel data (read-only during stepping)
+  const int lc = g.lcell[q];
+  const bool active = lc != 255;                // padding slots load nothing more
+  int cn = s0;
   float sa = 0.f, gw = 0.f;
-  float dmv[kMaxIons];
+  float dmv[NI];
 #pragma unroll
-  for (int i = 0; i < kMaxIons; ++i) dmv[i] = 0.f;
+  for (int i = 0; i < NI; ++i) dmv[i] = 0.f;
   if (active) {
-    c = c0 + g.lcell[m];
-    cn = g.nn_cell[m];
-    sa = g.mem_sa[m];
-    gw = g.gjw[m] * k.gj_block;
+    cn = g.nn_slot[q];
+    sa = g.mem_sa[q];
+    gw = g.gjw[q] * k.gj_block;
 #pragma unroll
-    for (int i = 0; i < kMaxIons; ++i)
-      if (i < I) dmv[i] = p.Dm[(size_t)i * g.M + m];
+    for (int i = 0; i < NI; ++i)
+      if (i < I) dmv[i] = p.Dm[(size_t)i * g.Q + q];
   }
-  // (ion, cell) operands: warp wid handles ion wid, lane handles cell c0+lane
-  const bool cell_thr = (wid < I) && (lane < ncell);
-  int a0 = 0, a1 = 0;
-  float dtv = 0.f, dvc = 0.f;
-  if (cell_thr) {
-    a0 = g.cell_ptr[c0 + lane] - m0;
-    a1 = g.cell_ptr[c0 + lane + 1] - m0;
-    dtv = g.dtv[c0 + lane];
-  }
-  if (t < ncell) dvc = g.dvc[c0 + t];
+  const int cl = g.blk_cluster[b];
+  const bool cell_thr = (wid < I);
+  const short2 rng = g.cell_rng[s0 + lane];
+  const float dtv = g.dtv[s0 + lane];
+  const float dvc = (t < kCellsPerCta) ? g.dvc[s0 + t] : 0.f;
 
   // ---- wait for the previous step's state
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
   cudaGridDependencySynchronize();
 #endif
   float2 x2 = make_float2(0.f, 0.f);
-  if (cell_thr) x2 = p.cc2[(size_t)wid * g.C + c0 + lane];
-  float env_acc[kMaxIons];
+  if (cell_thr) x2 = p.cc2[(size_t)wid * g.S + s0 + lane];
+  float own[REC], nbr[REC];
+  load_rec<REC>(p.rec_in, s0 + (active ? lc : 0), own);
+  load_rec<REC>(p.rec_in, cn, nbr);
+  const float* ce = p.cenv_f + (size_t)cl * I;
+  float cenv[NI];
 #pragma unroll
-  for (int i = 0; i < kMaxIons; ++i) env_acc[i] = 0.f;
+  for (int i = 0; i < NI; ++i) cenv[i] = (i < I) ? ce[i] : 0.f;
+  const float pc = p.pump_coef[cl];
 
+  float env_acc[NI];
+#pragma unroll
+  for (int i = 0; i < NI; ++i) env_acc[i] = 0.f;
   if (active) {
-    float own[REC], nbr[REC];
-    load_rec<REC>(p.rec_in, c, own);
-    load_rec<REC>(p.rec_in, cn, nbr);
     float v = own[REC - 1];
     float vn = nbr[REC - 1];
-    if (PHIB) { v -= p.phib[g.map_env[m]]; vn -= p.phib[g.map_env[g.nn[m]]]; }
+    if (PHIB) { v -= p.phib[g.map_env[q]]; vn -= p.phib[g.nn_env[q]]; }
     // BETSE's 1e-25 nonces (sim_toolbox.py:52-56) keep alpha != 0 at zero volts
     const float v1 = v + 1.0e-25f;
     const float vgj1 = ((vn + 1.0e-25f) - v1) + 1.0e-25f;
@@ -218,15 +242,15 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     sm.em1 = expm1f(-sm.a1); sm.e1 = 1.f + sm.em1; sm.r = rcp_fast(sm.em1); sm.q2 = rcp_fast(2.f + sm.em1);
     sg.a1 = vgj1 * k.F_RT;
     sg.em1 = expm1f(-sg.a1); sg.e1 = 1.f + sg.em1; sg.r = rcp_fast(sg.em1); sg.q2 = rcp_fast(2.f + sg.em1);
-    const float* ce = p.cenv_f + (size_t)cl * I;
     float fNa = 0.f;
-    const float pc = p.pump_coef[cl];
     if (pc != 0.f) {
-      // pumpNaKATP (sim_toolbox.py:71-122), one division
-      float cNai = 0.f, cKi = 0.f;
+      // pumpNaKATP (sim_toolbox.py:71-122), one reciprocal
+      float cNai = 0.f, cKi = 0.f, cNao = 0.f, cKo = 0.f;
 #pragma unroll
-      for (int i = 0; i < REC - 1; ++i) { if (i == k.iNa) cNai = own[i]; if (i == k.iK) cKi = own[i]; }
-      const float cNao = ce[k.iNa], cKo = ce[k.iK];
+      for (int i = 0; i < NI; ++i) {
+        if (i == IS::iNa(k)) { cNai = own[i]; cNao = cenv[i]; }
+        if (i == IS::iK(k)) { cKi = own[i]; cKo = cenv[i]; }
+      }
       const float nai = cNai * 1e-3f, nao = cNao * 1e-3f, ki = cKi * 1e-3f, ko = cKo * 1e-3f;
       const float qnum = k.qnum_c * (nao * nao * nao) * (ki * ki);
       float qden = k.qden_c * (nai * nai * nai) * (ko * ko);
@@ -238,30 +262,32 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
       fNa = pc * num_e * (qden * k.K0 - qnum * sm.e1) * rcp_fast(den_e * qden * k.K0);
     }
 #pragma unroll
-    for (int i = 0; i < REC - 1; ++i) {
+    for (int i = 0; i < NI; ++i) {
       if (i >= I) break;
+      const int z = IS::zc(k, i);
       const float cin = own[i];
-      float f = ghk_flux_f(sm, k.zcode[i], k.z[i], v1, k.F_RT, ce[i], cin, dmv[i], k.inv_tm);
-      if (i == k.iNa) f = fNa + f;
-      else if (i == k.iK) f = (-(2.f / 3.f)) * fNa + f;
-      const float fg = ghk_flux_f(sg, k.zcode[i], k.z[i], vgj1, k.F_RT, cin, nbr[i],
-                                  k.dgj_gs[i] * gw, k.inv_gjl);
+      float f = ghk_flux_f(sm, z, k.z[i], v1, k.F_RT, cenv[i], cin, dmv[i], k.inv_tm);
+      if (i == IS::iNa(k)) f = fNa + f;
+      else if (i == IS::iK(k)) f = (-(2.f / 3.f)) * fNa + f;
+      const float fg = ghk_flux_f(sg, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], k.dgj_gs[i] * gw, k.inv_gjl);
       const float a = f * sa;
       sA[i][t] = a;
       sB[i][t] = -fg * sa;
       env_acc[i] = a;
       if (OUT) {
-        p.o_fmem[(size_t)i * g.M + m] = (double)f;
-        p.o_fgj[(size_t)i * g.M + m] = (double)fg;
+        const int mn = g.tile_m0[b] + t;
+        p.o_fmem[(size_t)i * g.M + mn] = (double)f;
+        p.o_fgj[(size_t)i * g.M + mn] = (double)fg;
       }
     }
-    if (OUT) p.o_rate[m] = (double)(-fNa);
+    if (OUT) p.o_rate[g.tile_m0[b] + t] = (double)(-fNa);
   } else {
-    for (int i = 0; i < I; ++i) { sA[i][t] = 0.f; sB[i][t] = 0.f; }
-  }
-  // per-CTA partial sums of f_mem*sa per ion (the finalize kernel reduces them)
 #pragma unroll
-  for (int i = 0; i < kMaxIons; ++i) {
+    for (int i = 0; i < NI; ++i) if (i < I) { sA[i][t] = 0.f; sB[i][t] = 0.f; }
+  }
+  // per-tile partial sums of f_mem*sa per ion (k_split_env reduces them)
+#pragma unroll
+  for (int i = 0; i < NI; ++i) {
     if (i >= I) break;
     float s = env_acc[i];
 #pragma unroll
@@ -271,43 +297,53 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   __syncthreads();
   if (t < I) {
     float s = 0.f;
+#pragma unroll
     for (int w = 0; w < TPB / 32; ++w) s += red[t][w];
     p.env_part[(size_t)b * I + t] = s;
   }
 
   // ---- cells: warp = ion, lane = cell -- update_all_concs (sim.py:2086-2111)
   int bad = 0, neg = 0;
-  if (cell_thr) {
+  const bool cell_live = cell_thr && rng.y > rng.x;
+  if (cell_live) {
     const int i = wid;
     float s1 = 0.f, s2 = 0.f;
-    for (int j = a0; j < a1; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
+    for (int j = rng.x; j < rng.y; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
     df x{x2.x, x2.y};
     x = df_add_f(x, s1 * dtv);                         // update_Co
     sRec[lane][i] = x.hi + x.lo;                       // cc_at_mem (before the GJ term)
     x = df_add_f(x, s2 * dtv);                         // gap-junction term
     if (x.hi != x.hi) bad = 1;
     if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg = 1; }   // no_negs
-    p.cc2[(size_t)i * g.C + c0 + lane] = make_float2(x.hi, x.lo);
+    p.cc2[(size_t)i * g.S + s0 + lane] = make_float2(x.hi, x.lo);
     const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
     sQ[i][lane] = make_float2(qz.hi, qz.lo);
   }
   const int n_bad = __syncthreads_count(bad);
   const int n_neg = __syncthreads_count(neg);
   // ---- charge -> Vmem (update_V, sim.py:2027-2029), one lane per cell
-  if (t < ncell) {
-    const int cc = c0 + t;
-    df rho{0.f, 0.f};
-    for (int i = 0; i < I; ++i) rho = df_add(rho, df{sQ[i][t].x, sQ[i][t].y});
-    const float vc = (rho.hi + rho.lo) * dvc;
-    float o[REC];
+  if (t < kCellsPerCta) {
+    const short2 r0 = g.cell_rng[s0 + t];
+    if (r0.y > r0.x) {
+      df rho{0.f, 0.f};
 #pragma unroll
-    for (int i = 0; i < REC - 1; ++i) o[i] = (i < I) ? sRec[t][i] : 0.f;
-    o[REC - 1] = vc;
-    float4* out4 = reinterpret_cast<float4*>(p.rec_out + (size_t)cc * REC);
+      for (int i = 0; i < NI; ++i)
+        if (i < I) rho = df_add(rho, df{sQ[i][t].x, sQ[i][t].y});
+      const float vc = (rho.hi + rho.lo) * dvc;
+      float o[REC];
 #pragma unroll
-    for (int q = 0; q < REC / 4; ++q) out4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
-    if (vc != vc) atomicAdd(&p.status[0], 1ull);
-    if (OUT) { p.o_rho[cc] = (double)rho.hi + (double)rho.lo; p.o_vmem[cc] = (double)vc; }
+      for (int i = 0; i < REC - 1; ++i) o[i] = (i < I) ? sRec[t][i] : 0.f;
+      o[REC - 1] = vc;
+      float4* out4 = reinterpret_cast<float4*>(p.rec_out + (size_t)(s0 + t) * REC);
+#pragma unroll
+      for (int w = 0; w < REC / 4; ++w) out4[w] = make_float4(o[4 * w], o[4 * w + 1], o[4 * w + 2], o[4 * w + 3]);
+      if (vc != vc) atomicAdd(&p.status[0], 1ull);
+      if (OUT) {
+        const int cc = g.tile_c0[b] + t;
+        p.o_rho[cc] = (double)rho.hi + (double)rho.lo;
+        p.o_vmem[cc] = (double)vc;
+      }
+    }
   }
   if (t == 0) {
     if (n_bad) atomicAdd(&p.status[1], (unsigned long long)n_bad);
@@ -374,7 +410,7 @@ struct SplitOutGeom {
 };
 struct SplitOutPtrs {
   const double* fmem; const double* fgj; const float* rec_new; const float* rec_old; int rec;
-  const float2* cc2; const float* phib;
+  const float2* cc2; int S; const int* slot_of_cell; const float* phib;
   double* Jn; double* Imem; double* Jcx; double* Jcy; double* Jc; double* vmave; double* dvm;
   double* Ecx; double* Ecy; double* Emc; double* Egjx; double* Egjy; double* gjopen; double* sigma;
   double* vm_mem;      // [M] start-of-step Vmem per membrane (update_gj reads it)
@@ -404,8 +440,9 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
     for (int i = 0; i < k.I; ++i) { Jm += k.zF[i] * p.fmem[(size_t)i * g.M + m]; Jg += k.zF[i] * p.fgj[(size_t)i * g.M + m]; }
     Jraw = -Jm + Jg;
     const double ph = p.phib ? (double)p.phib[g.map_env[m]] : 0.0;
-    vm = (double)p.rec_new[(size_t)c * p.rec + p.rec - 1] - ph;
-    p.vm_mem[m] = (double)p.rec_old[(size_t)c * p.rec + p.rec - 1] - ph;
+    const int sc = p.slot_of_cell[c];
+    vm = (double)p.rec_new[(size_t)sc * p.rec + p.rec - 1] - ph;
+    p.vm_mem[m] = (double)p.rec_old[(size_t)sc * p.rec + p.rec - 1] - ph;
     sX[0][t] = Jraw * g.mem_sa[m];
     sX[1][t] = vm;
   } else { sX[0][t] = 0.0; sX[1][t] = 0.0; }
@@ -418,7 +455,8 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
     sC[0][t] = s / g.cell_sa[c];
     p.vmave[c] = sv / (double)(a1 - a0);
     double sig = 0.0;
-    for (int i = 0; i < k.I; ++i) { const float2 x = p.cc2[i * g.C + c]; sig += k.sig_coef[i] * ((double)x.x + (double)x.y); }
+    const int sc = p.slot_of_cell[c];
+    for (int i = 0; i < k.I; ++i) { const float2 x = p.cc2[(size_t)i * p.S + sc]; sig += k.sig_coef[i] * ((double)x.x + (double)x.y); }
     sig /= (double)k.I;
     p.sigma[c] = sig;
     sC[3][t] = sig;
@@ -431,7 +469,7 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
     sX[2][t] = Jn * g.nx[m] * g.mem_sa[m];
     sX[3][t] = Jn * g.ny[m] * g.mem_sa[m];
     const int c = c0 + lc;
-    double vmo = (double)p.rec_old[(size_t)c * p.rec + p.rec - 1] - (p.phib ? (double)p.phib[g.map_env[m]] : 0.0);
+    double vmo = (double)p.rec_old[(size_t)p.slot_of_cell[c] * p.rec + p.rec - 1] - (p.phib ? (double)p.phib[g.map_env[m]] : 0.0);
     for (int i = 0; i < k.I; ++i) vmo += kNonce;
     p.dvm[m] = (vm - vmo) / k.dt;
   } else { sX[2][t] = 0.0; sX[3][t] = 0.0; }
