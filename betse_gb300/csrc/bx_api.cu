@@ -71,7 +71,9 @@ struct bx_cluster {
   int precision = BX_PLAIN_FP64;
   int mode = MODE_PLAIN;
   int nblk = 0;
-  int tpb = kTPB;                  // membrane slots per CTA (autotuned: 128 or 256)
+  int tpb = kTPB;                  // membrane slots per CTA (autotuned)
+  bool persist = false;            // split form: persistent cp.async-pipelined kernel (autotuned)
+  int sm_count = 0;
   bool ecm = false;
   bx_params par{};                 // parameters of cluster 0 (the shared ones)
   std::vector<bx_params> cl_par;   // per-cluster parameters
@@ -306,6 +308,22 @@ inline int env_grid(int G) { return (G + kEnvTPB - 1) / kEnvTPB; }
 // launch with programmatic dependent launch: the kernel's prologue overlaps
 // the previous kernel; cudaGridDependencySynchronize orders the state accesses
 template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl_smem(void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                            Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+template <typename... KArgs, typename... Args>
 cudaError_t launch_pdl(void (*kern)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
@@ -329,7 +347,32 @@ cudaError_t launch_split_t(bx_cluster* h, int parity, cudaStream_t s) {
                     split_ptrs(h, parity), make_split_const(h));
 }
 
+// the persistent kernel: one wave of CTAs walking the tiles
+template <int TPB, int ZP>
+cudaError_t launch_persist_t(bx_cluster* h, int parity, cudaStream_t s) {
+  auto kern = bx::k_split_persist<TPB, ZP>;
+  const size_t smem = sizeof(bx::PersistSmem<TPB, bx::IonSet<ZP>::NI>);
+  static bool attr_set = false;   // per instantiation
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPB, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int grid = std::max(1, std::min(h->nblk, per_sm * h->sm_count));
+  return launch_pdl_smem(kern, (unsigned)grid, TPB, smem, s, split_geom(h), split_ptrs(h, parity),
+                         make_split_const(h), h->nblk);
+}
+
 cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
+  if (h->persist && !out && !h->phib_nonzero) {
+    const bool six = is_betse_six_ions(h);
+    if (h->tpb == 192) return six ? launch_persist_t<192, 1>(h, parity, s) : launch_persist_t<192, 0>(h, parity, s);
+    return six ? launch_persist_t<256, 1>(h, parity, s) : launch_persist_t<256, 0>(h, parity, s);
+  }
   const int code = (h->tpb == 192 ? 4 : 0) | (out ? 2 : 0) | (h->phib_nonzero ? 1 : 0);
   switch (code) {
     case 0: return launch_split_t<256, false, false>(h, parity, s);
@@ -716,6 +759,8 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   }
 
   if (cudaGetDevice(&h->dev) != cudaSuccess) return bail(BX_ECUDA, "no CUDA device");
+  if (cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->dev) != cudaSuccess)
+    return bail(BX_ECUDA, "cudaDeviceGetAttribute");
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(BX_ECUDA, "cudaStreamCreate failed");
 
@@ -1158,6 +1203,25 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
 
 int64_t bx_launch_count(bx_handle h) { return h ? h->launches : -1; }
 
+int bx_set_launch_config(bx_handle h, int tpb, int persistent) {
+  if (!h) return fail(BX_EINVAL, "null handle");
+  const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256) : (tpb == 128 || tpb == 256);
+  if (!ok) return fail(BX_EINVAL, "unsupported CTA size for this form");
+  if (persistent && h->mode != MODE_SPLIT) return fail(BX_EINVAL, "the persistent kernel is the split form's");
+  const size_t C = h->C, I = h->I, M = h->M;
+  const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
+  std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1);
+  bx_state sv{vm.data(), cc.data(), cam.data(), cenv.data(), h->ecm ? ex.data() : nullptr,
+              h->ecm ? ey.data() : nullptr};
+  const bool had_state = h->have_state;
+  int rc;
+  if (had_state && (rc = bx_state_download(h, &sv)) != BX_OK) return rc;
+  if ((rc = build_partition(h, tpb)) != BX_OK) return rc;
+  h->persist = persistent != 0;
+  if (had_state && (rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
+  return BX_OK;
+}
+
 // Autotuner: time `n_steps` eager steps for each CTA size, keep the fastest.
 // The state is downloaded before the trials and uploaded again after each
 // one (the split form's tile-major layout changes with the CTA size), so
@@ -1175,14 +1239,20 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   unsigned long long status[4];
   BX_CU(cudaMemcpy(status, h->d_status, sizeof(status), cudaMemcpyDeviceToHost));
   const int64_t launches0 = h->launches;
-  const int cands[2] = {256, (h->mode == MODE_SPLIT) ? 192 : 128};
+  struct Cand { int tpb; bool persist; };
+  std::vector<Cand> cands;
+  if (h->mode == MODE_SPLIT) cands = {{256, false}, {192, false}, {256, true}, {192, true}};
+  else cands = {{256, false}, {128, false}};
   double best = 1e300;
   int best_tpb = h->tpb;
+  bool best_persist = h->persist;
   cudaEvent_t e0, e1;
   BX_CU(cudaEventCreate(&e0));
   BX_CU(cudaEventCreate(&e1));
-  for (int tpb : cands) {
+  for (const Cand& cd : cands) {
+    const int tpb = cd.tpb;
     if (build_partition(h, tpb) != BX_OK) continue;
+    h->persist = cd.persist;
     if ((rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
     for (int w = 0; w < 2; ++w) { enqueue_step(h, h->parity, false, h->stream); h->parity ^= 1; }
     BX_CU(cudaEventRecord(e0, h->stream));
@@ -1192,11 +1262,12 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
     float ms = 0.f;
     BX_CU(cudaEventElapsedTime(&ms, e0, e1));
     const double per = ms / n_steps;
-    if (per < best) { best = per; best_tpb = tpb; }
+    if (per < best) { best = per; best_tpb = tpb; best_persist = cd.persist; }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if ((rc = build_partition(h, best_tpb)) != BX_OK) return rc;
+  h->persist = best_persist;
   if ((rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
   BX_CU(cudaMemcpy(h->d_status, status, sizeof(status), cudaMemcpyHostToDevice));
   h->launches = launches0;

@@ -351,6 +351,262 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent, software-pipelined form of k_split_step (no outputs, no Phi_b).
+// Each CTA walks tiles b = blockIdx.x + j*gridDim.x.  Tiles are staged in
+// shared memory with cp.async (16-byte asynchronous copies that complete at
+// cp.async.wait_group -- no waits of ours): the geometry of tile j+2 and the
+// state of tile j+1 (own and partner records, concentrations) are in flight
+// while tile j computes.  Same arithmetic, same order as k_split_step, so the
+// results are bit-identical.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <int TPB>
+__device__ __forceinline__ void cp_block(void* smem, const void* gmem, int bytes) {
+  char* s = static_cast<char*>(smem);
+  const char* gp = static_cast<const char*>(gmem);
+  for (int off = (int)threadIdx.x * 16; off < bytes; off += TPB * 16) cp16(s + off, gp + off);
+}
+
+template <int TPB, int NI>
+struct PersistSmem {
+  struct Geo {                       // one tile's geometry and channel data
+    float Dm[NI][TPB];
+    float sa[TPB];
+    float gw[TPB];
+    int nn[TPB];
+    uint8_t lcell[TPB];
+  };
+  struct State {                     // one tile's state
+    float own[kCellsPerCta][8];
+    float nbr[TPB][8];
+    float2 cc2[NI][kCellsPerCta];
+    short2 rng[kCellsPerCta];
+    float dtv[kCellsPerCta];
+    float dvc[kCellsPerCta];
+    int cl;
+    int pad[3];
+  };
+  Geo geo[3];
+  State st[2];
+  float sA[NI][TPB];
+  float sB[NI][TPB];
+  float red[NI][TPB / 32];
+  float sRec[kCellsPerCta][8];
+  float2 sQ[NI][kCellsPerCta];
+};
+
+template <int TPB, int ZP>
+__global__ void __launch_bounds__(TPB)
+k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
+  using IS = IonSet<ZP>;
+  constexpr int NI = IS::NI;
+  constexpr int REC = 8;
+  using SM = PersistSmem<TPB, NI>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SM& sm = *reinterpret_cast<SM*>(smem_raw);
+  const int I = IS::n(k);
+  const int t = threadIdx.x;
+  const int lane = t & 31, wid = t >> 5;
+  const int G = gridDim.x;
+
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
+  cudaTriggerProgrammaticLaunchCompletion();
+#endif
+  auto issue_geo = [&](int tile, int buf) {
+    if (tile >= ntile) return;
+    typename SM::Geo& ge = sm.geo[buf];
+    const size_t q0 = (size_t)tile * TPB;
+#pragma unroll
+    for (int i = 0; i < NI; ++i)
+      if (i < I) cp_block<TPB>(ge.Dm[i], p.Dm + (size_t)i * g.Q + q0, TPB * 4);
+    cp_block<TPB>(ge.sa, g.mem_sa + q0, TPB * 4);
+    cp_block<TPB>(ge.gw, g.gjw + q0, TPB * 4);
+    cp_block<TPB>(ge.nn, g.nn_slot + q0, TPB * 4);
+    cp_block<TPB>(ge.lcell, g.lcell + q0, TPB);
+  };
+  auto issue_state = [&](int tile, int sbuf, int gbuf) {
+    if (tile >= ntile) return;
+    typename SM::State& st = sm.st[sbuf];
+    const typename SM::Geo& ge = sm.geo[gbuf];
+    const int s0 = tile * kCellsPerCta;
+    cp_block<TPB>(st.own, p.rec_in + (size_t)s0 * REC, kCellsPerCta * REC * 4);
+#pragma unroll
+    for (int i = 0; i < NI; ++i)
+      if (i < I) cp_block<TPB>(st.cc2[i], p.cc2 + (size_t)i * g.S + s0, kCellsPerCta * 8);
+    cp_block<TPB>(st.rng, g.cell_rng + s0, kCellsPerCta * 4);
+    cp_block<TPB>(st.dtv, g.dtv + s0, kCellsPerCta * 4);
+    cp_block<TPB>(st.dvc, g.dvc + s0, kCellsPerCta * 4);
+    if (t == 0) cp4(&st.cl, g.blk_cluster + tile);
+    if (ge.lcell[t] != 255) {         // partner record of this slot
+      const float* src = p.rec_in + (size_t)ge.nn[t] * REC;
+      cp16(&st.nbr[t][0], src);
+      cp16(&st.nbr[t][4], src + 4);
+    }
+  };
+
+  // geometry is read-only while stepping: fetch it before the dependency wait
+  const int T0 = blockIdx.x;
+  issue_geo(T0, 0);
+  issue_geo(T0 + G, 1);
+  cp_commit();
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
+  cudaGridDependencySynchronize();
+#endif
+  cp_wait_all();
+  __syncthreads();
+  issue_state(T0, 0, 0);
+  cp_commit();
+
+  unsigned long long n_bad = 0, n_neg = 0, n_nan = 0;
+  int j = 0;
+  for (int tile = T0; tile < ntile; tile += G, ++j) {
+    const int gb = j % 3, sb = j & 1;
+    cp_wait_all();                   // state(tile) and geometry(tile + G) have landed
+    __syncthreads();
+    issue_state(tile + G, sb ^ 1, (j + 1) % 3);
+    issue_geo(tile + 2 * G, (j + 2) % 3);
+    cp_commit();
+
+    const typename SM::Geo& ge = sm.geo[gb];
+    const typename SM::State& st = sm.st[sb];
+    const int s0 = tile * kCellsPerCta;
+    const int cl = st.cl;
+    const int lc = ge.lcell[t];
+    const bool active = lc != 255;
+    float env_acc[NI];
+#pragma unroll
+    for (int i = 0; i < NI; ++i) env_acc[i] = 0.f;
+    if (active) {
+      float own[REC], nbr[REC];
+#pragma unroll
+      for (int r = 0; r < REC; ++r) { own[r] = st.own[lc][r]; nbr[r] = st.nbr[t][r]; }
+      const float* ce = p.cenv_f + (size_t)cl * I;
+      float cenv[NI];
+#pragma unroll
+      for (int i = 0; i < NI; ++i) cenv[i] = (i < I) ? ce[i] : 0.f;
+      const float pc = p.pump_coef[cl];
+      const float v = own[REC - 1];
+      const float vn = nbr[REC - 1];
+      const float v1 = v + 1.0e-25f;
+      const float vgj1 = ((vn + 1.0e-25f) - v1) + 1.0e-25f;
+      GhkShared<float> gm, gg;
+      gm.a1 = v1 * k.F_RT;
+      gm.em1 = expm1f(-gm.a1); gm.e1 = 1.f + gm.em1; gm.r = rcp_fast(gm.em1); gm.q2 = rcp_fast(2.f + gm.em1);
+      gg.a1 = vgj1 * k.F_RT;
+      gg.em1 = expm1f(-gg.a1); gg.e1 = 1.f + gg.em1; gg.r = rcp_fast(gg.em1); gg.q2 = rcp_fast(2.f + gg.em1);
+      float fNa = 0.f;
+      if (pc != 0.f) {
+        float cNai = 0.f, cKi = 0.f, cNao = 0.f, cKo = 0.f;
+#pragma unroll
+        for (int i = 0; i < NI; ++i) {
+          if (i == IS::iNa(k)) { cNai = own[i]; cNao = cenv[i]; }
+          if (i == IS::iK(k)) { cKi = own[i]; cKo = cenv[i]; }
+        }
+        const float nai = cNai * 1e-3f, nao = cNao * 1e-3f, ki = cKi * 1e-3f, ko = cKo * 1e-3f;
+        const float qnum = k.qnum_c * (nao * nao * nao) * (ki * ki);
+        float qden = k.qden_c * (nai * nai * nai) * (ko * ko);
+        if (qden == 0.f) qden = 1.0e-15f;
+        const float xna = cNai * k.inv_KmNa, xk = cKo * k.inv_KmK;
+        const float na3 = xna * xna * xna, k2 = xk * xk;
+        const float num_e = na3 * k2 * k.atp_term;
+        const float den_e = (1.f + na3) * (1.f + k2) * k.atp_den;
+        fNa = pc * num_e * (qden * k.K0 - qnum * gm.e1) * rcp_fast(den_e * qden * k.K0);
+      }
+      const float sa = ge.sa[t];
+      const float gw = ge.gw[t] * k.gj_block;
+#pragma unroll
+      for (int i = 0; i < NI; ++i) {
+        if (i >= I) break;
+        const int z = IS::zc(k, i);
+        const float cin = own[i];
+        float f = ghk_flux_f(gm, z, k.z[i], v1, k.F_RT, cenv[i], cin, ge.Dm[i][t], k.inv_tm);
+        if (i == IS::iNa(k)) f = fNa + f;
+        else if (i == IS::iK(k)) f = (-(2.f / 3.f)) * fNa + f;
+        const float fgv = ghk_flux_f(gg, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], k.dgj_gs[i] * gw, k.inv_gjl);
+        const float a = f * sa;
+        sm.sA[i][t] = a;
+        sm.sB[i][t] = -fgv * sa;
+        env_acc[i] = a;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < NI; ++i) if (i < I) { sm.sA[i][t] = 0.f; sm.sB[i][t] = 0.f; }
+    }
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      if (i >= I) break;
+      float s = env_acc[i];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) sm.red[i][wid] = s;
+    }
+    __syncthreads();
+    if (t < I) {
+      float s = 0.f;
+#pragma unroll
+      for (int w = 0; w < TPB / 32; ++w) s += sm.red[t][w];
+      p.env_part[(size_t)tile * I + t] = s;
+    }
+    // cells: warp = ion, lane = cell (update_all_concs)
+    int bad = 0, neg = 0;
+    const short2 rng = st.rng[lane];
+    if (wid < I && rng.y > rng.x) {
+      const int i = wid;
+      float s1 = 0.f, s2 = 0.f;
+      for (int jj = rng.x; jj < rng.y; ++jj) { s1 += sm.sA[i][jj]; s2 += sm.sB[i][jj]; }
+      const float dtv = st.dtv[lane];
+      const float2 x2 = st.cc2[i][lane];
+      df x{x2.x, x2.y};
+      x = df_add_f(x, s1 * dtv);
+      sm.sRec[lane][i] = x.hi + x.lo;
+      x = df_add_f(x, s2 * dtv);
+      if (x.hi != x.hi) bad = 1;
+      if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg = 1; }
+      p.cc2[(size_t)i * g.S + s0 + lane] = make_float2(x.hi, x.lo);
+      const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
+      sm.sQ[i][lane] = make_float2(qz.hi, qz.lo);
+    }
+    n_bad += __syncthreads_count(bad);
+    n_neg += __syncthreads_count(neg);
+    if (t < kCellsPerCta) {
+      const short2 r0 = st.rng[t];
+      if (r0.y > r0.x) {
+        df rho{0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < NI; ++i)
+          if (i < I) rho = df_add(rho, df{sm.sQ[i][t].x, sm.sQ[i][t].y});
+        const float vc = (rho.hi + rho.lo) * st.dvc[t];
+        float o[REC];
+#pragma unroll
+        for (int i = 0; i < REC - 1; ++i) o[i] = (i < I) ? sm.sRec[t][i] : 0.f;
+        o[REC - 1] = vc;
+        float4* out4 = reinterpret_cast<float4*>(p.rec_out + (size_t)(s0 + t) * REC);
+        out4[0] = make_float4(o[0], o[1], o[2], o[3]);
+        out4[1] = make_float4(o[4], o[5], o[6], o[7]);
+        if (vc != vc) ++n_nan;
+      }
+    }
+    __syncthreads();                 // the buffers of this tile are reused two tiles on
+  }
+  cp_wait_all();
+  if (t == 0) {
+    if (n_bad) atomicAdd(&p.status[1], n_bad);
+    if (n_neg) atomicAdd(&p.status[2], n_neg);
+  }
+  if (n_nan) atomicAdd(&p.status[0], n_nan);
+}
+
 // Well-mixed environment per cluster (sim_toolbox.py:1196-1205):
 // c_env <- mean_m(c_env - f_m sa_m / vol_env * dt).  One CTA per cluster sums
 // the cluster's per-CTA partials in a fixed order (double-float), so the

@@ -145,6 +145,11 @@ class ClusterEngine:
         _lib.check(self.lib.bx_time_cell_kernel(self.h, int(n), ct.byref(ms)), 'bx_time_cell_kernel')
         return ms.value
 
+    def set_launch_config(self, tpb, persistent=False):
+        """Pin the CTA size and (split form) the persistent kernel; state kept."""
+        _lib.check(self.lib.bx_set_launch_config(self.h, int(tpb), int(bool(persistent))),
+                   'bx_set_launch_config')
+
     def autotune(self, n_steps=20):
         """Pick the fastest CTA size for this cluster; the state is unchanged.
         Returns (threads per CTA, ms per step)."""

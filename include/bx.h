@@ -252,9 +252,15 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
                          double* vm_work, double* cc_cells, double* cc_mem, double* cc_mem_work,
                          double* cc_env, int n_steps, void* stream);
 
-/* Autotuner: times n_steps steps for each supported CTA size (128 and 256
- * membrane slots) on the uploaded state, keeps the fastest, and restores the
- * state so the simulation does not advance.  Reports the choice and its
+/* Launch configuration: CTA size (plain form 128 or 256; split form 192 or
+ * 256 membrane slots) and, for the split form, the persistent pipelined
+ * kernel.  The state is kept.  bx_autotune picks these by timing. */
+int bx_set_launch_config(bx_handle h, int tpb, int persistent);
+
+/* Autotuner: times n_steps steps for each launch configuration (CTA size,
+ * and for the split form tile-per-CTA or persistent pipelined kernel) on the
+ * uploaded state, keeps the fastest, and restores the state so the
+ * simulation does not advance.  Reports the choice and its
  * ms per step (either pointer may be NULL). */
 int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out);
 

@@ -16,12 +16,14 @@ def _clusters():
     return out
 
 
-@pytest.mark.parametrize('precision', ['split', 'fp64'])
-def test_batch_equals_individual_runs(precision):
+@pytest.mark.parametrize('precision,persist', [('split', False), ('split', True), ('fp64', False)])
+def test_batch_equals_individual_runs(precision, persist):
     from betse_gb300.engine import BatchEngine, ClusterEngine
     cl = _clusters()
     n = 150
     with BatchEngine([c[0] for c in cl], [c[1] for c in cl], precision) as b:
+        if persist:
+            b.set_launch_config(256, True)
         b.set_membrane_diffusivity([c[2] for c in cl])
         b.upload_states([c[3] for c in cl])
         b.step(n)

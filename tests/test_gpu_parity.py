@@ -170,3 +170,23 @@ def test_autotune_keeps_state_and_results(precision):
     tol = 0.0 if precision == 'fp64' else 1e-12
     for k in sa:
         assert gi.rel_err(sa[k], sb[k]) <= tol, k
+
+
+@pytest.mark.parametrize('tpb', [192, 256])
+def test_split_launch_configs_bit_identical(tpb):
+    """Tile-per-CTA and persistent pipelined split kernels, and both CTA sizes,
+    give bit-identical state: the same arithmetic in the same order."""
+    d = gi.load('noecm_r80_s1')
+    res = []
+    for persist in (False, True):
+        with _engine(d, 'split') as e:
+            e.set_launch_config(tpb, persist)
+            e.step(75)
+            e.check_stable()
+            res.append(e.download())
+    with _engine(d, 'split') as e:
+        e.step(75)
+        ref = e.download()
+    for k in ref:
+        assert np.array_equal(res[0][k], res[1][k]), k
+        assert np.array_equal(res[0][k], ref[k]), k
