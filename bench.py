@@ -302,8 +302,10 @@ def main():
     plain = make('fp64')
     n_mems = split.n_mems if sweep else g.n_mems
     n_cells = split.n_cells if sweep else g.n_cells
-    tune_split = split.autotune(20)
-    tune_plain = plain.autotune(3)
+    split.autotune(20)
+    plain.autotune(3)
+    tune_split = split.launch_config()
+    tune_plain = plain.launch_config()
 
     def barrier():
         torch.cuda.synchronize()
@@ -417,7 +419,8 @@ def main():
                        'time_steps_per_step': T, 'precision': 'split',
                        'l2': 'flushed (256 MiB write) before every timed run',
                        'parallelism': f'replicas x{world}',
-                       'autotuned_cta_threads': {'split': tune_split[0], 'plain_fp64': tune_plain[0]}},
+                       'autotuned_launch': {'split': {'cta_threads': tune_split[0], 'persistent': tune_split[1]},
+                                            'plain_fp64': {'cta_threads': tune_plain[0]}}},
             'plain_fp64': {'value': plain_value, 'unit': UNIT,
                            'ms_per_step': sum(ms_plain) / len(ms_plain),
                            'speedup_split_vs_plain': value / world / plain_value,

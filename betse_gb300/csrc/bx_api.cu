@@ -1203,6 +1203,13 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
 
 int64_t bx_launch_count(bx_handle h) { return h ? h->launches : -1; }
 
+int bx_get_launch_config(bx_handle h, int* tpb, int* persistent) {
+  if (!h || !tpb || !persistent) return fail(BX_EINVAL, "null argument");
+  *tpb = h->tpb;
+  *persistent = h->persist ? 1 : 0;
+  return BX_OK;
+}
+
 int bx_set_launch_config(bx_handle h, int tpb, int persistent) {
   if (!h) return fail(BX_EINVAL, "null handle");
   const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256) : (tpb == 128 || tpb == 256);

@@ -56,6 +56,51 @@ __device__ __forceinline__ df df_mul(df x, float khi, float klo) {
   return df{hi, __fsub_rn(lo, __fsub_rn(hi, p))};
 }
 
+// expm1 in FP32 from its Taylor series: x + x^2/2! + ... + x^7/7! for
+// |x| < 0.5 (truncation below 2e-8 relative), exp(x) - 1 with the MUFU
+// exponential above, where the cancellation factor e^x/(e^x - 1) is at most
+// 2.6.  Accurate to a few 1e-7 relative -- the FP32 flux budget of the split
+// form -- at a fraction of the instructions of the libm expm1f.
+__device__ __forceinline__ float expm1_split(float x) {
+  if (fabsf(x) < 0.5f) {
+    float p = 1.0f / 5040.0f;
+    p = fmaf(p, x, 1.0f / 720.0f);
+    p = fmaf(p, x, 1.0f / 120.0f);
+    p = fmaf(p, x, 1.0f / 24.0f);
+    p = fmaf(p, x, 1.0f / 6.0f);
+    p = fmaf(p, x, 0.5f);
+    return fmaf(p * x, x, x);
+  }
+  return __expf(x) - 1.0f;
+}
+
+// Shared exponentials of one voltage for the split form; ka1 = alpha1 / d.
+__device__ __forceinline__ void ghk_init_f(GhkShared<float>& s, float v_nonce, float F_RT) {
+  s.a1 = v_nonce * F_RT;
+  s.em1 = expm1_split(-s.a1);
+  s.e1 = 1.f + s.em1;
+  s.r = __fdividef(1.f, s.em1);
+  s.q2 = __fdividef(1.f, 2.f + s.em1);
+}
+
+// FP32 GHK flux (same identities as ghk_flux) with ka1 = alpha1/d hoisted;
+// the generic-charge branch evaluates BETSE's formula directly in FP32.
+__device__ __forceinline__ float ghk_flux_fk(const GhkShared<float>& s, float ka1, int zcode, float zval,
+                                             float v_nonce, float F_RT, float cA, float cB, float Dc,
+                                             float inv_d) {
+  const float kk = Dc * ka1;
+  switch (zcode) {
+    case 1:  return kk * (cB - cA * s.e1) * s.r;
+    case -1: return kk * (cB * s.e1 - cA) * s.r;
+    case 2:  { const float e2 = s.e1 * s.e1; return 2.f * kk * (cB - cA * e2) * s.r * s.q2; }
+    case -2: { const float e2 = s.e1 * s.e1; return 2.f * kk * (cB * e2 - cA) * s.r * s.q2; }
+    default: {
+      const float a = ((zval + 1.0e-25f) * v_nonce) * F_RT;
+      return -((Dc * a) * inv_d) * ((cB - cA * expf(-a)) / (-expm1f(-a)));
+    }
+  }
+}
+
 // FP32 GHK flux (same identities as ghk_flux); the generic-charge branch
 // evaluates BETSE's formula directly in FP32.
 __device__ __forceinline__ float ghk_flux_f(const GhkShared<float>& s, int zcode, float zval,
@@ -177,7 +222,6 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   constexpr int NI = IS::NI;
   __shared__ float sA[NI][TPB];
   __shared__ float sB[NI][TPB];
-  __shared__ float red[NI][TPB / 32];
   __shared__ float sRec[kCellsPerCta][REC];
   __shared__ float2 sQ[NI][kCellsPerCta];
   const int I = IS::n(k);
@@ -227,9 +271,6 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   for (int i = 0; i < NI; ++i) cenv[i] = (i < I) ? ce[i] : 0.f;
   const float pc = p.pump_coef[cl];
 
-  float env_acc[NI];
-#pragma unroll
-  for (int i = 0; i < NI; ++i) env_acc[i] = 0.f;
   if (active) {
     float v = own[REC - 1];
     float vn = nbr[REC - 1];
@@ -238,10 +279,9 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     const float v1 = v + 1.0e-25f;
     const float vgj1 = ((vn + 1.0e-25f) - v1) + 1.0e-25f;
     GhkShared<float> sm, sg;
-    sm.a1 = v1 * k.F_RT;
-    sm.em1 = expm1f(-sm.a1); sm.e1 = 1.f + sm.em1; sm.r = rcp_fast(sm.em1); sm.q2 = rcp_fast(2.f + sm.em1);
-    sg.a1 = vgj1 * k.F_RT;
-    sg.em1 = expm1f(-sg.a1); sg.e1 = 1.f + sg.em1; sg.r = rcp_fast(sg.em1); sg.q2 = rcp_fast(2.f + sg.em1);
+    ghk_init_f(sm, v1, k.F_RT);
+    ghk_init_f(sg, vgj1, k.F_RT);
+    const float ka_m = sm.a1 * k.inv_tm, ka_g = sg.a1 * k.inv_gjl;
     float fNa = 0.f;
     if (pc != 0.f) {
       // pumpNaKATP (sim_toolbox.py:71-122), one reciprocal
@@ -266,14 +306,12 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
       if (i >= I) break;
       const int z = IS::zc(k, i);
       const float cin = own[i];
-      float f = ghk_flux_f(sm, z, k.z[i], v1, k.F_RT, cenv[i], cin, dmv[i], k.inv_tm);
+      float f = ghk_flux_fk(sm, ka_m, z, k.z[i], v1, k.F_RT, cenv[i], cin, dmv[i], k.inv_tm);
       if (i == IS::iNa(k)) f = fNa + f;
       else if (i == IS::iK(k)) f = (-(2.f / 3.f)) * fNa + f;
-      const float fg = ghk_flux_f(sg, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], k.dgj_gs[i] * gw, k.inv_gjl);
-      const float a = f * sa;
-      sA[i][t] = a;
+      const float fg = ghk_flux_fk(sg, ka_g, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], k.dgj_gs[i] * gw, k.inv_gjl);
+      sA[i][t] = f * sa;
       sB[i][t] = -fg * sa;
-      env_acc[i] = a;
       if (OUT) {
         const int mn = g.tile_m0[b] + t;
         p.o_fmem[(size_t)i * g.M + mn] = (double)f;
@@ -285,30 +323,24 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
 #pragma unroll
     for (int i = 0; i < NI; ++i) if (i < I) { sA[i][t] = 0.f; sB[i][t] = 0.f; }
   }
-  // per-tile partial sums of f_mem*sa per ion (k_split_env reduces them)
-#pragma unroll
-  for (int i = 0; i < NI; ++i) {
-    if (i >= I) break;
-    float s = env_acc[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) red[i][wid] = s;
-  }
   __syncthreads();
-  if (t < I) {
-    float s = 0.f;
-#pragma unroll
-    for (int w = 0; w < TPB / 32; ++w) s += red[t][w];
-    p.env_part[(size_t)b * I + t] = s;
-  }
 
   // ---- cells: warp = ion, lane = cell -- update_all_concs (sim.py:2086-2111)
   int bad = 0, neg = 0;
   const bool cell_live = cell_thr && rng.y > rng.x;
+  float s1 = 0.f;
+  if (cell_thr) {
+    for (int j = rng.x; j < rng.y; ++j) s1 += sA[wid][j];
+    // per-tile partial sum of f_mem*sa of this ion (k_split_env reduces them)
+    float e = s1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+    if (lane == 0) p.env_part[(size_t)b * I + wid] = e;
+  }
   if (cell_live) {
     const int i = wid;
-    float s1 = 0.f, s2 = 0.f;
-    for (int j = rng.x; j < rng.y; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
+    float s2 = 0.f;
+    for (int j = rng.x; j < rng.y; ++j) s2 += sB[i][j];
     df x{x2.x, x2.y};
     x = df_add_f(x, s1 * dtv);                         // update_Co
     sRec[lane][i] = x.hi + x.lo;                       // cc_at_mem (before the GJ term)
@@ -401,7 +433,6 @@ struct PersistSmem {
   State st[2];
   float sA[NI][TPB];
   float sB[NI][TPB];
-  float red[NI][TPB / 32];
   float sRec[kCellsPerCta][8];
   float2 sQ[NI][kCellsPerCta];
 };
@@ -484,9 +515,6 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
     const int cl = st.cl;
     const int lc = ge.lcell[t];
     const bool active = lc != 255;
-    float env_acc[NI];
-#pragma unroll
-    for (int i = 0; i < NI; ++i) env_acc[i] = 0.f;
     if (active) {
       float own[REC], nbr[REC];
 #pragma unroll
@@ -501,10 +529,9 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
       const float v1 = v + 1.0e-25f;
       const float vgj1 = ((vn + 1.0e-25f) - v1) + 1.0e-25f;
       GhkShared<float> gm, gg;
-      gm.a1 = v1 * k.F_RT;
-      gm.em1 = expm1f(-gm.a1); gm.e1 = 1.f + gm.em1; gm.r = rcp_fast(gm.em1); gm.q2 = rcp_fast(2.f + gm.em1);
-      gg.a1 = vgj1 * k.F_RT;
-      gg.em1 = expm1f(-gg.a1); gg.e1 = 1.f + gg.em1; gg.r = rcp_fast(gg.em1); gg.q2 = rcp_fast(2.f + gg.em1);
+      ghk_init_f(gm, v1, k.F_RT);
+      ghk_init_f(gg, vgj1, k.F_RT);
+      const float ka_m = gm.a1 * k.inv_tm, ka_g = gg.a1 * k.inv_gjl;
       float fNa = 0.f;
       if (pc != 0.f) {
         float cNai = 0.f, cKi = 0.f, cNao = 0.f, cKo = 0.f;
@@ -530,41 +557,33 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
         if (i >= I) break;
         const int z = IS::zc(k, i);
         const float cin = own[i];
-        float f = ghk_flux_f(gm, z, k.z[i], v1, k.F_RT, cenv[i], cin, ge.Dm[i][t], k.inv_tm);
+        float f = ghk_flux_fk(gm, ka_m, z, k.z[i], v1, k.F_RT, cenv[i], cin, ge.Dm[i][t], k.inv_tm);
         if (i == IS::iNa(k)) f = fNa + f;
         else if (i == IS::iK(k)) f = (-(2.f / 3.f)) * fNa + f;
-        const float fgv = ghk_flux_f(gg, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], k.dgj_gs[i] * gw, k.inv_gjl);
-        const float a = f * sa;
-        sm.sA[i][t] = a;
+        const float fgv = ghk_flux_fk(gg, ka_g, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], k.dgj_gs[i] * gw, k.inv_gjl);
+        sm.sA[i][t] = f * sa;
         sm.sB[i][t] = -fgv * sa;
-        env_acc[i] = a;
       }
     } else {
 #pragma unroll
       for (int i = 0; i < NI; ++i) if (i < I) { sm.sA[i][t] = 0.f; sm.sB[i][t] = 0.f; }
     }
-#pragma unroll
-    for (int i = 0; i < NI; ++i) {
-      if (i >= I) break;
-      float s = env_acc[i];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if (lane == 0) sm.red[i][wid] = s;
-    }
     __syncthreads();
-    if (t < I) {
-      float s = 0.f;
-#pragma unroll
-      for (int w = 0; w < TPB / 32; ++w) s += sm.red[t][w];
-      p.env_part[(size_t)tile * I + t] = s;
-    }
     // cells: warp = ion, lane = cell (update_all_concs)
     int bad = 0, neg = 0;
     const short2 rng = st.rng[lane];
+    float s1 = 0.f;
+    if (wid < I) {
+      for (int jj = rng.x; jj < rng.y; ++jj) s1 += sm.sA[wid][jj];
+      float e = s1;                  // per-tile partial sum of f_mem*sa of this ion
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+      if (lane == 0) p.env_part[(size_t)tile * I + wid] = e;
+    }
     if (wid < I && rng.y > rng.x) {
       const int i = wid;
-      float s1 = 0.f, s2 = 0.f;
-      for (int jj = rng.x; jj < rng.y; ++jj) { s1 += sm.sA[i][jj]; s2 += sm.sB[i][jj]; }
+      float s2 = 0.f;
+      for (int jj = rng.x; jj < rng.y; ++jj) s2 += sm.sB[i][jj];
       const float dtv = st.dtv[lane];
       const float2 x2 = st.cc2[i][lane];
       df x{x2.x, x2.y};

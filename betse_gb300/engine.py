@@ -150,6 +150,12 @@ class ClusterEngine:
         _lib.check(self.lib.bx_set_launch_config(self.h, int(tpb), int(bool(persistent))),
                    'bx_set_launch_config')
 
+    def launch_config(self):
+        """(threads per CTA, persistent kernel) in use."""
+        tpb, per = ct.c_int(), ct.c_int()
+        _lib.check(self.lib.bx_get_launch_config(self.h, ct.byref(tpb), ct.byref(per)), 'bx_get_launch_config')
+        return tpb.value, bool(per.value)
+
     def autotune(self, n_steps=20):
         """Pick the fastest CTA size for this cluster; the state is unchanged.
         Returns (threads per CTA, ms per step)."""

@@ -256,6 +256,7 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
  * 256 membrane slots) and, for the split form, the persistent pipelined
  * kernel.  The state is kept.  bx_autotune picks these by timing. */
 int bx_set_launch_config(bx_handle h, int tpb, int persistent);
+int bx_get_launch_config(bx_handle h, int* tpb, int* persistent);
 
 /* Autotuner: times n_steps steps for each launch configuration (CTA size,
  * and for the split form tile-per-CTA or persistent pipelined kernel) on the
