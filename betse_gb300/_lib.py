@@ -94,7 +94,10 @@ SIGNATURES = {
     'bx_step': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p]),
     'bx_outputs_download': (ct.c_int, [ct.c_void_p, ct.POINTER(BxOutputs)]),
     'bx_status': (ct.c_int, [ct.c_void_p, ct.POINTER(BxStepStatus)]),
+    'bx_set_lap_env_inv': (ct.c_int, [ct.c_void_p, _dp]),
     'bx_env_fields': (ct.c_int, [ct.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    'bx_time_env_fields': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_double),
+                                      ct.POINTER(ct.c_double)]),
     'bx_dense_apply_f64': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int,
                                       ct.c_int, ct.c_void_p]),
     'bx_abi_version': (ct.c_int, []),

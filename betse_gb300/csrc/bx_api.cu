@@ -23,6 +23,7 @@
 
 #include "../../include/bx.h"
 #include "bx_env.cuh"
+#include "bx_fields.cuh"
 #include "bx_launch.cuh"
 #include "bx_split.cuh"
 
@@ -128,6 +129,12 @@ struct bx_cluster {
   bool graph_valid = false;
   std::vector<int> h_cell_ptr, h_m2c, h_map_env;
   std::vector<double> h_phib;
+  // ---- environment fields on demand (bx_env_fields)
+  float2* f_lap = nullptr;         // lapENVinv as double-float pairs [G][G]
+  float2* f_X = nullptr;           // two-column right-hand side [G][2]
+  double* f_buf = nullptr;         // field scratch, kFieldBufs x [G]
+  int* f_last = nullptr;           // last membrane of each grid cell (-1: none)
+  bool last_step_outputs = false;  // the latest bx_step computed outputs
 };
 
 namespace {
@@ -145,7 +152,8 @@ void free_all(bx_cluster* h) {
       h->d_mem_flux_sa, h->d_pump, h->d_env_scale, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy,
       h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
-      h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem};
+      h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
+      h->f_lap, h->f_X, h->f_buf, h->f_last};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->graph) cudaGraphExecDestroy(h->graph);
@@ -999,6 +1007,7 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
   }
   h->have_state = true;
   h->have_outputs = false;
+  h->last_step_outputs = false;
   return BX_OK;
 }
 
@@ -1109,6 +1118,7 @@ int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream) {
   }
   h->steps_done += n_steps;
   if (want_outputs) h->have_outputs = true;
+  h->last_step_outputs = want_outputs != 0;
   if (s != h->stream) {
     BX_CU(cudaEventRecord(ev, s));
     BX_CU(cudaStreamWaitEvent(h->stream, ev, 0));
@@ -1298,11 +1308,173 @@ int bx_dense_apply_f64(const double* A, const double* x, double* y, int n, int n
   return BX_OK;
 }
 
-int bx_env_fields(bx_handle h, const double* lap_env_inv, double* v_env, double* E_env_x, double* E_env_y,
+int bx_set_lap_env_inv(bx_handle h, const double* lap_env_inv) {
+  if (!h || !lap_env_inv) return fail(BX_EINVAL, "null argument");
+  if (h->ncl != 1) return fail(BX_EINVAL, "bx_set_lap_env_inv: single-cluster handles only");
+  const size_t G = (size_t)h->G;
+  if (!h->f_lap && cudaMalloc(&h->f_lap, G * G * sizeof(float2)) != cudaSuccess) {
+    h->f_lap = nullptr;
+    cudaGetLastError();
+    return fail(BX_ENOMEM, "cudaMalloc lapENVinv");
+  }
+  // stream the FP64 rows through a bounded staging buffer, splitting on device
+  const size_t rows_per = std::max<size_t>(1, std::min<size_t>(G, ((size_t)64 << 20) / (G * sizeof(double))));
+  double* stage = nullptr;
+  if (cudaMalloc(&stage, rows_per * G * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(BX_ENOMEM, "cudaMalloc staging");
+  }
+  int rc = BX_OK;
+  for (size_t r0 = 0; r0 < G && rc == BX_OK; r0 += rows_per) {
+    const size_t nr = std::min(rows_per, G - r0);
+    cudaError_t e = cudaMemcpyAsync(stage, lap_env_inv + r0 * G, nr * G * sizeof(double), cudaMemcpyHostToDevice,
+                                    h->stream);
+    if (e == cudaSuccess) {
+      const size_t n = nr * G;
+      const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)h->sm_count * 16);
+      bx::k_to_df<<<blocks, 256, 0, h->stream>>>(stage, h->f_lap + r0 * G, n);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) rc = fail(BX_ECUDA, std::string("lapENVinv upload: ") + cudaGetErrorString(e));
+  }
+  cudaFree(stage);
+  return rc;
+}
+
+namespace {
+
+constexpr int kFieldBufs = 14;
+
+bx::FieldGrid field_grid(const bx_cluster* h) {
+  bx::FieldGrid g{};
+  g.ny = h->ny;
+  g.nx = h->nx;
+  g.G = h->G;
+  g.delta = h->delta;
+  const bx::EnvConst e = make_env_const(h);
+  for (int q = 0; q < 9; ++q) g.gw[q] = e.gw[q];
+  return g;
+}
+
+// Enqueue the environment fields of the last step on the handle's stream;
+// results in f_buf slots 0..5 = v_env, E_env_x, E_env_y, J_env_x, J_env_y, B_field.
+int enqueue_env_fields(bx_cluster* h, const double* d_w) {
+  const int G = h->G;
+  const bx::FieldGrid fg = field_grid(h);
+  cudaStream_t s = h->stream;
+  double* b[kFieldBufs];
+  for (int q = 0; q < kFieldBufs; ++q) b[q] = h->f_buf + (size_t)q * G;
+  double *venv = b[0], *Ex = b[1], *Ey = b[2], *Jex = b[3], *Jey = b[4], *Bf = b[5];
+  double *t0 = b[6], *t1 = b[7], *t2 = b[8], *t3 = b[9], *Y = b[10];  // Y spans b[10], b[11]
+  double *jx = b[12], *jy = b[13];
+  const unsigned gg = (unsigned)((G + 255) / 256);
+  const unsigned rows = (unsigned)(((size_t)G * 32 + 255) / 256);
+  if (!h->ecm) {
+    const double* vm = (h->mode == MODE_SPLIT) ? h->o_vm_mem : h->d_vm[h->parity ^ 1];
+    bx::k_fields_vce<<<gg, 256, 0, s>>>(G, h->f_last, h->d_m2c, vm, t0);
+    bx::k_fields_gauss<true><<<gg, 256, 0, s>>>(t0, t1, 0, fg);
+    bx::k_fields_gauss<true><<<gg, 256, 0, s>>>(t1, venv, 1, fg);
+    // smooth_flux(gradient(delta * Phi)) (ion_current.py:133-136)
+    bx::k_fields_grad<<<gg, 256, 0, s>>>(venv, h->delta, t0, t1, fg);
+    bx::k_fields_hh_rhs<<<gg, 256, 0, s>>>(t0, t1, h->f_X, fg);
+    bx::k_dense_rows_df<2><<<rows, 256, 0, s>>>(h->f_lap, h->f_X, Y, G);
+    bx::k_fields_hh_out<<<gg, 256, 0, s>>>(Y, 1.0, nullptr, t0, t1, t2, t3, fg);
+    bx::k_fields_e_and_j<<<gg, 256, 0, s>>>(G, t0, t1, t2, t3, d_w, h->par.sigma, Ex, Ey, jx, jy);
+  } else {
+    BX_CU(cudaMemcpyAsync(venv, h->d_venv, (size_t)G * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    BX_CU(cudaMemcpyAsync(Ex, h->d_Ex, (size_t)G * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    BX_CU(cudaMemcpyAsync(Ey, h->d_Ey, (size_t)G * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    bx::ZF zf{};
+    for (int i = 0; i < h->I; ++i) zf.v[i] = h->par.zs[i] * h->par.F;
+    bx::k_fields_zf_sum<<<gg, 256, 0, s>>>(G, h->I, h->d_fx, h->d_fy, zf, jx, jy);
+  }
+  // J_env, B_field: Helmholtz-Hodge split of the current (ion_current.py:70, 147)
+  bx::k_fields_hh_rhs<<<gg, 256, 0, s>>>(jx, jy, h->f_X, fg);
+  bx::k_dense_rows_df<2><<<rows, 256, 0, s>>>(h->f_lap, h->f_X, Y, G);
+  bx::k_fields_hh_out<<<gg, 256, 0, s>>>(Y, h->par.mu, Bf, Jex, Jey, nullptr, nullptr, fg);
+  BX_CU(cudaGetLastError());
+  return BX_OK;
+}
+
+int prepare_env_fields(bx_cluster* h, const double* D_env_weight, double** d_w) {
+  if (h->ncl != 1) return fail(BX_EINVAL, "bx_env_fields: single-cluster handles only");
+  if (!h->f_lap) return fail(BX_ESTATE, "bx_env_fields before bx_set_lap_env_inv");
+  if (!h->last_step_outputs) return fail(BX_ESTATE, "bx_env_fields needs a last bx_step with want_outputs");
+  const size_t G = (size_t)h->G;
+  if (!h->f_buf) {
+    if (cudaMalloc(&h->f_buf, (kFieldBufs + 1) * G * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->f_X, 2 * G * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&h->f_last, G * sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(BX_ENOMEM, "cudaMalloc field scratch");
+    }
+    std::vector<int> last(G, -1);
+    for (int m = 0; m < h->M; ++m) last[h->h_map_env[m]] = m;  // numpy keeps the last repeat
+    BX_CU(cudaMemcpy(h->f_last, last.data(), G * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  *d_w = nullptr;
+  if (D_env_weight) {
+    double* w = h->f_buf + (size_t)kFieldBufs * G;  // the spare slot
+    BX_CU(cudaMemcpyAsync(w, D_env_weight, G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    *d_w = w;
+  }
+  return BX_OK;
+}
+
+}  // namespace
+
+int bx_env_fields(bx_handle h, const double* D_env_weight, double* v_env, double* E_env_x, double* E_env_y,
                   double* J_env_x, double* J_env_y, double* B_field) {
-  (void)lap_env_inv; (void)v_env; (void)E_env_x; (void)E_env_y; (void)J_env_x; (void)J_env_y; (void)B_field;
   if (!h) return fail(BX_EINVAL, "null handle");
-  return fail(BX_EINVAL, "bx_env_fields: not available in this build");
+  double* d_w = nullptr;
+  int rc = prepare_env_fields(h, D_env_weight, &d_w);
+  if (rc != BX_OK) return rc;
+  rc = enqueue_env_fields(h, d_w);
+  if (rc != BX_OK) return rc;
+  const size_t G = (size_t)h->G;
+  double* dst[6] = {v_env, E_env_x, E_env_y, J_env_x, J_env_y, B_field};
+  for (int q = 0; q < 6; ++q)
+    if (dst[q])
+      BX_CU(cudaMemcpyAsync(dst[q], h->f_buf + (size_t)q * G, G * sizeof(double), cudaMemcpyDeviceToHost,
+                            h->stream));
+  BX_CU(cudaStreamSynchronize(h->stream));
+  return BX_OK;
+}
+
+int bx_time_env_fields(bx_handle h, int n, double* ms_fields, double* ms_product) {
+  if (!h || n <= 0 || !ms_fields || !ms_product) return fail(BX_EINVAL, "bad arguments");
+  double* d_w = nullptr;
+  int rc = prepare_env_fields(h, nullptr, &d_w);
+  if (rc != BX_OK) return rc;
+  cudaEvent_t e0, e1, e2;
+  BX_CU(cudaEventCreate(&e0));
+  BX_CU(cudaEventCreate(&e1));
+  BX_CU(cudaEventCreate(&e2));
+  const int G = h->G;
+  const unsigned rows = (unsigned)(((size_t)G * 32 + 255) / 256);
+  double tf = 0.0, tp = 0.0;
+  for (int q = 0; q < n; ++q) {
+    BX_CU(cudaEventRecord(e0, h->stream));
+    rc = enqueue_env_fields(h, d_w);
+    if (rc != BX_OK) break;
+    BX_CU(cudaEventRecord(e1, h->stream));
+    bx::k_dense_rows_df<2><<<rows, 256, 0, h->stream>>>(h->f_lap, h->f_X, h->f_buf + (size_t)10 * G, G);
+    BX_CU(cudaEventRecord(e2, h->stream));
+    BX_CU(cudaEventSynchronize(e2));
+    float a = 0.f, b = 0.f;
+    BX_CU(cudaEventElapsedTime(&a, e0, e1));
+    BX_CU(cudaEventElapsedTime(&b, e1, e2));
+    tf += a;
+    tp += b;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  if (rc != BX_OK) return rc;
+  *ms_fields = tf / n;
+  *ms_product = tp / n;
+  return BX_OK;
 }
 
 }  // extern "C"

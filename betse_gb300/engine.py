@@ -124,6 +124,33 @@ class ClusterEngine:
         _lib.check(self.lib.bx_outputs_download(self.h, ct.byref(o)), 'bx_outputs_download')
         return arrs
 
+    def set_lap_env_inv(self, lap_env_inv):
+        """Keep ``cells.lapENVinv`` ([grid, grid]) on the GPU for ``env_fields``."""
+        A = _c(lap_env_inv)
+        if A.shape != (self.G, self.G):
+            raise ValueError(f'lapENVinv must be ({self.G}, {self.G})')
+        _lib.check(self.lib.bx_set_lap_env_inv(self.h, _lib.dptr(A)), 'bx_set_lap_env_inv')
+
+    def env_fields(self, D_env_weight=None):
+        """Environment fields of the last step (which ran with ``outputs=True``):
+        v_env, E_env_x/y, J_env_x/y, B_field, each of length grid."""
+        G = self.G
+        w = None if D_env_weight is None else _c(D_env_weight).ravel()
+        if w is not None and w.shape != (G,):
+            raise ValueError(f'D_env_weight must have {G} values')
+        names = ('v_env', 'E_env_x', 'E_env_y', 'J_env_x', 'J_env_y', 'B_field')
+        out = {k: np.empty(G) for k in names}
+        _lib.check(self.lib.bx_env_fields(self.h, _lib.dptr(w), *[_lib.dptr(out[k]) for k in names]),
+                   'bx_env_fields')
+        return out
+
+    def time_env_fields(self, n=5):
+        """(ms of the whole field computation, ms of one two-column lapENVinv product)."""
+        a, b = ct.c_double(), ct.c_double()
+        _lib.check(self.lib.bx_time_env_fields(self.h, int(n), ct.byref(a), ct.byref(b)),
+                   'bx_time_env_fields')
+        return a.value, b.value
+
     def status(self):
         st = _lib.BxStepStatus()
         _lib.check(self.lib.bx_status(self.h, ct.byref(st)), 'bx_status')

@@ -36,6 +36,7 @@
  *                       sigma_cell.
  *   bx_status           stb.check_v (sim_toolbox.py:332-344) and stb.no_negs
  *                       (sim_toolbox.py:475-503): NaN and clamp counters.
+ *   bx_set_lap_env_inv  cells.lapENVinv (cells.py:503-504), kept on the GPU
  *   bx_env_fields       get_current's environment branches
  *                       (physics/ion_current.py:50-171): v_env, E_env_x/y,
  *                       J_env_x/y, B_field with dense lapENVinv products.
@@ -205,13 +206,26 @@ int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream);
 int bx_outputs_download(bx_handle h, bx_outputs* o);
 int bx_status(bx_handle h, bx_step_status* st);
 
-/* Environment fields of get_current for the current state (outputs only
- * except E_env with ECM): v_env, E_env_x/y, J_env_x/y, B_field [grid].
- * lap_env_inv is the dense [grid x grid] row-major lapENVinv, copied to the
- * device on first use (pass NULL afterwards to reuse it). */
-int bx_env_fields(bx_handle h, const double* lap_env_inv, double* v_env,
+/* Dense lapENVinv ([grid x grid] row-major FP64, host) for bx_env_fields:
+ * cells.lapENVinv (cells.py:503-504, the pinv of
+ * FiniteDiffSolver.makeLaplacian, finitediff.py:252-431).  Stored on the GPU
+ * once as double-float (hi, lo) FP32 pairs; single-cluster handles only. */
+int bx_set_lap_env_inv(bx_handle h, const double* lap_env_inv);
+
+/* Environment fields of get_current (physics/ion_current.py:50-171) for the
+ * last step, which must have run with want_outputs: v_env, E_env_x/y,
+ * J_env_x/y and B_field, each [grid], any pointer NULL to skip.  Without ECM
+ * they come from that step's start-of-step Vmem (Gaussian LFP, smooth_flux,
+ * sigma*E*D_env_weight, HH_Decomp: sim_toolbox.py:1236-1333); with ECM v_env
+ * and E_env are the step's own and J_env/B_field come from the grid fluxes.
+ * D_env_weight [grid] (sim.D_env_weight; NULL = 1) weights the no-ECM current.
+ * Boundary voltages are zero (sim.bound_V, sim.py:702-706).  Synchronous. */
+int bx_env_fields(bx_handle h, const double* D_env_weight, double* v_env,
                   double* E_env_x, double* E_env_y, double* J_env_x,
                   double* J_env_y, double* B_field);
+/* Diagnostics: mean duration of bx_env_fields' device work and of one
+ * two-column lapENVinv product over n runs (CUDA events). */
+int bx_time_env_fields(bx_handle h, int n, double* ms_fields, double* ms_product);
 
 /* Dense products y[n x nrhs] = A[n x n] @ x[n x nrhs] (row-major, FP64) on the
  * GPU, device pointers; the kernel BETSE's lapENVinv / lapGJinv matvecs use. */

@@ -1,0 +1,111 @@
+"""The ``_run_sim_core_loop`` drop-in on the GPU against BETSE's results.
+
+A stand-in Simulator carries the golden fixture's initial state under BETSE's
+attribute names; the drop-in runs the loop with two sampled time steps (the
+fixture's checkpoints) and ``write2storage`` records what BETSE would store.
+Tolerances are those of the step and field parity tests.
+"""
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+import golden_io as gi
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+class _Sim:
+    def __init__(self):
+        self.stored = []
+
+    def write2storage(self, t, cells, p):
+        self.stored.append(dict(t=t, vm=self.vm.copy(), cc_cells=self.cc_cells.copy(),
+                                cc_env=np.copy(self.cc_env), v_env=np.copy(self.v_env),
+                                E_env_x=np.copy(self.E_env_x), J_env_x=np.copy(self.J_env_x),
+                                I_mem=self.I_mem.copy(), rho_cells=self.rho_cells.copy(),
+                                vm_ave=np.copy(self.vm_ave), E_gj_x=self.E_gj_x.copy(),
+                                B_field=np.copy(self.B_field)))
+
+
+class _Callbacks:
+    def __init__(self):
+        self.n = 0
+
+    def progressed_next(self):
+        self.n += 1
+
+
+def _fixture_sim(d):
+    g, p, s0 = gi.geometry(d), gi.params(d), gi.state(d)
+    I = len(p.zs)
+    sim = _Sim()
+    sim.zs, sim.D_free, sim.D_gj = p.zs, p.D_free, p.D_gj
+    sim.iNa, sim.iK, sim.T = p.iNa, p.iK, p.T
+    sim.ko_env = float(getattr(g, 'ko_env', 0.0))
+    sim.sigma = g.sigma
+    sim.c_env_bound = getattr(p, 'c_env_bound', np.zeros(I))
+    sim.smooth_weight_mem, sim.smooth_weight_o = g.smooth_weight_mem, g.smooth_weight_o
+    sim.D_env_weight = g.D_env_weight
+    sim.Dm_cells = p.Dm.copy()
+    sim.vm, sim.cc_cells, sim.cc_at_mem = s0.vm.copy(), s0.cc_cells.copy(), s0.cc_at_mem.copy()
+    sim.cc_env = np.asarray(d['init_cc_env']).copy()
+    sim.Phi_b = np.zeros(int(np.prod(g.grid_shape)))
+    if p.is_ecm:
+        sim.E_env_x, sim.E_env_y = s0.E_env_x, s0.E_env_y
+        sim.D_env = g.D_env
+        sim.TJ_modulator = np.ones_like(g.D_env)
+    g.lapENVinv = np.linalg.pinv(oracle.fields.make_laplacian(*g.grid_shape, g.delta))
+    phase = SimpleNamespace(p=p, cells=g, kind=SimpleNamespace(name='INIT'), callbacks=_Callbacks())
+    return sim, phase
+
+
+@pytest.mark.parametrize('name', gi.CASES)
+@pytest.mark.parametrize('precision', ['fp64', 'split'])
+def test_run_sim_core_loop_matches_betse(name, precision):
+    from betse_gb300.simulator import run_sim_core_loop
+    d = gi.load(name)
+    ecm = bool(d['par_is_ecm'])
+    if ecm and precision == 'split':
+        pytest.skip('split form with ECM is covered by the step tests')
+    sim, phase = _fixture_sim(d)
+    cps = [int(c) for c in d['meta_checkpoints'][:2]]
+    n = cps[-1] + 3
+    ts = np.arange(n) * phase.p.dt
+    sampled = {ts[c - 1] for c in cps}
+    run_sim_core_loop(sim, phase, ts, sampled, None, precision=precision)
+    assert phase.callbacks.n == 2 and len(sim.stored) == 2
+    for rec, cp in zip(sim.stored, cps):
+        assert rec['t'] == ts[cp - 1]
+        if precision == 'fp64':
+            ok, err, bound = gi.vm_err_ok(d, rec['vm'], d[f's{cp}_vm'], d[f's{cp}_cc_cells'])
+            assert ok, (cp, err, bound)
+            assert gi.rel_err(rec['cc_cells'], d[f's{cp}_cc_cells']) < 1e-10
+            assert gi.rel_err(rec['cc_env'], d[f's{cp}_cc_env']) < 1e-10
+        else:
+            assert np.max(np.abs(rec['vm'] - d[f's{cp}_vm'])) < 1e-6
+        assert rec['cc_env'].shape == np.asarray(d[f's{cp}_cc_env']).shape
+        if cp == cps[1]:
+            # outputs and fields of that step (the fixture keeps them at two checkpoints)
+            vfl = gi.vm_floor(d, d[f's{cp}_cc_cells'])
+            tol_v = 1e-6 if precision == 'split' else 1e-10 * np.max(np.abs(d[f's{cp}_v_env'])) + vfl
+            assert np.max(np.abs(rec['v_env'] - np.ravel(d[f's{cp}_v_env']))) <= tol_v
+            assert rec['E_env_x'].shape == np.asarray(d[f's{cp}_E_env_x']).shape
+            if precision == 'fp64':
+                assert gi.rel_err(rec['E_env_x'], d[f's{cp}_E_env_x']) < 1e-8
+                assert gi.rel_err(rec['rho_cells'], d[f's{cp}_rho_cells']) < 1e-10
+    # after the loop the attributes hold the last step
+    assert sim.vm.shape == rec['vm'].shape and not np.array_equal(sim.vm, sim.stored[-1]['vm'])
+
+
+def test_run_sim_core_loop_raises_unstable():
+    from betse_gb300.exceptions import BetseSimUnstableException
+    from betse_gb300.simulator import run_sim_core_loop
+    d = gi.load('noecm_r20_s2')
+    sim, phase = _fixture_sim(d)
+    sim.cc_cells[0, 3] = np.nan
+    ts = np.arange(4) * phase.p.dt
+    with pytest.raises(BetseSimUnstableException):
+        run_sim_core_loop(sim, phase, ts, {ts[2]}, None)
+    assert sim.stored == []
