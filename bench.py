@@ -51,6 +51,11 @@ WORKLOADS = {
     'plain250': dict(radius=80e-6, seed=1, is_ecm=False, dt=1e-2, dm=(1e-19, 1e-17),
                      time_steps=2000, grid_size=20,
                      desc='plain FP64 reference step, ~250 cells, no ECM, 2000 steps'),
+    'ecm20k': dict(radius=662e-6, seed=11, is_ecm=True, dt=5e-3, dm=(1e-19, 1e-17),
+                   time_steps=500, grid_size=200, cell_space=25e-9,
+                   desc='extracellular spaces: ~20k-cell jittered-hex Voronoi cluster (~123k '
+                        'membranes), 199x200 environment grid, cell_space 25 nm, Dm log-uniform '
+                        '[1e-19,1e-17], dt 5e-3 s, 500 steps per run'),
     'sweep512': dict(sweep=True, n_clusters=512, seed=7, dt=5e-3, dm=(1e-19, 1e-17),
                      time_steps=1000,
                      desc='batched sweep: 512 independent clusters, cells log-uniform [200,5000], '
@@ -133,7 +138,8 @@ def build_workload(name):
                                               dm_range=w['dm'])
         return w, gs, ps, Dms, sts, None
     g, p, Dm, st, D_env = gen.workload(w['radius'], w['seed'], is_ecm=w['is_ecm'], dt=w['dt'],
-                                       dm_range=w['dm'], grid_size=w['grid_size'])
+                                       dm_range=w['dm'], grid_size=w['grid_size'],
+                                       cell_space=w.get('cell_space', 26e-9))
     return w, g, p, Dm, st, D_env
 
 
@@ -166,30 +172,12 @@ class Sweep:
                 'cc_env': np.concatenate([x['cc_env'] for x in d])}
 
 
-def cpu_baseline(g, p, Dm, st, budget_s=12.0):
+def cpu_baseline(g, p, Dm, st, budget_s=12.0, D_env=None):
     """Oracle (NumPy restatement of BETSE's step) on a bounded sample: whole
     cluster, as many time steps as fit in about budget_s seconds."""
     import oracle
-    from types import SimpleNamespace
-    geo = SimpleNamespace(**{k: getattr(g, k) for k in (
-        'mem_to_cells', 'nn_i', 'map_mem2ecm', 'mem_sa', 'mem_nx', 'mem_ny', 'cell_vol',
-        'cell_sa', 'diviterm', 'num_mems', 'smooth_weight_mem', 'smooth_weight_o', 'delta',
-        'gj_len', 'cell_mem_ptr')})
-    geo.bflag = g.bflag.astype(bool)
-    geo.gj_weight = g.gj_weight
-    geo.grid_shape = tuple(g.grid_shape)
-    geo.mem_to_cells = g.mem_to_cells.astype(np.int64)
-    geo.nn_i = g.nn_i.astype(np.int64)
-    par = SimpleNamespace(**{k: getattr(p, k) for k in (
-        'F', 'R', 'T', 'dt', 'cm', 'tm', 'gj_surface', 'alpha_NaK', 'KmNK_Na', 'KmNK_K',
-        'KmNK_ATP', 'cATP', 'cADP', 'cPi', 'deltaGATP', 'vol_env', 'zs', 'D_free', 'D_gj',
-        'iNa', 'iK', 'is_ecm', 'gj_block', 'nakatp_block')})
-    par.Dm = Dm
-    I, M = Dm.shape
-    ce = np.repeat(np.asarray(st['cc_env'], np.float64)[:, None], M, axis=1)
-    s = oracle.OracleState(vm=st['vm'].copy(), cc_cells=st['cc_cells'].copy(),
-                           cc_at_mem=st['cc_at_mem'].copy(), cc_env=ce,
-                           Phi_b=np.zeros(g.n_grid))
+    from oracle.adapt import from_workload
+    geo, par, s = from_workload(g, p, Dm, st, D_env)
     t0 = time.perf_counter()
     oracle.step(geo, par, s)
     one = time.perf_counter() - t0
@@ -203,11 +191,67 @@ def cpu_baseline(g, p, Dm, st, budget_s=12.0):
                       f'cluster ({dt:.1f} s), NumPy oracle, one thread'}
 
 
+def secondary(stream, flush):
+    """Extra lines of evidence at N=1: the ECM workload's step rates and the
+    environment-field products at its full grid (output-only, sampled steps)."""
+    import torch
+    from betse_gb300.engine import ClusterEngine
+    w, g, p, Dm, st, D_env = build_workload('ecm20k')
+    T = 100
+    out = {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems,
+           'grid': list(g.grid_shape), 'time_steps_timed': T}
+    for prec in ('fp64', 'split'):
+        e = ClusterEngine(g, p, prec)
+        e.set_membrane_diffusivity(Dm)
+        e.set_env_diffusivity(D_env)
+        e.upload(**st)
+        e.step(T, stream=stream.cuda_stream)
+        ms = []
+        for _ in range(3):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            e.step(T, stream=stream.cuda_stream)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        e.check_stable()
+        out[prec] = {'value': g.n_mems * T / (min(ms) / 1e3), 'unit': UNIT,
+                     'ms_per_time_step': min(ms) / T}
+        if prec == 'fp64':
+            fields_eng = e
+        else:
+            e.close()
+    # the dense lapENVinv products: 8*G^2 bytes per product (the operator, once)
+    G = g.n_grid
+    phys = os.sysconf('SC_PHYS_PAGES') * os.sysconf('SC_PAGE_SIZE')
+    if phys < 4 * 8 * G * G:
+        out['env_fields'] = {'skipped': f'host memory {phys >> 30} GiB too small for the operator'}
+    else:
+        A = np.empty((G, G))
+        A.fill(1e-12)  # timing only: the products stream the operator whatever it holds
+        fields_eng.set_lap_env_inv(A)
+        del A
+        fields_eng.step(1, outputs=True)
+        ms_f, ms_p = fields_eng.time_env_fields(5)
+        hbm, src = peaks()
+        gbs = 8.0 * G * G / (ms_p / 1e3) / 1e9
+        out['env_fields'] = {
+            'operator': f'synthetic dense {G}x{G} (lapENVinv size), double-float storage',
+            'ms_per_sampled_step': ms_f, 'product_ms': ms_p, 'products_per_sample': 1,
+            'roofline': {'bound': 'hbm', 'achieved': gbs, 'peak': hbm, 'unit': 'GB/s',
+                         'frac': gbs / hbm, 'algorithmic_bytes_per_launch': 8 * G * G,
+                         'kernel': 'k_dense_rows_df<2>', 'peak_source': src}}
+    fields_eng.close()
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU restatement of BETSE's step on the host cores."""
     if rank != 0:
         return
-    w, g, p, Dm, st, _ = build_workload(args.workload)
+    w, g, p, Dm, st, D_env = build_workload(args.workload)
     budget = float(os.environ.get('BX_REF_BUDGET_S', '6'))
     n_cells, n_mems = (sum(x.n_cells for x in g), sum(x.n_mems for x in g)) if w.get('sweep') \
         else (g.n_cells, g.n_mems)
@@ -215,7 +259,7 @@ def run_reference(args, rank, world):
         g, p, Dm, st = g[0], p[0], Dm[0], st[0]
     samples = []
     for k in range(args.warmup + args.steps):
-        r = cpu_baseline(g, p, Dm, st, budget_s=budget)
+        r = cpu_baseline(g, p, Dm, st, budget_s=budget, D_env=None if w.get('sweep') else D_env)
         if k >= args.warmup:
             samples.append(r['value'])
     v = statistics.mean(samples)
@@ -234,13 +278,15 @@ def profile_run(args):
     """A short, deterministic launch sequence for ncu captures."""
     from betse_gb300.build import build
     build()
-    w, g, p, Dm, st, _ = build_workload(args.workload)
+    w, g, p, Dm, st, D_env = build_workload(args.workload)
     if w.get('sweep'):
         e = Sweep(g, p, Dm, st, args.precision)
     else:
         from betse_gb300.engine import ClusterEngine
         e = ClusterEngine(g, p, args.precision)
         e.set_membrane_diffusivity(Dm)
+        if D_env is not None:
+            e.set_env_diffusivity(D_env)
         e.upload(**st)
     e.step(4)
     e.check_stable()
@@ -257,6 +303,8 @@ def main():
     ap.add_argument('--workload', default='cluster100k', choices=sorted(WORKLOADS))
     ap.add_argument('--time-steps', type=int, default=None)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-secondary', action='store_true',
+                    help='skip the ECM workload and environment-field measurements')
     ap.add_argument('--profile-run', action='store_true',
                     help='for ncu: build the workload, upload it, run 4 eager steps, exit')
     ap.add_argument('--precision', default='split', choices=['split', 'fp64'])
@@ -295,6 +343,8 @@ def main():
             return Sweep(g, p, Dm, st, prec)
         e = ClusterEngine(g, p, prec)
         e.set_membrane_diffusivity(Dm)
+        if D_env is not None:
+            e.set_env_diffusivity(D_env)
         e.upload(**st)
         return e
 
@@ -407,7 +457,10 @@ def main():
             cpu = cpu_baseline(g[0], p[0], Dm[0], st[0])
             cpu['sample'] += ' (cluster 0 of the sweep)'
         else:
-            cpu = cpu_baseline(g, p, Dm, st)
+            cpu = cpu_baseline(g, p, Dm, st, D_env=D_env)
+    extra = None
+    if rank == 0 and world == 1 and args.workload == 'cluster100k' and not args.no_secondary:
+        extra = secondary(stream, flush)
 
     if rank == 0:
         line = {
@@ -436,6 +489,8 @@ def main():
             'gpu_launches': int(launches),
             'clocks': clk,
         }
+        if extra is not None:
+            line['secondary'] = extra
         print(json.dumps(line), flush=True)
     for e in (split, plain, e_s):
         e.close()
