@@ -95,6 +95,14 @@ SIGNATURES = {
     'bx_outputs_download': (ct.c_int, [ct.c_void_p, ct.POINTER(BxOutputs)]),
     'bx_status': (ct.c_int, [ct.c_void_p, ct.POINTER(BxStepStatus)]),
     'bx_set_lap_env_inv': (ct.c_int, [ct.c_void_p, _dp]),
+    'bx_dense_op_create': (ct.c_int, [_dp, ct.c_int, ct.POINTER(ct.c_void_p)]),
+    'bx_dense_op_set_forward': (ct.c_int, [ct.c_void_p, _ip, _ip, _dp]),
+    'bx_dense_op_apply': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p,
+                                     ct.c_int, ct.c_void_p]),
+    'bx_dense_op_status': (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int)]),
+    'bx_dense_op_time': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
+                                    ct.POINTER(ct.c_double)]),
+    'bx_dense_op_destroy': (ct.c_int, [ct.c_void_p]),
     'bx_env_fields': (ct.c_int, [ct.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     'bx_time_env_fields': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_double),
                                       ct.POINTER(ct.c_double)]),

@@ -37,6 +37,9 @@
  *   bx_status           stb.check_v (sim_toolbox.py:332-344) and stb.no_negs
  *                       (sim_toolbox.py:475-503): NaN and clamp counters.
  *   bx_set_lap_env_inv  cells.lapENVinv (cells.py:503-504), kept on the GPU
+ *   bx_dense_op_*       np.dot(cells.lapGJinv | cells.lapENVinv, block of
+ *                       right-hand sides) on tcgen05 (pressures.py:59,
+ *                       ion_current.py:90,170)
  *   bx_env_fields       get_current's environment branches
  *                       (physics/ion_current.py:50-171): v_env, E_env_x/y,
  *                       J_env_x/y, B_field with dense lapENVinv products.
@@ -231,6 +234,28 @@ int bx_time_env_fields(bx_handle h, int n, double* ms_fields, double* ms_product
  * GPU, device pointers; the kernel BETSE's lapENVinv / lapGJinv matvecs use. */
 int bx_dense_apply_f64(const double* A, const double* x, double* y, int n,
                        int nrhs, void* stream);
+
+/* Dense operator products on the tensor cores, for right-hand sides that
+ * batch: Y = A X with A [n x n] (np.dot(cells.lapGJinv, .), pressures.py:59;
+ * np.dot(cells.lapENVinv, .), ion_current.py:90,170) applied to nrhs columns.
+ * A is split once into BF16 hi/lo planes (BF16x3 products, FP32 accumulation
+ * in TMEM, tcgen05); bx_dense_op_set_forward gives the operator L that A
+ * inverts (CSR, FP64) and enables one refinement step Y += A (X - L Y).
+ * X, Y, col_scale are DEVICE pointers: X, Y [n x nrhs] row-major FP64,
+ * col_scale [nrhs] (NULL = 1) multiplies column j of the result (e.g. the
+ * delta^2 of clusters that share a grid-shape operator).  Asynchronous on
+ * `stream`; bx_dense_op_status synchronises and reports a pipeline timeout. */
+typedef struct bx_dense_op* bx_dense_op_handle;
+int bx_dense_op_create(const double* A, int n, bx_dense_op_handle* out);  /* host A */
+int bx_dense_op_set_forward(bx_dense_op_handle op, const int32_t* row_ptr,
+                            const int32_t* col, const double* val);      /* host CSR */
+int bx_dense_op_apply(bx_dense_op_handle op, const double* X, double* Y, int nrhs,
+                      const double* col_scale, int refine, void* stream);
+int bx_dense_op_status(bx_dense_op_handle op, int* timed_out);
+/* mean ms of one GEMM launch (no refinement) over n_iter, CUDA events */
+int bx_dense_op_time(bx_dense_op_handle op, const double* X, double* Y, int nrhs,
+                     int n_iter, double* ms);
+int bx_dense_op_destroy(bx_dense_op_handle op);
 
 /* Diagnostics: launch the fused cell kernel alone n times on the handle's
  * stream (state ping-pongs as in bx_step) and return the mean duration of one
