@@ -71,6 +71,13 @@ def _env_int(name, default):
         return default
 
 
+def bf16_peak():
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(path):
+        return float(json.load(open(path))['bf16_tflops']), 'measured (burst)'
+    return 1900.0, 'fallback'
+
+
 def peaks():
     path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
     if os.path.exists(path):
@@ -191,6 +198,21 @@ def cpu_baseline(g, p, Dm, st, budget_s=12.0, D_env=None):
                       f'cluster ({dt:.1f} s), NumPy oracle, one thread'}
 
 
+def init_time_to_steady(n_clusters=16, n_cells=5000):
+    """The learned warm start against the plain init on fresh clusters."""
+    from betse_gb300 import warmstart as ws
+    r = ws.evaluate(ws.WarmStart(), n_clusters=n_clusters, n_cells=n_cells, seed=9001, max_steps=1_500_000,
+                    log=lambda s: None)
+    w = r['warm'][0]
+    return {'metric': 'init steps to max|dVm/dt| < 1e-6 V/s per cluster, warm start vs uniform start',
+            'value': w.get('speedup_mean_steps'), 'unit': 'x (mean steps per cluster, cold / warm)',
+            'speedup_median_steps': w.get('speedup_median_steps'),
+            'speedup_wall_lockstep_batch': w['speedup_wall'],
+            'workload': f'{n_clusters} fresh clusters x {n_cells} cells, dt {ws.DT} s, split step, '
+                        f'residual checked every {r["check_every"]} steps',
+            'cold': r['cold'], 'warm': w}
+
+
 def secondary(stream, flush):
     """Extra lines of evidence at N=1: the ECM workload's step rates and the
     environment-field products at its full grid (output-only, sampled steps)."""
@@ -244,6 +266,27 @@ def secondary(stream, flush):
                          'frac': gbs / hbm, 'algorithmic_bytes_per_launch': 8 * G * G,
                          'kernel': 'k_dense_rows_df<2>', 'peak_source': src}}
     fields_eng.close()
+    # tensor-core stage: BF16x3 dense-operator GEMM (lapGJinv-sized, 20k cells)
+    from betse_gb300.dense import DenseOperator
+    n = 20480
+    A = np.empty((n, n))
+    A.fill(1e-3)  # timing only
+    with DenseOperator(A) as op:
+        del A
+        res = []
+        for nrhs in (256, 1024):
+            ms = op.time(nrhs, 10)
+            flops = 3 * 2.0 * n * n * nrhs
+            res.append({'nrhs': nrhs, 'ms': ms, 'tflops': flops / (ms / 1e3) / 1e12})
+    bf16 = bf16_peak()
+    best = max(res, key=lambda r: r['tflops'])
+    out['dense_op_gemm'] = {
+        'operator': f'synthetic dense {n}x{n} (lapGJinv of a {n}-cell cluster), BF16 hi/lo tiles',
+        'runs': res,
+        'roofline': {'bound': 'tensor', 'achieved': best['tflops'], 'peak': bf16[0], 'unit': 'TFLOP/s',
+                     'frac': best['tflops'] / bf16[0], 'flops_per_launch': 3 * 2.0 * n * n * best['nrhs'],
+                     'kernel': 'k_gemm_bf16x3 (tcgen05.mma kind::f16, 3 products per K step)',
+                     'peak_source': bf16[1]}}
     return out
 
 
@@ -458,9 +501,10 @@ def main():
             cpu['sample'] += ' (cluster 0 of the sweep)'
         else:
             cpu = cpu_baseline(g, p, Dm, st, D_env=D_env)
-    extra = None
+    extra = init_steady = None
     if rank == 0 and world == 1 and args.workload == 'cluster100k' and not args.no_secondary:
         extra = secondary(stream, flush)
+        init_steady = init_time_to_steady()
 
     if rank == 0:
         line = {
@@ -491,6 +535,8 @@ def main():
         }
         if extra is not None:
             line['secondary'] = extra
+        if init_steady is not None:
+            line['init_time_to_steady'] = init_steady
         print(json.dumps(line), flush=True)
     for e in (split, plain, e_s):
         e.close()

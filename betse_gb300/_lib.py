@@ -23,6 +23,7 @@ SPLIT_FP32 = 1
 
 _dp = ct.POINTER(ct.c_double)
 _ip = ct.POINTER(ct.c_int32)
+_fp = ct.POINTER(ct.c_float)
 _u8p = ct.POINTER(ct.c_uint8)
 
 
@@ -95,6 +96,7 @@ SIGNATURES = {
     'bx_outputs_download': (ct.c_int, [ct.c_void_p, ct.POINTER(BxOutputs)]),
     'bx_status': (ct.c_int, [ct.c_void_p, ct.POINTER(BxStepStatus)]),
     'bx_set_lap_env_inv': (ct.c_int, [ct.c_void_p, _dp]),
+    'bx_max_abs_dvm': (ct.c_int, [ct.c_void_p, _dp]),
     'bx_dense_op_create': (ct.c_int, [_dp, ct.c_int, ct.POINTER(ct.c_void_p)]),
     'bx_dense_op_set_forward': (ct.c_int, [ct.c_void_p, _ip, _ip, _dp]),
     'bx_dense_op_apply': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p,
@@ -103,6 +105,18 @@ SIGNATURES = {
     'bx_dense_op_time': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
                                     ct.POINTER(ct.c_double)]),
     'bx_dense_op_destroy': (ct.c_int, [ct.c_void_p]),
+    'bx_gnn_create': (ct.c_int, [ct.POINTER(ct.c_void_p)]),
+    'bx_gnn_n_params': (ct.c_int, []),
+    'bx_gnn_set_params': (ct.c_int, [ct.c_void_p, _fp]),
+    'bx_gnn_get_params': (ct.c_int, [ct.c_void_p, _fp]),
+    'bx_gnn_set_graph': (ct.c_int, [ct.c_void_p, ct.c_int, _ip, _ip]),
+    'bx_gnn_forward': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p,
+                                  ct.c_int]),
+    'bx_gnn_gradients': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p,
+                                    ct.c_int, _fp, _fp]),
+    'bx_gnn_train_step': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p,
+                                     ct.c_int, ct.c_float, _fp]),
+    'bx_gnn_destroy': (ct.c_int, [ct.c_void_p]),
     'bx_env_fields': (ct.c_int, [ct.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     'bx_time_env_fields': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_double),
                                       ct.POINTER(ct.c_double)]),

@@ -119,7 +119,7 @@ struct bx_cluster {
   double *o_fmem = nullptr, *o_fgj = nullptr, *o_rate = nullptr, *o_rho = nullptr, *o_Jn = nullptr,
          *o_Imem = nullptr, *o_Jcx = nullptr, *o_Jcy = nullptr, *o_Jc = nullptr, *o_vmave = nullptr,
          *o_dvm = nullptr, *o_Ecx = nullptr, *o_Ecy = nullptr, *o_Emc = nullptr, *o_Egjx = nullptr,
-         *o_Egjy = nullptr, *o_gjopen = nullptr, *o_sigma = nullptr, *o_vmc = nullptr,
+         *o_Egjy = nullptr, *o_gjopen = nullptr, *o_sigma = nullptr, *o_vmc = nullptr, *o_drho = nullptr,
          *o_vm_mem = nullptr;
   int parity = 0;
   bool have_state = false, have_dm = false, have_denv = false, have_outputs = false;
@@ -135,6 +135,8 @@ struct bx_cluster {
   double* f_buf = nullptr;         // field scratch, kFieldBufs x [G]
   int* f_last = nullptr;           // last membrane of each grid cell (-1: none)
   bool last_step_outputs = false;  // the latest bx_step computed outputs
+  int* d_cl_mem = nullptr;         // membrane offsets of the clusters [ncl+1] (residual test)
+  double* d_resid = nullptr;       // [ncl]
 };
 
 namespace {
@@ -153,7 +155,7 @@ void free_all(bx_cluster* h) {
       h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
-      h->f_lap, h->f_X, h->f_buf, h->f_last};
+      h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->graph) cudaGraphExecDestroy(h->graph);
@@ -299,6 +301,7 @@ bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
   p.env_part = h->s_part; p.status = h->d_status;
   p.o_fmem = h->o_fmem; p.o_fgj = h->o_fgj; p.o_rate = h->o_rate; p.o_rho = h->o_rho;
   p.o_vmem = h->o_vmc;
+  p.o_drho = h->o_drho;
   return p;
 }
 
@@ -422,7 +425,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
     if (out) {
       bx::SplitOutGeom og{h->C, h->M, h->I, h->d_cell_ptr, h->d_blk, h->d_nn, h->d_map_env,
                           h->d_mem_sa, h->d_nx, h->d_ny, h->d_swm, h->d_swo, h->d_cell_sa,
-                          h->d_gj_w, h->d_bflag};
+                          h->d_gj_w, h->d_bflag, h->d_diviterm, h->o_drho};
       bx::SplitOutPtrs op{h->o_fmem, h->o_fgj, h->s_rec[parity ^ 1], h->s_rec[parity], kRec, h->s_cc2,
                           h->S, h->t_slot_of_cell,
                           h->phib_nonzero ? h->s_phib : nullptr, h->o_Jn, h->o_Imem, h->o_Jcx,
@@ -432,7 +435,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
       const bx::StepConst d = make_step_const(h);
       oc.I = h->I;
       for (int i = 0; i < h->I; ++i) { oc.zF[i] = d.zF[i]; oc.sig_coef[i] = d.sig_coef[i]; }
-      oc.dt = d.dt; oc.gj_len = h->gj_len; oc.gj_block = d.gj_block;
+      oc.dt = d.dt; oc.gj_len = h->gj_len; oc.gj_block = d.gj_block; oc.cm = h->par.cm;
       if (h->tpb == 192) bx::k_split_outputs<192><<<h->nblk, 192, 0, s>>>(og, op, oc);
       else bx::k_split_outputs<256><<<h->nblk, 256, 0, s>>>(og, op, oc);
       bx::k_split_egj<<<(h->M + 255) / 256, 256, 0, s>>>(h->M, h->d_nn, h->o_vm_mem, h->d_nx, h->d_ny,
@@ -804,7 +807,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     ALLOC(h->s_pump, ncl);
     ALLOC(h->s_phib, G);
     if (cudaMemset(h->s_phib, 0, (size_t)G * sizeof(float)) != cudaSuccess) return bail(BX_ECUDA, "cudaMemset");
-    ALLOC(h->o_vmc, C); ALLOC(h->o_vm_mem, M);
+    ALLOC(h->o_vmc, C); ALLOC(h->o_vm_mem, M); ALLOC(h->o_drho, C);
   } else {
     std::vector<float> fsa(M), fgw(M);
     for (int m = 0; m < M; ++m) { fsa[m] = (float)msa[m]; fgw[m] = (float)gjw[m]; }
@@ -1305,6 +1308,54 @@ int bx_dense_apply_f64(const double* A, const double* x, double* y, int n, int n
     default: bx::k_dense_rows<4><<<(unsigned)blocks, threads, 0, s>>>(A, x, y, n); break;
   }
   BX_CU(cudaGetLastError());
+  return BX_OK;
+}
+
+}  // extern "C"
+
+namespace {
+__device__ __forceinline__ double nan_value() { return __longlong_as_double(0x7ff8000000000000LL); }
+// out[c] = max |dvm| over cluster c's membranes (one CTA per cluster)
+__global__ void k_max_abs_dvm(const int* __restrict__ cl_mem, const double* __restrict__ dvm, double* out) {
+  __shared__ double red[8];
+  const int c = blockIdx.x;
+  double m = 0.0;
+  bool nan = false;
+  for (int i = cl_mem[c] + threadIdx.x; i < cl_mem[c + 1]; i += blockDim.x) {
+    const double v = fabs(dvm[i]);
+    if (v != v) nan = true;
+    m = fmax(m, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  nan = __syncthreads_or(nan);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
+    out[c] = nan ? nan_value() : r;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int bx_max_abs_dvm(bx_handle h, double* per_cluster) {
+  if (!h || !per_cluster) return fail(BX_EINVAL, "null argument");
+  if (!h->last_step_outputs) return fail(BX_ESTATE, "bx_max_abs_dvm needs a last bx_step with want_outputs");
+  if (!h->d_cl_mem) {
+    if (cudaMalloc(&h->d_cl_mem, (size_t)(h->ncl + 1) * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&h->d_resid, (size_t)h->ncl * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(BX_ENOMEM, "cudaMalloc residual");
+    }
+    BX_CU(cudaMemcpy(h->d_cl_mem, h->cl_mem.data(), (size_t)(h->ncl + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  k_max_abs_dvm<<<h->ncl, 256, 0, h->stream>>>(h->d_cl_mem, h->o_dvm, h->d_resid);
+  BX_CU(cudaGetLastError());
+  BX_CU(cudaMemcpyAsync(per_cluster, h->d_resid, (size_t)h->ncl * sizeof(double), cudaMemcpyDeviceToHost,
+                        h->stream));
+  BX_CU(cudaStreamSynchronize(h->stream));
   return BX_OK;
 }
 

@@ -168,6 +168,7 @@ struct SplitPtrs {
   unsigned long long* status;              // nan_vm, nan_conc, neg clamps
   // outputs (OUT), natural order
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_vmem;
+  double* o_drho;      // [C] output steps: new minus old charge density (FP64 from double-float)
 };
 
 template <int REC>
@@ -224,6 +225,7 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   __shared__ float sB[NI][TPB];
   __shared__ float sRec[kCellsPerCta][REC];
   __shared__ float2 sQ[NI][kCellsPerCta];
+  __shared__ float2 sQo[OUT ? NI : 1][kCellsPerCta];   // output steps: charge of the old state
   const int I = IS::n(k);
   const int b = blockIdx.x;
   const int t = threadIdx.x;
@@ -342,6 +344,10 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     float s2 = 0.f;
     for (int j = rng.x; j < rng.y; ++j) s2 += sB[i][j];
     df x{x2.x, x2.y};
+    if (OUT) {
+      const df qo = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
+      sQo[i][lane] = make_float2(qo.hi, qo.lo);
+    }
     x = df_add_f(x, s1 * dtv);                         // update_Co
     sRec[lane][i] = x.hi + x.lo;                       // cc_at_mem (before the GJ term)
     x = df_add_f(x, s2 * dtv);                         // gap-junction term
@@ -374,6 +380,13 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
         const int cc = g.tile_c0[b] + t;
         p.o_rho[cc] = (double)rho.hi + (double)rho.lo;
         p.o_vmem[cc] = (double)vc;
+        df rho_o{0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < NI; ++i)
+          if (i < I) rho_o = df_add(rho_o, df{sQo[i][t].x, sQo[i][t].y});
+        // dVm/dt from the FP64 charge change: the FP32 record's Vmem resolves
+        // only ~4e-9 V, too coarse for a residual test on dVm/dt
+        p.o_drho[cc] = ((double)rho.hi + (double)rho.lo) - ((double)rho_o.hi + (double)rho_o.lo);
       }
     }
   }
@@ -682,6 +695,7 @@ struct SplitOutGeom {
   const int* cell_ptr; const int* blk_cell; const int* nn; const int* map_env;
   const double* mem_sa; const double* nx; const double* ny; const double* sw_mem;
   const double* sw_o; const double* cell_sa; const double* gj_w; const uint8_t* bflag;
+  const double* diviterm; const double* drho;
 };
 struct SplitOutPtrs {
   const double* fmem; const double* fgj; const float* rec_new; const float* rec_old; int rec;
@@ -692,6 +706,7 @@ struct SplitOutPtrs {
 };
 struct SplitOutConst {
   int I; double zF[kMaxIons]; double sig_coef[kMaxIons]; double dt; double gj_len; double gj_block;
+  double cm;
 };
 
 template <int TPB>
@@ -744,9 +759,7 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
     sX[2][t] = Jn * g.nx[m] * g.mem_sa[m];
     sX[3][t] = Jn * g.ny[m] * g.mem_sa[m];
     const int c = c0 + lc;
-    double vmo = (double)p.rec_old[(size_t)p.slot_of_cell[c] * p.rec + p.rec - 1] - (p.phib ? (double)p.phib[g.map_env[m]] : 0.0);
-    for (int i = 0; i < k.I; ++i) vmo += kNonce;
-    p.dvm[m] = (vm - vmo) / k.dt;
+    p.dvm[m] = g.drho[c] * g.diviterm[c] / k.cm / k.dt;   // update_V's (vm - vmo)/dt, sim.py:2083
   } else { sX[2][t] = 0.0; sX[3][t] = 0.0; }
   __syncthreads();
   if (t < ncell) {

@@ -124,6 +124,13 @@ class ClusterEngine:
         _lib.check(self.lib.bx_outputs_download(self.h, ct.byref(o)), 'bx_outputs_download')
         return arrs
 
+    def max_abs_dvm(self):
+        """Per-cluster max |dVm/dt| of the last step (which ran with outputs=True)."""
+        n = getattr(self, 'n_clusters', 1)
+        out = np.empty(n)
+        _lib.check(self.lib.bx_max_abs_dvm(self.h, _lib.dptr(out)), 'bx_max_abs_dvm')
+        return out
+
     def set_lap_env_inv(self, lap_env_inv):
         """Keep ``cells.lapENVinv`` ([grid, grid]) on the GPU for ``env_fields``."""
         A = _c(lap_env_inv)

@@ -282,10 +282,11 @@ def _sweep_member(args):
 
 
 def sweep_workload(n_clusters=512, seed=7, cells_range=(200, 5000), mult_range=(0.1, 10.0),
-                   dt=5e-3, dm_range=(1e-19, 1e-17), workers=None):
+                   dt=5e-3, dm_range=(1e-19, 1e-17), workers=None, pump_range=None):
     """A parameter sweep: ``n_clusters`` independent clusters with cell counts
     log-uniform in ``cells_range`` and per-cluster Na/K diffusivity and pump
-    multipliers log-uniform in ``mult_range``. Clusters are generated in a
+    multipliers log-uniform in ``mult_range`` (the pump's in ``pump_range`` when
+    given). Clusters are generated in a
     spawn-started process pool. Returns lists (geoms, params, Dms, states)."""
     import concurrent.futures as cf
     import multiprocessing as mp
@@ -294,8 +295,9 @@ def sweep_workload(n_clusters=512, seed=7, cells_range=(200, 5000), mult_range=(
     lo, hi = np.log(cells_range[0]), np.log(cells_range[1])
     counts = np.exp(rng.uniform(lo, hi, n_clusters))
     ml, mh = np.log(mult_range[0]), np.log(mult_range[1])
+    pr = mult_range if pump_range is None else pump_range
     dmm = np.exp(rng.uniform(ml, mh, n_clusters))
-    pmm = np.exp(rng.uniform(ml, mh, n_clusters))
+    pmm = np.exp(rng.uniform(np.log(pr[0]), np.log(pr[1]), n_clusters))
     jobs = [(k, float(counts[k]), seed * 1000 + k, float(dmm[k]), float(pmm[k]), dt, dm_range)
             for k in range(n_clusters)]
     workers = workers or min(16, os.cpu_count() or 1)

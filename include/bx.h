@@ -208,6 +208,10 @@ int bx_state_download(bx_handle h, bx_state* s);
 int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream);
 int bx_outputs_download(bx_handle h, bx_outputs* o);
 int bx_status(bx_handle h, bx_step_status* st);
+/* Steady-state residual of each cluster after a step with want_outputs:
+ * per_cluster[c] = max over its membranes of |dVm/dt| (sim.dvm, sim.py:2083),
+ * NaN if any is NaN.  n_clusters values (1 for bx_cluster_create).  Synchronous. */
+int bx_max_abs_dvm(bx_handle h, double* per_cluster);
 
 /* Dense lapENVinv ([grid x grid] row-major FP64, host) for bx_env_fields:
  * cells.lapENVinv (cells.py:503-504, the pinv of
@@ -256,6 +260,28 @@ int bx_dense_op_status(bx_dense_op_handle op, int* timed_out);
 int bx_dense_op_time(bx_dense_op_handle op, const double* X, double* Y, int nrhs,
                      int n_iter, double* ms);
 int bx_dense_op_destroy(bx_dense_op_handle op);
+
+/* Warm-start graph network (no reference counterpart: BETSE's init phase
+ * always starts from the uniform profile).  A 3-layer, 64-wide message-passing
+ * network on the cell adjacency predicts per-cell steady-state concentrations
+ * and Vmem; it is trained here in BF16 with FP32 master weights (Adam).
+ * Parameters are a flat FP32 vector of bx_gnn_n_params() values (layout:
+ * W0[64x64], b0, then (Ws, Wn, b) for each layer, Wd[64x64], bd).  The graph
+ * is host CSR over all nodes; calls act on a node range [lo, hi) that must
+ * hold whole clusters.  x [rows x n_in], y / targets [rows x n_out] are FP32
+ * DEVICE pointers (n_in, n_out <= 64). */
+typedef struct bx_gnn* bx_gnn_handle;
+int bx_gnn_create(bx_gnn_handle* out);
+int bx_gnn_n_params(void);
+int bx_gnn_set_params(bx_gnn_handle h, const float* params);   /* host; resets Adam */
+int bx_gnn_get_params(bx_gnn_handle h, float* params);         /* host */
+int bx_gnn_set_graph(bx_gnn_handle h, int n_nodes, const int32_t* ptr, const int32_t* nbr);
+int bx_gnn_forward(bx_gnn_handle h, int lo, int hi, const float* x, int n_in, float* y, int n_out);
+int bx_gnn_gradients(bx_gnn_handle h, int lo, int hi, const float* x, int n_in, const float* y,
+                     int n_out, float* grad_host, float* loss_host);
+int bx_gnn_train_step(bx_gnn_handle h, int lo, int hi, const float* x, int n_in, const float* y,
+                      int n_out, float lr, float* loss_host);
+int bx_gnn_destroy(bx_gnn_handle h);
 
 /* Diagnostics: launch the fused cell kernel alone n times on the handle's
  * stream (state ping-pongs as in bx_step) and return the mean duration of one
