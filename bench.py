@@ -317,6 +317,37 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def profile_kernel(which):
+    """One small launch sequence of a dense-product kernel for ncu captures:
+    'gemm' -- k_gemm_bf16x3 on an 8192 x 8192 operator with 1024 right-hand
+    sides (two warm-up launches, then the captured one); 'fields' --
+    k_dense_rows_df<2> on a 12000 x 12000 double-float operator."""
+    from betse_gb300.build import build
+    build()
+    if which == 'gemm':
+        from betse_gb300.dense import DenseOperator
+        n = 8192
+        A = np.empty((n, n))
+        A.fill(1e-3)
+        with DenseOperator(A) as op:
+            op.time(1024, 3)
+    else:
+        from betse_gb300 import generator as gen
+        from betse_gb300.engine import ClusterEngine
+        g, p, Dm, st, _ = gen.workload(400e-6, 5, dt=1e-2, grid_size=110)
+        G = g.n_grid
+        e = ClusterEngine(g, p, 'fp64')
+        e.set_membrane_diffusivity(Dm)
+        e.upload(**st)
+        A = np.empty((G, G))
+        A.fill(1e-12)
+        e.set_lap_env_inv(A)
+        e.step(1, outputs=True)
+        e.time_env_fields(2)
+        e.close()
+    print('profile kernel done:', which)
+
+
 def profile_run(args):
     """A short, deterministic launch sequence for ncu captures."""
     from betse_gb300.build import build
@@ -351,7 +382,11 @@ def main():
     ap.add_argument('--profile-run', action='store_true',
                     help='for ncu: build the workload, upload it, run 4 eager steps, exit')
     ap.add_argument('--precision', default='split', choices=['split', 'fp64'])
+    ap.add_argument('--profile-kernel', choices=['gemm', 'fields'],
+                    help='for ncu: run a small case of one dense-product kernel and exit')
     args = ap.parse_args()
+    if args.profile_kernel:
+        return profile_kernel(args.profile_kernel)
     world = _env_int('WORLD_SIZE', 1)
     if args.profile_run:
         return profile_run(args)
