@@ -362,10 +362,13 @@ def profile_run(args):
         if D_env is not None:
             e.set_env_diffusivity(D_env)
         e.upload(**st)
-    e.step(4)
+    if args.launch:
+        # the launch configuration the autotuner picks for this workload, pinned
+        e.set_launch_config(int(args.launch.rstrip('p')), args.launch.endswith('p'))
+    e.step(args.time_steps or 4)
     e.check_stable()
     e.close()
-    print('profile run done:', args.workload, args.precision)
+    print('profile run done:', args.workload, args.precision, args.launch or 'default launch')
 
 
 def main():
@@ -380,8 +383,10 @@ def main():
     ap.add_argument('--no-secondary', action='store_true',
                     help='skip the ECM workload and environment-field measurements')
     ap.add_argument('--profile-run', action='store_true',
-                    help='for ncu: build the workload, upload it, run 4 eager steps, exit')
+                    help='for ncu: build the workload, upload it, run 4 steps (or --time-steps), exit')
     ap.add_argument('--precision', default='split', choices=['split', 'fp64'])
+    ap.add_argument('--launch', default=None,
+                    help='with --profile-run: CTA size, suffix p for the persistent kernel (e.g. 192p)')
     ap.add_argument('--profile-kernel', choices=['gemm', 'fields'],
                     help='for ncu: run a small case of one dense-product kernel and exit')
     args = ap.parse_args()
@@ -492,7 +497,8 @@ def main():
     hbm, src = peaks()
     achieved = kbytes / (kern_ms / 1e3) / 1e9
     traffic = None
-    tp = os.path.join(ROOT, 'profiles', f'k_split_step_{args.workload}.traffic.json')
+    kname = 'k_split_persist' if e_s.launch_config()[1] else 'k_split_step'
+    tp = os.path.join(ROOT, 'profiles', f'{kname}_{args.workload}.traffic.json')
     if os.path.exists(tp):
         tj = json.load(open(tp))
         traffic = int(tj['dram_bytes_per_launch'] * n_mems / tj['membranes'])
@@ -559,7 +565,7 @@ def main():
                            'vm_max_abs_err_V': vm_err, 'vm_err_after_steps': T},
             'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
                          'frac': achieved / hbm, 'traffic': traffic,
-                         'kernel': 'k_split_step (fused membrane fluxes + cell update, split form)',
+                         'kernel': f'{kname} (fused membrane fluxes + cell update, split form)',
                          'algorithmic_bytes_per_launch': kbytes, 'launch_ms': kern_ms,
                          'peak_source': src},
             'cpu_baseline': cpu,
