@@ -113,7 +113,7 @@ struct bx_cluster {
   double *d_cenv = nullptr, *d_phib = nullptr, *d_env_part = nullptr, *d_mem_flux_sa = nullptr,
          *d_pump = nullptr, *d_env_scale = nullptr;
   double *d_Denv = nullptr, *d_Ex = nullptr, *d_Ey = nullptr, *d_fx = nullptr, *d_fy = nullptr,
-         *d_tmp = nullptr, *d_tmp2 = nullptr, *d_venv = nullptr, *d_rho_env = nullptr;
+         *d_tmp = nullptr, *d_tmp2 = nullptr, *d_venv = nullptr, *d_rho_env = nullptr, *d_vsrc = nullptr;
   unsigned long long* d_status = nullptr;
   // ---- outputs
   double *o_fmem = nullptr, *o_fgj = nullptr, *o_rate = nullptr, *o_rho = nullptr, *o_Jn = nullptr,
@@ -152,7 +152,7 @@ void free_all(bx_cluster* h) {
       h->t_gw, h->t_dtv, h->t_dvc, h->t_rng,
       h->s_cenv_f, h->s_pump, h->s_part, h->s_phib, h->d_cenv, h->d_phib, h->d_env_part,
       h->d_mem_flux_sa, h->d_pump, h->d_env_scale, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy,
-      h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
+      h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_vsrc, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid};
@@ -455,19 +455,22 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   bx::EnvConst ec = make_env_const(h);
   const int gg = env_grid(h->G);
   bx::k_env_np_flux<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
+  double* rho_out = out ? h->d_rho_env : nullptr;
   if (h->par.sharpness < 1.0) {
     bx::k_env_update<false><<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_fx, h->d_fy, h->d_env_ptr,
-                                                  h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
+                                                  h->d_env_mem, h->d_mem_flux_sa, h->M, h->d_touched,
+                                                  h->d_vsrc, rho_out, ec);
     bx::k_env_integrate_scatter<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_env_ptr, h->d_env_mem,
-                                                      h->d_mem_flux_sa, h->M, ec);
+                                                      h->d_mem_flux_sa, h->M, h->d_touched, h->d_vsrc,
+                                                      rho_out, ec);
     h->launches += 3;
   } else {
     bx::k_env_update<true><<<gg, kEnvTPB, 0, s>>>(h->d_cenv, nullptr, h->d_fx, h->d_fy, h->d_env_ptr,
-                                                 h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
+                                                 h->d_env_mem, h->d_mem_flux_sa, h->M, h->d_touched,
+                                                 h->d_vsrc, rho_out, ec);
     h->launches += 2;
   }
-  bx::k_env_charge_gauss_y<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_touched, out ? h->d_rho_env : nullptr,
-                                                 h->d_tmp, ec);
+  bx::k_env_gauss_y<<<gg, kEnvTPB, 0, s>>>(h->d_vsrc, h->d_tmp, ec);
   bx::k_env_gauss_x<<<gg, kEnvTPB, 0, s>>>(h->d_tmp, h->phib_nonzero ? h->d_phib : nullptr, h->d_venv, ec);
   bx::k_env_neg_grad<<<gg, kEnvTPB, 0, s>>>(h->d_venv, ec.screen, h->d_Ex, h->d_Ey, ec);
   h->launches += 3;
@@ -828,7 +831,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     ALLOC(h->d_Ex, G); ALLOC(h->d_Ey, G);
     ALLOC(h->d_fx, (size_t)I * G); ALLOC(h->d_fy, (size_t)I * G);
     ALLOC(h->d_tmp, G); ALLOC(h->d_tmp2, (size_t)I * G);
-    ALLOC(h->d_venv, G); ALLOC(h->d_rho_env, G);
+    ALLOC(h->d_venv, G); ALLOC(h->d_rho_env, G); ALLOC(h->d_vsrc, G);
   }
   ALLOC(h->o_fmem, (size_t)I * M); ALLOC(h->o_fgj, (size_t)I * M);
   ALLOC(h->o_rate, M); ALLOC(h->o_rho, C); ALLOC(h->o_Jn, M); ALLOC(h->o_Imem, M);

@@ -34,6 +34,9 @@ __device__ __forceinline__ double cb_at(const double* c, const EnvConst& e, int 
 // Nernst-Planck flux on the grid (update_ecm, sim.py:2219-2242;
 // stb.nernst_planck_flux, sim_toolbox.py:385-413) with fd.gradient
 // (finitediff.py:1236-1266).  E_env is the previous update_V's field.
+// The grid kernels multiply by 1/delta and 1/(2 delta) where the reference
+// divides (a difference of at most one rounding): an FP64 division costs
+// GB300 several FP64-pipe operations, and the stencils are otherwise cheap.
 __global__ void k_env_np_flux(const double* __restrict__ cenv, const double* __restrict__ Denv,
                               const double* __restrict__ Ex, const double* __restrict__ Ey,
                               double* fx, double* fy, EnvConst e) {
@@ -43,12 +46,12 @@ __global__ void k_env_np_flux(const double* __restrict__ cenv, const double* __r
   for (int ion = 0; ion < e.I; ++ion) {
     const double c0 = cb_at(cenv, e, ion, i, j);
     double gcx, gcy;
-    if (j == 0) gcx = (cb_at(cenv, e, ion, i, 1) - c0) / e.delta;
-    else if (j == e.nx - 1) gcx = (c0 - cb_at(cenv, e, ion, i, j - 1)) / e.delta;
-    else gcx = -(cb_at(cenv, e, ion, i, j - 1) - cb_at(cenv, e, ion, i, j + 1)) / (2 * e.delta);
-    if (i == 0) gcy = (cb_at(cenv, e, ion, 1, j) - c0) / e.delta;
-    else if (i == e.ny - 1) gcy = (c0 - cb_at(cenv, e, ion, i - 1, j)) / e.delta;
-    else gcy = -(cb_at(cenv, e, ion, i - 1, j) - cb_at(cenv, e, ion, i + 1, j)) / (2 * e.delta);
+    if (j == 0) gcx = (cb_at(cenv, e, ion, i, 1) - c0) * e.inv_delta;
+    else if (j == e.nx - 1) gcx = (c0 - cb_at(cenv, e, ion, i, j - 1)) * e.inv_delta;
+    else gcx = -(cb_at(cenv, e, ion, i, j - 1) - cb_at(cenv, e, ion, i, j + 1)) * e.inv_2delta;
+    if (i == 0) gcy = (cb_at(cenv, e, ion, 1, j) - c0) * e.inv_delta;
+    else if (i == e.ny - 1) gcy = (c0 - cb_at(cenv, e, ion, i - 1, j)) * e.inv_delta;
+    else gcy = -(cb_at(cenv, e, ion, i - 1, j) - cb_at(cenv, e, ion, i + 1, j)) * e.inv_2delta;
     const double D = Denv[(size_t)ion * e.G + k];
     const double alpha = D * e.np_alpha[ion];
     const double gvx = -Ex[k], gvy = -Ey[k];
@@ -61,29 +64,42 @@ __global__ void k_env_np_flux(const double* __restrict__ cenv, const double* __r
 __device__ __forceinline__ double ddx_neg(const double* f, const EnvConst& e, int i, int j) {
   // diff(-f, axis=0)
   const double* r = f + i * e.nx;
-  if (j == 0) return ((-r[0]) - (-r[1])) / e.delta;
-  if (j == e.nx - 1) return ((-r[j - 1]) - (-r[j])) / e.delta;
-  return -((-r[j - 1]) - (-r[j + 1])) / (2 * e.delta);
+  if (j == 0) return ((-r[0]) - (-r[1])) * e.inv_delta;
+  if (j == e.nx - 1) return ((-r[j - 1]) - (-r[j])) * e.inv_delta;
+  return -((-r[j - 1]) - (-r[j + 1])) * e.inv_2delta;
 }
 __device__ __forceinline__ double ddy_neg(const double* f, const EnvConst& e, int i, int j) {
   // diff(-f, axis=1)
   const int nx = e.nx;
-  if (i == 0) return -((-f[nx + j]) - (-f[j])) / e.delta;
-  if (i == e.ny - 1) return -((-f[i * nx + j]) - (-f[(i - 1) * nx + j])) / e.delta;
-  return -((-f[(i - 1) * nx + j]) - (-f[(i + 1) * nx + j])) / (2 * e.delta);
+  if (i == 0) return -((-f[nx + j]) - (-f[j])) * e.inv_delta;
+  if (i == e.ny - 1) return -((-f[i * nx + j]) - (-f[(i - 1) * nx + j])) * e.inv_delta;
+  return -((-f[(i - 1) * nx + j]) - (-f[(i + 1) * nx + j])) * e.inv_2delta;
 }
 
-// c <- cb + div(-f) dt  [+ membrane exchange if FUSE_SCATTER]
+// Environment charge of grid cell k from its new concentrations, for
+// get_current's ECM branch (ion_current.py:82-92): rho = sum_i F z_i c_i (ions
+// in order) and, on the membrane-touched cells, the surface-charge potential
+// source v = (rho surf_scale) / (ko_env eo er); written by the kernel that
+// produces the cell's final concentrations.
+__device__ __forceinline__ void env_charge_out(int k, double rho, const uint8_t* touched, double* vsrc,
+                                               double* rho_env, const EnvConst& e) {
+  vsrc[k] = touched[k] ? (rho * e.surf_scale) * e.inv_koeoer : 0.0;
+  if (rho_env) rho_env[k] = rho;
+}
+
+// c <- cb + div(-f) dt  [+ membrane exchange and charge if FUSE_SCATTER]
 // (update_ecm sim.py:2247-2254, then update_Co's ECM term sim_toolbox.py:1189-1195
 //  with div_env = M_divmap_mem2ecm @ (-flux) / (cell_height delta^2), :1229-1232)
 template <bool FUSE_SCATTER>
 __global__ void k_env_update(double* cenv, double* tmp, const double* __restrict__ fx,
                              const double* __restrict__ fy, const int* __restrict__ env_ptr,
                              const int* __restrict__ env_mem, const double* __restrict__ mem_flux_sa,
-                             int M, EnvConst e) {
+                             int M, const uint8_t* __restrict__ touched, double* vsrc, double* rho_env,
+                             EnvConst e) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= e.G) return;
   const int i = k / e.nx, j = k - i * e.nx;
+  double rho = 0.0;
   for (int ion = 0; ion < e.I; ++ion) {
     const double* fxi = fx + (size_t)ion * e.G;
     const double* fyi = fy + (size_t)ion * e.G;
@@ -94,20 +110,26 @@ __global__ void k_env_update(double* cenv, double* tmp, const double* __restrict
       for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
       c = c + (s * e.inv_h_d2) * e.dt;
       cenv[(size_t)ion * e.G + k] = c;
+      rho += e.zF[ion] * c;
     } else {
       tmp[(size_t)ion * e.G + k] = c;
     }
   }
+  if (FUSE_SCATTER) env_charge_out(k, rho, touched, vsrc, rho_env, e);
 }
 
-// fd.integrator (finitediff.py:1479-1512) when sharpness < 1, then the membrane exchange.
+// fd.integrator (finitediff.py:1479-1512) when sharpness < 1, then the membrane
+// exchange and the charge.
 __global__ void k_env_integrate_scatter(double* cenv, const double* __restrict__ tmp,
                                         const int* __restrict__ env_ptr, const int* __restrict__ env_mem,
-                                        const double* __restrict__ mem_flux_sa, int M, EnvConst e) {
+                                        const double* __restrict__ mem_flux_sa, int M,
+                                        const uint8_t* __restrict__ touched, double* vsrc, double* rho_env,
+                                        EnvConst e) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= e.G) return;
   const int i = k / e.nx, j = k - i * e.nx;
   const double sides = (1 - e.sharpness) / 4;
+  double rho = 0.0;
   for (int ion = 0; ion < e.I; ++ion) {
     const double* P = tmp + (size_t)ion * e.G;
     double F;
@@ -122,37 +144,28 @@ __global__ void k_env_integrate_scatter(double* cenv, const double* __restrict__
     }
     double s = 0.0;
     for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
-    cenv[(size_t)ion * e.G + k] = F + (s * e.inv_h_d2) * e.dt;
+    const double c = F + (s * e.inv_h_d2) * e.dt;
+    cenv[(size_t)ion * e.G + k] = c;
+    rho += e.zF[ion] * c;
   }
+  env_charge_out(k, rho, touched, vsrc, rho_env, e);
 }
 
-// get_current ECM branch (ion_current.py:79-110): environment charge on the
-// membrane-touched grid cells -> v, then the axis-0 pass of a sigma=1 Gaussian
-// with zero padding (scipy mode='constant').
-__global__ void k_env_charge_gauss_y(const double* __restrict__ cenv, const uint8_t* __restrict__ touched,
-                                     double* rho_env, double* tmp, EnvConst e) {
+// get_current ECM branch (ion_current.py:79-110): the axis-0 pass of a
+// sigma=1 Gaussian with zero padding (scipy mode='constant') over the
+// potential source the concentration kernel left in vsrc.
+__global__ void k_env_gauss_y(const double* __restrict__ vsrc, double* tmp, EnvConst e) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= e.G) return;
   const int i = k / e.nx, j = k - i * e.nx;
   double acc = 0.0;
+#pragma unroll
   for (int q = -4; q <= 4; ++q) {
     const int ii = i + q;
     if (ii < 0 || ii >= e.ny) continue;
-    const int kk = ii * e.nx + j;
-    double v = 0.0;
-    if (touched[kk]) {
-      double rho = 0.0;
-      for (int ion = 0; ion < e.I; ++ion) rho += e.zF[ion] * cenv[(size_t)ion * e.G + kk];
-      v = (rho * e.surf_scale) * e.inv_koeoer;
-    }
-    acc += e.gw[q + 4] * v;
+    acc += e.gw[q + 4] * vsrc[ii * e.nx + j];
   }
   tmp[k] = acc;
-  if (rho_env) {
-    double rho = 0.0;
-    for (int ion = 0; ion < e.I; ++ion) rho += e.zF[ion] * cenv[(size_t)ion * e.G + k];
-    rho_env[k] = rho;
-  }
 }
 
 // axis-1 pass of the Gaussian (+ Phi_b) -> v_env
@@ -179,12 +192,12 @@ __global__ void k_env_neg_grad(const double* __restrict__ F, double scale, doubl
   const int nx = e.nx;
   auto f = [&](int a, int bb) { return scale * F[a * nx + bb]; };
   double gx, gy;
-  if (j == 0) gx = (f(i, 1) - f(i, 0)) / e.delta;
-  else if (j == nx - 1) gx = (f(i, j) - f(i, j - 1)) / e.delta;
-  else gx = -(f(i, j - 1) - f(i, j + 1)) / (2 * e.delta);
-  if (i == 0) gy = (f(1, j) - f(0, j)) / e.delta;
-  else if (i == e.ny - 1) gy = (f(i, j) - f(i - 1, j)) / e.delta;
-  else gy = -(f(i - 1, j) - f(i + 1, j)) / (2 * e.delta);
+  if (j == 0) gx = (f(i, 1) - f(i, 0)) * e.inv_delta;
+  else if (j == nx - 1) gx = (f(i, j) - f(i, j - 1)) * e.inv_delta;
+  else gx = -(f(i, j - 1) - f(i, j + 1)) * e.inv_2delta;
+  if (i == 0) gy = (f(1, j) - f(0, j)) * e.inv_delta;
+  else if (i == e.ny - 1) gy = (f(i, j) - f(i - 1, j)) * e.inv_delta;
+  else gy = -(f(i - 1, j) - f(i + 1, j)) * e.inv_2delta;
   Ex[k] = -gx;
   Ey[k] = -gy;
 }

@@ -278,14 +278,16 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
   if (t < ncell) {
     const int cc = c0 + t;
     const int a0 = g.cell_ptr[cc] - m0, a1 = g.cell_ptr[cc + 1] - m0;
-    const double vol = g.cell_vol[cc];
+    // one FP64 division per cell: update_Co and the gap-junction term divide by
+    // cell_vol per ion; multiplying by 1/vol differs by at most one rounding
+    const double inv_vol = 1.0 / g.cell_vol[cc];
     double rho = 0.0, sig = 0.0;
     for (int i = 0; i < I; ++i) {
       double s1 = 0.0, s2 = 0.0;
       for (int j = a0; j < a1; ++j) { s1 += sA[i * TPB + j]; s2 += sB[i * TPB + j]; }
-      double x = p.cc[i * g.C + cc] + (s1 / vol) * k.dt;     // update_Co, sim_toolbox.py:1182-1183
+      double x = p.cc[i * g.C + cc] + (s1 * inv_vol) * k.dt;  // update_Co, sim_toolbox.py:1182-1183
       p.ccm_out[i * g.C + cc] = x;                            // cc_at_mem = cX_cell[mem_to_cells]
-      x = x + k.dt * (s2 / vol);                              // gap-junction term, sim.py:2105-2108
+      x = x + k.dt * (s2 * inv_vol);                          // gap-junction term, sim.py:2105-2108
       if (x != x) bad_conc++;
       if (x < 0.0) { x = 0.0; neg++; }                        // no_negs
       p.cc[i * g.C + cc] = x;
