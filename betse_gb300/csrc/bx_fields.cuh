@@ -50,7 +50,7 @@ __device__ __forceinline__ void df_dot_acc(float& sh, float& sl, float ah, float
 
 // Y[n x R] = A[n x n] X[n x R] with A and X in double-float, Y in FP64.
 // One warp per row; each lane streams 16-byte pieces (two elements) of the
-// row, four in flight; X (n*R*8 bytes) stays in L2/L1.  A row that starts
+// row, eight in flight; X (n*R*8 bytes) stays in L2/L1.  A row that starts
 // 8 bytes past a 16-byte boundary (odd n, odd row) peels its first element.
 template <int R>
 __global__ void __launch_bounds__(256) k_dense_rows_df(const float2* __restrict__ A, const float2* __restrict__ X,
@@ -87,15 +87,12 @@ __global__ void __launch_bounds__(256) k_dense_rows_df(const float2* __restrict_
     }
   };
   int q = lane;
-  for (; q + 96 < npair; q += 128) {
-    const float4 a0 = __ldcs(row4 + q);
-    const float4 a1 = __ldcs(row4 + q + 32);
-    const float4 a2 = __ldcs(row4 + q + 64);
-    const float4 a3 = __ldcs(row4 + q + 96);
-    consume(a0, q);
-    consume(a1, q + 32);
-    consume(a2, q + 64);
-    consume(a3, q + 96);
+  for (; q + 224 < npair; q += 256) {   // eight 16-byte loads per lane in flight
+    float4 a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = __ldcs(row4 + q + 32 * u);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) consume(a[u], q + 32 * u);
   }
   for (; q < npair; q += 32) consume(__ldcs(row4 + q), q);
   const int kt = k0 + 2 * npair;  // at most one element left

@@ -99,7 +99,7 @@ def install_reference(ref: str) -> None:
 ION_ORDER = ['Na', 'K', 'Cl', 'Ca', 'P', 'M']   # order of p.ions_dict (H off)
 
 
-def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9):
+def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpness=1.0):
     from betse.science.enum.enumconf import CellLatticeType, SolverType
     p = SimpleNamespace()
     # physical constants, parameters.py:1087-1122
@@ -134,7 +134,7 @@ def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9):
     p.grid_size = grid_size
     p.is_ecm = is_ecm
     p.cluster_open = True
-    p.sharpness = 1.0
+    p.sharpness = sharpness
     p.smooth_cells = 1 / 0.5
     p.true_cell_size = 1.0e-5
     p.cell_polarizability = 0.0
@@ -282,11 +282,11 @@ OUT_KEYS = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn',
 
 
 def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
-             dm_range=(1e-19, 1e-17), cell_space=26e-9):
+             dm_range=(1e-19, 1e-17), cell_space=26e-9, sharpness=1.0):
     from betse.science.sim import Simulator
     from betse.science.enum.enumphase import SimPhaseKind
     n_steps = max(checkpoints)
-    p = make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space)
+    p = make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space, sharpness)
     t0 = time.time()
     c = build_cells(p, radius, seed)
     t_seed = time.time() - t0
@@ -385,6 +385,9 @@ CASES = {
     # extracellular spaces on (finite-volume environment grid), 25 nm cleft
     'ecm_r50_s3': dict(radius=50e-6, seed=3, is_ecm=True, grid_size=20,
                        dt=5e-3, checkpoints=[1, 2, 50], cell_space=25e-9),
+    # extracellular spaces with environment smoothing (fd.integrator, sharpness < 1)
+    'ecm_r40_s5_sharp': dict(radius=40e-6, seed=5, is_ecm=True, grid_size=20,
+                             dt=5e-3, checkpoints=[1, 2, 30], cell_space=25e-9, sharpness=0.5),
     # a handful of cells: boundary-dominated edge case
     'noecm_r20_s2': dict(radius=20e-6, seed=2, is_ecm=False, grid_size=12,
                          dt=1e-2, checkpoints=[1, 20]),

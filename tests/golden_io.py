@@ -11,7 +11,7 @@ from types import SimpleNamespace
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
-CASES = ['noecm_r80_s1', 'noecm_r50_s7', 'ecm_r50_s3', 'noecm_r20_s2']
+CASES = ['noecm_r80_s1', 'noecm_r50_s7', 'ecm_r50_s3', 'ecm_r40_s5_sharp', 'noecm_r20_s2']
 
 
 def load(name):
