@@ -213,6 +213,37 @@ def init_time_to_steady(n_clusters=16, n_cells=5000):
             'cold': r['cold'], 'warm': w}
 
 
+def batch_fields_timing(n_clusters=128):
+    """Environment fields of a sweep at a sampled step: one tensor-core GEMM per
+    grid shape for all clusters (host wall time of bx_batch_env_fields, the
+    fields copied to the host)."""
+    import oracle.fields as off
+    from betse_gb300 import generator as gen
+    from betse_gb300.engine import BatchEngine
+    gs, ps, Dms, sts = gen.sweep_workload(n_clusters, 7, dt=5e-3)
+    b = BatchEngine(gs, ps, 'split')
+    b.set_membrane_diffusivity(Dms)
+    b.upload_states(sts)
+    b.step(2, outputs=True)
+    shapes = {}
+    for g in gs:
+        shapes.setdefault(tuple(g.grid_shape), g.delta)
+    for shp, d in shapes.items():
+        b.set_lap_env_inv_shape(np.linalg.inv(off.make_laplacian(*shp, d)), shp, d)
+    b.env_fields()
+    t = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        b.env_fields()
+        t.append(time.perf_counter() - t0)
+    b.close()
+    return {'clusters': n_clusters, 'grid_shapes': len(shapes), 'grid_cells': int(sum(g.n_grid for g in gs)),
+            'ms_per_sampled_step': 1e3 * min(t),
+            'gemms_per_sampled_step': 2 * len(shapes) * 2,
+            'note': 'all clusters of one grid shape share lapENVinv = delta^2 K(shape): their products run as one '
+                    'BF16x3 tcgen05 GEMM with a per-column delta^2 and one FP64 refinement'}
+
+
 def secondary(stream, flush):
     """Extra lines of evidence at N=1: the ECM workload's step rates and the
     environment-field products at its full grid (output-only, sampled steps)."""
@@ -545,6 +576,7 @@ def main():
     extra = init_steady = None
     if rank == 0 and world == 1 and args.workload == 'cluster100k' and not args.no_secondary:
         extra = secondary(stream, flush)
+        extra['batch_env_fields'] = batch_fields_timing()
         init_steady = init_time_to_steady()
 
     if rank == 0:

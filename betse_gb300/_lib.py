@@ -97,6 +97,8 @@ SIGNATURES = {
     'bx_status': (ct.c_int, [ct.c_void_p, ct.POINTER(BxStepStatus)]),
     'bx_set_lap_env_inv': (ct.c_int, [ct.c_void_p, _dp]),
     'bx_max_abs_dvm': (ct.c_int, [ct.c_void_p, _dp]),
+    'bx_batch_set_lap_env_inv': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_double, _dp]),
+    'bx_batch_env_fields': (ct.c_int, [ct.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     'bx_dense_op_create': (ct.c_int, [_dp, ct.c_int, ct.POINTER(ct.c_void_p)]),
     'bx_dense_op_set_forward': (ct.c_int, [ct.c_void_p, _ip, _ip, _dp]),
     'bx_dense_op_apply': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p,

@@ -137,6 +137,18 @@ struct bx_cluster {
   bool last_step_outputs = false;  // the latest bx_step computed outputs
   int* d_cl_mem = nullptr;         // membrane offsets of the clusters [ncl+1] (residual test)
   double* d_resid = nullptr;       // [ncl]
+  // ---- batched environment fields (bx_batch_env_fields)
+  std::vector<int> cl_ny, cl_nx, cl_goff;   // grid shape and offset in the concatenated grids
+  std::vector<double> cl_delta;
+  struct FieldShape {
+    int ny = 0, nx = 0, xoff = 0, ncols = 0, soff = 0;
+    std::vector<int> clusters;
+    bx_dense_op_handle op = nullptr;
+  };
+  std::vector<FieldShape> fshapes;
+  int Gtot = 0, Xtot = 0;
+  int *bf_ci = nullptr, *bf_last = nullptr;
+  double *bf_cd = nullptr, *bf_buf = nullptr, *bf_X = nullptr, *bf_Y = nullptr, *bf_scale = nullptr;
 };
 
 namespace {
@@ -155,9 +167,12 @@ void free_all(bx_cluster* h) {
       h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_vsrc, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
-      h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid};
+      h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
+      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (auto& fs : h->fshapes)
+    if (fs.op) bx_dense_op_destroy(fs.op);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
@@ -718,6 +733,11 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   };
   h->ncl = ncl; h->C = C; h->M = M; h->I = I;
   h->ny = gs[0].grid_ny; h->nx = gs[0].grid_nx; h->G = h->ny * h->nx;
+  for (int cl = 0; cl < ncl; ++cl) {
+    h->cl_ny.push_back(gs[cl].grid_ny);
+    h->cl_nx.push_back(gs[cl].grid_nx);
+    h->cl_delta.push_back(gs[cl].delta);
+  }
   h->precision = precision; h->par = p0; h->ecm = p0.is_ecm != 0;
   h->cl_par.assign(ps, ps + ncl);
   h->mode = (precision == BX_PLAIN_FP64) ? MODE_PLAIN : (h->ecm ? MODE_SPLIT_ECM : MODE_SPLIT);
@@ -1359,6 +1379,174 @@ int bx_max_abs_dvm(bx_handle h, double* per_cluster) {
   BX_CU(cudaMemcpyAsync(per_cluster, h->d_resid, (size_t)h->ncl * sizeof(double), cudaMemcpyDeviceToHost,
                         h->stream));
   BX_CU(cudaStreamSynchronize(h->stream));
+  return BX_OK;
+}
+
+namespace {
+
+bx::FieldGrid field_grid(const bx_cluster* h);
+constexpr int kBfPlanes = 17;
+
+// group the clusters by grid shape: each shape's operand has two columns per cluster
+void ensure_fshapes(bx_cluster* h) {
+  if (!h->fshapes.empty()) return;
+  h->cl_goff.assign(h->ncl + 1, 0);
+  for (int c = 0; c < h->ncl; ++c) {
+    h->cl_goff[c + 1] = h->cl_goff[c] + h->cl_ny[c] * h->cl_nx[c];
+    int s = -1;
+    for (size_t q = 0; q < h->fshapes.size(); ++q)
+      if (h->fshapes[q].ny == h->cl_ny[c] && h->fshapes[q].nx == h->cl_nx[c]) s = (int)q;
+    if (s < 0) {
+      bx_cluster::FieldShape fs;
+      fs.ny = h->cl_ny[c];
+      fs.nx = h->cl_nx[c];
+      h->fshapes.push_back(fs);
+      s = (int)h->fshapes.size() - 1;
+    }
+    h->fshapes[s].clusters.push_back(c);
+  }
+  h->Gtot = h->cl_goff[h->ncl];
+  int xo = 0, so = 0;
+  for (auto& fs : h->fshapes) {
+    fs.ncols = 2 * (int)fs.clusters.size();
+    fs.xoff = xo;
+    fs.soff = so;
+    xo += fs.ny * fs.nx * fs.ncols;
+    so += fs.ncols;
+  }
+  h->Xtot = xo;
+}
+
+int prepare_batch_fields(bx_cluster* h) {
+  if (h->bf_buf) return BX_OK;
+  const int ncl = h->ncl;
+  std::vector<int> ci((size_t)ncl * bx::kCi), last(h->Gtot, -1);
+  std::vector<double> cd((size_t)ncl * 2), scale(2 * ncl);
+  for (const auto& fs : h->fshapes) {
+    for (size_t j = 0; j < fs.clusters.size(); ++j) {
+      const int c = fs.clusters[j];
+      int* e = &ci[(size_t)c * bx::kCi];
+      e[0] = h->cl_goff[c]; e[1] = fs.ny; e[2] = fs.nx; e[3] = fs.xoff; e[4] = 2 * (int)j; e[5] = fs.ncols;
+      e[6] = h->cl_mem[c]; e[7] = h->cl_cell[c];
+      const double d2 = h->cl_delta[c] * h->cl_delta[c];   // lapENVinv = delta^2 K(shape)
+      scale[fs.soff + 2 * j] = d2;
+      scale[fs.soff + 2 * j + 1] = d2;
+    }
+  }
+  for (int c = 0; c < ncl; ++c) {
+    cd[2 * c] = h->cl_delta[c];
+    cd[2 * c + 1] = h->cl_par[c].sigma;
+    for (int m = h->cl_mem[c]; m < h->cl_mem[c + 1]; ++m) last[h->cl_goff[c] + h->h_map_env[m]] = m;
+  }
+  if (cudaMalloc(&h->bf_ci, ci.size() * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&h->bf_last, (size_t)h->Gtot * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&h->bf_cd, cd.size() * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&h->bf_scale, scale.size() * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&h->bf_X, (size_t)h->Xtot * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&h->bf_Y, (size_t)h->Xtot * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&h->bf_buf, (size_t)kBfPlanes * h->Gtot * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(BX_ENOMEM, "cudaMalloc batched field scratch");
+  }
+  BX_CU(cudaMemcpy(h->bf_ci, ci.data(), ci.size() * sizeof(int), cudaMemcpyHostToDevice));
+  BX_CU(cudaMemcpy(h->bf_last, last.data(), last.size() * sizeof(int), cudaMemcpyHostToDevice));
+  BX_CU(cudaMemcpy(h->bf_cd, cd.data(), cd.size() * sizeof(double), cudaMemcpyHostToDevice));
+  BX_CU(cudaMemcpy(h->bf_scale, scale.data(), scale.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return BX_OK;
+}
+
+}  // namespace
+
+int bx_batch_set_lap_env_inv(bx_handle h, int ny, int nx, double delta, const double* lap_env_inv) {
+  if (!h || !lap_env_inv || ny < 3 || nx < 3 || !(delta > 0.0)) return fail(BX_EINVAL, "bad arguments");
+  if (h->ecm) return fail(BX_EINVAL, "bx_batch_set_lap_env_inv: batches without extracellular spaces only");
+  ensure_fshapes(h);
+  bx_cluster::FieldShape* fs = nullptr;
+  for (auto& q : h->fshapes)
+    if (q.ny == ny && q.nx == nx) fs = &q;
+  if (!fs) return fail(BX_EINVAL, "bx_batch_set_lap_env_inv: no cluster of the batch has this grid shape");
+  const int G = ny * nx;
+  // the operator of unit spacing, K(shape) = lapENVinv / delta^2 (finitediff.py:426-429)
+  std::vector<double> A((size_t)G * G);
+  const double inv_d2 = 1.0 / (delta * delta);
+  for (size_t e = 0; e < A.size(); ++e) A[e] = lap_env_inv[e] * inv_d2;
+  if (fs->op) {
+    bx_dense_op_destroy(fs->op);
+    fs->op = nullptr;
+  }
+  int rc = bx_dense_op_create(A.data(), G, &fs->op);
+  if (rc != BX_OK) return rc;
+  // forward operator: makeLaplacian at unit spacing (finitediff.py:252-431):
+  // 5-point stencil inside, identity rows on the edges
+  std::vector<int> ptr(G + 1, 0), col;
+  std::vector<double> val;
+  for (int k = 0; k < G; ++k) {
+    const int i = k / nx, j = k % nx;
+    if (i == 0 || j == 0 || i == ny - 1 || j == nx - 1) {
+      col.push_back(k); val.push_back(1.0);
+    } else {
+      const int nb[5] = {k - nx, k - 1, k, k + 1, k + nx};
+      const double w[5] = {1.0, 1.0, -4.0, 1.0, 1.0};
+      for (int q = 0; q < 5; ++q) { col.push_back(nb[q]); val.push_back(w[q]); }
+    }
+    ptr[k + 1] = (int)col.size();
+  }
+  return bx_dense_op_set_forward(fs->op, ptr.data(), col.data(), val.data());
+}
+
+int bx_batch_env_fields(bx_handle h, const double* D_env_weight, double* v_env, double* E_env_x, double* E_env_y,
+                        double* J_env_x, double* J_env_y, double* B_field) {
+  if (!h) return fail(BX_EINVAL, "null handle");
+  if (h->ecm) return fail(BX_EINVAL, "bx_batch_env_fields: batches without extracellular spaces only");
+  if (!h->last_step_outputs) return fail(BX_ESTATE, "bx_batch_env_fields needs a last bx_step with want_outputs");
+  ensure_fshapes(h);
+  for (const auto& fs : h->fshapes)
+    if (!fs.op) return fail(BX_ESTATE, "bx_batch_env_fields: bx_batch_set_lap_env_inv missing for a grid shape");
+  int rc = prepare_batch_fields(h);
+  if (rc != BX_OK) return rc;
+  const int Gt = h->Gtot, ncl = h->ncl;
+  double* b[kBfPlanes];
+  for (int q = 0; q < kBfPlanes; ++q) b[q] = h->bf_buf + (size_t)q * Gt;
+  double *t0 = b[0], *t1 = b[1], *venv = b[2], *gx = b[3], *gy = b[4], *Frx = b[5], *Fry = b[6], *Fdx = b[7],
+         *Fdy = b[8], *Ex = b[9], *Ey = b[10], *jx = b[11], *jy = b[12], *Bf = b[13], *Jex = b[14], *Jey = b[15],
+         *w = b[16];
+  cudaStream_t s = h->stream;
+  if (D_env_weight) BX_CU(cudaMemcpyAsync(w, D_env_weight, (size_t)Gt * sizeof(double), cudaMemcpyHostToDevice, s));
+  bx::FieldGrid base = field_grid(h);
+  const double* vm = (h->mode == MODE_SPLIT) ? h->o_vm_mem : h->d_vm[h->parity ^ 1];
+  const int* ci = h->bf_ci;
+  const double* cd = h->bf_cd;
+  bx::kb_vce<<<ncl, 256, 0, s>>>(ci, cd, base, h->bf_last, h->d_m2c, vm, t0);
+  bx::kb_gauss<true><<<ncl, 256, 0, s>>>(ci, cd, base, t0, t1, 0);
+  bx::kb_gauss<true><<<ncl, 256, 0, s>>>(ci, cd, base, t1, venv, 1);
+  bx::kb_grad_delta<<<ncl, 256, 0, s>>>(ci, cd, base, venv, gx, gy);
+  auto products = [&]() -> int {
+    for (const auto& fs : h->fshapes) {
+      const int r = bx_dense_op_apply(fs.op, h->bf_X + fs.xoff, h->bf_Y + fs.xoff, fs.ncols, h->bf_scale + fs.soff,
+                                      1, s);
+      if (r != BX_OK) return r;
+    }
+    return BX_OK;
+  };
+  // smooth_flux(gradient(delta Phi)), then the current's Helmholtz-Hodge split
+  bx::kb_hh_rhs<<<ncl, 256, 0, s>>>(ci, cd, base, gx, gy, h->bf_X);
+  if ((rc = products()) != BX_OK) return rc;
+  bx::kb_hh_out<<<ncl, 256, 0, s>>>(ci, cd, base, h->bf_Y, 1.0, nullptr, Frx, Fry, Fdx, Fdy);
+  bx::kb_e_and_j<<<ncl, 256, 0, s>>>(ci, cd, base, Frx, Fry, Fdx, Fdy, D_env_weight ? w : nullptr, Ex, Ey, jx, jy);
+  bx::kb_hh_rhs<<<ncl, 256, 0, s>>>(ci, cd, base, jx, jy, h->bf_X);
+  if ((rc = products()) != BX_OK) return rc;
+  bx::kb_hh_out<<<ncl, 256, 0, s>>>(ci, cd, base, h->bf_Y, h->par.mu, Bf, Jex, Jey, nullptr, nullptr);
+  BX_CU(cudaGetLastError());
+  double* dst[6] = {v_env, E_env_x, E_env_y, J_env_x, J_env_y, B_field};
+  const double* src[6] = {venv, Ex, Ey, Jex, Jey, Bf};
+  for (int q = 0; q < 6; ++q)
+    if (dst[q]) BX_CU(cudaMemcpyAsync(dst[q], src[q], (size_t)Gt * sizeof(double), cudaMemcpyDeviceToHost, s));
+  BX_CU(cudaStreamSynchronize(s));
+  for (const auto& fs : h->fshapes) {
+    int timed_out = 0;
+    if ((rc = bx_dense_op_status(fs.op, &timed_out)) != BX_OK) return rc;
+    if (timed_out) return fail(BX_ECUDA, "bx_batch_env_fields: tensor-core pipeline wait timed out");
+  }
   return BX_OK;
 }
 

@@ -272,3 +272,146 @@ __global__ void k_fields_zf_sum(int G, int I, const double* __restrict__ fx, con
 }
 
 }  // namespace bx
+
+namespace bx {
+
+// ---------------------------------------------------------------------------
+// Batched environment fields: one CTA per cluster of a batch (each cluster
+// has its own, small grid), the two dense products per Helmholtz-Hodge split
+// done for all clusters of one grid shape as one GEMM (bx_dense_op_apply).
+// Per-cluster descriptor ci[c*kCi + .]: grid offset, ny, nx, X offset of the
+// cluster's shape, first column of the cluster in that shape's operand,
+// columns of that operand, first membrane, first cell; cd[c*2 + .]: grid
+// spacing, sigma.
+// ---------------------------------------------------------------------------
+constexpr int kCi = 8;
+
+__device__ __forceinline__ FieldGrid cluster_grid(const int* ci, const double* cd, int c, const FieldGrid& base) {
+  FieldGrid g = base;
+  g.ny = ci[c * kCi + 1];
+  g.nx = ci[c * kCi + 2];
+  g.G = g.ny * g.nx;
+  g.delta = cd[c * 2];
+  return g;
+}
+
+__global__ void kb_vce(const int* __restrict__ ci, const double* __restrict__ cd, FieldGrid base,
+                       const int* __restrict__ last_mem, const int* __restrict__ m2c, const double* __restrict__ vm,
+                       double* __restrict__ neg_vce) {
+  const int c = blockIdx.x;
+  const FieldGrid g = cluster_grid(ci, cd, c, base);
+  const int off = ci[c * kCi];
+  const int m0 = ci[c * kCi + 6], c0 = ci[c * kCi + 7];
+  for (int k = threadIdx.x; k < g.G; k += blockDim.x) {
+    // (vm/2)[mem_to_cells] within the cluster: its membrane vector indexed by
+    // its own cell indices (ion_current.py:120-122)
+    const int m = last_mem[off + k];
+    neg_vce[off + k] = (m >= 0) ? -(vm[m0 + (m2c[m] - c0)] / 2) : 0.0;
+  }
+}
+
+template <bool REFLECT>
+__global__ void kb_gauss(const int* __restrict__ ci, const double* __restrict__ cd, FieldGrid base,
+                         const double* __restrict__ in, double* __restrict__ out, int axis) {
+  const int c = blockIdx.x;
+  const FieldGrid g = cluster_grid(ci, cd, c, base);
+  const int off = ci[c * kCi];
+  for (int k = threadIdx.x; k < g.G; k += blockDim.x) {
+    const int i = k / g.nx, j = k - i * g.nx;
+    const int n = axis == 0 ? g.ny : g.nx;
+    const int pos = axis == 0 ? i : j;
+    double acc = 0.0;
+#pragma unroll
+    for (int t = -4; t <= 4; ++t) {
+      int r = pos + t;
+      if (REFLECT) {
+        while (r < 0 || r >= n) r = (r < 0) ? -r - 1 : 2 * n - r - 1;
+      } else if (r < 0 || r >= n) {
+        continue;
+      }
+      acc += g.gw[t + 4] * in[off + (axis == 0 ? r * g.nx + j : i * g.nx + r)];
+    }
+    out[off + k] = acc;
+  }
+}
+
+// (gx, gy) = gradient(delta_c * F) per cluster (ion_current.py:133)
+__global__ void kb_grad_delta(const int* __restrict__ ci, const double* __restrict__ cd, FieldGrid base,
+                              const double* __restrict__ F, double* __restrict__ gx, double* __restrict__ gy) {
+  const int c = blockIdx.x;
+  const FieldGrid g = cluster_grid(ci, cd, c, base);
+  const int off = ci[c * kCi];
+  for (int k = threadIdx.x; k < g.G; k += blockDim.x) {
+    double a, b;
+    fd_grad(F + off, 1, g.delta, k / g.nx, k % g.nx, g, a, b);
+    gx[off + k] = a;
+    gy[off + k] = b;
+  }
+}
+
+// HH_Decomp right-hand sides of each cluster into its two columns of its
+// shape's operand X[k][ncols] (FP64, row-major)
+__global__ void kb_hh_rhs(const int* __restrict__ ci, const double* __restrict__ cd, FieldGrid base,
+                          const double* __restrict__ Jx, const double* __restrict__ Jy, double* __restrict__ X) {
+  const int c = blockIdx.x;
+  const FieldGrid g = cluster_grid(ci, cd, c, base);
+  const int off = ci[c * kCi], xo = ci[c * kCi + 3], col = ci[c * kCi + 4], nc = ci[c * kCi + 5];
+  for (int k = threadIdx.x; k < g.G; k += blockDim.x) {
+    const int i = k / g.nx, j = k - i * g.nx;
+    double r0 = 0.0, r1 = 0.0;
+    if (!(i == 0 || j == 0 || i == g.ny - 1 || j == g.nx - 1)) {
+      r0 = -(ddx_in(Jy + off, -1.0, i, j, g) + ddy_in(Jx + off, 1.0, i, j, g));
+      r1 = ddx_in(Jx + off, 1.0, i, j, g) + ddy_in(Jy + off, 1.0, i, j, g);
+    }
+    X[xo + (size_t)k * nc + col] = r0;
+    X[xo + (size_t)k * nc + col + 1] = r1;
+  }
+}
+
+// from each cluster's two columns (AA, BB) of Y: AA_out = aa_scale AA (if
+// asked), (Fx, Fy) = (-dAA/dy, dAA/dx), (Gx, Gy) = grad BB (if asked)
+__global__ void kb_hh_out(const int* __restrict__ ci, const double* __restrict__ cd, FieldGrid base,
+                          const double* __restrict__ Y, double aa_scale, double* __restrict__ AA_out,
+                          double* __restrict__ Fx, double* __restrict__ Fy, double* __restrict__ Gx,
+                          double* __restrict__ Gy) {
+  const int c = blockIdx.x;
+  const FieldGrid g = cluster_grid(ci, cd, c, base);
+  const int off = ci[c * kCi], xo = ci[c * kCi + 3], col = ci[c * kCi + 4], nc = ci[c * kCi + 5];
+  const double* Ya = Y + xo + col;
+  for (int k = threadIdx.x; k < g.G; k += blockDim.x) {
+    const int i = k / g.nx, j = k - i * g.nx;
+    double ax, ay;
+    fd_grad(Ya, nc, 1.0, i, j, g, ax, ay);
+    if (AA_out) AA_out[off + k] = aa_scale * Ya[(size_t)k * nc];
+    Fx[off + k] = -ay;
+    Fy[off + k] = ax;
+    if (Gx) {
+      double bx_, by_;
+      fd_grad(Ya + 1, nc, 1.0, i, j, g, bx_, by_);
+      Gx[off + k] = bx_;
+      Gy[off + k] = by_;
+    }
+  }
+}
+
+__global__ void kb_e_and_j(const int* __restrict__ ci, const double* __restrict__ cd, FieldGrid base,
+                           const double* __restrict__ Frx, const double* __restrict__ Fry,
+                           const double* __restrict__ Fdx, const double* __restrict__ Fdy,
+                           const double* __restrict__ w, double* __restrict__ Ex, double* __restrict__ Ey,
+                           double* __restrict__ Jx, double* __restrict__ Jy) {
+  const int c = blockIdx.x;
+  const FieldGrid g = cluster_grid(ci, cd, c, base);
+  const int off = ci[c * kCi];
+  const double sigma = cd[c * 2 + 1];
+  for (int k = off + threadIdx.x; k < off + g.G; k += blockDim.x) {
+    const double ex = -(Frx[k] + Fdx[k]);
+    const double ey = -(Fry[k] + Fdy[k]);
+    Ex[k] = ex;
+    Ey[k] = ey;
+    const double wk = w ? w[k] : 1.0;
+    Jx[k] = sigma * ex * wk;
+    Jy[k] = sigma * ey * wk;
+  }
+}
+
+}  // namespace bx

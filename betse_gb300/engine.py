@@ -271,6 +271,32 @@ class BatchEngine(ClusterEngine):
         _lib.check(self.lib.bx_state_download(self.h, ct.byref(st)), 'bx_state_download')
         return out
 
+    def set_lap_env_inv_shape(self, lap_env_inv, grid_shape, delta):
+        """lapENVinv of one cluster of the batch with this grid shape and spacing;
+        every cluster of that shape uses it (scaled by its own delta^2)."""
+        ny, nx = (int(x) for x in grid_shape)
+        A = _c(lap_env_inv)
+        if A.shape != (ny * nx, ny * nx):
+            raise ValueError(f'lapENVinv must be ({ny * nx}, {ny * nx})')
+        _lib.check(self.lib.bx_batch_set_lap_env_inv(self.h, ny, nx, float(delta), _lib.dptr(A)),
+                   'bx_batch_set_lap_env_inv')
+
+    def env_fields(self, D_env_weights=None):
+        """Environment fields of the last step for every cluster (list of dicts),
+        the dense products of each grid shape done as one tensor-core GEMM."""
+        sizes = [g.n_grid for g in self.geoms]
+        offs = np.concatenate([[0], np.cumsum(sizes)])
+        w = None
+        if D_env_weights is not None:
+            w = _c(np.concatenate([np.ravel(x) for x in D_env_weights]))
+            if w.shape != (offs[-1],):
+                raise ValueError('one D_env_weight per grid cell of every cluster')
+        names = ('v_env', 'E_env_x', 'E_env_y', 'J_env_x', 'J_env_y', 'B_field')
+        out = {k: np.empty(offs[-1]) for k in names}
+        _lib.check(self.lib.bx_batch_env_fields(self.h, _lib.dptr(w), *[_lib.dptr(out[k]) for k in names]),
+                   'bx_batch_env_fields')
+        return [{k: out[k][offs[c]:offs[c + 1]].copy() for k in names} for c in range(len(sizes))]
+
     def download_states(self):
         I = self.I
         vm, cc, cam = np.empty(self.M), np.empty((I, self.C)), np.empty((I, self.M))

@@ -230,6 +230,18 @@ int bx_set_lap_env_inv(bx_handle h, const double* lap_env_inv);
 int bx_env_fields(bx_handle h, const double* D_env_weight, double* v_env,
                   double* E_env_x, double* E_env_y, double* J_env_x,
                   double* J_env_y, double* B_field);
+/* Environment fields for a batch of clusters without ECM (a parameter sweep):
+ * clusters that share a grid shape share lapENVinv = delta^2 K(shape)
+ * (finitediff.py:426-429), so every product of every such cluster runs as one
+ * tcgen05 GEMM (bx_dense_op_*) with a per-column delta^2, refined once against
+ * the 5-point Laplacian.  bx_batch_set_lap_env_inv gives one cluster's
+ * lapENVinv (host, [ny*nx]^2) and its grid spacing for each grid shape in the
+ * batch; bx_batch_env_fields then returns the fields of the last step (which
+ * ran with want_outputs) for all clusters, concatenated over the clusters'
+ * grids in batch order (D_env_weight likewise, NULL = 1).  Synchronous. */
+int bx_batch_set_lap_env_inv(bx_handle h, int ny, int nx, double delta, const double* lap_env_inv);
+int bx_batch_env_fields(bx_handle h, const double* D_env_weight, double* v_env, double* E_env_x,
+                        double* E_env_y, double* J_env_x, double* J_env_y, double* B_field);
 /* Diagnostics: mean duration of bx_env_fields' device work and of one
  * two-column lapENVinv product over n runs (CUDA events). */
 int bx_time_env_fields(bx_handle h, int n, double* ms_fields, double* ms_product);
