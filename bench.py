@@ -217,8 +217,8 @@ def batch_fields_timing(n_clusters=128):
     """Environment fields of a sweep at a sampled step: one tensor-core GEMM per
     grid shape for all clusters (host wall time of bx_batch_env_fields, the
     fields copied to the host)."""
-    import oracle.fields as off
     from betse_gb300 import generator as gen
+    from betse_gb300.fields import lap_env_inverse
     from betse_gb300.engine import BatchEngine
     gs, ps, Dms, sts = gen.sweep_workload(n_clusters, 7, dt=5e-3)
     b = BatchEngine(gs, ps, 'split')
@@ -229,7 +229,7 @@ def batch_fields_timing(n_clusters=128):
     for g in gs:
         shapes.setdefault(tuple(g.grid_shape), g.delta)
     for shp, d in shapes.items():
-        b.set_lap_env_inv_shape(np.linalg.inv(off.make_laplacian(*shp, d)), shp, d)
+        b.set_lap_env_inv_shape(lap_env_inverse(*shp, d), shp, d)
     b.env_fields()
     t = []
     for _ in range(5):

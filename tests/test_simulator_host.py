@@ -61,3 +61,12 @@ def test_install_patches_and_returns_original():
     ph = _phase(grn_enabled=True)
     with pytest.raises(NotImplementedError, match='gene regulatory'):
         Simulator()._run_sim_core_loop(ph, np.arange(2), set(), None)
+
+
+def test_product_laplacian_matches_oracle():
+    import oracle
+    from betse_gb300.fields import lap_env_inverse, make_laplacian
+    L = make_laplacian(9, 11, 2.5e-6).toarray()
+    assert np.array_equal(L, oracle.fields.make_laplacian(9, 11, 2.5e-6))
+    A = lap_env_inverse(9, 11, 2.5e-6)
+    assert np.allclose(A @ L, np.eye(99), atol=1e-10)
