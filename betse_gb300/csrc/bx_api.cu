@@ -60,7 +60,7 @@ constexpr int kEnvTPB = 256;
 constexpr int kTPB = 256;        // membrane slots per CTA of the cell kernels
 constexpr int kRec = 8;          // floats per cell record of the split form (<= 7 ions + Vmem)
 
-enum Mode { MODE_PLAIN = 0, MODE_SPLIT = 1, MODE_SPLIT_ECM = 2 };
+enum Mode { MODE_PLAIN = 0, MODE_SPLIT = 1 };
 
 }  // namespace
 
@@ -317,6 +317,8 @@ bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
   p.o_fmem = h->o_fmem; p.o_fgj = h->o_fgj; p.o_rate = h->o_rate; p.o_rho = h->o_rho;
   p.o_vmem = h->o_vmc;
   p.o_drho = h->o_drho;
+  p.cenv_grid = h->ecm ? h->d_cenv : nullptr;
+  p.mfs = h->d_mem_flux_sa;
   return p;
 }
 
@@ -364,13 +366,19 @@ cudaError_t launch_pdl(void (*kern)(KArgs...), unsigned grid, unsigned block, cu
   return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
-template <int TPB, bool OUT, bool PHIB>
+template <int TPB, bool OUT, bool PHIB, bool ECM>
 cudaError_t launch_split_t(bx_cluster* h, int parity, cudaStream_t s) {
   if (is_betse_six_ions(h))
-    return launch_pdl(bx::k_split_step<TPB, kRec, 1, OUT, PHIB>, (unsigned)h->nblk, TPB, s, split_geom(h),
+    return launch_pdl(bx::k_split_step<TPB, kRec, 1, OUT, PHIB, ECM>, (unsigned)h->nblk, TPB, s, split_geom(h),
                       split_ptrs(h, parity), make_split_const(h));
-  return launch_pdl(bx::k_split_step<TPB, kRec, 0, OUT, PHIB>, (unsigned)h->nblk, TPB, s, split_geom(h),
+  return launch_pdl(bx::k_split_step<TPB, kRec, 0, OUT, PHIB, ECM>, (unsigned)h->nblk, TPB, s, split_geom(h),
                     split_ptrs(h, parity), make_split_const(h));
+}
+
+template <int TPB, bool OUT, bool PHIB>
+cudaError_t launch_split_e(bx_cluster* h, int parity, cudaStream_t s) {
+  return h->ecm ? launch_split_t<TPB, OUT, PHIB, true>(h, parity, s)
+                : launch_split_t<TPB, OUT, PHIB, false>(h, parity, s);
 }
 
 // the persistent kernel: one wave of CTAs walking the tiles
@@ -394,21 +402,21 @@ cudaError_t launch_persist_t(bx_cluster* h, int parity, cudaStream_t s) {
 }
 
 cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
-  if (h->persist && !out && !h->phib_nonzero) {
+  if (h->persist && !out && !h->phib_nonzero && !h->ecm) {
     const bool six = is_betse_six_ions(h);
     if (h->tpb == 192) return six ? launch_persist_t<192, 1>(h, parity, s) : launch_persist_t<192, 0>(h, parity, s);
     return six ? launch_persist_t<256, 1>(h, parity, s) : launch_persist_t<256, 0>(h, parity, s);
   }
   const int code = (h->tpb == 192 ? 4 : 0) | (out ? 2 : 0) | (h->phib_nonzero ? 1 : 0);
   switch (code) {
-    case 0: return launch_split_t<256, false, false>(h, parity, s);
-    case 1: return launch_split_t<256, false, true>(h, parity, s);
-    case 2: return launch_split_t<256, true, false>(h, parity, s);
-    case 3: return launch_split_t<256, true, true>(h, parity, s);
-    case 4: return launch_split_t<192, false, false>(h, parity, s);
-    case 5: return launch_split_t<192, false, true>(h, parity, s);
-    case 6: return launch_split_t<192, true, false>(h, parity, s);
-    default: return launch_split_t<192, true, true>(h, parity, s);
+    case 0: return launch_split_e<256, false, false>(h, parity, s);
+    case 1: return launch_split_e<256, false, true>(h, parity, s);
+    case 2: return launch_split_e<256, true, false>(h, parity, s);
+    case 3: return launch_split_e<256, true, true>(h, parity, s);
+    case 4: return launch_split_e<192, false, false>(h, parity, s);
+    case 5: return launch_split_e<192, false, true>(h, parity, s);
+    case 6: return launch_split_e<192, true, false>(h, parity, s);
+    default: return launch_split_e<192, true, true>(h, parity, s);
   }
 }
 
@@ -421,11 +429,34 @@ cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   bx::DevGeom g = dev_geom(h);
   bx::StepConst k = make_step_const(h);
   bx::StepPtrs p = step_ptrs(h, parity);
-  if (h->mode == MODE_SPLIT_ECM)
-    return h->tpb == 128 ? bx::launch_cell_step<float, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k)
-                         : bx::launch_cell_step<float, 256>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
   return h->tpb == 128 ? bx::launch_cell_step<double, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k)
                        : bx::launch_cell_step<double, 256>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+}
+
+// The extracellular grid of one step (update_ecm, update_Co's ECM term, get_current's E_env).
+cudaError_t enqueue_env(bx_cluster* h, bool out, cudaStream_t s) {
+  bx::EnvConst ec = make_env_const(h);
+  const int gg = env_grid(h->G);
+  const int gi = env_grid(h->G * h->I);   // one thread per (ion, grid cell)
+  bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
+  if (h->par.sharpness < 1.0) {
+    bx::k_env_update<false><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_fx, h->d_fy, h->d_env_ptr,
+                                                  h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
+    bx::k_env_integrate_scatter<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_env_ptr, h->d_env_mem,
+                                                      h->d_mem_flux_sa, h->M, ec);
+    h->launches += 3;
+  } else {
+    bx::k_env_update<true><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, nullptr, h->d_fx, h->d_fy, h->d_env_ptr,
+                                                 h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
+    h->launches += 2;
+  }
+  bx::k_env_charge<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_touched, h->d_vsrc, out ? h->d_rho_env : nullptr, ec);
+  h->launches += 1;
+  bx::k_env_gauss_y<<<gg, kEnvTPB, 0, s>>>(h->d_vsrc, h->d_tmp, ec);
+  bx::k_env_gauss_x<<<gg, kEnvTPB, 0, s>>>(h->d_tmp, h->phib_nonzero ? h->d_phib : nullptr, h->d_venv, ec);
+  bx::k_env_neg_grad<<<gg, kEnvTPB, 0, s>>>(h->d_venv, ec.screen, h->d_Ex, h->d_Ey, ec);
+  h->launches += 3;
+  return cudaGetLastError();
 }
 
 // Enqueue one time step (reads parity, writes parity^1).
@@ -434,9 +465,14 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   if (h->mode == MODE_SPLIT) {
     e = launch_split(h, parity, out, s);
     if (e != cudaSuccess) return e;
-    e = launch_split_env(h, s);
+    h->launches += 1;
+    if (h->ecm) {
+      e = enqueue_env(h, out, s);
+    } else {
+      e = launch_split_env(h, s);
+      h->launches += 1;
+    }
     if (e != cudaSuccess) return e;
-    h->launches += 2;
     if (out) {
       bx::SplitOutGeom og{h->C, h->M, h->I, h->d_cell_ptr, h->d_blk, h->d_nn, h->d_map_env,
                           h->d_mem_sa, h->d_nx, h->d_ny, h->d_swm, h->d_swo, h->d_cell_sa,
@@ -467,35 +503,12 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
     h->launches++;
     return cudaGetLastError();
   }
-  bx::EnvConst ec = make_env_const(h);
-  const int gg = env_grid(h->G);
-  bx::k_env_np_flux<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
-  double* rho_out = out ? h->d_rho_env : nullptr;
-  if (h->par.sharpness < 1.0) {
-    bx::k_env_update<false><<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_fx, h->d_fy, h->d_env_ptr,
-                                                  h->d_env_mem, h->d_mem_flux_sa, h->M, h->d_touched,
-                                                  h->d_vsrc, rho_out, ec);
-    bx::k_env_integrate_scatter<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_env_ptr, h->d_env_mem,
-                                                      h->d_mem_flux_sa, h->M, h->d_touched, h->d_vsrc,
-                                                      rho_out, ec);
-    h->launches += 3;
-  } else {
-    bx::k_env_update<true><<<gg, kEnvTPB, 0, s>>>(h->d_cenv, nullptr, h->d_fx, h->d_fy, h->d_env_ptr,
-                                                 h->d_env_mem, h->d_mem_flux_sa, h->M, h->d_touched,
-                                                 h->d_vsrc, rho_out, ec);
-    h->launches += 2;
-  }
-  bx::k_env_gauss_y<<<gg, kEnvTPB, 0, s>>>(h->d_vsrc, h->d_tmp, ec);
-  bx::k_env_gauss_x<<<gg, kEnvTPB, 0, s>>>(h->d_tmp, h->phib_nonzero ? h->d_phib : nullptr, h->d_venv, ec);
-  bx::k_env_neg_grad<<<gg, kEnvTPB, 0, s>>>(h->d_venv, ec.screen, h->d_Ex, h->d_Ey, ec);
-  h->launches += 3;
-  return cudaGetLastError();
+  return enqueue_env(h, out, s);
 }
 
 int launches_per_step(const bx_cluster* h) {
-  if (h->mode == MODE_SPLIT) return 2;
   if (!h->ecm) return 2;
-  return h->par.sharpness < 1.0 ? 7 : 6;
+  return h->par.sharpness < 1.0 ? 8 : 7;
 }
 
 // per-cluster constants that depend on the parameters (dt, cm, alpha_NaK, vol_env)
@@ -740,7 +753,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   }
   h->precision = precision; h->par = p0; h->ecm = p0.is_ecm != 0;
   h->cl_par.assign(ps, ps + ncl);
-  h->mode = (precision == BX_PLAIN_FP64) ? MODE_PLAIN : (h->ecm ? MODE_SPLIT_ECM : MODE_SPLIT);
+  h->mode = (precision == BX_PLAIN_FP64) ? MODE_PLAIN : MODE_SPLIT;
   if (h->mode == MODE_SPLIT && I > kRec - 1) {
     delete h;
     return fail(BX_EINVAL, "the split form holds at most 7 ions (BETSE's full ion set)");
@@ -826,17 +839,13 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   if (h->mode == MODE_SPLIT) {
     // host copies for the tile-major relayout (build_split_layout)
     h->h_msa = msa; h->h_gjw = gjw; h->h_bflag = bflag; h->h_nn = nn; h->h_vol = vol; h->h_div = div;
-    ALLOC(h->s_cenv_f, (size_t)ncl * I); ALLOC(h->d_cenv, (size_t)ncl * I);
+    ALLOC(h->s_cenv_f, (size_t)ncl * I); ALLOC(h->d_cenv, h->ecm ? (size_t)I * G : (size_t)ncl * I);
     ALLOC(h->s_pump, ncl);
     ALLOC(h->s_phib, G);
     if (cudaMemset(h->s_phib, 0, (size_t)G * sizeof(float)) != cudaSuccess) return bail(BX_ECUDA, "cudaMemset");
     ALLOC(h->o_vmc, C); ALLOC(h->o_vm_mem, M); ALLOC(h->o_drho, C);
   } else {
-    std::vector<float> fsa(M), fgw(M);
-    for (int m = 0; m < M; ++m) { fsa[m] = (float)msa[m]; fgw[m] = (float)gjw[m]; }
-    ALLOC(h->d_mem_sa_f, M); H2D(h->d_mem_sa_f, fsa.data(), M);
-    ALLOC(h->d_gj_w_f, M); H2D(h->d_gj_w_f, fgw.data(), M);
-    if (h->mode == MODE_SPLIT_ECM) { ALLOC(h->d_Dm_f, (size_t)I * M); } else { ALLOC(h->d_Dm, (size_t)I * M); }
+    ALLOC(h->d_Dm, (size_t)I * M);
     ALLOC(h->d_vm[0], M); ALLOC(h->d_vm[1], M);
     ALLOC(h->d_ccm[0], (size_t)I * C); ALLOC(h->d_ccm[1], (size_t)I * C);
     ALLOC(h->d_cc, (size_t)I * C);
@@ -1015,12 +1024,17 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
         cc2[(size_t)i * S + sc] = make_float2(hi, (float)(x - (double)hi));
       }
     }
-    std::vector<float> cef(nenv);
-    for (size_t q = 0; q < nenv; ++q) cef[q] = (float)s->cc_env[q];
     BX_CU(h2d(h->s_rec[0], rec.data(), rec.size()));
     BX_CU(h2d(h->s_cc2, cc2.data(), cc2.size()));
     BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
-    BX_CU(h2d(h->s_cenv_f, cef.data(), nenv));
+    if (h->ecm) {
+      BX_CU(h2d(h->d_Ex, s->E_env_x, h->G));
+      BX_CU(h2d(h->d_Ey, s->E_env_y, h->G));
+    } else {
+      std::vector<float> cef(nenv);
+      for (size_t q = 0; q < nenv; ++q) cef[q] = (float)s->cc_env[q];
+      BX_CU(h2d(h->s_cenv_f, cef.data(), nenv));
+    }
   } else {
     BX_CU(h2d(h->d_vm[0], s->vm, M));
     BX_CU(h2d(h->d_cc, s->cc_cells, (size_t)I * C));
@@ -1063,6 +1077,10 @@ int bx_state_download(bx_handle h, bx_state* s) {
         }
         ccm[(size_t)i * C + c] = (double)rec[(size_t)sc * kRec + i];
       }
+    }
+    if (h->ecm) {
+      if (s->E_env_x) BX_CU(cudaMemcpy(s->E_env_x, h->d_Ex, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
+      if (s->E_env_y) BX_CU(cudaMemcpy(s->E_env_y, h->d_Ey, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
     }
   } else {
     if (s->vm) BX_CU(cudaMemcpy(s->vm, h->d_vm[h->parity], (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1226,10 +1244,12 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
   if (h->mode == MODE_SPLIT) {
     // membrane: Dm (4I), nn_slot 4, lcell 1, mem_sa 4, gjw 4
     // cell: cc2 in+out 16I, record in+out 2*4*kRec, dt/vol 4, diviterm/cm 4, range 4
-    // tile: partial sums 4I, cluster id 4
+    // tile: partial sums 4I, cluster id 4; ECM: map_env 4, grid concentration
+    // 8I and the f*sa export 8I per membrane instead of the partial sums
+    if (h->ecm) return M * (4 * I + 13 + 4 + 16 * I) + C * (16 * I + 8 * kRec + 12) + B * 4;
     return M * (4 * I + 13) + C * (16 * I + 8 * kRec + 12) + B * (4 * I + 4);
   }
-  const int64_t w = (h->mode == MODE_SPLIT_ECM) ? 4 : 8;  // Dm, mem_sa, gj_w width
+  const int64_t w = 8;  // Dm, mem_sa, gj_w width
   // membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env and the f*sa
   // export with ECM); cell: cc in+out, cc_mem in+out, cell_vol, diviterm, ptr
   const int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0);
@@ -1251,6 +1271,7 @@ int bx_set_launch_config(bx_handle h, int tpb, int persistent) {
   const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256) : (tpb == 128 || tpb == 256);
   if (!ok) return fail(BX_EINVAL, "unsupported CTA size for this form");
   if (persistent && h->mode != MODE_SPLIT) return fail(BX_EINVAL, "the persistent kernel is the split form's");
+  if (persistent && h->ecm) return fail(BX_EINVAL, "the persistent kernel has no extracellular-space variant");
   const size_t C = h->C, I = h->I, M = h->M;
   const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
   std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1);
@@ -1284,7 +1305,8 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   const int64_t launches0 = h->launches;
   struct Cand { int tpb; bool persist; };
   std::vector<Cand> cands;
-  if (h->mode == MODE_SPLIT) cands = {{256, false}, {192, false}, {256, true}, {192, true}};
+  if (h->mode == MODE_SPLIT && h->ecm) cands = {{256, false}, {192, false}};
+  else if (h->mode == MODE_SPLIT) cands = {{256, false}, {192, false}, {256, true}, {192, true}};
   else cands = {{256, false}, {128, false}};
   double best = 1e300;
   int best_tpb = h->tpb;

@@ -37,13 +37,15 @@ __device__ __forceinline__ double cb_at(const double* c, const EnvConst& e, int 
 // The grid kernels multiply by 1/delta and 1/(2 delta) where the reference
 // divides (a difference of at most one rounding): an FP64 division costs
 // GB300 several FP64-pipe operations, and the stencils are otherwise cheap.
+// One thread per (ion, grid cell): t = ion*G + k.
 __global__ void k_env_np_flux(const double* __restrict__ cenv, const double* __restrict__ Denv,
                               const double* __restrict__ Ex, const double* __restrict__ Ey,
                               double* fx, double* fy, EnvConst e) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= e.G) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e.I * e.G) return;
+  const int ion = t / e.G, k = t - ion * e.G;
   const int i = k / e.nx, j = k - i * e.nx;
-  for (int ion = 0; ion < e.I; ++ion) {
+  {
     const double c0 = cb_at(cenv, e, ion, i, j);
     double gcx, gcy;
     if (j == 0) gcx = (cb_at(cenv, e, ion, i, 1) - c0) * e.inv_delta;
@@ -87,20 +89,21 @@ __device__ __forceinline__ void env_charge_out(int k, double rho, const uint8_t*
   if (rho_env) rho_env[k] = rho;
 }
 
-// c <- cb + div(-f) dt  [+ membrane exchange and charge if FUSE_SCATTER]
+// c <- cb + div(-f) dt  [+ membrane exchange if FUSE_SCATTER]
 // (update_ecm sim.py:2247-2254, then update_Co's ECM term sim_toolbox.py:1189-1195
-//  with div_env = M_divmap_mem2ecm @ (-flux) / (cell_height delta^2), :1229-1232)
+//  with div_env = M_divmap_mem2ecm @ (-flux) / (cell_height delta^2), :1229-1232).
+// One thread per (ion, grid cell); while the new concentration is written in
+// place, the kernel reads only fluxes and its own cell's value.
 template <bool FUSE_SCATTER>
 __global__ void k_env_update(double* cenv, double* tmp, const double* __restrict__ fx,
                              const double* __restrict__ fy, const int* __restrict__ env_ptr,
                              const int* __restrict__ env_mem, const double* __restrict__ mem_flux_sa,
-                             int M, const uint8_t* __restrict__ touched, double* vsrc, double* rho_env,
-                             EnvConst e) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= e.G) return;
+                             int M, EnvConst e) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e.I * e.G) return;
+  const int ion = t / e.G, k = t - ion * e.G;
   const int i = k / e.nx, j = k - i * e.nx;
-  double rho = 0.0;
-  for (int ion = 0; ion < e.I; ++ion) {
+  {
     const double* fxi = fx + (size_t)ion * e.G;
     const double* fyi = fy + (size_t)ion * e.G;
     const double div = ddx_neg(fxi, e, i, j) + ddy_neg(fyi, e, i, j);
@@ -110,27 +113,34 @@ __global__ void k_env_update(double* cenv, double* tmp, const double* __restrict
       for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
       c = c + (s * e.inv_h_d2) * e.dt;
       cenv[(size_t)ion * e.G + k] = c;
-      rho += e.zF[ion] * c;
     } else {
       tmp[(size_t)ion * e.G + k] = c;
     }
   }
-  if (FUSE_SCATTER) env_charge_out(k, rho, touched, vsrc, rho_env, e);
+}
+
+// The environment charge of each grid cell from its final concentrations
+// (ions in order), for get_current's ECM branch.
+__global__ void k_env_charge(const double* __restrict__ cenv, const uint8_t* __restrict__ touched, double* vsrc,
+                             double* rho_env, EnvConst e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e.G) return;
+  double rho = 0.0;
+  for (int ion = 0; ion < e.I; ++ion) rho += e.zF[ion] * cenv[(size_t)ion * e.G + k];
+  env_charge_out(k, rho, touched, vsrc, rho_env, e);
 }
 
 // fd.integrator (finitediff.py:1479-1512) when sharpness < 1, then the membrane
-// exchange and the charge.
+// exchange.  One thread per (ion, grid cell).
 __global__ void k_env_integrate_scatter(double* cenv, const double* __restrict__ tmp,
                                         const int* __restrict__ env_ptr, const int* __restrict__ env_mem,
-                                        const double* __restrict__ mem_flux_sa, int M,
-                                        const uint8_t* __restrict__ touched, double* vsrc, double* rho_env,
-                                        EnvConst e) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= e.G) return;
+                                        const double* __restrict__ mem_flux_sa, int M, EnvConst e) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e.I * e.G) return;
+  const int ion = t / e.G, k = t - ion * e.G;
   const int i = k / e.nx, j = k - i * e.nx;
   const double sides = (1 - e.sharpness) / 4;
-  double rho = 0.0;
-  for (int ion = 0; ion < e.I; ++ion) {
+  {
     const double* P = tmp + (size_t)ion * e.G;
     double F;
     if (on_edge(i, j, e.ny, e.nx)) {
@@ -144,11 +154,8 @@ __global__ void k_env_integrate_scatter(double* cenv, const double* __restrict__
     }
     double s = 0.0;
     for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
-    const double c = F + (s * e.inv_h_d2) * e.dt;
-    cenv[(size_t)ion * e.G + k] = c;
-    rho += e.zF[ion] * c;
+    cenv[(size_t)ion * e.G + k] = F + (s * e.inv_h_d2) * e.dt;
   }
-  env_charge_out(k, rho, touched, vsrc, rho_env, e);
 }
 
 // get_current ECM branch (ion_current.py:79-110): the axis-0 pass of a

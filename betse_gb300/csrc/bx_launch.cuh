@@ -1,6 +1,6 @@
-// bx_launch.cuh -- host-side launchers of the templated step kernels; the
-// instantiations live in bx_step_f64.cu (plain form) and bx_step_f32.cu
-// (split form) so the two compile in parallel.
+// bx_launch.cuh -- host-side launcher of the templated plain-form step kernel;
+// the instantiations live in bx_step_f64.cu so they compile in parallel with
+// the rest of the library.
 #pragma once
 #include "bx_kernels.cuh"
 

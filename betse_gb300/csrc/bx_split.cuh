@@ -165,6 +165,8 @@ struct SplitPtrs {
   const float* __restrict__ pump_coef;     // [ncl] -3 block alpha_NaK (0 = pump off)
   const float* __restrict__ phib;          // [G] (PHIB)
   float* __restrict__ env_part;            // [nblk][I] per-tile partial sums
+  const double* __restrict__ cenv_grid;    // [I][G] environment grid concentrations (ECM)
+  double* __restrict__ mfs;                // [I][M] f_mem*sa per membrane, natural order (ECM scatter)
   unsigned long long* status;              // nan_vm, nan_conc, neg clamps
   // outputs (OUT), natural order
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_vmem;
@@ -216,7 +218,10 @@ template <> struct IonSet<1> {
 //   membranes GHK + pump + gap-junction fluxes (FP32), per-ion f*sa into smem
 //   cells     warp i = ion i, lane = cell: update_all_concs in double-float
 //   charge    warp 0: rho = sum_i z_i F c_i (double-float) -> Vmem record
-template <int TPB, int REC, int ZP, bool OUT, bool PHIB>
+// ECM: the environment concentration of each membrane is its grid cell's
+// (cc_env[i][map_mem2ecm], sim.py:1256-1259) and f_mem*sa is exported for the
+// grid scatter (update_Co's ECM term) instead of the well-mixed partials.
+template <int TPB, int REC, int ZP, bool OUT, bool PHIB, bool ECM = false>
 __global__ void __launch_bounds__(TPB, 2048 / TPB / 2)
 k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   using IS = IonSet<ZP>;
@@ -267,10 +272,16 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   float own[REC], nbr[REC];
   load_rec<REC>(p.rec_in, s0 + (active ? lc : 0), own);
   load_rec<REC>(p.rec_in, cn, nbr);
-  const float* ce = p.cenv_f + (size_t)cl * I;
   float cenv[NI];
+  if (ECM) {
+    const int ge = active ? g.map_env[q] : 0;
 #pragma unroll
-  for (int i = 0; i < NI; ++i) cenv[i] = (i < I) ? ce[i] : 0.f;
+    for (int i = 0; i < NI; ++i) cenv[i] = (i < I && active) ? (float)p.cenv_grid[(size_t)i * g.G + ge] : 0.f;
+  } else {
+    const float* ce = p.cenv_f + (size_t)cl * I;
+#pragma unroll
+    for (int i = 0; i < NI; ++i) cenv[i] = (i < I) ? ce[i] : 0.f;
+  }
   const float pc = p.pump_coef[cl];
 
   if (active) {
@@ -314,6 +325,7 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
       const float fg = ghk_flux_fk(sg, ka_g, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], k.dgj_gs[i] * gw, k.inv_gjl);
       sA[i][t] = f * sa;
       sB[i][t] = -fg * sa;
+      if (ECM) p.mfs[(size_t)i * g.M + g.tile_m0[b] + t] = (double)(f * sa);
       if (OUT) {
         const int mn = g.tile_m0[b] + t;
         p.o_fmem[(size_t)i * g.M + mn] = (double)f;
@@ -337,7 +349,7 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     float e = s1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
-    if (lane == 0) p.env_part[(size_t)b * I + wid] = e;
+    if (!ECM && lane == 0) p.env_part[(size_t)b * I + wid] = e;
   }
   if (cell_live) {
     const int i = wid;
