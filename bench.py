@@ -71,6 +71,19 @@ def _env_int(name, default):
         return default
 
 
+def job_throughput(t_local, units_per_rank, world, dist=None, device=None):
+    """Whole-job throughput of N replicas: every rank processed units_per_rank in
+    t_local seconds; the job time is the maximum over ranks.  Returns (t_max,
+    units of all ranks / t_max)."""
+    t_max = t_local
+    if dist is not None:
+        import torch
+        tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    return t_max, units_per_rank * world / t_max
+
+
 def bf16_peak():
     path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
     if os.path.exists(path):
@@ -503,14 +516,7 @@ def main():
     split.check_stable()
     plain.check_stable()
 
-    t_local = sum(ms_split) / 1e3
-    if dist is not None:
-        tt = torch.tensor([t_local], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    else:
-        t_max = t_local
-    value = n_mems * T * args.steps * world / t_max
+    t_max, value = job_throughput(sum(ms_split) / 1e3, n_mems * T * args.steps, world, dist, dev)
     plain_value = n_mems * T * len(ms_plain) / (sum(ms_plain) / 1e3)
 
     # ---- Vmem error of the split form against the plain FP64 form, equal steps
