@@ -308,7 +308,7 @@ def secondary(stream, flush):
             'ms_per_sampled_step': ms_f, 'product_ms': ms_p, 'products_per_sample': 1,
             'roofline': {'bound': 'hbm', 'achieved': gbs, 'peak': hbm, 'unit': 'GB/s',
                          'frac': gbs / hbm, 'algorithmic_bytes_per_launch': 8 * G * G,
-                         'kernel': 'k_dense_rows_df<2>', 'peak_source': src}}
+                         'kernel': 'k_dense_rows2_df', 'peak_source': src}}
     fields_eng.close()
     # tensor-core stage: BF16x3 dense-operator GEMM (lapGJinv-sized, 20k cells)
     from betse_gb300.dense import DenseOperator
@@ -365,7 +365,7 @@ def profile_kernel(which):
     """One small launch sequence of a dense-product kernel for ncu captures:
     'gemm' -- k_gemm_bf16x3 on an 8192 x 8192 operator with 1024 right-hand
     sides (two warm-up launches, then the captured one); 'fields' --
-    k_dense_rows_df<2> on a 12000 x 12000 double-float operator."""
+    k_dense_rows2_df on a 12000 x 12000 double-float operator."""
     from betse_gb300.build import build
     build()
     if which == 'gemm':

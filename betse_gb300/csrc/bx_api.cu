@@ -130,7 +130,8 @@ struct bx_cluster {
   std::vector<int> h_cell_ptr, h_m2c, h_map_env;
   std::vector<double> h_phib;
   // ---- environment fields on demand (bx_env_fields)
-  float2* f_lap = nullptr;         // lapENVinv as double-float pairs [G][G]
+  float2* f_lap = nullptr;         // lapENVinv as double-float pairs [G][f_ld], columns >= G zero
+  int f_ld = 0;                    // row pitch of f_lap (G rounded up to even)
   float2* f_X = nullptr;           // two-column right-hand side [G][2]
   double* f_buf = nullptr;         // field scratch, kFieldBufs x [G]
   int* f_last = nullptr;           // last membrane of each grid cell (-1: none)
@@ -1576,7 +1577,9 @@ int bx_set_lap_env_inv(bx_handle h, const double* lap_env_inv) {
   if (!h || !lap_env_inv) return fail(BX_EINVAL, "null argument");
   if (h->ncl != 1) return fail(BX_EINVAL, "bx_set_lap_env_inv: single-cluster handles only");
   const size_t G = (size_t)h->G;
-  if (!h->f_lap && cudaMalloc(&h->f_lap, G * G * sizeof(float2)) != cudaSuccess) {
+  const size_t ld = G + (G & 1);
+  h->f_ld = (int)ld;
+  if (!h->f_lap && cudaMalloc(&h->f_lap, G * ld * sizeof(float2)) != cudaSuccess) {
     h->f_lap = nullptr;
     cudaGetLastError();
     return fail(BX_ENOMEM, "cudaMalloc lapENVinv");
@@ -1594,9 +1597,9 @@ int bx_set_lap_env_inv(bx_handle h, const double* lap_env_inv) {
     cudaError_t e = cudaMemcpyAsync(stage, lap_env_inv + r0 * G, nr * G * sizeof(double), cudaMemcpyHostToDevice,
                                     h->stream);
     if (e == cudaSuccess) {
-      const size_t n = nr * G;
+      const size_t n = nr * ld;
       const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)h->sm_count * 16);
-      bx::k_to_df<<<blocks, 256, 0, h->stream>>>(stage, h->f_lap + r0 * G, n);
+      bx::k_to_df_rows<<<blocks, 256, 0, h->stream>>>(stage, (int)nr, (int)G, h->f_lap + r0 * ld, (int)ld);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -1633,7 +1636,7 @@ int enqueue_env_fields(bx_cluster* h, const double* d_w) {
   double *t0 = b[6], *t1 = b[7], *t2 = b[8], *t3 = b[9], *Y = b[10];  // Y spans b[10], b[11]
   double *jx = b[12], *jy = b[13];
   const unsigned gg = (unsigned)((G + 255) / 256);
-  const unsigned rows = (unsigned)(((size_t)G * 32 + 255) / 256);
+  const unsigned rows = (unsigned)((((size_t)G + 1) / 2 * 32 + 255) / 256);   // a warp per row pair
   if (!h->ecm) {
     const double* vm = (h->mode == MODE_SPLIT) ? h->o_vm_mem : h->d_vm[h->parity ^ 1];
     bx::k_fields_vce<<<gg, 256, 0, s>>>(G, h->f_last, h->d_m2c, vm, t0);
@@ -1642,7 +1645,7 @@ int enqueue_env_fields(bx_cluster* h, const double* d_w) {
     // smooth_flux(gradient(delta * Phi)) (ion_current.py:133-136)
     bx::k_fields_grad<<<gg, 256, 0, s>>>(venv, h->delta, t0, t1, fg);
     bx::k_fields_hh_rhs<<<gg, 256, 0, s>>>(t0, t1, h->f_X, fg);
-    bx::k_dense_rows_df<2><<<rows, 256, 0, s>>>(h->f_lap, h->f_X, Y, G);
+    bx::k_dense_rows2_df<<<rows, 256, 0, s>>>(h->f_lap, h->f_ld, h->f_X, Y, G);
     bx::k_fields_hh_out<<<gg, 256, 0, s>>>(Y, 1.0, nullptr, t0, t1, t2, t3, fg);
     bx::k_fields_e_and_j<<<gg, 256, 0, s>>>(G, t0, t1, t2, t3, d_w, h->par.sigma, Ex, Ey, jx, jy);
   } else {
@@ -1655,7 +1658,7 @@ int enqueue_env_fields(bx_cluster* h, const double* d_w) {
   }
   // J_env, B_field: Helmholtz-Hodge split of the current (ion_current.py:70, 147)
   bx::k_fields_hh_rhs<<<gg, 256, 0, s>>>(jx, jy, h->f_X, fg);
-  bx::k_dense_rows_df<2><<<rows, 256, 0, s>>>(h->f_lap, h->f_X, Y, G);
+  bx::k_dense_rows2_df<<<rows, 256, 0, s>>>(h->f_lap, h->f_ld, h->f_X, Y, G);
   bx::k_fields_hh_out<<<gg, 256, 0, s>>>(Y, h->par.mu, Bf, Jex, Jey, nullptr, nullptr, fg);
   BX_CU(cudaGetLastError());
   return BX_OK;
@@ -1668,11 +1671,12 @@ int prepare_env_fields(bx_cluster* h, const double* D_env_weight, double** d_w) 
   const size_t G = (size_t)h->G;
   if (!h->f_buf) {
     if (cudaMalloc(&h->f_buf, (kFieldBufs + 1) * G * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&h->f_X, 2 * G * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&h->f_X, 2 * (G + 1) * sizeof(float2)) != cudaSuccess ||
         cudaMalloc(&h->f_last, G * sizeof(int)) != cudaSuccess) {
       cudaGetLastError();
       return fail(BX_ENOMEM, "cudaMalloc field scratch");
     }
+    BX_CU(cudaMemset(h->f_X, 0, 2 * (G + 1) * sizeof(float2)));   // the padding row stays zero
     std::vector<int> last(G, -1);
     for (int m = 0; m < h->M; ++m) last[h->h_map_env[m]] = m;  // numpy keeps the last repeat
     BX_CU(cudaMemcpy(h->f_last, last.data(), G * sizeof(int), cudaMemcpyHostToDevice));
@@ -1716,14 +1720,14 @@ int bx_time_env_fields(bx_handle h, int n, double* ms_fields, double* ms_product
   BX_CU(cudaEventCreate(&e1));
   BX_CU(cudaEventCreate(&e2));
   const int G = h->G;
-  const unsigned rows = (unsigned)(((size_t)G * 32 + 255) / 256);
+  const unsigned rows = (unsigned)((((size_t)G + 1) / 2 * 32 + 255) / 256);
   double tf = 0.0, tp = 0.0;
   for (int q = 0; q < n; ++q) {
     BX_CU(cudaEventRecord(e0, h->stream));
     rc = enqueue_env_fields(h, d_w);
     if (rc != BX_OK) break;
     BX_CU(cudaEventRecord(e1, h->stream));
-    bx::k_dense_rows_df<2><<<rows, 256, 0, h->stream>>>(h->f_lap, h->f_X, h->f_buf + (size_t)10 * G, G);
+    bx::k_dense_rows2_df<<<rows, 256, 0, h->stream>>>(h->f_lap, h->f_ld, h->f_X, h->f_buf + (size_t)10 * G, G);
     BX_CU(cudaEventRecord(e2, h->stream));
     BX_CU(cudaEventSynchronize(e2));
     float a = 0.f, b = 0.f;

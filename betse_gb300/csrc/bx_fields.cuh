@@ -29,12 +29,6 @@ __device__ __forceinline__ float2 split_df(double a) {
   return make_float2(hi, lo);
 }
 
-// dst[i] = (hi, lo) of src[i]
-__global__ void k_to_df(const double* __restrict__ src, float2* __restrict__ dst, size_t n) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = split_df(src[i]);
-}
-
 // (sh, sl) += (ah + al) * (xh + xl), dropping al*xl (below 2^-48 relative).
 __device__ __forceinline__ void df_dot_acc(float& sh, float& sl, float ah, float al, float xh, float xl) {
   const float p = __fmul_rn(ah, xh);
@@ -48,66 +42,66 @@ __device__ __forceinline__ void df_dot_acc(float& sh, float& sl, float ah, float
   sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
 
-// Y[n x R] = A[n x n] X[n x R] with A and X in double-float, Y in FP64.
-// One warp per row; each lane streams 16-byte pieces (two elements) of the
-// row, eight in flight; X (n*R*8 bytes) stays in L2/L1.  A row that starts
-// 8 bytes past a 16-byte boundary (odd n, odd row) peels its first element.
-template <int R>
-__global__ void __launch_bounds__(256) k_dense_rows_df(const float2* __restrict__ A, const float2* __restrict__ X,
-                                                       double* __restrict__ Y, int n) {
-  const int row_id = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (row_id >= n) return;
-  const float2* row = A + (size_t)row_id * n;
-  float sh[R], sl[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) sh[r] = sl[r] = 0.0f;
-  int k0 = 0;
-  if ((reinterpret_cast<uintptr_t>(row) & 15) != 0) {
-    if (lane == 0) {
-      const float2 a = row[0];
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float2 x = __ldg(X + r);
-        df_dot_acc(sh[r], sl[r], a.x, a.y, x.x, x.y);
-      }
-    }
-    k0 = 1;
+// rows of src (n doubles each) -> double-float rows of pitch ld >= n, the
+// columns [n, ld) zeroed
+__global__ void k_to_df_rows(const double* __restrict__ src, int nrows, int n, float2* __restrict__ dst, int ld) {
+  const size_t tot = (size_t)nrows * ld;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = e / ld;
+    const int c = (int)(e - r * ld);
+    dst[e] = c < n ? split_df(src[r * n + c]) : make_float2(0.f, 0.f);
   }
-  const int npair = (n - k0) >> 1;
-  const float4* row4 = reinterpret_cast<const float4*>(row + k0);
-  auto consume = [&](const float4 a, int q) {
-    const int kk = k0 + 2 * q;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const float2 x0 = __ldg(X + (size_t)kk * R + r);
-      const float2 x1 = __ldg(X + (size_t)(kk + 1) * R + r);
-      df_dot_acc(sh[r], sl[r], a.x, a.y, x0.x, x0.y);
-      df_dot_acc(sh[r], sl[r], a.z, a.w, x1.x, x1.y);
-    }
+}
+
+// Y[n x 2] = A X with A [n][ld] double-float (ld even, zero-padded columns, so
+// every row is 16-byte aligned and holds ld/2 element pairs) and X [ld][2]
+// double-float (zero-padded rows).  Two rows per warp: each 16-byte load of X
+// feeds both rows, halving X traffic per operator byte; four pieces of each
+// row in flight per lane.
+__global__ void __launch_bounds__(256) k_dense_rows2_df(const float2* __restrict__ A, int ld,
+                                                        const float2* __restrict__ X, double* __restrict__ Y,
+                                                        int n) {
+  const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  const int r0 = 2 * warp;
+  if (r0 >= n) return;
+  const bool two = r0 + 1 < n;
+  const float4* a0p = reinterpret_cast<const float4*>(A + (size_t)r0 * ld);
+  const float4* a1p = reinterpret_cast<const float4*>(A + (size_t)(two ? r0 + 1 : r0) * ld);
+  const float4* x4 = reinterpret_cast<const float4*>(X);   // pair q: x4[2q] = (x0 of k, x1 of k), x4[2q+1] = k+1
+  float sh[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, sl[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+  const int npair = ld >> 1;
+  auto consume = [&](const float4 a, const float4 b, int q) {
+    const float4 xa = __ldg(x4 + 2 * q);       // element 2q: (hi0, lo0, hi1, lo1) of the two columns
+    const float4 xb = __ldg(x4 + 2 * q + 1);   // element 2q + 1
+    df_dot_acc(sh[0][0], sl[0][0], a.x, a.y, xa.x, xa.y);
+    df_dot_acc(sh[0][1], sl[0][1], a.x, a.y, xa.z, xa.w);
+    df_dot_acc(sh[0][0], sl[0][0], a.z, a.w, xb.x, xb.y);
+    df_dot_acc(sh[0][1], sl[0][1], a.z, a.w, xb.z, xb.w);
+    df_dot_acc(sh[1][0], sl[1][0], b.x, b.y, xa.x, xa.y);
+    df_dot_acc(sh[1][1], sl[1][1], b.x, b.y, xa.z, xa.w);
+    df_dot_acc(sh[1][0], sl[1][0], b.z, b.w, xb.x, xb.y);
+    df_dot_acc(sh[1][1], sl[1][1], b.z, b.w, xb.z, xb.w);
   };
   int q = lane;
-  for (; q + 224 < npair; q += 256) {   // eight 16-byte loads per lane in flight
-    float4 a[8];
+  for (; q + 96 < npair; q += 128) {
+    float4 a[4], b[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) a[u] = __ldcs(row4 + q + 32 * u);
-#pragma unroll
-    for (int u = 0; u < 8; ++u) consume(a[u], q + 32 * u);
-  }
-  for (; q < npair; q += 32) consume(__ldcs(row4 + q), q);
-  const int kt = k0 + 2 * npair;  // at most one element left
-  if (kt < n && lane == 0) {
-    const float2 a = row[kt];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const float2 x = __ldg(X + (size_t)kt * R + r);
-      df_dot_acc(sh[r], sl[r], a.x, a.y, x.x, x.y);
+    for (int u = 0; u < 4; ++u) {
+      a[u] = __ldcs(a0p + q + 32 * u);
+      b[u] = __ldcs(a1p + q + 32 * u);
     }
-  }
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const double v = warp_sum((double)sh[r] + (double)sl[r]);
-    if (lane == 0) Y[(size_t)row_id * R + r] = v;
+    for (int u = 0; u < 4; ++u) consume(a[u], b[u], q + 32 * u);
+  }
+  for (; q < npair; q += 32) consume(__ldcs(a0p + q), __ldcs(a1p + q), q);
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr) {
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const double v = warp_sum((double)sh[rr][c] + (double)sl[rr][c]);
+      if (lane == 0 && (rr == 0 || two)) Y[(size_t)(r0 + rr) * 2 + c] = v;
+    }
   }
 }
 
