@@ -1636,7 +1636,7 @@ int enqueue_env_fields(bx_cluster* h, const double* d_w) {
   double *t0 = b[6], *t1 = b[7], *t2 = b[8], *t3 = b[9], *Y = b[10];  // Y spans b[10], b[11]
   double *jx = b[12], *jy = b[13];
   const unsigned gg = (unsigned)((G + 255) / 256);
-  const unsigned rows = (unsigned)((((size_t)G + 1) / 2 * 32 + 255) / 256);   // a warp per row pair
+  const unsigned rows = (unsigned)((((size_t)G + bx::kDenseRows - 1) / bx::kDenseRows * 32 + 255) / 256);
   if (!h->ecm) {
     const double* vm = (h->mode == MODE_SPLIT) ? h->o_vm_mem : h->d_vm[h->parity ^ 1];
     bx::k_fields_vce<<<gg, 256, 0, s>>>(G, h->f_last, h->d_m2c, vm, t0);
@@ -1645,7 +1645,7 @@ int enqueue_env_fields(bx_cluster* h, const double* d_w) {
     // smooth_flux(gradient(delta * Phi)) (ion_current.py:133-136)
     bx::k_fields_grad<<<gg, 256, 0, s>>>(venv, h->delta, t0, t1, fg);
     bx::k_fields_hh_rhs<<<gg, 256, 0, s>>>(t0, t1, h->f_X, fg);
-    bx::k_dense_rows2_df<<<rows, 256, 0, s>>>(h->f_lap, h->f_ld, h->f_X, Y, G);
+    bx::k_dense_rows2_df<bx::kDenseRows><<<rows, 256, 0, s>>>(h->f_lap, h->f_ld, h->f_X, Y, G);
     bx::k_fields_hh_out<<<gg, 256, 0, s>>>(Y, 1.0, nullptr, t0, t1, t2, t3, fg);
     bx::k_fields_e_and_j<<<gg, 256, 0, s>>>(G, t0, t1, t2, t3, d_w, h->par.sigma, Ex, Ey, jx, jy);
   } else {
@@ -1658,7 +1658,7 @@ int enqueue_env_fields(bx_cluster* h, const double* d_w) {
   }
   // J_env, B_field: Helmholtz-Hodge split of the current (ion_current.py:70, 147)
   bx::k_fields_hh_rhs<<<gg, 256, 0, s>>>(jx, jy, h->f_X, fg);
-  bx::k_dense_rows2_df<<<rows, 256, 0, s>>>(h->f_lap, h->f_ld, h->f_X, Y, G);
+  bx::k_dense_rows2_df<bx::kDenseRows><<<rows, 256, 0, s>>>(h->f_lap, h->f_ld, h->f_X, Y, G);
   bx::k_fields_hh_out<<<gg, 256, 0, s>>>(Y, h->par.mu, Bf, Jex, Jey, nullptr, nullptr, fg);
   BX_CU(cudaGetLastError());
   return BX_OK;
@@ -1720,14 +1720,14 @@ int bx_time_env_fields(bx_handle h, int n, double* ms_fields, double* ms_product
   BX_CU(cudaEventCreate(&e1));
   BX_CU(cudaEventCreate(&e2));
   const int G = h->G;
-  const unsigned rows = (unsigned)((((size_t)G + 1) / 2 * 32 + 255) / 256);
+  const unsigned rows = (unsigned)((((size_t)G + bx::kDenseRows - 1) / bx::kDenseRows * 32 + 255) / 256);
   double tf = 0.0, tp = 0.0;
   for (int q = 0; q < n; ++q) {
     BX_CU(cudaEventRecord(e0, h->stream));
     rc = enqueue_env_fields(h, d_w);
     if (rc != BX_OK) break;
     BX_CU(cudaEventRecord(e1, h->stream));
-    bx::k_dense_rows2_df<<<rows, 256, 0, h->stream>>>(h->f_lap, h->f_ld, h->f_X, h->f_buf + (size_t)10 * G, G);
+    bx::k_dense_rows2_df<bx::kDenseRows><<<rows, 256, 0, h->stream>>>(h->f_lap, h->f_ld, h->f_X, h->f_buf + (size_t)10 * G, G);
     BX_CU(cudaEventRecord(e2, h->stream));
     BX_CU(cudaEventSynchronize(e2));
     float a = 0.f, b = 0.f;

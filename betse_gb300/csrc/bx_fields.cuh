@@ -55,55 +55,63 @@ __global__ void k_to_df_rows(const double* __restrict__ src, int nrows, int n, f
 
 // Y[n x 2] = A X with A [n][ld] double-float (ld even, zero-padded columns, so
 // every row is 16-byte aligned and holds ld/2 element pairs) and X [ld][2]
-// double-float (zero-padded rows).  Two rows per warp: each 16-byte load of X
-// feeds both rows, halving X traffic per operator byte; four pieces of each
-// row in flight per lane.
+// double-float (zero-padded rows).  ROWS rows per warp: each 16-byte load of X
+// feeds all of them, dividing X traffic per operator byte by ROWS; four
+// pieces of each row in flight per lane.
+template <int ROWS>
 __global__ void __launch_bounds__(256) k_dense_rows2_df(const float2* __restrict__ A, int ld,
                                                         const float2* __restrict__ X, double* __restrict__ Y,
                                                         int n) {
   const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  const int r0 = 2 * warp;
+  const int r0 = ROWS * warp;
   if (r0 >= n) return;
-  const bool two = r0 + 1 < n;
-  const float4* a0p = reinterpret_cast<const float4*>(A + (size_t)r0 * ld);
-  const float4* a1p = reinterpret_cast<const float4*>(A + (size_t)(two ? r0 + 1 : r0) * ld);
-  const float4* x4 = reinterpret_cast<const float4*>(X);   // pair q: x4[2q] = (x0 of k, x1 of k), x4[2q+1] = k+1
-  float sh[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, sl[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+  const float4* ap[ROWS];
+#pragma unroll
+  for (int rr = 0; rr < ROWS; ++rr)
+    ap[rr] = reinterpret_cast<const float4*>(A + (size_t)(r0 + rr < n ? r0 + rr : r0) * ld);
+  const float4* x4 = reinterpret_cast<const float4*>(X);   // x4[k] = (hi0, lo0, hi1, lo1) of element k
+  float sh[ROWS][2], sl[ROWS][2];
+#pragma unroll
+  for (int rr = 0; rr < ROWS; ++rr) sh[rr][0] = sh[rr][1] = sl[rr][0] = sl[rr][1] = 0.f;
   const int npair = ld >> 1;
-  auto consume = [&](const float4 a, const float4 b, int q) {
-    const float4 xa = __ldg(x4 + 2 * q);       // element 2q: (hi0, lo0, hi1, lo1) of the two columns
+  auto consume = [&](const float4 (&a)[ROWS], int q) {
+    const float4 xa = __ldg(x4 + 2 * q);       // element 2q
     const float4 xb = __ldg(x4 + 2 * q + 1);   // element 2q + 1
-    df_dot_acc(sh[0][0], sl[0][0], a.x, a.y, xa.x, xa.y);
-    df_dot_acc(sh[0][1], sl[0][1], a.x, a.y, xa.z, xa.w);
-    df_dot_acc(sh[0][0], sl[0][0], a.z, a.w, xb.x, xb.y);
-    df_dot_acc(sh[0][1], sl[0][1], a.z, a.w, xb.z, xb.w);
-    df_dot_acc(sh[1][0], sl[1][0], b.x, b.y, xa.x, xa.y);
-    df_dot_acc(sh[1][1], sl[1][1], b.x, b.y, xa.z, xa.w);
-    df_dot_acc(sh[1][0], sl[1][0], b.z, b.w, xb.x, xb.y);
-    df_dot_acc(sh[1][1], sl[1][1], b.z, b.w, xb.z, xb.w);
+#pragma unroll
+    for (int rr = 0; rr < ROWS; ++rr) {
+      df_dot_acc(sh[rr][0], sl[rr][0], a[rr].x, a[rr].y, xa.x, xa.y);
+      df_dot_acc(sh[rr][1], sl[rr][1], a[rr].x, a[rr].y, xa.z, xa.w);
+      df_dot_acc(sh[rr][0], sl[rr][0], a[rr].z, a[rr].w, xb.x, xb.y);
+      df_dot_acc(sh[rr][1], sl[rr][1], a[rr].z, a[rr].w, xb.z, xb.w);
+    }
   };
   int q = lane;
   for (; q + 96 < npair; q += 128) {
-    float4 a[4], b[4];
+    float4 a[4][ROWS];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      a[u] = __ldcs(a0p + q + 32 * u);
-      b[u] = __ldcs(a1p + q + 32 * u);
-    }
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
-    for (int u = 0; u < 4; ++u) consume(a[u], b[u], q + 32 * u);
+      for (int rr = 0; rr < ROWS; ++rr) a[u][rr] = __ldcs(ap[rr] + q + 32 * u);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) consume(a[u], q + 32 * u);
   }
-  for (; q < npair; q += 32) consume(__ldcs(a0p + q), __ldcs(a1p + q), q);
+  for (; q < npair; q += 32) {
+    float4 a[ROWS];
 #pragma unroll
-  for (int rr = 0; rr < 2; ++rr) {
+    for (int rr = 0; rr < ROWS; ++rr) a[rr] = __ldcs(ap[rr] + q);
+    consume(a, q);
+  }
+#pragma unroll
+  for (int rr = 0; rr < ROWS; ++rr) {
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
       const double v = warp_sum((double)sh[rr][c] + (double)sl[rr][c]);
-      if (lane == 0 && (rr == 0 || two)) Y[(size_t)(r0 + rr) * 2 + c] = v;
+      if (lane == 0 && r0 + rr < n) Y[(size_t)(r0 + rr) * 2 + c] = v;
     }
   }
 }
+constexpr int kDenseRows = 4;   // rows per warp of the lapENVinv product
 
 // ---------------------------------------------------------------------------
 // field stencils on the (ny, nx) grid, k = i*nx + j
