@@ -11,7 +11,7 @@ gives the predicted Vmem exactly, the well-mixed environment adjusted so that
 every ion's total amount equals the initial one -- and the ordinary time
 stepping runs from there until its own residual test passes (max |dVm/dt| below
 a tolerance, ``sim.dvm``, sim.py:2083).  The network only chooses the starting
-point; the method stays the judge.
+point; the time stepping alone decides when the cluster has settled.
 
 ``python -m betse_gb300.warmstart train --out FILE`` generates the training
 steady states with the GPU step itself (the split form on batches of
