@@ -146,7 +146,7 @@ def graph_of(geoms):
 # stepping to steady state
 # ---------------------------------------------------------------------------
 def run_to_steady(geoms, params, Dms, states, tol=1e-6, chunk=1000, max_steps=400_000, precision='split',
-                  restart_states=()):
+                  restart_states=(), compact=True):
     """Step a batch of clusters until every cluster's max |dVm/dt| < tol.
 
     Returns (final states, steps at which each cluster first passed -- -1 if
@@ -156,42 +156,63 @@ def run_to_steady(geoms, params, Dms, states, tol=1e-6, chunk=1000, max_steps=40
     (clusters share no data).  ``restart_states`` is a sequence of fallback
     state lists: a cluster that goes unstable restarts from the next one in
     turn, and its count of steps keeps running (steps before a restart count
-    against it)."""
+    against it).  With ``compact``, once half of the clusters still stepping
+    have passed (or given up), the batch is rebuilt from the others, so the
+    last slow clusters do not carry the finished ones; a retired cluster's
+    final state is the one it had when it left the batch."""
     import torch
-    eng = BatchEngine(geoms, params, precision)
-    eng.set_membrane_diffusivity(Dms)
-    eng.upload_states(states)
     n = len(geoms)
     passed = np.full(n, -1, np.int64)
     level = np.zeros(n, np.int64)
+    final = [None] * n
+
+    def make(idx, sts):
+        e = BatchEngine([geoms[i] for i in idx], [params[i] for i in idx], precision)
+        e.set_membrane_diffusivity([Dms[i] for i in idx])
+        e.upload_states(sts)
+        return e
+
+    active = np.arange(n)
+    eng = make(active, list(states))
     done = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     while done < max_steps:
         eng.step(chunk, outputs=True)
         done += chunk
-        worst = eng.max_abs_dvm()
+        worst = eng.max_abs_dvm()                      # per cluster of the engine
         nonfinite = ~np.isfinite(worst)
-        bad = (passed == -1) & nonfinite
-        fresh = bad & (level < len(restart_states))
-        passed[bad & ~fresh] = -2
+        bad = (passed[active] == -1) & nonfinite
+        fresh = bad & (level[active] < len(restart_states))
+        passed[active[bad & ~fresh]] = -2
         if np.any(fresh):
             cur = eng.download_states()
-            for k in np.nonzero(nonfinite)[0]:
-                if fresh[k]:
-                    cur[k] = restart_states[level[k]][k]
-                    level[k] += 1
+            for j in np.nonzero(nonfinite)[0]:
+                g = active[j]
+                if fresh[j]:
+                    cur[j] = restart_states[level[g]][g]
+                    level[g] += 1
                 else:   # given up or already recorded: any finite state keeps the upload valid
-                    cur[k] = restart_states[-1][k]
+                    cur[j] = (restart_states[-1] if restart_states else states)[g]
             eng.upload_states(cur)
-        newly = (passed == -1) & (worst < tol)
-        passed[newly] = done
-        if np.all(passed != -1):
+        newly = (passed[active] == -1) & (worst < tol)
+        passed[active[newly]] = done
+        still = np.nonzero(passed[active] == -1)[0]
+        if len(still) == 0:
             break
+        if compact and len(active) > 1 and len(still) <= len(active) // 2:
+            cur = eng.download_states()
+            for j, g in enumerate(active):
+                final[g] = cur[j]
+            eng.close()
+            active = active[still]
+            eng = make(active, [cur[j] for j in still])
     wall = time.perf_counter() - t0
-    out = eng.download_states()
+    cur = eng.download_states()
+    for j, g in enumerate(active):
+        final[g] = cur[j]
     eng.close()
-    return out, passed, wall, level
+    return final, passed, wall, level
 
 
 # ---------------------------------------------------------------------------
