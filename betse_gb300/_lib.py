@@ -53,12 +53,14 @@ class BxParams(ct.Structure):
             'er', 'sharpness', 'cell_radius', 'true_cell_size', 'ko_env', 'sigma',
             'mu')] + \
         [('zs', ct.c_double * MAX_IONS), ('D_free', ct.c_double * MAX_IONS),
-         ('D_gj', ct.c_double * MAX_IONS), ('c_env_bound', ct.c_double * MAX_IONS)]
+         ('D_gj', ct.c_double * MAX_IONS), ('c_env_bound', ct.c_double * MAX_IONS),
+         ('v_sensitive_gj', ct.c_int32), ('reserved0', ct.c_int32), ('gj_vthresh', ct.c_double),
+         ('gj_min', ct.c_double)]
 
 
 class BxState(ct.Structure):
     _fields_ = [('vm', _dp), ('cc_cells', _dp), ('cc_at_mem', _dp),
-                ('cc_env', _dp), ('E_env_x', _dp), ('E_env_y', _dp)]
+                ('cc_env', _dp), ('E_env_x', _dp), ('E_env_y', _dp), ('gjopen', _dp)]
 
 
 OUTPUT_FIELDS = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn',

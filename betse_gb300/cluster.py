@@ -198,6 +198,9 @@ class StepParams:
     mu: float = 1.275e-6
     c_env_bound: np.ndarray | None = None
     ion_names: list | None = None
+    v_sensitive_gj: bool = False     # voltage-gated gap junctions (gjopen is then state)
+    gj_vthresh: float = 15.0         # mV
+    gj_min: float = 0.10
 
     @property
     def n_ions(self) -> int:
@@ -222,6 +225,8 @@ class StepParams:
             if not np.all(D_gj == D_gj[:, :1]):
                 raise NotImplementedError('per-membrane D_gj')
             D_gj = D_gj[:, 0]
+        if bool(getattr(p, 'v_sensitive_gj', False)):
+            kw.update(v_sensitive_gj=True, gj_vthresh=float(p.gj_vthresh), gj_min=float(p.gj_min))
         return cls(zs=np.asarray(sim.zs, np.float64), D_free=np.asarray(sim.D_free, np.float64),
                    D_gj=D_gj, iNa=int(sim.iNa), iK=int(sim.iK), is_ecm=bool(p.is_ecm),
                    T=float(sim.T), gj_block=float(np.ravel(gjb)[0]),
@@ -245,6 +250,8 @@ class StepParams:
             c.D_free[i] = float(self.D_free[i])
             c.D_gj[i] = float(self.D_gj[i])
             c.c_env_bound[i] = float(cb[i])
+        c.v_sensitive_gj = int(bool(self.v_sensitive_gj))
+        c.gj_vthresh, c.gj_min = float(self.gj_vthresh), float(self.gj_min)
         return c
 
     def replace(self, **kw):

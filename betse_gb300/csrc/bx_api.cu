@@ -76,6 +76,9 @@ struct bx_cluster {
   bool persist = false;            // split form: persistent cp.async-pipelined kernel (autotuned)
   int sm_count = 0;
   bool ecm = false;
+  bool vgj = false;                // voltage-gated gap junctions: the open fraction is state
+  double* d_gjo = nullptr;         // [M] plain form
+  float* t_gjo = nullptr;          // [Q] split form, per membrane slot
   bx_params par{};                 // parameters of cluster 0 (the shared ones)
   std::vector<bx_params> cl_par;   // per-cluster parameters
   std::vector<int> cl_cell, cl_mem, cl_blk;   // offsets [ncl+1]
@@ -169,7 +172,7 @@ void free_all(bx_cluster* h) {
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
-      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale};
+      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& fs : h->fshapes)
@@ -206,6 +209,10 @@ bx::StepConst make_step_const(const bx_cluster* h) {
   k.tm = p.tm;
   k.gj_len = h->gj_len;
   k.gj_block = p.gj_block;
+  k.vgj = h->vgj ? 1 : 0;
+  k.gj_vth = p.gj_vthresh;
+  k.gj_min = p.gj_min;
+  k.gj_dt_ms = p.dt * 1e3;
   k.inv_KmNa = 1.0 / p.KmNK_Na;
   k.inv_KmK = 1.0 / p.KmNK_K;
   k.atp_term = p.cATP / p.KmNK_ATP;
@@ -233,6 +240,10 @@ bx::SplitConst make_split_const(const bx_cluster* h) {
   k.inv_tm = (float)(1.0 / d.tm);
   k.inv_gjl = (float)(1.0 / d.gj_len);
   k.gj_block = (float)d.gj_block;
+  k.vgj = d.vgj;
+  k.gj_vth = (float)d.gj_vth;
+  k.gj_min = (float)d.gj_min;
+  k.gj_dt_ms = (float)d.gj_dt_ms;
   k.inv_KmNa = (float)d.inv_KmNa;
   k.inv_KmK = (float)d.inv_KmK;
   k.atp_term = (float)d.atp_term;
@@ -297,6 +308,7 @@ bx::StepPtrs step_ptrs(bx_cluster* h, int parity) {
   p.o_Jc = h->o_Jc; p.o_vmave = h->o_vmave; p.o_dvm = h->o_dvm; p.o_Ecx = h->o_Ecx;
   p.o_Ecy = h->o_Ecy; p.o_Emc = h->o_Emc; p.o_Egjx = h->o_Egjx; p.o_Egjy = h->o_Egjy;
   p.o_gjopen = h->o_gjopen; p.o_sigma = h->o_sigma;
+  p.gjo = h->d_gjo;
   return p;
 }
 
@@ -320,6 +332,8 @@ bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
   p.o_drho = h->o_drho;
   p.cenv_grid = h->ecm ? h->d_cenv : nullptr;
   p.mfs = h->d_mem_flux_sa;
+  p.gjo = h->t_gjo;
+  p.o_gjopen = h->o_gjopen;
   return p;
 }
 
@@ -403,7 +417,7 @@ cudaError_t launch_persist_t(bx_cluster* h, int parity, cudaStream_t s) {
 }
 
 cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
-  if (h->persist && !out && !h->phib_nonzero && !h->ecm) {
+  if (h->persist && !out && !h->phib_nonzero && !h->ecm && !h->vgj) {
     const bool six = is_betse_six_ions(h);
     if (h->tpb == 192) return six ? launch_persist_t<192, 1>(h, parity, s) : launch_persist_t<192, 0>(h, parity, s);
     return six ? launch_persist_t<256, 1>(h, parity, s) : launch_persist_t<256, 0>(h, parity, s);
@@ -488,6 +502,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
       oc.I = h->I;
       for (int i = 0; i < h->I; ++i) { oc.zF[i] = d.zF[i]; oc.sig_coef[i] = d.sig_coef[i]; }
       oc.dt = d.dt; oc.gj_len = h->gj_len; oc.gj_block = d.gj_block; oc.cm = h->par.cm;
+      oc.vgj = h->vgj ? 1 : 0;
       if (h->tpb == 192) bx::k_split_outputs<192><<<h->nblk, 192, 0, s>>>(og, op, oc);
       else bx::k_split_outputs<256><<<h->nblk, 256, 0, s>>>(og, op, oc);
       bx::k_split_egj<<<(h->M + 255) / 256, 256, 0, s>>>(h->M, h->d_nn, h->o_vm_mem, h->d_nx, h->d_ny,
@@ -543,6 +558,7 @@ int upload_param_arrays(bx_cluster* h) {
 
 bool same_shared_params(const bx_params& a, const bx_params& b) {
   if (a.n_ions != b.n_ions || a.iNa != b.iNa || a.iK != b.iK || a.is_ecm != b.is_ecm) return false;
+  if (a.v_sensitive_gj != b.v_sensitive_gj || a.gj_vthresh != b.gj_vthresh || a.gj_min != b.gj_min) return false;
   const double sa[] = {a.F, a.R, a.T, a.dt, a.cm, a.tm, a.gj_surface, a.gj_block, a.KmNK_Na, a.KmNK_K,
                        a.KmNK_ATP, a.cATP, a.cADP, a.cPi, a.deltaGATP};
   const double sb[] = {b.F, b.R, b.T, b.dt, b.cm, b.tm, b.gj_surface, b.gj_block, b.KmNK_Na, b.KmNK_K,
@@ -621,13 +637,19 @@ int build_split_layout(bx_cluster* h, const std::vector<int>& blk) {
     nn_env[qq] = h->h_map_env[h->h_nn[m]];
   }
   void* old[] = {h->t_lcell, h->t_nn, h->t_map_env, h->t_nn_env, h->t_c0, h->t_m0, h->t_slot_of_cell,
-                 h->t_sa, h->t_gw, h->t_dtv, h->t_dvc, h->t_rng, h->d_Dm_f, h->s_cc2, h->s_rec[0], h->s_rec[1]};
+                 h->t_sa, h->t_gw, h->t_dtv, h->t_dvc, h->t_rng, h->d_Dm_f, h->s_cc2, h->s_rec[0], h->s_rec[1],
+                 h->t_gjo};
   for (void* q : old)
     if (q) cudaFree(q);
   h->t_lcell = nullptr; h->t_nn = h->t_map_env = h->t_nn_env = h->t_c0 = h->t_m0 = h->t_slot_of_cell = nullptr;
   h->t_sa = h->t_gw = h->t_dtv = h->t_dvc = nullptr; h->t_rng = nullptr; h->d_Dm_f = nullptr;
   h->s_cc2 = nullptr; h->s_rec[0] = h->s_rec[1] = nullptr;
+  h->t_gjo = nullptr;
   h->Q = Q;
+  if (h->vgj) {
+    BX_CU(dalloc(&h->t_gjo, Q));
+    BX_CU(cudaMemset(h->t_gjo, 0, (size_t)Q * sizeof(float)));
+  }
   h->S = S;
   BX_CU(dalloc(&h->t_lcell, Q)); BX_CU(h2d(h->t_lcell, lcell.data(), Q));
   BX_CU(dalloc(&h->t_nn, Q)); BX_CU(h2d(h->t_nn, nn_slot.data(), Q));
@@ -752,7 +774,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     h->cl_nx.push_back(gs[cl].grid_nx);
     h->cl_delta.push_back(gs[cl].delta);
   }
-  h->precision = precision; h->par = p0; h->ecm = p0.is_ecm != 0;
+  h->precision = precision; h->par = p0; h->ecm = p0.is_ecm != 0; h->vgj = p0.v_sensitive_gj != 0;
   h->cl_par.assign(ps, ps + ncl);
   h->mode = (precision == BX_PLAIN_FP64) ? MODE_PLAIN : MODE_SPLIT;
   if (h->mode == MODE_SPLIT && I > kRec - 1) {
@@ -791,6 +813,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   for (int m = 0; m < M; ++m) nn_cell[m] = m2c[nn[m]];
   h->h_cell_ptr = ptr; h->h_m2c = m2c; h->h_map_env = map_env;
   h->h_phib.assign(G, 0.0);
+  h->h_gjw = gjw;
 
   // environment CSR (grid cell -> its membranes, ascending) for the ECM scatter
   std::vector<int> env_ptr(G + 1, 0), env_mem(M);
@@ -839,7 +862,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     return bail(BX_ECUDA, "cudaMemset");
   if (h->mode == MODE_SPLIT) {
     // host copies for the tile-major relayout (build_split_layout)
-    h->h_msa = msa; h->h_gjw = gjw; h->h_bflag = bflag; h->h_nn = nn; h->h_vol = vol; h->h_div = div;
+    h->h_msa = msa; h->h_bflag = bflag; h->h_nn = nn; h->h_vol = vol; h->h_div = div;
     ALLOC(h->s_cenv_f, (size_t)ncl * I); ALLOC(h->d_cenv, h->ecm ? (size_t)I * G : (size_t)ncl * I);
     ALLOC(h->s_pump, ncl);
     ALLOC(h->s_phib, G);
@@ -851,6 +874,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     ALLOC(h->d_ccm[0], (size_t)I * C); ALLOC(h->d_ccm[1], (size_t)I * C);
     ALLOC(h->d_cc, (size_t)I * C);
     ALLOC(h->d_cenv, h->ecm ? (size_t)I * G : (size_t)ncl * I);
+    if (h->vgj) ALLOC(h->d_gjo, M);
   }
   if (h->ecm) {
     ALLOC(h->d_env_ptr, G + 1); H2D(h->d_env_ptr, env_ptr.data(), G + 1);
@@ -914,8 +938,8 @@ void bx_destroy(bx_handle h) {
 
 int bx_set_params(bx_handle h, const bx_params* p) {
   if (!h || !p) return fail(BX_EINVAL, "null argument");
-  if (p->n_ions != h->I || (p->is_ecm != 0) != h->ecm)
-    return fail(BX_EINVAL, "n_ions / is_ecm cannot change after create");
+  if (p->n_ions != h->I || (p->is_ecm != 0) != h->ecm || (p->v_sensitive_gj != 0) != h->vgj)
+    return fail(BX_EINVAL, "n_ions / is_ecm / v_sensitive_gj cannot change after create");
   if (h->ncl > 1) return fail(BX_EINVAL, "use bx_batch_set_params for a batch");
   h->par = *p;
   h->cl_par[0] = *p;
@@ -1027,6 +1051,12 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
     }
     BX_CU(h2d(h->s_rec[0], rec.data(), rec.size()));
     BX_CU(h2d(h->s_cc2, cc2.data(), cc2.size()));
+    if (h->vgj) {
+      std::vector<float> go((size_t)h->Q, 0.0f);
+      for (int m = 0; m < M; ++m)
+        go[h->h_slot_of_mem[m]] = (float)(s->gjopen ? s->gjopen[m] : h->h_gjw[m]);
+      BX_CU(h2d(h->t_gjo, go.data(), go.size()));
+    }
     BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
     if (h->ecm) {
       BX_CU(h2d(h->d_Ex, s->E_env_x, h->G));
@@ -1041,6 +1071,7 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
     BX_CU(h2d(h->d_cc, s->cc_cells, (size_t)I * C));
     BX_CU(h2d(h->d_ccm[0], ccm.data(), ccm.size()));
     BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
+    if (h->vgj) BX_CU(h2d(h->d_gjo, s->gjopen ? s->gjopen : h->h_gjw.data(), M));
     if (h->ecm) {
       BX_CU(h2d(h->d_Ex, s->E_env_x, h->G));
       BX_CU(h2d(h->d_Ey, s->E_env_y, h->G));
@@ -1083,11 +1114,18 @@ int bx_state_download(bx_handle h, bx_state* s) {
       if (s->E_env_x) BX_CU(cudaMemcpy(s->E_env_x, h->d_Ex, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
       if (s->E_env_y) BX_CU(cudaMemcpy(s->E_env_y, h->d_Ey, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
     }
+    if (h->vgj && s->gjopen) {
+      std::vector<float> go((size_t)h->Q);
+      BX_CU(cudaMemcpy(go.data(), h->t_gjo, go.size() * sizeof(float), cudaMemcpyDeviceToHost));
+      for (int m = 0; m < M; ++m) s->gjopen[m] = (double)go[h->h_slot_of_mem[m]];
+    }
   } else {
     if (s->vm) BX_CU(cudaMemcpy(s->vm, h->d_vm[h->parity], (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
     if (s->cc_cells)
       BX_CU(cudaMemcpy(s->cc_cells, h->d_cc, (size_t)I * C * sizeof(double), cudaMemcpyDeviceToHost));
     BX_CU(cudaMemcpy(ccm.data(), h->d_ccm[h->parity], ccm.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (h->vgj && s->gjopen)
+      BX_CU(cudaMemcpy(s->gjopen, h->d_gjo, (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
     if (h->ecm) {
       if (s->E_env_x) BX_CU(cudaMemcpy(s->E_env_x, h->d_Ex, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
       if (s->E_env_y) BX_CU(cudaMemcpy(s->E_env_y, h->d_Ey, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1247,13 +1285,15 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
     // cell: cc2 in+out 16I, record in+out 2*4*kRec, dt/vol 4, diviterm/cm 4, range 4
     // tile: partial sums 4I, cluster id 4; ECM: map_env 4, grid concentration
     // 8I and the f*sa export 8I per membrane instead of the partial sums
-    if (h->ecm) return M * (4 * I + 13 + 4 + 16 * I) + C * (16 * I + 8 * kRec + 12) + B * 4;
-    return M * (4 * I + 13) + C * (16 * I + 8 * kRec + 12) + B * (4 * I + 4);
+    // voltage-gated gap junctions: the open fraction in+out, 8 per membrane
+    const int64_t gv = h->vgj ? 8 : 0;
+    if (h->ecm) return M * (4 * I + 13 + 4 + 16 * I + gv) + C * (16 * I + 8 * kRec + 12) + B * 4;
+    return M * (4 * I + 13 + gv) + C * (16 * I + 8 * kRec + 12) + B * (4 * I + 4);
   }
   const int64_t w = 8;  // Dm, mem_sa, gj_w width
   // membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env and the f*sa
   // export with ECM); cell: cc in+out, cc_mem in+out, cell_vol, diviterm, ptr
-  const int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0);
+  const int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0) + (h->vgj ? 16 : 0);
   const int64_t cell = 4 * I * 8 + 16 + 4;
   return M * mem + C * cell + (h->ecm ? 0 : B * I * 8);
 }
@@ -1273,11 +1313,13 @@ int bx_set_launch_config(bx_handle h, int tpb, int persistent) {
   if (!ok) return fail(BX_EINVAL, "unsupported CTA size for this form");
   if (persistent && h->mode != MODE_SPLIT) return fail(BX_EINVAL, "the persistent kernel is the split form's");
   if (persistent && h->ecm) return fail(BX_EINVAL, "the persistent kernel has no extracellular-space variant");
+  if (persistent && h->vgj) return fail(BX_EINVAL, "the persistent kernel has no voltage-gated gap-junction variant");
   const size_t C = h->C, I = h->I, M = h->M;
   const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
-  std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1);
+  std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1),
+      gjo(h->vgj ? M : 1);
   bx_state sv{vm.data(), cc.data(), cam.data(), cenv.data(), h->ecm ? ex.data() : nullptr,
-              h->ecm ? ey.data() : nullptr};
+              h->ecm ? ey.data() : nullptr, h->vgj ? gjo.data() : nullptr};
   const bool had_state = h->have_state;
   int rc;
   if (had_state && (rc = bx_state_download(h, &sv)) != BX_OK) return rc;
@@ -1296,9 +1338,10 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   if (!h->have_state || !h->have_dm) return fail(BX_ESTATE, "upload state and Dm first");
   const size_t C = h->C, I = h->I, M = h->M;
   const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
-  std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1);
+  std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1),
+      gjo(h->vgj ? M : 1);
   bx_state sv{vm.data(), cc.data(), cam.data(), cenv.data(), h->ecm ? ex.data() : nullptr,
-              h->ecm ? ey.data() : nullptr};
+              h->ecm ? ey.data() : nullptr, h->vgj ? gjo.data() : nullptr};
   int rc = bx_state_download(h, &sv);
   if (rc != BX_OK) return rc;
   unsigned long long status[4];
@@ -1306,7 +1349,7 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   const int64_t launches0 = h->launches;
   struct Cand { int tpb; bool persist; };
   std::vector<Cand> cands;
-  if (h->mode == MODE_SPLIT && h->ecm) cands = {{256, false}, {192, false}};
+  if (h->mode == MODE_SPLIT && (h->ecm || h->vgj)) cands = {{256, false}, {192, false}};
   else if (h->mode == MODE_SPLIT) cands = {{256, false}, {192, false}, {256, true}, {192, true}};
   else cands = {{256, false}, {128, false}};
   double best = 1e300;

@@ -63,7 +63,12 @@ struct StepConst {
   double qnum_c;           // (cADP*1e-3)*(cPi*1e-3)
   double qden_c;           // cATP*1e-3
   double K0;               // exp(-deltaGATP / (R T))
+  int vgj;                 // voltage-gated gap junctions: gjopen is state (p.gjo)
+  double gj_vth, gj_min, gj_dt_ms;   // threshold (mV), closed fraction, dt in ms
 };
+
+// Harris et al. (1983) gap-junction gating constants (channels/gap_junction.py:26-31)
+constexpr double kGjLambda = 0.0013, kGjA1 = 0.077, kGjA2 = 0.14;
 
 struct StepPtrs {
   const double* vm_in;  double* vm_out;
@@ -77,6 +82,7 @@ struct StepPtrs {
   double* env_part;                        // [nblk][I] partial sums (no ECM)
   double* mem_flux_sa;                     // [I][M] f_mem*sa (ECM scatter input)
   unsigned long long* status;              // [4]: nan_vm, nan_conc, neg clamps, spare
+  double* gjo;                             // [M] gap-junction open fraction (vgj), in place
   // outputs (OUT variant)
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_Jn;
   double* o_Imem; double* o_Jcx; double* o_Jcy; double* o_Jc; double* o_vmave;
@@ -230,6 +236,19 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       fNa = pump_fna<T>(k, (T)pcoef, sm.e1, cNai, cNao, cKi, cKo);
     }
     rate_o = -fNa;
+    // Gap_Junction.run (channels/gap_junction.py:52-81): alpha, beta from
+    // |vgj| in mV; one implicit-Euler update per ion, as update_gj calls it
+    // once per ion (sim.py:2181-2183), each before that ion's flux
+    double gg = 0.0, ga = 0.0, gr = 0.0;
+    if (k.vgj) {
+      const double V1 = 1.0e3 * fabs(vgj);
+      const double al = kGjLambda * exp(-kGjA1 * (V1 - k.gj_vth));
+      double be = kGjLambda * exp(kGjA2 * (V1 - k.gj_vth));
+      be = be / (1.0 + 50.0 * be);
+      ga = k.gj_dt_ms * (al + be * k.gj_min);
+      gr = 1.0 / (1.0 + al * k.gj_dt_ms + be * k.gj_dt_ms);
+      gg = p.gjo[m];
+    }
     for (int i = 0; i < I; ++i) {
       const T cin = (T)p.ccm_in[i * g.C + c];
       const T cout = (T)(ECM ? cenv_cl[i * g.G + ge] : cenv_cl[i]);
@@ -241,7 +260,13 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       else if (i == k.iK) f = (T)(-(2.0 / 3.0)) * fNa + f;
       // gap junction (sim.py:2189-2206): from this membrane's cell into the partner's
       const T cn_i = (T)p.ccm_in[i * g.C + cn];
-      const T dgj = (T)k.dgj_gs[i] * (gjw_t * (T)k.gj_block);
+      T dgj;
+      if (k.vgj) {
+        gg = k.gj_block * ((gg + ga) * gr);
+        dgj = (T)(k.dgj_gs[i] * gg);
+      } else {
+        dgj = (T)k.dgj_gs[i] * (gjw_t * (T)k.gj_block);
+      }
       T fg = ghk_flux<T>(sg, k.zcode[i], k.z[i], vgj1, k.F_RT, cin, cn_i, dgj, inv_gjl);
       if (bnd) fg = (T)0;
       const double a = (double)(f * msa_t);
@@ -251,6 +276,7 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       else env_acc[i] = a;
       if (OUT) { fmem_o[i] = f; fgj_o[i] = fg; }
     }
+    if (k.vgj) p.gjo[m] = gg;
     (void)msa;
   } else {
     for (int i = 0; i < I; ++i) { sA[i * TPB + t] = 0.0; sB[i * TPB + t] = 0.0; }
@@ -326,7 +352,7 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       const double Egj = -vgj / k.gj_len;
       p.o_Egjx[m] = Egj * g.mem_nx[m];
       p.o_Egjy[m] = Egj * g.mem_ny[m];
-      p.o_gjopen[m] = k.gj_block * g.gj_w[m];
+      p.o_gjopen[m] = k.vgj ? p.gjo[m] : k.gj_block * g.gj_w[m];
       sX[t] = Jraw * g.mem_sa[m];
       sX[TPB + t] = vnew;
     } else { sX[t] = 0.0; sX[TPB + t] = 0.0; }

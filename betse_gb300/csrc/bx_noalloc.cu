@@ -146,6 +146,8 @@ extern "C" int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const 
   if (I <= 0 || I > BX_MAX_IONS || p->iNa < 0 || p->iNa >= I || p->iK < 0 || p->iK >= I)
     return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: bad ion indices");
   if (p->is_ecm) return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs is_ecm == 0");
+  if (p->v_sensitive_gj)
+    return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs v_sensitive_gj == 0 (the open fraction is state)");
   if (!g->cell_mem_ptr || !g->nn_i || !g->bflag || !g->map_mem2ecm || !g->mem_sa || !g->gj_weight ||
       !g->cell_vol || !g->diviterm)
     return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: missing geometry array");

@@ -152,6 +152,8 @@ struct SplitConst {
   float F_RT;
   float inv_tm, inv_gjl, gj_block;
   float inv_KmNa, inv_KmK, atp_term, atp_den, qnum_c, qden_c, K0;
+  int vgj;                                  // voltage-gated gap junctions (gjo is state)
+  float gj_vth, gj_min, gj_dt_ms;
 };
 
 // Per-cell record, REC floats, 16-byte aligned: slots [0, I) hold the
@@ -167,6 +169,8 @@ struct SplitPtrs {
   float* __restrict__ env_part;            // [nblk][I] per-tile partial sums
   const double* __restrict__ cenv_grid;    // [I][G] environment grid concentrations (ECM)
   double* __restrict__ mfs;                // [I][M] f_mem*sa per membrane, natural order (ECM scatter)
+  float* __restrict__ gjo;                 // [Q] gap-junction open fraction per slot (vgj), in place
+  double* __restrict__ o_gjopen;           // [M] output steps with vgj: the open fraction
   unsigned long long* status;              // nan_vm, nan_conc, neg clamps
   // outputs (OUT), natural order
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_vmem;
@@ -295,6 +299,17 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     ghk_init_f(sm, v1, k.F_RT);
     ghk_init_f(sg, vgj1, k.F_RT);
     const float ka_m = sm.a1 * k.inv_tm, ka_g = sg.a1 * k.inv_gjl;
+    // Gap_Junction.run (channels/gap_junction.py:52-81), once per ion
+    float gg = 0.f, ga = 0.f, gr = 0.f;
+    if (k.vgj) {
+      const float V1 = 1.0e3f * fabsf(vn - v);
+      const float al = 0.0013f * __expf(-0.077f * (V1 - k.gj_vth));
+      float be = 0.0013f * __expf(0.14f * (V1 - k.gj_vth));
+      be = be * rcp_fast(1.f + 50.f * be);
+      ga = k.gj_dt_ms * (al + be * k.gj_min);
+      gr = rcp_fast(1.f + al * k.gj_dt_ms + be * k.gj_dt_ms);
+      gg = p.gjo[q];
+    }
     float fNa = 0.f;
     if (pc != 0.f) {
       // pumpNaKATP (sim_toolbox.py:71-122), one reciprocal
@@ -322,7 +337,12 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
       float f = ghk_flux_fk(sm, ka_m, z, k.z[i], v1, k.F_RT, cenv[i], cin, dmv[i], k.inv_tm);
       if (i == IS::iNa(k)) f = fNa + f;
       else if (i == IS::iK(k)) f = (-(2.f / 3.f)) * fNa + f;
-      const float fg = ghk_flux_fk(sg, ka_g, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], k.dgj_gs[i] * gw, k.inv_gjl);
+      float dgjv = k.dgj_gs[i] * gw;
+      if (k.vgj) {
+        gg = k.gj_block * ((gg + ga) * gr);
+        dgjv = k.dgj_gs[i] * gg;
+      }
+      const float fg = ghk_flux_fk(sg, ka_g, z, k.z[i], vgj1, k.F_RT, cin, nbr[i], dgjv, k.inv_gjl);
       sA[i][t] = f * sa;
       sB[i][t] = -fg * sa;
       if (ECM) p.mfs[(size_t)i * g.M + g.tile_m0[b] + t] = (double)(f * sa);
@@ -333,6 +353,10 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
       }
     }
     if (OUT) p.o_rate[g.tile_m0[b] + t] = (double)(-fNa);
+    if (k.vgj) {
+      p.gjo[q] = gg;
+      if (OUT) p.o_gjopen[g.tile_m0[b] + t] = (double)gg;
+    }
   } else {
 #pragma unroll
     for (int i = 0; i < NI; ++i) if (i < I) { sA[i][t] = 0.f; sB[i][t] = 0.f; }
@@ -719,6 +743,7 @@ struct SplitOutPtrs {
 struct SplitOutConst {
   int I; double zF[kMaxIons]; double sig_coef[kMaxIons]; double dt; double gj_len; double gj_block;
   double cm;
+  int vgj;   // the open fraction was written by the step kernel
 };
 
 template <int TPB>
@@ -791,7 +816,7 @@ k_split_outputs(SplitOutGeom g, SplitOutPtrs p, SplitOutConst k) {
     p.Jc[m] = sC[1][lc] * nxm + sC[2][lc] * nym;
     p.Emc[m] = (sC[1][lc] / sC[3][lc]) * nxm + (sC[2][lc] / sC[3][lc]) * nym;
     (void)c;
-    p.gjopen[m] = k.gj_block * g.gj_w[m];
+    if (!k.vgj) p.gjopen[m] = k.gj_block * g.gj_w[m];
   }
 }
 

@@ -39,6 +39,7 @@ class ClusterEngine:
         self.I = params.n_ions
         self.C, self.M, self.G = geom.n_cells, geom.n_mems, geom.n_grid
         self.ecm = bool(params.is_ecm)
+        self.vgj = bool(params.v_sensitive_gj)
 
     # ------------------------------------------------------------------
     def close(self):
@@ -80,7 +81,10 @@ class ClusterEngine:
         _lib.check(self.lib.bx_set_boundary_potential(self.h, _lib.dptr(a)),
                    'bx_set_boundary_potential')
 
-    def upload(self, vm, cc_cells, cc_at_mem, cc_env, E_env_x=None, E_env_y=None):
+    def upload(self, vm, cc_cells, cc_at_mem, cc_env, E_env_x=None, E_env_y=None, gjopen=None):
+        """Upload one state. ``gjopen`` (voltage-gated gap junctions only) is the
+        per-membrane open fraction; None starts from the static gj weights, as
+        BETSE's ``sim.gjopen`` does before its first step."""
         vm = _c(vm)
         cc = _c(cc_cells)
         cam = _c(cc_at_mem)
@@ -92,8 +96,9 @@ class ClusterEngine:
             ce = _c(ce[:, 0])
         ex = _c(E_env_x).ravel() if E_env_x is not None else None
         ey = _c(E_env_y).ravel() if E_env_y is not None else None
+        go = _c(gjopen).ravel() if (gjopen is not None and self.vgj) else None
         s = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(ce),
-                         _lib.dptr(ex), _lib.dptr(ey))
+                         _lib.dptr(ex), _lib.dptr(ey), _lib.dptr(go))
         _lib.check(self.lib.bx_state_upload(self.h, ct.byref(s)), 'bx_state_upload')
 
     def step(self, n_steps=1, outputs=False, stream=None):
@@ -107,8 +112,10 @@ class ClusterEngine:
         if self.ecm:
             out['E_env_x'] = np.empty(G)
             out['E_env_y'] = np.empty(G)
+        if self.vgj:
+            out['gjopen'] = np.empty(M)
         s = _lib.BxState(*[_lib.dptr(out.get(k)) for k in
-                           ('vm', 'cc_cells', 'cc_at_mem', 'cc_env', 'E_env_x', 'E_env_y')])
+                           ('vm', 'cc_cells', 'cc_at_mem', 'cc_env', 'E_env_x', 'E_env_y', 'gjopen')])
         _lib.check(self.lib.bx_state_download(self.h, ct.byref(s)), 'bx_state_download')
         return out
 
@@ -232,6 +239,7 @@ class BatchEngine(ClusterEngine):
         self.M = sum(g.n_mems for g in self.geoms)
         self.G = self.geoms[0].n_grid
         self.ecm = False
+        self.vgj = bool(self.params.v_sensitive_gj)
         co = np.zeros(n + 1, np.int32)
         mo = np.zeros(n + 1, np.int32)
         _lib.check(self.lib.bx_batch_layout(self.h, _lib.iptr(co), _lib.iptr(mo)), 'bx_batch_layout')
@@ -253,21 +261,25 @@ class BatchEngine(ClusterEngine):
                 e = e[:, 0]
             ce.append(e)
         vm, cc, cam, cenv = cat('vm', 0), cat('cc_cells', 1), cat('cc_at_mem', 1), _c(np.stack(ce))
-        st = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(cenv), None, None)
+        go = None
+        if self.vgj and all(s.get('gjopen') is not None for s in states):
+            go = cat('gjopen', 0)
+        st = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(cenv), None, None,
+                          _lib.dptr(go))
         _lib.check(self.lib.bx_state_upload(self.h, ct.byref(st)), 'bx_state_upload')
 
     def upload_concat(self, vm, cc_cells, cc_at_mem, cc_env):
         """Upload the concatenated state directly (cc_env is [n_clusters, n_ions]);
         the arrays are passed to the C ABI as they are (e.g. pinned views)."""
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (vm, cc_cells, cc_at_mem, cc_env)]
-        st = _lib.BxState(*[_lib.dptr(a) for a in arrs], None, None)
+        st = _lib.BxState(*[_lib.dptr(a) for a in arrs], None, None, None)
         _lib.check(self.lib.bx_state_upload(self.h, ct.byref(st)), 'bx_state_upload')
 
     def download_concat(self):
         I = self.I
         out = dict(vm=np.empty(self.M), cc_cells=np.empty((I, self.C)), cc_at_mem=np.empty((I, self.M)),
                    cc_env=np.empty((self.n_clusters, I)))
-        st = _lib.BxState(*[_lib.dptr(out[k]) for k in ('vm', 'cc_cells', 'cc_at_mem', 'cc_env')], None, None)
+        st = _lib.BxState(*[_lib.dptr(out[k]) for k in ('vm', 'cc_cells', 'cc_at_mem', 'cc_env')], None, None, None)
         _lib.check(self.lib.bx_state_download(self.h, ct.byref(st)), 'bx_state_download')
         return out
 
@@ -301,7 +313,9 @@ class BatchEngine(ClusterEngine):
         I = self.I
         vm, cc, cam = np.empty(self.M), np.empty((I, self.C)), np.empty((I, self.M))
         cenv = np.empty((self.n_clusters, I))
-        st = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(cenv), None, None)
+        go = np.empty(self.M) if self.vgj else None
+        st = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(cenv), None, None,
+                          _lib.dptr(go))
         _lib.check(self.lib.bx_state_download(self.h, ct.byref(st)), 'bx_state_download')
         out = []
         for k in range(self.n_clusters):
@@ -309,4 +323,6 @@ class BatchEngine(ClusterEngine):
             m0, m1 = self.mem_offsets[k], self.mem_offsets[k + 1]
             out.append(dict(vm=vm[m0:m1].copy(), cc_cells=cc[:, c0:c1].copy(),
                             cc_at_mem=cam[:, m0:m1].copy(), cc_env=cenv[k].copy()))
+            if go is not None:
+                out[-1]['gjopen'] = go[m0:m1].copy()
         return out

@@ -2,7 +2,9 @@
 
 ``run_sim_core_loop`` has the signature and the observable behaviour of
 ``Simulator._run_sim_core_loop`` (``betse/science/sim.py:1132-1390``) for the
-electrodiffusion step: Na/K-ATPase, transmembrane GHK fluxes, gap junctions,
+electrodiffusion step: Na/K-ATPase, transmembrane GHK fluxes, gap junctions
+(static, or voltage-gated as ``Gap_Junction.run`` gates them when
+``p.v_sensitive_gj``, ``betse/science/channels/gap_junction.py:52-75``),
 extracellular spaces when ``p.is_ecm``, ``update_all_concs``, ``update_V`` /
 ``get_current`` and ``check_v``.  The state stays on the GPU between sampled
 time steps; at each sampled step the Simulator's attributes are refreshed from
@@ -13,8 +15,8 @@ hold the last step, so ``run_sim_core``'s pickling and the plotting pipeline
 see what the reference would leave.
 
 Features of the reference loop outside the electrodiffusion step (Ca-ATPase,
-molecules/GRN networks, pressures, flow, deformation, voltage-gated gap
-junctions, polarizability, scheduled events of the SIM phase, dynamic protein
+molecules/GRN networks, pressures, flow, deformation, polarizability,
+scheduled events of the SIM phase, dynamic protein
 noise) are refused with ``NotImplementedError`` naming them, before any work.
 
 ``install()`` patches the method on BETSE's ``Simulator`` class.
@@ -42,8 +44,7 @@ def unsupported_features(sim, phase, assume_no_events=False):
                        ('grn_enabled', 'gene regulatory network'),
                        ('deform_osmo', 'osmotic pressure'),
                        ('fluid_flow', 'fluid flow'),
-                       ('deformation', 'deformation'),
-                       ('v_sensitive_gj', 'voltage-gated gap junctions')):
+                       ('deformation', 'deformation')):
         if bool(getattr(p, flag, False)):
             reasons.append(f'{what} ({flag})')
     if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
@@ -132,9 +133,12 @@ def run_sim_core_loop(sim, phase, time_steps, time_steps_sampled, anim_cells=Non
         Phi_b = getattr(sim, 'Phi_b', None)
         if Phi_b is not None and np.any(np.asarray(Phi_b) != 0):
             eng.set_boundary_potential(Phi_b)
+        # with voltage-gated gap junctions sim.gjopen is state (sim.py:732 sets
+        # it to the static weights; Gap_Junction.run updates it every step)
         eng.upload(sim.vm, sim.cc_cells, sim.cc_at_mem, sim.cc_env,
                    getattr(sim, 'E_env_x', None) if eng.ecm else None,
-                   getattr(sim, 'E_env_y', None) if eng.ecm else None)
+                   getattr(sim, 'E_env_y', None) if eng.ecm else None,
+                   getattr(sim, 'gjopen', None) if eng.vgj else None)
         if lap is not None:
             eng.set_lap_env_inv(lap)
         if launch_config == 'auto':

@@ -117,6 +117,12 @@ typedef struct bx_params {
     double D_free[BX_MAX_IONS];
     double D_gj[BX_MAX_IONS];
     double c_env_bound[BX_MAX_IONS]; /* Dirichlet value on the grid edge (ECM) */
+    /* voltage-gated gap junctions (p.v_sensitive_gj; channels/gap_junction.py:57-81):
+     * the open fraction is state (bx_state.gjopen) and replaces gj_weight */
+    int32_t v_sensitive_gj;
+    int32_t reserved0;
+    double gj_vthresh;           /* mV at which junctions are half closed */
+    double gj_min;               /* open fraction of a closed junction */
 } bx_params;
 
 /* Host views of the evolving state, BETSE layouts (row = ion).
@@ -132,6 +138,8 @@ typedef struct bx_state {
     double* cc_env;
     double* E_env_x;
     double* E_env_y;
+    double* gjopen;   /* [n_mems] gap-junction open fraction (v_sensitive_gj only;
+                         NULL on upload = gj_weight, BETSE's initial value) */
 } bx_state;
 
 /* Host destinations for one step's outputs; any pointer may be NULL. */

@@ -83,12 +83,29 @@ class OracleState:
     E_env_x: np.ndarray | None = None   # (ny, nx), ECM only
     E_env_y: np.ndarray | None = None
     extra: dict = field(default_factory=dict)
+    gjopen: np.ndarray | None = None     # (M,), voltage-gated gap junctions only
 
     def copy(self):
         c = lambda a: None if a is None else np.array(a, copy=True)  # noqa: E731
         return OracleState(c(self.vm), c(self.cc_cells), c(self.cc_at_mem),
                            c(self.cc_env), c(self.Phi_b), c(self.E_env_x),
-                           c(self.E_env_y), dict(self.extra))
+                           c(self.E_env_y), dict(self.extra), c(self.gjopen))
+
+
+# Harris et al. (1983) gating constants of channels/gap_junction.py:26-31
+GJ_LAMBDA, GJ_A1, GJ_A2 = 0.0013, 0.077, 0.14
+
+
+def gap_junction_run(gjopen, vgj, p):
+    """One ``Gap_Junction.run`` (channels/gap_junction.py:52-81): implicit
+    Euler step of the open fraction in ms units, then the block factor."""
+    V1 = 1.0e3 * np.abs(vgj)
+    alpha = GJ_LAMBDA * np.exp(-GJ_A1 * (V1 - p.gj_vthresh))
+    beta = GJ_LAMBDA * np.exp(GJ_A2 * (V1 - p.gj_vthresh))
+    beta = beta / (1 + 50 * beta)
+    dt = p.dt * 1e3
+    g = (gjopen + dt * (alpha + beta * p.gj_min)) / (1 + alpha * dt + beta * dt)
+    return p.gj_block * g
 
 
 def init_vm(g, p, s):
@@ -160,7 +177,12 @@ def step(g, p, s, outputs=False):
         fluxes_mem[i] += f_ED
         # gap junctions (sim.py:2162-2206)
         vgj = vm[nn] - vm
-        gjopen = p.gj_block * g.gj_weight
+        if getattr(p, 'v_sensitive_gj', False):
+            # update_gj runs the gating object once per ion (sim.py:2181-2183)
+            s.gjopen = gap_junction_run(s.gjopen, vgj, p)
+            gjopen = s.gjopen
+        else:
+            gjopen = p.gj_block * g.gj_weight
         conc_mem = s.cc_at_mem[i]
         fgj = electroflux(conc_mem, conc_mem[nn],
                           p.D_gj[i] * p.gj_surface * gjopen, g.gj_len,

@@ -99,7 +99,7 @@ def install_reference(ref: str) -> None:
 ION_ORDER = ['Na', 'K', 'Cl', 'Ca', 'P', 'M']   # order of p.ions_dict (H off)
 
 
-def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpness=1.0):
+def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False):
     from betse.science.enum.enumconf import CellLatticeType, SolverType
     p = SimpleNamespace()
     # physical constants, parameters.py:1087-1122
@@ -139,7 +139,9 @@ def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpn
     p.true_cell_size = 1.0e-5
     p.cell_polarizability = 0.0
     p.gj_surface = 5.0e-8
-    p.v_sensitive_gj = False
+    p.v_sensitive_gj = v_sensitive_gj
+    # gating constants of sim_config.yaml's 'gap junctions' block
+    p.gj_vthresh, p.gj_vgrad, p.gj_min = 15.0, 15.0, 0.10
     p.fast_update_ecm = False
     p.D_tj, p.D_adh = 1.0, 1.0
     p.channel_noise_level = 0.0
@@ -282,11 +284,11 @@ OUT_KEYS = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn',
 
 
 def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
-             dm_range=(1e-19, 1e-17), cell_space=26e-9, sharpness=1.0):
+             dm_range=(1e-19, 1e-17), cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False):
     from betse.science.sim import Simulator
     from betse.science.enum.enumphase import SimPhaseKind
     n_steps = max(checkpoints)
-    p = make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space, sharpness)
+    p = make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space, sharpness, v_sensitive_gj)
     t0 = time.time()
     c = build_cells(p, radius, seed)
     t_seed = time.time() - t0
@@ -335,7 +337,8 @@ def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
               vol_env=p.vol_env, cell_height=p.cell_height, q=p.q, kb=p.kb,
               eo=p.eo, er=p.er, mu=p.mu, sharpness=p.sharpness,
               cell_radius=p.cell_radius, true_cell_size=p.true_cell_size,
-              sigma=np.float64(s.sigma), is_ecm=float(is_ecm))
+              sigma=np.float64(s.sigma), is_ecm=float(is_ecm),
+              v_sensitive_gj=float(bool(v_sensitive_gj)), gj_vthresh=p.gj_vthresh, gj_min=p.gj_min)
     for k, v in sc.items():
         out['par_' + k] = np.float64(v)
     out['par_zs'] = np.asarray(s.zs, np.float64)
@@ -345,8 +348,10 @@ def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
     out['par_smooth_weight_o'] = s.smooth_weight_o
     out['par_Dm_cells'] = np.asarray(s.Dm_cells, np.float64)
     out['par_ion_names'] = np.asarray(ION_ORDER)
-    for k in STATE_KEYS:
-        out['init_' + k] = np.array(getattr(s, k), np.float64)
+    state_keys = STATE_KEYS + (['gjopen'] if v_sensitive_gj else [])
+    for k in state_keys:
+        v = np.array(getattr(s, k), np.float64)
+        out['init_' + k] = v * np.ones(len(c.mem_i)) if k == 'gjopen' else v
     cps = sorted(set(checkpoints))
     time_steps = np.arange(n_steps) * p.dt
     done = 0
@@ -356,7 +361,7 @@ def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
         s._run_sim_core_loop(phase, time_steps[done:cp], set(), None)
         t_loop += time.time() - t0
         done = cp
-        for k in STATE_KEYS:
+        for k in state_keys:
             out[f's{cp}_' + k] = np.array(getattr(s, k), np.float64)
         for k in OUT_KEYS:
             if cp in cps[:2] and hasattr(s, k):
@@ -388,6 +393,9 @@ CASES = {
     # extracellular spaces with environment smoothing (fd.integrator, sharpness < 1)
     'ecm_r40_s5_sharp': dict(radius=40e-6, seed=5, is_ecm=True, grid_size=20,
                              dt=5e-3, checkpoints=[1, 2, 30], cell_space=25e-9, sharpness=0.5),
+    # voltage-gated gap junctions (BETSE's default 'voltage sensitive gj: True')
+    'noecm_r50_s9_vgj': dict(radius=50e-6, seed=9, is_ecm=False, grid_size=20,
+                             dt=1e-2, checkpoints=[1, 2, 40], v_sensitive_gj=True),
     # a handful of cells: boundary-dominated edge case
     'noecm_r20_s2': dict(radius=20e-6, seed=2, is_ecm=False, grid_size=12,
                          dt=1e-2, checkpoints=[1, 20]),

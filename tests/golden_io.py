@@ -11,7 +11,7 @@ from types import SimpleNamespace
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
-CASES = ['noecm_r80_s1', 'noecm_r50_s7', 'ecm_r50_s3', 'ecm_r40_s5_sharp', 'noecm_r20_s2']
+CASES = ['noecm_r80_s1', 'noecm_r50_s7', 'ecm_r50_s3', 'ecm_r40_s5_sharp', 'noecm_r50_s9_vgj', 'noecm_r20_s2']
 
 
 def load(name):
@@ -57,6 +57,7 @@ def params(d):
     p.ion_names = names
     p.iNa, p.iK = names.index('Na'), names.index('K')
     p.is_ecm = bool(p.is_ecm)
+    p.v_sensitive_gj = bool(getattr(p, 'v_sensitive_gj', 0.0))
     p.nakatp_block = 1.0
     p.gj_block = 1.0
     if 'geom_c_env_bound' in d:
@@ -73,6 +74,8 @@ def state(d, prefix='init'):
                     cc_at_mem=d[prefix + '_cc_at_mem'].copy(),
                     cc_env=d[prefix + '_cc_env'].copy(),
                     Phi_b=np.zeros(G))
+    if prefix + '_gjopen' in d:
+        s.gjopen = d[prefix + '_gjopen'].copy()
     if bool(d['par_is_ecm']):
         s.E_env_x = np.zeros(g.grid_shape)
         s.E_env_y = np.zeros(g.grid_shape)
@@ -106,9 +109,12 @@ def engine_inputs(d):
     sp = StepParams(zs=p.zs, D_free=p.D_free, D_gj=p.D_gj, iNa=p.iNa, iK=p.iK,
                     is_ecm=p.is_ecm, ko_env=getattr(g, 'ko_env', 0.0), sigma=g.sigma,
                     c_env_bound=getattr(p, 'c_env_bound', None), ion_names=p.ion_names,
-                    **kw)
+                    v_sensitive_gj=p.v_sensitive_gj, gj_vthresh=getattr(p, 'gj_vthresh', 15.0),
+                    gj_min=getattr(p, 'gj_min', 0.10), **kw)
     s = state(d)
     st = dict(vm=s.vm, cc_cells=s.cc_cells, cc_at_mem=s.cc_at_mem, cc_env=s.cc_env)
+    if p.v_sensitive_gj:
+        st['gjopen'] = s.gjopen
     if p.is_ecm:
         st.update(E_env_x=s.E_env_x, E_env_y=s.E_env_y)
     D_env = getattr(g, 'D_env', None)

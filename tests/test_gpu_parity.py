@@ -57,6 +57,10 @@ def test_state_fp64_matches_betse(name):
             assert e_cc < TOL_FP64, (cp, e_cc)
             assert e_cm < TOL_FP64, (cp, e_cm)
             assert e_env < TOL_FP64, (cp, e_env)
+            if 'gjopen' in s:
+                # voltage-gated gap junctions: the open fraction is state
+                e_go = gi.rel_err(s['gjopen'], d[f's{cp}_gjopen'])
+                assert e_go < TOL_FP64, (cp, e_go)
             assert st['steps_done'] == done
 
 
@@ -96,6 +100,9 @@ def test_split_precision_vmem_error(name):
             err = np.max(np.abs(s['vm'] - d[f's{cp}_vm']))
             assert err < TOL_SPLIT_V, (cp, err)
             assert gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells']) < 1e-5
+            if 'gjopen' in s:
+                # FP32 open fraction (values in [gj_min, 1])
+                assert np.max(np.abs(s['gjopen'] - d[f's{cp}_gjopen'])) < 1e-5
 
 
 @pytest.mark.parametrize('precision', ['fp64', 'split'])
@@ -190,3 +197,26 @@ def test_split_launch_configs_bit_identical(tpb):
     for k in ref:
         assert np.array_equal(res[0][k], res[1][k]), k
         assert np.array_equal(res[0][k], ref[k]), k
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split'])
+def test_voltage_gated_gj_state_round_trip_and_autotune(precision):
+    """The gap-junction open fraction survives download/upload and the
+    autotuner's re-partitioning; the persistent kernel is refused with gating."""
+    d = gi.load('noecm_r50_s9_vgj')
+    with _engine(d, precision) as a, _engine(d, precision) as b:
+        a.step(5)
+        b.step(5)
+        s = a.download()
+        assert 'gjopen' in s and np.all(s['gjopen'] <= 1.0)
+        a.upload(**s)
+        a.autotune(3)
+        a.step(7)
+        b.step(7)
+        sa, sb = a.download(), b.download()
+        if precision == 'split':
+            with pytest.raises(Exception):
+                a.set_launch_config(256, True)
+    tol = 0.0 if precision == 'fp64' else 1e-12
+    for k in sa:
+        assert gi.rel_err(sa[k], sb[k]) <= tol, k

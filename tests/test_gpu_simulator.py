@@ -26,7 +26,7 @@ class _Sim:
                                 E_env_x=np.copy(self.E_env_x), J_env_x=np.copy(self.J_env_x),
                                 I_mem=self.I_mem.copy(), rho_cells=self.rho_cells.copy(),
                                 vm_ave=np.copy(self.vm_ave), E_gj_x=self.E_gj_x.copy(),
-                                B_field=np.copy(self.B_field)))
+                                B_field=np.copy(self.B_field), gjopen=np.copy(self.gjopen)))
 
 
 class _Callbacks:
@@ -52,6 +52,8 @@ def _fixture_sim(d):
     sim.vm, sim.cc_cells, sim.cc_at_mem = s0.vm.copy(), s0.cc_cells.copy(), s0.cc_at_mem.copy()
     sim.cc_env = np.asarray(d['init_cc_env']).copy()
     sim.Phi_b = np.zeros(int(np.prod(g.grid_shape)))
+    # sim.py:732: the open fraction starts at the static gap-junction weights
+    sim.gjopen = np.asarray(getattr(s0, 'gjopen', g.gj_weight), np.float64).copy()
     if p.is_ecm:
         sim.E_env_x, sim.E_env_y = s0.E_env_x, s0.E_env_y
         sim.D_env = g.D_env
@@ -85,6 +87,10 @@ def test_run_sim_core_loop_matches_betse(name, precision):
             assert gi.rel_err(rec['cc_env'], d[f's{cp}_cc_env']) < 1e-10
         else:
             assert np.max(np.abs(rec['vm'] - d[f's{cp}_vm'])) < 1e-6
+        if f's{cp}_gjopen' in d:
+            # voltage-gated gap junctions: sim.gjopen follows Gap_Junction.run
+            tol_g = 1e-10 if precision == 'fp64' else 1e-5
+            assert np.max(np.abs(rec['gjopen'] - d[f's{cp}_gjopen'])) < tol_g
         assert rec['cc_env'].shape == np.asarray(d[f's{cp}_cc_env']).shape
         if cp == cps[1]:
             # outputs and fields of that step (the fixture keeps them at two checkpoints)

@@ -15,6 +15,8 @@ def _phase(kind='INIT', **popts):
 
 def test_default_electrodiffusion_config_is_supported():
     assert simulator.unsupported_features(None, _phase()) == []
+    # BETSE's default configuration gates its gap junctions by voltage
+    assert simulator.unsupported_features(None, _phase(v_sensitive_gj=True)) == []
 
 
 @pytest.mark.parametrize('opt,frag', [
@@ -24,7 +26,6 @@ def test_default_electrodiffusion_config_is_supported():
     (dict(deform_osmo=True), 'osmotic'),
     (dict(fluid_flow=True), 'fluid flow'),
     (dict(deformation=True), 'deformation'),
-    (dict(v_sensitive_gj=True), 'voltage-gated'),
     (dict(cell_polarizability=1e-3), 'polarizability'),
     (dict(cluster_open=False), 'closed cluster'),
 ])
