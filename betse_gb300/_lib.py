@@ -54,8 +54,9 @@ class BxParams(ct.Structure):
             'mu')] + \
         [('zs', ct.c_double * MAX_IONS), ('D_free', ct.c_double * MAX_IONS),
          ('D_gj', ct.c_double * MAX_IONS), ('c_env_bound', ct.c_double * MAX_IONS),
-         ('v_sensitive_gj', ct.c_int32), ('reserved0', ct.c_int32), ('gj_vthresh', ct.c_double),
-         ('gj_min', ct.c_double)]
+         ('v_sensitive_gj', ct.c_int32), ('iCa', ct.c_int32), ('gj_vthresh', ct.c_double),
+         ('gj_min', ct.c_double), ('alpha_Ca', ct.c_double), ('KmCa_Ca', ct.c_double),
+         ('KmCa_ATP', ct.c_double)]
 
 
 class BxState(ct.Structure):

@@ -201,6 +201,10 @@ class StepParams:
     v_sensitive_gj: bool = False     # voltage-gated gap junctions (gjopen is then state)
     gj_vthresh: float = 15.0         # mV
     gj_min: float = 0.10
+    iCa: int = -1                    # Ca2+ row; the Ca-ATPase runs when iCa >= 0 and alpha_Ca > 0
+    alpha_Ca: float = 0.0
+    KmCa_Ca: float = 1.0e-3
+    KmCa_ATP: float = 0.5
 
     @property
     def n_ions(self) -> int:
@@ -227,6 +231,12 @@ class StepParams:
             D_gj = D_gj[:, 0]
         if bool(getattr(p, 'v_sensitive_gj', False)):
             kw.update(v_sensitive_gj=True, gj_vthresh=float(p.gj_vthresh), gj_min=float(p.gj_min))
+        ions = getattr(p, 'ions_dict', {}) or {}
+        if ions.get('Ca', 0) == 1 and hasattr(sim, 'iCa'):
+            # ca_handler runs for the Ca ion (sim.py:1282-1283)
+            kw.update(iCa=int(sim.iCa), alpha_Ca=float(getattr(p, 'alpha_Ca', 0.0)),
+                      KmCa_Ca=float(getattr(p, 'KmCa_Ca', 1.0e-3)),
+                      KmCa_ATP=float(getattr(p, 'KmCa_ATP', 0.5)))
         return cls(zs=np.asarray(sim.zs, np.float64), D_free=np.asarray(sim.D_free, np.float64),
                    D_gj=D_gj, iNa=int(sim.iNa), iK=int(sim.iK), is_ecm=bool(p.is_ecm),
                    T=float(sim.T), gj_block=float(np.ravel(gjb)[0]),
@@ -252,6 +262,10 @@ class StepParams:
             c.c_env_bound[i] = float(cb[i])
         c.v_sensitive_gj = int(bool(self.v_sensitive_gj))
         c.gj_vthresh, c.gj_min = float(self.gj_vthresh), float(self.gj_min)
+        if not -1 <= int(self.iCa) < I:
+            raise ValueError('iCa must be -1 or an ion row')
+        c.iCa = int(self.iCa)
+        c.alpha_Ca, c.KmCa_Ca, c.KmCa_ATP = float(self.alpha_Ca), float(self.KmCa_Ca), float(self.KmCa_ATP)
         return c
 
     def replace(self, **kw):

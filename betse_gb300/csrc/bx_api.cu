@@ -76,6 +76,9 @@ struct bx_cluster {
   bool persist = false;            // split form: persistent cp.async-pipelined kernel (autotuned)
   int sm_count = 0;
   bool ecm = false;
+  bool ca = false;                 // Ca-ATPase on (iCa >= 0 and alpha_Ca > 0)
+  double* d_cnew = nullptr;        // [I][G] ECM with the Ca-ATPase: environment after the
+                                   // Nernst-Planck update and smoothing, before the membrane scatter
   bool vgj = false;                // voltage-gated gap junctions: the open fraction is state
   double* d_gjo = nullptr;         // [M] plain form
   float* t_gjo = nullptr;          // [Q] split form, per membrane slot
@@ -172,7 +175,7 @@ void free_all(bx_cluster* h) {
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
-      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo};
+      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo, h->d_cnew};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& fs : h->fshapes)
@@ -187,6 +190,17 @@ int zcode_of(double z) {
   if (z == 2.0) return 2;
   if (z == -2.0) return -2;
   return 0;
+}
+
+// ca_handler runs its pump when Ca2+ is an ion and alpha_Ca > 0 (sim.py:1282-1283, 2129)
+bool ca_pump_on(const bx_params& p) { return p.iCa >= 0 && p.iCa < p.n_ions && p.alpha_Ca > 0.0; }
+
+// ECM with the Ca-ATPase: the Ca2+ row of the environment the pump reads
+// (after the Nernst-Planck update and smoothing, before the scatter)
+const double* ca_env_ptr(const bx_cluster* h) {
+  if (!(h->ca && h->ecm)) return nullptr;
+  const double* src = (h->par.sharpness < 1.0) ? h->d_cnew : h->d_tmp2;
+  return src + (size_t)h->par.iCa * h->G;
 }
 
 bx::StepConst make_step_const(const bx_cluster* h) {
@@ -213,6 +227,13 @@ bx::StepConst make_step_const(const bx_cluster* h) {
   k.gj_vth = p.gj_vthresh;
   k.gj_min = p.gj_min;
   k.gj_dt_ms = p.dt * 1e3;
+  k.iCa = h->ca ? p.iCa : -1;
+  k.ca_alpha = p.alpha_Ca;
+  k.ca_inv_Km = 1.0 / p.KmCa_Ca;
+  k.ca_atp_term = p.cATP / p.KmCa_ATP;
+  k.ca_atp_den = 1.0 + p.cATP / p.KmCa_ATP;
+  k.ca_qnum_c = p.cADP * p.cPi;
+  k.ca_qden_c = p.cATP;
   k.inv_KmNa = 1.0 / p.KmNK_Na;
   k.inv_KmK = 1.0 / p.KmNK_K;
   k.atp_term = p.cATP / p.KmNK_ATP;
@@ -244,6 +265,13 @@ bx::SplitConst make_split_const(const bx_cluster* h) {
   k.gj_vth = (float)d.gj_vth;
   k.gj_min = (float)d.gj_min;
   k.gj_dt_ms = (float)d.gj_dt_ms;
+  k.iCa = d.iCa;
+  k.ca_alpha = (float)d.ca_alpha;
+  k.ca_inv_Km = (float)d.ca_inv_Km;
+  k.ca_atp_term = (float)d.ca_atp_term;
+  k.ca_atp_den = (float)d.ca_atp_den;
+  k.ca_qnum_c = (float)d.ca_qnum_c;
+  k.ca_qden_c = (float)d.ca_qden_c;
   k.inv_KmNa = (float)d.inv_KmNa;
   k.inv_KmK = (float)d.inv_KmK;
   k.atp_term = (float)d.atp_term;
@@ -309,6 +337,7 @@ bx::StepPtrs step_ptrs(bx_cluster* h, int parity) {
   p.o_Ecy = h->o_Ecy; p.o_Emc = h->o_Emc; p.o_Egjx = h->o_Egjx; p.o_Egjy = h->o_Egjy;
   p.o_gjopen = h->o_gjopen; p.o_sigma = h->o_sigma;
   p.gjo = h->d_gjo;
+  p.ca_env = ca_env_ptr(h);
   return p;
 }
 
@@ -334,6 +363,7 @@ bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
   p.mfs = h->d_mem_flux_sa;
   p.gjo = h->t_gjo;
   p.o_gjopen = h->o_gjopen;
+  p.ca_env = ca_env_ptr(h);
   return p;
 }
 
@@ -417,7 +447,7 @@ cudaError_t launch_persist_t(bx_cluster* h, int parity, cudaStream_t s) {
 }
 
 cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
-  if (h->persist && !out && !h->phib_nonzero && !h->ecm && !h->vgj) {
+  if (h->persist && !out && !h->phib_nonzero && !h->ecm && !h->vgj && !h->ca) {
     const bool six = is_betse_six_ions(h);
     if (h->tpb == 192) return six ? launch_persist_t<192, 1>(h, parity, s) : launch_persist_t<192, 0>(h, parity, s);
     return six ? launch_persist_t<256, 1>(h, parity, s) : launch_persist_t<256, 0>(h, parity, s);
@@ -449,18 +479,44 @@ cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
 }
 
 // The extracellular grid of one step (update_ecm, update_Co's ECM term, get_current's E_env).
+// ECM with the Ca-ATPase, before the step kernel: BETSE's update_ecm runs per
+// ion inside the ion loop and ca_handler reads the result, so the
+// Nernst-Planck update (and smoothing) of every ion goes first, into d_tmp2 /
+// d_cnew, and enqueue_env adds the membrane scatter afterwards.  The
+// arithmetic of each grid value is that of the fused path.
+cudaError_t enqueue_env_pre(bx_cluster* h, cudaStream_t s) {
+  bx::EnvConst ec = make_env_const(h);
+  const int gi = env_grid(h->G * h->I);
+  bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
+  bx::k_env_update<false><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_fx, h->d_fy, h->d_env_ptr,
+                                                h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
+  h->launches += 2;
+  if (h->par.sharpness < 1.0) {
+    bx::k_env_integrate_scatter<false><<<gi, kEnvTPB, 0, s>>>(h->d_cnew, h->d_tmp2, h->d_env_ptr, h->d_env_mem,
+                                                             h->d_mem_flux_sa, h->M, ec);
+    h->launches += 1;
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t enqueue_env(bx_cluster* h, bool out, cudaStream_t s) {
   bx::EnvConst ec = make_env_const(h);
   const int gg = env_grid(h->G);
   const int gi = env_grid(h->G * h->I);   // one thread per (ion, grid cell)
-  bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
-  if (h->par.sharpness < 1.0) {
+  if (h->ca) {
+    const double* src = (h->par.sharpness < 1.0) ? h->d_cnew : h->d_tmp2;
+    bx::k_env_scatter_add<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, src, h->d_env_ptr, h->d_env_mem,
+                                                h->d_mem_flux_sa, h->M, ec);
+    h->launches += 1;
+  } else if (h->par.sharpness < 1.0) {
+    bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
     bx::k_env_update<false><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_fx, h->d_fy, h->d_env_ptr,
                                                   h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
-    bx::k_env_integrate_scatter<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_env_ptr, h->d_env_mem,
-                                                      h->d_mem_flux_sa, h->M, ec);
+    bx::k_env_integrate_scatter<true><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_env_ptr,
+                                                            h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
     h->launches += 3;
   } else {
+    bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
     bx::k_env_update<true><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, nullptr, h->d_fx, h->d_fy, h->d_env_ptr,
                                                  h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
     h->launches += 2;
@@ -477,6 +533,10 @@ cudaError_t enqueue_env(bx_cluster* h, bool out, cudaStream_t s) {
 // Enqueue one time step (reads parity, writes parity^1).
 cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   cudaError_t e;
+  if (h->ca && h->ecm) {
+    e = enqueue_env_pre(h, s);
+    if (e != cudaSuccess) return e;
+  }
   if (h->mode == MODE_SPLIT) {
     e = launch_split(h, parity, out, s);
     if (e != cudaSuccess) return e;
@@ -524,6 +584,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
 
 int launches_per_step(const bx_cluster* h) {
   if (!h->ecm) return 2;
+  if (h->ca) return h->par.sharpness < 1.0 ? 9 : 8;
   return h->par.sharpness < 1.0 ? 8 : 7;
 }
 
@@ -559,6 +620,7 @@ int upload_param_arrays(bx_cluster* h) {
 bool same_shared_params(const bx_params& a, const bx_params& b) {
   if (a.n_ions != b.n_ions || a.iNa != b.iNa || a.iK != b.iK || a.is_ecm != b.is_ecm) return false;
   if (a.v_sensitive_gj != b.v_sensitive_gj || a.gj_vthresh != b.gj_vthresh || a.gj_min != b.gj_min) return false;
+  if (a.iCa != b.iCa || a.alpha_Ca != b.alpha_Ca || a.KmCa_Ca != b.KmCa_Ca || a.KmCa_ATP != b.KmCa_ATP) return false;
   const double sa[] = {a.F, a.R, a.T, a.dt, a.cm, a.tm, a.gj_surface, a.gj_block, a.KmNK_Na, a.KmNK_K,
                        a.KmNK_ATP, a.cATP, a.cADP, a.cPi, a.deltaGATP};
   const double sb[] = {b.F, b.R, b.T, b.dt, b.cm, b.tm, b.gj_surface, b.gj_block, b.KmNK_Na, b.KmNK_K,
@@ -746,6 +808,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   if (I <= 0 || I > BX_MAX_IONS) return fail(BX_EINVAL, "n_ions must be in [1, 8]");
   if (p0.iNa < 0 || p0.iNa >= I || p0.iK < 0 || p0.iK >= I || p0.iNa == p0.iK)
     return fail(BX_EINVAL, "iNa/iK out of range");
+  if (p0.iCa < -1 || p0.iCa >= I) return fail(BX_EINVAL, "iCa must be -1 or an ion row");
   if (ncl > 1 && p0.is_ecm) return fail(BX_EINVAL, "batches of clusters need is_ecm == 0");
   long long Ctot = 0, Mtot = 0;
   for (int c = 0; c < ncl; ++c) {
@@ -775,6 +838,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     h->cl_delta.push_back(gs[cl].delta);
   }
   h->precision = precision; h->par = p0; h->ecm = p0.is_ecm != 0; h->vgj = p0.v_sensitive_gj != 0;
+  h->ca = ca_pump_on(p0);
   h->cl_par.assign(ps, ps + ncl);
   h->mode = (precision == BX_PLAIN_FP64) ? MODE_PLAIN : MODE_SPLIT;
   if (h->mode == MODE_SPLIT && I > kRec - 1) {
@@ -886,6 +950,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
     ALLOC(h->d_fx, (size_t)I * G); ALLOC(h->d_fy, (size_t)I * G);
     ALLOC(h->d_tmp, G); ALLOC(h->d_tmp2, (size_t)I * G);
     ALLOC(h->d_venv, G); ALLOC(h->d_rho_env, G); ALLOC(h->d_vsrc, G);
+    if (h->ca) ALLOC(h->d_cnew, (size_t)I * G);
   }
   ALLOC(h->o_fmem, (size_t)I * M); ALLOC(h->o_fgj, (size_t)I * M);
   ALLOC(h->o_rate, M); ALLOC(h->o_rho, C); ALLOC(h->o_Jn, M); ALLOC(h->o_Imem, M);
@@ -940,6 +1005,9 @@ int bx_set_params(bx_handle h, const bx_params* p) {
   if (!h || !p) return fail(BX_EINVAL, "null argument");
   if (p->n_ions != h->I || (p->is_ecm != 0) != h->ecm || (p->v_sensitive_gj != 0) != h->vgj)
     return fail(BX_EINVAL, "n_ions / is_ecm / v_sensitive_gj cannot change after create");
+  if (p->iCa < -1 || p->iCa >= p->n_ions) return fail(BX_EINVAL, "iCa must be -1 or an ion row");
+  if (ca_pump_on(*p) != h->ca || (h->ca && p->iCa != h->par.iCa))
+    return fail(BX_EINVAL, "the Ca-ATPase cannot be switched on or off, or move row, after create");
   if (h->ncl > 1) return fail(BX_EINVAL, "use bx_batch_set_params for a batch");
   h->par = *p;
   h->cl_par[0] = *p;
@@ -952,6 +1020,8 @@ int bx_batch_set_params(bx_handle h, const bx_params* p) {
   for (int c = 0; c < h->ncl; ++c)
     if (!same_shared_params(p[0], p[c]) || p[c].n_ions != h->I || (p[c].is_ecm != 0) != h->ecm)
       return fail(BX_EINVAL, "clusters of a batch may differ only in alpha_NaK, nakatp_block, vol_env");
+  if ((p[0].v_sensitive_gj != 0) != h->vgj || ca_pump_on(p[0]) != h->ca || (h->ca && p[0].iCa != h->par.iCa))
+    return fail(BX_EINVAL, "v_sensitive_gj and the Ca-ATPase cannot change after create");
   h->par = p[0];
   h->cl_par.assign(p, p + h->ncl);
   h->graph_valid = false;
@@ -1286,14 +1356,16 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
     // tile: partial sums 4I, cluster id 4; ECM: map_env 4, grid concentration
     // 8I and the f*sa export 8I per membrane instead of the partial sums
     // voltage-gated gap junctions: the open fraction in+out, 8 per membrane
-    const int64_t gv = h->vgj ? 8 : 0;
+    // Ca-ATPase with ECM: the grid's Ca2+ after the Nernst-Planck update, 8 per membrane
+    const int64_t gv = (h->vgj ? 8 : 0) + (h->ca && h->ecm ? 8 : 0);
     if (h->ecm) return M * (4 * I + 13 + 4 + 16 * I + gv) + C * (16 * I + 8 * kRec + 12) + B * 4;
     return M * (4 * I + 13 + gv) + C * (16 * I + 8 * kRec + 12) + B * (4 * I + 4);
   }
   const int64_t w = 8;  // Dm, mem_sa, gj_w width
   // membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env and the f*sa
   // export with ECM); cell: cc in+out, cc_mem in+out, cell_vol, diviterm, ptr
-  const int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0) + (h->vgj ? 16 : 0);
+  const int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0) + (h->vgj ? 16 : 0) +
+                      (h->ca && h->ecm ? 8 : 0);
   const int64_t cell = 4 * I * 8 + 16 + 4;
   return M * mem + C * cell + (h->ecm ? 0 : B * I * 8);
 }
@@ -1314,6 +1386,7 @@ int bx_set_launch_config(bx_handle h, int tpb, int persistent) {
   if (persistent && h->mode != MODE_SPLIT) return fail(BX_EINVAL, "the persistent kernel is the split form's");
   if (persistent && h->ecm) return fail(BX_EINVAL, "the persistent kernel has no extracellular-space variant");
   if (persistent && h->vgj) return fail(BX_EINVAL, "the persistent kernel has no voltage-gated gap-junction variant");
+  if (persistent && h->ca) return fail(BX_EINVAL, "the persistent kernel has no Ca-ATPase variant");
   const size_t C = h->C, I = h->I, M = h->M;
   const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
   std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1),
@@ -1349,7 +1422,7 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   const int64_t launches0 = h->launches;
   struct Cand { int tpb; bool persist; };
   std::vector<Cand> cands;
-  if (h->mode == MODE_SPLIT && (h->ecm || h->vgj)) cands = {{256, false}, {192, false}};
+  if (h->mode == MODE_SPLIT && (h->ecm || h->vgj || h->ca)) cands = {{256, false}, {192, false}};
   else if (h->mode == MODE_SPLIT) cands = {{256, false}, {192, false}, {256, true}, {192, true}};
   else cands = {{256, false}, {128, false}};
   double best = 1e300;

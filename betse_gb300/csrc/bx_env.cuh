@@ -131,7 +131,9 @@ __global__ void k_env_charge(const double* __restrict__ cenv, const uint8_t* __r
 }
 
 // fd.integrator (finitediff.py:1479-1512) when sharpness < 1, then the membrane
-// exchange.  One thread per (ion, grid cell).
+// exchange (SCATTER; without it the smoothed grid is written to cenv, which is
+// then a separate buffer).  One thread per (ion, grid cell).
+template <bool SCATTER = true>
 __global__ void k_env_integrate_scatter(double* cenv, const double* __restrict__ tmp,
                                         const int* __restrict__ env_ptr, const int* __restrict__ env_mem,
                                         const double* __restrict__ mem_flux_sa, int M, EnvConst e) {
@@ -152,10 +154,28 @@ __global__ void k_env_integrate_scatter(double* cenv, const double* __restrict__
       F += sides * P[k + 1];
       F += sides * P[k - 1];
     }
+    if (!SCATTER) {
+      cenv[(size_t)ion * e.G + k] = F;
+      return;
+    }
     double s = 0.0;
     for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
     cenv[(size_t)ion * e.G + k] = F + (s * e.inv_h_d2) * e.dt;
   }
+}
+
+// The membrane exchange onto an environment already advanced by the
+// Nernst-Planck update (and smoothing): update_Co's ECM term
+// (sim_toolbox.py:1185-1200), the same arithmetic as the fused kernels.
+__global__ void k_env_scatter_add(double* cenv, const double* __restrict__ src,
+                                  const int* __restrict__ env_ptr, const int* __restrict__ env_mem,
+                                  const double* __restrict__ mem_flux_sa, int M, EnvConst e) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= e.I * e.G) return;
+  const int ion = t / e.G, k = t - ion * e.G;
+  double s = 0.0;
+  for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
+  cenv[t] = src[t] + (s * e.inv_h_d2) * e.dt;
 }
 
 // get_current ECM branch (ion_current.py:79-110): the axis-0 pass of a

@@ -65,6 +65,13 @@ struct StepConst {
   double K0;               // exp(-deltaGATP / (R T))
   int vgj;                 // voltage-gated gap junctions: gjopen is state (p.gjo)
   double gj_vth, gj_min, gj_dt_ms;   // threshold (mV), closed fraction, dt in ms
+  int iCa;                 // Ca-ATPase ion row, -1 = pump off
+  double ca_alpha;         // alpha_Ca
+  double ca_inv_Km;        // 1/KmCa_Ca
+  double ca_atp_term;      // cATP/KmCa_ATP
+  double ca_atp_den;       // 1 + cATP/KmCa_ATP
+  double ca_qnum_c;        // cADP*cPi
+  double ca_qden_c;        // cATP
 };
 
 // Harris et al. (1983) gap-junction gating constants (channels/gap_junction.py:26-31)
@@ -83,6 +90,8 @@ struct StepPtrs {
   double* mem_flux_sa;                     // [I][M] f_mem*sa (ECM scatter input)
   unsigned long long* status;              // [4]: nan_vm, nan_conc, neg clamps, spare
   double* gjo;                             // [M] gap-junction open fraction (vgj), in place
+  const double* ca_env;                    // [G] Ca2+ of the environment after this step's
+                                           // Nernst-Planck update (ECM with the Ca-ATPase)
   // outputs (OUT variant)
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_Jn;
   double* o_Imem; double* o_Jcx; double* o_Jcy; double* o_Jc; double* o_vmave;
@@ -157,6 +166,24 @@ __device__ __forceinline__ T pump_fna(const StepConst& k, T pcoef, T e1, T cNai,
   // fwd * (1 - Q/Keq) = num_e (qden K0 - qnum e1) / (den_e qden K0)
   const T K0 = (T)k.K0;
   return pcoef * num_e * (qden * K0 - qnum * e1) / (den_e * qden * K0);
+}
+
+// pumpCaATP (sim_toolbox.py:124-180), into the cell positive:
+// -alpha_Ca fwd (1 - Q/Keq) with Q = cADP cPi cCao / (cATP cCai) (1e-16 for a
+// zero denominator) and Keq = exp(-(dG/RT - 2 F Vm/RT)) = K0 / e1^2.
+// The reference clamps both concentrations at zero first (no_negs).
+template <typename T>
+__device__ __forceinline__ T pump_fca(const StepConst& k, T e1, T cCai, T cCao) {
+  cCai = cCai > (T)0 ? cCai : (T)0;
+  cCao = cCao > (T)0 ? cCao : (T)0;
+  const T qnum = (T)k.ca_qnum_c * cCao;
+  T qden = (T)k.ca_qden_c * cCai;
+  if (qden == (T)0) qden = (T)1.0e-16;
+  const T x = cCai * (T)k.ca_inv_Km;
+  const T num_e = x * (T)k.ca_atp_term;
+  const T den_e = ((T)1 + x) * (T)k.ca_atp_den;
+  const T K0 = (T)k.K0;
+  return -(T)k.ca_alpha * num_e * (qden * K0 - qnum * (e1 * e1)) / (den_e * qden * K0);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -258,6 +285,13 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       T f = ghk_flux<T>(sm, k.zcode[i], k.z[i], v1, k.F_RT, cout, cin, dm, inv_tm);
       if (i == k.iNa) f = fNa + f;
       else if (i == k.iK) f = (T)(-(2.0 / 3.0)) * fNa + f;
+      if (i == k.iCa) {
+        // ca_handler after the ion loop (sim.py:2126-2155): cell side is
+        // cc_cells at the start of the step (update_intra), environment side
+        // after this step's Nernst-Planck update with extracellular spaces
+        const T cCao = (T)(ECM ? p.ca_env[ge] : cenv_cl[i]);
+        f = f + pump_fca<T>(k, sm.e1, (T)p.cc[i * g.C + c], cCao);
+      }
       // gap junction (sim.py:2189-2206): from this membrane's cell into the partner's
       const T cn_i = (T)p.ccm_in[i * g.C + cn];
       T dgj;

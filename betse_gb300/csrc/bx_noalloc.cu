@@ -148,6 +148,8 @@ extern "C" int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const 
   if (p->is_ecm) return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs is_ecm == 0");
   if (p->v_sensitive_gj)
     return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs v_sensitive_gj == 0 (the open fraction is state)");
+  if (p->iCa >= 0 && p->alpha_Ca > 0.0)
+    return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs the Ca-ATPase off (alpha_Ca == 0 or iCa == -1)");
   if (!g->cell_mem_ptr || !g->nn_i || !g->bflag || !g->map_mem2ecm || !g->mem_sa || !g->gj_weight ||
       !g->cell_vol || !g->diviterm)
     return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: missing geometry array");
@@ -183,6 +185,7 @@ extern "C" int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const 
 
   bx::StepConst k{};
   k.I = I; k.iNa = p->iNa; k.iK = p->iK;
+  k.iCa = -1;  // Ca-ATPase off
   const double RT = p->R * p->T;
   for (int i = 0; i < I; ++i) {
     k.z[i] = p->zs[i]; k.zcode[i] = zc(p->zs[i]); k.zF[i] = p->zs[i] * p->F;

@@ -154,6 +154,8 @@ struct SplitConst {
   float inv_KmNa, inv_KmK, atp_term, atp_den, qnum_c, qden_c, K0;
   int vgj;                                  // voltage-gated gap junctions (gjo is state)
   float gj_vth, gj_min, gj_dt_ms;
+  int iCa;                                  // Ca-ATPase ion row, -1 = pump off
+  float ca_alpha, ca_inv_Km, ca_atp_term, ca_atp_den, ca_qnum_c, ca_qden_c;
 };
 
 // Per-cell record, REC floats, 16-byte aligned: slots [0, I) hold the
@@ -171,6 +173,8 @@ struct SplitPtrs {
   double* __restrict__ mfs;                // [I][M] f_mem*sa per membrane, natural order (ECM scatter)
   float* __restrict__ gjo;                 // [Q] gap-junction open fraction per slot (vgj), in place
   double* __restrict__ o_gjopen;           // [M] output steps with vgj: the open fraction
+  const double* __restrict__ ca_env;       // [G] Ca2+ of the grid after this step's Nernst-Planck
+                                           // update (ECM with the Ca-ATPase)
   unsigned long long* status;              // nan_vm, nan_conc, neg clamps
   // outputs (OUT), natural order
   double* o_fmem; double* o_fgj; double* o_rate; double* o_rho; double* o_vmem;
@@ -337,6 +341,22 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
       float f = ghk_flux_fk(sm, ka_m, z, k.z[i], v1, k.F_RT, cenv[i], cin, dmv[i], k.inv_tm);
       if (i == IS::iNa(k)) f = fNa + f;
       else if (i == IS::iK(k)) f = (-(2.f / 3.f)) * fNa + f;
+      if (i == k.iCa) {
+        // ca_handler (sim.py:2126-2155) on the start-of-step cell
+        // concentration (update_intra) and, with ECM, the environment after
+        // this step's Nernst-Planck update; pumpCaATP in FP32, one reciprocal
+        float cCai = p.cc2[(size_t)i * g.S + s0 + lc].x;
+        float cCao = ECM ? (float)p.ca_env[g.map_env[q]] : cenv[i];
+        cCai = cCai > 0.f ? cCai : 0.f;
+        cCao = cCao > 0.f ? cCao : 0.f;
+        const float qn = k.ca_qnum_c * cCao;
+        float qd = k.ca_qden_c * cCai;
+        if (qd == 0.f) qd = 1.0e-16f;
+        const float x = cCai * k.ca_inv_Km;
+        const float num_e = x * k.ca_atp_term;
+        const float den_e = (1.f + x) * k.ca_atp_den;
+        f = f - k.ca_alpha * num_e * (qd * k.K0 - qn * (sm.e1 * sm.e1)) * rcp_fast(den_e * qd * k.K0);
+      }
       float dgjv = k.dgj_gs[i] * gw;
       if (k.vgj) {
         gg = k.gj_block * ((gg + ga) * gr);

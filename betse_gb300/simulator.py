@@ -4,8 +4,8 @@
 ``Simulator._run_sim_core_loop`` (``betse/science/sim.py:1132-1390``) for the
 electrodiffusion step: Na/K-ATPase, transmembrane GHK fluxes, gap junctions
 (static, or voltage-gated as ``Gap_Junction.run`` gates them when
-``p.v_sensitive_gj``, ``betse/science/channels/gap_junction.py:52-75``),
-extracellular spaces when ``p.is_ecm``, ``update_all_concs``, ``update_V`` /
+``p.v_sensitive_gj``, ``betse/science/channels/gap_junction.py:52-75``), the
+Ca-ATPase of ``ca_handler`` (``sim.py:2126-2155``), extracellular spaces when ``p.is_ecm``, ``update_all_concs``, ``update_V`` /
 ``get_current`` and ``check_v``.  The state stays on the GPU between sampled
 time steps; at each sampled step the Simulator's attributes are refreshed from
 the device under BETSE's names, then -- as the reference loop does --
@@ -14,8 +14,8 @@ the device under BETSE's names, then -- as the reference loop does --
 hold the last step, so ``run_sim_core``'s pickling and the plotting pipeline
 see what the reference would leave.
 
-Features of the reference loop outside the electrodiffusion step (Ca-ATPase,
-molecules/GRN networks, pressures, flow, deformation, polarizability,
+Features of the reference loop outside the electrodiffusion step (endoplasmic
+reticulum calcium dynamics, molecules/GRN networks, pressures, flow, deformation, polarizability,
 scheduled events of the SIM phase, dynamic protein
 noise) are refused with ``NotImplementedError`` naming them, before any work.
 
@@ -38,8 +38,8 @@ def unsupported_features(sim, phase, assume_no_events=False):
     p = phase.p
     reasons = []
     ions = getattr(p, 'ions_dict', {}) or {}
-    if ions.get('Ca', 0) == 1 and float(getattr(p, 'alpha_Ca', 0.0)) > 0.0:
-        reasons.append('Ca-ATPase (alpha_Ca > 0, sim.py:2126-2159)')
+    if ions.get('Ca', 0) == 1 and bool(getattr(p, 'Ca_dyn', False)):
+        reasons.append('endoplasmic reticulum calcium dynamics (Ca_dyn, sim.py:2157-2159)')
     for flag, what in (('molecules_enabled', 'molecules network'),
                        ('grn_enabled', 'gene regulatory network'),
                        ('deform_osmo', 'osmotic pressure'),

@@ -120,9 +120,13 @@ typedef struct bx_params {
     /* voltage-gated gap junctions (p.v_sensitive_gj; channels/gap_junction.py:57-81):
      * the open fraction is state (bx_state.gjopen) and replaces gj_weight */
     int32_t v_sensitive_gj;
-    int32_t reserved0;
+    /* Ca-ATPase (Simulator.ca_handler, sim.py:2126-2155; pumpCaATP,
+     * sim_toolbox.py:124-180): on when iCa >= 0 and alpha_Ca > 0, so a
+     * zero-initialised struct leaves it off */
+    int32_t iCa;                 /* ion row of Ca2+ */
     double gj_vthresh;           /* mV at which junctions are half closed */
     double gj_min;               /* open fraction of a closed junction */
+    double alpha_Ca, KmCa_Ca, KmCa_ATP;
 } bx_params;
 
 /* Host views of the evolving state, BETSE layouts (row = ion).

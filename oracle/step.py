@@ -53,6 +53,31 @@ def pump_nakatp(cNai, cNao, cKi, cKo, Vm, T, p, block=1.0):
     return f_Na, f_K, -f_Na
 
 
+def pump_caatp(cCai, cCao, Vm, T, p):
+    """Ca-ATPase flux, into the cell positive (sim_toolbox.py:124-180).
+
+    The reference clamps both concentration arrays in place first
+    (``no_negs``) and computes, but never uses, a backward coefficient; its
+    ``block`` and ``met`` arguments are unused as well."""
+    cCai = np.maximum(cCai, 0.0)
+    cCao = np.maximum(cCao, 0.0)
+    Qnumo = p.cADP * p.cPi * cCao
+    Qdenomo = p.cATP * cCai
+    Qdenomo = np.where(Qdenomo == 0.0, 1.0e-16, Qdenomo)
+    Q = Qnumo / Qdenomo
+    Keq = np.exp(-(p.deltaGATP / (p.R * T) - 2 * ((p.F * Vm) / (p.R * T))))
+    numo_E = (cCai / p.KmCa_Ca) * (p.cATP / p.KmCa_ATP)
+    denomo_E = (1 + (cCai / p.KmCa_Ca)) * (1 + (p.cATP / p.KmCa_ATP))
+    frwd = numo_E / denomo_E
+    return -p.alpha_Ca * frwd * (1 - (Q / Keq))
+
+
+def ca_pump_on(p):
+    """ca_handler runs its pump when Ca is an ion and alpha_Ca > 0
+    (sim.py:1282-1283, 2129)."""
+    return getattr(p, 'iCa', -1) >= 0 and float(getattr(p, 'alpha_Ca', 0.0)) > 0.0
+
+
 def seg_sum(g, x):
     """``cells.M_sum_mems @ x`` (cells.py:1297-1306): sum over each cell's
     contiguous membrane range."""
@@ -215,6 +240,16 @@ def step(g, p, s, outputs=False):
             out['E_gj_x'] = (-vgj / g.gj_len) * g.mem_nx
             out['E_gj_y'] = (-vgj / g.gj_len) * g.mem_ny
             out['gjopen'] = gjopen * np.ones(M)
+
+    # ---- ca_handler (sim.py:2126-2155): after every ion's update_intra, so the
+    # cell side is cc_cells at the start of the step and, with extracellular
+    # spaces, the environment side is after this step's Nernst-Planck update;
+    # vm carries the I in-place nonces (irrelevant at FP64 resolution)
+    if ca_pump_on(p):
+        iCa = p.iCa
+        f_Ca = pump_caatp(s.cc_at_mem[iCa], env_at_mem(iCa), vm, T, p)
+        fluxes_mem[iCa] += f_Ca
+        out['rate_CaATP'] = f_Ca
 
     # ---- update_all_concs (sim.py:2086-2111, sim_toolbox.py:1155-1232)
     for i in range(I):

@@ -99,7 +99,8 @@ def install_reference(ref: str) -> None:
 ION_ORDER = ['Na', 'K', 'Cl', 'Ca', 'P', 'M']   # order of p.ions_dict (H off)
 
 
-def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False):
+def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False,
+                alpha_Ca=0.0):
     from betse.science.enum.enumconf import CellLatticeType, SolverType
     p = SimpleNamespace()
     # physical constants, parameters.py:1087-1122
@@ -115,7 +116,7 @@ def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpn
     p.T = 310.15
     p.cm = 0.022
     p.alpha_NaK = 5e-8
-    p.alpha_Ca = 0.0
+    p.alpha_Ca = alpha_Ca   # Ca-ATPase rate (sim_config.yaml default 5e-8; 0 turns ca_handler's pump off)
     p.dt = dt
     p.cell_radius = 5e-6
     p.d_cell = 2 * p.cell_radius
@@ -284,11 +285,12 @@ OUT_KEYS = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn',
 
 
 def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
-             dm_range=(1e-19, 1e-17), cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False):
+             dm_range=(1e-19, 1e-17), cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False,
+             alpha_Ca=0.0):
     from betse.science.sim import Simulator
     from betse.science.enum.enumphase import SimPhaseKind
     n_steps = max(checkpoints)
-    p = make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space, sharpness, v_sensitive_gj)
+    p = make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space, sharpness, v_sensitive_gj, alpha_Ca)
     t0 = time.time()
     c = build_cells(p, radius, seed)
     t_seed = time.time() - t0
@@ -338,7 +340,8 @@ def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
               eo=p.eo, er=p.er, mu=p.mu, sharpness=p.sharpness,
               cell_radius=p.cell_radius, true_cell_size=p.true_cell_size,
               sigma=np.float64(s.sigma), is_ecm=float(is_ecm),
-              v_sensitive_gj=float(bool(v_sensitive_gj)), gj_vthresh=p.gj_vthresh, gj_min=p.gj_min)
+              v_sensitive_gj=float(bool(v_sensitive_gj)), gj_vthresh=p.gj_vthresh, gj_min=p.gj_min,
+              alpha_Ca=p.alpha_Ca, KmCa_Ca=p.KmCa_Ca, KmCa_ATP=p.KmCa_ATP)
     for k, v in sc.items():
         out['par_' + k] = np.float64(v)
     out['par_zs'] = np.asarray(s.zs, np.float64)
@@ -396,6 +399,15 @@ CASES = {
     # voltage-gated gap junctions (BETSE's default 'voltage sensitive gj: True')
     'noecm_r50_s9_vgj': dict(radius=50e-6, seed=9, is_ecm=False, grid_size=20,
                              dt=1e-2, checkpoints=[1, 2, 40], v_sensitive_gj=True),
+    # Ca-ATPase on (ca_handler; the mammal profile with sim_config.yaml's alpha_Ca)
+    # together with voltage-gated gap junctions
+    'noecm_r50_s11_ca': dict(radius=50e-6, seed=11, is_ecm=False, grid_size=20,
+                             dt=1e-2, checkpoints=[1, 2, 40], alpha_Ca=5e-8, v_sensitive_gj=True),
+    # Ca-ATPase with extracellular spaces and environment smoothing: the pump
+    # reads the environment after that step's Nernst-Planck update
+    'ecm_r40_s13_ca': dict(radius=40e-6, seed=13, is_ecm=True, grid_size=20,
+                           dt=5e-3, checkpoints=[1, 2, 30], cell_space=25e-9, sharpness=0.5,
+                           alpha_Ca=5e-8),
     # a handful of cells: boundary-dominated edge case
     'noecm_r20_s2': dict(radius=20e-6, seed=2, is_ecm=False, grid_size=12,
                          dt=1e-2, checkpoints=[1, 20]),

@@ -11,7 +11,8 @@ from types import SimpleNamespace
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
-CASES = ['noecm_r80_s1', 'noecm_r50_s7', 'ecm_r50_s3', 'ecm_r40_s5_sharp', 'noecm_r50_s9_vgj', 'noecm_r20_s2']
+CASES = ['noecm_r80_s1', 'noecm_r50_s7', 'ecm_r50_s3', 'ecm_r40_s5_sharp', 'noecm_r50_s9_vgj',
+         'noecm_r50_s11_ca', 'ecm_r40_s13_ca', 'noecm_r20_s2']
 
 
 def load(name):
@@ -56,6 +57,8 @@ def params(d):
     names = [str(x) for x in d['par_ion_names']]
     p.ion_names = names
     p.iNa, p.iK = names.index('Na'), names.index('K')
+    p.iCa = names.index('Ca') if 'Ca' in names else -1
+    p.alpha_Ca = float(getattr(p, 'alpha_Ca', 0.0))
     p.is_ecm = bool(p.is_ecm)
     p.v_sensitive_gj = bool(getattr(p, 'v_sensitive_gj', 0.0))
     p.nakatp_block = 1.0
@@ -110,7 +113,8 @@ def engine_inputs(d):
                     is_ecm=p.is_ecm, ko_env=getattr(g, 'ko_env', 0.0), sigma=g.sigma,
                     c_env_bound=getattr(p, 'c_env_bound', None), ion_names=p.ion_names,
                     v_sensitive_gj=p.v_sensitive_gj, gj_vthresh=getattr(p, 'gj_vthresh', 15.0),
-                    gj_min=getattr(p, 'gj_min', 0.10), **kw)
+                    gj_min=getattr(p, 'gj_min', 0.10), iCa=p.iCa, alpha_Ca=p.alpha_Ca,
+                    KmCa_Ca=getattr(p, 'KmCa_Ca', 1.0e-3), KmCa_ATP=getattr(p, 'KmCa_ATP', 0.5), **kw)
     s = state(d)
     st = dict(vm=s.vm, cc_cells=s.cc_cells, cc_at_mem=s.cc_at_mem, cc_env=s.cc_env)
     if p.v_sensitive_gj:

@@ -105,10 +105,12 @@ def test_split_precision_vmem_error(name):
                 assert np.max(np.abs(s['gjopen'] - d[f's{cp}_gjopen'])) < 1e-5
 
 
+@pytest.mark.parametrize('name', ['noecm_r50_s7', 'ecm_r40_s13_ca'])
 @pytest.mark.parametrize('precision', ['fp64', 'split'])
-def test_graph_chunks_equal_eager_steps(precision):
-    """CUDA-graph-replayed steps give bit-identical state to eager steps."""
-    d = gi.load('noecm_r50_s7')
+def test_graph_chunks_equal_eager_steps(precision, name):
+    """CUDA-graph-replayed steps give bit-identical state to eager steps
+    (also through the extracellular pipeline the Ca-ATPase reorders)."""
+    d = gi.load(name)
     with _engine(d, precision) as a, _engine(d, precision) as b:
         a.step(70)                 # graph chunks of 32 + eager tail
         for _ in range(70):

@@ -43,6 +43,9 @@ def _fixture_sim(d):
     sim = _Sim()
     sim.zs, sim.D_free, sim.D_gj = p.zs, p.D_free, p.D_gj
     sim.iNa, sim.iK, sim.T = p.iNa, p.iK, p.T
+    p.ions_dict = {k: 1 for k in p.ion_names}
+    if p.iCa >= 0:
+        sim.iCa = p.iCa
     sim.ko_env = float(getattr(g, 'ko_env', 0.0))
     sim.sigma = g.sigma
     sim.c_env_bound = getattr(p, 'c_env_bound', np.zeros(I))

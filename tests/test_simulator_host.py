@@ -17,10 +17,14 @@ def test_default_electrodiffusion_config_is_supported():
     assert simulator.unsupported_features(None, _phase()) == []
     # BETSE's default configuration gates its gap junctions by voltage
     assert simulator.unsupported_features(None, _phase(v_sensitive_gj=True)) == []
+    # the mammal/amphibian profiles run ca_handler's Ca-ATPase with alpha_Ca > 0
+    ph = _phase()
+    ph.p.alpha_Ca = 5e-8
+    assert simulator.unsupported_features(None, ph) == []
 
 
 @pytest.mark.parametrize('opt,frag', [
-    (dict(alpha_Ca=1e-8), 'Ca-ATPase'),
+    (dict(Ca_dyn=True), 'endoplasmic reticulum'),
     (dict(molecules_enabled=True), 'molecules'),
     (dict(grn_enabled=True), 'gene regulatory'),
     (dict(deform_osmo=True), 'osmotic'),
