@@ -196,7 +196,23 @@ __device__ __forceinline__ void load_rec(const float* __restrict__ rec, int c, f
 // them above 1e-24.
 __device__ __forceinline__ float rcp_fast(float x) { return __fdividef(1.f, x); }
 
-constexpr int kCellsPerCta = 32;   // cells per tile: the (ion, cell) phase maps ion -> warp, cell -> lane
+constexpr int kCellsPerCta = 32;
+
+// The two segmented sums of one cell (update_all_concs' M_sum_mems products):
+// membranes [rng.x, rng.y) of the tile, added in order.  The first eight terms
+// are predicated straight-line code (a Voronoi cell has ~6 membranes), so a
+// warp whose cells differ in size runs no loop for them.
+__device__ __forceinline__ void seg_sums(const float* __restrict__ a, const float* __restrict__ b, short2 rng,
+                                         float& s1, float& s2) {
+  float x = 0.f, y = 0.f;
+  const int j0 = rng.x, n = rng.y - rng.x;
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+    if (u < n) { x += a[j0 + u]; y += b[j0 + u]; }
+  for (int j = j0 + 8; j < rng.y; ++j) { x += a[j]; y += b[j]; }
+  s1 = x;
+  s2 = y;
+}   // cells per tile: the (ion, cell) phase maps ion -> warp, cell -> lane
 
 // Charge patterns compiled as constants.  ZP = 0: any ion set, charges read
 // at run time.  ZP = 1: BETSE's six-ion set (ion profiles 'mammal' and
@@ -386,9 +402,9 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   // ---- cells: warp = ion, lane = cell -- update_all_concs (sim.py:2086-2111)
   int bad = 0, neg = 0;
   const bool cell_live = cell_thr && rng.y > rng.x;
-  float s1 = 0.f;
+  float s1 = 0.f, s2 = 0.f;
   if (cell_thr) {
-    for (int j = rng.x; j < rng.y; ++j) s1 += sA[wid][j];
+    seg_sums(sA[wid], sB[wid], rng, s1, s2);
     // per-tile partial sum of f_mem*sa of this ion (k_split_env reduces them)
     float e = s1;
 #pragma unroll
@@ -397,8 +413,6 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
   }
   if (cell_live) {
     const int i = wid;
-    float s2 = 0.f;
-    for (int j = rng.x; j < rng.y; ++j) s2 += sB[i][j];
     df x{x2.x, x2.y};
     if (OUT) {
       const df qo = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
@@ -413,8 +427,10 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
     const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
     sQ[i][lane] = make_float2(qz.hi, qz.lo);
   }
-  const int n_bad = __syncthreads_count(bad);
-  const int n_neg = __syncthreads_count(neg);
+  // NaN and no_negs counts: rare, one atomic per affected (ion, cell)
+  if (bad) atomicAdd(&p.status[1], 1ull);
+  if (neg) atomicAdd(&p.status[2], 1ull);
+  __syncthreads();
   // ---- charge -> Vmem (update_V, sim.py:2027-2029), one lane per cell
   if (t < kCellsPerCta) {
     const short2 r0 = g.cell_rng[s0 + t];
@@ -445,10 +461,6 @@ k_split_step(SplitGeom g, SplitPtrs p, SplitConst k) {
         p.o_drho[cc] = ((double)rho.hi + (double)rho.lo) - ((double)rho_o.hi + (double)rho_o.lo);
       }
     }
-  }
-  if (t == 0) {
-    if (n_bad) atomicAdd(&p.status[1], (unsigned long long)n_bad);
-    if (n_neg) atomicAdd(&p.status[2], (unsigned long long)n_neg);
   }
 }
 
@@ -639,11 +651,11 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
     }
     __syncthreads();
     // cells: warp = ion, lane = cell (update_all_concs)
-    int bad = 0, neg = 0;
+    // one pass over the cell's membranes for both sums, each in the order of k_split_step
     const short2 rng = st.rng[lane];
-    float s1 = 0.f;
+    float s1 = 0.f, s2 = 0.f;
     if (wid < I) {
-      for (int jj = rng.x; jj < rng.y; ++jj) s1 += sm.sA[wid][jj];
+      seg_sums(sm.sA[wid], sm.sB[wid], rng, s1, s2);
       float e = s1;                  // per-tile partial sum of f_mem*sa of this ion
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
@@ -651,22 +663,19 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
     }
     if (wid < I && rng.y > rng.x) {
       const int i = wid;
-      float s2 = 0.f;
-      for (int jj = rng.x; jj < rng.y; ++jj) s2 += sm.sB[i][jj];
       const float dtv = st.dtv[lane];
       const float2 x2 = st.cc2[i][lane];
       df x{x2.x, x2.y};
       x = df_add_f(x, s1 * dtv);
       sm.sRec[lane][i] = x.hi + x.lo;
       x = df_add_f(x, s2 * dtv);
-      if (x.hi != x.hi) bad = 1;
-      if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; neg = 1; }
+      if (x.hi != x.hi) ++n_bad;
+      if (x.hi < 0.f || (x.hi == 0.f && x.lo < 0.f)) { x = df{0.f, 0.f}; ++n_neg; }
       p.cc2[(size_t)i * g.S + s0 + lane] = make_float2(x.hi, x.lo);
       const df qz = df_mul(x, k.zF_hi[i], k.zF_lo[i]);
       sm.sQ[i][lane] = make_float2(qz.hi, qz.lo);
     }
-    n_bad += __syncthreads_count(bad);
-    n_neg += __syncthreads_count(neg);
+    __syncthreads();
     if (t < kCellsPerCta) {
       const short2 r0 = st.rng[t];
       if (r0.y > r0.x) {
@@ -685,13 +694,12 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
         if (vc != vc) ++n_nan;
       }
     }
-    __syncthreads();                 // the buffers of this tile are reused two tiles on
+    // no barrier here: the buffers of this tile are refilled only after the
+    // next tile's first barrier, which every thread reaches after this tile
   }
   cp_wait_all();
-  if (t == 0) {
-    if (n_bad) atomicAdd(&p.status[1], n_bad);
-    if (n_neg) atomicAdd(&p.status[2], n_neg);
-  }
+  if (n_bad) atomicAdd(&p.status[1], n_bad);
+  if (n_neg) atomicAdd(&p.status[2], n_neg);
   if (n_nan) atomicAdd(&p.status[0], n_nan);
 }
 
