@@ -1060,6 +1060,14 @@ int bx_set_env_diffusivity(bx_handle h, const double* D_env) {
   return BX_OK;
 }
 
+// Phi_b at membrane m's grid cell.  A boundary potential needs a single
+// cluster (bx_set_boundary_potential), and a batch's membranes index their own
+// clusters' grids, which h_phib (sized by the first cluster's grid) does not
+// cover: without a potential the value is zero and h_phib is not read.
+double phib_at(const bx_cluster* h, int m) {
+  return h->phib_nonzero ? h->h_phib[h->h_map_env[m]] : 0.0;
+}
+
 int bx_set_boundary_potential(bx_handle h, const double* Phi_b) {
   if (!h) return fail(BX_EINVAL, "null handle");
   bool nz = false;
@@ -1104,9 +1112,9 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
     std::vector<float> rec((size_t)kRec * S, 0.0f);
     std::vector<float2> cc2((size_t)I * S, make_float2(0.f, 0.f));
     for (int c = 0; c < C; ++c) {
-      const double v0 = s->vm[ptr[c]] + h->h_phib[h->h_map_env[ptr[c]]];
+      const double v0 = s->vm[ptr[c]] + phib_at(h, ptr[c]);
       for (int m = ptr[c] + 1; m < ptr[c + 1]; ++m) {
-        const double v = s->vm[m] + h->h_phib[h->h_map_env[m]];
+        const double v = s->vm[m] + phib_at(h, m);
         if (std::fabs(v - v0) > 1e-12 * std::fabs(v0) + 1e-18)
           return fail(BX_EINVAL, "split form: vm must be uniform over each cell's membranes");
       }
@@ -1168,8 +1176,7 @@ int bx_state_download(bx_handle h, bx_state* s) {
     BX_CU(cudaMemcpy(cc2.data(), h->s_cc2, cc2.size() * sizeof(float2), cudaMemcpyDeviceToHost));
     if (s->vm)
       for (int m = 0; m < M; ++m)
-        s->vm[m] = (double)rec[(size_t)h->h_slot_of_cell[h->h_m2c[m]] * kRec + kRec - 1] -
-                   h->h_phib[h->h_map_env[m]];
+        s->vm[m] = (double)rec[(size_t)h->h_slot_of_cell[h->h_m2c[m]] * kRec + kRec - 1] - phib_at(h, m);
     for (int c = 0; c < C; ++c) {
       const int sc = h->h_slot_of_cell[c];
       for (int i = 0; i < I; ++i) {
