@@ -192,9 +192,36 @@ class Sweep:
                 'cc_env': np.concatenate([x['cc_env'] for x in d])}
 
 
+def _c_steppers(clusters):
+    """C restatements (oracle/c, OpenMP) of no-ECM clusters, or None when
+    the C oracle cannot be built or does not cover the configuration."""
+    try:
+        from oracle import cstep
+        from oracle.adapt import from_workload
+        return [cstep.Stepper(*from_workload(g, p, Dm, st)) for g, p, Dm, st in clusters], cstep.max_threads()
+    except Exception as e:
+        print(f'C restatement unavailable, timing the NumPy oracle: {e}', file=sys.stderr)
+        return None, 1
+
+
 def cpu_baseline(g, p, Dm, st, budget_s=12.0, D_env=None):
-    """Oracle (NumPy restatement of BETSE's step) on a bounded sample: whole
-    cluster, as many time steps as fit in about budget_s seconds."""
+    """BETSE's step restated for the CPU, on a bounded sample: the whole
+    cluster, as many time steps as fit in about budget_s seconds.  Without
+    extracellular spaces it is the C restatement on every host thread
+    (OpenMP); with them, the NumPy oracle on one thread."""
+    steppers, threads = (None, 1) if p.is_ecm else _c_steppers([(g, p, Dm, st)])
+    if steppers:
+        s0 = steppers[0]
+        t0 = time.perf_counter()
+        s0.step(1)
+        one = time.perf_counter() - t0
+        n = max(1, int(budget_s / max(one, 1e-4)) - 1)
+        t0 = time.perf_counter()
+        s0.step(n)
+        dt = time.perf_counter() - t0
+        return {'value': g.n_mems * n / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+                'sample': f'{n} time steps of the full {g.n_cells}-cell / {g.n_mems}-membrane '
+                          f'cluster ({dt:.1f} s), C restatement of the step (oracle/c), {threads} OpenMP threads'}
     import oracle
     from oracle.adapt import from_workload
     geo, par, s = from_workload(g, p, Dm, st, D_env)
@@ -209,6 +236,28 @@ def cpu_baseline(g, p, Dm, st, budget_s=12.0, D_env=None):
     return {'value': g.n_mems * n / dt, 'unit': UNIT, 'cores': 1, 'kind': 'port',
             'sample': f'{n} time steps of the full {g.n_cells}-cell / {g.n_mems}-membrane '
                       f'cluster ({dt:.1f} s), NumPy oracle, one thread'}
+
+
+def cpu_baseline_sweep(gs, ps, Dms, sts, budget_s=12.0):
+    """The sweep on the C restatement: every cluster, as many time steps as
+    fit in about budget_s seconds (each step visits all clusters in turn, each
+    on every host thread)."""
+    steppers, threads = _c_steppers(list(zip(gs, ps, Dms, sts)))
+    if not steppers:
+        return cpu_baseline(gs[0], ps[0], Dms[0], sts[0], budget_s)
+    M = sum(g.n_mems for g in gs)
+    t0 = time.perf_counter()
+    for s in steppers:
+        s.step(1)
+    one = time.perf_counter() - t0
+    n = max(1, int(budget_s / max(one, 1e-4)) - 1)
+    t0 = time.perf_counter()
+    for s in steppers:
+        s.step(n)
+    dt = time.perf_counter() - t0
+    return {'value': M * n / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'sample': f'{n} time steps of all {len(gs)} clusters ({M} membranes, {dt:.1f} s), '
+                      f'C restatement of the step (oracle/c), {threads} OpenMP threads'}
 
 
 def init_time_to_steady(n_clusters=16, n_cells=5000):
@@ -335,27 +384,33 @@ def secondary(stream, flush):
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the CPU restatement of BETSE's step on the host cores."""
+    """--impl reference: the CPU restatement of BETSE's step on the host cores
+    (the C restatement on every OpenMP thread without extracellular spaces,
+    the NumPy oracle with them); each step is a bounded sample of the
+    workload, about BX_REF_BUDGET_S seconds."""
     if rank != 0:
         return
     w, g, p, Dm, st, D_env = build_workload(args.workload)
     budget = float(os.environ.get('BX_REF_BUDGET_S', '6'))
     n_cells, n_mems = (sum(x.n_cells for x in g), sum(x.n_mems for x in g)) if w.get('sweep') \
         else (g.n_cells, g.n_mems)
-    if w.get('sweep'):      # a bounded sample of the sweep: its first cluster
-        g, p, Dm, st = g[0], p[0], Dm[0], st[0]
     samples = []
     for k in range(args.warmup + args.steps):
-        r = cpu_baseline(g, p, Dm, st, budget_s=budget, D_env=None if w.get('sweep') else D_env)
+        if w.get('sweep'):
+            r = cpu_baseline_sweep(g, p, Dm, st, budget_s=budget)
+        else:
+            r = cpu_baseline(g, p, Dm, st, budget_s=budget, D_env=D_env)
         if k >= args.warmup:
             samples.append(r['value'])
     v = statistics.mean(samples)
     line = {'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': 1e3 * g.n_mems / v,
+            # one step of the workload is time_steps time steps of it, as in our arm
+            'warmup': args.warmup, 'ms_per_step': 1e3 * n_mems * w['time_steps'] / v,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
             'data': 'synthetic', 'impl': 'reference',
-            'config': {'workload': w['desc'], 'cells': n_cells, 'membranes': n_mems},
-            'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': 1, 'kind': 'port',
+            'config': {'workload': w['desc'], 'cells': n_cells, 'membranes': n_mems,
+                       'time_steps_per_step': w['time_steps']},
+            'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': r['cores'], 'kind': 'port',
                              'sample': r['sample']},
             'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(line), flush=True)
@@ -575,8 +630,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         if sweep:
-            cpu = cpu_baseline(g[0], p[0], Dm[0], st[0])
-            cpu['sample'] += ' (cluster 0 of the sweep)'
+            cpu = cpu_baseline_sweep(g, p, Dm, st)
         else:
             cpu = cpu_baseline(g, p, Dm, st, D_env=D_env)
     extra = init_steady = None

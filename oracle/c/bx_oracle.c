@@ -1,0 +1,182 @@
+/* bx_oracle.c -- TEST INFRASTRUCTURE AND CPU BASELINE ONLY.
+ *
+ * A C restatement of BETSE's per-timestep electrodiffusion step without
+ * extracellular spaces (Simulator._run_sim_core_loop, betse/science/sim.py:
+ * 1169-1363), following the NumPy oracle (oracle/step.py) operator by
+ * operator, with OpenMP over membranes and over cells.  Only tests/ and the
+ * CPU legs of bench.py load it; the CUDA library never does.
+ *
+ * Order within one step (sim.py:1196-1363):
+ *   Na/K-ATPase on the start-of-step state (sim_toolbox.py:71-122);
+ *   per ion: GHK transmembrane flux (sim_toolbox.py:18-69, sim.py:1256-1269),
+ *     then vm += 1e-25 in place (sim_toolbox.py:54), then the gap-junction
+ *     flux from this membrane's cell into its partner's (update_gj,
+ *     sim.py:2162-2206; boundary membranes carry none);
+ *   update_all_concs (sim.py:2086-2111, sim_toolbox.py:1155-1207): the
+ *     membrane-flux segment sum per cell, the well-mixed environment mean,
+ *     the gap-junction segment sum, no_negs;
+ *   update_V (sim.py:2007-2029): rho = sum_i z_i F c_i, vm = rho diviterm / cm.
+ * Voltage-gated gap junctions and the Ca-ATPase are not restated here (the
+ * NumPy oracle covers them); callers pass configurations without them.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define BXO_MAX_IONS 8
+#define BXO_NONCE 1.0e-25
+
+typedef struct bxo_cluster {
+  int32_t C, M, I, iNa, iK;
+  int32_t pad0;
+  const int64_t* cell_ptr;   /* [C+1] membranes of cell c: [cell_ptr[c], cell_ptr[c+1]) */
+  const int64_t* m2c;        /* [M] mem_to_cells */
+  const int64_t* nn;         /* [M] nn_i: the gap-junction partner membrane */
+  const uint8_t* bflag;      /* [M] boundary membrane */
+  const double* mem_sa;      /* [M] */
+  const double* gj_w;        /* [M] gj_default_weights */
+  const double* cell_vol;    /* [C] */
+  const double* diviterm;    /* [C] */
+  const double* Dm;          /* [I][M] Dm_cells */
+  double zs[BXO_MAX_IONS];
+  double D_gj[BXO_MAX_IONS];
+  double F, R, T, dt, cm, tm, gj_surface, gj_block, gj_len, nakatp_block;
+  double alpha_NaK, KmNK_Na, KmNK_K, KmNK_ATP, cATP, cADP, cPi, deltaGATP, vol_env;
+} bxo_cluster;
+
+/* GHK flux from A (outside) into B (inside), sim_toolbox.py:18-69 */
+static inline double electroflux(double cA, double cB, double Dc, double d, double z, double vBA,
+                                 double F, double R, double T) {
+  const double v = vBA + BXO_NONCE;
+  const double zc = z + BXO_NONCE;
+  const double alpha = (zc * v * F) / (R * T);
+  const double exp_alpha = exp(-alpha);
+  const double deno = -expm1(-alpha);
+  return -((Dc * alpha) / d) * ((cB - cA * exp_alpha) / deno);
+}
+
+/* f_Na of the Na/K-ATPase, sim_toolbox.py:71-122 */
+static inline double pump_fna(const bxo_cluster* k, double cNai, double cNao, double cKi, double cKo, double Vm) {
+  const double nao = cNao * 1e-3, ki = cKi * 1e-3, nai = cNai * 1e-3, ko = cKo * 1e-3;
+  const double Qnumo = (k->cADP * 1e-3) * (k->cPi * 1e-3) * (nao * nao * nao) * (ki * ki);
+  double Qdenomo = (k->cATP * 1e-3) * (nai * nai * nai) * (ko * ko);
+  if (Qdenomo == 0.0) Qdenomo = 1.0e-15;
+  const double Q = Qnumo / Qdenomo;
+  const double Keq = exp(-(k->deltaGATP / (k->R * k->T) - ((k->F * Vm) / (k->R * k->T))));
+  const double xna = cNai / k->KmNK_Na, xk = cKo / k->KmNK_K;
+  const double numo_E = (xna * xna * xna) * (xk * xk) * (k->cATP / k->KmNK_ATP);
+  const double denomo_E = (1 + xna * xna * xna) * (1 + xk * xk) * (1 + (k->cATP / k->KmNK_ATP));
+  const double fwd_co = numo_E / denomo_E;
+  return -3 * k->nakatp_block * k->alpha_NaK * fwd_co * (1 - (Q / Keq));
+}
+
+int bxo_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* Advance n_steps.  State: vm [M], cc_cells [I][C], cc_mem [I][C] (BETSE's
+ * cc_at_mem, constant over each cell's membranes), cc_env [I] (the well-mixed
+ * environment).  threads <= 0 uses every thread OpenMP offers.  Returns 0, or
+ * 1 when a concentration or Vmem became NaN (check_v / no_negs). */
+int bxo_step_noecm(const bxo_cluster* k, double* vm, double* cc_cells, double* cc_mem, double* cc_env,
+                   int n_steps, int threads) {
+  const int C = k->C, M = k->M, I = k->I;
+  if (I <= 0 || I > BXO_MAX_IONS || C <= 0 || M <= 0) return 2;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#else
+  (void)threads;
+#endif
+  double* fmem = (double*)malloc(sizeof(double) * (size_t)I * M);
+  double* fgj = (double*)malloc(sizeof(double) * (size_t)I * M);
+  /* fixed-size blocks of membranes for the environment mean: the partial sums
+   * and their order do not depend on the thread count */
+  const int kBlk = 4096;
+  const int nblk = (M + kBlk - 1) / kBlk;
+  double* part = (double*)malloc(sizeof(double) * (size_t)I * nblk);
+  if (!fmem || !fgj || !part) { free(fmem); free(fgj); free(part); return 3; }
+  const double inv_cm = 1.0 / k->cm;
+  int bad = 0;
+  for (int step = 0; step < n_steps && !bad; ++step) {
+    /* ---- membranes: pump, GHK and gap-junction fluxes */
+#pragma omp parallel for schedule(static)
+    for (int m = 0; m < M; ++m) {
+      const int64_t c = k->m2c[m], n = k->nn[m], cn = k->m2c[n];
+      double fNa = 0.0, fK = 0.0;
+      if (k->alpha_NaK > 0.0) {
+        fNa = pump_fna(k, cc_mem[(size_t)k->iNa * C + c], cc_env[k->iNa], cc_mem[(size_t)k->iK * C + c],
+                       cc_env[k->iK], vm[m]);
+        fK = -(2.0 / 3.0) * fNa;
+      }
+      double v = vm[m], vn = vm[n];            /* in-place nonces of the reference */
+      for (int i = 0; i < I; ++i) {
+        const double cin = cc_mem[(size_t)i * C + c];
+        const double f_ED = electroflux(cc_env[i], cin, k->Dm[(size_t)i * M + m], k->tm, k->zs[i], v,
+                                        k->F, k->R, k->T);
+        double f = 0.0;
+        if (i == k->iNa) f = fNa;
+        else if (i == k->iK) f = fK;
+        fmem[(size_t)i * M + m] = f + f_ED;
+        v = v + BXO_NONCE;
+        vn = vn + BXO_NONCE;
+        const double vgj = vn - v;
+        const double gjopen = k->gj_block * k->gj_w[m];
+        double fg = electroflux(cin, cc_mem[(size_t)i * C + cn], k->D_gj[i] * k->gj_surface * gjopen,
+                                k->gj_len, k->zs[i], vgj, k->F, k->R, k->T);
+        if (k->bflag[m]) fg = 0.0;
+        fgj[(size_t)i * M + m] = 0.0 + fg;
+      }
+    }
+    /* ---- environment: mean over membranes of c_env - f sa / vol_env dt */
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < nblk; ++b) {
+      const int m0 = b * kBlk, m1 = (m0 + kBlk < M) ? m0 + kBlk : M;
+      for (int i = 0; i < I; ++i) {
+        double s = 0.0;
+        for (int m = m0; m < m1; ++m)
+          s += cc_env[i] + (-fmem[(size_t)i * M + m] * (k->mem_sa[m] / k->vol_env)) * k->dt;
+        part[(size_t)i * nblk + b] = s;
+      }
+    }
+    /* ---- cells: update_all_concs and update_V */
+#pragma omp parallel for schedule(static) reduction(|| : bad)
+    for (int c = 0; c < C; ++c) {
+      const int64_t a0 = k->cell_ptr[c], a1 = k->cell_ptr[c + 1];
+      double rho = 0.0;
+      for (int i = 0; i < I; ++i) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int64_t m = a0; m < a1; ++m) {
+          s1 += fmem[(size_t)i * M + m] * k->mem_sa[m];
+          s2 += -fgj[(size_t)i * M + m] * k->mem_sa[m];
+        }
+        double x = cc_cells[(size_t)i * C + c] + (s1 / k->cell_vol[c]) * k->dt;
+        cc_mem[(size_t)i * C + c] = x;
+        x = x + k->dt * (s2 / k->cell_vol[c]);
+        if (x != x) bad = 1;
+        if (x < 0.0) x = 0.0;
+        cc_cells[(size_t)i * C + c] = x;
+        rho += (k->zs[i] * k->F) * x;
+      }
+      const double vc = inv_cm * (rho * k->diviterm[c]);
+      if (vc != vc) bad = 1;
+      for (int64_t m = a0; m < a1; ++m) vm[m] = vc;
+    }
+    for (int i = 0; i < I; ++i) {
+      double s = 0.0;
+      for (int b = 0; b < nblk; ++b) s += part[(size_t)i * nblk + b];
+      cc_env[i] = s / (double)M;
+    }
+  }
+  free(fmem);
+  free(fgj);
+  free(part);
+  return bad;
+}

@@ -1,0 +1,144 @@
+"""ctypes wrapper of the C restatement ``oracle/c/bx_oracle.c`` -- TEST
+INFRASTRUCTURE AND CPU BASELINE ONLY.
+
+``build()`` compiles it with gcc and OpenMP into ``oracle/_build/``;
+``Stepper`` advances a no-ECM cluster given in the records ``oracle.step``
+reads (``oracle.adapt.from_workload`` or the golden fixtures), on every host
+thread OpenMP offers unless told otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, 'c', 'bx_oracle.c')
+OUT_DIR = os.path.join(HERE, '_build')
+LIB = os.path.join(OUT_DIR, 'libbx_oracle.so')
+MAX_IONS = 8
+
+# IEEE arithmetic without contraction into FMA, so x86 and Arm builds agree;
+# no -march=native (the library is rebuilt on each machine)
+CFLAGS = ['-O2', '-fopenmp', '-ffp-contract=off', '-fno-fast-math', '-fPIC', '-shared', '-std=c11']
+
+
+def build(force=False):
+    """Compile the C restatement if it is missing or older than its source."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    tmp = LIB + '.tmp'
+    subprocess.run(['gcc', *CFLAGS, '-o', tmp, SRC, '-lm'], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class _Cluster(ct.Structure):
+    _fields_ = [('C', ct.c_int32), ('M', ct.c_int32), ('I', ct.c_int32), ('iNa', ct.c_int32),
+                ('iK', ct.c_int32), ('pad0', ct.c_int32),
+                ('cell_ptr', ct.c_void_p), ('m2c', ct.c_void_p), ('nn', ct.c_void_p),
+                ('bflag', ct.c_void_p), ('mem_sa', ct.c_void_p), ('gj_w', ct.c_void_p),
+                ('cell_vol', ct.c_void_p), ('diviterm', ct.c_void_p), ('Dm', ct.c_void_p),
+                ('zs', ct.c_double * MAX_IONS), ('D_gj', ct.c_double * MAX_IONS)] + \
+        [(n, ct.c_double) for n in ('F', 'R', 'T', 'dt', 'cm', 'tm', 'gj_surface', 'gj_block', 'gj_len',
+                                    'nakatp_block', 'alpha_NaK', 'KmNK_Na', 'KmNK_K', 'KmNK_ATP', 'cATP',
+                                    'cADP', 'cPi', 'deltaGATP', 'vol_env')]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        try:
+            lib = ct.CDLL(build())
+        except OSError:         # a library built for another machine: rebuild here
+            lib = ct.CDLL(build(force=True))
+        lib.bxo_step_noecm.restype = ct.c_int
+        lib.bxo_step_noecm.argtypes = [ct.POINTER(_Cluster)] + [ct.c_void_p] * 4 + [ct.c_int, ct.c_int]
+        lib.bxo_max_threads.restype = ct.c_int
+        _lib = lib
+    return _lib
+
+
+def max_threads():
+    return int(load().bxo_max_threads())
+
+
+def _ptr(a):
+    return ct.c_void_p(a.ctypes.data)
+
+
+class Stepper:
+    """A no-ECM cluster on the C restatement.  ``g``/``p``/``s`` are the records
+    ``oracle.step`` reads (BETSE attribute names); the state is copied in and
+    ``state()`` returns it in the same shapes."""
+
+    def __init__(self, g, p, s, threads=0):
+        if bool(getattr(p, 'is_ecm', False)):
+            raise ValueError('the C restatement covers the step without extracellular spaces')
+        if bool(getattr(p, 'v_sensitive_gj', False)) or (getattr(p, 'iCa', -1) >= 0
+                                                           and float(getattr(p, 'alpha_Ca', 0.0)) > 0):
+            raise ValueError('voltage-gated gap junctions and the Ca-ATPase are not restated in C')
+        self.lib = load()
+        self.threads = int(threads)
+        m2c = np.ascontiguousarray(g.mem_to_cells, np.int64)
+        M = len(m2c)
+        C = len(g.cell_vol)
+        ptr = np.asarray(getattr(g, 'cell_mem_ptr', None) if getattr(g, 'cell_mem_ptr', None) is not None
+                         else np.concatenate([[0], np.cumsum(np.bincount(m2c, minlength=C))]), np.int64)
+        bflag = np.zeros(M, np.uint8)
+        bf = np.asarray(g.bflag)
+        if bf.dtype == bool and bf.shape == (M,):
+            bflag[:] = bf
+        else:
+            bflag[np.asarray(bf, np.int64)] = 1
+        Dm = np.ascontiguousarray(p.Dm, np.float64)
+        I = Dm.shape[0]
+        self._keep = dict(ptr=np.ascontiguousarray(ptr), m2c=m2c, nn=np.ascontiguousarray(g.nn_i, np.int64),
+                          bflag=bflag, sa=np.ascontiguousarray(g.mem_sa, np.float64),
+                          gjw=np.ascontiguousarray(getattr(g, 'gj_weight', None) if getattr(g, 'gj_weight', None)
+                                                   is not None else g.gj_default_weights, np.float64),
+                          vol=np.ascontiguousarray(g.cell_vol, np.float64),
+                          div=np.ascontiguousarray(g.diviterm, np.float64), Dm=Dm)
+        k = _Cluster()
+        k.C, k.M, k.I, k.iNa, k.iK = C, M, I, int(p.iNa), int(p.iK)
+        kp = self._keep
+        k.cell_ptr, k.m2c, k.nn, k.bflag = _ptr(kp['ptr']), _ptr(kp['m2c']), _ptr(kp['nn']), _ptr(kp['bflag'])
+        k.mem_sa, k.gj_w, k.cell_vol, k.diviterm = _ptr(kp['sa']), _ptr(kp['gjw']), _ptr(kp['vol']), _ptr(kp['div'])
+        k.Dm = _ptr(kp['Dm'])
+        for i in range(I):
+            k.zs[i] = float(p.zs[i])
+            k.D_gj[i] = float(np.ravel(p.D_gj)[i])
+        for n in ('F', 'R', 'T', 'dt', 'cm', 'tm', 'gj_surface', 'alpha_NaK', 'KmNK_Na', 'KmNK_K', 'KmNK_ATP',
+                  'cATP', 'cADP', 'cPi', 'deltaGATP', 'vol_env'):
+            setattr(k, n, float(getattr(p, n)))
+        k.gj_block = float(getattr(p, 'gj_block', 1.0))
+        k.nakatp_block = float(getattr(p, 'nakatp_block', 1.0))
+        k.gj_len = float(g.gj_len)
+        self.k = k
+        self.C, self.M, self.I = C, M, I
+        self.m2c = m2c
+        self.vm = np.ascontiguousarray(s.vm, np.float64).copy()
+        self.cc = np.ascontiguousarray(s.cc_cells, np.float64).copy()
+        cam = np.asarray(s.cc_at_mem, np.float64)
+        first = kp['ptr'][:-1]
+        self.ccm = np.ascontiguousarray(cam[:, first])
+        ce = np.asarray(s.cc_env, np.float64)
+        self.cenv = np.ascontiguousarray(ce[:, 0] if ce.ndim == 2 else ce).copy()
+
+    def step(self, n=1):
+        rc = self.lib.bxo_step_noecm(ct.byref(self.k), _ptr(self.vm), _ptr(self.cc), _ptr(self.ccm),
+                                     _ptr(self.cenv), int(n), self.threads)
+        if rc == 1:
+            raise FloatingPointError('NaN concentration or Vmem (check_v / no_negs)')
+        if rc != 0:
+            raise RuntimeError(f'bxo_step_noecm failed ({rc})')
+
+    def state(self):
+        return dict(vm=self.vm.copy(), cc_cells=self.cc.copy(), cc_at_mem=self.ccm[:, self.m2c].copy(),
+                    cc_env=np.repeat(self.cenv[:, None], self.M, axis=1))

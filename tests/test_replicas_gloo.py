@@ -33,7 +33,7 @@ def _rank(rank, world, port, out):
 
 def test_two_replicas_take_the_slowest_rank():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context('spawn').Manager() as m:   # no fork of a multi-threaded parent
         out = m.dict()
         mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)
