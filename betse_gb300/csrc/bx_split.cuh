@@ -499,6 +499,8 @@ struct PersistSmem {
     float gw[TPB];
     int nn[TPB];
     uint8_t lcell[TPB];
+    int cl;                          // the tile's cluster
+    int pad[3];
   };
   struct State {                     // one tile's state
     float own[kCellsPerCta][8];
@@ -507,9 +509,13 @@ struct PersistSmem {
     short2 rng[kCellsPerCta];
     float dtv[kCellsPerCta];
     float dvc[kCellsPerCta];
-    int cl;
+    float cenv[kMaxIons];            // the cluster's environment (written by the previous step)
+    float pump;                      // and its pump coefficient
     int pad[3];
   };
+  // 16-byte copies land at 16-byte multiples of the (16-byte aligned) base
+  static_assert(sizeof(Geo) % 16 == 0 && sizeof(State) % 16 == 0, "16-byte staging blocks");
+  static_assert(NI <= kMaxIons, "ion rows");
   Geo geo[3];
   State st[2];
   float sA[NI][TPB];
@@ -546,6 +552,7 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
     cp_block<TPB>(ge.gw, g.gjw + q0, TPB * 4);
     cp_block<TPB>(ge.nn, g.nn_slot + q0, TPB * 4);
     cp_block<TPB>(ge.lcell, g.lcell + q0, TPB);
+    if (t == 0) cp4(&ge.cl, g.blk_cluster + tile);
   };
   auto issue_state = [&](int tile, int sbuf, int gbuf) {
     if (tile >= ntile) return;
@@ -559,7 +566,10 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
     cp_block<TPB>(st.rng, g.cell_rng + s0, kCellsPerCta * 4);
     cp_block<TPB>(st.dtv, g.dtv + s0, kCellsPerCta * 4);
     cp_block<TPB>(st.dvc, g.dvc + s0, kCellsPerCta * 4);
-    if (t == 0) cp4(&st.cl, g.blk_cluster + tile);
+    // the cluster's environment and pump rate: the cluster index came with the
+    // geometry, so these loads do not wait on another load in the tile's compute
+    if (t < I) cp4(&st.cenv[t], p.cenv_f + (size_t)ge.cl * I + t);
+    else if (t == I) cp4(&st.pump, p.pump_coef + ge.cl);
     if (ge.lcell[t] != 255) {         // partner record of this slot
       const float* src = p.rec_in + (size_t)ge.nn[t] * REC;
       cp16(&st.nbr[t][0], src);
@@ -593,18 +603,16 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
     const typename SM::Geo& ge = sm.geo[gb];
     const typename SM::State& st = sm.st[sb];
     const int s0 = tile * kCellsPerCta;
-    const int cl = st.cl;
     const int lc = ge.lcell[t];
     const bool active = lc != 255;
     if (active) {
       float own[REC], nbr[REC];
 #pragma unroll
       for (int r = 0; r < REC; ++r) { own[r] = st.own[lc][r]; nbr[r] = st.nbr[t][r]; }
-      const float* ce = p.cenv_f + (size_t)cl * I;
       float cenv[NI];
 #pragma unroll
-      for (int i = 0; i < NI; ++i) cenv[i] = (i < I) ? ce[i] : 0.f;
-      const float pc = p.pump_coef[cl];
+      for (int i = 0; i < NI; ++i) cenv[i] = (i < I) ? st.cenv[i] : 0.f;
+      const float pc = st.pump;
       const float v = own[REC - 1];
       const float vn = nbr[REC - 1];
       const float v1 = v + 1.0e-25f;
