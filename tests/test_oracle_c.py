@@ -67,3 +67,19 @@ def test_c_restatement_refuses_what_it_does_not_cover(cstep):
     d = gi.load('ecm_r50_s3')
     with pytest.raises(ValueError, match='extracellular'):
         cstep.Stepper(gi.geometry(d), gi.params(d), gi.state(d))
+
+
+def test_c_restatement_on_ragged_cells(cstep):
+    """Cells of 1 to 20 membranes and random partners (tests/synthetic.py)."""
+    import oracle
+    import synthetic
+    d = synthetic.ragged_fixture()
+    g, p, s = gi.geometry(d), gi.params(d), gi.state(d)
+    st = cstep.Stepper(g, p, s)
+    st.step(30)
+    oracle.run(g, p, s, 30)
+    got = st.state()
+    for k in ('cc_cells', 'cc_at_mem', 'cc_env'):
+        assert gi.rel_err(got[k], getattr(s, k)) < 1e-12, k
+    ok, err, bound = gi.vm_err_ok(d, got['vm'], s.vm, s.cc_cells, rel=1e-12)
+    assert ok, (err, bound)
