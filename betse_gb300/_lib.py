@@ -40,7 +40,7 @@ class BxGeom(ct.Structure):
                 ('smooth_weight_mem', _dp), ('smooth_weight_o', _dp),
                 ('cell_vol', _dp), ('cell_sa', _dp), ('diviterm', _dp),
                 ('mem_sa_per_env', _dp), ('gj_len', ct.c_double),
-                ('delta', ct.c_double)]
+                ('delta', ct.c_double), ('R_rads', _dp)]
 
 
 class BxParams(ct.Structure):
@@ -56,7 +56,7 @@ class BxParams(ct.Structure):
          ('D_gj', ct.c_double * MAX_IONS), ('c_env_bound', ct.c_double * MAX_IONS),
          ('v_sensitive_gj', ct.c_int32), ('iCa', ct.c_int32), ('gj_vthresh', ct.c_double),
          ('gj_min', ct.c_double), ('alpha_Ca', ct.c_double), ('KmCa_Ca', ct.c_double),
-         ('KmCa_ATP', ct.c_double)]
+         ('KmCa_ATP', ct.c_double), ('cell_polarizability', ct.c_double)]
 
 
 class BxState(ct.Structure):

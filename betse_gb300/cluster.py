@@ -50,6 +50,7 @@ class ClusterGeometry:
     D_env_weight: np.ndarray | None = None     # f64 [G]
     cell_nn_ptr: np.ndarray | None = None      # cell adjacency CSR (warm start)
     cell_nn: np.ndarray | None = None
+    R_rads: np.ndarray | None = None           # f64 [M] membrane distance from the cell centre
     extra: dict = field(default_factory=dict)
 
     @property
@@ -70,7 +71,7 @@ class ClusterGeometry:
                     mem_nx, mem_ny, gj_weight, cell_vol, cell_sa, diviterm, grid_shape,
                     delta, gj_len, smooth_cells=2.0, smooth_weight_mem=None,
                     smooth_weight_o=None, mem_sa_per_env=None, D_env_weight=None,
-                    cell_nn_ptr=None, cell_nn=None):
+                    cell_nn_ptr=None, cell_nn=None, R_rads=None):
         m2c = np.asarray(mem_to_cells)
         C = len(cell_vol)
         M = len(m2c)
@@ -105,7 +106,8 @@ class ClusterGeometry:
                    mem_sa_per_env=None if mem_sa_per_env is None else _f64(mem_sa_per_env),
                    D_env_weight=None if D_env_weight is None else _f64(np.ravel(D_env_weight)),
                    cell_nn_ptr=None if cell_nn_ptr is None else _i32(cell_nn_ptr),
-                   cell_nn=None if cell_nn is None else _i32(cell_nn))
+                   cell_nn=None if cell_nn is None else _i32(cell_nn),
+                   R_rads=None if R_rads is None else _f64(R_rads))
 
     @classmethod
     def from_cells(cls, cells, sim=None, p=None):
@@ -132,7 +134,8 @@ class ClusterGeometry:
             delta=cells.delta, gj_len=cells.gj_len, smooth_cells=smooth,
             smooth_weight_mem=swm, smooth_weight_o=swo,
             mem_sa_per_env=getattr(cells, 'memSa_per_envSquare', None),
-            D_env_weight=dw, cell_nn_ptr=cnn_ptr, cell_nn=cnn_flat)
+            D_env_weight=dw, cell_nn_ptr=cnn_ptr, cell_nn=cnn_flat,
+            R_rads=getattr(cells, 'R_rads', None))
 
     def to_c(self):
         """A ``bx_geom`` whose pointers stay valid while ``self`` lives."""
@@ -148,6 +151,7 @@ class ClusterGeometry:
             setattr(g, n, _lib.dptr(getattr(self, n)))
         g.mem_sa_per_env = _lib.dptr(self.mem_sa_per_env) if self.mem_sa_per_env is not None else None
         g.gj_len, g.delta = self.gj_len, self.delta
+        g.R_rads = _lib.dptr(self.R_rads) if self.R_rads is not None else None
         return g
 
 
@@ -205,6 +209,7 @@ class StepParams:
     alpha_Ca: float = 0.0
     KmCa_Ca: float = 1.0e-3
     KmCa_ATP: float = 0.5
+    cell_polarizability: float = 0.0  # != 0: update_V's implicit per-membrane Vmem (plain form)
 
     @property
     def n_ions(self) -> int:
@@ -231,6 +236,8 @@ class StepParams:
             D_gj = D_gj[:, 0]
         if bool(getattr(p, 'v_sensitive_gj', False)):
             kw.update(v_sensitive_gj=True, gj_vthresh=float(p.gj_vthresh), gj_min=float(p.gj_min))
+        if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
+            kw.update(cell_polarizability=float(p.cell_polarizability))
         ions = getattr(p, 'ions_dict', {}) or {}
         if ions.get('Ca', 0) == 1 and hasattr(sim, 'iCa'):
             # ca_handler runs for the Ca ion (sim.py:1282-1283)
@@ -266,6 +273,7 @@ class StepParams:
             raise ValueError('iCa must be -1 or an ion row')
         c.iCa = int(self.iCa)
         c.alpha_Ca, c.KmCa_Ca, c.KmCa_ATP = float(self.alpha_Ca), float(self.KmCa_Ca), float(self.KmCa_ATP)
+        c.cell_polarizability = float(self.cell_polarizability)
         return c
 
     def replace(self, **kw):

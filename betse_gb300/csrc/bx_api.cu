@@ -77,6 +77,8 @@ struct bx_cluster {
   int sm_count = 0;
   bool ecm = false;
   bool ca = false;                 // Ca-ATPase on (iCa >= 0 and alpha_Ca > 0)
+  bool polar = false;              // cell polarizability: per-membrane Vmem (plain form)
+  double* d_Rrads = nullptr;       // [M] membrane distance from the cell centre
   double* d_cnew = nullptr;        // [I][G] ECM with the Ca-ATPase: environment after the
                                    // Nernst-Planck update and smoothing, before the membrane scatter
   bool vgj = false;                // voltage-gated gap junctions: the open fraction is state
@@ -175,7 +177,7 @@ void free_all(bx_cluster* h) {
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
-      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo, h->d_cnew};
+      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo, h->d_cnew, h->d_Rrads};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& fs : h->fshapes)
@@ -228,6 +230,9 @@ bx::StepConst make_step_const(const bx_cluster* h) {
   k.gj_min = p.gj_min;
   k.gj_dt_ms = p.dt * 1e3;
   k.iCa = h->ca ? p.iCa : -1;
+  k.polar = h->polar ? 1 : 0;
+  k.cm = p.cm;
+  k.true_ratio = p.true_cell_size / p.cell_radius;
   k.ca_alpha = p.alpha_Ca;
   k.ca_inv_Km = 1.0 / p.KmCa_Ca;
   k.ca_atp_term = p.cATP / p.KmCa_ATP;
@@ -321,6 +326,7 @@ bx::DevGeom dev_geom(const bx_cluster* h) {
   g.gj_w = h->d_gj_w; g.gj_w_f = h->d_gj_w_f; g.mem_nx = h->d_nx; g.mem_ny = h->d_ny;
   g.sw_mem = h->d_swm; g.sw_o = h->d_swo; g.cell_vol = h->d_cell_vol; g.cell_sa = h->d_cell_sa;
   g.diviterm = h->d_diviterm; g.blk_cell = h->d_blk; g.blk_cluster = h->d_blk_cl;
+  g.R_rads = h->d_Rrads;
   return g;
 }
 
@@ -621,6 +627,7 @@ bool same_shared_params(const bx_params& a, const bx_params& b) {
   if (a.n_ions != b.n_ions || a.iNa != b.iNa || a.iK != b.iK || a.is_ecm != b.is_ecm) return false;
   if (a.v_sensitive_gj != b.v_sensitive_gj || a.gj_vthresh != b.gj_vthresh || a.gj_min != b.gj_min) return false;
   if (a.iCa != b.iCa || a.alpha_Ca != b.alpha_Ca || a.KmCa_Ca != b.KmCa_Ca || a.KmCa_ATP != b.KmCa_ATP) return false;
+  if (a.cell_polarizability != b.cell_polarizability) return false;
   const double sa[] = {a.F, a.R, a.T, a.dt, a.cm, a.tm, a.gj_surface, a.gj_block, a.KmNK_Na, a.KmNK_K,
                        a.KmNK_ATP, a.cATP, a.cADP, a.cPi, a.deltaGATP};
   const double sb[] = {b.F, b.R, b.T, b.dt, b.cm, b.tm, b.gj_surface, b.gj_block, b.KmNK_Na, b.KmNK_K,
@@ -809,6 +816,16 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   if (p0.iNa < 0 || p0.iNa >= I || p0.iK < 0 || p0.iK >= I || p0.iNa == p0.iK)
     return fail(BX_EINVAL, "iNa/iK out of range");
   if (p0.iCa < -1 || p0.iCa >= I) return fail(BX_EINVAL, "iCa must be -1 or an ion row");
+  if (p0.cell_polarizability != 0.0) {
+    if (precision != BX_PLAIN_FP64)
+      return fail(BX_EINVAL, "cell polarizability makes Vmem per-membrane state: the split form keeps one "
+                             "Vmem per cell, use BX_PLAIN_FP64");
+    for (int c = 0; c < ncl; ++c) {
+      if (!gs[c].R_rads) return fail(BX_EINVAL, "cell polarizability needs bx_geom.R_rads");
+      for (int m = 0; m < gs[c].n_mems; ++m)
+        if (!(gs[c].R_rads[m] > 0.0)) return fail(BX_EINVAL, "R_rads must be positive");
+    }
+  }
   if (ncl > 1 && p0.is_ecm) return fail(BX_EINVAL, "batches of clusters need is_ecm == 0");
   long long Ctot = 0, Mtot = 0;
   for (int c = 0; c < ncl; ++c) {
@@ -839,6 +856,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   }
   h->precision = precision; h->par = p0; h->ecm = p0.is_ecm != 0; h->vgj = p0.v_sensitive_gj != 0;
   h->ca = ca_pump_on(p0);
+  h->polar = p0.cell_polarizability != 0.0;
   h->cl_par.assign(ps, ps + ncl);
   h->mode = (precision == BX_PLAIN_FP64) ? MODE_PLAIN : MODE_SPLIT;
   if (h->mode == MODE_SPLIT && I > kRec - 1) {
@@ -851,7 +869,8 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   // ---- concatenate the clusters
   std::vector<int> ptr(C + 1), nn(M), m2c(M), nn_cell(M), map_env(M);
   std::vector<uint8_t> bflag(M);
-  std::vector<double> msa(M), mnx(M), mny(M), gjw(M), swm(M), swo(M), vol(C), csa(C), div(C);
+  std::vector<double> msa(M), mnx(M), mny(M), gjw(M), swm(M), swo(M), vol(C), csa(C), div(C),
+      rr(h->polar ? M : 0);
   h->cl_cell.assign(ncl + 1, 0); h->cl_mem.assign(ncl + 1, 0);
   int coff = 0, moff = 0;
   ptr[0] = 0;
@@ -868,6 +887,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
       map_env[moff + m] = g.map_mem2ecm[m];
       msa[moff + m] = g.mem_sa[m]; mnx[moff + m] = g.mem_nx[m]; mny[moff + m] = g.mem_ny[m];
       gjw[moff + m] = g.gj_weight[m]; swm[moff + m] = g.smooth_weight_mem[m]; swo[moff + m] = g.smooth_weight_o[m];
+      if (h->polar) rr[moff + m] = g.R_rads[m];
     }
     coff += g.n_cells;
     moff += g.n_mems;
@@ -918,6 +938,7 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   ALLOC(h->d_cell_vol, C); H2D(h->d_cell_vol, vol.data(), C);
   ALLOC(h->d_cell_sa, C); H2D(h->d_cell_sa, csa.data(), C);
   ALLOC(h->d_diviterm, C); H2D(h->d_diviterm, div.data(), C);
+  if (h->polar) { ALLOC(h->d_Rrads, M); H2D(h->d_Rrads, rr.data(), M); }
   ALLOC(h->d_pump, ncl); ALLOC(h->d_env_scale, ncl);
   ALLOC(h->d_phib, G);
   ALLOC(h->d_status, 4);
@@ -1008,6 +1029,8 @@ int bx_set_params(bx_handle h, const bx_params* p) {
   if (p->iCa < -1 || p->iCa >= p->n_ions) return fail(BX_EINVAL, "iCa must be -1 or an ion row");
   if (ca_pump_on(*p) != h->ca || (h->ca && p->iCa != h->par.iCa))
     return fail(BX_EINVAL, "the Ca-ATPase cannot be switched on or off, or move row, after create");
+  if ((p->cell_polarizability != 0.0) != h->polar)
+    return fail(BX_EINVAL, "cell polarizability cannot be switched on or off after create");
   if (h->ncl > 1) return fail(BX_EINVAL, "use bx_batch_set_params for a batch");
   h->par = *p;
   h->cl_par[0] = *p;
@@ -1020,8 +1043,9 @@ int bx_batch_set_params(bx_handle h, const bx_params* p) {
   for (int c = 0; c < h->ncl; ++c)
     if (!same_shared_params(p[0], p[c]) || p[c].n_ions != h->I || (p[c].is_ecm != 0) != h->ecm)
       return fail(BX_EINVAL, "clusters of a batch may differ only in alpha_NaK, nakatp_block, vol_env");
-  if ((p[0].v_sensitive_gj != 0) != h->vgj || ca_pump_on(p[0]) != h->ca || (h->ca && p[0].iCa != h->par.iCa))
-    return fail(BX_EINVAL, "v_sensitive_gj and the Ca-ATPase cannot change after create");
+  if ((p[0].v_sensitive_gj != 0) != h->vgj || ca_pump_on(p[0]) != h->ca || (h->ca && p[0].iCa != h->par.iCa) ||
+      (p[0].cell_polarizability != 0.0) != h->polar)
+    return fail(BX_EINVAL, "v_sensitive_gj, the Ca-ATPase and cell polarizability cannot change after create");
   h->par = p[0];
   h->cl_par.assign(p, p + h->ncl);
   h->graph_valid = false;
@@ -1371,8 +1395,9 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
   const int64_t w = 8;  // Dm, mem_sa, gj_w width
   // membrane: Dm, vm in+out, m2c, nn, nn_cell, bflag, mem_sa, gj_w (+ map_env and the f*sa
   // export with ECM); cell: cc in+out, cc_mem in+out, cell_vol, diviterm, ptr
+  // polarizability: R_rads and the two smoothing weights, 24 per membrane
   const int64_t mem = I * w + 16 + 12 + 1 + 2 * w + (h->ecm ? 4 + I * 8 : 0) + (h->vgj ? 16 : 0) +
-                      (h->ca && h->ecm ? 8 : 0);
+                      (h->ca && h->ecm ? 8 : 0) + (h->polar ? 24 : 0);
   const int64_t cell = 4 * I * 8 + 16 + 4;
   return M * mem + C * cell + (h->ecm ? 0 : B * I * 8);
 }

@@ -45,6 +45,7 @@ struct DevGeom {
   const double* diviterm; // [C]
   const int* blk_cell;    // [nblk+1]
   const int* blk_cluster; // [nblk] cluster of each CTA (batched sweeps)
+  const double* R_rads;   // [M] membrane distance from the cell centre (cell polarizability)
 };
 
 // Per-step constants (kernel parameter, passed by value).
@@ -72,6 +73,9 @@ struct StepConst {
   double ca_atp_den;       // 1 + cATP/KmCa_ATP
   double ca_qnum_c;        // cADP*cPi
   double ca_qden_c;        // cATP
+  int polar;               // cell polarizability != 0: the implicit Vmem update of update_V
+  double cm;               // membrane capacitance
+  double true_ratio;       // true_cell_size / cell_radius
 };
 
 // Harris et al. (1983) gap-junction gating constants (channels/gap_junction.py:26-31)
@@ -207,7 +211,7 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
   double* sA = smem;                    // [I][TPB] f_mem*sa
   double* sB = sA + I * TPB;            // [I][TPB] -f_gj*sa
   double* sV = sB + I * TPB;            // [TPB]   per-cell Vmem (by local cell)
-  double* sX = sV + TPB;                // [4][TPB] output scratch
+  double* sX = sV + TPB;                // [4][TPB] output scratch; [7][TPB] with polarizability
 
   const int b = blockIdx.x;
   const int c0 = g.blk_cell[b], c1 = g.blk_cell[b + 1];
@@ -225,6 +229,7 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
   for (int i = 0; i < kMaxIons; ++i) env_acc[i] = 0.0;
 
   double v = 0.0, vgj = 0.0;
+  double Jraw_p = 0.0;                    // polarizability: -sum z F f_mem + sum z F f_gj
   int c = 0, lc = 0;
   T fmem_o[kMaxIons], fgj_o[kMaxIons];
   T rate_o = (T)0;
@@ -267,6 +272,7 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
     // |vgj| in mV; one implicit-Euler update per ion, as update_gj calls it
     // once per ion (sim.py:2181-2183), each before that ion's flux
     double gg = 0.0, ga = 0.0, gr = 0.0;
+    double jm = 0.0, jg = 0.0;
     if (k.vgj) {
       const double V1 = 1.0e3 * fabs(vgj);
       const double al = kGjLambda * exp(-kGjA1 * (V1 - k.gj_vth));
@@ -309,11 +315,17 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       if (ECM) p.mem_flux_sa[(size_t)i * g.M + m] = a;
       else env_acc[i] = a;
       if (OUT) { fmem_o[i] = f; fgj_o[i] = fg; }
+      if (k.polar) { jm += k.zF[i] * (double)f; jg += k.zF[i] * (double)fg; }
     }
     if (k.vgj) p.gjo[m] = gg;
+    if (k.polar) {
+      Jraw_p = -jm + jg;                       // Jmem + Jgj (ion_current.py:22-28)
+      sX[t] = Jraw_p * g.mem_sa[m];
+    }
     (void)msa;
   } else {
     for (int i = 0; i < I; ++i) { sA[i * TPB + t] = 0.0; sB[i * TPB + t] = 0.0; }
+    if (k.polar) sX[t] = 0.0;
   }
 
   // no-ECM well-mixed environment: per-CTA partial sums of f_mem*sa per ion
@@ -352,11 +364,18 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       if (x < 0.0) { x = 0.0; neg++; }                        // no_negs
       p.cc[i * g.C + cc] = x;
       rho += k.zF[i] * x;                                     // rho_cells, ion_current.py:19
-      if (OUT) sig += k.sig_coef[i] * x;
+      if (OUT || k.polar) sig += k.sig_coef[i] * x;
     }
     const double vcell = k.inv_cm * (rho * g.diviterm[cc]);   // sim.py:2027-2029
     sV[t] = vcell;
     if (OUT) { p.o_rho[cc] = rho; p.o_sigma[cc] = sig / (double)I; }
+    if (k.polar) {
+      // Jn averaged over the cell (ion_current.py:31), sigma_cell (sim.py:2016-2017)
+      double sj = 0.0;
+      for (int j = a0; j < a1; ++j) sj += sX[j];
+      sX[TPB + t] = sj / g.cell_sa[cc];
+      sX[2 * TPB + t] = sig / (double)I;
+    }
   }
   if (bad_conc) atomicAdd(&p.status[1], (unsigned long long)bad_conc);
   if (neg) atomicAdd(&p.status[2], (unsigned long long)neg);
@@ -365,13 +384,28 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
   // ---- membrane phase 2: new Vmem
   double vnew = 0.0;
   if (active) {
-    vnew = sV[lc];
-    if (PHIB) vnew -= p.phib[g.map_env[m]];
+    if (k.polar) {
+      // implicit polarizable form (sim.py:2048-2058): the smoothed Jn
+      // (ion_current.py:33) charges the membrane while the cytoplasm relaxes
+      // it towards the cell's charge potential; self.vm carries the I
+      // in-place nonces of the ion loop
+      const double Jn = g.sw_mem[m] * Jraw_p + sX[TPB + lc] * g.sw_o[m];
+      const double sg = sX[2 * TPB + lc];
+      double vold = v;
+      for (int i = 0; i < I; ++i) vold += kNonce;
+      const double R = g.R_rads[m];
+      vnew = (vold - (k.dt / k.cm) * Jn + ((k.dt * sg * sV[lc]) / (k.cm * R))) /
+             (1 + ((k.dt * sg) / (k.cm * R)));
+    } else {
+      vnew = sV[lc];
+      if (PHIB) vnew -= p.phib[g.map_env[m]];
+    }
     p.vm_out[m] = vnew;
     if (vnew != vnew) atomicAdd(&p.status[0], 1ull);
   }
 
   if constexpr (OUT) {
+    if (k.polar) __syncthreads();      // phase 2 read the scratch rows the outputs reuse
     // fluxes, rate, Jn smoothing and cell currents (ion_current.py:19-47, sim.py:2031-2083)
     double Jraw = 0.0;
     if (active) {
@@ -398,6 +432,7 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       for (int j = a0; j < a1; ++j) { s += sX[j]; sv += sX[TPB + j]; }
       sV[t] = s / g.cell_sa[cc];              // Jn_ave
       p.o_vmave[cc] = sv / (double)(a1 - a0);
+      if (k.polar) sX[4 * TPB + t] = sv / (double)(a1 - a0);
     }
     __syncthreads();
     double Jn = 0.0;
@@ -410,7 +445,16 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       double vmo = v;
       for (int i = 0; i < I; ++i) vmo += kNonce;
       p.o_dvm[m] = (vnew - vmo) / k.dt;
-    } else { sX[2 * TPB + t] = 0.0; sX[3 * TPB + t] = 0.0; }
+      if (k.polar) {
+        // cell field from the membrane voltage profile (sim.py:2063-2074)
+        const double gE = (vnew - sX[4 * TPB + lc]) / (g.R_rads[m] * k.true_ratio);
+        sX[5 * TPB + t] = (-gE * g.mem_nx[m]) * g.mem_sa[m];
+        sX[6 * TPB + t] = (-gE * g.mem_ny[m]) * g.mem_sa[m];
+      }
+    } else {
+      sX[2 * TPB + t] = 0.0; sX[3 * TPB + t] = 0.0;
+      if (k.polar) { sX[5 * TPB + t] = 0.0; sX[6 * TPB + t] = 0.0; }
+    }
     __syncthreads();
     if (t < ncell) {
       const int cc = c0 + t;
@@ -420,8 +464,15 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
       const double jx = sx / g.cell_sa[cc], jy = sy / g.cell_sa[cc];
       p.o_Jcx[cc] = jx; p.o_Jcy[cc] = jy;
       const double sg = p.o_sigma[cc];
-      p.o_Ecx[cc] = jx / sg; p.o_Ecy[cc] = jy / sg;
-      sA[t] = jx; sA[TPB + t] = jy; sB[t] = jx / sg; sB[TPB + t] = jy / sg;
+      double ex = jx / sg, ey = jy / sg;
+      if (k.polar) {
+        double gx = 0.0, gy = 0.0;
+        for (int j = a0; j < a1; ++j) { gx += sX[5 * TPB + j]; gy += sX[6 * TPB + j]; }
+        ex = gx / g.cell_sa[cc];
+        ey = gy / g.cell_sa[cc];
+      }
+      p.o_Ecx[cc] = ex; p.o_Ecy[cc] = ey;
+      sA[t] = jx; sA[TPB + t] = jy; sB[t] = ex; sB[TPB + t] = ey;
     }
     __syncthreads();
     if (active) {

@@ -6,8 +6,11 @@
 
 namespace bx {
 
-inline size_t cell_step_smem(int I, int tpb, bool out) {
-  return sizeof(double) * (size_t)tpb * (2 * (size_t)I + 1 + (out ? 4 : 0));
+// per-ion flux rows, the cell Vmem row, and scratch rows: four for outputs,
+// seven for outputs with polarizability (at most 48 KB: 8 ions, 256 threads)
+inline size_t cell_step_smem(int I, int tpb, bool out, bool polar) {
+  const size_t scratch = polar ? (out ? 7 : 4) : (out ? 4 : 0);
+  return sizeof(double) * (size_t)tpb * (2 * (size_t)I + 1 + scratch);
 }
 
 template <typename T, int TPB>
@@ -18,7 +21,7 @@ cudaError_t launch_cell_step(bool ecm, bool out, bool phib, int nblk, cudaStream
   template <>                                                                                   \
   cudaError_t launch_cell_step<T, TPB>(bool ecm, bool out, bool phib, int nblk, cudaStream_t s, \
                                        const DevGeom& g, const StepPtrs& p, const StepConst& k) { \
-    const size_t sm = cell_step_smem(k.I, TPB, out);                                            \
+    const size_t sm = cell_step_smem(k.I, TPB, out, k.polar != 0);                                            \
     const int code = (ecm ? 4 : 0) | (out ? 2 : 0) | (phib ? 1 : 0);                            \
     switch (code) {                                                                             \
       case 0: k_cell_step<T, TPB, false, false, false><<<nblk, TPB, sm, s>>>(g, p, k); break;  \

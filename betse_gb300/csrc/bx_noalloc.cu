@@ -150,6 +150,8 @@ extern "C" int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const 
     return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs v_sensitive_gj == 0 (the open fraction is state)");
   if (p->iCa >= 0 && p->alpha_Ca > 0.0)
     return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs the Ca-ATPase off (alpha_Ca == 0 or iCa == -1)");
+  if (p->cell_polarizability != 0.0)
+    return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: needs cell_polarizability == 0");
   if (!g->cell_mem_ptr || !g->nn_i || !g->bflag || !g->map_mem2ecm || !g->mem_sa || !g->gj_weight ||
       !g->cell_vol || !g->diviterm)
     return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: missing geometry array");

@@ -15,8 +15,8 @@ hold the last step, so ``run_sim_core``'s pickling and the plotting pipeline
 see what the reference would leave.
 
 Features of the reference loop outside the electrodiffusion step (endoplasmic
-reticulum calcium dynamics, molecules/GRN networks, pressures, flow, deformation, polarizability,
-scheduled events of the SIM phase, dynamic protein
+reticulum calcium dynamics, molecules/GRN networks, pressures, flow, deformation, polarizability in the
+split form, scheduled events of the SIM phase, dynamic protein
 noise) are refused with ``NotImplementedError`` naming them, before any work.
 
 ``install()`` patches the method on BETSE's ``Simulator`` class.
@@ -31,10 +31,11 @@ from .cluster import ClusterGeometry, StepParams
 from .engine import ClusterEngine
 
 
-def unsupported_features(sim, phase, assume_no_events=False):
+def unsupported_features(sim, phase, assume_no_events=False, precision='fp64'):
     """Reasons the GPU loop cannot stand in for the reference loop here
     (empty when it can).  Each names the option of ``phase.p`` that enables a
-    branch of ``sim.py:1169-1363`` this step does not compute."""
+    branch of ``sim.py:1169-1363`` this step does not compute (with
+    ``precision``, the form that would run)."""
     p = phase.p
     reasons = []
     ions = getattr(p, 'ions_dict', {}) or {}
@@ -47,8 +48,9 @@ def unsupported_features(sim, phase, assume_no_events=False):
                        ('deformation', 'deformation')):
         if bool(getattr(p, flag, False)):
             reasons.append(f'{what} ({flag})')
-    if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
-        reasons.append('cell polarizability (sim.py:2048-2080)')
+    if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0 and precision != 'fp64':
+        reasons.append('cell polarizability in the split form (sim.py:2048-2080 makes Vmem per-membrane '
+                       'state; the plain form, precision="fp64", computes it)')
     if not bool(getattr(p, 'cluster_open', True)):
         reasons.append('closed cluster boundary (cluster_open False)')
     kind = getattr(getattr(phase, 'kind', None), 'name', str(getattr(phase, 'kind', '')))
@@ -110,7 +112,7 @@ def run_sim_core_loop(sim, phase, time_steps, time_steps_sampled, anim_cells=Non
     launch_config: (threads per CTA, persistent) to pin, or 'auto' to time
     the candidates once before stepping.
     """
-    reasons = unsupported_features(sim, phase, assume_no_events)
+    reasons = unsupported_features(sim, phase, assume_no_events, precision)
     if reasons:
         raise NotImplementedError('the GPU step does not cover: ' + '; '.join(reasons))
     p, cells = phase.p, phase.cells

@@ -98,6 +98,8 @@ typedef struct bx_geom {
     const double* mem_sa_per_env; /* [grid] cells.memSa_per_envSquare (ECM only; may be NULL) */
     double gj_len;               /* cells.gj_len (= p.cell_space) */
     double delta;                /* environment grid spacing (cells.delta) */
+    const double* R_rads;        /* [n_mems] membrane distance from the cell centre (cells.R_rads,
+                                    cells.py:1173); read only with cell_polarizability, else may be NULL */
 } bx_geom;
 
 /* Scalar parameters and per-ion constants (Parameters + Simulator fields). */
@@ -127,6 +129,10 @@ typedef struct bx_params {
     double gj_vthresh;           /* mV at which junctions are half closed */
     double gj_min;               /* open fraction of a closed junction */
     double alpha_Ca, KmCa_Ca, KmCa_ATP;
+    /* p.cell_polarizability != 0 selects update_V's implicit membrane-voltage
+     * form (sim.py:2048-2080): Vmem becomes per-membrane state (plain FP64
+     * form only; needs bx_geom.R_rads) */
+    double cell_polarizability;
 } bx_params;
 
 /* Host views of the evolving state, BETSE layouts (row = ion).

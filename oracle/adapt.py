@@ -30,6 +30,8 @@ def from_workload(g, p, Dm, st, D_env=None):
     geo.nn_i = np.asarray(g.nn_i, np.int64)
     geo.map_mem2ecm = np.asarray(g.map_mem2ecm, np.int64)
     geo.sigma = float(p.sigma)
+    if getattr(g, 'R_rads', None) is not None:
+        geo.R_rads = np.asarray(g.R_rads, np.float64)
     geo.ko_env = float(p.ko_env)
     if g.D_env_weight is not None:
         geo.D_env_weight = np.asarray(g.D_env_weight)

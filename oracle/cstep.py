@@ -84,6 +84,8 @@ class Stepper:
         if bool(getattr(p, 'v_sensitive_gj', False)) or (getattr(p, 'iCa', -1) >= 0
                                                            and float(getattr(p, 'alpha_Ca', 0.0)) > 0):
             raise ValueError('voltage-gated gap junctions and the Ca-ATPase are not restated in C')
+        if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
+            raise ValueError('the polarizable Vmem update is not restated in C')
         self.lib = load()
         self.threads = int(threads)
         m2c = np.ascontiguousarray(g.mem_to_cells, np.int64)

@@ -134,8 +134,17 @@ def gap_junction_run(gjopen, vgj, p):
 
 
 def init_vm(g, p, s):
-    """Initial ``update_V`` (sim.py:1041 -> 2007-2029) for a fresh state."""
+    """Initial ``update_V`` (sim.py:1041 -> 2007-2029) for a fresh state.  With
+    cell polarizability the implicit form runs from vm = 0 (sim.py:550) with no
+    fluxes yet, so Jn = 0 (sim.py:2048-2058)."""
     rho = np.dot(p.zs * p.F, s.cc_cells)
+    if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
+        sigma_cell = np.asarray([((z ** 2) * (p.F ** 2) * cc * D * 0.1) / (p.R * p.T)
+                                 for z, cc, D in zip(p.zs, s.cc_cells, p.D_free)]).mean(axis=0)
+        vm_o = (1 / p.cm) * (rho * g.diviterm)[g.mem_to_cells]
+        sig = sigma_cell[g.mem_to_cells]
+        return ((0.0 - (p.dt / p.cm) * 0.0 + ((p.dt * sig * vm_o) / (p.cm * g.R_rads)))
+                / (1 + ((p.dt * sig) / (p.cm * g.R_rads))))
     Phi_b = s.Phi_b if s.Phi_b is not None else np.zeros(int(np.prod(g.grid_shape)))
     return (1 / p.cm) * (rho * g.diviterm)[g.mem_to_cells] - Phi_b[g.map_mem2ecm]
 
@@ -275,28 +284,48 @@ def step(g, p, s, outputs=False):
     rho_cells = np.dot(p.zs * F, s.cc_cells)
     if is_ecm:
         s.E_env_x, s.E_env_y, v_env, rho_env = _env_E_field(g, p, s)
-    vm_new = (1 / p.cm) * (rho_cells * g.diviterm)[m2c] - s.Phi_b[g.map_mem2ecm]
+    polar = float(getattr(p, 'cell_polarizability', 0.0)) != 0.0
+    if polar or outputs:
+        # get_current (ion_current.py:19-37): smoothed normal current density
+        zF = p.zs * F
+        Jn = -np.dot(zF, fluxes_mem) + np.dot(zF, fluxes_gj)
+        Jn_ave = seg_sum(g, Jn * g.mem_sa) / g.cell_sa
+        Jn = g.smooth_weight_mem * Jn + Jn_ave[m2c] * g.smooth_weight_o
+        sigma_cell = np.asarray([((z ** 2) * (F ** 2) * cc * D * 0.1) / (R * T)
+                                 for z, cc, D in zip(p.zs, s.cc_cells, p.D_free)]).mean(axis=0)
+    if polar:
+        # implicit polarizable form (sim.py:2048-2058): vm relaxes towards the
+        # cell's charge potential through the cytoplasm, driven by Jn; vm here
+        # carries the in-place nonces, as self.vm does in the reference
+        vm_o = (1 / p.cm) * (rho_cells * g.diviterm)[m2c]
+        sig = sigma_cell[m2c]
+        vm_new = ((vm - (p.dt / p.cm) * Jn + ((p.dt * sig * vm_o) / (p.cm * g.R_rads)))
+                  / (1 + ((p.dt * sig) / (p.cm * g.R_rads))))
+    else:
+        vm_new = (1 / p.cm) * (rho_cells * g.diviterm)[m2c] - s.Phi_b[g.map_mem2ecm]
     if np.isnan(vm_new).any():
         raise FloatingPointError('NaN Vmem (check_v)')
     s.vm = vm_new
 
     if outputs:
-        zF = p.zs * F
-        Jn = -np.dot(zF, fluxes_mem) + np.dot(zF, fluxes_gj)
-        Jn_ave = seg_sum(g, Jn * g.mem_sa) / g.cell_sa
-        Jn = g.smooth_weight_mem * Jn + Jn_ave[m2c] * g.smooth_weight_o
         J_cell_x = seg_sum(g, Jn * g.mem_nx * g.mem_sa) / g.cell_sa
         J_cell_y = seg_sum(g, Jn * g.mem_ny * g.mem_sa) / g.cell_sa
-        sigma_cell = np.asarray([((z ** 2) * (F ** 2) * cc * D * 0.1) / (R * T)
-                                 for z, cc, D in zip(p.zs, s.cc_cells, p.D_free)]).mean(axis=0)
-        E_cell_x = J_cell_x / sigma_cell
-        E_cell_y = J_cell_y / sigma_cell
+        vm_ave = seg_sum(g, s.vm) / g.num_mems
+        if polar:
+            # cell field from the membrane voltage profile (sim.py:2063-2074)
+            Rcells = g.R_rads * (p.true_cell_size / p.cell_radius)
+            gE = (s.vm - vm_ave[m2c]) / Rcells
+            E_cell_x = seg_sum(g, -gE * g.mem_nx * g.mem_sa) / g.cell_sa
+            E_cell_y = seg_sum(g, -gE * g.mem_ny * g.mem_sa) / g.cell_sa
+        else:
+            E_cell_x = J_cell_x / sigma_cell
+            E_cell_y = J_cell_y / sigma_cell
         out.update(
             fluxes_mem=fluxes_mem, fluxes_gj=fluxes_gj, rate_NaKATP=rate,
             rho_cells=rho_cells, Jn=Jn, I_mem=-Jn * g.mem_sa,
             J_cell_x=J_cell_x, J_cell_y=J_cell_y,
             Jc=J_cell_x[m2c] * g.mem_nx + J_cell_y[m2c] * g.mem_ny,
-            vm_ave=seg_sum(g, s.vm) / g.num_mems,
+            vm_ave=vm_ave,
             dvm=(s.vm - vmo) / p.dt, sigma_cell=sigma_cell,
             E_cell_x=E_cell_x, E_cell_y=E_cell_y,
             Emc=E_cell_x[m2c] * g.mem_nx + E_cell_y[m2c] * g.mem_ny,

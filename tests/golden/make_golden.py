@@ -100,7 +100,7 @@ ION_ORDER = ['Na', 'K', 'Cl', 'Ca', 'P', 'M']   # order of p.ions_dict (H off)
 
 
 def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False,
-                alpha_Ca=0.0):
+                alpha_Ca=0.0, cell_polarizability=0.0):
     from betse.science.enum.enumconf import CellLatticeType, SolverType
     p = SimpleNamespace()
     # physical constants, parameters.py:1087-1122
@@ -138,7 +138,7 @@ def make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space=26e-9, sharpn
     p.sharpness = sharpness
     p.smooth_cells = 1 / 0.5
     p.true_cell_size = 1.0e-5
-    p.cell_polarizability = 0.0
+    p.cell_polarizability = cell_polarizability
     p.gj_surface = 5.0e-8
     p.v_sensitive_gj = v_sensitive_gj
     # gating constants of sim_config.yaml's 'gap junctions' block
@@ -286,11 +286,12 @@ OUT_KEYS = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn',
 
 def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
              dm_range=(1e-19, 1e-17), cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False,
-             alpha_Ca=0.0):
+             alpha_Ca=0.0, cell_polarizability=0.0):
     from betse.science.sim import Simulator
     from betse.science.enum.enumphase import SimPhaseKind
     n_steps = max(checkpoints)
-    p = make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space, sharpness, v_sensitive_gj, alpha_Ca)
+    p = make_params(radius, grid_size, is_ecm, dt, n_steps, cell_space, sharpness, v_sensitive_gj, alpha_Ca,
+                    cell_polarizability)
     t0 = time.time()
     c = build_cells(p, radius, seed)
     t_seed = time.time() - t0
@@ -341,7 +342,8 @@ def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
               cell_radius=p.cell_radius, true_cell_size=p.true_cell_size,
               sigma=np.float64(s.sigma), is_ecm=float(is_ecm),
               v_sensitive_gj=float(bool(v_sensitive_gj)), gj_vthresh=p.gj_vthresh, gj_min=p.gj_min,
-              alpha_Ca=p.alpha_Ca, KmCa_Ca=p.KmCa_Ca, KmCa_ATP=p.KmCa_ATP)
+              alpha_Ca=p.alpha_Ca, KmCa_Ca=p.KmCa_Ca, KmCa_ATP=p.KmCa_ATP,
+              cell_polarizability=p.cell_polarizability)
     for k, v in sc.items():
         out['par_' + k] = np.float64(v)
     out['par_zs'] = np.asarray(s.zs, np.float64)
@@ -408,6 +410,10 @@ CASES = {
     'ecm_r40_s13_ca': dict(radius=40e-6, seed=13, is_ecm=True, grid_size=20,
                            dt=5e-3, checkpoints=[1, 2, 30], cell_space=25e-9, sharpness=0.5,
                            alpha_Ca=5e-8),
+    # cell polarizability on: the implicit membrane-voltage update of update_V
+    # (the value phasereqs.py sets when a phase asks for it)
+    'noecm_r50_s17_pol': dict(radius=50e-6, seed=17, is_ecm=False, grid_size=20,
+                              dt=1e-2, checkpoints=[1, 2, 40], cell_polarizability=1e-4),
     # a handful of cells: boundary-dominated edge case
     'noecm_r20_s2': dict(radius=20e-6, seed=2, is_ecm=False, grid_size=12,
                          dt=1e-2, checkpoints=[1, 20]),

@@ -12,11 +12,17 @@ import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
 CASES = ['noecm_r80_s1', 'noecm_r50_s7', 'ecm_r50_s3', 'ecm_r40_s5_sharp', 'noecm_r50_s9_vgj',
-         'noecm_r50_s11_ca', 'ecm_r40_s13_ca', 'noecm_r20_s2']
+         'noecm_r50_s11_ca', 'ecm_r40_s13_ca', 'noecm_r50_s17_pol', 'noecm_r20_s2']
 
 
 def load(name):
     return dict(np.load(os.path.join(GOLDEN, name + '.npz')))
+
+
+def polar(d):
+    """Cell polarizability on: Vmem is per-membrane state, which only the
+    plain FP64 form keeps (the split form refuses the configuration)."""
+    return float(d.get('par_cell_polarizability', 0.0)) != 0.0
 
 
 def geometry(d):
@@ -114,7 +120,8 @@ def engine_inputs(d):
                     c_env_bound=getattr(p, 'c_env_bound', None), ion_names=p.ion_names,
                     v_sensitive_gj=p.v_sensitive_gj, gj_vthresh=getattr(p, 'gj_vthresh', 15.0),
                     gj_min=getattr(p, 'gj_min', 0.10), iCa=p.iCa, alpha_Ca=p.alpha_Ca,
-                    KmCa_Ca=getattr(p, 'KmCa_Ca', 1.0e-3), KmCa_ATP=getattr(p, 'KmCa_ATP', 0.5), **kw)
+                    KmCa_Ca=getattr(p, 'KmCa_Ca', 1.0e-3), KmCa_ATP=getattr(p, 'KmCa_ATP', 0.5),
+                    cell_polarizability=getattr(p, 'cell_polarizability', 0.0), **kw)
     s = state(d)
     st = dict(vm=s.vm, cc_cells=s.cc_cells, cc_at_mem=s.cc_at_mem, cc_env=s.cc_env)
     if p.v_sensitive_gj:

@@ -39,8 +39,8 @@ def test_library_exports_every_declared_symbol(lib):
 def test_struct_layouts_match_header(lib):
     from betse_gb300 import _lib
     # bx_params: 4 int32 + 29 doubles + 4 arrays of 8 doubles + gating (2 int32 + 2 doubles)
-    assert ct.sizeof(_lib.BxParams) == 16 + 8 * 29 + 4 * 8 * 8 + 8 + 16 + 24
-    assert ct.sizeof(_lib.BxGeom) == 16 + 8 * 14 + 16
+    assert ct.sizeof(_lib.BxParams) == 16 + 8 * 29 + 4 * 8 * 8 + 8 + 16 + 24 + 8
+    assert ct.sizeof(_lib.BxGeom) == 16 + 8 * 14 + 16 + 8
     assert ct.sizeof(_lib.BxStepStatus) == 8 + 4 + 4 + 8 + 4 + 4
 
 

@@ -5,7 +5,7 @@ import pytest
 
 import golden_io as gi
 
-CASES = [c for c in gi.CASES if c.startswith('noecm') and not c.endswith(('_vgj', '_ca'))]
+CASES = [c for c in gi.CASES if c.startswith('noecm') and not c.endswith(('_vgj', '_ca', '_pol'))]
 
 
 @pytest.fixture(scope='module')

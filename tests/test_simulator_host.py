@@ -30,7 +30,6 @@ def test_default_electrodiffusion_config_is_supported():
     (dict(deform_osmo=True), 'osmotic'),
     (dict(fluid_flow=True), 'fluid flow'),
     (dict(deformation=True), 'deformation'),
-    (dict(cell_polarizability=1e-3), 'polarizability'),
     (dict(cluster_open=False), 'closed cluster'),
 ])
 def test_unsupported_options_are_named(opt, frag):
@@ -39,6 +38,14 @@ def test_unsupported_options_are_named(opt, frag):
         setattr(ph.p, k, v)
     reasons = simulator.unsupported_features(None, ph)
     assert len(reasons) == 1 and frag in reasons[0]
+
+
+def test_polarizability_needs_the_plain_form():
+    ph = _phase()
+    ph.p.cell_polarizability = 1e-4
+    assert simulator.unsupported_features(None, ph, precision='fp64') == []
+    reasons = simulator.unsupported_features(None, ph, precision='split')
+    assert len(reasons) == 1 and 'polarizability' in reasons[0]
 
 
 def test_sim_phase_needs_event_free_configuration():
