@@ -612,6 +612,10 @@ def main():
     up()
     e_s.step(T)
     torch.cuda.synchronize()
+    # the result is read back into page-locked arrays the caller allocates once
+    # and reuses, as a host loop over sampled steps would
+    first = e_s.e.download_concat() if sweep else e_s.download()
+    pin_out = {k: pinned(v) for k, v in first.items()}
     d2h = 0
     t_e2e = []
     for k in range(args.warmup + args.steps):
@@ -620,7 +624,7 @@ def main():
         t0 = time.perf_counter()
         up()
         e_s.step(T)
-        out = e_s.e.download_concat() if sweep else e_s.download()
+        out = e_s.e.download_concat(out=pin_out) if sweep else e_s.download(out=pin_out)
         t1 = time.perf_counter()
         d2h = sum(v.nbytes for v in out.values())
         if k >= args.warmup:

@@ -26,6 +26,7 @@
 #include "bx_fields.cuh"
 #include "bx_launch.cuh"
 #include "bx_split.cuh"
+#include "bx_state.cuh"
 
 namespace {
 
@@ -78,6 +79,13 @@ struct bx_cluster {
   bool ecm = false;
   bool ca = false;                 // Ca-ATPase on (iCa >= 0 and alpha_Ca > 0)
   bool polar = false;              // cell polarizability: per-membrane Vmem (plain form)
+  // state transfers: the caller's arrays staged on the device (BETSE layouts)
+  double* st_vm = nullptr;         // [M]
+  double* st_cc = nullptr;         // [I][C]
+  double* st_cam = nullptr;        // [I][M]
+  double* st_go = nullptr;         // [M]
+  int* d_flag = nullptr;           // [2] upload checks
+  int* t_slot_of_mem = nullptr;    // [M] split form: membrane slot of each membrane
   double* d_Rrads = nullptr;       // [M] membrane distance from the cell centre
   double* d_cnew = nullptr;        // [I][G] ECM with the Ca-ATPase: environment after the
                                    // Nernst-Planck update and smoothing, before the membrane scatter
@@ -177,7 +185,8 @@ void free_all(bx_cluster* h) {
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
-      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo, h->d_cnew, h->d_Rrads};
+      h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo, h->d_cnew, h->d_Rrads,
+      h->st_vm, h->st_cc, h->st_cam, h->st_go, h->d_flag, h->t_slot_of_mem};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& fs : h->fshapes)
@@ -707,13 +716,14 @@ int build_split_layout(bx_cluster* h, const std::vector<int>& blk) {
   }
   void* old[] = {h->t_lcell, h->t_nn, h->t_map_env, h->t_nn_env, h->t_c0, h->t_m0, h->t_slot_of_cell,
                  h->t_sa, h->t_gw, h->t_dtv, h->t_dvc, h->t_rng, h->d_Dm_f, h->s_cc2, h->s_rec[0], h->s_rec[1],
-                 h->t_gjo};
+                 h->t_gjo, h->t_slot_of_mem};
   for (void* q : old)
     if (q) cudaFree(q);
   h->t_lcell = nullptr; h->t_nn = h->t_map_env = h->t_nn_env = h->t_c0 = h->t_m0 = h->t_slot_of_cell = nullptr;
   h->t_sa = h->t_gw = h->t_dtv = h->t_dvc = nullptr; h->t_rng = nullptr; h->d_Dm_f = nullptr;
   h->s_cc2 = nullptr; h->s_rec[0] = h->s_rec[1] = nullptr;
   h->t_gjo = nullptr;
+  h->t_slot_of_mem = nullptr;
   h->Q = Q;
   if (h->vgj) {
     BX_CU(dalloc(&h->t_gjo, Q));
@@ -727,6 +737,7 @@ int build_split_layout(bx_cluster* h, const std::vector<int>& blk) {
   BX_CU(dalloc(&h->t_c0, nblk)); BX_CU(h2d(h->t_c0, t_c0.data(), nblk));
   BX_CU(dalloc(&h->t_m0, nblk)); BX_CU(h2d(h->t_m0, t_m0.data(), nblk));
   BX_CU(dalloc(&h->t_slot_of_cell, C)); BX_CU(h2d(h->t_slot_of_cell, h->h_slot_of_cell.data(), C));
+  BX_CU(dalloc(&h->t_slot_of_mem, M)); BX_CU(h2d(h->t_slot_of_mem, h->h_slot_of_mem.data(), M));
   BX_CU(dalloc(&h->t_sa, Q)); BX_CU(h2d(h->t_sa, sa.data(), Q));
   BX_CU(dalloc(&h->t_gw, Q)); BX_CU(h2d(h->t_gw, gw.data(), Q));
   BX_CU(dalloc(&h->t_rng, S)); BX_CU(h2d(h->t_rng, rng.data(), S));
@@ -1084,6 +1095,29 @@ int bx_set_env_diffusivity(bx_handle h, const double* D_env) {
   return BX_OK;
 }
 
+// Device staging for state transfers: the caller's arrays in BETSE's layouts
+// (allocated at the first transfer).
+int ensure_state_staging(bx_cluster* h) {
+  if (h->st_cam) return BX_OK;
+  const size_t M = h->M, C = h->C, I = h->I;
+  if (dalloc(&h->st_vm, M) != cudaSuccess || dalloc(&h->st_cc, I * C) != cudaSuccess ||
+      dalloc(&h->st_go, M) != cudaSuccess || dalloc(&h->d_flag, 2) != cudaSuccess ||
+      dalloc(&h->st_cam, I * M) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(BX_ENOMEM, "cudaMalloc state staging");
+  }
+  return BX_OK;
+}
+
+bx::StateIO state_io(const bx_cluster* h) {
+  bx::StateIO io{};
+  io.C = h->C; io.M = h->M; io.I = h->I; io.S = h->S; io.rec = kRec;
+  io.cell_ptr = h->d_cell_ptr; io.m2c = h->d_m2c; io.map_env = h->d_map_env;
+  io.phib = h->d_phib; io.phib_on = h->phib_nonzero ? 1 : 0;
+  io.slot_of_cell = h->t_slot_of_cell; io.slot_of_mem = h->t_slot_of_mem;
+  return io;
+}
+
 // Phi_b at membrane m's grid cell.  A boundary potential needs a single
 // cluster (bx_set_boundary_potential), and a batch's membranes index their own
 // clusters' grids, which h_phib (sized by the first cluster's grid) does not
@@ -1115,70 +1149,75 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
   if (!h || !s || !s->vm || !s->cc_cells || !s->cc_at_mem || !s->cc_env)
     return fail(BX_EINVAL, "null argument");
   const int C = h->C, M = h->M, I = h->I;
-  const std::vector<int>& ptr = h->h_cell_ptr;
-  std::vector<double> ccm((size_t)I * C);
-  for (int i = 0; i < I; ++i)
-    for (int c = 0; c < C; ++c) {
-      const double v = s->cc_at_mem[(size_t)i * M + ptr[c]];
-      for (int m = ptr[c] + 1; m < ptr[c + 1]; ++m)
-        if (s->cc_at_mem[(size_t)i * M + m] != v)
-          return fail(BX_EINVAL, "cc_at_mem must be constant over each cell's membranes");
-      ccm[(size_t)i * C + c] = v;
-    }
   if (h->ecm && (!s->E_env_x || !s->E_env_y)) return fail(BX_EINVAL, "ECM state needs E_env_x/E_env_y");
   BX_CU(cudaStreamSynchronize(h->stream));
-  h->parity = 0;
+  int rc = ensure_state_staging(h);
+  if (rc != BX_OK) return rc;
+  cudaStream_t st = h->stream;
+  const bx::StateIO io = state_io(h);
+  const bool split = h->mode == MODE_SPLIT;
   const size_t nenv = h->ecm ? (size_t)I * h->G : (size_t)h->ncl * I;
-  if (h->mode == MODE_SPLIT) {
-    // Vmem is constant per cell (minus Phi_b per membrane) in BETSE's full
-    // solver with cell_polarizability == 0 (sim.py:2027-2029)
-    const int S = h->S;
-    std::vector<float> rec((size_t)kRec * S, 0.0f);
-    std::vector<float2> cc2((size_t)I * S, make_float2(0.f, 0.f));
-    for (int c = 0; c < C; ++c) {
-      const double v0 = s->vm[ptr[c]] + phib_at(h, ptr[c]);
-      for (int m = ptr[c] + 1; m < ptr[c + 1]; ++m) {
-        const double v = s->vm[m] + phib_at(h, m);
-        if (std::fabs(v - v0) > 1e-12 * std::fabs(v0) + 1e-18)
-          return fail(BX_EINVAL, "split form: vm must be uniform over each cell's membranes");
-      }
-      const int sc = h->h_slot_of_cell[c];
-      rec[(size_t)sc * kRec + kRec - 1] = (float)v0;
-      for (int i = 0; i < I; ++i) {
-        rec[(size_t)sc * kRec + i] = (float)ccm[(size_t)i * C + c];
-        const double x = s->cc_cells[(size_t)i * C + c];
-        const float hi = (float)x;
-        cc2[(size_t)i * S + sc] = make_float2(hi, (float)(x - (double)hi));
-      }
-    }
-    BX_CU(h2d(h->s_rec[0], rec.data(), rec.size()));
-    BX_CU(h2d(h->s_cc2, cc2.data(), cc2.size()));
+  // the caller's arrays cross as they are; the checks and the re-layout run
+  // on the device.  A failed check leaves the handle without a state.
+  h->have_state = false;
+  double* vm_dst = split ? h->st_vm : h->d_vm[0];
+  double* cc_dst = split ? h->st_cc : h->d_cc;
+  BX_CU(cudaMemcpyAsync(vm_dst, s->vm, (size_t)M * sizeof(double), cudaMemcpyHostToDevice, st));
+  BX_CU(cudaMemcpyAsync(cc_dst, s->cc_cells, (size_t)I * C * sizeof(double), cudaMemcpyHostToDevice, st));
+  BX_CU(cudaMemcpyAsync(h->st_cam, s->cc_at_mem, (size_t)I * M * sizeof(double), cudaMemcpyHostToDevice, st));
+  BX_CU(cudaMemsetAsync(h->d_flag, 0, 2 * sizeof(int), st));
+  const int tb = 256;
+  bx::k_state_check<<<(M + tb - 1) / tb, tb, 0, st>>>(io, vm_dst, h->st_cam, split ? 1 : 0, h->d_flag);
+  BX_CU(cudaGetLastError());
+  int flag[2] = {0, 0};
+  BX_CU(cudaMemcpyAsync(flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, st));
+  BX_CU(cudaStreamSynchronize(st));
+  if (flag[0]) return fail(BX_EINVAL, "cc_at_mem must be constant over each cell's membranes");
+  // Vmem is constant per cell (minus Phi_b per membrane) in BETSE's full
+  // solver with cell_polarizability == 0 (sim.py:2027-2029)
+  if (flag[1]) return fail(BX_EINVAL, "split form: vm must be uniform over each cell's membranes");
+  h->parity = 0;
+  if (split) {
+    BX_CU(cudaMemsetAsync(h->s_rec[0], 0, (size_t)kRec * h->S * sizeof(float), st));
+    BX_CU(cudaMemsetAsync(h->s_cc2, 0, (size_t)I * h->S * sizeof(float2), st));
+    bx::k_state_pack_split<<<(C + tb - 1) / tb, tb, 0, st>>>(io, h->st_vm, h->st_cc, h->st_cam, h->s_rec[0],
+                                                            h->s_cc2);
+    BX_CU(cudaGetLastError());
     if (h->vgj) {
-      std::vector<float> go((size_t)h->Q, 0.0f);
-      for (int m = 0; m < M; ++m)
-        go[h->h_slot_of_mem[m]] = (float)(s->gjopen ? s->gjopen[m] : h->h_gjw[m]);
-      BX_CU(h2d(h->t_gjo, go.data(), go.size()));
+      if (s->gjopen)
+        BX_CU(cudaMemcpyAsync(h->st_go, s->gjopen, (size_t)M * sizeof(double), cudaMemcpyHostToDevice, st));
+      else
+        BX_CU(cudaMemcpyAsync(h->st_go, h->d_gj_w, (size_t)M * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      BX_CU(cudaMemsetAsync(h->t_gjo, 0, (size_t)h->Q * sizeof(float), st));
+      bx::k_state_pack_gjo<<<(M + tb - 1) / tb, tb, 0, st>>>(io, h->st_go, h->t_gjo);
+      BX_CU(cudaGetLastError());
     }
-    BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
+    BX_CU(cudaMemcpyAsync(h->d_cenv, s->cc_env, nenv * sizeof(double), cudaMemcpyHostToDevice, st));
     if (h->ecm) {
-      BX_CU(h2d(h->d_Ex, s->E_env_x, h->G));
-      BX_CU(h2d(h->d_Ey, s->E_env_y, h->G));
+      BX_CU(cudaMemcpyAsync(h->d_Ex, s->E_env_x, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
+      BX_CU(cudaMemcpyAsync(h->d_Ey, s->E_env_y, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
     } else {
       std::vector<float> cef(nenv);
       for (size_t q = 0; q < nenv; ++q) cef[q] = (float)s->cc_env[q];
-      BX_CU(h2d(h->s_cenv_f, cef.data(), nenv));
+      BX_CU(cudaMemcpyAsync(h->s_cenv_f, cef.data(), nenv * sizeof(float), cudaMemcpyHostToDevice, st));
+      BX_CU(cudaStreamSynchronize(st));   // cef is a local buffer
     }
   } else {
-    BX_CU(h2d(h->d_vm[0], s->vm, M));
-    BX_CU(h2d(h->d_cc, s->cc_cells, (size_t)I * C));
-    BX_CU(h2d(h->d_ccm[0], ccm.data(), ccm.size()));
-    BX_CU(h2d(h->d_cenv, s->cc_env, nenv));
-    if (h->vgj) BX_CU(h2d(h->d_gjo, s->gjopen ? s->gjopen : h->h_gjw.data(), M));
+    bx::k_state_pack_ccm<<<(C + tb - 1) / tb, tb, 0, st>>>(io, h->st_cam, h->d_ccm[0]);
+    BX_CU(cudaGetLastError());
+    BX_CU(cudaMemcpyAsync(h->d_cenv, s->cc_env, nenv * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (h->vgj) {
+      if (s->gjopen)
+        BX_CU(cudaMemcpyAsync(h->d_gjo, s->gjopen, (size_t)M * sizeof(double), cudaMemcpyHostToDevice, st));
+      else
+        BX_CU(cudaMemcpyAsync(h->d_gjo, h->d_gj_w, (size_t)M * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
     if (h->ecm) {
-      BX_CU(h2d(h->d_Ex, s->E_env_x, h->G));
-      BX_CU(h2d(h->d_Ey, s->E_env_y, h->G));
+      BX_CU(cudaMemcpyAsync(h->d_Ex, s->E_env_x, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
+      BX_CU(cudaMemcpyAsync(h->d_Ey, s->E_env_y, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
     }
   }
+  BX_CU(cudaStreamSynchronize(st));
   h->have_state = true;
   h->have_outputs = false;
   h->last_step_outputs = false;
@@ -1190,52 +1229,39 @@ int bx_state_download(bx_handle h, bx_state* s) {
   if (!h->have_state) return fail(BX_ESTATE, "no state uploaded");
   const int C = h->C, M = h->M, I = h->I;
   BX_CU(cudaStreamSynchronize(h->stream));
+  int rc = ensure_state_staging(h);
+  if (rc != BX_OK) return rc;
+  cudaStream_t st = h->stream;
+  const bx::StateIO io = state_io(h);
   const size_t nenv = h->ecm ? (size_t)I * h->G : (size_t)h->ncl * I;
-  std::vector<double> ccm((size_t)I * C);
+  const int tb = 256;
+  auto d2h = [&](double* dst, const double* src, size_t n) {
+    return dst ? cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st) : cudaSuccess;
+  };
   if (h->mode == MODE_SPLIT) {
-    const int S = h->S;
-    std::vector<float> rec((size_t)kRec * S);
-    std::vector<float2> cc2((size_t)I * S);
-    BX_CU(cudaMemcpy(rec.data(), h->s_rec[h->parity], rec.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    BX_CU(cudaMemcpy(cc2.data(), h->s_cc2, cc2.size() * sizeof(float2), cudaMemcpyDeviceToHost));
-    if (s->vm)
-      for (int m = 0; m < M; ++m)
-        s->vm[m] = (double)rec[(size_t)h->h_slot_of_cell[h->h_m2c[m]] * kRec + kRec - 1] - phib_at(h, m);
-    for (int c = 0; c < C; ++c) {
-      const int sc = h->h_slot_of_cell[c];
-      for (int i = 0; i < I; ++i) {
-        if (s->cc_cells) {
-          const float2 x = cc2[(size_t)i * S + sc];
-          s->cc_cells[(size_t)i * C + c] = (double)x.x + (double)x.y;
-        }
-        ccm[(size_t)i * C + c] = (double)rec[(size_t)sc * kRec + i];
-      }
-    }
-    if (h->ecm) {
-      if (s->E_env_x) BX_CU(cudaMemcpy(s->E_env_x, h->d_Ex, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
-      if (s->E_env_y) BX_CU(cudaMemcpy(s->E_env_y, h->d_Ey, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
-    }
-    if (h->vgj && s->gjopen) {
-      std::vector<float> go((size_t)h->Q);
-      BX_CU(cudaMemcpy(go.data(), h->t_gjo, go.size() * sizeof(float), cudaMemcpyDeviceToHost));
-      for (int m = 0; m < M; ++m) s->gjopen[m] = (double)go[h->h_slot_of_mem[m]];
-    }
+    const int n = std::max(M, C);
+    const bool go = h->vgj && s->gjopen;
+    bx::k_state_unpack_split<<<(n + tb - 1) / tb, tb, 0, st>>>(io, h->s_rec[h->parity], h->s_cc2,
+                                                              go ? h->t_gjo : nullptr, h->st_vm, h->st_cam,
+                                                              h->st_cc, h->st_go);
+    BX_CU(cudaGetLastError());
+    BX_CU(d2h(s->vm, h->st_vm, M));
+    BX_CU(d2h(s->cc_cells, h->st_cc, (size_t)I * C));
+    if (go) BX_CU(d2h(s->gjopen, h->st_go, M));
   } else {
-    if (s->vm) BX_CU(cudaMemcpy(s->vm, h->d_vm[h->parity], (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
-    if (s->cc_cells)
-      BX_CU(cudaMemcpy(s->cc_cells, h->d_cc, (size_t)I * C * sizeof(double), cudaMemcpyDeviceToHost));
-    BX_CU(cudaMemcpy(ccm.data(), h->d_ccm[h->parity], ccm.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    if (h->vgj && s->gjopen)
-      BX_CU(cudaMemcpy(s->gjopen, h->d_gjo, (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
-    if (h->ecm) {
-      if (s->E_env_x) BX_CU(cudaMemcpy(s->E_env_x, h->d_Ex, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
-      if (s->E_env_y) BX_CU(cudaMemcpy(s->E_env_y, h->d_Ey, (size_t)h->G * sizeof(double), cudaMemcpyDeviceToHost));
-    }
+    bx::k_state_unpack_cam<<<(M + tb - 1) / tb, tb, 0, st>>>(io, h->d_ccm[h->parity], h->st_cam);
+    BX_CU(cudaGetLastError());
+    BX_CU(d2h(s->vm, h->d_vm[h->parity], M));
+    BX_CU(d2h(s->cc_cells, h->d_cc, (size_t)I * C));
+    if (h->vgj) BX_CU(d2h(s->gjopen, h->d_gjo, M));
   }
-  if (s->cc_at_mem)
-    for (int i = 0; i < I; ++i)
-      for (int m = 0; m < M; ++m) s->cc_at_mem[(size_t)i * M + m] = ccm[(size_t)i * C + h->h_m2c[m]];
-  if (s->cc_env) BX_CU(cudaMemcpy(s->cc_env, h->d_cenv, nenv * sizeof(double), cudaMemcpyDeviceToHost));
+  BX_CU(d2h(s->cc_at_mem, h->st_cam, (size_t)I * M));
+  if (h->ecm) {
+    BX_CU(d2h(s->E_env_x, h->d_Ex, h->G));
+    BX_CU(d2h(s->E_env_y, h->d_Ey, h->G));
+  }
+  BX_CU(d2h(s->cc_env, h->d_cenv, nenv));
+  BX_CU(cudaStreamSynchronize(st));
   return BX_OK;
 }
 

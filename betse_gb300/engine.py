@@ -24,6 +24,21 @@ def _c(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
 
 
+def _destinations(shapes, out):
+    """Destination arrays for a download: the caller's (checked) or new ones."""
+    if out is None:
+        return {k: np.empty(v) for k, v in shapes.items()}
+    res = {}
+    for k, shape in shapes.items():
+        a = out.get(k)
+        if a is None:
+            a = np.empty(shape)
+        elif a.shape != tuple(shape) or a.dtype != np.float64 or not a.flags['C_CONTIGUOUS']:
+            raise ValueError(f'{k}: need a C-contiguous float64 array of shape {tuple(shape)}')
+        res[k] = a
+    return res
+
+
 class ClusterEngine:
     def __init__(self, geom: ClusterGeometry, params: StepParams, precision='fp64'):
         self.lib = _lib.load()
@@ -105,15 +120,17 @@ class ClusterEngine:
         st = None if stream is None else ct.c_void_p(int(stream))
         _lib.check(self.lib.bx_step(self.h, int(n_steps), int(bool(outputs)), st), 'bx_step')
 
-    def download(self):
+    def download(self, out=None):
+        """The state in BETSE's layouts.  ``out`` (optional) holds destination
+        arrays to fill, e.g. page-locked buffers reused across sampled steps;
+        each must be C-contiguous float64 of the shape returned here."""
         I, C, M, G = self.I, self.C, self.M, self.G
-        out = dict(vm=np.empty(M), cc_cells=np.empty((I, C)), cc_at_mem=np.empty((I, M)),
-                   cc_env=np.empty((I, G) if self.ecm else I))
+        shapes = dict(vm=(M,), cc_cells=(I, C), cc_at_mem=(I, M), cc_env=(I, G) if self.ecm else (I,))
         if self.ecm:
-            out['E_env_x'] = np.empty(G)
-            out['E_env_y'] = np.empty(G)
+            shapes.update(E_env_x=(G,), E_env_y=(G,))
         if self.vgj:
-            out['gjopen'] = np.empty(M)
+            shapes['gjopen'] = (M,)
+        out = _destinations(shapes, out)
         s = _lib.BxState(*[_lib.dptr(out.get(k)) for k in
                            ('vm', 'cc_cells', 'cc_at_mem', 'cc_env', 'E_env_x', 'E_env_y', 'gjopen')])
         _lib.check(self.lib.bx_state_download(self.h, ct.byref(s)), 'bx_state_download')
@@ -275,10 +292,12 @@ class BatchEngine(ClusterEngine):
         st = _lib.BxState(*[_lib.dptr(a) for a in arrs], None, None, None)
         _lib.check(self.lib.bx_state_upload(self.h, ct.byref(st)), 'bx_state_upload')
 
-    def download_concat(self):
+    def download_concat(self, out=None):
+        """The concatenated state (``out``: optional destination arrays, as in
+        ``ClusterEngine.download``)."""
         I = self.I
-        out = dict(vm=np.empty(self.M), cc_cells=np.empty((I, self.C)), cc_at_mem=np.empty((I, self.M)),
-                   cc_env=np.empty((self.n_clusters, I)))
+        out = _destinations(dict(vm=(self.M,), cc_cells=(I, self.C), cc_at_mem=(I, self.M),
+                                 cc_env=(self.n_clusters, I)), out)
         st = _lib.BxState(*[_lib.dptr(out[k]) for k in ('vm', 'cc_cells', 'cc_at_mem', 'cc_env')], None, None, None)
         _lib.check(self.lib.bx_state_download(self.h, ct.byref(st)), 'bx_state_download')
         return out

@@ -227,3 +227,38 @@ def test_voltage_gated_gj_state_round_trip_and_autotune(precision):
     tol = 0.0 if precision == 'fp64' else 1e-12
     for k in sa:
         assert gi.rel_err(sa[k], sb[k]) <= tol, k
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split'])
+def test_upload_checks_and_download_into_given_arrays(precision):
+    """The device-side upload checks refuse what BETSE's layouts cannot hold
+    (and leave no state behind); downloads fill caller-given arrays."""
+    from betse_gb300._lib import BxLibraryError
+    from betse_gb300.engine import ClusterEngine
+    d = gi.load('noecm_r50_s7')
+    cg, sp, Dm, st, _ = gi.engine_inputs(d)
+    with ClusterEngine(cg, sp, precision) as eng:
+        eng.set_membrane_diffusivity(Dm)
+        bad = dict(st)
+        cam = st['cc_at_mem'].copy()
+        cam[0, 1] += 1.0                     # membrane 1 of cell 0 differs from membrane 0
+        bad['cc_at_mem'] = cam
+        with pytest.raises(BxLibraryError, match='cc_at_mem must be constant'):
+            eng.upload(**bad)
+        with pytest.raises(BxLibraryError):
+            eng.step(1)                      # no state after a failed upload
+        if precision == 'split':
+            bad = dict(st)
+            vm = st['vm'].copy()
+            vm[1] += 1e-3
+            bad['vm'] = vm
+            with pytest.raises(BxLibraryError, match='uniform'):
+                eng.upload(**bad)
+        eng.upload(**st)
+        eng.step(5)
+        ref = eng.download()
+        out = {k: np.full_like(v, np.nan) for k, v in ref.items()}
+        got = eng.download(out=out)
+        for k in ref:
+            assert got[k] is out[k]
+            assert np.array_equal(out[k], ref[k]), k
