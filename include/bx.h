@@ -216,7 +216,12 @@ int bx_set_boundary_potential(bx_handle h, const double* Phi_b);
 /* Replace the scalar parameters (e.g. dt between phases). */
 int bx_set_params(bx_handle h, const bx_params* p);
 
-/* Copy state in / out (synchronous on the handle's stream). */
+/* Copy state in / out (synchronous on the handle's stream).  The arrays
+ * cross as they are and are checked and re-laid on the device.  Upload
+ * refuses (BX_EINVAL) a cc_at_mem that differs within a cell and, in the
+ * split form, a vm that is not uniform within a cell; after a refused upload
+ * the handle holds no state until the next successful one.  Download fills
+ * every non-NULL pointer (page-locked destinations copy fastest). */
 int bx_state_upload(bx_handle h, const bx_state* s);
 int bx_state_download(bx_handle h, bx_state* s);
 
