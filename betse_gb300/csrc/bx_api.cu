@@ -86,6 +86,8 @@ struct bx_cluster {
   double* st_go = nullptr;         // [M]
   int* d_flag = nullptr;           // [2] upload checks
   int* t_slot_of_mem = nullptr;    // [M] split form: membrane slot of each membrane
+  void* t_blob = nullptr;          // [nblk] PersistGeo: the persistent kernel's static tile data
+  size_t t_blob_bytes = 0;
   double* d_Rrads = nullptr;       // [M] membrane distance from the cell centre
   double* d_cnew = nullptr;        // [I][G] ECM with the Ca-ATPase: environment after the
                                    // Nernst-Planck update and smoothing, before the membrane scatter
@@ -186,7 +188,7 @@ void free_all(bx_cluster* h) {
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
       h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo, h->d_cnew, h->d_Rrads,
-      h->st_vm, h->st_cc, h->st_cam, h->st_go, h->d_flag, h->t_slot_of_mem};
+      h->st_vm, h->st_cc, h->st_cam, h->st_go, h->d_flag, h->t_slot_of_mem, h->t_blob};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& fs : h->fshapes)
@@ -362,6 +364,7 @@ bx::SplitGeom split_geom(const bx_cluster* h) {
   g.lcell = h->t_lcell; g.nn_slot = h->t_nn; g.mem_sa = h->t_sa; g.gjw = h->t_gw;
   g.cell_rng = h->t_rng; g.dtv = h->t_dtv; g.dvc = h->t_dvc; g.blk_cluster = h->d_blk_cl;
   g.tile_c0 = h->t_c0; g.tile_m0 = h->t_m0; g.map_env = h->t_map_env; g.nn_env = h->t_nn_env;
+  g.geo_blob = h->t_blob;
   return g;
 }
 
@@ -392,6 +395,33 @@ bool is_betse_six_ions(const bx_cluster* h) {
 }
 
 inline int env_grid(int G) { return (G + kEnvTPB - 1) / kEnvTPB; }
+
+// The persistent kernel's contiguous per-tile static data (PersistGeo), for
+// the instantiation that will read it; rebuilt after every layout or Dm change.
+template <int TPB, int NI>
+cudaError_t build_geo_blob_t(bx_cluster* h) {
+  using PG = bx::PersistGeo<TPB, NI>;
+  const size_t bytes = sizeof(PG) * (size_t)h->nblk;
+  if (h->t_blob_bytes != bytes) {
+    if (h->t_blob) cudaFree(h->t_blob);
+    h->t_blob = nullptr;
+    h->t_blob_bytes = 0;
+    cudaError_t e = cudaMalloc(&h->t_blob, bytes);
+    if (e != cudaSuccess) return e;
+    h->t_blob_bytes = bytes;
+  }
+  bx::k_split_blob<TPB, NI><<<h->nblk, TPB, 0, h->stream>>>(static_cast<PG*>(h->t_blob), h->d_Dm_f, h->t_sa,
+                                                            h->t_gw, h->t_nn, h->t_lcell, h->d_blk_cl, h->I,
+                                                            h->Q);
+  return cudaGetLastError();
+}
+
+cudaError_t build_geo_blob(bx_cluster* h) {
+  if (h->mode != MODE_SPLIT || !h->t_lcell) return cudaSuccess;
+  const bool six = is_betse_six_ions(h);
+  if (h->tpb == 192) return six ? build_geo_blob_t<192, 6>(h) : build_geo_blob_t<192, bx::kMaxIons>(h);
+  return six ? build_geo_blob_t<256, 6>(h) : build_geo_blob_t<256, bx::kMaxIons>(h);
+}
 
 // launch with programmatic dependent launch: the kernel's prologue overlaps
 // the previous kernel; cudaGridDependencySynchronize orders the state accesses
@@ -756,6 +786,8 @@ int build_split_layout(bx_cluster* h, const std::vector<int>& blk) {
   BX_CU(dalloc(&h->s_rec[1], (size_t)kRec * S));
   BX_CU(cudaMemset(h->s_rec[0], 0, (size_t)kRec * S * sizeof(float)));
   BX_CU(cudaMemset(h->s_rec[1], 0, (size_t)kRec * S * sizeof(float)));
+  BX_CU(build_geo_blob(h));
+  BX_CU(cudaStreamSynchronize(h->stream));
   h->have_state = false;
   return upload_param_arrays(h);
 }
@@ -1075,6 +1107,8 @@ int bx_set_membrane_diffusivity(bx_handle h, const double* Dm) {
     for (int i = 0; i < h->I; ++i)
       for (int m = 0; m < h->M; ++m) f[(size_t)i * h->Q + h->h_slot_of_mem[m]] = (float)Dm[(size_t)i * h->M + m];
     BX_CU(cudaMemcpy(h->d_Dm_f, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    BX_CU(build_geo_blob(h));
+    BX_CU(cudaStreamSynchronize(h->stream));
   } else if (h->d_Dm_f) {
     std::vector<float> f(n);
     for (size_t q = 0; q < n; ++q) f[q] = (float)Dm[q];

@@ -140,6 +140,7 @@ struct SplitGeom {
   const int* __restrict__ tile_m0;         // [nblk] first membrane (natural order) of the tile
   const int* __restrict__ map_env;         // [Q]  (PHIB only)
   const int* __restrict__ nn_env;          // [Q]  map_mem2ecm of the partner membrane (PHIB only)
+  const void* __restrict__ geo_blob;       // [nblk] PersistGeo: each tile's static data, contiguous
 };
 
 struct SplitConst {
@@ -491,17 +492,42 @@ __device__ __forceinline__ void cp_block(void* smem, const void* gmem, int bytes
   for (int off = (int)threadIdx.x * 16; off < bytes; off += TPB * 16) cp16(s + off, gp + off);
 }
 
+// One tile's static data for the persistent kernel, laid out in global memory
+// exactly as it is staged in shared memory, so one contiguous copy moves it:
+// Dm per ion, membrane area, gap-junction weight, partner cell slot, cell of
+// the slot, and the tile's cluster.  k_split_blob builds it from the
+// tile-major arrays whenever the layout or Dm changes.
+template <int TPB, int NI>
+struct PersistGeo {
+  float Dm[NI][TPB];
+  float sa[TPB];
+  float gw[TPB];
+  int nn[TPB];
+  uint8_t lcell[TPB];
+  int cl;                            // the tile's cluster
+  int pad[3];
+};
+
+template <int TPB, int NI>
+__global__ void __launch_bounds__(TPB)
+k_split_blob(PersistGeo<TPB, NI>* blob, const float* __restrict__ Dm, const float* __restrict__ sa,
+             const float* __restrict__ gw, const int* __restrict__ nn, const uint8_t* __restrict__ lcell,
+             const int* __restrict__ blk_cluster, int I, int Q) {
+  const int b = blockIdx.x, t = threadIdx.x;
+  const size_t q = (size_t)b * TPB + t;
+  PersistGeo<TPB, NI>& g = blob[b];
+#pragma unroll
+  for (int i = 0; i < NI; ++i) g.Dm[i][t] = (i < I) ? Dm[(size_t)i * Q + q] : 0.f;
+  g.sa[t] = sa[q];
+  g.gw[t] = gw[q];
+  g.nn[t] = nn[q];
+  g.lcell[t] = lcell[q];
+  if (t == 0) { g.cl = blk_cluster[b]; g.pad[0] = g.pad[1] = g.pad[2] = 0; }
+}
+
 template <int TPB, int NI>
 struct PersistSmem {
-  struct Geo {                       // one tile's geometry and channel data
-    float Dm[NI][TPB];
-    float sa[TPB];
-    float gw[TPB];
-    int nn[TPB];
-    uint8_t lcell[TPB];
-    int cl;                          // the tile's cluster
-    int pad[3];
-  };
+  using Geo = PersistGeo<TPB, NI>;
   struct State {                     // one tile's state
     float own[kCellsPerCta][8];
     float nbr[TPB][8];
@@ -541,31 +567,43 @@ k_split_persist(SplitGeom g, SplitPtrs p, SplitConst k, int ntile) {
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
   cudaTriggerProgrammaticLaunchCompletion();
 #endif
+  // the tile's static data: one contiguous block (PersistGeo), 16 bytes a copy
   auto issue_geo = [&](int tile, int buf) {
     if (tile >= ntile) return;
-    typename SM::Geo& ge = sm.geo[buf];
-    const size_t q0 = (size_t)tile * TPB;
-#pragma unroll
-    for (int i = 0; i < NI; ++i)
-      if (i < I) cp_block<TPB>(ge.Dm[i], p.Dm + (size_t)i * g.Q + q0, TPB * 4);
-    cp_block<TPB>(ge.sa, g.mem_sa + q0, TPB * 4);
-    cp_block<TPB>(ge.gw, g.gjw + q0, TPB * 4);
-    cp_block<TPB>(ge.nn, g.nn_slot + q0, TPB * 4);
-    cp_block<TPB>(ge.lcell, g.lcell + q0, TPB);
-    if (t == 0) cp4(&ge.cl, g.blk_cluster + tile);
+    cp_block<TPB>(&sm.geo[buf], static_cast<const typename SM::Geo*>(g.geo_blob) + tile,
+                  (int)sizeof(typename SM::Geo));
   };
+  // the tile's state as one flat range of 16-byte copies: the own records
+  // (64 copies), then 16 per ion of (hi, lo) pairs, then 8 each of the
+  // membrane ranges, dt/vol and diviterm/cm
   auto issue_state = [&](int tile, int sbuf, int gbuf) {
     if (tile >= ntile) return;
     typename SM::State& st = sm.st[sbuf];
     const typename SM::Geo& ge = sm.geo[gbuf];
     const int s0 = tile * kCellsPerCta;
-    cp_block<TPB>(st.own, p.rec_in + (size_t)s0 * REC, kCellsPerCta * REC * 4);
-#pragma unroll
-    for (int i = 0; i < NI; ++i)
-      if (i < I) cp_block<TPB>(st.cc2[i], p.cc2 + (size_t)i * g.S + s0, kCellsPerCta * 8);
-    cp_block<TPB>(st.rng, g.cell_rng + s0, kCellsPerCta * 4);
-    cp_block<TPB>(st.dtv, g.dtv + s0, kCellsPerCta * 4);
-    cp_block<TPB>(st.dvc, g.dvc + s0, kCellsPerCta * 4);
+    constexpr int kOwn = kCellsPerCta * REC * 4 / 16, kPair = kCellsPerCta * 8 / 16, kSmall = kCellsPerCta * 4 / 16;
+    const int n_copy = kOwn + kPair * I + 3 * kSmall;
+    for (int c = t; c < n_copy; c += TPB) {
+      const char* src;
+      char* dst;
+      if (c < kOwn) {
+        src = reinterpret_cast<const char*>(p.rec_in + (size_t)s0 * REC) + 16 * c;
+        dst = reinterpret_cast<char*>(&st.own[0][0]) + 16 * c;
+      } else if (c < kOwn + kPair * I) {
+        const int i = (c - kOwn) / kPair, o = 16 * ((c - kOwn) % kPair);
+        src = reinterpret_cast<const char*>(p.cc2 + (size_t)i * g.S + s0) + o;
+        dst = reinterpret_cast<char*>(st.cc2[i]) + o;
+      } else {
+        const int r = c - kOwn - kPair * I, which = r / kSmall, o = 16 * (r % kSmall);
+        src = which == 0 ? reinterpret_cast<const char*>(g.cell_rng + s0) + o
+            : which == 1 ? reinterpret_cast<const char*>(g.dtv + s0) + o
+                         : reinterpret_cast<const char*>(g.dvc + s0) + o;
+        dst = which == 0 ? reinterpret_cast<char*>(st.rng) + o
+            : which == 1 ? reinterpret_cast<char*>(st.dtv) + o
+                         : reinterpret_cast<char*>(st.dvc) + o;
+      }
+      cp16(dst, src);
+    }
     // the cluster's environment and pump rate: the cluster index came with the
     // geometry, so these loads do not wait on another load in the tile's compute
     if (t < I) cp4(&st.cenv[t], p.cenv_f + (size_t)ge.cl * I + t);
