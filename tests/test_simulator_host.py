@@ -82,3 +82,46 @@ def test_product_laplacian_matches_oracle():
     assert np.array_equal(L, oracle.fields.make_laplacian(9, 11, 2.5e-6))
     A = lap_env_inverse(9, 11, 2.5e-6)
     assert np.allclose(A @ L, np.eye(99), atol=1e-10)
+
+
+def _betse_objects(**popts):
+    """A BETSE Parameters / Simulator pair with the fields StepParams reads."""
+    p = SimpleNamespace(F=96485.0, R=8.314, dt=1e-2, cm=0.022, tm=7.5e-9, gj_surface=5e-8, alpha_NaK=5e-8,
+                        KmNK_Na=12.0, KmNK_K=0.2, KmNK_ATP=0.5, cATP=1.5, cADP=0.1, cPi=0.1,
+                        deltaGATP=-37000.0, vol_env=1e-12, is_ecm=False,
+                        ions_dict={'Na': 1, 'K': 1, 'Cl': 1, 'Ca': 1, 'P': 1, 'M': 1}, alpha_Ca=0.0,
+                        KmCa_Ca=1e-3, KmCa_ATP=0.5, v_sensitive_gj=False, gj_vthresh=15.0, gj_min=0.1,
+                        cell_polarizability=0.0)
+    for k, v in popts.items():
+        setattr(p, k, v)
+    sim = SimpleNamespace(zs=np.array([1, 1, -1, 2, -1, -1.0]), D_free=np.ones(6) * 1e-9,
+                          D_gj=np.ones(6) * 1e-18, iNa=0, iK=1, iCa=3, T=310.15, gj_block=1, NaKATP_block=1)
+    return p, sim
+
+
+def test_step_params_follow_betse_options():
+    from betse_gb300.cluster import StepParams
+    p, sim = _betse_objects()
+    sp = StepParams.from_betse(p, sim)
+    assert (sp.iCa, sp.alpha_Ca, sp.v_sensitive_gj, sp.cell_polarizability) == (3, 0.0, False, 0.0)
+    c = sp.to_c()
+    assert c.iCa == 3 and c.alpha_Ca == 0.0          # the pump stays off with alpha_Ca == 0
+    p, sim = _betse_objects(alpha_Ca=5e-8, v_sensitive_gj=True, gj_vthresh=12.0, cell_polarizability=1e-4)
+    sp = StepParams.from_betse(p, sim)
+    assert sp.iCa == 3 and sp.alpha_Ca == 5e-8
+    assert sp.v_sensitive_gj and sp.gj_vthresh == 12.0
+    assert sp.cell_polarizability == 1e-4
+    c = sp.to_c()
+    assert (c.v_sensitive_gj, c.gj_vthresh, c.cell_polarizability, c.alpha_Ca) == (1, 12.0, 1e-4, 5e-8)
+    # a profile without Ca leaves ca_handler's pump out whatever alpha_Ca says
+    p, sim = _betse_objects(alpha_Ca=5e-8)
+    p.ions_dict = dict(p.ions_dict, Ca=0)
+    assert StepParams.from_betse(p, sim).iCa == -1
+
+
+def test_step_params_reject_a_ca_row_out_of_range():
+    from betse_gb300.cluster import StepParams
+    p, sim = _betse_objects(alpha_Ca=5e-8)
+    sp = StepParams.from_betse(p, sim).replace(iCa=9)
+    with pytest.raises(ValueError, match='iCa'):
+        sp.to_c()
