@@ -24,6 +24,12 @@ def _c(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
 
 
+def _need(a, n, what):
+    """The C library reads exactly n values: refuse anything of another size."""
+    if a.size != n:
+        raise ValueError(f'{what}: expected {n} values, got {a.size}')
+
+
 def _destinations(shapes, out):
     """Destination arrays for a download: the caller's (checked) or new ones."""
     if out is None:
@@ -112,6 +118,16 @@ class ClusterEngine:
         ex = _c(E_env_x).ravel() if E_env_x is not None else None
         ey = _c(E_env_y).ravel() if E_env_y is not None else None
         go = _c(gjopen).ravel() if (gjopen is not None and self.vgj) else None
+        I, C, M, G = self.I, self.C, self.M, self.G
+        _need(vm, M, 'vm')
+        _need(cc, I * C, 'cc_cells')
+        _need(cam, I * M, 'cc_at_mem')
+        _need(ce, I * G if self.ecm else I, 'cc_env')
+        for a, k in ((ex, 'E_env_x'), (ey, 'E_env_y')):
+            if a is not None:
+                _need(a, G, k)
+        if go is not None:
+            _need(go, M, 'gjopen')
         s = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(ce),
                          _lib.dptr(ex), _lib.dptr(ey), _lib.dptr(go))
         _lib.check(self.lib.bx_state_upload(self.h, ct.byref(s)), 'bx_state_upload')
@@ -278,9 +294,13 @@ class BatchEngine(ClusterEngine):
                 e = e[:, 0]
             ce.append(e)
         vm, cc, cam, cenv = cat('vm', 0), cat('cc_cells', 1), cat('cc_at_mem', 1), _c(np.stack(ce))
+        for a, n, k in ((vm, self.M, 'vm'), (cc, self.I * self.C, 'cc_cells'), (cam, self.I * self.M, 'cc_at_mem'),
+                        (cenv, self.n_clusters * self.I, 'cc_env')):
+            _need(a, n, k)
         go = None
         if self.vgj and all(s.get('gjopen') is not None for s in states):
             go = cat('gjopen', 0)
+            _need(go, self.M, 'gjopen')
         st = _lib.BxState(_lib.dptr(vm), _lib.dptr(cc), _lib.dptr(cam), _lib.dptr(cenv), None, None,
                           _lib.dptr(go))
         _lib.check(self.lib.bx_state_upload(self.h, ct.byref(st)), 'bx_state_upload')
@@ -289,6 +309,9 @@ class BatchEngine(ClusterEngine):
         """Upload the concatenated state directly (cc_env is [n_clusters, n_ions]);
         the arrays are passed to the C ABI as they are (e.g. pinned views)."""
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (vm, cc_cells, cc_at_mem, cc_env)]
+        for a, n, k in zip(arrs, (self.M, self.I * self.C, self.I * self.M, self.n_clusters * self.I),
+                           ('vm', 'cc_cells', 'cc_at_mem', 'cc_env')):
+            _need(a, n, k)
         st = _lib.BxState(*[_lib.dptr(a) for a in arrs], None, None, None)
         _lib.check(self.lib.bx_state_upload(self.h, ct.byref(st)), 'bx_state_upload')
 

@@ -247,6 +247,8 @@ def test_upload_checks_and_download_into_given_arrays(precision):
             eng.upload(**bad)
         with pytest.raises(BxLibraryError):
             eng.step(1)                      # no state after a failed upload
+        with pytest.raises(ValueError, match='vm: expected'):
+            eng.upload(**dict(st, vm=st['vm'][:-1]))   # refused before the C library reads it
         if precision == 'split':
             bad = dict(st)
             vm = st['vm'].copy()
