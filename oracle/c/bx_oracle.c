@@ -16,8 +16,10 @@
  *     membrane-flux segment sum per cell, the well-mixed environment mean,
  *     the gap-junction segment sum, no_negs;
  *   update_V (sim.py:2007-2029): rho = sum_i z_i F c_i, vm = rho diviterm / cm.
- * Voltage-gated gap junctions and the Ca-ATPase are not restated here (the
- * NumPy oracle covers them); callers pass configurations without them.
+ * Voltage-gated gap junctions (Gap_Junction.run, channels/gap_junction.py:
+ * 52-75, once per ion before that ion's gap-junction flux) and the Ca-ATPase
+ * of ca_handler (sim.py:2126-2155, after the ion loop) are restated as well;
+ * the polarizable Vmem form is not (the NumPy oracle covers it).
  */
 #include <math.h>
 #include <stdint.h>
@@ -46,6 +48,9 @@ typedef struct bxo_cluster {
   double D_gj[BXO_MAX_IONS];
   double F, R, T, dt, cm, tm, gj_surface, gj_block, gj_len, nakatp_block;
   double alpha_NaK, KmNK_Na, KmNK_K, KmNK_ATP, cATP, cADP, cPi, deltaGATP, vol_env;
+  int32_t vgj;               /* voltage-gated gap junctions: gjopen is state */
+  int32_t iCa;               /* Ca2+ row; the Ca-ATPase runs when iCa >= 0 and alpha_Ca > 0 */
+  double gj_vthresh, gj_min, alpha_Ca, KmCa_Ca, KmCa_ATP;
 } bxo_cluster;
 
 /* GHK flux from A (outside) into B (inside), sim_toolbox.py:18-69 */
@@ -74,6 +79,32 @@ static inline double pump_fna(const bxo_cluster* k, double cNai, double cNao, do
   return -3 * k->nakatp_block * k->alpha_NaK * fwd_co * (1 - (Q / Keq));
 }
 
+/* Gap_Junction.run: implicit Euler step of the open fraction (ms units), then
+ * the block factor; Harris et al. (1983) rates */
+static inline double gj_run(const bxo_cluster* k, double g, double vgj) {
+  const double V1 = 1.0e3 * fabs(vgj);
+  const double alpha = 0.0013 * exp(-0.077 * (V1 - k->gj_vthresh));
+  double beta = 0.0013 * exp(0.14 * (V1 - k->gj_vthresh));
+  beta = beta / (1 + 50 * beta);
+  const double dt = k->dt * 1e3;
+  return k->gj_block * ((g + dt * (alpha + beta * k->gj_min)) / (1 + alpha * dt + beta * dt));
+}
+
+/* pumpCaATP (sim_toolbox.py:124-180), into the cell positive; both
+ * concentrations clamped at zero first (no_negs) */
+static inline double pump_fca(const bxo_cluster* k, double cCai, double cCao, double Vm) {
+  cCai = cCai > 0.0 ? cCai : 0.0;
+  cCao = cCao > 0.0 ? cCao : 0.0;
+  const double Qnumo = k->cADP * k->cPi * cCao;
+  double Qdenomo = k->cATP * cCai;
+  if (Qdenomo == 0.0) Qdenomo = 1.0e-16;
+  const double Q = Qnumo / Qdenomo;
+  const double Keq = exp(-(k->deltaGATP / (k->R * k->T) - 2 * ((k->F * Vm) / (k->R * k->T))));
+  const double numo_E = (cCai / k->KmCa_Ca) * (k->cATP / k->KmCa_ATP);
+  const double denomo_E = (1 + (cCai / k->KmCa_Ca)) * (1 + (k->cATP / k->KmCa_ATP));
+  return -k->alpha_Ca * (numo_E / denomo_E) * (1 - (Q / Keq));
+}
+
 int bxo_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
@@ -84,12 +115,14 @@ int bxo_max_threads(void) {
 
 /* Advance n_steps.  State: vm [M], cc_cells [I][C], cc_mem [I][C] (BETSE's
  * cc_at_mem, constant over each cell's membranes), cc_env [I] (the well-mixed
- * environment).  threads <= 0 uses every thread OpenMP offers.  Returns 0, or
- * 1 when a concentration or Vmem became NaN (check_v / no_negs). */
+ * environment), gjopen [M] (with vgj).  threads <= 0 uses every thread OpenMP
+ * offers.  Returns 0, or 1 when a concentration or Vmem became NaN (check_v /
+ * no_negs). */
 int bxo_step_noecm(const bxo_cluster* k, double* vm, double* cc_cells, double* cc_mem, double* cc_env,
-                   int n_steps, int threads) {
+                   double* gjopen, int n_steps, int threads) {
   const int C = k->C, M = k->M, I = k->I;
-  if (I <= 0 || I > BXO_MAX_IONS || C <= 0 || M <= 0) return 2;
+  if (I <= 0 || I > BXO_MAX_IONS || C <= 0 || M <= 0 || (k->vgj && !gjopen)) return 2;
+  const int ca_on = k->iCa >= 0 && k->iCa < I && k->alpha_Ca > 0.0;
 #ifdef _OPENMP
   if (threads > 0) omp_set_num_threads(threads);
 #else
@@ -128,11 +161,23 @@ int bxo_step_noecm(const bxo_cluster* k, double* vm, double* cc_cells, double* c
         v = v + BXO_NONCE;
         vn = vn + BXO_NONCE;
         const double vgj = vn - v;
-        const double gjopen = k->gj_block * k->gj_w[m];
-        double fg = electroflux(cin, cc_mem[(size_t)i * C + cn], k->D_gj[i] * k->gj_surface * gjopen,
+        double go;
+        if (k->vgj) {
+          gjopen[m] = gj_run(k, gjopen[m], vgj);
+          go = gjopen[m];
+        } else {
+          go = k->gj_block * k->gj_w[m];
+        }
+        double fg = electroflux(cin, cc_mem[(size_t)i * C + cn], k->D_gj[i] * k->gj_surface * go,
                                 k->gj_len, k->zs[i], vgj, k->F, k->R, k->T);
         if (k->bflag[m]) fg = 0.0;
         fgj[(size_t)i * M + m] = 0.0 + fg;
+      }
+      /* ca_handler after the ion loop: the cell side is cc_cells at the start
+       * of the step (update_intra), vm carries the I in-place nonces */
+      if (ca_on) {
+        const int i = k->iCa;
+        fmem[(size_t)i * M + m] += pump_fca(k, cc_cells[(size_t)i * C + c], cc_env[i], v);
       }
     }
     /* ---- environment: mean over membranes of c_env - f sa / vol_env dt */

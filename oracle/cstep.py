@@ -45,7 +45,9 @@ class _Cluster(ct.Structure):
                 ('zs', ct.c_double * MAX_IONS), ('D_gj', ct.c_double * MAX_IONS)] + \
         [(n, ct.c_double) for n in ('F', 'R', 'T', 'dt', 'cm', 'tm', 'gj_surface', 'gj_block', 'gj_len',
                                     'nakatp_block', 'alpha_NaK', 'KmNK_Na', 'KmNK_K', 'KmNK_ATP', 'cATP',
-                                    'cADP', 'cPi', 'deltaGATP', 'vol_env')]
+                                    'cADP', 'cPi', 'deltaGATP', 'vol_env')] + \
+        [('vgj', ct.c_int32), ('iCa', ct.c_int32)] + \
+        [(n, ct.c_double) for n in ('gj_vthresh', 'gj_min', 'alpha_Ca', 'KmCa_Ca', 'KmCa_ATP')]
 
 
 _lib = None
@@ -59,7 +61,7 @@ def load():
         except OSError:         # a library built for another machine: rebuild here
             lib = ct.CDLL(build(force=True))
         lib.bxo_step_noecm.restype = ct.c_int
-        lib.bxo_step_noecm.argtypes = [ct.POINTER(_Cluster)] + [ct.c_void_p] * 4 + [ct.c_int, ct.c_int]
+        lib.bxo_step_noecm.argtypes = [ct.POINTER(_Cluster)] + [ct.c_void_p] * 5 + [ct.c_int, ct.c_int]
         lib.bxo_max_threads.restype = ct.c_int
         _lib = lib
     return _lib
@@ -81,9 +83,6 @@ class Stepper:
     def __init__(self, g, p, s, threads=0):
         if bool(getattr(p, 'is_ecm', False)):
             raise ValueError('the C restatement covers the step without extracellular spaces')
-        if bool(getattr(p, 'v_sensitive_gj', False)) or (getattr(p, 'iCa', -1) >= 0
-                                                           and float(getattr(p, 'alpha_Ca', 0.0)) > 0):
-            raise ValueError('voltage-gated gap junctions and the Ca-ATPase are not restated in C')
         if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
             raise ValueError('the polarizable Vmem update is not restated in C')
         self.lib = load()
@@ -122,6 +121,13 @@ class Stepper:
         k.gj_block = float(getattr(p, 'gj_block', 1.0))
         k.nakatp_block = float(getattr(p, 'nakatp_block', 1.0))
         k.gj_len = float(g.gj_len)
+        k.vgj = int(bool(getattr(p, 'v_sensitive_gj', False)))
+        k.iCa = int(getattr(p, 'iCa', -1))
+        k.alpha_Ca = float(getattr(p, 'alpha_Ca', 0.0))
+        k.KmCa_Ca = float(getattr(p, 'KmCa_Ca', 1e-3))
+        k.KmCa_ATP = float(getattr(p, 'KmCa_ATP', 0.5))
+        k.gj_vthresh = float(getattr(p, 'gj_vthresh', 15.0))
+        k.gj_min = float(getattr(p, 'gj_min', 0.10))
         self.k = k
         self.C, self.M, self.I = C, M, I
         self.m2c = m2c
@@ -132,15 +138,23 @@ class Stepper:
         self.ccm = np.ascontiguousarray(cam[:, first])
         ce = np.asarray(s.cc_env, np.float64)
         self.cenv = np.ascontiguousarray(ce[:, 0] if ce.ndim == 2 else ce).copy()
+        # the open fraction with gating (sim.gjopen; the static weights before the first step)
+        go = getattr(s, 'gjopen', None)
+        self.gjopen = (np.ascontiguousarray(go if go is not None else kp['gjw'], np.float64).copy()
+                       if k.vgj else None)
 
     def step(self, n=1):
         rc = self.lib.bxo_step_noecm(ct.byref(self.k), _ptr(self.vm), _ptr(self.cc), _ptr(self.ccm),
-                                     _ptr(self.cenv), int(n), self.threads)
+                                     _ptr(self.cenv), None if self.gjopen is None else _ptr(self.gjopen),
+                                     int(n), self.threads)
         if rc == 1:
             raise FloatingPointError('NaN concentration or Vmem (check_v / no_negs)')
         if rc != 0:
             raise RuntimeError(f'bxo_step_noecm failed ({rc})')
 
     def state(self):
-        return dict(vm=self.vm.copy(), cc_cells=self.cc.copy(), cc_at_mem=self.ccm[:, self.m2c].copy(),
-                    cc_env=np.repeat(self.cenv[:, None], self.M, axis=1))
+        out = dict(vm=self.vm.copy(), cc_cells=self.cc.copy(), cc_at_mem=self.ccm[:, self.m2c].copy(),
+                   cc_env=np.repeat(self.cenv[:, None], self.M, axis=1))
+        if self.gjopen is not None:
+            out['gjopen'] = self.gjopen.copy()
+        return out

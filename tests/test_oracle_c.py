@@ -5,7 +5,7 @@ import pytest
 
 import golden_io as gi
 
-CASES = [c for c in gi.CASES if c.startswith('noecm') and not c.endswith(('_vgj', '_ca', '_pol'))]
+CASES = [c for c in gi.CASES if c.startswith('noecm') and not c.endswith('_pol')]
 
 
 @pytest.fixture(scope='module')
@@ -33,6 +33,8 @@ def test_c_restatement_matches_betse(cstep, name):
         assert gi.rel_err(got['cc_cells'], d[f's{cp}_cc_cells']) < 1e-10
         assert gi.rel_err(got['cc_at_mem'], d[f's{cp}_cc_at_mem']) < 1e-10
         assert gi.rel_err(got['cc_env'], d[f's{cp}_cc_env']) < 1e-10
+        if 'gjopen' in got:
+            assert gi.rel_err(got['gjopen'], d[f's{cp}_gjopen']) < 1e-10
 
 
 def test_c_restatement_matches_numpy_oracle(cstep):
@@ -61,8 +63,8 @@ def test_c_restatement_thread_count_independent(cstep):
 
 
 def test_c_restatement_refuses_what_it_does_not_cover(cstep):
-    d = gi.load('noecm_r50_s9_vgj')
-    with pytest.raises(ValueError, match='voltage-gated'):
+    d = gi.load('noecm_r50_s17_pol')
+    with pytest.raises(ValueError, match='polarizable'):
         cstep.Stepper(gi.geometry(d), gi.params(d), gi.state(d))
     d = gi.load('ecm_r50_s3')
     with pytest.raises(ValueError, match='extracellular'):
