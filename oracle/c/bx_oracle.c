@@ -123,9 +123,11 @@ int bxo_step_noecm(const bxo_cluster* k, double* vm, double* cc_cells, double* c
   const int C = k->C, M = k->M, I = k->I;
   if (I <= 0 || I > BXO_MAX_IONS || C <= 0 || M <= 0 || (k->vgj && !gjopen)) return 2;
   const int ca_on = k->iCa >= 0 && k->iCa < I && k->alpha_Ca > 0.0;
+  /* the thread count applies to this call's parallel regions only */
 #ifdef _OPENMP
-  if (threads > 0) omp_set_num_threads(threads);
+  const int nt = threads > 0 ? threads : omp_get_max_threads();
 #else
+  const int nt = 1;
   (void)threads;
 #endif
   double* fmem = (double*)malloc(sizeof(double) * (size_t)I * M);
@@ -140,7 +142,7 @@ int bxo_step_noecm(const bxo_cluster* k, double* vm, double* cc_cells, double* c
   int bad = 0;
   for (int step = 0; step < n_steps && !bad; ++step) {
     /* ---- membranes: pump, GHK and gap-junction fluxes */
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(nt)
     for (int m = 0; m < M; ++m) {
       const int64_t c = k->m2c[m], n = k->nn[m], cn = k->m2c[n];
       double fNa = 0.0, fK = 0.0;
@@ -181,7 +183,7 @@ int bxo_step_noecm(const bxo_cluster* k, double* vm, double* cc_cells, double* c
       }
     }
     /* ---- environment: mean over membranes of c_env - f sa / vol_env dt */
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(nt)
     for (int b = 0; b < nblk; ++b) {
       const int m0 = b * kBlk, m1 = (m0 + kBlk < M) ? m0 + kBlk : M;
       for (int i = 0; i < I; ++i) {
@@ -192,7 +194,7 @@ int bxo_step_noecm(const bxo_cluster* k, double* vm, double* cc_cells, double* c
       }
     }
     /* ---- cells: update_all_concs and update_V */
-#pragma omp parallel for schedule(static) reduction(|| : bad)
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(|| : bad)
     for (int c = 0; c < C; ++c) {
       const int64_t a0 = k->cell_ptr[c], a1 = k->cell_ptr[c + 1];
       double rho = 0.0;
