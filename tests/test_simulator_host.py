@@ -125,3 +125,52 @@ def test_step_params_reject_a_ca_row_out_of_range():
     sp = StepParams.from_betse(p, sim).replace(iCa=9)
     with pytest.raises(ValueError, match='iCa'):
         sp.to_c()
+
+
+class _FakeEngine:
+    """Stands in for ClusterEngine: arrays of the shapes the device returns."""
+
+    def __init__(self, I, C, M, shape, ecm):
+        self.I, self.C, self.M, self.ecm = I, C, M, ecm
+        self.G = int(np.prod(shape))
+        self.shape = shape
+
+    def download(self):
+        st = dict(vm=np.zeros(self.M), cc_cells=np.ones((self.I, self.C)), cc_at_mem=np.ones((self.I, self.M)),
+                  cc_env=np.ones((self.I, self.G)) if self.ecm else np.ones(self.I))
+        if self.ecm:
+            st.update(E_env_x=np.zeros(self.G), E_env_y=np.zeros(self.G))
+        return st
+
+    def outputs(self):
+        I, C, M = self.I, self.C, self.M
+        o = dict(fluxes_mem=np.zeros((I, M)), fluxes_gj=np.zeros((I, M)), rate_NaKATP=np.zeros(M),
+                 rho_cells=np.zeros(C), Jn=np.zeros(M), I_mem=np.zeros(M), J_cell_x=np.zeros(C),
+                 J_cell_y=np.zeros(C), Jc=np.zeros(M), vm_ave=np.zeros(C), dvm=np.zeros(M),
+                 E_cell_x=np.zeros(C), E_cell_y=np.zeros(C), Emc=np.zeros(M), E_gj_x=np.zeros(M),
+                 E_gj_y=np.zeros(M), gjopen=np.ones(M), sigma_cell=np.ones(C))
+        if self.ecm:
+            o['rho_env'] = np.zeros(self.G)
+        return o
+
+    def env_fields(self, D_env_weight=None):
+        return {k: np.zeros(self.G) for k in ('v_env', 'E_env_x', 'E_env_y', 'J_env_x', 'J_env_y', 'B_field')}
+
+
+@pytest.mark.parametrize('ecm', [False, True])
+def test_mirror_leaves_what_write2storage_reads(ecm):
+    """After a sampled step the Simulator holds, under BETSE's names and shapes,
+    every step quantity Simulator.write2storage stores (sim.py:1789-1884)."""
+    I, C, M, shape = 6, 10, 46, (4, 5)
+    cells = SimpleNamespace(grid_shape=shape, mem_vects_flat=np.zeros((M, 4)),
+                            map_mem2ecm=np.zeros(M, np.int64))
+    sim = SimpleNamespace()
+    simulator._mirror(sim, cells, _FakeEngine(I, C, M, shape, ecm), True, None)
+    G = int(np.prod(shape))
+    want = dict(vm=(M,), cc_cells=(I, C), cc_env=(I, G) if ecm else (I, M), E_gj_x=(M,), E_gj_y=(M,),
+                I_mem=(M,), J_cell_x=(C,), J_cell_y=(C,), J_env_x=shape, J_env_y=shape, gjopen=(M,),
+                rate_NaKATP=(M,), rho_cells=(C,), v_env=(G,), vm_ave=(C,), E_env_x=shape, E_env_y=shape,
+                B_field=(G,), cc_at_mem=(I, M), Eme=(M,))
+    for k, shp in want.items():
+        assert hasattr(sim, k), k
+        assert np.shape(getattr(sim, k)) == shp, (k, np.shape(getattr(sim, k)), shp)
