@@ -192,13 +192,14 @@ class Sweep:
                 'cc_env': np.concatenate([x['cc_env'] for x in d])}
 
 
-def _c_steppers(clusters):
-    """C restatements (oracle/c, OpenMP) of no-ECM clusters, or None when
-    the C oracle cannot be built or does not cover the configuration."""
+def _c_steppers(clusters, D_env=None):
+    """C restatements (oracle/c, OpenMP) of the clusters, or None when the C
+    oracle cannot be built or does not cover the configuration."""
     try:
         from oracle import cstep
         from oracle.adapt import from_workload
-        return [cstep.Stepper(*from_workload(g, p, Dm, st)) for g, p, Dm, st in clusters], cstep.max_threads()
+        return ([cstep.Stepper(*from_workload(g, p, Dm, st, D_env)) for g, p, Dm, st in clusters],
+                cstep.max_threads())
     except Exception as e:
         print(f'C restatement unavailable, timing the NumPy oracle: {e}', file=sys.stderr)
         return None, 1
@@ -206,15 +207,16 @@ def _c_steppers(clusters):
 
 def cpu_baseline(g, p, Dm, st, budget_s=12.0, D_env=None):
     """BETSE's step restated for the CPU, on a bounded sample: the whole
-    cluster, as many time steps as fit in about budget_s seconds.  Without
-    extracellular spaces it is the C restatement on every host thread
-    (OpenMP); with them, the NumPy oracle on one thread."""
-    steppers, threads = (None, 1) if p.is_ecm else _c_steppers([(g, p, Dm, st)])
+    cluster, as many time steps as fit in about budget_s seconds, with the C
+    restatement on every host thread (OpenMP); the NumPy oracle on one thread
+    if the C one cannot be built."""
+    steppers, threads = _c_steppers([(g, p, Dm, st)], D_env)
     if steppers:
         s0 = steppers[0]
+        s0.step(1)                   # the thread pool and first touches
         t0 = time.perf_counter()
-        s0.step(1)
-        one = time.perf_counter() - t0
+        s0.step(2)
+        one = (time.perf_counter() - t0) / 2
         n = max(1, int(budget_s / max(one, 1e-4)) - 1)
         t0 = time.perf_counter()
         s0.step(n)
@@ -246,6 +248,7 @@ def cpu_baseline_sweep(gs, ps, Dms, sts, budget_s=12.0):
     if not steppers:
         return cpu_baseline(gs[0], ps[0], Dms[0], sts[0], budget_s)
     M = sum(g.n_mems for g in gs)
+    steppers[0].step(1)              # the thread pool and first touches
     t0 = time.perf_counter()
     for s in steppers:
         s.step(1)

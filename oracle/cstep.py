@@ -2,9 +2,9 @@
 INFRASTRUCTURE AND CPU BASELINE ONLY.
 
 ``build()`` compiles it with gcc and OpenMP into ``oracle/_build/``;
-``Stepper`` advances a no-ECM cluster given in the records ``oracle.step``
-reads (``oracle.adapt.from_workload`` or the golden fixtures), on every host
-thread OpenMP offers unless told otherwise.
+``Stepper`` advances a cluster, with or without extracellular spaces, given in
+the records ``oracle.step`` reads (``oracle.adapt.from_workload`` or the
+golden fixtures), on every host thread OpenMP offers unless told otherwise.
 """
 from __future__ import annotations
 
@@ -47,7 +47,12 @@ class _Cluster(ct.Structure):
                                     'nakatp_block', 'alpha_NaK', 'KmNK_Na', 'KmNK_K', 'KmNK_ATP', 'cATP',
                                     'cADP', 'cPi', 'deltaGATP', 'vol_env')] + \
         [('vgj', ct.c_int32), ('iCa', ct.c_int32)] + \
-        [(n, ct.c_double) for n in ('gj_vthresh', 'gj_min', 'alpha_Ca', 'KmCa_Ca', 'KmCa_ATP')]
+        [(n, ct.c_double) for n in ('gj_vthresh', 'gj_min', 'alpha_Ca', 'KmCa_Ca', 'KmCa_ATP')] + \
+        [('is_ecm', ct.c_int32), ('ny', ct.c_int32), ('nx', ct.c_int32), ('pad1', ct.c_int32),
+         ('map_env', ct.c_void_p), ('D_env', ct.c_void_p), ('msa_env', ct.c_void_p),
+         ('c_bound', ct.c_double * MAX_IONS)] + \
+        [(n, ct.c_double) for n in ('delta', 'cell_height', 'q', 'kb', 'eo', 'er', 'ko_env', 'cell_radius',
+                                    'true_cell_size', 'sharpness')]
 
 
 _lib = None
@@ -60,8 +65,8 @@ def load():
             lib = ct.CDLL(build())
         except OSError:         # a library built for another machine: rebuild here
             lib = ct.CDLL(build(force=True))
-        lib.bxo_step_noecm.restype = ct.c_int
-        lib.bxo_step_noecm.argtypes = [ct.POINTER(_Cluster)] + [ct.c_void_p] * 5 + [ct.c_int, ct.c_int]
+        lib.bxo_step.restype = ct.c_int
+        lib.bxo_step.argtypes = [ct.POINTER(_Cluster)] + [ct.c_void_p] * 7 + [ct.c_int, ct.c_int]
         lib.bxo_max_threads.restype = ct.c_int
         _lib = lib
     return _lib
@@ -76,13 +81,13 @@ def _ptr(a):
 
 
 class Stepper:
-    """A no-ECM cluster on the C restatement.  ``g``/``p``/``s`` are the records
+    """A cluster on the C restatement.  ``g``/``p``/``s`` are the records
     ``oracle.step`` reads (BETSE attribute names); the state is copied in and
     ``state()`` returns it in the same shapes."""
 
     def __init__(self, g, p, s, threads=0):
-        if bool(getattr(p, 'is_ecm', False)):
-            raise ValueError('the C restatement covers the step without extracellular spaces')
+        if s.Phi_b is not None and np.any(np.asarray(s.Phi_b) != 0):
+            raise ValueError('the C restatement takes no boundary potential (Phi_b = 0)')
         if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
             raise ValueError('the polarizable Vmem update is not restated in C')
         self.lib = load()
@@ -128,6 +133,20 @@ class Stepper:
         k.KmCa_ATP = float(getattr(p, 'KmCa_ATP', 0.5))
         k.gj_vthresh = float(getattr(p, 'gj_vthresh', 15.0))
         k.gj_min = float(getattr(p, 'gj_min', 0.10))
+        self.ecm = bool(getattr(p, 'is_ecm', False))
+        if self.ecm:
+            ny, nx = (int(x) for x in g.grid_shape)
+            G = ny * nx
+            kp.update(map_env=np.ascontiguousarray(g.map_mem2ecm, np.int64),
+                      D_env=np.ascontiguousarray(np.asarray(g.D_env, np.float64).reshape(I, G)),
+                      msa_env=np.ascontiguousarray(np.ravel(g.memSa_per_envSquare), np.float64))
+            k.is_ecm, k.ny, k.nx = 1, ny, nx
+            k.map_env, k.D_env, k.msa_env = _ptr(kp['map_env']), _ptr(kp['D_env']), _ptr(kp['msa_env'])
+            for i in range(I):
+                k.c_bound[i] = float(np.ravel(p.c_env_bound)[i])
+            for n in ('cell_height', 'q', 'kb', 'eo', 'er', 'cell_radius', 'true_cell_size', 'sharpness'):
+                setattr(k, n, float(getattr(p, n)))
+            k.delta, k.ko_env = float(g.delta), float(g.ko_env)
         self.k = k
         self.C, self.M, self.I = C, M, I
         self.m2c = m2c
@@ -137,16 +156,23 @@ class Stepper:
         first = kp['ptr'][:-1]
         self.ccm = np.ascontiguousarray(cam[:, first])
         ce = np.asarray(s.cc_env, np.float64)
-        self.cenv = np.ascontiguousarray(ce[:, 0] if ce.ndim == 2 else ce).copy()
+        if self.ecm:
+            self.cenv = np.ascontiguousarray(ce.reshape(I, -1)).copy()
+            self.grid_shape = tuple(int(x) for x in g.grid_shape)
+            self.Ex = np.ascontiguousarray(np.ravel(s.E_env_x), np.float64).copy()
+            self.Ey = np.ascontiguousarray(np.ravel(s.E_env_y), np.float64).copy()
+        else:
+            self.cenv = np.ascontiguousarray(ce[:, 0] if ce.ndim == 2 else ce).copy()
+            self.Ex = self.Ey = None
         # the open fraction with gating (sim.gjopen; the static weights before the first step)
         go = getattr(s, 'gjopen', None)
         self.gjopen = (np.ascontiguousarray(go if go is not None else kp['gjw'], np.float64).copy()
                        if k.vgj else None)
 
     def step(self, n=1):
-        rc = self.lib.bxo_step_noecm(ct.byref(self.k), _ptr(self.vm), _ptr(self.cc), _ptr(self.ccm),
-                                     _ptr(self.cenv), None if self.gjopen is None else _ptr(self.gjopen),
-                                     int(n), self.threads)
+        opt = lambda a: None if a is None else _ptr(a)  # noqa: E731
+        rc = self.lib.bxo_step(ct.byref(self.k), _ptr(self.vm), _ptr(self.cc), _ptr(self.ccm), _ptr(self.cenv),
+                               opt(self.gjopen), opt(self.Ex), opt(self.Ey), int(n), self.threads)
         if rc == 1:
             raise FloatingPointError('NaN concentration or Vmem (check_v / no_negs)')
         if rc != 0:
@@ -154,7 +180,10 @@ class Stepper:
 
     def state(self):
         out = dict(vm=self.vm.copy(), cc_cells=self.cc.copy(), cc_at_mem=self.ccm[:, self.m2c].copy(),
-                   cc_env=np.repeat(self.cenv[:, None], self.M, axis=1))
+                   cc_env=self.cenv.copy() if self.ecm else np.repeat(self.cenv[:, None], self.M, axis=1))
+        if self.ecm:
+            out['E_env_x'] = self.Ex.reshape(self.grid_shape).copy()
+            out['E_env_y'] = self.Ey.reshape(self.grid_shape).copy()
         if self.gjopen is not None:
             out['gjopen'] = self.gjopen.copy()
         return out

@@ -1,11 +1,12 @@
 """The C restatement of the step (``oracle/c/bx_oracle.c``, the multi-threaded
-CPU baseline) against BETSE's golden states and the NumPy oracle.  CPU only."""
+CPU baseline) against BETSE's golden states and the NumPy oracle, with and
+without extracellular spaces.  CPU only."""
 import numpy as np
 import pytest
 
 import golden_io as gi
 
-CASES = [c for c in gi.CASES if c.startswith('noecm') and not c.endswith('_pol')]
+CASES = [c for c in gi.CASES if not c.endswith('_pol')]
 
 
 @pytest.fixture(scope='module')
@@ -37,18 +38,22 @@ def test_c_restatement_matches_betse(cstep, name):
             assert gi.rel_err(got['gjopen'], d[f's{cp}_gjopen']) < 1e-10
 
 
-def test_c_restatement_matches_numpy_oracle(cstep):
+@pytest.mark.parametrize('name', ['noecm_r50_s7', 'ecm_r40_s5_sharp'])
+def test_c_restatement_matches_numpy_oracle(cstep, name):
     import oracle
-    d = gi.load('noecm_r50_s7')
+    d = gi.load(name)
     g, p, s = gi.geometry(d), gi.params(d), gi.state(d)
     st = cstep.Stepper(g, p, s)
     st.step(25)
     oracle.run(g, p, s, 25)
     got = st.state()
     for k in ('cc_cells', 'cc_at_mem', 'cc_env'):
-        assert gi.rel_err(got[k], getattr(s, k)) < 1e-12, k
+        assert gi.rel_err(got[k], np.asarray(getattr(s, k)).reshape(got[k].shape)) < 1e-12, k
     ok, err, bound = gi.vm_err_ok(d, got['vm'], s.vm, s.cc_cells, rel=1e-12)
     assert ok, (err, bound)
+    if bool(p.is_ecm):
+        for k in ('E_env_x', 'E_env_y'):
+            assert gi.rel_err(got[k], getattr(s, k)) < 1e-9, k
 
 
 def test_c_restatement_thread_count_independent(cstep):
@@ -67,8 +72,10 @@ def test_c_restatement_refuses_what_it_does_not_cover(cstep):
     with pytest.raises(ValueError, match='polarizable'):
         cstep.Stepper(gi.geometry(d), gi.params(d), gi.state(d))
     d = gi.load('ecm_r50_s3')
-    with pytest.raises(ValueError, match='extracellular'):
-        cstep.Stepper(gi.geometry(d), gi.params(d), gi.state(d))
+    s = gi.state(d)
+    s.Phi_b = np.ones_like(s.Phi_b)
+    with pytest.raises(ValueError, match='Phi_b'):
+        cstep.Stepper(gi.geometry(d), gi.params(d), s)
 
 
 def test_c_restatement_on_ragged_cells(cstep):
