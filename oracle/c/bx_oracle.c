@@ -26,9 +26,10 @@
  *     the environment charge on the touched grid cells, a sigma-1 Gaussian
  *     with zero padding, the screened gradient.
  * Voltage-gated gap junctions (Gap_Junction.run, channels/gap_junction.py:
- * 52-75, once per ion before that ion's gap-junction flux) and the Ca-ATPase
- * of ca_handler (sim.py:2126-2155, after the ion loop) are restated as well;
- * the polarizable Vmem form is not (the NumPy oracle covers it).
+ * 52-75, once per ion before that ion's gap-junction flux), the Ca-ATPase of
+ * ca_handler (sim.py:2126-2155, after the ion loop) and the polarizable Vmem
+ * form of update_V (sim.py:2048-2058, from get_current's smoothed Jn,
+ * ion_current.py:19-33) are restated as well.
  */
 #include <math.h>
 #include <stdint.h>
@@ -67,6 +68,13 @@ typedef struct bxo_cluster {
   const double* msa_env;     /* [G] memSa_per_envSquare */
   double c_bound[BXO_MAX_IONS];  /* c_env_bound: the grid-edge concentration */
   double delta, cell_height, q, kb, eo, er, ko_env, cell_radius, true_cell_size, sharpness;
+  /* cell polarizability (polar): Vmem is per-membrane state */
+  int32_t polar, pad2;
+  const double* R_rads;      /* [M] */
+  const double* sw_mem;      /* [M] smooth_weight_mem */
+  const double* sw_o;        /* [M] smooth_weight_o */
+  const double* cell_sa;     /* [C] */
+  double D_free[BXO_MAX_IONS];
 } bxo_cluster;
 
 /* GHK flux from A (outside) into B (inside), sim_toolbox.py:18-69 */
@@ -169,6 +177,7 @@ int bxo_step(const bxo_cluster* k, double* vm, double* cc_cells, double* cc_mem,
   const int ecm = k->is_ecm != 0, ny = k->ny, nx = k->nx, G = ecm ? ny * nx : 1;
   if (I <= 0 || I > BXO_MAX_IONS || C <= 0 || M <= 0 || (k->vgj && !gjopen)) return 2;
   if (ecm && (ny < 3 || nx < 3 || !k->map_env || !k->D_env || !k->msa_env || !E_env_x || !E_env_y)) return 2;
+  if (k->polar && (!k->R_rads || !k->sw_mem || !k->sw_o || !k->cell_sa)) return 2;
   const int ca_on = k->iCa >= 0 && k->iCa < I && k->alpha_Ca > 0.0;
   /* the thread count applies to this call's parallel regions only */
 #ifdef _OPENMP
@@ -339,7 +348,42 @@ int bxo_step(const bxo_cluster* k, double* vm, double* cc_cells, double* cc_mem,
       }
       const double vc = inv_cm * (rho * k->diviterm[c]);
       if (vc != vc) bad = 1;
-      for (int64_t m = a0; m < a1; ++m) vm[m] = vc;
+      if (!k->polar) {
+        for (int64_t m = a0; m < a1; ++m) vm[m] = vc;
+      } else {
+        /* get_current's smoothed Jn (ion_current.py:22-33) and sigma_cell
+         * (sim.py:2016-2017), then the implicit update of each membrane's
+         * vm, which carries the I in-place nonces (sim.py:2058-2059) */
+        double sj = 0.0, sig = 0.0;
+        for (int64_t m = a0; m < a1; ++m) {
+          double jm = 0.0, jg = 0.0;
+          for (int i = 0; i < I; ++i) {
+            jm += (k->zs[i] * k->F) * fmem[(size_t)i * M + m];
+            jg += (k->zs[i] * k->F) * fgj[(size_t)i * M + m];
+          }
+          sj += (-jm + jg) * k->mem_sa[m];
+        }
+        for (int i = 0; i < I; ++i)
+          sig += ((k->zs[i] * k->zs[i]) * (k->F * k->F) * cc_cells[(size_t)i * C + c] * k->D_free[i] * 0.1) /
+                 (k->R * k->T);
+        sig = sig / (double)I;
+        const double jave = sj / k->cell_sa[c];
+        for (int64_t m = a0; m < a1; ++m) {
+          double jm = 0.0, jg = 0.0;
+          for (int i = 0; i < I; ++i) {
+            jm += (k->zs[i] * k->F) * fmem[(size_t)i * M + m];
+            jg += (k->zs[i] * k->F) * fgj[(size_t)i * M + m];
+          }
+          const double Jn = k->sw_mem[m] * (-jm + jg) + jave * k->sw_o[m];
+          double v = vm[m];
+          for (int q = 0; q < I; ++q) v = v + BXO_NONCE;
+          const double R = k->R_rads[m];
+          const double vn = (v - (k->dt / k->cm) * Jn + ((k->dt * sig * vc) / (k->cm * R))) /
+                            (1 + ((k->dt * sig) / (k->cm * R)));
+          if (vn != vn) bad = 1;
+          vm[m] = vn;
+        }
+      }
     }
     if (!ecm) {
       for (int i = 0; i < I; ++i) {

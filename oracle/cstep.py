@@ -52,7 +52,9 @@ class _Cluster(ct.Structure):
          ('map_env', ct.c_void_p), ('D_env', ct.c_void_p), ('msa_env', ct.c_void_p),
          ('c_bound', ct.c_double * MAX_IONS)] + \
         [(n, ct.c_double) for n in ('delta', 'cell_height', 'q', 'kb', 'eo', 'er', 'ko_env', 'cell_radius',
-                                    'true_cell_size', 'sharpness')]
+                                    'true_cell_size', 'sharpness')] + \
+        [('polar', ct.c_int32), ('pad2', ct.c_int32), ('R_rads', ct.c_void_p), ('sw_mem', ct.c_void_p),
+         ('sw_o', ct.c_void_p), ('cell_sa', ct.c_void_p), ('D_free', ct.c_double * MAX_IONS)]
 
 
 _lib = None
@@ -88,8 +90,6 @@ class Stepper:
     def __init__(self, g, p, s, threads=0):
         if s.Phi_b is not None and np.any(np.asarray(s.Phi_b) != 0):
             raise ValueError('the C restatement takes no boundary potential (Phi_b = 0)')
-        if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
-            raise ValueError('the polarizable Vmem update is not restated in C')
         self.lib = load()
         self.threads = int(threads)
         m2c = np.ascontiguousarray(g.mem_to_cells, np.int64)
@@ -133,6 +133,16 @@ class Stepper:
         k.KmCa_ATP = float(getattr(p, 'KmCa_ATP', 0.5))
         k.gj_vthresh = float(getattr(p, 'gj_vthresh', 15.0))
         k.gj_min = float(getattr(p, 'gj_min', 0.10))
+        if float(getattr(p, 'cell_polarizability', 0.0)) != 0.0:
+            kp.update(R_rads=np.ascontiguousarray(g.R_rads, np.float64),
+                      sw_mem=np.ascontiguousarray(g.smooth_weight_mem, np.float64),
+                      sw_o=np.ascontiguousarray(g.smooth_weight_o, np.float64),
+                      cell_sa=np.ascontiguousarray(g.cell_sa, np.float64))
+            k.polar = 1
+            k.R_rads, k.sw_mem, k.sw_o, k.cell_sa = (_ptr(kp['R_rads']), _ptr(kp['sw_mem']), _ptr(kp['sw_o']),
+                                                     _ptr(kp['cell_sa']))
+            for i in range(I):
+                k.D_free[i] = float(np.ravel(p.D_free)[i])
         self.ecm = bool(getattr(p, 'is_ecm', False))
         if self.ecm:
             ny, nx = (int(x) for x in g.grid_shape)

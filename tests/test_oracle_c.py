@@ -6,7 +6,7 @@ import pytest
 
 import golden_io as gi
 
-CASES = [c for c in gi.CASES if not c.endswith('_pol')]
+CASES = list(gi.CASES)
 
 
 @pytest.fixture(scope='module')
@@ -68,9 +68,6 @@ def test_c_restatement_thread_count_independent(cstep):
 
 
 def test_c_restatement_refuses_what_it_does_not_cover(cstep):
-    d = gi.load('noecm_r50_s17_pol')
-    with pytest.raises(ValueError, match='polarizable'):
-        cstep.Stepper(gi.geometry(d), gi.params(d), gi.state(d))
     d = gi.load('ecm_r50_s3')
     s = gi.state(d)
     s.Phi_b = np.ones_like(s.Phi_b)
