@@ -75,6 +75,8 @@ typedef struct bxo_cluster {
   const double* sw_o;        /* [M] smooth_weight_o */
   const double* cell_sa;     /* [C] */
   double D_free[BXO_MAX_IONS];
+  /* boundary potential Phi_b [G] (NULL: zero), read through map_env */
+  const double* phib;
 } bxo_cluster;
 
 /* GHK flux from A (outside) into B (inside), sim_toolbox.py:18-69 */
@@ -178,6 +180,7 @@ int bxo_step(const bxo_cluster* k, double* vm, double* cc_cells, double* cc_mem,
   if (I <= 0 || I > BXO_MAX_IONS || C <= 0 || M <= 0 || (k->vgj && !gjopen)) return 2;
   if (ecm && (ny < 3 || nx < 3 || !k->map_env || !k->D_env || !k->msa_env || !E_env_x || !E_env_y)) return 2;
   if (k->polar && (!k->R_rads || !k->sw_mem || !k->sw_o || !k->cell_sa)) return 2;
+  if (k->phib && !k->map_env) return 2;
   const int ca_on = k->iCa >= 0 && k->iCa < I && k->alpha_Ca > 0.0;
   /* the thread count applies to this call's parallel regions only */
 #ifdef _OPENMP
@@ -349,7 +352,8 @@ int bxo_step(const bxo_cluster* k, double* vm, double* cc_cells, double* cc_mem,
       const double vc = inv_cm * (rho * k->diviterm[c]);
       if (vc != vc) bad = 1;
       if (!k->polar) {
-        for (int64_t m = a0; m < a1; ++m) vm[m] = vc;
+        /* vm = rho diviterm / cm - Phi_b[map_mem2ecm] (sim.py:2029) */
+        for (int64_t m = a0; m < a1; ++m) vm[m] = k->phib ? vc - k->phib[k->map_env[m]] : vc;
       } else {
         /* get_current's smoothed Jn (ion_current.py:22-33) and sigma_cell
          * (sim.py:2016-2017), then the implicit update of each membrane's
@@ -431,7 +435,7 @@ int bxo_step(const bxo_cluster* k, double* vm, double* cc_cells, double* cc_mem,
           const int jj = gj + q - 4;
           a += gw[q] * ((jj >= 0 && jj < nx) ? tmp[gi * nx + jj] : 0.0);
         }
-        vsrc[g] = screen * a;      /* Phi_b is zero for this restatement */
+        vsrc[g] = screen * (k->phib ? a + k->phib[g] : a);   /* v_env = Gaussian + Phi_b */
       }
 #pragma omp parallel for schedule(static) num_threads(nt)
       for (int g = 0; g < G; ++g) {

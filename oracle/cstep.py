@@ -54,7 +54,8 @@ class _Cluster(ct.Structure):
         [(n, ct.c_double) for n in ('delta', 'cell_height', 'q', 'kb', 'eo', 'er', 'ko_env', 'cell_radius',
                                     'true_cell_size', 'sharpness')] + \
         [('polar', ct.c_int32), ('pad2', ct.c_int32), ('R_rads', ct.c_void_p), ('sw_mem', ct.c_void_p),
-         ('sw_o', ct.c_void_p), ('cell_sa', ct.c_void_p), ('D_free', ct.c_double * MAX_IONS)]
+         ('sw_o', ct.c_void_p), ('cell_sa', ct.c_void_p), ('D_free', ct.c_double * MAX_IONS),
+         ('phib', ct.c_void_p)]
 
 
 _lib = None
@@ -88,8 +89,6 @@ class Stepper:
     ``state()`` returns it in the same shapes."""
 
     def __init__(self, g, p, s, threads=0):
-        if s.Phi_b is not None and np.any(np.asarray(s.Phi_b) != 0):
-            raise ValueError('the C restatement takes no boundary potential (Phi_b = 0)')
         self.lib = load()
         self.threads = int(threads)
         m2c = np.ascontiguousarray(g.mem_to_cells, np.int64)
@@ -144,6 +143,11 @@ class Stepper:
             for i in range(I):
                 k.D_free[i] = float(np.ravel(p.D_free)[i])
         self.ecm = bool(getattr(p, 'is_ecm', False))
+        phib = getattr(s, 'Phi_b', None)
+        if phib is not None and np.any(np.asarray(phib) != 0):
+            kp.update(phib=np.ascontiguousarray(np.ravel(phib), np.float64),
+                      map_env=np.ascontiguousarray(g.map_mem2ecm, np.int64))
+            k.phib, k.map_env = _ptr(kp['phib']), _ptr(kp['map_env'])
         if self.ecm:
             ny, nx = (int(x) for x in g.grid_shape)
             G = ny * nx

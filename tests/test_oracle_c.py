@@ -67,12 +67,23 @@ def test_c_restatement_thread_count_independent(cstep):
         assert np.array_equal(out[0][k], out[1][k]), k
 
 
-def test_c_restatement_refuses_what_it_does_not_cover(cstep):
-    d = gi.load('ecm_r50_s3')
-    s = gi.state(d)
-    s.Phi_b = np.ones_like(s.Phi_b)
-    with pytest.raises(ValueError, match='Phi_b'):
-        cstep.Stepper(gi.geometry(d), gi.params(d), s)
+@pytest.mark.parametrize('name', ['noecm_r50_s7', 'ecm_r50_s3'])
+def test_c_restatement_with_a_boundary_potential(cstep, name):
+    """An applied boundary potential (sim.Phi_b) shifts vm and, with ECM,
+    v_env: the C restatement follows the NumPy oracle."""
+    import oracle
+    d = gi.load(name)
+    g, p, s = gi.geometry(d), gi.params(d), gi.state(d)
+    rng = np.random.default_rng(8)
+    s.Phi_b = rng.uniform(-2e-3, 2e-3, size=s.Phi_b.shape)
+    st = cstep.Stepper(g, p, s)
+    st.step(10)
+    oracle.run(g, p, s, 10)
+    got = st.state()
+    for k in ('cc_cells', 'cc_env'):
+        assert gi.rel_err(got[k], np.asarray(getattr(s, k)).reshape(got[k].shape)) < 1e-12, k
+    ok, err, bound = gi.vm_err_ok(d, got['vm'], s.vm, s.cc_cells, rel=1e-12)
+    assert ok, (err, bound)
 
 
 def test_c_restatement_on_ragged_cells(cstep):
