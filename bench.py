@@ -181,9 +181,6 @@ class Sweep:
     def upload(self, **_):
         self.e.upload_states(self.sts)
 
-    def upload_pinned(self, pin_states):
-        self.e.upload_states(pin_states)
-
     def download(self):
         d = self.e.download_states()
         return {'vm': np.concatenate([x['vm'] for x in d]),
