@@ -123,11 +123,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Offset (elements) of (r, k) inside a packed 128x64 tile.
-__host__ __device__ __forceinline__ int tile_off(int r, int k) {
-  return (((r >> 3) << 3) + (k >> 3)) * 64 + ((r & 7) << 3) + (k & 7);
-}
-
 struct GemmArgs {
   const __nv_bfloat16* a_hi;  // [Mt][Kt] tiles
   const __nv_bfloat16* a_lo;

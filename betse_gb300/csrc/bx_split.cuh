@@ -101,24 +101,6 @@ __device__ __forceinline__ float ghk_flux_fk(const GhkShared<float>& s, float ka
   }
 }
 
-// FP32 GHK flux (same identities as ghk_flux); the generic-charge branch
-// evaluates BETSE's formula directly in FP32.
-__device__ __forceinline__ float ghk_flux_f(const GhkShared<float>& s, int zcode, float zval,
-                                            float v_nonce, float F_RT, float cA, float cB,
-                                            float Dc, float inv_d) {
-  const float kk = Dc * s.a1 * inv_d;
-  switch (zcode) {
-    case 1:  return kk * (cB - cA * s.e1) * s.r;
-    case -1: return kk * (cB * s.e1 - cA) * s.r;
-    case 2:  { const float e2 = s.e1 * s.e1; return 2.f * kk * (cB - cA * e2) * s.r * s.q2; }
-    case -2: { const float e2 = s.e1 * s.e1; return 2.f * kk * (cB * e2 - cA) * s.r * s.q2; }
-    default: {
-      const float a = ((zval + 1.0e-25f) * v_nonce) * F_RT;
-      return -((Dc * a) * inv_d) * ((cB - cA * expf(-a)) / (-expm1f(-a)));
-    }
-  }
-}
-
 // Tile-major layout of the split form.  Tile b (a run of at most 32 whole
 // cells of one cluster holding at most TPB membranes) owns membrane slots
 // [b*TPB, (b+1)*TPB) and cell slots [32b, 32b+32); unused slots are padding.
