@@ -1307,12 +1307,16 @@ int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream) {
   if (h->ecm && !h->have_denv) return fail(BX_ESTATE, "ECM step before bx_set_env_diffusivity");
   if (n_steps == 0) return BX_OK;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : h->stream;
-  cudaEvent_t ev = nullptr;
+  // the cross-stream event, destroyed on every return path
+  struct EventGuard {
+    cudaEvent_t ev = nullptr;
+    ~EventGuard() { if (ev) cudaEventDestroy(ev); }
+  } guard;
   if (s != h->stream) {
     // the caller's stream runs after the handle's pending work
-    BX_CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    BX_CU(cudaEventRecord(ev, h->stream));
-    BX_CU(cudaStreamWaitEvent(s, ev, 0));
+    BX_CU(cudaEventCreateWithFlags(&guard.ev, cudaEventDisableTiming));
+    BX_CU(cudaEventRecord(guard.ev, h->stream));
+    BX_CU(cudaStreamWaitEvent(s, guard.ev, 0));
   }
   int left = n_steps;
   const int tail_out = want_outputs ? 1 : 0;
@@ -1364,9 +1368,8 @@ int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream) {
   if (want_outputs) h->have_outputs = true;
   h->last_step_outputs = want_outputs != 0;
   if (s != h->stream) {
-    BX_CU(cudaEventRecord(ev, s));
-    BX_CU(cudaStreamWaitEvent(h->stream, ev, 0));
-    cudaEventDestroy(ev);
+    BX_CU(cudaEventRecord(guard.ev, s));
+    BX_CU(cudaStreamWaitEvent(h->stream, guard.ev, 0));
   }
   return BX_OK;
 }

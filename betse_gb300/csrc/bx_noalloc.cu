@@ -7,12 +7,15 @@
 // real-time loop, an allocator-free embedding).  bx_cluster_create allocates
 // every buffer a handle needs; this entry point instead takes the caller's
 // device buffers and keeps the step's scratch (derived index maps, the CTA
-// tiling and the per-CTA partial sums of the well-mixed environment) in one
-// file-scope __device__ array of fixed size.
+// tiling, the per-CTA partial sums of the well-mixed environment and the
+// check_v / no_negs counters) in one file-scope __device__ array of fixed size.
 //
-// Limits (checked before any work; BX_EINVAL beyond them):
+// Limits (checked before any step; BX_EINVAL beyond them):
 //   n_cells <= 16384, n_mems <= 131072, n_ions <= 8, and every run of 16
 //   consecutive cells has at most 256 membranes.
+// The caller's cell_mem_ptr and nn_i are checked on the device before any
+// step (cell_mem_ptr[0] == 0, cell_mem_ptr[C] == M, strictly increasing;
+// 0 <= nn_i[m] < M); no index outside the array is written or read.
 // The array lives on every GPU that loads the library until the process
 // exits: 140,297 doubles, about 1.1 MB (kScratchDoubles).
 //
@@ -24,6 +27,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include "../../include/bx.h"
@@ -46,7 +50,7 @@ constexpr size_t kOffPart = kOffClBlk + 1;                      // double [kMaxT
 constexpr size_t kOffPump = kOffPart + (size_t)kMaxTiles * BX_MAX_IONS;  // double [1]
 constexpr size_t kOffEscale = kOffPump + 1;                     // double [1]
 constexpr size_t kOffStatus = kOffEscale + 1;                   // u64 [4]
-constexpr size_t kOffFlag = kOffStatus + 4;                     // int32 [2]: tile overflow flag
+constexpr size_t kOffFlag = kOffStatus + 4;                     // int32 [2]: tile overflow, bad map
 constexpr size_t kScratchDoubles = kOffFlag + 1;
 
 static __device__ __align__(256) double g_scratch[kScratchDoubles];
@@ -63,34 +67,80 @@ int na_fail(int code, const char* msg) {
   return code;
 }
 
-// set-up, once per device, with that device current: the device address of
-// the scratch array (its name in host code is only a host-side stand-in)
+// Set-up: the device address of the scratch array (its name in host code is
+// only a host-side stand-in).  It is looked up once per CUDA context, with
+// that context current, and cached under its context id: a context that was
+// destroyed and created again (cudaDeviceReset) reloads the module, and the
+// new context gets a new id, so a stale address is never reused.  The cache
+// is guarded by a mutex, so host threads may call concurrently (their GPU
+// work still races on the array, see above).
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+bool current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_cur = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  void* ctx = nullptr;
+  if (!get_cur || !get_id || get_cur(&ctx) != 0 || !ctx) return false;
+  return get_id(ctx, id) == 0;
+}
+
 double* scratch_address(int* rc) {
-  static double* addr[64] = {nullptr};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-    *rc = na_fail(BX_ECUDA, "bx_step_fp64_noalloc: no current CUDA device");
-    return nullptr;
-  }
-  if (!addr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) {
-      *rc = na_fail(BX_ECUDA, "bx_step_fp64_noalloc: cudaGetSymbolAddress failed");
+  struct Entry { unsigned long long ctx; double* addr; };
+  static std::mutex mu;
+  static Entry cache[64];
+  static int n_cache = 0;
+  unsigned long long ctx = 0;
+  if (!current_context_id(&ctx)) {
+    // no context is current on this thread yet: make the current device's
+    // primary context current (cudaSetDevice initialises it), then ask again
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) {
+      *rc = na_fail(BX_ECUDA, "bx_step_fp64_noalloc: no usable CUDA device");
       return nullptr;
     }
-    addr[dev] = static_cast<double*>(p);
   }
+  if (!ctx && !current_context_id(&ctx)) {
+    *rc = na_fail(BX_ECUDA, "bx_step_fp64_noalloc: cannot identify the current CUDA context");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  for (int k = 0; k < n_cache; ++k)
+    if (cache[k].ctx == ctx) { *rc = BX_OK; return cache[k].addr; }
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) {
+    *rc = na_fail(BX_ECUDA, "bx_step_fp64_noalloc: cudaGetSymbolAddress failed");
+    return nullptr;
+  }
+  const Entry e{ctx, static_cast<double*>(p)};
+  if (n_cache < 64) cache[n_cache++] = e;
+  else cache[ctx % 64] = e;          // more contexts than slots: replace one
   *rc = BX_OK;
-  return addr[dev];
+  return e.addr;
 }
 
 // Rebuild the derived maps in the scratch: mem_to_cells, the partner's cell,
-// the fixed 16-cell tiling, the per-cluster constants; clear the counters and
-// raise the flag if a tile holds more than 256 membranes.
+// the fixed 16-cell tiling, the per-cluster constants; clear the counters.
+// The caller's maps are checked as they are read: flag[0] is raised if a
+// tile holds more than 256 membranes, flag[1] if cell_mem_ptr is not a CSR
+// row pointer over M membranes or a partner index is out of range, and no
+// write or read leaves the arrays.  The host clears both flags before this
+// launch.
 __global__ void k_noalloc_prep(const int* __restrict__ ptr, const int* __restrict__ nn, int C, int M,
                                double* scratch, double pump, double escale) {
   int* m2c = reinterpret_cast<int*>(scratch + kOffM2c);
-  int* nn_cell = reinterpret_cast<int*>(scratch + kOffNnCell);
   int* blk = reinterpret_cast<int*>(scratch + kOffBlk);
   int* blk_cl = reinterpret_cast<int*>(scratch + kOffBlkCl);
   int* cl_blk = reinterpret_cast<int*>(scratch + kOffClBlk);
@@ -98,8 +148,14 @@ __global__ void k_noalloc_prep(const int* __restrict__ ptr, const int* __restric
   const int ntile = (C + kTileCells - 1) / kTileCells;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
-  for (int c = tid; c < C; c += stride)
-    for (int m = ptr[c]; m < ptr[c + 1]; ++m) m2c[m] = c;
+  if (tid == 0 && (ptr[0] != 0 || ptr[C] != M)) atomicExch(flag + 1, 1);
+  for (int c = tid; c < C; c += stride) {
+    const int a = ptr[c], e = ptr[c + 1];
+    if (a >= e || a < 0 || e > M) { atomicExch(flag + 1, 1); continue; }
+    for (int m = a; m < e; ++m) m2c[m] = c;
+  }
+  for (int m = tid; m < M; m += stride)
+    if (nn[m] < 0 || nn[m] >= M) atomicExch(flag + 1, 1);
   for (int b = tid; b <= ntile; b += stride) {
     const int cb = min(b * kTileCells, C);
     blk[b] = cb;
@@ -119,15 +175,15 @@ __global__ void k_noalloc_prep(const int* __restrict__ ptr, const int* __restric
   }
 }
 
+// The partner's cell; an out-of-range partner (flagged by the prep kernel) is
+// skipped, and the call returns before any step reads the map.
 __global__ void k_noalloc_nn_cell(const int* __restrict__ nn, int M, double* scratch) {
   const int* m2c = reinterpret_cast<const int*>(scratch + kOffM2c);
   int* nn_cell = reinterpret_cast<int*>(scratch + kOffNnCell);
-  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x)
-    nn_cell[m] = m2c[nn[m]];
-}
-
-__global__ void k_noalloc_clear_flag(double* scratch) {
-  reinterpret_cast<int*>(scratch + kOffFlag)[0] = 0;
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const int q = nn[m];
+    nn_cell[m] = (q >= 0 && q < M) ? m2c[q] : 0;
+  }
 }
 
 int zc(double z) { return z == 1.0 ? 1 : z == -1.0 ? -1 : z == 2.0 ? 2 : z == -2.0 ? -2 : 0; }
@@ -164,14 +220,18 @@ extern "C" int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const 
   const double pump = -3.0 * p->nakatp_block * p->alpha_NaK;
   const double escale = p->dt / (p->vol_env * (double)M);
 
-  k_noalloc_clear_flag<<<1, 1, 0, s>>>(scratch);
+  if (cudaMemsetAsync(scratch + kOffFlag, 0, 2 * sizeof(int), s) != cudaSuccess)
+    return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: clearing the set-up flags failed");
   k_noalloc_prep<<<64, 256, 0, s>>>(g->cell_mem_ptr, g->nn_i, C, M, scratch, pump, escale);
   k_noalloc_nn_cell<<<64, 256, 0, s>>>(g->nn_i, M, scratch);
-  int flag = 0;
-  if (cudaMemcpyAsync(&flag, scratch + kOffFlag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+  int flag[2] = {0, 0};
+  if (cudaMemcpyAsync(flag, scratch + kOffFlag, sizeof(flag), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: set-up kernels failed");
-  if (flag) return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: 16 consecutive cells hold more than 256 membranes");
+  if (flag[1])
+    return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: cell_mem_ptr is not a row pointer over n_mems membranes "
+                              "(ptr[0] == 0, ptr[n_cells] == n_mems, strictly increasing) or nn_i is out of range");
+  if (flag[0]) return na_fail(BX_EINVAL, "bx_step_fp64_noalloc: 16 consecutive cells hold more than 256 membranes");
 
   bx::DevGeom dg{};
   dg.C = C; dg.M = M; dg.I = I; dg.G = g->grid_ny * g->grid_nx; dg.ny = g->grid_ny; dg.nx = g->grid_nx;
@@ -224,5 +284,18 @@ extern "C" int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const 
       return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: copy-back failed");
   }
   if (cudaGetLastError() != cudaSuccess) return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: launch failed");
+  // check_v / no_negs (sim_toolbox.py:332-344, 475-503): the step kernels
+  // count NaN Vmem, NaN concentrations and clamped negatives into the
+  // scratch; a NaN is reported as BX_EUNSTABLE, as bx_status does for handles
+  unsigned long long st[3] = {0ull, 0ull, 0ull};
+  if (cudaMemcpyAsync(st, scratch + kOffStatus, sizeof(st), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return na_fail(BX_ECUDA, "bx_step_fp64_noalloc: reading the step status failed");
+  if (st[0] || st[1]) {
+    const std::string msg = "bx_step_fp64_noalloc: unstable: NaN in Vmem (" + std::to_string(st[0]) +
+                            " membrane values) or in cell concentrations (" + std::to_string(st[1]) + ")";
+    bx_record_error(msg.c_str());
+    return BX_EUNSTABLE;
+  }
   return BX_OK;
 }

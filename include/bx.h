@@ -343,11 +343,18 @@ int64_t bx_cell_kernel_bytes(bx_handle h);
  *          cc_cells [n_ions * n_cells], cc_env [n_ions] (well mixed); updated
  *   vm_work [n_mems], cc_mem_work [n_ions * n_cells]   device work buffers
  * Limits (BX_EINVAL beyond them): n_cells <= 16384, n_mems <= 131072, and at
- * most 256 membranes in any 16 consecutive cells.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress).  Every call
- * shares the array and leaves the last call's contents in it; calls that
- * overlap on the GPU race on it, so serialise them.  Synchronises `stream`
- * once per call to check the limits. */
+ * most 256 membranes in any 16 consecutive cells.  cell_mem_ptr and nn_i are
+ * checked on the device before the first step (ptr[0] == 0, ptr[n_cells] ==
+ * n_mems, strictly increasing; 0 <= nn_i < n_mems): BX_EINVAL, nothing
+ * stepped.  check_v / no_negs (sim_toolbox.py:332-344, 475-503): a NaN in
+ * Vmem or a cell concentration during the call returns BX_EUNSTABLE (the
+ * buffers then hold the unstable state); negatives are clamped to 0 as BETSE
+ * does.  The first call in a CUDA context looks up the array's device address
+ * (cudaGetSymbolAddress) and caches it per context; make that first call
+ * before any stream capture.  Every call shares the array and leaves the last
+ * call's contents in it; calls that overlap on the GPU race on it, so
+ * serialise them.  Synchronises `stream` twice per call: after the checks and
+ * after the last step, to read the NaN counters. */
 int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm, double* vm,
                          double* vm_work, double* cc_cells, double* cc_mem, double* cc_mem_work,
                          double* cc_env, int n_steps, void* stream);

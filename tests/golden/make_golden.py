@@ -13,7 +13,7 @@ BETSE's own ``Cells`` code, runs BETSE's own ``Simulator`` time loop
 The checkout cannot travel with the repository, so the fixtures are committed
 and the tests read only them. Run it from the repository root::
 
-    python tests/golden/make_golden.py --ref /root/reference
+    python tests/golden/make_golden.py --ref <path of a BETSE checkout>
 
 BETSE's package ``__init__`` modules pull in beartype, dill, matplotlib,
 ruamel.yaml and PIL, none of which the hot path uses. The loader below stubs
@@ -422,9 +422,12 @@ CASES = {
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default=os.environ.get('BETSE_REF', '/root/reference'))
+    ap.add_argument('--ref', default=os.environ.get('BETSE_REF'),
+                    help='path of a BETSE source checkout (or set BETSE_REF)')
     ap.add_argument('--only', default=None)
     a = ap.parse_args()
+    if not a.ref:
+        ap.error('give --ref <path of a BETSE checkout> or set BETSE_REF')
     install_reference(a.ref)
     for name, kw in CASES.items():
         if a.only and name not in a.only.split(','):

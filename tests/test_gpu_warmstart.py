@@ -4,8 +4,8 @@ Fresh clusters (seeds outside the training set) step from the uniform initial
 profile and from the committed network's prediction until max |dVm/dt| < 1e-6
 V/s.  The warm start must reach the test on every cluster the plain method
 settles (one whose explicit step diverges is left out of both arms) and cut the mean
-number of steps per cluster at least 3x on this small sample (the full
-evaluation, 64 x 5000 cells, is reported by bench.py)."""
+number of steps per cluster at least 3x on this small sample (bench.py
+reports the same measurement on a larger sample of fresh 5000-cell clusters)."""
 import numpy as np
 import pytest
 
