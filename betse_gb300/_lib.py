@@ -135,6 +135,9 @@ SIGNATURES = {
     'bx_set_launch_config': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int]),
     'bx_get_launch_config': (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int)]),
     'bx_autotune': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int), ct.POINTER(ct.c_double)]),
+    'bx_resident_info': (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int),
+                                    ct.POINTER(ct.c_int), ct.POINTER(ct.c_int64)]),
+    'bx_resident_barrier_check': (ct.c_int, [ct.c_void_p, ct.c_int64, ct.POINTER(ct.c_int)]),
     'bx_step_fp64_noalloc': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p]),

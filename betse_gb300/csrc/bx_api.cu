@@ -23,6 +23,7 @@
 
 #include "../../include/bx.h"
 #include "bx_env.cuh"
+#include "bx_factored.cuh"
 #include "bx_fields.cuh"
 #include "bx_launch.cuh"
 #include "bx_split.cuh"
@@ -62,6 +63,9 @@ constexpr int kTPB = 256;        // membrane slots per CTA of the cell kernels
 constexpr int kRec = 8;          // floats per cell record of the split form (<= 7 ions + Vmem)
 
 enum Mode { MODE_PLAIN = 0, MODE_SPLIT = 1 };
+// kernels of the split form (bx_set_launch_config's `kernel`)
+enum Kind { KIND_TILE = 0, KIND_PERSIST = 1, KIND_FACT = 2, KIND_RESIDENT = 3 };
+constexpr long long kResTimeoutNs = 2000000000LL;   // grid-barrier wait limit of k_split_resident
 
 }  // namespace
 
@@ -74,7 +78,7 @@ struct bx_cluster {
   int mode = MODE_PLAIN;
   int nblk = 0;
   int tpb = kTPB;                  // membrane slots per CTA (autotuned)
-  bool persist = false;            // split form: persistent cp.async-pipelined kernel (autotuned)
+  int kind = KIND_TILE;            // split form: tile, persistent, factored or resident kernel (autotuned)
   int sm_count = 0;
   bool ecm = false;
   bool ca = false;                 // Ca-ATPase on (iCa >= 0 and alpha_Ca > 0)
@@ -168,6 +172,26 @@ struct bx_cluster {
   int Gtot = 0, Xtot = 0;
   int *bf_ci = nullptr, *bf_last = nullptr;
   double *bf_cd = nullptr, *bf_buf = nullptr, *bf_X = nullptr, *bf_Y = nullptr, *bf_scale = nullptr;
+  // ---- factored split form (bx_factored.cuh), per cell slot
+  float* f_dsa = nullptr;          // [I][S] sum of Dm_i * mem_sa over the cell's membranes
+  float4* f_cst = nullptr;         // [S] {sum mem_sa, dt/cell_vol, diviterm/cm, gap-junction count | -1}
+  int* f_gbeg = nullptr;           // [S] first gap-junction entry
+  int2* f_gj = nullptr;            // [P] {partner cell slot, bits of gj_weight*mem_sa}
+  int f_P = 0;
+  std::vector<float> h_fsa;        // [S] sum of mem_sa (host, for f_cst)
+  std::vector<int> h_gbeg, h_gcnt; // [S] (gcnt -1 = padding slot)
+  std::vector<int2> h_gj;          // [P]
+  // ---- resident cooperative kernel: built on first use, dropped with the layout
+  int r_state = 0;                 // 0 not built, 1 ready, -1 does not fit (r_why)
+  std::string r_why;
+  int r_grid = 0, r_threads = 0, r_ntile_max = 0, r_nent_max = 0, r_nhalo_max = 0;
+  size_t r_smem = 0;
+  bx::ResCta* r_cta = nullptr;
+  int2* r_gj = nullptr;
+  int* r_gbeg = nullptr;
+  int* r_halo = nullptr;
+  float2* r_cpart = nullptr;
+  unsigned* r_ctl = nullptr;       // [0] barrier counter, [1] timeout flag
 };
 
 namespace {
@@ -188,7 +212,8 @@ void free_all(bx_cluster* h) {
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
       h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo, h->d_cnew, h->d_Rrads,
-      h->st_vm, h->st_cc, h->st_cam, h->st_go, h->d_flag, h->t_slot_of_mem, h->t_blob};
+      h->st_vm, h->st_cc, h->st_cam, h->st_go, h->d_flag, h->t_slot_of_mem, h->t_blob,
+      h->f_dsa, h->f_cst, h->f_gbeg, h->f_gj, h->r_cta, h->r_gj, h->r_gbeg, h->r_halo, h->r_cpart, h->r_ctl};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& fs : h->fshapes)
@@ -386,6 +411,20 @@ bx::SplitPtrs split_ptrs(bx_cluster* h, int parity) {
 }
 
 // BETSE's six-ion set compiled as constants (bx_split.cuh IonSet<1>)
+bx::FactGeom fact_geom(const bx_cluster* h) {
+  bx::FactGeom g{};
+  g.S = h->S; g.ntile = h->nblk;
+  g.dsa = h->f_dsa; g.cst = h->f_cst; g.gbeg = h->f_gbeg; g.gj = h->f_gj; g.blk_cluster = h->d_blk_cl;
+  return g;
+}
+
+// The factored and resident kernels need one Vmem and one environment per
+// cell: no Phi_b, no extracellular spaces, no per-membrane gating state, no
+// Ca-ATPase (which reads the cell concentration per membrane), no outputs.
+bool fact_eligible(const bx_cluster* h, bool out) {
+  return h->mode == MODE_SPLIT && !out && !h->phib_nonzero && !h->ecm && !h->vgj && !h->ca;
+}
+
 bool is_betse_six_ions(const bx_cluster* h) {
   const double z6[6] = {1, 1, -1, 2, -1, -1};
   if (h->I != 6 || h->par.iNa != 0 || h->par.iK != 1) return false;
@@ -491,8 +530,141 @@ cudaError_t launch_persist_t(bx_cluster* h, int parity, cudaStream_t s) {
                          make_split_const(h), h->nblk);
 }
 
+// the factored step: 8 tiles (warps) per CTA
+constexpr int kFactWarps = 8;
+cudaError_t launch_fact(bx_cluster* h, int parity, cudaStream_t s) {
+  const unsigned grid = (unsigned)((h->nblk + kFactWarps - 1) / kFactWarps);
+  if (is_betse_six_ions(h))
+    return launch_pdl(bx::k_split_fact<kFactWarps, 1>, grid, kFactWarps * 32, s, fact_geom(h), split_ptrs(h, parity),
+                      make_split_const(h));
+  return launch_pdl(bx::k_split_fact<kFactWarps, 0>, grid, kFactWarps * 32, s, fact_geom(h), split_ptrs(h, parity),
+                    make_split_const(h));
+}
+
+void drop_resident(bx_cluster* h) {
+  void* ptrs[] = {h->r_cta, h->r_gj, h->r_gbeg, h->r_halo, h->r_cpart, h->r_ctl};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  h->r_cta = nullptr; h->r_gj = nullptr; h->r_gbeg = nullptr; h->r_halo = nullptr; h->r_cpart = nullptr;
+  h->r_ctl = nullptr;
+  h->r_state = 0;
+}
+
+template <int ZP>
+void* resident_kernel() { return reinterpret_cast<void*>(bx::k_split_resident<ZP>); }
+
+// Partition of the tiles over one CTA per SM for k_split_resident, each CTA's
+// gap-junction entries re-indexed into its record table (own cells, then
+// the halo of partner cells it does not own), and the shared-memory size.
+// Marks the handle "does not fit" (r_state = -1, reason in r_why) when a
+// CTA's cells and entries exceed the shared memory of one SM, when more than
+// 32 tiles would share a CTA, or for a batch of clusters.
+int build_resident(bx_cluster* h) {
+  drop_resident(h);
+  auto refuse = [&](const std::string& why) {
+    h->r_state = -1;
+    h->r_why = why;
+    return BX_OK;
+  };
+  if (h->ncl != 1) return refuse("the resident kernel steps one cluster (its environment is one sum)");
+  const int nblk = h->nblk, nsm = h->sm_count;
+  const int grid = std::min(nblk, nsm);
+  const int ntile_max = (nblk + grid - 1) / grid;
+  if (ntile_max > 32) return refuse("more than 32 tiles per SM");
+  std::vector<bx::ResCta> cta(grid);
+  std::vector<int2> ent;
+  std::vector<int> gbeg(h->S, 0), halo;
+  int nent_max = 0, nhalo_max = 0;
+  for (int j = 0; j < grid; ++j) {
+    const int t0 = (int)((long long)j * nblk / grid), t1 = (int)((long long)(j + 1) * nblk / grid);
+    const int slot0 = 32 * t0, n_own = 32 * (t1 - t0);
+    bx::ResCta& c = cta[j];
+    c.tile0 = t0; c.ntile = t1 - t0; c.ent0 = (int)ent.size(); c.halo0 = (int)halo.size();
+    c.pad[0] = c.pad[1] = 0;
+    std::vector<int> hl;                       // this CTA's halo, sorted
+    for (int ls = 0; ls < n_own; ++ls) {
+      const int sl = slot0 + ls;
+      for (int q = 0; q < std::max(0, h->h_gcnt[sl]); ++q) {
+        const int p = h->h_gj[h->h_gbeg[sl] + q].x;
+        if (p < slot0 || p >= slot0 + n_own) hl.push_back(p);
+      }
+    }
+    std::sort(hl.begin(), hl.end());
+    hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
+    for (int ls = 0; ls < n_own; ++ls) {
+      const int sl = slot0 + ls;
+      gbeg[sl] = (int)ent.size() - c.ent0;
+      for (int q = 0; q < std::max(0, h->h_gcnt[sl]); ++q) {
+        const int2 e = h->h_gj[h->h_gbeg[sl] + q];
+        int loc;
+        if (e.x >= slot0 && e.x < slot0 + n_own) loc = e.x - slot0;
+        else loc = n_own + (int)(std::lower_bound(hl.begin(), hl.end(), e.x) - hl.begin());
+        ent.push_back(make_int2(loc, e.y));
+      }
+    }
+    c.nent = (int)ent.size() - c.ent0;
+    c.nhalo = (int)hl.size();
+    halo.insert(halo.end(), hl.begin(), hl.end());
+    nent_max = std::max(nent_max, c.nent);
+    nhalo_max = std::max(nhalo_max, c.nhalo);
+  }
+  const bool six = is_betse_six_ions(h);
+  const int NI = six ? 6 : bx::kMaxIons;
+  const bx::ResSmem L(ntile_max, nent_max, nhalo_max, NI);
+  int optin = 0;
+  BX_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->dev));
+  if (L.total > (size_t)optin)
+    return refuse("the cells of one SM need " + std::to_string(L.total) + " bytes of shared memory (" +
+                  std::to_string(optin) + " available)");
+  const void* kern = six ? resident_kernel<1>() : resident_kernel<0>();
+  // the device's limit, so handles of different sizes never undercut each other
+  BX_CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  const int threads = 32 * ntile_max;
+  int per_sm = 0;
+  BX_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, L.total));
+  if (per_sm < 1) return refuse("one CTA of the resident kernel does not fit an SM");
+  int coop = 0;
+  BX_CU(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->dev));
+  if (!coop) return refuse("the device has no cooperative launch");
+  BX_CU(dalloc(&h->r_cta, cta.size())); BX_CU(h2d(h->r_cta, cta.data(), cta.size()));
+  BX_CU(dalloc(&h->r_gj, std::max<size_t>(1, ent.size())));
+  if (!ent.empty()) BX_CU(h2d(h->r_gj, ent.data(), ent.size()));
+  BX_CU(dalloc(&h->r_gbeg, gbeg.size())); BX_CU(h2d(h->r_gbeg, gbeg.data(), gbeg.size()));
+  BX_CU(dalloc(&h->r_halo, std::max<size_t>(1, halo.size())));
+  if (!halo.empty()) BX_CU(h2d(h->r_halo, halo.data(), halo.size()));
+  BX_CU(dalloc(&h->r_cpart, (size_t)2 * grid * h->I));
+  BX_CU(dalloc(&h->r_ctl, 2));
+  BX_CU(cudaMemset(h->r_ctl, 0, 2 * sizeof(unsigned)));
+  h->r_grid = grid; h->r_threads = threads; h->r_smem = L.total;
+  h->r_ntile_max = ntile_max; h->r_nent_max = nent_max; h->r_nhalo_max = nhalo_max;
+  h->r_state = 1;
+  return BX_OK;
+}
+
+// n_steps time steps in one cooperative launch of k_split_resident (reads
+// parity, leaves the state at parity ^ (n_steps & 1)).
+cudaError_t launch_resident(bx_cluster* h, int parity, int n_steps, cudaStream_t s,
+                            long long timeout_ns = kResTimeoutNs, unsigned bias = 0) {
+  cudaError_t e = cudaMemsetAsync(h->r_ctl, 0, sizeof(unsigned), s);   // the barrier counter
+  if (e != cudaSuccess) return e;
+  bx::ResArrays ra{};
+  ra.cta = h->r_cta; ra.gj = h->r_gj; ra.gbeg = h->r_gbeg; ra.halo = h->r_halo; ra.cpart = h->r_cpart;
+  ra.ctl = h->r_ctl; ra.cenv64 = h->d_cenv; ra.cenv_f = h->s_cenv_f; ra.env_scale = h->d_env_scale;
+  ra.rec_glob[0] = h->s_rec[parity]; ra.rec_glob[1] = h->s_rec[parity ^ 1];
+  ra.ntile_max = h->r_ntile_max; ra.nent_max = h->r_nent_max; ra.nhalo_max = h->r_nhalo_max;
+  ra.timeout_ns = timeout_ns;
+  ra.barrier_bias = bias;
+  bx::FactGeom fg = fact_geom(h);
+  bx::SplitPtrs sp = split_ptrs(h, parity);
+  bx::SplitConst k = make_split_const(h);
+  void* args[] = {&fg, &sp, &k, &ra, &n_steps};
+  const void* kern = is_betse_six_ions(h) ? resident_kernel<1>() : resident_kernel<0>();
+  return cudaLaunchCooperativeKernel(kern, dim3(h->r_grid), dim3(h->r_threads), args, h->r_smem, s);
+}
+
 cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
-  if (h->persist && !out && !h->phib_nonzero && !h->ecm && !h->vgj && !h->ca) {
+  if ((h->kind == KIND_FACT || h->kind == KIND_RESIDENT) && fact_eligible(h, out)) return launch_fact(h, parity, s);
+  if (h->kind == KIND_PERSIST && !out && !h->phib_nonzero && !h->ecm && !h->vgj && !h->ca) {
     const bool six = is_betse_six_ions(h);
     if (h->tpb == 192) return six ? launch_persist_t<192, 1>(h, parity, s) : launch_persist_t<192, 0>(h, parity, s);
     return six ? launch_persist_t<256, 1>(h, parity, s) : launch_persist_t<256, 0>(h, parity, s);
@@ -633,6 +805,8 @@ int launches_per_step(const bx_cluster* h) {
   return h->par.sharpness < 1.0 ? 8 : 7;
 }
 
+int upload_fact_cst(bx_cluster* h);
+
 // per-cluster constants that depend on the parameters (dt, cm, alpha_NaK, vol_env)
 int upload_param_arrays(bx_cluster* h) {
   std::vector<double> pump(h->ncl), escale(h->ncl);
@@ -658,6 +832,8 @@ int upload_param_arrays(bx_cluster* h) {
       BX_CU(h2d(h->t_dtv, dtv.data(), h->S));
       BX_CU(h2d(h->t_dvc, dvc.data(), h->S));
     }
+    int rc = upload_fact_cst(h);
+    if (rc != BX_OK) return rc;
   }
   return BX_OK;
 }
@@ -704,6 +880,85 @@ int check_geom(const bx_geom* g, const bx_params* p) {
   }
   if (p->is_ecm && !g->mem_sa_per_env) return fail(BX_EINVAL, "ECM needs mem_sa_per_env");
   return BX_OK;
+}
+
+// bit casts on the host
+inline float bits_to_float(int v) { float f; std::memcpy(&f, &v, sizeof f); return f; }
+inline int float_to_bits(float f) { int v; std::memcpy(&v, &f, sizeof v); return v; }
+
+// DSA_i of every cell slot (sum over the cell's membranes of Dm_i * mem_sa,
+// accumulated in FP64), for the factored kernels; zero until Dm is set.
+int upload_fact_dsa(bx_cluster* h) {
+  if (!h->f_dsa) return BX_OK;
+  const int I = h->I, S = h->S;
+  std::vector<double> acc((size_t)I * S, 0.0);
+  if (!h->h_Dm.empty())
+    for (int m = 0; m < h->M; ++m) {
+      const int sl = h->h_slot_of_cell[h->h_m2c[m]];
+      for (int i = 0; i < I; ++i) acc[(size_t)i * S + sl] += h->h_Dm[(size_t)i * h->M + m] * h->h_msa[m];
+    }
+  std::vector<float> f(acc.size());
+  for (size_t q = 0; q < acc.size(); ++q) f[q] = (float)acc[q];
+  BX_CU(h2d(h->f_dsa, f.data(), f.size()));
+  return BX_OK;
+}
+
+// {sum mem_sa, dt/cell_vol, diviterm/cm, gap-junction count} of every cell slot
+// (the parameters dt and cm enter here)
+int upload_fact_cst(bx_cluster* h) {
+  if (!h->f_cst) return BX_OK;
+  std::vector<float4> cst(h->S);
+  for (int sl = 0; sl < h->S; ++sl) cst[sl] = make_float4(0.f, 0.f, 0.f, bits_to_float(-1));
+  for (int c = 0; c < h->C; ++c) {
+    const int sl = h->h_slot_of_cell[c];
+    cst[sl] = make_float4(h->h_fsa[sl], (float)(h->par.dt / h->h_vol[c]), (float)(h->h_div[c] / h->par.cm),
+                          bits_to_float(h->h_gcnt[sl]));
+  }
+  BX_CU(h2d(h->f_cst, cst.data(), cst.size()));
+  return BX_OK;
+}
+
+// The factored form's gap-junction lists: per cell slot, the cell's
+// membranes that have a partner and a nonzero weight (BETSE zeroes the flux
+// of boundary membranes, sim.py:2203), in membrane order, each as the
+// partner's cell slot and gj_weight * mem_sa.
+int build_fact_layout(bx_cluster* h) {
+  const int S = h->S;
+  const std::vector<int>& ptr = h->h_cell_ptr;
+  h->h_fsa.assign(S, 0.f);
+  h->h_gbeg.assign(S, 0);
+  h->h_gcnt.assign(S, -1);
+  h->h_gj.clear();
+  std::vector<int> cell_of_slot(S, -1);
+  for (int c = 0; c < h->C; ++c) cell_of_slot[h->h_slot_of_cell[c]] = c;
+  for (int sl = 0; sl < S; ++sl) {
+    h->h_gbeg[sl] = (int)h->h_gj.size();
+    const int c = cell_of_slot[sl];
+    if (c < 0) continue;
+    double sa = 0.0;
+    for (int m = ptr[c]; m < ptr[c + 1]; ++m) {
+      sa += h->h_msa[m];
+      if (h->h_bflag[m] || h->h_gjw[m] == 0.0) continue;
+      const int ps = h->h_slot_of_cell[h->h_m2c[h->h_nn[m]]];
+      h->h_gj.push_back(make_int2(ps, float_to_bits((float)(h->h_gjw[m] * h->h_msa[m]))));
+    }
+    h->h_fsa[sl] = (float)sa;
+    h->h_gcnt[sl] = (int)h->h_gj.size() - h->h_gbeg[sl];
+  }
+  h->f_P = (int)h->h_gj.size();
+  void* old[] = {h->f_dsa, h->f_cst, h->f_gbeg, h->f_gj};
+  for (void* q : old)
+    if (q) cudaFree(q);
+  h->f_dsa = nullptr; h->f_cst = nullptr; h->f_gbeg = nullptr; h->f_gj = nullptr;
+  drop_resident(h);
+  BX_CU(dalloc(&h->f_dsa, (size_t)h->I * S));
+  BX_CU(dalloc(&h->f_cst, S));
+  BX_CU(dalloc(&h->f_gbeg, S)); BX_CU(h2d(h->f_gbeg, h->h_gbeg.data(), S));
+  BX_CU(dalloc(&h->f_gj, std::max(1, h->f_P)));
+  if (h->f_P) BX_CU(h2d(h->f_gj, h->h_gj.data(), h->f_P));
+  int rc = upload_fact_dsa(h);
+  if (rc != BX_OK) return rc;
+  return upload_fact_cst(h);
 }
 
 // Tile-major slot layout of the split form for the partition `blk`: tile b
@@ -789,6 +1044,8 @@ int build_split_layout(bx_cluster* h, const std::vector<int>& blk) {
   BX_CU(build_geo_blob(h));
   BX_CU(cudaStreamSynchronize(h->stream));
   h->have_state = false;
+  int rc = build_fact_layout(h);
+  if (rc != BX_OK) return rc;
   return upload_param_arrays(h);
 }
 
@@ -1109,6 +1366,8 @@ int bx_set_membrane_diffusivity(bx_handle h, const double* Dm) {
     BX_CU(cudaMemcpy(h->d_Dm_f, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
     BX_CU(build_geo_blob(h));
     BX_CU(cudaStreamSynchronize(h->stream));
+    const int rc = upload_fact_dsa(h);
+    if (rc != BX_OK) return rc;
   } else if (h->d_Dm_f) {
     std::vector<float> f(n);
     for (size_t q = 0; q < n; ++q) f[q] = (float)Dm[q];
@@ -1251,6 +1510,7 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
       BX_CU(cudaMemcpyAsync(h->d_Ey, s->E_env_y, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
     }
   }
+  if (h->r_ctl) BX_CU(cudaMemsetAsync(h->r_ctl, 0, 2 * sizeof(unsigned), st));   // a fresh state: no timeout
   BX_CU(cudaStreamSynchronize(st));
   h->have_state = true;
   h->have_outputs = false;
@@ -1320,6 +1580,23 @@ int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream) {
   }
   int left = n_steps;
   const int tail_out = want_outputs ? 1 : 0;
+  if (h->kind == KIND_RESIDENT && fact_eligible(h, false) && left - tail_out >= 2) {
+    if (h->r_state == 0) {
+      const int rc = build_resident(h);
+      if (rc != BX_OK) return rc;
+    }
+    if (h->r_state == 1) {
+      // one cooperative launch per at most 2^20 steps (the barrier counter is 32-bit)
+      while (left - tail_out > 0) {
+        const int n = std::min(left - tail_out, 1 << 20);
+        cudaError_t e = launch_resident(h, h->parity, n, s);
+        if (e != cudaSuccess) return fail(BX_ECUDA, std::string("resident step launch: ") + cudaGetErrorString(e));
+        h->launches += 1;
+        h->parity ^= (n & 1);
+        left -= n;
+      }
+    }
+  }
   if (left - tail_out >= kGraphChunk) {
     if (h->parity != 0) {
       cudaError_t e = enqueue_step(h, h->parity, false, s);
@@ -1385,6 +1662,17 @@ int bx_status(bx_handle h, bx_step_status* st) {
   st->neg_clamped = (int64_t)v[2];
   st->unstable = (v[0] || v[1]) ? 1 : 0;
   st->precision = h->precision;
+  if (h->r_ctl) {
+    // the resident kernel's grid barrier gave up (its wait is bounded): the
+    // state of that run is incomplete
+    unsigned ctl[2] = {0u, 0u};
+    BX_CU(cudaMemcpy(ctl, h->r_ctl, sizeof(ctl), cudaMemcpyDeviceToHost));
+    if (ctl[1]) {
+      h->have_state = false;
+      BX_CU(cudaMemset(h->r_ctl, 0, sizeof(ctl)));
+      return fail(BX_ECUDA, "the resident kernel's grid barrier timed out; upload the state again");
+    }
+  }
   return BX_OK;
 }
 
@@ -1421,6 +1709,28 @@ int bx_time_cell_kernel(bx_handle h, int n, double* ms_per_launch) {
   cudaEvent_t e0, e1;
   BX_CU(cudaEventCreate(&e0));
   BX_CU(cudaEventCreate(&e1));
+  if (h->kind == KIND_RESIDENT && fact_eligible(h, false)) {
+    // one cooperative launch of n steps (the kernel's unit of work), per step
+    if (h->r_state == 0) {
+      const int rc = build_resident(h);
+      if (rc != BX_OK) return rc;
+    }
+    if (h->r_state == 1 && n >= 2) {
+      BX_CU(cudaEventRecord(e0, h->stream));
+      cudaError_t e = launch_resident(h, h->parity, n, h->stream);
+      if (e != cudaSuccess) return fail(BX_ECUDA, cudaGetErrorString(e));
+      BX_CU(cudaEventRecord(e1, h->stream));
+      BX_CU(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      BX_CU(cudaEventElapsedTime(&ms, e0, e1));
+      h->parity ^= (n & 1);
+      h->launches++;
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      *ms_per_launch = ms / n;
+      return BX_OK;
+    }
+  }
   double tot = 0.0;
   for (int q = 0; q < n; ++q) {
     BX_CU(cudaEventRecord(e0, h->stream));
@@ -1444,6 +1754,13 @@ int bx_time_cell_kernel(bx_handle h, int n, double* ms_per_launch) {
 int64_t bx_cell_kernel_bytes(bx_handle h) {
   if (!h) return -1;
   const int64_t M = h->M, C = h->C, I = h->I, B = h->nblk;
+  if (h->mode == MODE_SPLIT && (h->kind == KIND_FACT || h->kind == KIND_RESIDENT) && fact_eligible(h, false)) {
+    // factored form, per cell slot: cc2 in+out 16I, record in+out 2*4*kRec,
+    // DSA 4I, {SA, dt/vol, diviterm/cm, count} 16, first entry 4; per
+    // gap-junction entry 8; per tile the partial sums 4I and the cluster id 4
+    const int64_t S = h->S, P = h->f_P;
+    return S * (16 * I + 8 * kRec + 4 * I + 16 + 4) + P * 8 + B * (4 * I + 4);
+  }
   if (h->mode == MODE_SPLIT) {
     // membrane: Dm (4I), nn_slot 4, lcell 1, mem_sa 4, gjw 4
     // cell: cc2 in+out 16I, record in+out 2*4*kRec, dt/vol 4, diviterm/cm 4, range 4
@@ -1467,21 +1784,24 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
 
 int64_t bx_launch_count(bx_handle h) { return h ? h->launches : -1; }
 
-int bx_get_launch_config(bx_handle h, int* tpb, int* persistent) {
-  if (!h || !tpb || !persistent) return fail(BX_EINVAL, "null argument");
+int bx_get_launch_config(bx_handle h, int* tpb, int* kernel) {
+  if (!h || !tpb || !kernel) return fail(BX_EINVAL, "null argument");
   *tpb = h->tpb;
-  *persistent = h->persist ? 1 : 0;
+  *kernel = h->kind;
   return BX_OK;
 }
 
-int bx_set_launch_config(bx_handle h, int tpb, int persistent) {
+int bx_set_launch_config(bx_handle h, int tpb, int kernel) {
   if (!h) return fail(BX_EINVAL, "null handle");
   const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256) : (tpb == 128 || tpb == 256);
   if (!ok) return fail(BX_EINVAL, "unsupported CTA size for this form");
-  if (persistent && h->mode != MODE_SPLIT) return fail(BX_EINVAL, "the persistent kernel is the split form's");
-  if (persistent && h->ecm) return fail(BX_EINVAL, "the persistent kernel has no extracellular-space variant");
-  if (persistent && h->vgj) return fail(BX_EINVAL, "the persistent kernel has no voltage-gated gap-junction variant");
-  if (persistent && h->ca) return fail(BX_EINVAL, "the persistent kernel has no Ca-ATPase variant");
+  if (kernel < KIND_TILE || kernel > KIND_RESIDENT) return fail(BX_EINVAL, "kernel must be 0, 1, 2 or 3");
+  if (kernel != KIND_TILE && h->mode != MODE_SPLIT)
+    return fail(BX_EINVAL, "the persistent, factored and resident kernels are the split form's");
+  if (kernel != KIND_TILE && h->ecm) return fail(BX_EINVAL, "only the tile kernel has an extracellular-space variant");
+  if (kernel != KIND_TILE && h->vgj)
+    return fail(BX_EINVAL, "only the tile kernel has a voltage-gated gap-junction variant");
+  if (kernel != KIND_TILE && h->ca) return fail(BX_EINVAL, "only the tile kernel has a Ca-ATPase variant");
   const size_t C = h->C, I = h->I, M = h->M;
   const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
   std::vector<double> vm(M), cc(I * C), cam(I * M), cenv(nenv), ex(h->ecm ? h->G : 1), ey(h->ecm ? h->G : 1),
@@ -1492,15 +1812,61 @@ int bx_set_launch_config(bx_handle h, int tpb, int persistent) {
   int rc;
   if (had_state && (rc = bx_state_download(h, &sv)) != BX_OK) return rc;
   if ((rc = build_partition(h, tpb)) != BX_OK) return rc;
-  h->persist = persistent != 0;
+  h->kind = kernel;
+  h->graph_valid = false;
   if (had_state && (rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
   return BX_OK;
 }
 
-// Autotuner: time `n_steps` eager steps for each CTA size, keep the fastest.
-// The state is downloaded before the trials and uploaded again after each
-// one (the split form's tile-major layout changes with the CTA size), so
-// tuning does not advance the simulation.
+// Failure detection of the resident kernel without a fault: one launch whose
+// grid barrier waits for one CTA more than the grid has, so every CTA's wait
+// runs out after timeout_ns; the kernel then raises its timeout flag and
+// returns, leaving the state as it was (the run never writes it back).
+int bx_resident_barrier_check(bx_handle h, int64_t timeout_ns, int* timed_out) {
+  if (!h || !timed_out || timeout_ns <= 0 || timeout_ns > kResTimeoutNs)
+    return fail(BX_EINVAL, "timeout_ns must be in (0, 2e9]");
+  if (!h->have_state || !h->have_dm) return fail(BX_ESTATE, "upload state and Dm first");
+  if (!fact_eligible(h, false)) return fail(BX_EINVAL, "the resident kernel does not cover this handle");
+  if (h->r_state == 0) {
+    const int rc = build_resident(h);
+    if (rc != BX_OK) return rc;
+  }
+  if (h->r_state != 1) return fail(BX_EINVAL, h->r_why);
+  cudaError_t e = launch_resident(h, h->parity, 2, h->stream, (long long)timeout_ns, 1u);
+  if (e != cudaSuccess) return fail(BX_ECUDA, cudaGetErrorString(e));
+  h->launches++;
+  BX_CU(cudaStreamSynchronize(h->stream));
+  unsigned ctl[2] = {0u, 0u};
+  BX_CU(cudaMemcpy(ctl, h->r_ctl, sizeof(ctl), cudaMemcpyDeviceToHost));
+  *timed_out = ctl[1] ? 1 : 0;
+  BX_CU(cudaMemset(h->r_ctl, 0, sizeof(ctl)));
+  return BX_OK;
+}
+
+int bx_resident_info(bx_handle h, int* fits, int* grid, int* threads, int64_t* smem_bytes) {
+  if (!h || !fits) return fail(BX_EINVAL, "null argument");
+  if (h->mode != MODE_SPLIT || !fact_eligible(h, false)) {
+    *fits = 0;
+    return fail(BX_EINVAL, "the resident kernel needs the split form without ECM, Phi_b, gating or Ca-ATPase");
+  }
+  if (h->r_state == 0) {
+    const int rc = build_resident(h);
+    if (rc != BX_OK) return rc;
+  }
+  *fits = h->r_state == 1 ? 1 : 0;
+  if (grid) *grid = h->r_grid;
+  if (threads) *threads = h->r_threads;
+  if (smem_bytes) *smem_bytes = (int64_t)h->r_smem;
+  if (h->r_state != 1) return fail(BX_EINVAL, h->r_why);
+  return BX_OK;
+}
+
+// Autotuner: time `n_steps` steps (as bx_step runs them: graph chunks, or
+// one cooperative launch for the resident kernel) for each candidate
+// partition and kernel, after one untimed run of the same length, and keep
+// the fastest.  The state is downloaded before the trials and uploaded
+// again after each one (the split form's tile-major layout changes with the
+// CTA size), so tuning does not advance the simulation.
 int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out) {
   if (!h || n_steps <= 0) return fail(BX_EINVAL, "bad arguments");
   if (!h->have_state || !h->have_dm) return fail(BX_ESTATE, "upload state and Dm first");
@@ -1514,40 +1880,47 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   if (rc != BX_OK) return rc;
   unsigned long long status[4];
   BX_CU(cudaMemcpy(status, h->d_status, sizeof(status), cudaMemcpyDeviceToHost));
-  const int64_t launches0 = h->launches;
-  struct Cand { int tpb; bool persist; };
+  const int64_t launches0 = h->launches, steps0 = h->steps_done;
+  struct Cand { int tpb; int kind; };
   std::vector<Cand> cands;
-  if (h->mode == MODE_SPLIT && (h->ecm || h->vgj || h->ca)) cands = {{256, false}, {192, false}};
-  else if (h->mode == MODE_SPLIT) cands = {{256, false}, {192, false}, {256, true}, {192, true}};
-  else cands = {{256, false}, {128, false}};
+  if (h->mode == MODE_SPLIT && !fact_eligible(h, false)) cands = {{256, KIND_TILE}, {192, KIND_TILE}};
+  else if (h->mode == MODE_SPLIT)
+    cands = {{256, KIND_TILE}, {192, KIND_TILE}, {256, KIND_PERSIST}, {192, KIND_PERSIST},
+             {256, KIND_FACT}, {192, KIND_FACT}, {256, KIND_RESIDENT}, {192, KIND_RESIDENT}};
+  else cands = {{256, KIND_TILE}, {128, KIND_TILE}};
   double best = 1e300;
-  int best_tpb = h->tpb;
-  bool best_persist = h->persist;
+  int best_tpb = h->tpb, best_kind = h->kind;
   cudaEvent_t e0, e1;
   BX_CU(cudaEventCreate(&e0));
   BX_CU(cudaEventCreate(&e1));
   for (const Cand& cd : cands) {
-    const int tpb = cd.tpb;
-    if (build_partition(h, tpb) != BX_OK) continue;
-    h->persist = cd.persist;
+    if (build_partition(h, cd.tpb) != BX_OK) continue;
+    h->kind = cd.kind;
+    h->graph_valid = false;
+    if (cd.kind == KIND_RESIDENT) {
+      if ((rc = build_resident(h)) != BX_OK) return rc;
+      if (h->r_state != 1) continue;            // does not fit: not a candidate
+    }
     if ((rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
-    for (int w = 0; w < 2; ++w) { enqueue_step(h, h->parity, false, h->stream); h->parity ^= 1; }
+    if ((rc = bx_step(h, n_steps, 0, h->stream)) != BX_OK) return rc;
     BX_CU(cudaEventRecord(e0, h->stream));
-    for (int q = 0; q < n_steps; ++q) { enqueue_step(h, h->parity, false, h->stream); h->parity ^= 1; }
+    if ((rc = bx_step(h, n_steps, 0, h->stream)) != BX_OK) return rc;
     BX_CU(cudaEventRecord(e1, h->stream));
     BX_CU(cudaEventSynchronize(e1));
     float ms = 0.f;
     BX_CU(cudaEventElapsedTime(&ms, e0, e1));
     const double per = ms / n_steps;
-    if (per < best) { best = per; best_tpb = tpb; best_persist = cd.persist; }
+    if (per < best) { best = per; best_tpb = cd.tpb; best_kind = cd.kind; }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if ((rc = build_partition(h, best_tpb)) != BX_OK) return rc;
-  h->persist = best_persist;
+  h->kind = best_kind;
+  h->graph_valid = false;
   if ((rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
   BX_CU(cudaMemcpy(h->d_status, status, sizeof(status), cudaMemcpyHostToDevice));
   h->launches = launches0;
+  h->steps_done = steps0;
   if (tpb_out) *tpb_out = best_tpb;
   if (ms_per_step_out) *ms_per_step_out = best;
   return BX_OK;

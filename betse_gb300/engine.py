@@ -18,6 +18,9 @@ from .exceptions import BetseSimUnstableException
 
 PRECISIONS = {'fp64': _lib.PLAIN_FP64, 'plain': _lib.PLAIN_FP64,
               'split': _lib.SPLIT_FP32, 'fp32': _lib.SPLIT_FP32}
+# kernels of the split form (bx_set_launch_config)
+KERNELS = {'tile': 0, 'persistent': 1, 'factored': 2, 'resident': 3}
+KERNEL_NAMES = {v: k for k, v in KERNELS.items()}
 
 
 def _c(a):
@@ -219,16 +222,35 @@ class ClusterEngine:
         _lib.check(self.lib.bx_time_cell_kernel(self.h, int(n), ct.byref(ms)), 'bx_time_cell_kernel')
         return ms.value
 
-    def set_launch_config(self, tpb, persistent=False):
-        """Pin the CTA size and (split form) the persistent kernel; state kept."""
-        _lib.check(self.lib.bx_set_launch_config(self.h, int(tpb), int(bool(persistent))),
-                   'bx_set_launch_config')
+    def set_launch_config(self, tpb, kernel=0):
+        """Pin the tile size (membrane slots per tile) and, for the split form,
+        the kernel: 0/'tile', 1/'persistent' (True), 2/'factored',
+        3/'resident'; the state is kept."""
+        k = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+        _lib.check(self.lib.bx_set_launch_config(self.h, int(tpb), k), 'bx_set_launch_config')
 
     def launch_config(self):
-        """(threads per CTA, persistent kernel) in use."""
-        tpb, per = ct.c_int(), ct.c_int()
-        _lib.check(self.lib.bx_get_launch_config(self.h, ct.byref(tpb), ct.byref(per)), 'bx_get_launch_config')
-        return tpb.value, bool(per.value)
+        """(membrane slots per tile, kernel number) in use."""
+        tpb, kind = ct.c_int(), ct.c_int()
+        _lib.check(self.lib.bx_get_launch_config(self.h, ct.byref(tpb), ct.byref(kind)), 'bx_get_launch_config')
+        return tpb.value, kind.value
+
+    def resident_barrier_check(self, timeout_s=0.05):
+        """Run the resident kernel once with a grid barrier that cannot
+        complete; True if its bounded wait ran out and was reported (the
+        state is unchanged)."""
+        t = ct.c_int()
+        _lib.check(self.lib.bx_resident_barrier_check(self.h, int(timeout_s * 1e9), ct.byref(t)),
+                   'bx_resident_barrier_check')
+        return bool(t.value)
+
+    def resident_info(self):
+        """Whether the resident kernel fits this cluster: dict(fits, grid,
+        threads, smem_bytes, why)."""
+        fits, grid, thr, smem = ct.c_int(), ct.c_int(), ct.c_int(), ct.c_int64()
+        rc = self.lib.bx_resident_info(self.h, ct.byref(fits), ct.byref(grid), ct.byref(thr), ct.byref(smem))
+        why = '' if rc == _lib.BX_OK else (self.lib.bx_last_error() or b'').decode()
+        return dict(fits=bool(fits.value), grid=grid.value, threads=thr.value, smem_bytes=smem.value, why=why)
 
     def autotune(self, n_steps=20):
         """Pick the fastest CTA size for this cluster; the state is unchanged.

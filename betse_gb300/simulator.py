@@ -109,7 +109,7 @@ def run_sim_core_loop(sim, phase, time_steps, time_steps_sampled, anim_cells=Non
     (FP32 fluxes, FP64 concentrations and Vmem).  fields: compute v_env,
     E_env, J_env and B_field at sampled steps from ``cells.lapENVinv`` (False,
     or no ``lapENVinv`` on ``cells``, leaves those attributes untouched).
-    launch_config: (threads per CTA, persistent) to pin, or 'auto' to time
+    launch_config: (membrane slots per tile, kernel) to pin, or 'auto' to time
     the candidates once before stepping.
     """
     reasons = unsupported_features(sim, phase, assume_no_events, precision)

@@ -360,16 +360,35 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
                          double* cc_env, int n_steps, void* stream);
 
 /* Launch configuration: CTA size (plain form 128 or 256; split form 192 or
- * 256 membrane slots) and, for the split form, the persistent pipelined
- * kernel.  The state is kept.  bx_autotune picks these by timing. */
-int bx_set_launch_config(bx_handle h, int tpb, int persistent);
-int bx_get_launch_config(bx_handle h, int* tpb, int* persistent);
+ * 256 membrane slots per tile, which sets how cells are grouped into tiles)
+ * and, for the split form, the kernel:
+ *   0  tile kernel (one tile per CTA, one launch per step; every variant)
+ *   1  persistent pipelined tile kernel
+ *   2  factored kernel: one thread per cell; the transmembrane flux and the
+ *      pump are computed once per cell from the cell's sum of Dm * mem_sa,
+ *      the gap-junction flux once per paired membrane (one launch per step)
+ *   3  resident kernel: the factored step for many steps in one cooperative
+ *      launch, each SM keeping its cells in shared memory (one cluster that
+ *      fits; otherwise kernel 2 runs)
+ * Kernels 1-3 need no extracellular spaces, no voltage-gated gap junctions
+ * and no Ca-ATPase; steps with outputs or a nonzero Phi_b always run the
+ * tile kernel.  The state is kept.  bx_autotune picks these by timing. */
+int bx_set_launch_config(bx_handle h, int tpb, int kernel);
+int bx_get_launch_config(bx_handle h, int* tpb, int* kernel);
+/* Whether the resident kernel fits this handle (*fits), and its grid, CTA
+ * size and shared memory per CTA.  BX_EINVAL (with the reason) if not. */
+int bx_resident_info(bx_handle h, int* fits, int* grid, int* threads, int64_t* smem_bytes);
+/* Failure detection of the resident kernel, tested without a fault: one
+ * launch whose grid barrier can never complete, so every CTA's bounded wait
+ * runs out after timeout_ns (at most 2e9).  *timed_out = 1 if the kernel
+ * reported the timeout; the state is left as it was. */
+int bx_resident_barrier_check(bx_handle h, int64_t timeout_ns, int* timed_out);
 
-/* Autotuner: times n_steps steps for each launch configuration (CTA size,
- * and for the split form tile-per-CTA or persistent pipelined kernel) on the
- * uploaded state, keeps the fastest, and restores the state so the
- * simulation does not advance.  Reports the choice and its
- * ms per step (either pointer may be NULL). */
+/* Autotuner: times n_steps steps (run as bx_step runs them) for each
+ * launch configuration -- CTA size and, for the split form, the tile,
+ * persistent, factored and resident kernels -- on the uploaded state, keeps
+ * the fastest, and restores the state so the simulation does not advance.
+ * Reports the choice and its ms per step (either pointer may be NULL). */
 int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out);
 
 /* Version / diagnostics. */
