@@ -447,6 +447,17 @@ def profile_kernel(which):
     print('profile kernel done:', which)
 
 
+# kernels of the split form, by the number bx_set_launch_config takes
+KERNEL_NAMES = {0: 'k_split_step', 1: 'k_split_persist', 2: 'k_split_fact', 3: 'k_split_resident'}
+LAUNCH_SUFFIX = {'': 0, 'p': 1, 'f': 2, 'r': 3}
+
+
+def parse_launch(text):
+    """'192' tile kernel, '192p' persistent, '192f' factored, '256r' resident."""
+    suffix = text.lstrip('0123456789')
+    return int(text[:len(text) - len(suffix)]), LAUNCH_SUFFIX[suffix]
+
+
 def profile_run(args):
     """A short, deterministic launch sequence for ncu captures."""
     from betse_gb300.build import build
@@ -463,7 +474,7 @@ def profile_run(args):
         e.upload(**st)
     if args.launch:
         # the launch configuration the autotuner picks for this workload, pinned
-        e.set_launch_config(int(args.launch.rstrip('p')), args.launch.endswith('p'))
+        e.set_launch_config(*parse_launch(args.launch))
     e.step(args.time_steps or 4)
     e.check_stable()
     e.close()
@@ -485,7 +496,8 @@ def main():
                     help='for ncu: build the workload, upload it, run 4 steps (or --time-steps), exit')
     ap.add_argument('--precision', default='split', choices=['split', 'fp64'])
     ap.add_argument('--launch', default=None,
-                    help='with --profile-run: CTA size, suffix p for the persistent kernel (e.g. 192p)')
+                    help='with --profile-run: membrane slots per tile, suffix p persistent, f factored, '
+                         'r resident kernel (e.g. 192r)')
     ap.add_argument('--profile-kernel', choices=['gemm', 'fields'],
                     help='for ncu: run a small case of one dense-product kernel and exit')
     args = ap.parse_args()

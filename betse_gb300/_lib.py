@@ -138,6 +138,7 @@ SIGNATURES = {
     'bx_resident_info': (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int),
                                     ct.POINTER(ct.c_int), ct.POINTER(ct.c_int64)]),
     'bx_resident_barrier_check': (ct.c_int, [ct.c_void_p, ct.c_int64, ct.POINTER(ct.c_int)]),
+    'bx_autotune_table': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.POINTER(ct.c_int), _ip, _ip, _ip, _dp]),
     'bx_step_fp64_noalloc': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p]),

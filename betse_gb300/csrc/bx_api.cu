@@ -79,6 +79,8 @@ struct bx_cluster {
   int nblk = 0;
   int tpb = kTPB;                  // membrane slots per CTA (autotuned)
   int kind = KIND_TILE;            // split form: tile, persistent, factored or resident kernel (autotuned)
+  int fact_unroll = 4;             // factored kernel: gap junctions loaded per round (2 or 4, autotuned)
+  double tune_ms = -1.0;           // ms per step of the configuration the last autotune chose
   int sm_count = 0;
   bool ecm = false;
   bool ca = false;                 // Ca-ATPase on (iCa >= 0 and alpha_Ca > 0)
@@ -188,7 +190,7 @@ struct bx_cluster {
   size_t r_smem = 0;
   bx::ResCta* r_cta = nullptr;
   int2* r_gj = nullptr;
-  int* r_gbeg = nullptr;
+  int2* r_gbeg = nullptr;
   int* r_halo = nullptr;
   float2* r_cpart = nullptr;
   unsigned* r_ctl = nullptr;       // [0] barrier counter, [1] timeout flag
@@ -532,13 +534,18 @@ cudaError_t launch_persist_t(bx_cluster* h, int parity, cudaStream_t s) {
 
 // the factored step: 8 tiles (warps) per CTA
 constexpr int kFactWarps = 8;
-cudaError_t launch_fact(bx_cluster* h, int parity, cudaStream_t s) {
+template <int U>
+cudaError_t launch_fact_u(bx_cluster* h, int parity, cudaStream_t s) {
   const unsigned grid = (unsigned)((h->nblk + kFactWarps - 1) / kFactWarps);
   if (is_betse_six_ions(h))
-    return launch_pdl(bx::k_split_fact<kFactWarps, 1>, grid, kFactWarps * 32, s, fact_geom(h), split_ptrs(h, parity),
-                      make_split_const(h));
-  return launch_pdl(bx::k_split_fact<kFactWarps, 0>, grid, kFactWarps * 32, s, fact_geom(h), split_ptrs(h, parity),
-                    make_split_const(h));
+    return launch_pdl(bx::k_split_fact<kFactWarps, 1, U>, grid, kFactWarps * 32, s, fact_geom(h),
+                      split_ptrs(h, parity), make_split_const(h));
+  return launch_pdl(bx::k_split_fact<kFactWarps, 0, U>, grid, kFactWarps * 32, s, fact_geom(h),
+                    split_ptrs(h, parity), make_split_const(h));
+}
+
+cudaError_t launch_fact(bx_cluster* h, int parity, cudaStream_t s) {
+  return h->fact_unroll == 2 ? launch_fact_u<2>(h, parity, s) : launch_fact_u<4>(h, parity, s);
 }
 
 void drop_resident(bx_cluster* h) {
@@ -570,10 +577,12 @@ int build_resident(bx_cluster* h) {
   const int nblk = h->nblk, nsm = h->sm_count;
   const int grid = std::min(nblk, nsm);
   const int ntile_max = (nblk + grid - 1) / grid;
-  if (ntile_max > 32) return refuse("more than 32 tiles per SM");
+  // one thread per cell, at most two cells per thread (1024 threads)
+  if (ntile_max > 64) return refuse("more than 64 tiles per SM");
   std::vector<bx::ResCta> cta(grid);
   std::vector<int2> ent;
-  std::vector<int> gbeg(h->S, 0), halo;
+  std::vector<int2> gbeg(h->S, make_int2(0, 0));
+  std::vector<int> halo;
   int nent_max = 0, nhalo_max = 0;
   for (int j = 0; j < grid; ++j) {
     const int t0 = (int)((long long)j * nblk / grid), t1 = (int)((long long)(j + 1) * nblk / grid);
@@ -591,16 +600,23 @@ int build_resident(bx_cluster* h) {
     }
     std::sort(hl.begin(), hl.end());
     hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
+    // each cell's entries: partners this CTA owns first (in membrane order),
+    // then halo partners (in membrane order); gbeg = {first, owned count}
     for (int ls = 0; ls < n_own; ++ls) {
       const int sl = slot0 + ls;
-      gbeg[sl] = (int)ent.size() - c.ent0;
-      for (int q = 0; q < std::max(0, h->h_gcnt[sl]); ++q) {
-        const int2 e = h->h_gj[h->h_gbeg[sl] + q];
-        int loc;
-        if (e.x >= slot0 && e.x < slot0 + n_own) loc = e.x - slot0;
-        else loc = n_own + (int)(std::lower_bound(hl.begin(), hl.end(), e.x) - hl.begin());
-        ent.push_back(make_int2(loc, e.y));
-      }
+      const int first = (int)ent.size() - c.ent0;
+      int nloc = 0;
+      for (int pass = 0; pass < 2; ++pass)
+        for (int q = 0; q < std::max(0, h->h_gcnt[sl]); ++q) {
+          const int2 e = h->h_gj[h->h_gbeg[sl] + q];
+          const bool local = e.x >= slot0 && e.x < slot0 + n_own;
+          if (local != (pass == 0)) continue;
+          int loc;
+          if (local) { loc = e.x - slot0; ++nloc; }
+          else loc = n_own + (int)(std::lower_bound(hl.begin(), hl.end(), e.x) - hl.begin());
+          ent.push_back(make_int2(loc, e.y));
+        }
+      gbeg[sl] = make_int2(first, nloc);
     }
     c.nent = (int)ent.size() - c.ent0;
     c.nhalo = (int)hl.size();
@@ -619,7 +635,7 @@ int build_resident(bx_cluster* h) {
   const void* kern = six ? resident_kernel<1>() : resident_kernel<0>();
   // the device's limit, so handles of different sizes never undercut each other
   BX_CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  const int threads = 32 * ntile_max;
+  const int threads = 32 * std::min(ntile_max, 32);
   int per_sm = 0;
   BX_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, L.total));
   if (per_sm < 1) return refuse("one CTA of the resident kernel does not fit an SM");
@@ -1867,8 +1883,10 @@ int bx_resident_info(bx_handle h, int* fits, int* grid, int* threads, int64_t* s
 // the fastest.  The state is downloaded before the trials and uploaded
 // again after each one (the split form's tile-major layout changes with the
 // CTA size), so tuning does not advance the simulation.
-int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out) {
-  if (!h || n_steps <= 0) return fail(BX_EINVAL, "bad arguments");
+int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* tpb, int* kernel, int* unroll,
+                      double* ms_per_step) {
+  if (!h || n_steps <= 0 || max_rows < 0) return fail(BX_EINVAL, "bad arguments");
+  if (n_rows) *n_rows = 0;
   if (!h->have_state || !h->have_dm) return fail(BX_ESTATE, "upload state and Dm first");
   const size_t C = h->C, I = h->I, M = h->M;
   const size_t nenv = h->ecm ? I * h->G : (size_t)h->ncl * I;
@@ -1881,21 +1899,23 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
   unsigned long long status[4];
   BX_CU(cudaMemcpy(status, h->d_status, sizeof(status), cudaMemcpyDeviceToHost));
   const int64_t launches0 = h->launches, steps0 = h->steps_done;
-  struct Cand { int tpb; int kind; };
+  struct Cand { int tpb; int kind; int unroll; };
   std::vector<Cand> cands;
-  if (h->mode == MODE_SPLIT && !fact_eligible(h, false)) cands = {{256, KIND_TILE}, {192, KIND_TILE}};
+  if (h->mode == MODE_SPLIT && !fact_eligible(h, false)) cands = {{256, KIND_TILE, 4}, {192, KIND_TILE, 4}};
   else if (h->mode == MODE_SPLIT)
-    cands = {{256, KIND_TILE}, {192, KIND_TILE}, {256, KIND_PERSIST}, {192, KIND_PERSIST},
-             {256, KIND_FACT}, {192, KIND_FACT}, {256, KIND_RESIDENT}, {192, KIND_RESIDENT}};
-  else cands = {{256, KIND_TILE}, {128, KIND_TILE}};
+    cands = {{256, KIND_TILE, 4},     {192, KIND_TILE, 4},     {256, KIND_PERSIST, 4}, {192, KIND_PERSIST, 4},
+             {256, KIND_FACT, 4},     {192, KIND_FACT, 4},     {256, KIND_FACT, 2},    {192, KIND_FACT, 2},
+             {256, KIND_RESIDENT, 4}, {192, KIND_RESIDENT, 4}};
+  else cands = {{256, KIND_TILE, 4}, {128, KIND_TILE, 4}};
   double best = 1e300;
-  int best_tpb = h->tpb, best_kind = h->kind;
+  int best_tpb = h->tpb, best_kind = h->kind, best_unroll = h->fact_unroll;
   cudaEvent_t e0, e1;
   BX_CU(cudaEventCreate(&e0));
   BX_CU(cudaEventCreate(&e1));
   for (const Cand& cd : cands) {
     if (build_partition(h, cd.tpb) != BX_OK) continue;
     h->kind = cd.kind;
+    h->fact_unroll = cd.unroll;
     h->graph_valid = false;
     if (cd.kind == KIND_RESIDENT) {
       if ((rc = build_resident(h)) != BX_OK) return rc;
@@ -1910,19 +1930,34 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
     float ms = 0.f;
     BX_CU(cudaEventElapsedTime(&ms, e0, e1));
     const double per = ms / n_steps;
-    if (per < best) { best = per; best_tpb = cd.tpb; best_kind = cd.kind; }
+    if (per < best) { best = per; best_tpb = cd.tpb; best_kind = cd.kind; best_unroll = cd.unroll; }
+    if (n_rows && *n_rows < max_rows) {
+      const int r = (*n_rows)++;
+      if (tpb) tpb[r] = cd.tpb;
+      if (kernel) kernel[r] = cd.kind;
+      if (unroll) unroll[r] = cd.unroll;
+      if (ms_per_step) ms_per_step[r] = per;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if ((rc = build_partition(h, best_tpb)) != BX_OK) return rc;
   h->kind = best_kind;
+  h->fact_unroll = best_unroll;
+  h->tune_ms = best;
   h->graph_valid = false;
   if ((rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
   BX_CU(cudaMemcpy(h->d_status, status, sizeof(status), cudaMemcpyHostToDevice));
   h->launches = launches0;
   h->steps_done = steps0;
-  if (tpb_out) *tpb_out = best_tpb;
-  if (ms_per_step_out) *ms_per_step_out = best;
+  return BX_OK;
+}
+
+int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out) {
+  const int rc = bx_autotune_table(h, n_steps, 0, nullptr, nullptr, nullptr, nullptr, nullptr);
+  if (rc != BX_OK) return rc;
+  if (tpb_out) *tpb_out = h->tpb;
+  if (ms_per_step_out) *ms_per_step_out = h->tune_ms;
   return BX_OK;
 }
 

@@ -187,10 +187,14 @@ __device__ __forceinline__ float warp_sum_down(float v) {
 
 // ---------------------------------------------------------------------------
 // One time step, streaming: NW warps per CTA, warp = tile, lane = cell slot.
-// Launched with programmatic dependent launch after k_split_env of the
-// previous step; the static data is read before the dependency wait.
+// Each lane walks its cell's gap-junction entries U at a time (U = 2 or 4,
+// chosen by the autotuner): the U entries, then the U partner records, are
+// loaded before any of them is used, so a cell waits on two latency rounds
+// per U junctions rather than two per junction.  Launched with programmatic dependent launch after
+// k_split_env of the previous step; the static data is read before the
+// dependency wait.
 // ---------------------------------------------------------------------------
-template <int NW, int ZP>
+template <int NW, int ZP, int U>
 __global__ void __launch_bounds__(NW * 32)
 k_split_fact(FactGeom fg, SplitPtrs p, SplitConst k) {
   using IS = IonSet<ZP>;
@@ -239,10 +243,20 @@ k_split_fact(FactGeom fg, SplitPtrs p, SplitConst k) {
     const float pc = p.pump_coef[cl];
     const float v1 = own[7] + 1.0e-25f;
     const int2* e = fg.gj + gb;
-    for (int j = 0; j < gcnt; ++j) {
-      const int2 en = e[j];
-      const float4* r4 = reinterpret_cast<const float4*>(p.rec_in + (size_t)en.x * 8);
-      fact_gj_add<ZP, NI>(k, I, v1, cin, r4[0], r4[1], __int_as_float(en.y), s2);
+    for (int j = 0; j < gcnt; j += U) {
+      int2 en[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) en[u] = (j + u < gcnt) ? e[j + u] : make_int2(s, 0);
+      float4 r0[U], r1[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float4* r4 = reinterpret_cast<const float4*>(p.rec_in + (size_t)en[u].x * 8);
+        r0[u] = r4[0];
+        r1[u] = r4[1];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (j + u < gcnt) fact_gj_add<ZP, NI>(k, I, v1, cin, r0[u], r1[u], __int_as_float(en[u].y), s2);
     }
     fact_trans<ZP, NI>(k, I, v1, cin, cenv, pc, dsa, cs.x, s1);
     float rec[8];
@@ -271,18 +285,25 @@ k_split_fact(FactGeom fg, SplitPtrs p, SplitConst k) {
 // its shared memory holds the cells' static data, their concentrations
 // (double-float) and a table of 32-byte cell records: its own cells first,
 // then the "halo", the cells outside the CTA that its gap junctions name.
-// Gap-junction entries carry the partner's index in that table.  A step:
-//   1. every cell advances from the table of the step's parity; the new
-//      record goes to the other table and to the global record buffer;
-//   2. the CTA's environment partial (double-float, tiles in order) goes to
-//      global memory, double-buffered by step parity;
-//   3. grid barrier (release/acquire on a counter, bounded wait);
-//   4. every CTA sums the CTAs' partials in a fixed order (the same in
-//      every CTA, so the environment is identical everywhere), updates the
-//      well-mixed environment in FP64 as k_split_env does, and copies its
-//      halo records from global memory into the new table.
-// The barrier's wait gives up after `timeout_ns` (it then raises
-// ctl[1] = 1 and returns), so a lost CTA cannot hang the GPU.
+// Each cell's gap-junction entries carry the partner's index in that table,
+// the partners the CTA owns first.  One thread advances one cell.  Step t:
+//   a. the gap junctions to halo partners (table of parity t);
+//   b. the per-cell terms and the update; the new record goes to the other
+//      table and to the global record buffer, s1 to shared memory;
+//   c. warp i sums ion i's s1 over the CTA's cells in a fixed order
+//      (double-float), stores the CTA's partial in global memory
+//      (double-buffered by parity) and arrives at the grid barrier (release);
+//   d. meanwhile, and until the barrier completes, every thread sums the gap
+//      junctions of step t+1 to partners the CTA owns: their records are in
+//      the new table already;
+//   e. thread 0 waits for the barrier (acquire, bounded);
+//   f. every CTA sums all CTAs' partials in the same fixed order (so the
+//      environment is identical everywhere), updates the well-mixed
+//      environment in FP64 as k_split_env does, and copies its halo records
+//      from global memory into the new table.
+// So the barrier's latency overlaps most of the gap-junction work.  The wait
+// gives up after `timeout_ns` (it then raises ctl[1] = 1 and returns), so a
+// lost CTA cannot hang the GPU.
 // ---------------------------------------------------------------------------
 struct ResCta {
   int tile0, ntile;        // tiles (cell slots [32*tile0, 32*(tile0+ntile)))
@@ -294,7 +315,7 @@ struct ResCta {
 struct ResArrays {
   const ResCta* __restrict__ cta;          // [grid]
   const int2* __restrict__ gj;             // {index in the CTA's record table, bits of gj_weight*mem_sa}
-  const int* __restrict__ gbeg;            // [S] first entry of the cell, relative to its CTA's ent0
+  const int2* __restrict__ gbeg;           // [S] {first entry relative to the CTA's ent0, entries to owned cells}
   const int* __restrict__ halo;            // global cell slots of each CTA's halo
   float2* __restrict__ cpart;              // [2][grid][I] per-CTA environment partials (hi, lo)
   unsigned* __restrict__ ctl;              // [0] barrier counter (zeroed before the launch), [1] timeout flag
@@ -311,7 +332,7 @@ struct ResArrays {
 // aligned) base; the host sizes the launch with the same function.
 struct ResSmem {
   int n_own, n_tab;
-  size_t tab, cc2, dsa, cst, gbeg, gj, halo, tpart, cenv, flag, total;
+  size_t tab, cc2, dsa, s1, cst, gbeg, gj, halo, cenv, flag, total;
   __host__ __device__ static size_t up16(size_t x) { return (x + 15) & ~size_t(15); }
   __host__ __device__ ResSmem(int ntile_max, int nent_max, int nhalo_max, int NI) {
     n_own = 32 * ntile_max;
@@ -320,11 +341,11 @@ struct ResSmem {
     tab = o;   o = up16(o + (size_t)2 * n_tab * 8 * sizeof(float));
     cc2 = o;   o = up16(o + (size_t)NI * n_own * sizeof(float2));
     dsa = o;   o = up16(o + (size_t)NI * n_own * sizeof(float));
+    s1 = o;    o = up16(o + (size_t)NI * n_own * sizeof(float));
     cst = o;   o = up16(o + (size_t)n_own * sizeof(float4));
-    gbeg = o;  o = up16(o + (size_t)n_own * sizeof(int));
+    gbeg = o;  o = up16(o + (size_t)n_own * sizeof(int2));
     gj = o;    o = up16(o + (size_t)(nent_max > 0 ? nent_max : 1) * sizeof(int2));
     halo = o;  o = up16(o + (size_t)(nhalo_max > 0 ? nhalo_max : 1) * sizeof(int));
-    tpart = o; o = up16(o + (size_t)ntile_max * NI * sizeof(float));
     cenv = o;  o = up16(o + (size_t)NI * (sizeof(double) + sizeof(float)));
     flag = o;  o = up16(o + 16);
     total = o;
@@ -337,15 +358,17 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Grid barrier for a cooperative launch: every CTA adds 1 to ctl[0] and waits
-// until it reaches `target` (= steps so far x grid), or until another CTA
-// raised ctl[1], or until timeout_ns passed (then it raises ctl[1] itself).
-// Returns false if the barrier failed; the caller then returns.
-__device__ __forceinline__ bool res_grid_sync(unsigned* ctl, unsigned target, long long timeout_ns, int* sflag) {
-  __syncthreads();
+// Arrival at the grid barrier: release, so this thread's writes (and those
+// it observed, e.g. through the preceding bar.sync) are visible first.
+__device__ __forceinline__ void res_arrive(unsigned* ctl) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctl) : "memory");
+}
+
+// Thread 0 waits until ctl[0] reaches `target` (acquire), or until another
+// CTA raised ctl[1], or until timeout_ns passed (then it raises ctl[1]
+// itself); the result is broadcast through *sflag after a bar.sync.
+__device__ __forceinline__ bool res_wait(unsigned* ctl, unsigned target, long long timeout_ns, int* sflag) {
   if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(ctl, 1u);
     const unsigned long long t0 = global_ns();
     int ok = 1;
     unsigned n = 0;
@@ -363,11 +386,29 @@ __device__ __forceinline__ bool res_grid_sync(unsigned* ctl, unsigned target, lo
         }
       }
     }
-    __threadfence();
     *sflag = ok;
   }
   __syncthreads();
   return *sflag != 0;
+}
+
+// Gap-junction entries [j0, j1) of one cell from table T into s2.
+template <int ZP, int NI>
+__device__ __forceinline__ void res_gj_range(const SplitConst& k, int I, const float* __restrict__ T,
+                                             const int2* __restrict__ e, int j0, int j1, const float* own,
+                                             float (&s2)[NI]) {
+  const float4 o1 = reinterpret_cast<const float4*>(own)[1];
+  const float4 o0 = reinterpret_cast<const float4*>(own)[0];
+  const float ov[8] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z, o1.w};
+  float cin[NI];
+#pragma unroll
+  for (int i = 0; i < NI; ++i) cin[i] = (i < I && i < 7) ? ov[i] : 0.f;
+  const float v1 = o1.w + 1.0e-25f;
+  for (int j = j0; j < j1; ++j) {
+    const int2 en = e[j];
+    const float4* r4 = reinterpret_cast<const float4*>(T + (size_t)en.x * 8);
+    fact_gj_add<ZP, NI>(k, I, v1, cin, r4[0], r4[1], __int_as_float(en.y), s2);
+  }
 }
 
 template <int ZP>
@@ -375,18 +416,19 @@ __global__ void __launch_bounds__(1024, 1)
 k_split_resident(FactGeom fg, SplitPtrs p, SplitConst k, ResArrays ra, int n_steps) {
   using IS = IonSet<ZP>;
   constexpr int NI = IS::NI;
+  constexpr int CPT = 2;                                         // cells per thread kept in registers (max)
   const int I = IS::n(k);
   extern __shared__ __align__(16) unsigned char res_smem[];
   const ResSmem L(ra.ntile_max, ra.nent_max, ra.nhalo_max, NI);
-  float* tab = reinterpret_cast<float*>(res_smem + L.tab);          // [2][n_tab][8]
-  float2* scc = reinterpret_cast<float2*>(res_smem + L.cc2);        // [NI][n_own]
-  float* sdsa = reinterpret_cast<float*>(res_smem + L.dsa);         // [NI][n_own]
-  float4* scst = reinterpret_cast<float4*>(res_smem + L.cst);       // [n_own]
-  int* sgb = reinterpret_cast<int*>(res_smem + L.gbeg);             // [n_own]
-  int2* sgj = reinterpret_cast<int2*>(res_smem + L.gj);             // [nent]
-  int* shalo = reinterpret_cast<int*>(res_smem + L.halo);           // [nhalo]
-  float* tpart = reinterpret_cast<float*>(res_smem + L.tpart);      // [ntile][NI]
-  double* cenv64 = reinterpret_cast<double*>(res_smem + L.cenv);    // [NI]
+  float* tab = reinterpret_cast<float*>(res_smem + L.tab);      // [2][n_tab][8]
+  float2* scc = reinterpret_cast<float2*>(res_smem + L.cc2);    // [NI][n_own]
+  float* sdsa = reinterpret_cast<float*>(res_smem + L.dsa);     // [NI][n_own]
+  float* ss1 = reinterpret_cast<float*>(res_smem + L.s1);       // [NI][n_own]
+  float4* scst = reinterpret_cast<float4*>(res_smem + L.cst);   // [n_own]
+  int2* sgb = reinterpret_cast<int2*>(res_smem + L.gbeg);       // [n_own]
+  int2* sgj = reinterpret_cast<int2*>(res_smem + L.gj);         // [nent]
+  int* shalo = reinterpret_cast<int*>(res_smem + L.halo);       // [nhalo]
+  double* cenv64 = reinterpret_cast<double*>(res_smem + L.cenv);  // [NI]
   float* cenvf = reinterpret_cast<float*>(cenv64 + NI);         // [NI]
   int* sflag = reinterpret_cast<int*>(res_smem + L.flag);
 
@@ -406,6 +448,7 @@ k_split_resident(FactGeom fg, SplitPtrs p, SplitConst k, ResArrays ra, int n_ste
       if (i < I) {
         sdsa[(size_t)i * n_own + ls] = fg.dsa[(size_t)i * fg.S + s];
         scc[(size_t)i * n_own + ls] = p.cc2[(size_t)i * fg.S + s];
+        ss1[(size_t)i * n_own + ls] = 0.f;
       }
     const float4* r4 = reinterpret_cast<const float4*>(ra.rec_glob[0] + (size_t)s * 8);
     float4* t4 = reinterpret_cast<float4*>(tab + (size_t)ls * 8);
@@ -429,6 +472,20 @@ k_split_resident(FactGeom fg, SplitPtrs p, SplitConst k, ResArrays ra, int n_ste
   const double escale = ra.env_scale[0];
   __syncthreads();
 
+  // cells of this thread: ls = t + q * NT (q < CPT); their gap-junction sums
+  // to owned partners are carried across the barrier in registers
+  float s2c[CPT][NI];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    const int ls = t + q * NT;
+#pragma unroll
+    for (int i = 0; i < NI; ++i) s2c[q][i] = 0.f;
+    if (ls < n_own && __float_as_int(scst[ls].w) >= 0) {
+      const int2 gb = sgb[ls];
+      res_gj_range<ZP, NI>(k, I, tab, sgj, gb.x, gb.x + gb.y, tab + (size_t)ls * 8, s2c[q]);
+    }
+  }
+
   unsigned bad = 0, neg = 0, nanv = 0;
   int step = 0;
   for (; step < n_steps; ++step) {
@@ -436,65 +493,77 @@ k_split_resident(FactGeom fg, SplitPtrs p, SplitConst k, ResArrays ra, int n_ste
     const float* T = tab + (size_t)par * n_tab * 8;
     float* Tn = tab + (size_t)(par ^ 1) * n_tab * 8;
     float* rg = ra.rec_glob[par ^ 1];
-    for (int tl = w; tl < me.ntile; tl += NW) {
-      const int ls = tl * 32 + lane;
+    // ---- a, b: halo gap junctions, per-cell terms, update
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      const int ls = t + q * NT;
+      if (ls >= n_own) continue;
       const float4 cs = scst[ls];
       const int gcnt = __float_as_int(cs.w);
-      float s1[NI];
-#pragma unroll
-      for (int i = 0; i < NI; ++i) s1[i] = 0.f;
-      if (gcnt >= 0) {
-        const float4 o0 = reinterpret_cast<const float4*>(T + (size_t)ls * 8)[0];
-        const float4 o1 = reinterpret_cast<const float4*>(T + (size_t)ls * 8)[1];
-        const float own[8] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z, o1.w};
-        float cin[NI], cenv[NI], s2[NI], dsa[NI];
-#pragma unroll
-        for (int i = 0; i < NI; ++i) {
-          cin[i] = (i < I && i < 7) ? own[i] : 0.f;
-          cenv[i] = (i < I) ? cenvf[i] : 0.f;
-          dsa[i] = (i < I) ? sdsa[(size_t)i * n_own + ls] : 0.f;
-          s2[i] = 0.f;
-        }
-        const float v1 = o1.w + 1.0e-25f;
-        const int2* e = sgj + sgb[ls];
-        for (int j = 0; j < gcnt; ++j) {
-          const int2 en = e[j];
-          const float4* r4 = reinterpret_cast<const float4*>(T + (size_t)en.x * 8);
-          fact_gj_add<ZP, NI>(k, I, v1, cin, r4[0], r4[1], __int_as_float(en.y), s2);
-        }
-        fact_trans<ZP, NI>(k, I, v1, cin, cenv, pc, dsa, cs.x, s1);
-        float rec[8];
-        fact_update<NI>(k, I, s1, s2, cs.y, cs.z, scc + ls, (size_t)n_own, rec, bad, neg, nanv);
-        const float4 r0 = make_float4(rec[0], rec[1], rec[2], rec[3]);
-        const float4 r1 = make_float4(rec[4], rec[5], rec[6], rec[7]);
-        reinterpret_cast<float4*>(Tn + (size_t)ls * 8)[0] = r0;
-        reinterpret_cast<float4*>(Tn + (size_t)ls * 8)[1] = r1;
-        reinterpret_cast<float4*>(rg + (size_t)(slot0 + ls) * 8)[0] = r0;
-        reinterpret_cast<float4*>(rg + (size_t)(slot0 + ls) * 8)[1] = r1;
-      }
+      if (gcnt < 0) continue;
+      const float* own = T + (size_t)ls * 8;
+      const int2 gb = sgb[ls];
+      res_gj_range<ZP, NI>(k, I, T, sgj, gb.x + gb.y, gb.x + gcnt, own, s2c[q]);
+      const float4 o0 = reinterpret_cast<const float4*>(own)[0];
+      const float4 o1 = reinterpret_cast<const float4*>(own)[1];
+      const float ov[8] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z, o1.w};
+      float cin[NI], cenv[NI], dsa[NI], s1[NI];
 #pragma unroll
       for (int i = 0; i < NI; ++i) {
-        if (i >= I) break;
-        const float e = warp_sum_down(s1[i]);
-        if (lane == 0) tpart[tl * NI + i] = e;
+        cin[i] = (i < I && i < 7) ? ov[i] : 0.f;
+        cenv[i] = (i < I) ? cenvf[i] : 0.f;
+        dsa[i] = (i < I) ? sdsa[(size_t)i * n_own + ls] : 0.f;
       }
+      fact_trans<ZP, NI>(k, I, o1.w + 1.0e-25f, cin, cenv, pc, dsa, cs.x, s1);
+      float rec[8];
+      fact_update<NI>(k, I, s1, s2c[q], cs.y, cs.z, scc + ls, (size_t)n_own, rec, bad, neg, nanv);
+#pragma unroll
+      for (int i = 0; i < NI; ++i)
+        if (i < I) ss1[(size_t)i * n_own + ls] = s1[i];
+      const float4 r0 = make_float4(rec[0], rec[1], rec[2], rec[3]);
+      const float4 r1 = make_float4(rec[4], rec[5], rec[6], rec[7]);
+      reinterpret_cast<float4*>(Tn + (size_t)ls * 8)[0] = r0;
+      reinterpret_cast<float4*>(Tn + (size_t)ls * 8)[1] = r1;
+      reinterpret_cast<float4*>(rg + (size_t)(slot0 + ls) * 8)[0] = r0;
+      reinterpret_cast<float4*>(rg + (size_t)(slot0 + ls) * 8)[1] = r1;
     }
     __syncthreads();
-    // the CTA's partial: warp w sums ions w, w + NW, ... over the CTA's tiles in order
+    // ---- c: the CTA's partial of ion i (warp w takes ions w, w + NW, ...),
+    // lane l sums cells l, l + 32, ... in order, then a fixed shuffle tree
     float2* cp = ra.cpart + (size_t)par * gridDim.x * I;
     for (int i = w; i < I; i += NW) {
-      df a{0.f, 0.f};
-      for (int tl = lane; tl < me.ntile; tl += 32) a = df_add_f(a, tpart[tl * NI + i]);
+      const float* v = ss1 + (size_t)i * n_own;
+      float f = 0.f;
+      for (int ls = lane; ls < n_own; ls += 32) f += v[ls];
+      df a{f, 0.f};
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const df b{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
         a = df_add(a, b);
       }
-      if (lane == 0) cp[(size_t)blockIdx.x * I + i] = make_float2(a.hi, a.lo);
+      if (lane == 0) {
+        cp[(size_t)blockIdx.x * I + i] = make_float2(a.hi, a.lo);
+        res_arrive(ra.ctl);
+      }
     }
-    if (!res_grid_sync(ra.ctl, (unsigned)(step + 1) * gridDim.x + ra.barrier_bias, ra.timeout_ns, sflag)) break;
-    // the environment: every CTA sums the same partials in the same order
-    // (warp w takes ions w, w + NW, ...)
+    const bool last = step + 1 == n_steps;
+    // ---- d: gap junctions of step t+1 to owned partners, from the new table
+    if (!last) {
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) {
+        const int ls = t + q * NT;
+#pragma unroll
+        for (int i = 0; i < NI; ++i) s2c[q][i] = 0.f;
+        if (ls < n_own && __float_as_int(scst[ls].w) >= 0) {
+          const int2 gb = sgb[ls];
+          res_gj_range<ZP, NI>(k, I, Tn, sgj, gb.x, gb.x + gb.y, Tn + (size_t)ls * 8, s2c[q]);
+        }
+      }
+    }
+    // ---- e: the barrier
+    const unsigned target = (unsigned)(step + 1) * gridDim.x * (unsigned)I + ra.barrier_bias;
+    if (!res_wait(ra.ctl, target, ra.timeout_ns, sflag)) break;
+    // ---- f: the environment (identical in every CTA) and the halo records
     for (int i = w; i < I; i += NW) {
       df a{0.f, 0.f};
       for (int c = lane; c < (int)gridDim.x; c += 32) {
@@ -512,13 +581,13 @@ k_split_resident(FactGeom fg, SplitPtrs p, SplitConst k, ResArrays ra, int n_ste
         cenvf[i] = (float)v;
       }
     }
-    // the halo records of the new table
-    for (int h = t; h < me.nhalo; h += NT) {
-      const float4* r4 = reinterpret_cast<const float4*>(rg + (size_t)shalo[h] * 8);
-      float4* t4 = reinterpret_cast<float4*>(Tn + (size_t)(n_own + h) * 8);
-      t4[0] = __ldcg(r4);
-      t4[1] = __ldcg(r4 + 1);
-    }
+    if (!last)
+      for (int h = t; h < me.nhalo; h += NT) {
+        const float4* r4 = reinterpret_cast<const float4*>(rg + (size_t)shalo[h] * 8);
+        float4* t4 = reinterpret_cast<float4*>(Tn + (size_t)(n_own + h) * 8);
+        t4[0] = __ldcg(r4);
+        t4[1] = __ldcg(r4 + 1);
+      }
     __syncthreads();
   }
   // ---- write back: concentrations; CTA 0 the environment

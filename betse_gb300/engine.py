@@ -260,6 +260,18 @@ class ClusterEngine:
         _lib.check(self.lib.bx_autotune(self.h, int(n_steps), ct.byref(tpb), ct.byref(ms)), 'bx_autotune')
         return tpb.value, ms.value
 
+    def autotune_table(self, n_steps=20):
+        """Time every candidate launch configuration (as ``autotune``) and keep
+        the fastest; returns the rows as dicts (tpb, kernel, unroll, ms_per_step)."""
+        n = 32
+        tpb, ker, unr = (np.zeros(n, np.int32) for _ in range(3))
+        ms = np.zeros(n)
+        rows = ct.c_int()
+        _lib.check(self.lib.bx_autotune_table(self.h, int(n_steps), n, ct.byref(rows), _lib.iptr(tpb),
+                                              _lib.iptr(ker), _lib.iptr(unr), _lib.dptr(ms)), 'bx_autotune_table')
+        return [dict(tpb=int(tpb[r]), kernel=KERNEL_NAMES.get(int(ker[r]), str(ker[r])), unroll=int(unr[r]),
+                     ms_per_step=float(ms[r])) for r in range(rows.value)]
+
     def cell_kernel_bytes(self) -> int:
         return int(self.lib.bx_cell_kernel_bytes(self.h))
 

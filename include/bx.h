@@ -385,11 +385,18 @@ int bx_resident_info(bx_handle h, int* fits, int* grid, int* threads, int64_t* s
 int bx_resident_barrier_check(bx_handle h, int64_t timeout_ns, int* timed_out);
 
 /* Autotuner: times n_steps steps (run as bx_step runs them) for each
- * launch configuration -- CTA size and, for the split form, the tile,
- * persistent, factored and resident kernels -- on the uploaded state, keeps
- * the fastest, and restores the state so the simulation does not advance.
+ * launch configuration -- tile size and, for the split form, the tile,
+ * persistent, factored (at two load depths) and resident kernels -- on the
+ * uploaded state, keeps the fastest, and restores the state so the
+ * simulation does not advance.
  * Reports the choice and its ms per step (either pointer may be NULL). */
 int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out);
+/* The same search, reporting every candidate it timed: up to max_rows rows of
+ * (membrane slots per tile, kernel, gap junctions loaded per round by the
+ * factored kernel, ms per step); *n_rows is set to the rows written.  The
+ * fastest candidate is kept, as by bx_autotune. */
+int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* tpb, int* kernel, int* unroll,
+                      double* ms_per_step);
 
 /* Version / diagnostics. */
 int bx_abi_version(void);
