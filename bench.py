@@ -10,16 +10,22 @@ of ~100k cells (~600k membranes), no extracellular spaces, diffusivities
 log-uniform in [1e-19, 1e-16] m^2/s, dt 5e-3 s. One bench step is one run of
 1000 time steps of that cluster (the run length of the workload); W warm-up
 runs, then K timed runs bracketed by synchronisation, with the L2 flushed
-(a 256 MiB write) before every run. The plain FP64 form is timed on the same
-cluster and its Vmem after the same steps is the error reference of the split
-form.
+(a 256 MiB write) before every run. The split form runs the kernel the
+autotuner picks (its table is in the line). The plain FP64 form is timed on
+the same cluster, and both are stepped side by side from the same start to
+give the split form's Vmem error curve over the run.
 
 ``value``: device-resident throughput of the split form. ``e2e``: the same
 metric through the C ABI with host buffers: every run uploads the state from
 pinned host memory, steps, and downloads the state.
 
-``--impl reference`` times the CPU restatement of BETSE's step (the oracle,
-NumPy) on the host cores on a bounded sample of the same cluster.
+``configs``: the other workloads, each with its value, roofline and CPU
+baseline -- the ~250-cell plain FP64 case, the ~20k-cell case with
+extracellular spaces, the 512-cluster sweep, and the learned warm start.
+
+``--impl reference`` times the CPU restatement of BETSE's step (C with
+OpenMP on every host thread; the NumPy oracle where no C compiler exists) on
+a bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -306,50 +312,154 @@ def batch_fields_timing(n_clusters=128):
                     'BF16x3 tcgen05 GEMM with a per-column delta^2 and one FP64 refinement'}
 
 
-def secondary(stream, flush):
-    """Extra lines of evidence at N=1: the ECM workload's step rates and the
-    environment-field products at its full grid (output-only, sampled steps)."""
+def survey_bytes(form, C, M, G=0, ecm=False):
+    """Algorithmic bytes of one time step by the per-array count BETSE's step
+    implies (each array once at its stored width, reads plus writes): plain
+    FP64 104 B per membrane + 124 B per cell; split form 64 + 112; with
+    extracellular spaces 4 B more per membrane (map_mem2ecm) and 160 B per
+    grid cell (six ions' concentrations read and written, D, E_x, E_y)."""
+    b = (104 * M + 124 * C) if form == 'fp64' else (64 * M + 112 * C)
+    if ecm:
+        b += 4 * M + 160 * G
+    return b
+
+
+def roofline_entry(bytes_per_step, s_per_step, kernel, note=None, survey=None):
+    hbm, src = peaks()
+    a = bytes_per_step / s_per_step / 1e9
+    r = {'bound': 'hbm', 'achieved': a, 'peak': hbm, 'unit': 'GB/s', 'frac': a / hbm,
+         'algorithmic_bytes_per_step': int(bytes_per_step), 'kernel': kernel, 'peak_source': src}
+    if survey is not None:
+        r['survey_bytes_per_step'] = int(survey)
+        r['frac_on_survey_bytes'] = survey / s_per_step / 1e9 / hbm
+    if note:
+        r['note'] = note
+    return r
+
+
+def timed_run_ms(eng, T, stream, flush, reps=3):
+    """Best of `reps` runs of T time steps on `stream` (CUDA events), the L2
+    flushed before each; one untimed run first."""
     import torch
+    eng.step(T, stream=stream.cuda_stream)
+    ms = []
+    for _ in range(reps):
+        flush.fill_(1)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.step(T, stream=stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    eng.check_stable()
+    return min(ms)
+
+
+def config_plain250(wl, stream, flush, cpu=True):
+    """Config 1: the plain FP64 step on the ~250-cell cluster, 2000 steps."""
     from betse_gb300.engine import ClusterEngine
-    w, g, p, Dm, st, D_env = build_workload('ecm20k')
-    T = 100
-    out = {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems,
-           'grid': list(g.grid_shape), 'time_steps_timed': T}
-    for prec in ('fp64', 'split'):
-        e = ClusterEngine(g, p, prec)
+    w, g, p, Dm, st, D_env = wl
+    T = w['time_steps']
+    with ClusterEngine(g, p, 'fp64') as e:
         e.set_membrane_diffusivity(Dm)
-        e.set_env_diffusivity(D_env)
         e.upload(**st)
-        e.step(T, stream=stream.cuda_stream)
-        ms = []
-        for _ in range(3):
-            flush.fill_(1)
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            e.step(T, stream=stream.cuda_stream)
-            b.record(stream)
-            torch.cuda.synchronize()
-            ms.append(a.elapsed_time(b))
-        e.check_stable()
-        out[prec] = {'value': g.n_mems * T / (min(ms) / 1e3), 'unit': UNIT,
-                     'ms_per_time_step': min(ms) / T}
-        if prec == 'fp64':
-            fields_eng = e
-        else:
-            e.close()
-    # the dense lapENVinv products: 8*G^2 bytes per product (the operator, once)
+        e.autotune(3)
+        ms = timed_run_ms(e, T, stream, flush)
+        e.upload(**st)
+        kms = e.time_cell_kernel(200)
+        kb = e.cell_kernel_bytes()
+    out = {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems, 'time_steps_per_run': T,
+           'form': 'plain FP64', 'value': g.n_mems * T / (ms / 1e3), 'unit': UNIT, 'ms_per_run': ms,
+           'roofline': roofline_entry(kb, kms / 1e3, 'k_cell_step<double>',
+                                      note='a 1.4k-membrane cluster fills a few CTAs: launch- and '
+                                           'latency-bound, the roofline is far away by construction',
+                                      survey=survey_bytes('fp64', g.n_cells, g.n_mems)),
+           'kernel_launches_per_step': 2}
+    if cpu:
+        out['cpu_baseline'] = cpu_baseline(g, p, Dm, st, budget_s=6.0)
+    return out
+
+
+def config_ecm20k(wl, stream, flush, cpu=True):
+    """Config 2: extracellular spaces, ~20k cells on a 199x200 grid, 500
+    steps; the plain FP64 form (the config's) and the split form."""
+    from betse_gb300.engine import ClusterEngine
+    w, g, p, Dm, st, D_env = wl
+    T = w['time_steps']
+    G = g.n_grid
+    out = {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems, 'grid': list(g.grid_shape),
+           'time_steps_per_run': T}
+    for prec in ('fp64', 'split'):
+        with ClusterEngine(g, p, prec) as e:
+            e.set_membrane_diffusivity(Dm)
+            e.set_env_diffusivity(D_env)
+            e.upload(**st)
+            e.autotune(5)
+            ms = timed_run_ms(e, T, stream, flush)
+        sv = survey_bytes(prec, g.n_cells, g.n_mems, G, ecm=True)
+        out[prec] = {'value': g.n_mems * T / (ms / 1e3), 'unit': UNIT, 'ms_per_run': ms,
+                     'ms_per_time_step': ms / T,
+                     'roofline': roofline_entry(sv, ms / 1e3 / T, 'whole step (cell kernel + grid stencils)',
+                                                note='bytes by the per-array count with the grid terms; the '
+                                                     'per-kernel shares are in profiles/launch_list_ecm20k.md')}
+    out['value'] = out['fp64']['value']
+    out['unit'] = UNIT
+    out['form'] = 'plain FP64 (split form beside it)'
+    if cpu:
+        out['cpu_baseline'] = cpu_baseline(g, p, Dm, st, budget_s=6.0, D_env=D_env)
+    return out
+
+
+def config_sweep512(wl, stream, flush, cpu=True):
+    """Config 4: 512 clusters of uneven size in one batch, split form, the
+    kernel the autotuner picks, 1000 steps per run."""
+    w, gs, ps, Dms, sts, _ = wl
+    T = w['time_steps']
+    S = Sweep(gs, ps, Dms, sts, 'split')
+    table = S.e.autotune_table(64)
+    tpb, kind = S.launch_config()
+    ms = timed_run_ms(S, T, stream, flush)
+    S.upload()
+    kms = S.time_cell_kernel(50)
+    kb = S.cell_kernel_bytes()
+    M, C = S.n_mems, S.n_cells
+    kname = KERNEL_NAMES.get(kind, str(kind))
+    out = {'workload': w['desc'], 'clusters': len(gs), 'cells': C, 'membranes': M, 'time_steps_per_run': T,
+           'form': 'split', 'value': M * T / (ms / 1e3), 'unit': UNIT, 'ms_per_run': ms,
+           'autotuned': {'tpb': tpb, 'kernel': kname}, 'autotune_table': table,
+           'roofline': roofline_entry(kb, kms / 1e3, kname, survey=survey_bytes('split', C, M),
+                                      note='algorithmic bytes of the kernel that runs (the factored form '
+                                           'reads one sum of Dm*mem_sa per cell instead of Dm per membrane); '
+                                           'frac_on_survey_bytes counts the per-membrane arrays instead')}
+    S.close()
+    if cpu:
+        out['cpu_baseline'] = cpu_baseline_sweep(gs, ps, Dms, sts, budget_s=8.0)
+    return out
+
+
+def dense_products(stream, flush, wl_ecm):
+    """Output-side dense products: lapENVinv at the ECM workload's full grid
+    (double-float streaming GEMV) and the BF16x3 tcgen05 GEMM of a
+    lapGJinv-sized operator."""
+    from betse_gb300.engine import ClusterEngine
+    w, g, p, Dm, st, D_env = wl_ecm
+    out = {}
     G = g.n_grid
     phys = os.sysconf('SC_PHYS_PAGES') * os.sysconf('SC_PAGE_SIZE')
     if phys < 4 * 8 * G * G:
         out['env_fields'] = {'skipped': f'host memory {phys >> 30} GiB too small for the operator'}
     else:
-        A = np.empty((G, G))
-        A.fill(1e-12)  # timing only: the products stream the operator whatever it holds
-        fields_eng.set_lap_env_inv(A)
-        del A
-        fields_eng.step(1, outputs=True)
-        ms_f, ms_p = fields_eng.time_env_fields(5)
+        with ClusterEngine(g, p, 'fp64') as fields_eng:
+            fields_eng.set_membrane_diffusivity(Dm)
+            fields_eng.set_env_diffusivity(D_env)
+            fields_eng.upload(**st)
+            A = np.empty((G, G))
+            A.fill(1e-12)  # timing only: the products stream the operator whatever it holds
+            fields_eng.set_lap_env_inv(A)
+            del A
+            fields_eng.step(1, outputs=True)
+            ms_f, ms_p = fields_eng.time_env_fields(5)
         hbm, src = peaks()
         gbs = 8.0 * G * G / (ms_p / 1e3) / 1e9
         out['env_fields'] = {
@@ -358,8 +468,6 @@ def secondary(stream, flush):
             'roofline': {'bound': 'hbm', 'achieved': gbs, 'peak': hbm, 'unit': 'GB/s',
                          'frac': gbs / hbm, 'algorithmic_bytes_per_launch': 8 * G * G,
                          'kernel': 'k_dense_rows2_df', 'peak_source': src}}
-    fields_eng.close()
-    # tensor-core stage: BF16x3 dense-operator GEMM (lapGJinv-sized, 20k cells)
     from betse_gb300.dense import DenseOperator
     n = 20480
     A = np.empty((n, n))
@@ -513,6 +621,9 @@ def main():
 
     w, g, p, Dm, st, D_env = build_workload(args.workload)
     sweep = bool(w.get('sweep'))
+    full = rank == 0 and world == 1 and args.workload == 'cluster100k' and not args.no_secondary
+    # the other configurations' workloads, built before the GPU is touched
+    others = {n: build_workload(n) for n in ('plain250', 'ecm20k', 'sweep512')} if full else {}
     import torch
     dist = None
     if world > 1:
@@ -546,10 +657,11 @@ def main():
     plain = make('fp64')
     n_mems = split.n_mems if sweep else g.n_mems
     n_cells = split.n_cells if sweep else g.n_cells
-    split.autotune(20)
+    tune_table = split.autotune_table(64)
     plain.autotune(3)
     tune_split = split.launch_config()
     tune_plain = plain.launch_config()
+    kname = KERNEL_NAMES.get(tune_split[1], str(tune_split[1]))
 
     def barrier():
         torch.cuda.synchronize()
@@ -586,26 +698,38 @@ def main():
     t_max, value = job_throughput(sum(ms_split) / 1e3, n_mems * T * args.steps, world, dist, dev)
     plain_value = n_mems * T * len(ms_plain) / (sum(ms_plain) / 1e3)
 
-    # ---- Vmem error of the split form against the plain FP64 form, equal steps
-    e_s, e_p = make('split'), make('fp64')
-    e_s.step(T)
-    e_p.step(T)
-    vm_err = float(np.max(np.abs(e_s.download()['vm'] - e_p.download()['vm'])))
-    e_p.close()
+    # ---- Vmem error of the split form against the plain FP64 form (which
+    # matches the FP64 oracle at 1e-10), stepped side by side from the same
+    # start, at checkpoints up to the run length (the autotuned handles
+    # themselves, back at the initial state)
+    e_s, e_p = split, plain
+    for e_ in (e_s, e_p):
+        e_.upload(**({} if sweep else st))
+    curve, done = [], 0
+    for cp in sorted({c for c in (1, 10, 100, 250, 500, 1000, T) if c <= T}):
+        e_s.step(cp - done)
+        e_p.step(cp - done)
+        done = cp
+        curve.append([cp, float(np.max(np.abs(e_s.download()['vm'] - e_p.download()['vm'])))])
+    vm_err = curve[-1][1]
 
-    # ---- roofline of the dominant kernel (the fused cell step), events on its stream
+    # ---- roofline of the split kernel the autotuner chose, events on its stream
     e_s.upload(**({} if sweep else st))
-    e_s.autotune(10)
-    kern_ms = e_s.time_cell_kernel(50)
+    kern_ms = e_s.time_cell_kernel(200)
     kbytes = e_s.cell_kernel_bytes()
-    hbm, src = peaks()
-    achieved = kbytes / (kern_ms / 1e3) / 1e9
     traffic = None
-    kname = 'k_split_persist' if e_s.launch_config()[1] else 'k_split_step'
     tp = os.path.join(ROOT, 'profiles', f'{kname}_{args.workload}.traffic.json')
     if os.path.exists(tp):
         tj = json.load(open(tp))
-        traffic = int(tj['dram_bytes_per_launch'] * n_mems / tj['membranes'])
+        traffic = int(tj.get('dram_bytes_per_step', tj.get('dram_bytes_per_launch')) * n_mems / tj['membranes'])
+    roof = roofline_entry(kbytes, kern_ms / 1e3, kname, survey=survey_bytes('split', n_cells, n_mems),
+                          note='achieved = the chosen kernel\'s algorithmic bytes per time step (each array once '
+                               'at its stored width; the factored kernels read one sum of Dm*mem_sa per cell '
+                               'where the per-membrane form reads Dm per membrane) / its time per step; the '
+                               'resident kernel keeps that data in shared memory across steps, so HBM does '
+                               'not bound it; frac_on_survey_bytes counts the per-membrane arrays')
+    roof['traffic'] = traffic
+    roof['ms_per_step'] = kern_ms
 
     # ---- end to end through the C ABI with host buffers (pinned)
     def pinned(a):
@@ -642,6 +766,8 @@ def main():
         if k >= args.warmup:
             t_e2e.append(t1 - t0)
     e2e_val = n_mems * T * len(t_e2e) * world / sum(t_e2e)
+    for e in (split, plain):
+        e.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -649,46 +775,47 @@ def main():
             cpu = cpu_baseline_sweep(g, p, Dm, st)
         else:
             cpu = cpu_baseline(g, p, Dm, st, D_env=D_env)
-    extra = init_steady = None
-    if rank == 0 and world == 1 and args.workload == 'cluster100k' and not args.no_secondary:
-        extra = secondary(stream, flush)
+    configs = extra = None
+    if full:
+        cpu_on = not args.no_cpu_baseline
+        configs = {'plain250': config_plain250(others['plain250'], stream, flush, cpu_on),
+                   'ecm20k': config_ecm20k(others['ecm20k'], stream, flush, cpu_on),
+                   'sweep512': config_sweep512(others['sweep512'], stream, flush, cpu_on),
+                   'warm_start': init_time_to_steady()}
+        extra = dense_products(stream, flush, others['ecm20k'])
         extra['batch_env_fields'] = batch_fields_timing()
-        init_steady = init_time_to_steady()
 
     if rank == 0:
         line = {
             'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_max * 1e3 / args.steps,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-            'dtype': 'f32 fluxes / f64 concentrations+Vmem', 'data': 'synthetic',
+            'dtype': 'f32 fluxes and pumps; compensated-f32 (hi+lo) concentrations and charge; f32 Vmem record',
+            'data': 'synthetic',
             'config': {'workload': w['desc'], 'cells': n_cells, 'membranes': n_mems,
                        'time_steps_per_step': T, 'precision': 'split',
                        'l2': 'flushed (256 MiB write) before every timed run',
                        'parallelism': f'replicas x{world}',
-                       'autotuned_launch': {'split': {'cta_threads': tune_split[0], 'persistent': tune_split[1]},
-                                            'plain_fp64': {'cta_threads': tune_plain[0]}}},
+                       'autotuned_launch': {'split': {'tpb': tune_split[0], 'kernel': kname},
+                                            'plain_fp64': {'cta_threads': tune_plain[0]}},
+                       'autotune_table': tune_table},
             'plain_fp64': {'value': plain_value, 'unit': UNIT,
                            'ms_per_step': sum(ms_plain) / len(ms_plain),
                            'speedup_split_vs_plain': value / world / plain_value,
-                           'vm_max_abs_err_V': vm_err, 'vm_err_after_steps': T},
-            'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
-                         'frac': achieved / hbm, 'traffic': traffic,
-                         'kernel': f'{kname} (fused membrane fluxes + cell update, split form)',
-                         'algorithmic_bytes_per_launch': kbytes, 'launch_ms': kern_ms,
-                         'peak_source': src},
+                           'vm_max_abs_err_V': vm_err, 'vm_err_after_steps': T,
+                           'vm_err_curve_V': curve},
+            'roofline': roof,
             'cpu_baseline': cpu,
             'e2e': {'value': e2e_val, 'unit': UNIT, 'h2d_bytes_per_step': int(h2d),
                     'd2h_bytes_per_step': int(d2h)},
             'gpu_launches': int(launches),
             'clocks': clk,
         }
+        if configs is not None:
+            line['configs'] = configs
         if extra is not None:
             line['secondary'] = extra
-        if init_steady is not None:
-            line['init_time_to_steady'] = init_steady
         print(json.dumps(line), flush=True)
-    for e in (split, plain, e_s):
-        e.close()
     if dist is not None:
         dist.destroy_process_group()
 
