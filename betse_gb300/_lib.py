@@ -130,6 +130,7 @@ SIGNATURES = {
     'bx_abi_version': (ct.c_int, []),
     'bx_last_error': (ct.c_char_p, []),
     'bx_launch_count': (ct.c_int64, [ct.c_void_p]),
+    'bx_cluster_info': (ct.c_int, [ct.c_void_p, _ip]),
     'bx_time_cell_kernel': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_double)]),
     'bx_cell_kernel_bytes': (ct.c_int64, [ct.c_void_p]),
     'bx_set_launch_config': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int]),

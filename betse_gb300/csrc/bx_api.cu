@@ -1404,6 +1404,12 @@ int bx_set_env_diffusivity(bx_handle h, const double* D_env) {
   return BX_OK;
 }
 
+// FP32 copy of the well-mixed environment, rounded to nearest on the device
+__global__ void k_round_to_float(const double* __restrict__ a, float* __restrict__ b, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = __double2float_rn(a[i]);
+}
+
 // Device staging for state transfers: the caller's arrays in BETSE's layouts
 // (allocated at the first transfer).
 int ensure_state_staging(bx_cluster* h) {
@@ -1471,9 +1477,9 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
   h->have_state = false;
   double* vm_dst = split ? h->st_vm : h->d_vm[0];
   double* cc_dst = split ? h->st_cc : h->d_cc;
-  BX_CU(cudaMemcpyAsync(vm_dst, s->vm, (size_t)M * sizeof(double), cudaMemcpyHostToDevice, st));
-  BX_CU(cudaMemcpyAsync(cc_dst, s->cc_cells, (size_t)I * C * sizeof(double), cudaMemcpyHostToDevice, st));
-  BX_CU(cudaMemcpyAsync(h->st_cam, s->cc_at_mem, (size_t)I * M * sizeof(double), cudaMemcpyHostToDevice, st));
+  BX_CU(cudaMemcpyAsync(vm_dst, s->vm, (size_t)M * sizeof(double), cudaMemcpyDefault, st));
+  BX_CU(cudaMemcpyAsync(cc_dst, s->cc_cells, (size_t)I * C * sizeof(double), cudaMemcpyDefault, st));
+  BX_CU(cudaMemcpyAsync(h->st_cam, s->cc_at_mem, (size_t)I * M * sizeof(double), cudaMemcpyDefault, st));
   BX_CU(cudaMemsetAsync(h->d_flag, 0, 2 * sizeof(int), st));
   const int tb = 256;
   bx::k_state_check<<<(M + tb - 1) / tb, tb, 0, st>>>(io, vm_dst, h->st_cam, split ? 1 : 0, h->d_flag);
@@ -1494,36 +1500,34 @@ int bx_state_upload(bx_handle h, const bx_state* s) {
     BX_CU(cudaGetLastError());
     if (h->vgj) {
       if (s->gjopen)
-        BX_CU(cudaMemcpyAsync(h->st_go, s->gjopen, (size_t)M * sizeof(double), cudaMemcpyHostToDevice, st));
+        BX_CU(cudaMemcpyAsync(h->st_go, s->gjopen, (size_t)M * sizeof(double), cudaMemcpyDefault, st));
       else
         BX_CU(cudaMemcpyAsync(h->st_go, h->d_gj_w, (size_t)M * sizeof(double), cudaMemcpyDeviceToDevice, st));
       BX_CU(cudaMemsetAsync(h->t_gjo, 0, (size_t)h->Q * sizeof(float), st));
       bx::k_state_pack_gjo<<<(M + tb - 1) / tb, tb, 0, st>>>(io, h->st_go, h->t_gjo);
       BX_CU(cudaGetLastError());
     }
-    BX_CU(cudaMemcpyAsync(h->d_cenv, s->cc_env, nenv * sizeof(double), cudaMemcpyHostToDevice, st));
+    BX_CU(cudaMemcpyAsync(h->d_cenv, s->cc_env, nenv * sizeof(double), cudaMemcpyDefault, st));
     if (h->ecm) {
-      BX_CU(cudaMemcpyAsync(h->d_Ex, s->E_env_x, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
-      BX_CU(cudaMemcpyAsync(h->d_Ey, s->E_env_y, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
+      BX_CU(cudaMemcpyAsync(h->d_Ex, s->E_env_x, (size_t)h->G * sizeof(double), cudaMemcpyDefault, st));
+      BX_CU(cudaMemcpyAsync(h->d_Ey, s->E_env_y, (size_t)h->G * sizeof(double), cudaMemcpyDefault, st));
     } else {
-      std::vector<float> cef(nenv);
-      for (size_t q = 0; q < nenv; ++q) cef[q] = (float)s->cc_env[q];
-      BX_CU(cudaMemcpyAsync(h->s_cenv_f, cef.data(), nenv * sizeof(float), cudaMemcpyHostToDevice, st));
-      BX_CU(cudaStreamSynchronize(st));   // cef is a local buffer
+      k_round_to_float<<<(unsigned)((nenv + 255) / 256), 256, 0, st>>>(h->d_cenv, h->s_cenv_f, (int)nenv);
+      BX_CU(cudaGetLastError());
     }
   } else {
     bx::k_state_pack_ccm<<<(C + tb - 1) / tb, tb, 0, st>>>(io, h->st_cam, h->d_ccm[0]);
     BX_CU(cudaGetLastError());
-    BX_CU(cudaMemcpyAsync(h->d_cenv, s->cc_env, nenv * sizeof(double), cudaMemcpyHostToDevice, st));
+    BX_CU(cudaMemcpyAsync(h->d_cenv, s->cc_env, nenv * sizeof(double), cudaMemcpyDefault, st));
     if (h->vgj) {
       if (s->gjopen)
-        BX_CU(cudaMemcpyAsync(h->d_gjo, s->gjopen, (size_t)M * sizeof(double), cudaMemcpyHostToDevice, st));
+        BX_CU(cudaMemcpyAsync(h->d_gjo, s->gjopen, (size_t)M * sizeof(double), cudaMemcpyDefault, st));
       else
         BX_CU(cudaMemcpyAsync(h->d_gjo, h->d_gj_w, (size_t)M * sizeof(double), cudaMemcpyDeviceToDevice, st));
     }
     if (h->ecm) {
-      BX_CU(cudaMemcpyAsync(h->d_Ex, s->E_env_x, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
-      BX_CU(cudaMemcpyAsync(h->d_Ey, s->E_env_y, (size_t)h->G * sizeof(double), cudaMemcpyHostToDevice, st));
+      BX_CU(cudaMemcpyAsync(h->d_Ex, s->E_env_x, (size_t)h->G * sizeof(double), cudaMemcpyDefault, st));
+      BX_CU(cudaMemcpyAsync(h->d_Ey, s->E_env_y, (size_t)h->G * sizeof(double), cudaMemcpyDefault, st));
     }
   }
   if (h->r_ctl) BX_CU(cudaMemsetAsync(h->r_ctl, 0, 2 * sizeof(unsigned), st));   // a fresh state: no timeout
@@ -1546,7 +1550,7 @@ int bx_state_download(bx_handle h, bx_state* s) {
   const size_t nenv = h->ecm ? (size_t)I * h->G : (size_t)h->ncl * I;
   const int tb = 256;
   auto d2h = [&](double* dst, const double* src, size_t n) {
-    return dst ? cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st) : cudaSuccess;
+    return dst ? cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDefault, st) : cudaSuccess;
   };
   if (h->mode == MODE_SPLIT) {
     const int n = std::max(M, C);
@@ -1715,7 +1719,7 @@ int bx_outputs_download(bx_handle h, bx_outputs* o) {
       {o->v_env, h->ecm ? h->d_venv : nullptr, G},
   };
   for (const Pair& p : pairs)
-    if (p.dst && p.src) BX_CU(cudaMemcpy(p.dst, p.src, p.n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (p.dst && p.src) BX_CU(cudaMemcpy(p.dst, p.src, p.n * sizeof(double), cudaMemcpyDefault));
   return BX_OK;
 }
 
@@ -1799,6 +1803,13 @@ int64_t bx_cell_kernel_bytes(bx_handle h) {
 }
 
 int64_t bx_launch_count(bx_handle h) { return h ? h->launches : -1; }
+
+int bx_cluster_info(bx_handle h, int32_t* info) {
+  if (!h || !info) return fail(BX_EINVAL, "null argument");
+  const int32_t v[8] = {h->ncl, h->C, h->M, h->I, h->ny, h->nx, h->ecm ? 1 : 0, h->precision};
+  for (int q = 0; q < 8; ++q) info[q] = v[q];
+  return BX_OK;
+}
 
 int bx_get_launch_config(bx_handle h, int* tpb, int* kernel) {
   if (!h || !tpb || !kernel) return fail(BX_EINVAL, "null argument");
@@ -2153,7 +2164,7 @@ int bx_batch_env_fields(bx_handle h, const double* D_env_weight, double* v_env, 
          *Fdy = b[8], *Ex = b[9], *Ey = b[10], *jx = b[11], *jy = b[12], *Bf = b[13], *Jex = b[14], *Jey = b[15],
          *w = b[16];
   cudaStream_t s = h->stream;
-  if (D_env_weight) BX_CU(cudaMemcpyAsync(w, D_env_weight, (size_t)Gt * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (D_env_weight) BX_CU(cudaMemcpyAsync(w, D_env_weight, (size_t)Gt * sizeof(double), cudaMemcpyDefault, s));
   bx::FieldGrid base = field_grid(h);
   const double* vm = (h->mode == MODE_SPLIT) ? h->o_vm_mem : h->d_vm[h->parity ^ 1];
   const int* ci = h->bf_ci;
@@ -2182,7 +2193,7 @@ int bx_batch_env_fields(bx_handle h, const double* D_env_weight, double* v_env, 
   double* dst[6] = {v_env, E_env_x, E_env_y, J_env_x, J_env_y, B_field};
   const double* src[6] = {venv, Ex, Ey, Jex, Jey, Bf};
   for (int q = 0; q < 6; ++q)
-    if (dst[q]) BX_CU(cudaMemcpyAsync(dst[q], src[q], (size_t)Gt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (dst[q]) BX_CU(cudaMemcpyAsync(dst[q], src[q], (size_t)Gt * sizeof(double), cudaMemcpyDefault, s));
   BX_CU(cudaStreamSynchronize(s));
   for (const auto& fs : h->fshapes) {
     int timed_out = 0;
@@ -2303,7 +2314,7 @@ int prepare_env_fields(bx_cluster* h, const double* D_env_weight, double** d_w) 
   *d_w = nullptr;
   if (D_env_weight) {
     double* w = h->f_buf + (size_t)kFieldBufs * G;  // the spare slot
-    BX_CU(cudaMemcpyAsync(w, D_env_weight, G * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    BX_CU(cudaMemcpyAsync(w, D_env_weight, G * sizeof(double), cudaMemcpyDefault, h->stream));
     *d_w = w;
   }
   return BX_OK;
@@ -2323,7 +2334,7 @@ int bx_env_fields(bx_handle h, const double* D_env_weight, double* v_env, double
   double* dst[6] = {v_env, E_env_x, E_env_y, J_env_x, J_env_y, B_field};
   for (int q = 0; q < 6; ++q)
     if (dst[q])
-      BX_CU(cudaMemcpyAsync(dst[q], h->f_buf + (size_t)q * G, G * sizeof(double), cudaMemcpyDeviceToHost,
+      BX_CU(cudaMemcpyAsync(dst[q], h->f_buf + (size_t)q * G, G * sizeof(double), cudaMemcpyDefault,
                             h->stream));
   BX_CU(cudaStreamSynchronize(h->stream));
   return BX_OK;

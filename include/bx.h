@@ -217,7 +217,8 @@ int bx_set_boundary_potential(bx_handle h, const double* Phi_b);
 int bx_set_params(bx_handle h, const bx_params* p);
 
 /* Copy state in / out (synchronous on the handle's stream).  The arrays
- * cross as they are and are checked and re-laid on the device.  Upload
+ * cross as they are and are checked and re-laid on the device; each pointer
+ * may be host or device memory (copies use unified addressing).  Upload
  * refuses (BX_EINVAL) a cc_at_mem that differs within a cell and, in the
  * split form, a vm that is not uniform within a cell; after a refused upload
  * the handle holds no state until the next successful one.  Download fills
@@ -229,7 +230,7 @@ int bx_state_download(bx_handle h, bx_state* s);
  * own stream).  If want_outputs != 0 the last step also computes the step
  * outputs.  Asynchronous: returns after enqueueing; bx_status synchronises. */
 int bx_step(bx_handle h, int n_steps, int want_outputs, void* stream);
-int bx_outputs_download(bx_handle h, bx_outputs* o);
+int bx_outputs_download(bx_handle h, bx_outputs* o);   /* host or device destinations */
 int bx_status(bx_handle h, bx_step_status* st);
 /* Steady-state residual of each cluster after a step with want_outputs:
  * per_cluster[c] = max over its membranes of |dVm/dt| (sim.dvm, sim.py:2083),
@@ -403,6 +404,10 @@ int bx_abi_version(void);
 const char* bx_last_error(void);
 /* Number of kernel launches this handle has enqueued (cumulative). */
 int64_t bx_launch_count(bx_handle h);
+/* Sizes of a handle, for callers that hold only the handle (the PyTorch
+ * operators): info[8] = {n_clusters, n_cells, n_mems, n_ions, grid_ny,
+ * grid_nx, is_ecm, precision} (cells and membranes summed over a batch). */
+int bx_cluster_info(bx_handle h, int32_t* info);
 
 #ifdef __cplusplus
 }

@@ -82,3 +82,62 @@ def test_split_matches_oracle_at_full_size(case):
     err = np.max(np.abs(out['vm'] - s.vm))
     assert err < 1e-6, (name, err)
     assert gi.rel_err(out['cc_cells'], s.cc_cells) < 1e-6
+
+
+# ---- the full run length of each workload against the C restatement of the
+# oracle (OpenMP; the same step, pinned to BETSE in test_oracle_c.py)
+HORIZON = {'cluster100k': 1000, 'ecm20k': 500}
+CHECKPOINTS = (1, 10, 100, 500, 1000)
+
+
+def _c_stepper(g, p, Dm, st, D_env):
+    cstep = pytest.importorskip('oracle.cstep')
+    try:
+        cstep.build()
+    except Exception as e:          # no C compiler on this host
+        pytest.skip(f'C restatement not built: {e}')
+    geo, par, s = from_workload(g, p, Dm, st, D_env)
+    return cstep.Stepper(geo, par, s)
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split'])
+def test_full_horizon_matches_c_oracle(case, precision):
+    """FP64: concentrations within 1e-10 relative and Vmem within 1e-10
+    relative plus the FP64 cancellation floor at every checkpoint of the
+    run; split form (the kernel the autotuner picks): |Vmem - Vmem_oracle| <
+    1e-6 V at every checkpoint.  The per-checkpoint errors are printed (run
+    with -s to see config 3's error curve)."""
+    name, g, p, Dm, st, D_env = case
+    n_total = HORIZON[name]
+    ref = _c_stepper(g, p, Dm, st, D_env)
+    curve = []
+    with _engine(g, p, Dm, st, D_env, precision) as e:
+        if precision == 'split':
+            e.autotune(20)
+        done = 0
+        for cp in [c for c in CHECKPOINTS if c <= n_total]:
+            e.step(cp - done)
+            ref.step(cp - done)
+            done = cp
+            e.check_stable()
+            out = e.download()
+            r = ref.state()
+            err = float(np.max(np.abs(out['vm'] - r['vm'])))
+            e_cc = gi.rel_err(out['cc_cells'], r['cc_cells'])
+            e_env = gi.rel_err(out['cc_env'], r['cc_env'] if p.is_ecm else r['cc_env'][:, 0])
+            curve.append((cp, err, e_cc, e_env))
+            if precision == 'fp64':
+                bound = 1e-10 * np.max(np.abs(r['vm'])) + _vm_floor(p, g, r['cc_cells'])
+                assert err <= bound, (name, cp, err, bound)
+                assert e_cc < 1e-10, (name, cp, e_cc)
+                assert e_env < 1e-10, (name, cp, e_env)
+                if p.is_ecm:
+                    assert gi.rel_err(out['E_env_x'], np.ravel(r['E_env_x'])) < 1e-8, (name, cp)
+                    assert gi.rel_err(out['E_env_y'], np.ravel(r['E_env_y'])) < 1e-8, (name, cp)
+            else:
+                assert err < 1e-6, (name, cp, err)
+                assert e_cc < 1e-5, (name, cp, e_cc)
+        kernel = e.launch_config()
+    print(f'\n{name} {precision} launch {kernel}: step, max|dVm| (V), cc rel, env rel')
+    for row in curve:
+        print('  %5d  %.3e  %.3e  %.3e' % row)
