@@ -99,6 +99,8 @@ SIGNATURES = {
     'bx_outputs_download': (ct.c_int, [ct.c_void_p, ct.POINTER(BxOutputs)]),
     'bx_status': (ct.c_int, [ct.c_void_p, ct.POINTER(BxStepStatus)]),
     'bx_set_lap_env_inv': (ct.c_int, [ct.c_void_p, _dp]),
+    'bx_build_lap_env_inv': (ct.c_int, [ct.c_void_p]),
+    'bx_lap_env_inv_build': (ct.c_int, [ct.c_int, ct.c_int, ct.c_double, ct.c_void_p, ct.c_int64, ct.c_void_p]),
     'bx_max_abs_dvm': (ct.c_int, [ct.c_void_p, _dp]),
     'bx_batch_set_lap_env_inv': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_double, _dp]),
     'bx_batch_env_fields': (ct.c_int, [ct.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),

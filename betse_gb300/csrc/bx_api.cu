@@ -26,6 +26,7 @@
 #include "bx_factored.cuh"
 #include "bx_fields.cuh"
 #include "bx_launch.cuh"
+#include "bx_lapinv.cuh"
 #include "bx_split.cuh"
 #include "bx_state.cuh"
 
@@ -2200,6 +2201,32 @@ int bx_batch_env_fields(bx_handle h, const double* D_env_weight, double* v_env, 
     if ((rc = bx_dense_op_status(fs.op, &timed_out)) != BX_OK) return rc;
     if (timed_out) return fail(BX_ECUDA, "bx_batch_env_fields: tensor-core pipeline wait timed out");
   }
+  return BX_OK;
+}
+
+int bx_lap_env_inv_build(int ny, int nx, double delta, double* A, int64_t lda, void* stream) {
+  if (!A || ny < 3 || nx < 3 || !(delta > 0.0) || lda < (int64_t)ny * nx)
+    return fail(BX_EINVAL, "bx_lap_env_inv_build: need ny, nx >= 3, delta > 0, lda >= ny*nx");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  BX_CU(cudaMemsetAsync(A, 0, (size_t)ny * nx * (size_t)lda * sizeof(double), s));
+  BX_CU(bx::build_lap_env_inv<double>(ny, nx, delta, A, (size_t)lda, s));
+  return BX_OK;
+}
+
+int bx_build_lap_env_inv(bx_handle h) {
+  if (!h) return fail(BX_EINVAL, "null handle");
+  if (h->ncl != 1) return fail(BX_EINVAL, "bx_build_lap_env_inv: single-cluster handles only");
+  const size_t G = (size_t)h->G;
+  const size_t ld = G + (G & 1);
+  h->f_ld = (int)ld;
+  if (!h->f_lap && cudaMalloc(&h->f_lap, G * ld * sizeof(float2)) != cudaSuccess) {
+    h->f_lap = nullptr;
+    cudaGetLastError();
+    return fail(BX_ENOMEM, "cudaMalloc lapENVinv");
+  }
+  BX_CU(cudaStreamSynchronize(h->stream));
+  BX_CU(cudaMemsetAsync(h->f_lap, 0, G * ld * sizeof(float2), h->stream));
+  BX_CU(bx::build_lap_env_inv<float2>(h->ny, h->nx, h->delta, h->f_lap, ld, h->stream));
   return BX_OK;
 }
 

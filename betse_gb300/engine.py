@@ -174,6 +174,11 @@ class ClusterEngine:
         _lib.check(self.lib.bx_max_abs_dvm(self.h, _lib.dptr(out)), 'bx_max_abs_dvm')
         return out
 
+    def build_lap_env_inv(self):
+        """Build ``cells.lapENVinv`` for this cluster's grid on the GPU (no
+        host array; the eigenvector construction of ``bx_build_lap_env_inv``)."""
+        _lib.check(self.lib.bx_build_lap_env_inv(self.h), 'bx_build_lap_env_inv')
+
     def set_lap_env_inv(self, lap_env_inv):
         """Keep ``cells.lapENVinv`` ([grid, grid]) on the GPU for ``env_fields``."""
         A = _c(lap_env_inv)

@@ -7,6 +7,8 @@ the four edges, then ``pinv``s it densely (``cells.py:503-504``).  The matrix
 is non-singular, so its inverse is the same operator; it equals
 ``delta**2 * K(ny, nx)`` with ``K`` the inverse at unit spacing, which is
 what lets clusters of one grid shape share it (``bx_batch_set_lap_env_inv``).
+The inverse is built on the GPU from the sine-transform eigenvectors of the
+interior block (``csrc/bx_lapinv.cuh``), not by dense inversion.
 """
 from __future__ import annotations
 
@@ -27,6 +29,18 @@ def make_laplacian(ny, nx, delta=1.0):
     return sp.csr_matrix((vals / delta ** 2, (rows, cols)), shape=(G, G))
 
 
-def lap_env_inverse(ny, nx, delta=1.0):
-    """``cells.lapENVinv`` for a grid of this shape and spacing (dense FP64)."""
-    return np.linalg.inv(make_laplacian(ny, nx, 1.0).toarray()) * delta ** 2
+def lap_env_inverse(ny, nx, delta=1.0, device=None):
+    """``cells.lapENVinv`` for a grid of this shape and spacing, built on the
+    GPU (``bx_lap_env_inv_build``: the eigenvector construction, no dense
+    inversion).  Returns a CUDA float64 tensor ``[G, G]`` when ``device`` is a
+    CUDA device, else a NumPy array copied back to the host."""
+    import ctypes as ct
+    import torch
+    from . import _lib
+    G = ny * nx
+    dev = torch.device(device) if device is not None else torch.device('cuda', torch.cuda.current_device())
+    A = torch.empty((G, G), dtype=torch.float64, device=dev)
+    _lib.check(_lib.load().bx_lap_env_inv_build(int(ny), int(nx), float(delta), ct.c_void_p(A.data_ptr()), G,
+                                                ct.c_void_p(torch.cuda.current_stream(dev).cuda_stream)),
+               'bx_lap_env_inv_build')
+    return A if device is not None else A.cpu().numpy()

@@ -242,6 +242,17 @@ int bx_max_abs_dvm(bx_handle h, double* per_cluster);
  * FiniteDiffSolver.makeLaplacian, finitediff.py:252-431).  Stored on the GPU
  * once as double-float (hi, lo) FP32 pairs; single-cluster handles only. */
 int bx_set_lap_env_inv(bx_handle h, const double* lap_env_inv);
+/* The same operator built on the GPU from the handle's grid shape and
+ * spacing, with no host array: makeLaplacian (finitediff.py:252-431) is the
+ * identity on the grid edges and the 5-point Laplacian inside, and its
+ * interior block is diagonalised by sine transforms, so its inverse is one
+ * FP64 GEMM over the eigenvectors (about (ny nx)^2 sqrt(ny nx) multiply-adds
+ * instead of BETSE's O((ny nx)^3) pinv).  Synchronous. */
+int bx_build_lap_env_inv(bx_handle h);
+/* cells.lapENVinv (cells.py:503-504) for an (ny, nx) grid of spacing delta,
+ * built as above into the DEVICE array A ([ny*nx] rows of lda >= ny*nx FP64
+ * values, row-major), on `stream` (synchronous). */
+int bx_lap_env_inv_build(int ny, int nx, double delta, double* A, int64_t lda, void* stream);
 
 /* Environment fields of get_current (physics/ion_current.py:50-171) for the
  * last step, which must have run with want_outputs: v_env, E_env_x/y,

@@ -76,12 +76,11 @@ def test_install_patches_and_returns_original():
 
 
 def test_product_laplacian_matches_oracle():
+    """The forward operator (its GPU inverse is checked in test_gpu_lapinv.py)."""
     import oracle
-    from betse_gb300.fields import lap_env_inverse, make_laplacian
+    from betse_gb300.fields import make_laplacian
     L = make_laplacian(9, 11, 2.5e-6).toarray()
     assert np.array_equal(L, oracle.fields.make_laplacian(9, 11, 2.5e-6))
-    A = lap_env_inverse(9, 11, 2.5e-6)
-    assert np.allclose(A @ L, np.eye(99), atol=1e-10)
 
 
 def _betse_objects(**popts):
