@@ -21,6 +21,41 @@ import numpy as np
 from . import _lib
 
 
+def lap_gj_operators(tri_edges, tri_edge_len, vor_edge_len, vor_sa):
+    """``cells.lapGJinv`` and ``cells.lapGJ`` (``Cells.graphLaplacian``,
+    ``betse/science/cells.py:1845-1894``) from the DEC mesh of the cluster
+    (``cells.mesh.tri_edges``, ``tri_edge_len``, ``vor_edge_len``, ``vor_sa``).
+
+    BETSE forms ``pinv(D) W (-pinv(D)^T) A`` with ``D`` the edge-vertex
+    incidence matrix (``-1`` at ``tri_edges[:, 0]``, ``+1`` at
+    ``tri_edges[:, 1]``), ``W = diag(tri_len / vor_len)``, ``A = diag(vor_sa)``
+    and ``pinv(D)`` from a dense SVD of the ``[edges, cells]`` matrix.  For a
+    connected graph ``pinv(D) = L+ D^T`` with ``L = D^T D`` the (sparse,
+    unweighted) graph Laplacian and ``L+ = (L + J/n)^-1 - J/n``, so
+
+        lapGJinv = -L+ (D^T W D) L+ A,
+
+    one dense solve of size ``n`` instead of the SVD of an ``[edges, n]``
+    matrix (FP64, on the host: a set-up step, O(n^3)).  Note that ``lapGJ`` is
+    not the inverse of ``lapGJinv`` (their product differs from the identity
+    by ~0.25 on BETSE's own clusters): BETSE pairs a pseudo-inverse of the
+    unweighted incidence with a weighted forward operator."""
+    import scipy.sparse as sp
+    e = np.asarray(tri_edges, np.int64)
+    A = np.asarray(vor_sa, np.float64)
+    n, m = len(A), len(e)
+    rows = np.repeat(np.arange(m), 2)
+    D = sp.csr_matrix((np.tile([-1.0, 1.0], m), (rows, e.ravel())), shape=(m, n))
+    w = np.asarray(tri_edge_len, np.float64) / np.asarray(vor_edge_len, np.float64)
+    L = (D.T @ D).toarray()
+    J = np.full((n, n), 1.0 / n)
+    Lp = np.linalg.solve(L + J, np.eye(n)) - J
+    Lw = (D.T @ sp.diags(w) @ D).toarray()
+    lap_inv = -(Lp @ Lw @ Lp) * A[None, :]
+    lap = -(sp.diags(1.0 / A) @ (D.T @ sp.diags(1.0 / w) @ D)).toarray()
+    return lap_inv, lap
+
+
 class DenseOperator:
     def __init__(self, A, forward=None):
         A = np.ascontiguousarray(np.asarray(A, np.float64))

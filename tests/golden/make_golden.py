@@ -420,6 +420,37 @@ CASES = {
 }
 
 
+def graph_case(name, radius, seed):
+    """BETSE's Cells.graphLaplacian (cells.py:1845-1894) on a seeded cluster:
+    the DEC-mesh inputs it reads (triangulation edges with their incidence
+    signs, edge lengths, Voronoi areas), the lapGJinv and lapGJ it builds, and
+    the product pressures.osmotic_P forms with it (physics/pressures.py:59,
+    sim.PP = lapGJinv @ (-div_u_osmo * rho * dt)) on a seeded divergence."""
+    p = make_params(radius, 20, False, 1e-2, 1)
+    c = build_cells(p, radius, seed)
+    c.graphLaplacian(p)
+    m = c.mesh
+    D = np.asarray(m.delta_tri_0)
+    e = np.asarray(m.tri_edges, np.int64)
+    rows = np.arange(len(e))
+    assert np.all(D[rows, e[:, 0]] == -1) and np.all(D[rows, e[:, 1]] == 1)
+    assert np.all((D != 0).sum(axis=1) == 2)
+    rng = np.random.default_rng(seed + 100)
+    div_u = rng.standard_normal(D.shape[1]) * 1e-3
+    rho, dt = 1000.0, p.dt
+    out = dict(mesh_tri_edges=e, mesh_tri_edge_len=np.asarray(m.tri_edge_len),
+               mesh_vor_edge_len=np.asarray(m.vor_edge_len), mesh_vor_sa=np.asarray(m.vor_sa),
+               lapGJinv=np.asarray(c.lapGJinv), lapGJ=np.asarray(c.lapGJ),
+               press_div_u_osmo=div_u, press_rho=np.float64(rho), press_dt=np.float64(dt),
+               press_PP=np.dot(c.lapGJinv, -div_u * rho * dt))
+    path = os.path.join(HERE, name + '.npz')
+    np.savez_compressed(path, **out)
+    print(f'{name}: {D.shape[1]} cells, {len(e)} edges -> {path}')
+
+
+GRAPH_CASES = {'lapgj_r80_s1': dict(radius=80e-6, seed=1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default=os.environ.get('BETSE_REF'),
@@ -433,6 +464,10 @@ def main():
         if a.only and name not in a.only.split(','):
             continue
         run_case(name, **kw)
+    for name, kw in GRAPH_CASES.items():
+        if a.only and name not in a.only.split(','):
+            continue
+        graph_case(name, **kw)
 
 
 if __name__ == '__main__':

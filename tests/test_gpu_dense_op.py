@@ -73,3 +73,25 @@ def test_repeat_is_deterministic():
     X = rng.standard_normal((700, 130))
     with _op(A) as op:
         assert np.array_equal(op.apply(X), op.apply(X))
+
+
+def test_lapgj_inverse_products_match_betse():
+    """BETSE's own cells.lapGJinv (graphLaplacian, cells.py:1845-1894) applied
+    on the tensor cores: the pressures.py:59 product sim.PP = lapGJinv @
+    (-div_u_osmo rho dt) against BETSE's, and a block of 64 right-hand sides
+    against FP64, within the BF16x3 bound (no refinement: BETSE's lapGJ is not
+    the inverse of its lapGJinv, so the forward-operator step does not apply).
+    The errors are printed."""
+    import os
+    d = dict(np.load(os.path.join(gi.GOLDEN, 'lapgj_r80_s1.npz')))
+    A = d['lapGJinv']
+    rhs = -d['press_div_u_osmo'] * d['press_rho'] * d['press_dt']
+    rng = np.random.default_rng(3)
+    X = np.concatenate([rhs[:, None], rng.standard_normal((len(rhs), 63))], axis=1)
+    with _op(A) as op:
+        Y = op.apply(X)
+    e_pp = gi.rel_err(Y[:, 0], d['press_PP'])
+    e_blk = gi.rel_err(Y, A @ X)
+    print(f'\nlapGJinv ({len(A)} cells) on tcgen05 BF16x3: pressures product rel err {e_pp:.2e}, '
+          f'64-column block {e_blk:.2e}')
+    assert e_pp < 1e-4 and e_blk < 1e-4
