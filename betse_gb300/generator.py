@@ -84,40 +84,76 @@ class GeneratedCluster:
     world: float       # side of the square world (p.wsx after the disorder margin)
 
 
-def make_cluster(radius, seed, d_cell=10e-6, disorder=0.4, cell_height=1e-5,
-                 cell_space=26e-9, scale_cell=0.99, grid_size=20, smooth_cells=2.0):
-    """A jittered-hex Voronoi cluster clipped to a disc of ``radius`` (m)."""
+def poly_centroid(P):
+    """Area centroid of a polygon (vertices in order), as DECMesh.poly_centroid."""
+    Q = np.roll(P, -1, axis=0)
+    a = P[:, 0] * Q[:, 1] - Q[:, 0] * P[:, 1]
+    A = a.sum() / 2
+    return np.array([((P[:, 0] + Q[:, 0]) * a).sum(), ((P[:, 1] + Q[:, 1]) * a).sum()]) / (6 * A)
+
+
+def _centroid_voronoi(pts):
+    """Delaunay triangulation of ``pts`` and, per point, its triangles in
+    counter-clockwise order; the Voronoi vertices are triangle centroids
+    (DECMesh(use_centroids=True)).  Returns (simplices, triangle centroids,
+    fan triangle ids, fan pointer, hull mask)."""
     from scipy.spatial import Delaunay
-
-    cell_radius = d_cell / 2
-    world = 2 * radius + 20e-6
-    wsx = wsy = world + 5 * disorder * d_cell
-    rs = np.random.RandomState(seed)
-    pts = hex_lattice(wsx, wsy, d_cell, disorder, rs)
-    centre = pts.mean(axis=0)
-    xmin, ymin = pts.min(axis=0) - cell_radius
-    xmax, ymax = pts.max(axis=0) + cell_radius
-
     tri = Delaunay(pts)
     simp = tri.simplices
-    tcent = pts[simp].mean(axis=1)                # centroid Voronoi vertices
+    tcent = pts[simp].mean(axis=1)
     n = len(pts)
-    # triangles around each seed, ordered by angle (counter-clockwise)
     owner = simp.ravel()
     tid = np.repeat(np.arange(len(simp)), 3)
     ang = np.arctan2(tcent[tid, 1] - pts[owner, 1], tcent[tid, 0] - pts[owner, 0])
     order = np.lexsort((ang, owner))
     owner, tid = owner[order], tid[order]
     fan_ptr = np.concatenate([[0], np.cumsum(np.bincount(owner, minlength=n))])
-    # closed fan: seeds not on the hull
     hull = np.zeros(n, bool)
     hull[np.unique(tri.convex_hull.ravel())] = True
-    keep = (~hull) & (np.hypot(pts[:, 0] - centre[0], pts[:, 1] - centre[1]) < radius)
-    keep &= np.diff(fan_ptr) >= 3
+    return simp, tcent, tid, fan_ptr, hull
+
+
+def make_cluster(radius, seed, d_cell=10e-6, disorder=0.4, cell_height=1e-5,
+                 cell_space=26e-9, scale_cell=0.99, grid_size=20, smooth_cells=2.0):
+    """A jittered-hex Voronoi cluster clipped to a disc of ``radius`` (m).
+
+    BETSE's seeding (Cells.make_world -> DECMesh.clip_and_refine,
+    math/mesh.py:189, 2290-2372) in two passes: the centroid-Voronoi cells of
+    the lattice (plus its four bounding-box corners, Cells.clust_xy), of
+    which those whose area centroid lies in the disc are kept; then the
+    mesh is rebuilt with those area centroids as its points, and the cells
+    are the centroid-Voronoi cells of the rebuilt mesh, centred at their area
+    centroids (cells.cell_centres).  BETSE cuts the boundary cells of the
+    first pass with the disc before taking their centroids and closes the
+    outer cells of the second along the cut; here the first-pass cells are
+    whole and the outer ring of the second pass (open Voronoi fans) is left
+    out, so the interior is BETSE's and the boundary ring differs."""
+    cell_radius = d_cell / 2
+    world = 2 * radius + 20e-6
+    # the world of BETSE's configuration: world_len plus the disorder margin
+    wsx = wsy = world + 5 * disorder * d_cell
+    rs = np.random.RandomState(seed)
+    lat = hex_lattice(wsx, wsy, d_cell, disorder, rs)
+    centre = lat.mean(axis=0)
+    lo, hi = lat.min(axis=0), lat.max(axis=0)
+    xmin, ymin = lo - cell_radius
+    xmax, ymax = hi + cell_radius
+    # first pass: the lattice and its bounding-box corners
+    corners = np.array([[lo[0], lo[1]], [hi[0], lo[1]], [hi[0], hi[1]], [lo[0], hi[1]]])
+    allp = np.vstack([lat, corners])
+    simp0, tcent0, tid0, fan0, hull0 = _centroid_voronoi(allp)
+    first = [s for s in range(len(lat)) if not hull0[s] and fan0[s + 1] - fan0[s] >= 3]
+    c0 = np.array([poly_centroid(tcent0[tid0[fan0[s]:fan0[s + 1]]]) for s in first])
+    pts = c0[np.hypot(c0[:, 0] - centre[0], c0[:, 1] - centre[1]) < radius]
+
+    # second pass: the cells of the rebuilt mesh
+    simp, tcent, tid, fan_ptr, hull = _centroid_voronoi(pts)
+    n = len(pts)
+    keep = (~hull) & (np.diff(fan_ptr) >= 3)
     seeds = np.nonzero(keep)[0]
     # polygon of each kept seed, then cell order along a Z curve of the centroid
     polys = [tcent[tid[fan_ptr[s]:fan_ptr[s + 1]]] for s in seeds]
-    cents = np.array([p.mean(axis=0) for p in polys])
+    cents = np.array([poly_centroid(p) for p in polys])
     zo = np.argsort(_zorder(cents), kind='stable')
     seeds = seeds[zo]
     polys = [polys[i] for i in zo]
@@ -129,8 +165,8 @@ def make_cluster(radius, seed, d_cell=10e-6, disorder=0.4, cell_height=1e-5,
     M = int(counts.sum())
     ptr = np.concatenate([[0], np.cumsum(counts)])
     m2c = np.repeat(np.arange(C), counts)
-    # vertices scaled toward the centroid (cellVerts: p.scale_cell)
-    poly_c = np.array([p.mean(axis=0) for p in polys])
+    # vertices scaled toward the cell centre, the area centroid (cellVerts: p.scale_cell)
+    poly_c = cents[zo]
     V = np.concatenate(polys)
     V = scale_cell * (V - poly_c[m2c]) + poly_c[m2c]
     # membrane k of a cell joins vertex k-1 and vertex k (cellVerts' loop)

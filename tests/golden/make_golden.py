@@ -451,6 +451,30 @@ def graph_case(name, radius, seed):
 GRAPH_CASES = {'lapgj_r80_s1': dict(radius=80e-6, seed=1)}
 
 
+def lattice_cases(name, cases):
+    """BETSE's seed lattice (Cells._make_cell_lattice, cells.py:742-801) and the
+    cells it clips from it (DECMesh.clip_and_refine, cellVerts, cell_vols,
+    mem_processing, near_neigh) for each (radius, seed): what the synthetic
+    cluster generator is checked against."""
+    out = {}
+    for key, (radius, seed) in cases.items():
+        p = make_params(radius, 20, False, 1e-2, 1)
+        c = build_cells(p, radius, seed)
+        out.update({f'{key}_xypts': np.asarray(c.clust_xy)[:-4], f'{key}_wsx': np.float64(p.wsx),
+                    f'{key}_centre': np.asarray(c.centre), f'{key}_cell_centres': np.asarray(c.cell_centres),
+                    f'{key}_mem_to_cells': np.asarray(c.mem_to_cells, np.int64),
+                    f'{key}_nn_i': np.asarray(c.nn_i, np.int64),
+                    f'{key}_bflags_mems': np.asarray(c.bflags_mems, np.int64),
+                    f'{key}_mem_sa': np.asarray(c.mem_sa), f'{key}_cell_vol': np.asarray(c.cell_vol)})
+        print(f'{name}/{key}: {len(c.cell_centres)} cells, {len(c.mem_i)} membranes')
+    path = os.path.join(HERE, name + '.npz')
+    np.savez_compressed(path, **out)
+    print(f'-> {path}')
+
+
+LATTICE_CASES = {'cells_lattice': {'r80_s1': (80e-6, 1), 'r50_s7': (50e-6, 7), 'r50_s3': (50e-6, 3)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default=os.environ.get('BETSE_REF'),
@@ -468,6 +492,10 @@ def main():
         if a.only and name not in a.only.split(','):
             continue
         graph_case(name, **kw)
+    for name, cases in LATTICE_CASES.items():
+        if a.only and name not in a.only.split(','):
+            continue
+        lattice_cases(name, cases)
 
 
 if __name__ == '__main__':
