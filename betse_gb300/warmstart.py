@@ -146,7 +146,7 @@ def graph_of(geoms):
 # stepping to steady state
 # ---------------------------------------------------------------------------
 def run_to_steady(geoms, params, Dms, states, tol=1e-6, chunk=1000, max_steps=400_000, precision='split',
-                  restart_states=(), compact=True):
+                  restart_states=(), compact=True, autotune=True):
     """Step a batch of clusters until every cluster's max |dVm/dt| < tol.
 
     Returns (final states, steps at which each cluster first passed -- -1 if
@@ -170,6 +170,8 @@ def run_to_steady(geoms, params, Dms, states, tol=1e-6, chunk=1000, max_steps=40
         e = BatchEngine([geoms[i] for i in idx], [params[i] for i in idx], precision)
         e.set_membrane_diffusivity([Dms[i] for i in idx])
         e.upload_states(sts)
+        if autotune:
+            e.autotune(64)          # the kernel and tile size for this batch; the state is kept
         return e
 
     active = np.arange(n)
