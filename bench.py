@@ -558,12 +558,14 @@ def profile_kernel(which):
 
 
 # kernels of the split form, by the number bx_set_launch_config takes
-KERNEL_NAMES = {0: 'k_split_step', 1: 'k_split_persist', 2: 'k_split_fact', 3: 'k_split_resident'}
-LAUNCH_SUFFIX = {'': 0, 'p': 1, 'f': 2, 'r': 3}
+KERNEL_NAMES = {0: 'k_split_step', 1: 'k_split_persist', 2: 'k_split_fact', 3: 'k_split_resident',
+                4: 'k_split_fact_pipe'}
+LAUNCH_SUFFIX = {'': 0, 'p': 1, 'f': 2, 'r': 3, 'q': 4}
 
 
 def parse_launch(text):
-    """'192' tile kernel, '192p' persistent, '192f' factored, '256r' resident."""
+    """'192' tile kernel, '192p' persistent, '192f' factored, '256r' resident,
+    '256q' pipelined factored."""
     suffix = text.lstrip('0123456789')
     return int(text[:len(text) - len(suffix)]), LAUNCH_SUFFIX[suffix]
 

@@ -59,6 +59,41 @@ class BxParams(ct.Structure):
          ('KmCa_ATP', ct.c_double), ('cell_polarizability', ct.c_double)]
 
 
+NET_MAX_SUBSTANCES = 16
+NET_MAX_REACTIONS = 32
+NET_MAX_TERMS = 256
+NET_MAX_STOICH = 4
+TERM_ACT, TERM_ACT_INDEP, TERM_INH, TERM_DIRECT_POS, TERM_DIRECT_NEG = 0, 1, 2, 3, 4
+
+
+class BxNetTerm(ct.Structure):
+    _fields_ = [('kind', ct.c_int32), ('substance', ct.c_int32), ('env_zone', ct.c_int32),
+                ('pad', ct.c_int32), ('Km', ct.c_double), ('n', ct.c_double)]
+
+
+class BxNetSubstance(ct.Structure):
+    _fields_ = [(n, ct.c_double) for n in ('z', 'Dm', 'Do', 'Dgj', 'time_factor', 'r_production',
+                                          'r_decay', 'decay_max', 'gad_scale_factor')] + \
+        [(n, ct.c_int32) for n in ('growth', 'update_intra', 'gj_impermeable', 'growth_term0',
+                                   'growth_nterm', 'decay_term0', 'decay_nterm', 'pad')] + \
+        [('growth_mod', _dp), ('growth_target', _u8p)]
+
+
+class BxNetReaction(ct.Structure):
+    _fields_ = [('n_reactants', ct.c_int32), ('n_products', ct.c_int32),
+                ('reactant', ct.c_int32 * NET_MAX_STOICH), ('product', ct.c_int32 * NET_MAX_STOICH),
+                ('reactant_coeff', ct.c_double * NET_MAX_STOICH), ('reactant_Km', ct.c_double * NET_MAX_STOICH),
+                ('product_coeff', ct.c_double * NET_MAX_STOICH), ('vmax', ct.c_double), ('keq', ct.c_double),
+                ('term0', ct.c_int32), ('nterm', ct.c_int32)]
+
+
+class BxNetSpec(ct.Structure):
+    _fields_ = [('n_substances', ct.c_int32), ('n_reactions', ct.c_int32), ('n_terms', ct.c_int32),
+                ('pad', ct.c_int32), ('substances', ct.POINTER(BxNetSubstance)),
+                ('reactions', ct.POINTER(BxNetReaction)), ('terms', ct.POINTER(BxNetTerm)),
+                ('mem_vol', _dp), ('R_rads', _dp)]
+
+
 class BxState(ct.Structure):
     _fields_ = [('vm', _dp), ('cc_cells', _dp), ('cc_at_mem', _dp),
                 ('cc_env', _dp), ('E_env_x', _dp), ('E_env_y', _dp), ('gjopen', _dp)]
@@ -142,6 +177,13 @@ SIGNATURES = {
                                     ct.POINTER(ct.c_int), ct.POINTER(ct.c_int64)]),
     'bx_resident_barrier_check': (ct.c_int, [ct.c_void_p, ct.c_int64, ct.POINTER(ct.c_int)]),
     'bx_autotune_table': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.POINTER(ct.c_int), _ip, _ip, _ip, _dp]),
+    'bx_network_create': (ct.c_int, [ct.c_void_p, ct.POINTER(BxNetSpec), ct.POINTER(ct.c_void_p)]),
+    'bx_network_upload': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    'bx_network_download': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    'bx_network_step': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int]),
+    'bx_network_fluxes': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    'bx_network_status': (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int64)]),
+    'bx_network_destroy': (ct.c_int, [ct.c_void_p]),
     'bx_step_fp64_noalloc': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p]),

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -27,6 +28,7 @@
 #include "bx_fields.cuh"
 #include "bx_launch.cuh"
 #include "bx_lapinv.cuh"
+#include "bx_network.cuh"
 #include "bx_split.cuh"
 #include "bx_state.cuh"
 
@@ -65,7 +67,7 @@ constexpr int kRec = 8;          // floats per cell record of the split form (<=
 
 enum Mode { MODE_PLAIN = 0, MODE_SPLIT = 1 };
 // kernels of the split form (bx_set_launch_config's `kernel`)
-enum Kind { KIND_TILE = 0, KIND_PERSIST = 1, KIND_FACT = 2, KIND_RESIDENT = 3 };
+enum Kind { KIND_TILE = 0, KIND_PERSIST = 1, KIND_FACT = 2, KIND_RESIDENT = 3, KIND_FACT_PIPE = 4 };
 constexpr long long kResTimeoutNs = 2000000000LL;   // grid-barrier wait limit of k_split_resident
 
 }  // namespace
@@ -179,8 +181,10 @@ struct bx_cluster {
   float* f_dsa = nullptr;          // [I][S] sum of Dm_i * mem_sa over the cell's membranes
   float4* f_cst = nullptr;         // [S] {sum mem_sa, dt/cell_vol, diviterm/cm, gap-junction count | -1}
   int* f_gbeg = nullptr;           // [S] first gap-junction entry
-  int2* f_gj = nullptr;            // [P] {partner cell slot, bits of gj_weight*mem_sa}
+  int2* f_gj = nullptr;            // [P + 2] {partner cell slot, bits of gj_weight*mem_sa} (+2: aligned copies)
   int f_P = 0;
+  int* f_tile_e0 = nullptr;        // [nblk + 1] first gap-junction entry of each tile
+  int f_max_ent = 0;               // entries of the largest tile
   std::vector<float> h_fsa;        // [S] sum of mem_sa (host, for f_cst)
   std::vector<int> h_gbeg, h_gcnt; // [S] (gcnt -1 = padding slot)
   std::vector<int2> h_gj;          // [P]
@@ -216,7 +220,7 @@ void free_all(bx_cluster* h) {
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
       h->bf_ci, h->bf_last, h->bf_cd, h->bf_buf, h->bf_X, h->bf_Y, h->bf_scale, h->d_gjo, h->t_gjo, h->d_cnew, h->d_Rrads,
       h->st_vm, h->st_cc, h->st_cam, h->st_go, h->d_flag, h->t_slot_of_mem, h->t_blob,
-      h->f_dsa, h->f_cst, h->f_gbeg, h->f_gj, h->r_cta, h->r_gj, h->r_gbeg, h->r_halo, h->r_cpart, h->r_ctl};
+      h->f_dsa, h->f_cst, h->f_gbeg, h->f_gj, h->f_tile_e0, h->r_cta, h->r_gj, h->r_gbeg, h->r_halo, h->r_cpart, h->r_ctl};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& fs : h->fshapes)
@@ -545,7 +549,30 @@ cudaError_t launch_fact_u(bx_cluster* h, int parity, cudaStream_t s) {
                     split_ptrs(h, parity), make_split_const(h));
 }
 
+// the pipelined factored step: one warp per CTA, as many CTAs as fit an SM
+template <int ZP>
+cudaError_t launch_fact_pipe_t(bx_cluster* h, int parity, cudaStream_t s) {
+  auto kern = bx::k_split_fact_pipe<1, ZP>;
+  const bx::FactPipeSmem L(h->f_max_ent, bx::IonSet<ZP>::NI);
+  const size_t smem = L.warp_bytes;
+  static int attr_set = 0;      // per instantiation: the largest size set so far
+  if ((int)smem > attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = (int)smem;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int grid = std::max(1, std::min(h->nblk, per_sm * h->sm_count));
+  return launch_pdl_smem(kern, (unsigned)grid, 32, smem, s, fact_geom(h), split_ptrs(h, parity),
+                         make_split_const(h), (const int*)h->f_tile_e0, h->f_max_ent);
+}
+
 cudaError_t launch_fact(bx_cluster* h, int parity, cudaStream_t s) {
+  if (h->kind == KIND_FACT_PIPE)
+    return is_betse_six_ions(h) ? launch_fact_pipe_t<1>(h, parity, s) : launch_fact_pipe_t<0>(h, parity, s);
   return h->fact_unroll == 2 ? launch_fact_u<2>(h, parity, s) : launch_fact_u<4>(h, parity, s);
 }
 
@@ -680,7 +707,8 @@ cudaError_t launch_resident(bx_cluster* h, int parity, int n_steps, cudaStream_t
 }
 
 cudaError_t launch_split(bx_cluster* h, int parity, bool out, cudaStream_t s) {
-  if ((h->kind == KIND_FACT || h->kind == KIND_RESIDENT) && fact_eligible(h, out)) return launch_fact(h, parity, s);
+  if ((h->kind == KIND_FACT || h->kind == KIND_RESIDENT || h->kind == KIND_FACT_PIPE) && fact_eligible(h, out))
+    return launch_fact(h, parity, s);
   if (h->kind == KIND_PERSIST && !out && !h->phib_nonzero && !h->ecm && !h->vgj && !h->ca) {
     const bool six = is_betse_six_ions(h);
     if (h->tpb == 192) return six ? launch_persist_t<192, 1>(h, parity, s) : launch_persist_t<192, 0>(h, parity, s);
@@ -963,15 +991,23 @@ int build_fact_layout(bx_cluster* h) {
     h->h_gcnt[sl] = (int)h->h_gj.size() - h->h_gbeg[sl];
   }
   h->f_P = (int)h->h_gj.size();
-  void* old[] = {h->f_dsa, h->f_cst, h->f_gbeg, h->f_gj};
+  void* old[] = {h->f_dsa, h->f_cst, h->f_gbeg, h->f_gj, h->f_tile_e0};
   for (void* q : old)
     if (q) cudaFree(q);
-  h->f_dsa = nullptr; h->f_cst = nullptr; h->f_gbeg = nullptr; h->f_gj = nullptr;
+  h->f_dsa = nullptr; h->f_cst = nullptr; h->f_gbeg = nullptr; h->f_gj = nullptr; h->f_tile_e0 = nullptr;
   drop_resident(h);
+  // each tile's entries: contiguous, from the first slot's first entry
+  std::vector<int> te(h->nblk + 1);
+  h->f_max_ent = 0;
+  for (int b = 0; b < h->nblk; ++b) te[b] = h->h_gbeg[32 * b];
+  te[h->nblk] = h->f_P;
+  for (int b = 0; b < h->nblk; ++b) h->f_max_ent = std::max(h->f_max_ent, te[b + 1] - te[b]);
   BX_CU(dalloc(&h->f_dsa, (size_t)h->I * S));
   BX_CU(dalloc(&h->f_cst, S));
   BX_CU(dalloc(&h->f_gbeg, S)); BX_CU(h2d(h->f_gbeg, h->h_gbeg.data(), S));
-  BX_CU(dalloc(&h->f_gj, std::max(1, h->f_P)));
+  BX_CU(dalloc(&h->f_tile_e0, h->nblk + 1)); BX_CU(h2d(h->f_tile_e0, te.data(), h->nblk + 1));
+  BX_CU(dalloc(&h->f_gj, h->f_P + 2));
+  BX_CU(cudaMemset(h->f_gj, 0, (size_t)(h->f_P + 2) * sizeof(int2)));
   if (h->f_P) BX_CU(h2d(h->f_gj, h->h_gj.data(), h->f_P));
   int rc = upload_fact_dsa(h);
   if (rc != BX_OK) return rc;
@@ -1775,7 +1811,8 @@ int bx_time_cell_kernel(bx_handle h, int n, double* ms_per_launch) {
 int64_t bx_cell_kernel_bytes(bx_handle h) {
   if (!h) return -1;
   const int64_t M = h->M, C = h->C, I = h->I, B = h->nblk;
-  if (h->mode == MODE_SPLIT && (h->kind == KIND_FACT || h->kind == KIND_RESIDENT) && fact_eligible(h, false)) {
+  if (h->mode == MODE_SPLIT && (h->kind == KIND_FACT || h->kind == KIND_RESIDENT || h->kind == KIND_FACT_PIPE) &&
+      fact_eligible(h, false)) {
     // factored form, per cell slot: cc2 in+out 16I, record in+out 2*4*kRec,
     // DSA 4I, {SA, dt/vol, diviterm/cm, count} 16, first entry 4; per
     // gap-junction entry 8; per tile the partial sums 4I and the cluster id 4
@@ -1823,7 +1860,7 @@ int bx_set_launch_config(bx_handle h, int tpb, int kernel) {
   if (!h) return fail(BX_EINVAL, "null handle");
   const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256) : (tpb == 128 || tpb == 256);
   if (!ok) return fail(BX_EINVAL, "unsupported CTA size for this form");
-  if (kernel < KIND_TILE || kernel > KIND_RESIDENT) return fail(BX_EINVAL, "kernel must be 0, 1, 2 or 3");
+  if (kernel < KIND_TILE || kernel > KIND_FACT_PIPE) return fail(BX_EINVAL, "kernel must be 0 to 4");
   if (kernel != KIND_TILE && h->mode != MODE_SPLIT)
     return fail(BX_EINVAL, "the persistent, factored and resident kernels are the split form's");
   if (kernel != KIND_TILE && h->ecm) return fail(BX_EINVAL, "only the tile kernel has an extracellular-space variant");
@@ -1917,6 +1954,7 @@ int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* 
   else if (h->mode == MODE_SPLIT)
     cands = {{256, KIND_TILE, 4},     {192, KIND_TILE, 4},     {256, KIND_PERSIST, 4}, {192, KIND_PERSIST, 4},
              {256, KIND_FACT, 4},     {192, KIND_FACT, 4},     {256, KIND_FACT, 2},    {192, KIND_FACT, 2},
+             {256, KIND_FACT_PIPE, 4}, {192, KIND_FACT_PIPE, 4},
              {256, KIND_RESIDENT, 4}, {192, KIND_RESIDENT, 4}};
   else cands = {{256, KIND_TILE, 4}, {128, KIND_TILE, 4}};
   double best = 1e300;
@@ -2399,6 +2437,364 @@ int bx_time_env_fields(bx_handle h, int n, double* ms_fields, double* ms_product
   if (rc != BX_OK) return rc;
   *ms_fields = tf / n;
   *ms_product = tp / n;
+  return BX_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Molecule and gene regulatory networks (bx_network.cuh)
+// ---------------------------------------------------------------------------
+struct bx_network {
+  bx_cluster* h = nullptr;
+  int S = 0, R = 0, nblk = 0;
+  bool any_ui = false, have_state = false, have_fluxes = false;
+  bx::NetTables* d_tab = nullptr;
+  double *d_gamma = nullptr, *d_Rr = nullptr, *d_gmod = nullptr, *d_cc = nullptr, *d_cm = nullptr,
+         *d_cmid = nullptr, *d_cmmid = nullptr, *d_env = nullptr, *d_part = nullptr, *d_fmem = nullptr,
+         *d_fgj = nullptr;
+  uint8_t* d_gmask = nullptr;
+  unsigned long long* d_neg = nullptr;
+  cudaGraphExec_t graph = nullptr;   // kGraphChunk coupled steps from ion parity 0
+  cudaGraphExec_t graph_net = nullptr;   // kGraphChunk network-only steps
+  int graph_net_parity = -1;
+};
+
+namespace {
+
+void net_free(bx_network* n) {
+  void* ptrs[] = {n->d_tab, n->d_gamma, n->d_Rr, n->d_gmod, n->d_cc, n->d_cm, n->d_cmid, n->d_cmmid,
+                  n->d_env, n->d_part, n->d_fmem, n->d_fgj, n->d_gmask, n->d_neg};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (n->graph) cudaGraphExecDestroy(n->graph);
+  if (n->graph_net) cudaGraphExecDestroy(n->graph_net);
+}
+
+// Checks one influencer range and its order (multiplicative, independent,
+// inhibitors, direct), which is how the kernel evaluates it.
+bool net_range_ok(const bx_net_spec* sp, int t0, int nt, std::string* why) {
+  if (nt == 0) return true;
+  if (t0 < 0 || nt < 0 || t0 + nt > sp->n_terms) { *why = "influencer range outside the term table"; return false; }
+  int last = 0;
+  for (int q = t0; q < t0 + nt; ++q) {
+    const bx_net_term& t = sp->terms[q];
+    if (t.kind < 0 || t.kind > BX_TERM_DIRECT_NEG) { *why = "unknown influencer kind"; return false; }
+    const int rank = t.kind >= BX_TERM_DIRECT_POS ? 3 : t.kind;
+    if (rank < last) { *why = "influencer terms out of order (act, independent, inhibitor, direct)"; return false; }
+    last = rank;
+    if (t.substance < 0 || t.substance >= sp->n_substances) { *why = "influencer names no substance"; return false; }
+    if (t.kind != BX_TERM_DIRECT_POS && t.kind != BX_TERM_DIRECT_NEG && !(t.Km > 0.0)) {
+      *why = "influencer Km must be > 0";
+      return false;
+    }
+  }
+  return true;
+}
+
+bx::NetArgs net_args(bx_network* n, int vm_parity) {
+  bx_cluster* h = n->h;
+  bx::NetArgs a{};
+  a.C = h->C; a.M = h->M;
+  a.dt = h->par.dt; a.tm = h->par.tm; a.F_RT = h->par.F / (h->par.R * h->par.T);
+  a.gj_len = h->gj_len; a.gj_block = h->par.gj_block;
+  a.inv_vol_env_M = 1.0 / (h->par.vol_env * (double)h->M);
+  a.cell_ptr = h->d_cell_ptr; a.nn = h->d_nn; a.nn_cell = h->d_nn_cell; a.bflag = h->d_bflag;
+  a.mem_sa = h->d_mem_sa; a.cell_vol = h->d_cell_vol; a.gj_w = h->d_gj_w;
+  a.gjo = h->vgj ? h->d_gjo : nullptr;
+  a.vm = h->d_vm[vm_parity];
+  a.tab = n->d_tab; a.gamma = n->d_gamma; a.R_rads = n->d_Rr; a.gmod = n->d_gmod; a.gmask = n->d_gmask;
+  a.c_cells = n->d_cc; a.cmem = n->d_cm; a.c_mid = n->d_cmid; a.cmem_mid = n->d_cmmid; a.env = n->d_env;
+  a.env_part = n->d_part; a.f_mem = n->d_fmem; a.f_gj = n->d_fgj; a.neg = n->d_neg; a.nblk = n->nblk;
+  return a;
+}
+
+cudaError_t net_enqueue(bx_network* n, int vm_parity, bool out, cudaStream_t s) {
+  const bx::NetArgs a = net_args(n, vm_parity);
+  if (out) {
+    bx::k_net_cell<true><<<n->nblk, bx::kNetTPB, 0, s>>>(a);
+    bx::k_net_gj<true><<<n->nblk, bx::kNetTPB, 0, s>>>(a);
+  } else {
+    bx::k_net_cell<false><<<n->nblk, bx::kNetTPB, 0, s>>>(a);
+    bx::k_net_gj<false><<<n->nblk, bx::kNetTPB, 0, s>>>(a);
+  }
+  n->h->launches += 2;
+  return cudaGetLastError();
+}
+
+// One time step: the ion step at the cluster's parity (reading Vmem from
+// d_vm[parity], writing d_vm[parity ^ 1]) then the network on d_vm[parity].
+cudaError_t net_enqueue_coupled(bx_network* n, int parity, bool out, cudaStream_t s) {
+  cudaError_t e = enqueue_step(n->h, parity, out, s);
+  if (e != cudaSuccess) return e;
+  return net_enqueue(n, parity, out, s);
+}
+
+int net_capture(bx_network* n, bool coupled, int parity, cudaGraphExec_t* exec) {
+  bx_cluster* h = n->h;
+  cudaStream_t cs;
+  BX_CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t graph;
+  const int64_t l0 = h->launches;
+  BX_CU(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  int par = parity;
+  for (int q = 0; q < kGraphChunk; ++q) {
+    if (coupled) {
+      net_enqueue_coupled(n, par, false, cs);
+      par ^= 1;
+    } else {
+      net_enqueue(n, par, false, cs);
+    }
+  }
+  cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+  cudaStreamDestroy(cs);
+  h->launches = l0;
+  if (ce != cudaSuccess) return fail(BX_ECUDA, std::string("network graph capture: ") + cudaGetErrorString(ce));
+  ce = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) return fail(BX_ECUDA, std::string("network graph instantiate: ") + cudaGetErrorString(ce));
+  return BX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bx_network_create(bx_handle h, const bx_net_spec* sp, bx_network_handle* out) {
+  if (!h || !sp || !out) return fail(BX_EINVAL, "null argument");
+  *out = nullptr;
+  if (h->mode != MODE_PLAIN) return fail(BX_EINVAL, "networks step with the plain FP64 form");
+  if (h->ncl != 1) return fail(BX_EINVAL, "networks step on a single-cluster handle");
+  if (h->ecm) return fail(BX_EINVAL, "networks with extracellular spaces are not built");
+  if (sp->n_substances < 1 || sp->n_substances > bx::kNetMaxSub)
+    return fail(BX_EINVAL, "n_substances must be 1.." + std::to_string(bx::kNetMaxSub));
+  if (sp->n_reactions < 0 || sp->n_reactions > bx::kNetMaxReact)
+    return fail(BX_EINVAL, "n_reactions must be 0.." + std::to_string(bx::kNetMaxReact));
+  if (sp->n_terms < 0 || sp->n_terms > bx::kNetMaxTerms)
+    return fail(BX_EINVAL, "n_terms must be 0.." + std::to_string(bx::kNetMaxTerms));
+  if (!sp->substances || (sp->n_reactions && !sp->reactions) || (sp->n_terms && !sp->terms))
+    return fail(BX_EINVAL, "null table");
+  const int S = sp->n_substances, R = sp->n_reactions, C = h->C, M = h->M;
+  std::unique_ptr<bx::NetTables> tb(new bx::NetTables());
+  std::memset(tb.get(), 0, sizeof(bx::NetTables));
+  tb->S = S; tb->R = R; tb->T = sp->n_terms;
+  std::string why;
+  bool any_ui = false;
+  int mod_rows = 0, mask_rows = 0;
+  for (int k = 0; k < S; ++k) {
+    const bx_net_substance& u = sp->substances[k];
+    bx::NetSubD& d = tb->sub[k];
+    d.z = u.z; d.Dm = u.Dm; d.Do = u.Do; d.Dgj = u.Dgj; d.tdf = u.time_factor;
+    d.r_prod = u.r_production; d.r_decay = u.r_decay; d.decay_max = u.decay_max; d.gsf = u.gad_scale_factor;
+    d.growth = u.growth ? 1 : 0; d.ui = u.update_intra ? 1 : 0; d.gj_imp = u.gj_impermeable ? 1 : 0;
+    d.gt0 = u.growth_term0; d.gnt = u.growth_nterm; d.dt0 = u.decay_term0; d.dnt = u.decay_nterm;
+    d.mod_row = (u.growth && u.growth_mod) ? mod_rows++ : -1;
+    d.mask_row = (u.growth && u.growth_target) ? mask_rows++ : -1;
+    if (u.growth && !(u.gad_scale_factor != 0.0)) return fail(BX_EINVAL, "gad_scale_factor must be nonzero");
+    if (u.update_intra) {
+      if (u.z != 0.0)
+        return fail(BX_EINVAL, "intracellular transport of a charged substance reads the intracellular field "
+                               "E_cell; not built ('update intracellular' with z != 0)");
+      any_ui = true;
+    }
+    if (u.growth && (!net_range_ok(sp, u.growth_term0, u.growth_nterm, &why) ||
+                     !net_range_ok(sp, u.decay_term0, u.decay_nterm, &why)))
+      return fail(BX_EINVAL, "substance " + std::to_string(k) + ": " + why);
+  }
+  if (any_ui && (!sp->mem_vol || !sp->R_rads))
+    return fail(BX_EINVAL, "'update intracellular' needs mem_vol and R_rads");
+  for (int j = 0; j < R; ++j) {
+    const bx_net_reaction& r = sp->reactions[j];
+    bx::NetReactD& d = tb->react[j];
+    if (r.n_reactants < 1 || r.n_reactants > BX_NET_MAX_STOICH || r.n_products < 0 ||
+        r.n_products > BX_NET_MAX_STOICH)
+      return fail(BX_EINVAL, "reaction " + std::to_string(j) + ": 1..4 reactants and 0..4 products");
+    if (r.keq != 0.0 && r.n_products < 1)
+      return fail(BX_EINVAL, "reaction " + std::to_string(j) + ": a standard free energy needs products");
+    d.nr = r.n_reactants; d.np = r.n_products; d.vmax = r.vmax; d.keq = r.keq; d.t0 = r.term0; d.nt = r.nterm;
+    for (int q = 0; q < r.n_reactants; ++q) {
+      if (r.reactant[q] < 0 || r.reactant[q] >= S) return fail(BX_EINVAL, "reactant names no substance");
+      if (!(r.reactant_Km[q] > 0.0)) return fail(BX_EINVAL, "reactant Km must be > 0");
+      d.r[q] = r.reactant[q]; d.rc[q] = r.reactant_coeff[q]; d.rkm[q] = r.reactant_Km[q];
+      tb->rm[r.reactant[q]][j] += -r.reactant_coeff[q];
+    }
+    for (int q = 0; q < r.n_products; ++q) {
+      if (r.product[q] < 0 || r.product[q] >= S) return fail(BX_EINVAL, "product names no substance");
+      d.p[q] = r.product[q]; d.pc[q] = r.product_coeff[q];
+      tb->rm[r.product[q]][j] += r.product_coeff[q];
+    }
+    if (!net_range_ok(sp, r.term0, r.nterm, &why)) return fail(BX_EINVAL, "reaction " + std::to_string(j) + ": " + why);
+  }
+  for (int q = 0; q < sp->n_terms; ++q) {
+    const bx_net_term& t = sp->terms[q];
+    tb->term[q] = bx::NetTermD{t.kind, t.substance, t.env_zone ? 1 : 0, 0, t.Km, t.n};
+  }
+  std::unique_ptr<bx_network> n(new bx_network());
+  struct Guard {
+    std::unique_ptr<bx_network>* p;
+    ~Guard() { if (*p) net_free(p->get()); }
+  } guard{&n};
+  n->h = h; n->S = S; n->R = R; n->any_ui = any_ui;
+  n->nblk = (C + bx::kNetTPB - 1) / bx::kNetTPB;
+  if (dalloc(&n->d_tab, 1) != cudaSuccess || dalloc(&n->d_cc, (size_t)S * C) != cudaSuccess ||
+      dalloc(&n->d_cm, (size_t)S * M) != cudaSuccess || dalloc(&n->d_cmid, (size_t)S * C) != cudaSuccess ||
+      dalloc(&n->d_cmmid, (size_t)S * M) != cudaSuccess || dalloc(&n->d_env, (size_t)S) != cudaSuccess ||
+      dalloc(&n->d_part, (size_t)n->nblk * S) != cudaSuccess || dalloc(&n->d_fmem, (size_t)S * M) != cudaSuccess ||
+      dalloc(&n->d_fgj, (size_t)S * M) != cudaSuccess || dalloc(&n->d_neg, 1) != cudaSuccess)
+    return fail(BX_ENOMEM, "network allocation");
+  BX_CU(cudaMemcpy(n->d_tab, tb.get(), sizeof(bx::NetTables), cudaMemcpyHostToDevice));
+  BX_CU(cudaMemset(n->d_neg, 0, sizeof(unsigned long long)));
+  BX_CU(cudaMemset(n->d_fmem, 0, (size_t)S * M * sizeof(double)));
+  BX_CU(cudaMemset(n->d_fgj, 0, (size_t)S * M * sizeof(double)));
+  if (any_ui) {
+    std::vector<double> msa(M);
+    BX_CU(cudaMemcpy(msa.data(), h->d_mem_sa, (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<double> gam(M), rr(M);
+    for (int m = 0; m < M; ++m) {
+      const double mv = sp->mem_vol[m];
+      if (!(mv > 0.0) || !(sp->R_rads[m] > 0.0)) return fail(BX_EINVAL, "mem_vol and R_rads must be > 0");
+      gam[m] = msa[m] / ((3.0 / 4.0) * mv);
+      rr[m] = sp->R_rads[m];
+    }
+    if (dalloc(&n->d_gamma, M) != cudaSuccess || dalloc(&n->d_Rr, M) != cudaSuccess)
+      return fail(BX_ENOMEM, "network allocation");
+    BX_CU(cudaMemcpy(n->d_gamma, gam.data(), (size_t)M * sizeof(double), cudaMemcpyHostToDevice));
+    BX_CU(cudaMemcpy(n->d_Rr, rr.data(), (size_t)M * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (mod_rows) {
+    if (dalloc(&n->d_gmod, (size_t)mod_rows * C) != cudaSuccess) return fail(BX_ENOMEM, "network allocation");
+    for (int k = 0; k < S; ++k)
+      if (tb->sub[k].mod_row >= 0)
+        BX_CU(cudaMemcpy(n->d_gmod + (size_t)tb->sub[k].mod_row * C, sp->substances[k].growth_mod,
+                         (size_t)C * sizeof(double), cudaMemcpyDefault));
+  }
+  if (mask_rows) {
+    if (dalloc(&n->d_gmask, (size_t)mask_rows * C) != cudaSuccess) return fail(BX_ENOMEM, "network allocation");
+    for (int k = 0; k < S; ++k)
+      if (tb->sub[k].mask_row >= 0)
+        BX_CU(cudaMemcpy(n->d_gmask + (size_t)tb->sub[k].mask_row * C, sp->substances[k].growth_target,
+                         (size_t)C, cudaMemcpyDefault));
+  }
+  *out = n.release();
+  return BX_OK;
+}
+
+int bx_network_upload(bx_network_handle n, const double* c_cells, const double* cc_at_mem, const double* c_env) {
+  if (!n || !c_cells || !cc_at_mem || !c_env) return fail(BX_EINVAL, "null argument");
+  const size_t S = n->S, C = n->h->C, M = n->h->M;
+  cudaStream_t s = n->h->stream;
+  BX_CU(cudaMemcpyAsync(n->d_cc, c_cells, S * C * sizeof(double), cudaMemcpyDefault, s));
+  BX_CU(cudaMemcpyAsync(n->d_cm, cc_at_mem, S * M * sizeof(double), cudaMemcpyDefault, s));
+  BX_CU(cudaMemcpyAsync(n->d_env, c_env, S * sizeof(double), cudaMemcpyDefault, s));
+  BX_CU(cudaMemsetAsync(n->d_neg, 0, sizeof(unsigned long long), s));
+  BX_CU(cudaStreamSynchronize(s));
+  n->have_state = true;
+  n->have_fluxes = false;
+  return BX_OK;
+}
+
+int bx_network_download(bx_network_handle n, double* c_cells, double* cc_at_mem, double* c_env) {
+  if (!n) return fail(BX_EINVAL, "null handle");
+  if (!n->have_state) return fail(BX_ESTATE, "bx_network_download before bx_network_upload");
+  const size_t S = n->S, C = n->h->C, M = n->h->M;
+  cudaStream_t s = n->h->stream;
+  if (c_cells) BX_CU(cudaMemcpyAsync(c_cells, n->d_cc, S * C * sizeof(double), cudaMemcpyDefault, s));
+  if (cc_at_mem) BX_CU(cudaMemcpyAsync(cc_at_mem, n->d_cm, S * M * sizeof(double), cudaMemcpyDefault, s));
+  if (c_env) BX_CU(cudaMemcpyAsync(c_env, n->d_env, S * sizeof(double), cudaMemcpyDefault, s));
+  BX_CU(cudaStreamSynchronize(s));
+  return BX_OK;
+}
+
+int bx_network_fluxes(bx_network_handle n, double* f_mem, double* f_gj) {
+  if (!n) return fail(BX_EINVAL, "null handle");
+  if (!n->have_fluxes) return fail(BX_ESTATE, "no network step with want_outputs yet");
+  const size_t bytes = (size_t)n->S * n->h->M * sizeof(double);
+  cudaStream_t s = n->h->stream;
+  if (f_mem) BX_CU(cudaMemcpyAsync(f_mem, n->d_fmem, bytes, cudaMemcpyDefault, s));
+  if (f_gj) BX_CU(cudaMemcpyAsync(f_gj, n->d_fgj, bytes, cudaMemcpyDefault, s));
+  BX_CU(cudaStreamSynchronize(s));
+  return BX_OK;
+}
+
+int bx_network_step(bx_network_handle n, int n_steps, int with_ions, int want_outputs) {
+  if (!n) return fail(BX_EINVAL, "null handle");
+  if (n_steps < 0) return fail(BX_EINVAL, "n_steps must be >= 0");
+  if (!n->have_state) return fail(BX_ESTATE, "bx_network_step before bx_network_upload");
+  bx_cluster* h = n->h;
+  if (!h->have_state) return fail(BX_ESTATE, "bx_network_step before the cluster's bx_state_upload");
+  if (with_ions && !h->have_dm) return fail(BX_ESTATE, "bx_network_step before bx_set_membrane_diffusivity");
+  if (n_steps == 0) return BX_OK;
+  cudaStream_t s = h->stream;
+  int left = n_steps;
+  const int tail = want_outputs ? 1 : 0;
+  if (with_ions) {
+    if (left - tail >= kGraphChunk) {
+      if (h->parity != 0) {
+        cudaError_t e = net_enqueue_coupled(n, h->parity, false, s);
+        if (e != cudaSuccess) return fail(BX_ECUDA, std::string("network step launch: ") + cudaGetErrorString(e));
+        h->parity ^= 1;
+        --left;
+      }
+      if (!n->graph) {
+        const int rc = net_capture(n, true, 0, &n->graph);
+        if (rc != BX_OK) return rc;
+      }
+      while (left - tail >= kGraphChunk) {
+        BX_CU(cudaGraphLaunch(n->graph, s));
+        h->launches += (int64_t)kGraphChunk * (launches_per_step(h) + 2);
+        left -= kGraphChunk;
+      }
+    }
+    while (left > 0) {
+      const bool out = want_outputs && left == 1;
+      cudaError_t e = net_enqueue_coupled(n, h->parity, out, s);
+      if (e != cudaSuccess) return fail(BX_ECUDA, std::string("network step launch: ") + cudaGetErrorString(e));
+      h->parity ^= 1;
+      --left;
+    }
+    h->steps_done += n_steps;
+    if (want_outputs) h->have_outputs = true;
+    h->last_step_outputs = want_outputs != 0;
+  } else {
+    if (left - tail >= kGraphChunk) {
+      if (!n->graph_net || n->graph_net_parity != h->parity) {
+        if (n->graph_net) cudaGraphExecDestroy(n->graph_net);
+        n->graph_net = nullptr;
+        const int rc = net_capture(n, false, h->parity, &n->graph_net);
+        if (rc != BX_OK) return rc;
+        n->graph_net_parity = h->parity;
+      }
+      while (left - tail >= kGraphChunk) {
+        BX_CU(cudaGraphLaunch(n->graph_net, s));
+        h->launches += (int64_t)kGraphChunk * 2;
+        left -= kGraphChunk;
+      }
+    }
+    while (left > 0) {
+      const bool out = want_outputs && left == 1;
+      cudaError_t e = net_enqueue(n, h->parity, out, s);
+      if (e != cudaSuccess) return fail(BX_ECUDA, std::string("network step launch: ") + cudaGetErrorString(e));
+      --left;
+    }
+  }
+  if (want_outputs) n->have_fluxes = true;
+  return BX_OK;
+}
+
+int bx_network_status(bx_network_handle n, int64_t* negative) {
+  if (!n || !negative) return fail(BX_EINVAL, "null argument");
+  unsigned long long v = 0;
+  BX_CU(cudaStreamSynchronize(n->h->stream));
+  BX_CU(cudaMemcpy(&v, n->d_neg, sizeof(v), cudaMemcpyDeviceToHost));
+  *negative = (int64_t)v;
+  return BX_OK;
+}
+
+int bx_network_destroy(bx_network_handle n) {
+  if (!n) return BX_OK;
+  if (n->h && n->h->stream) cudaStreamSynchronize(n->h->stream);
+  net_free(n);
+  delete n;
   return BX_OK;
 }
 

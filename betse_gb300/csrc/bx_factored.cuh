@@ -608,4 +608,188 @@ k_split_resident(FactGeom fg, SplitPtrs p, SplitConst k, ResArrays ra, int n_ste
   if (neg) atomicAdd(&p.status[2], (unsigned long long)neg);
 }
 
+// ---------------------------------------------------------------------------
+// The streaming factored step, persistent and software-pipelined.  Each warp
+// walks its own tiles t_j = warp + j * (warps of the grid) and stages them in
+// shared memory with cp.async (16-byte asynchronous copies that complete at
+// cp.async.wait_group -- no waits of ours): while it computes tile t_j, the
+// cell data of t_{j+1}, the gap-junction entries of t_{j+2} and the partner
+// records of t_{j+1} (gathered by the entries, which landed one iteration
+// earlier) are in flight.  The arithmetic is k_split_fact's, term by term, so
+// the results are bit-identical.  Per warp: two cell-data buffers, three
+// entry buffers and two record buffers (FactPipeSmem).
+// ---------------------------------------------------------------------------
+template <int NI>
+struct FactCellBuf {                   // one tile's cell data, in the order of its copy
+  float4 cst[32];
+  int gbeg[32];
+  float dsa[NI][32];
+  float2 cc2[NI][32];
+  float rec[32][8];
+};
+
+struct FactPipeSmem {
+  int emax;                            // entries per tile buffer (the largest tile's, + 2 for alignment)
+  size_t cell_bytes, ent_bytes, rec_bytes, warp_bytes;
+  __host__ __device__ FactPipeSmem(int max_entries, int NI) {
+    emax = max_entries + 2;
+    cell_bytes = (size_t)32 * 16 + 32 * 4 + (size_t)NI * 32 * 4 + (size_t)NI * 32 * 8 + 32 * 32;
+    ent_bytes = (size_t)emax * 8;
+    ent_bytes = (ent_bytes + 15) & ~(size_t)15;
+    rec_bytes = (size_t)emax * 32;
+    warp_bytes = 2 * cell_bytes + 3 * ent_bytes + 2 * rec_bytes;
+  }
+};
+
+template <int NW, int ZP>
+__global__ void __launch_bounds__(NW * 32)
+k_split_fact_pipe(FactGeom fg, SplitPtrs p, SplitConst k, const int* __restrict__ tile_e0, int max_entries) {
+  using IS = IonSet<ZP>;
+  constexpr int NI = IS::NI;
+  using CB = FactCellBuf<NI>;
+  const int I = IS::n(k);
+  extern __shared__ __align__(16) unsigned char fp_smem[];
+  const FactPipeSmem L(max_entries, NI);
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  unsigned char* base = fp_smem + (size_t)wl * L.warp_bytes;
+  const unsigned cell_b = (unsigned)L.cell_bytes, ent_b = (unsigned)L.ent_bytes, rec_b = (unsigned)L.rec_bytes;
+  auto cb = [&](int q) { return reinterpret_cast<CB*>(base + q * cell_b); };
+  auto eb = [&](int q) { return reinterpret_cast<int2*>(base + 2 * cell_b + q * ent_b); };
+  auto rb = [&](int q) { return reinterpret_cast<float*>(base + 2 * cell_b + 3 * ent_b + q * rec_b); };
+  const int stride = gridDim.x * NW;
+  const int t0 = blockIdx.x * NW + wl;
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
+  cudaTriggerProgrammaticLaunchCompletion();
+  cudaGridDependencySynchronize();
+#endif
+  // the copies of one tile's cell data (contiguous ranges of the per-slot arrays)
+  auto issue_cells = [&](int t, CB* d) {
+    if (t >= fg.ntile) return;
+    const int s0 = t * 32;
+    char* dst = reinterpret_cast<char*>(d);
+    const int n_cst = 32, n_gb = 8, n_dsa = NI * 8, n_cc = NI * 16, n_rec = 64;
+    const int total = n_cst + n_gb + n_dsa + n_cc + n_rec;
+    for (int c = lane; c < total; c += 32) {
+      const char* src;
+      char* to;
+      int r = c;
+      if (r < n_cst) { src = reinterpret_cast<const char*>(fg.cst + s0) + 16 * r; to = reinterpret_cast<char*>(d->cst) + 16 * r; }
+      else if ((r -= n_cst) < n_gb) { src = reinterpret_cast<const char*>(fg.gbeg + s0) + 16 * r; to = reinterpret_cast<char*>(d->gbeg) + 16 * r; }
+      else if ((r -= n_gb) < n_dsa) {
+        const int i = r / 8, o = 16 * (r % 8);
+        if (i >= I) continue;
+        src = reinterpret_cast<const char*>(fg.dsa + (size_t)i * fg.S + s0) + o; to = reinterpret_cast<char*>(d->dsa[i]) + o;
+      } else if ((r -= n_dsa) < n_cc) {
+        const int i = r / 16, o = 16 * (r % 16);
+        if (i >= I) continue;
+        src = reinterpret_cast<const char*>(p.cc2 + (size_t)i * fg.S + s0) + o; to = reinterpret_cast<char*>(d->cc2[i]) + o;
+      } else {
+        r -= n_cc;
+        src = reinterpret_cast<const char*>(p.rec_in + (size_t)s0 * 8) + 16 * r; to = reinterpret_cast<char*>(d->rec) + 16 * r;
+      }
+      (void)dst;
+      cp16(to, src);
+    }
+  };
+  // the tile's entries, from the 16-byte boundary at or below its first
+  auto issue_entries = [&](int t, int2* d) {
+    if (t >= fg.ntile) return;
+    const int e0 = tile_e0[t] & ~1, e1 = tile_e0[t + 1];
+    const int n16 = (e1 - e0 + 1) >> 1;
+    for (int c = lane; c < n16; c += 32) cp16(d + 2 * c, fg.gj + e0 + 2 * c);
+  };
+  // the partner records of the tile's entries, in entry order
+  auto issue_records = [&](int t, const int2* e, float* d) {
+    if (t >= fg.ntile) return;
+    const int ea = tile_e0[t], off = ea - (ea & ~1), n = tile_e0[t + 1] - ea;
+    for (int j = lane; j < n; j += 32) {
+      const float* src = p.rec_in + (size_t)e[off + j].x * 8;
+      cp16(d + 8 * j, src);
+      cp16(d + 8 * j + 4, src + 4);
+    }
+  };
+
+  // prologue: cells and entries of t0, entries of t1; then records of t0
+  issue_cells(t0, cb(0));
+  issue_entries(t0, eb(0));
+  cp_commit();
+  issue_entries(t0 + stride, eb(1));
+  cp_commit();
+  asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+  __syncwarp();
+  issue_records(t0, eb(0), rb(0));
+  cp_commit();
+
+  unsigned bad = 0, neg = 0, nanv = 0;
+  int j = 0;
+  for (int t = t0; t < fg.ntile; t += stride, ++j) {
+    const int ca = j & 1, ea = j % 3;
+    issue_cells(t + stride, cb(ca ^ 1));
+    issue_entries(t + 2 * stride, eb((j + 2) % 3));
+    cp_commit();
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");   // cells, entries and records of t; entries of t+1
+    __syncwarp();
+    issue_records(t + stride, eb((j + 1) % 3), rb(ca ^ 1));
+    cp_commit();
+
+    const CB& c = *cb(ca);
+    const int2* e = eb(ea);
+    const float* rr = rb(ca);
+    const float4 cs = c.cst[lane];
+    const int gcnt = __float_as_int(cs.w);
+    const int cl = fg.blk_cluster[t];
+    const int tfirst = tile_e0[t];
+    const int eoff = tfirst - (tfirst & ~1);
+    float s1[NI];
+#pragma unroll
+    for (int i = 0; i < NI; ++i) s1[i] = 0.f;
+    if (gcnt >= 0) {
+      const float* own = c.rec[lane];
+      const float4 o0 = reinterpret_cast<const float4*>(own)[0];
+      const float4 o1 = reinterpret_cast<const float4*>(own)[1];
+      const float ov[8] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y, o1.z, o1.w};
+      float cin[NI], cenv[NI], s2[NI], dsa[NI];
+#pragma unroll
+      for (int i = 0; i < NI; ++i) {
+        cin[i] = (i < I && i < 7) ? ov[i] : 0.f;
+        cenv[i] = (i < I) ? p.cenv_f[(size_t)cl * I + i] : 0.f;
+        dsa[i] = (i < I) ? c.dsa[i][lane] : 0.f;
+        s2[i] = 0.f;
+      }
+      const float pc = p.pump_coef[cl];
+      const float v1 = o1.w + 1.0e-25f;
+      const int j0 = c.gbeg[lane] - tfirst;
+      for (int q = j0; q < j0 + gcnt; ++q) {
+        const float4* r4 = reinterpret_cast<const float4*>(rr + 8 * q);
+        fact_gj_add<ZP, NI>(k, I, v1, cin, r4[0], r4[1], __int_as_float(e[eoff + q].y), s2);
+      }
+      fact_trans<ZP, NI>(k, I, v1, cin, cenv, pc, dsa, cs.x, s1);
+      // the update reads the staged concentrations and writes the new ones to global memory
+      float2 x2[NI];
+#pragma unroll
+      for (int i = 0; i < NI; ++i) x2[i] = (i < I) ? c.cc2[i][lane] : make_float2(0.f, 0.f);
+      float rec[8];
+      fact_update<NI>(k, I, s1, s2, cs.y, cs.z, x2, (size_t)1, rec, bad, neg, nanv);
+      const int s = t * 32 + lane;
+#pragma unroll
+      for (int i = 0; i < NI; ++i)
+        if (i < I) p.cc2[(size_t)i * fg.S + s] = x2[i];
+      float4* o4 = reinterpret_cast<float4*>(p.rec_out + (size_t)s * 8);
+      o4[0] = make_float4(rec[0], rec[1], rec[2], rec[3]);
+      o4[1] = make_float4(rec[4], rec[5], rec[6], rec[7]);
+    }
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      if (i >= I) break;
+      const float v = warp_sum_down(s1[i]);
+      if (lane == 0) p.env_part[(size_t)t * I + i] = v;
+    }
+    __syncwarp();     // every lane is done with the buffers of t before they are refilled
+  }
+  cp_wait_all();
+  if (nanv) atomicAdd(&p.status[0], (unsigned long long)nanv);
+  if (bad) atomicAdd(&p.status[1], (unsigned long long)bad);
+  if (neg) atomicAdd(&p.status[2], (unsigned long long)neg);
+}
+
 }  // namespace bx

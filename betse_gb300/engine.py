@@ -19,7 +19,7 @@ from .exceptions import BetseSimUnstableException
 PRECISIONS = {'fp64': _lib.PLAIN_FP64, 'plain': _lib.PLAIN_FP64,
               'split': _lib.SPLIT_FP32, 'fp32': _lib.SPLIT_FP32}
 # kernels of the split form (bx_set_launch_config)
-KERNELS = {'tile': 0, 'persistent': 1, 'factored': 2, 'resident': 3}
+KERNELS = {'tile': 0, 'persistent': 1, 'factored': 2, 'resident': 3, 'pipelined': 4}
 KERNEL_NAMES = {v: k for k, v in KERNELS.items()}
 
 
@@ -230,7 +230,7 @@ class ClusterEngine:
     def set_launch_config(self, tpb, kernel=0):
         """Pin the tile size (membrane slots per tile) and, for the split form,
         the kernel: 0/'tile', 1/'persistent' (True), 2/'factored',
-        3/'resident'; the state is kept."""
+        3/'resident', 4/'pipelined' (factored, persistent); the state is kept."""
         k = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
         _lib.check(self.lib.bx_set_launch_config(self.h, int(tpb), k), 'bx_set_launch_config')
 

@@ -382,7 +382,10 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
  *   3  resident kernel: the factored step for many steps in one cooperative
  *      launch, each SM keeping its cells in shared memory (one cluster that
  *      fits; otherwise kernel 2 runs)
- * Kernels 1-3 need no extracellular spaces, no voltage-gated gap junctions
+ *   4  factored kernel, persistent and software-pipelined: each warp stages
+ *      its next tiles' cell data, gap-junction entries and partner records
+ *      in shared memory (cp.async) while it computes (results as kernel 2)
+ * Kernels 1-4 need no extracellular spaces, no voltage-gated gap junctions
  * and no Ca-ATPase; steps with outputs or a nonzero Phi_b always run the
  * tile kernel.  The state is kept.  bx_autotune picks these by timing. */
 int bx_set_launch_config(bx_handle h, int tpb, int kernel);
@@ -398,7 +401,8 @@ int bx_resident_barrier_check(bx_handle h, int64_t timeout_ns, int* timed_out);
 
 /* Autotuner: times n_steps steps (run as bx_step runs them) for each
  * launch configuration -- tile size and, for the split form, the tile,
- * persistent, factored (at two load depths) and resident kernels -- on the
+ * persistent, factored (at two load depths), pipelined factored and
+ * resident kernels -- on the
  * uploaded state, keeps the fastest, and restores the state so the
  * simulation does not advance.
  * Reports the choice and its ms per step (either pointer may be NULL). */
@@ -419,6 +423,97 @@ int64_t bx_launch_count(bx_handle h);
  * operators): info[8] = {n_clusters, n_cells, n_mems, n_ions, grid_ny,
  * grid_nx, is_ecm, precision} (cells and membranes summed over a batch). */
 int bx_cluster_info(bx_handle h, int32_t* info);
+
+/* ---- Molecule and gene regulatory networks ------------------------------
+ * MasterOfNetworks.run_loop (chemistry/networks.py:2805-2983) for the
+ * user-defined substances of a general network (sim.molecules, sim.py:
+ * 1290-1303) or a gene regulatory network (sim.grn, sim.py:1305-1319;
+ * gene.py:220-308 runs it without the ions), on a plain FP64 single-cluster
+ * handle without extracellular spaces.  BETSE builds every rate as a Python
+ * string and evals it each step; the network here is the same arithmetic as
+ * tables: substances, influencer terms and cell-zone reactions.
+ *
+ * An influencer factor (get_influencers, networks.py:5084-5600) is a range of
+ * terms; its value is
+ *   (prod of BX_TERM_ACT terms, or 1 if none) + sum of BX_TERM_ACT_INDEP terms
+ *   times prod of BX_TERM_INH terms, times the sum of the direct terms if any,
+ * with act = (c/Km)^n / (1 + (c/Km)^n), inh = 1 / (1 + (c/Km)^n) and direct
+ * terms +c (BX_TERM_DIRECT_POS, an '&' activator) or -c (BX_TERM_DIRECT_NEG,
+ * an '&' inhibitor); c is the substance's cell concentration, or its
+ * well-mixed environment concentration when env_zone is 1. */
+#define BX_NET_MAX_SUBSTANCES 16
+#define BX_NET_MAX_REACTIONS 32
+#define BX_NET_MAX_TERMS 256
+#define BX_NET_MAX_STOICH 4
+#define BX_TERM_ACT 0
+#define BX_TERM_ACT_INDEP 1
+#define BX_TERM_INH 2
+#define BX_TERM_DIRECT_POS 3
+#define BX_TERM_DIRECT_NEG 4
+
+typedef struct bx_net_term {
+    int32_t kind;        /* BX_TERM_* */
+    int32_t substance;   /* index into the network's substances */
+    int32_t env_zone;    /* 0: cell concentration, 1: environment */
+    int32_t pad;
+    double Km, n;
+} bx_net_term;
+
+typedef struct bx_net_substance {   /* Molecule fields (networks.py:337-600) */
+    double z, Dm, Do, Dgj;
+    double time_factor;             /* modify_time_factor: the time dilation factor or 1 */
+    double r_production, r_decay, decay_max, gad_scale_factor;
+    int32_t growth;                 /* 'growth and decay' given (simple_growth) */
+    int32_t update_intra;           /* 'update intracellular' */
+    int32_t gj_impermeable;         /* 'GJ impermeable' */
+    int32_t growth_term0, growth_nterm;   /* growth influencers */
+    int32_t decay_term0, decay_nterm;     /* decay influencers */
+    int32_t pad;
+    const double* growth_mod;       /* [n_cells] growth_mod_function_cells, or NULL (1) */
+    const uint8_t* growth_target;   /* [n_cells] 1 on growth_targets_cell, or NULL (all) */
+} bx_net_substance;
+
+typedef struct bx_net_reaction {    /* Reaction fields (networks.py:814-922) */
+    int32_t n_reactants, n_products;
+    int32_t reactant[BX_NET_MAX_STOICH], product[BX_NET_MAX_STOICH];
+    double reactant_coeff[BX_NET_MAX_STOICH], reactant_Km[BX_NET_MAX_STOICH];
+    double product_coeff[BX_NET_MAX_STOICH];
+    double vmax;
+    double keq;                     /* exp(-delta_Go / (R T)); 0: no standard free energy */
+    int32_t term0, nterm;           /* reaction activators and inhibitors */
+} bx_net_reaction;
+
+typedef struct bx_net_spec {
+    int32_t n_substances, n_reactions, n_terms, pad;
+    const bx_net_substance* substances;
+    const bx_net_reaction* reactions;
+    const bx_net_term* terms;
+    const double* mem_vol;          /* [n_mems] cells.mem_vol (update intracellular) */
+    const double* R_rads;           /* [n_mems] cells.R_rads (update intracellular) */
+} bx_net_spec;
+
+typedef struct bx_network* bx_network_handle;
+/* Build a network on a cluster handle; copies the spec.  The handle must
+ * outlive the network.  Refuses (BX_EINVAL) split-form, batched and ECM
+ * handles and out-of-range tables. */
+int bx_network_create(bx_handle cluster, const bx_net_spec* spec, bx_network_handle* out);
+/* The substance state (Molecule.c_cells [S][C], cc_at_mem [S][M], c_env [S]:
+ * the well-mixed value), host or device arrays. */
+int bx_network_upload(bx_network_handle n, const double* c_cells, const double* cc_at_mem, const double* c_env);
+int bx_network_download(bx_network_handle n, double* c_cells, double* cc_at_mem, double* c_env);
+/* n_steps time steps.  with_ions = 1: each step is the cluster's ion step
+ * (bx_step) followed by the network step in BETSE's order -- the network
+ * reads Vmem from the start of the step and the gap-junction state that
+ * step leaves; with_ions = 0: the network alone on the cluster's current
+ * Vmem and gap-junction state (gene.py:220-308).  want_fluxes = 1 keeps the
+ * last step's membrane and gap-junction fluxes for bx_network_fluxes. */
+int bx_network_step(bx_network_handle n, int n_steps, int with_ions, int want_fluxes);
+int bx_network_fluxes(bx_network_handle n, double* f_mem, double* f_gj);   /* [S][M] each */
+/* Negative substance concentrations seen since the upload (BETSE raises
+ * BetseSimUnstableException on them, sim_toolbox.py:1132-1151,
+ * networks.py:5802-5807). */
+int bx_network_status(bx_network_handle n, int64_t* negative);
+int bx_network_destroy(bx_network_handle n);
 
 #ifdef __cplusplus
 }

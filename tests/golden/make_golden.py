@@ -286,7 +286,7 @@ OUT_KEYS = ['fluxes_mem', 'fluxes_gj', 'rate_NaKATP', 'rho_cells', 'Jn',
 
 def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
              dm_range=(1e-19, 1e-17), cell_space=26e-9, sharpness=1.0, v_sensitive_gj=False,
-             alpha_Ca=0.0, cell_polarizability=0.0):
+             alpha_Ca=0.0, cell_polarizability=0.0, network=None):
     from betse.science.sim import Simulator
     from betse.science.enum.enumphase import SimPhaseKind
     n_steps = max(checkpoints)
@@ -307,6 +307,7 @@ def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
     s.clear_storage(c, p)
     s.update_V(c, p)
     out = {}
+    core = attach_network(phase, network, out) if network else None
     # ---- geometry and index maps, exactly as Cells built them
     g = dict(
         mem_to_cells=np.asarray(c.mem_to_cells, np.int64),
@@ -368,6 +369,8 @@ def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
         done = cp
         for k in state_keys:
             out[f's{cp}_' + k] = np.array(getattr(s, k), np.float64)
+        if core is not None:
+            save_network_state(core, out, f's{cp}_')
         for k in OUT_KEYS:
             if cp in cps[:2] and hasattr(s, k):
                 v = getattr(s, k)
@@ -383,6 +386,120 @@ def run_case(name, radius, seed, is_ecm, grid_size, dt, checkpoints,
           f'{1e3 * t_loop / n_steps:.2f} ms/step, '
           f'{os.path.getsize(path) / 1024:.0f} KiB')
     return out
+
+
+# --------------------------------------------------------------------------
+# Molecule networks (MasterOfNetworks, chemistry/networks.py)
+# --------------------------------------------------------------------------
+# A four-substance, two-reaction network written for these fixtures in the
+# configuration format BETSE reads ('general network' -> 'biomolecules' and
+# 'reactions'). Between them the entries use each influencer kind that
+# get_influencers composes (networks.py:5084-5600): multiplicative, '!'
+# independent and '&' direct activators, inhibitors, an 'env'-zone inhibitor
+# and decay activators; growth restricted to a tissue profile and modulated by
+# gradient_x; time dilation; 'update intracellular' on and off; a charged and
+# neutral substances crossing the membrane and the gap junctions; one
+# irreversible reaction and one with a standard free energy. Absent entries
+# are the string 'None', as BETSE's YAML loader gives them.
+def _plot_block():
+    return {'plot 2D': False, 'animate': False, 'autoscale colorbar': True, 'max val': 1.0, 'min val': 0.0}
+
+
+def _substance(name, z, Dm, Do, Dgj, env, cell, gad, update_intra=False, gj_impermeable=False,
+               time_dilation=False):
+    return {'name': name, 'Dm': Dm, 'Do': Do, 'Dgj': Dgj, 'z': z, 'env conc': env, 'cell conc': cell,
+            'update intracellular': update_intra, 'use time dilation': time_dilation,
+            'TJ permeable': False, 'GJ impermeable': gj_impermeable, 'TJ factor': 1.0,
+            'growth and decay': gad, 'plotting': _plot_block()}
+
+
+NETWORK_SUBSTANCES = [
+    _substance('A', 0, 0.0, 1.0e-12, 2.0e-15, 0.0, 0.1,
+               {'production rate': 0.5, 'decay rate': 0.2, 'apply to': 'all',
+                'modulator function': 'gradient_x', 'activators': 'None', 'Km activators': 'None',
+                'n activators': 'None', 'inhibitors': ['C'], 'Km inhibitors': [0.3], 'n inhibitors': [2.0]}),
+    _substance('B', 0, 0.0, 1.0e-12, 1.0e-15, 0.0, 0.05,
+               {'production rate': 1.0, 'decay rate': 0.5, 'apply to': ['spot'],
+                'modulator function': 'None', 'activators': ['A', 'C!'], 'Km activators': [0.2, 0.5],
+                'n activators': [2.0, 1.0], 'inhibitors': 'None', 'Km inhibitors': 'None', 'n inhibitors': 'None',
+                'decay max': 0.3, 'decay activators': ['A'], 'Km decay activators': [0.4],
+                'n decay activators': [1.0]}, gj_impermeable=True),
+    _substance('C', -1, 1.0e-18, 1.0e-11, 1.0e-14, 0.5, 0.2,
+               {'production rate': 0.2, 'decay rate': 0.1, 'apply to': 'all', 'modulator function': 'None',
+                'activators': ['B', 'A&'], 'Km activators': [0.1, 1.0], 'n activators': [1.0, 1.0],
+                'inhibitors': 'None', 'Km inhibitors': 'None', 'n inhibitors': 'None'}),
+    _substance('D', 0, 5.0e-19, 1.0e-11, 1.0e-15, 1.0, 0.1,
+               {'production rate': 0.05, 'decay rate': 0.05, 'apply to': 'all', 'modulator function': 'None',
+                'activators': 'None', 'Km activators': 'None', 'n activators': 'None',
+                'inhibitors': ['C'], 'zone inhibitors': ['env'], 'Km inhibitors': [0.4],
+                'n inhibitors': [1.0]}, update_intra=True, time_dilation=True),
+]
+
+NETWORK_REACTIONS = [
+    {'name': 'r1', 'reaction zone': 'cell', 'reactants': ['A', 'C'], 'reactant multipliers': [1, 1],
+     'Km reactants': [0.1, 0.2], 'products': ['D'], 'product multipliers': [1], 'Km products': [0.5],
+     'max rate': 0.01, 'standard free energy': 'None', 'reaction activators': ['B'], 'activator Km': [0.1],
+     'activator n': [2.0]},
+    {'name': 'r2', 'reaction zone': 'cell', 'reactants': ['D'], 'reactant multipliers': [1],
+     'Km reactants': [0.3], 'products': ['B'], 'product multipliers': [2], 'Km products': [0.4],
+     'max rate': 0.02, 'standard free energy': -5000.0, 'reaction inhibitors': ['A'], 'inhibitor Km': [0.5],
+     'inhibitor n': [1.0]},
+]
+
+NETWORK = dict(substances=NETWORK_SUBSTANCES, reactions=NETWORK_REACTIONS, time_dilation=2.0,
+               spot_fraction=0.3, gradient_x={'x-offset': 0.1, 'exponent': 3.0, 'slope': 1.0, 'z-offset': 0.2})
+
+
+def attach_network(phase, net, out):
+    """Build BETSE's MasterOfNetworks the way MasterOfMolecules.read_mol_config
+    does (chemistry/molecules.py) and hook it into the step loop
+    (sim.py:1290-1303, p.molecules_enabled)."""
+    from betse.science.chemistry.networks import MasterOfNetworks
+    sim, cells, p = phase.sim, phase.cells, phase.p
+    p.substances_affect_charge = False
+    p.gradient_x_properties = dict(net['gradient_x'])
+    rng = np.random.default_rng(1234)
+    n_c = len(cells.cell_i)
+    spot = np.sort(rng.choice(n_c, size=max(1, int(net['spot_fraction'] * n_c)), replace=False))
+    phase.dyna.cell_target_inds = {'spot': list(spot)}
+    mem_spot = np.nonzero(np.isin(np.asarray(cells.mem_to_cells), spot))[0]
+    phase.dyna.tissue_target_inds = {'spot': list(mem_spot)}
+    core = MasterOfNetworks(sim, cells, net['substances'], p)
+    core.time_dila = float(net['time_dilation'])
+    core.read_substances(sim, cells, net['substances'], p)
+    core.tissue_init(phase, net['substances'])
+    core.read_reactions(net['reactions'], sim, cells, p)
+    core.write_reactions()
+    core.create_reaction_matrix()
+    core.write_reactions_env()
+    core.create_reaction_matrix_env()
+    sim.molecules = SimpleNamespace(core=core, transporters=False, channels=False, modulators=False)
+    p.molecules_enabled = True
+    import json
+    out['net_config'] = np.asarray(json.dumps({'substances': net['substances'], 'reactions': net['reactions'],
+                                               'time_dilation': net['time_dilation']}))
+    out['net_spot_cells'] = spot.astype(np.int64)
+    out['net_names'] = np.asarray(list(core.molecules))
+    out['net_reaction_matrix'] = np.asarray(core.reaction_matrix)
+    out['net_mem_vol'] = np.asarray(cells.mem_vol, np.float64)
+    out['net_growth_mod'] = np.stack([np.asarray(m.growth_mod_function_cells, np.float64) *
+                                      np.ones(n_c) if m.simple_growth else np.ones(n_c)
+                                      for m in core.molecules.values()])
+    save_network_state(core, out, 'init_')
+    return core
+
+
+def save_network_state(core, out, prefix):
+    mols = list(core.molecules.values())
+    out[prefix + 'net_c_cells'] = np.stack([np.array(m.c_cells, np.float64) for m in mols])
+    out[prefix + 'net_cc_at_mem'] = np.stack([np.array(m.cc_at_mem, np.float64) for m in mols])
+    out[prefix + 'net_c_env'] = np.stack([np.array(m.c_env, np.float64) for m in mols])
+    if prefix != 'init_':
+        out[prefix + 'net_f_mem'] = np.stack([np.array(m.f_mem, np.float64) * np.ones(len(m.cc_at_mem))
+                                              for m in mols])
+        out[prefix + 'net_f_gj'] = np.stack([np.array(m.f_gj, np.float64) * np.ones(len(m.cc_at_mem))
+                                             for m in mols])
+
 
 
 CASES = {
@@ -414,6 +531,9 @@ CASES = {
     # (the value phasereqs.py sets when a phase asks for it)
     'noecm_r50_s17_pol': dict(radius=50e-6, seed=17, is_ecm=False, grid_size=20,
                               dt=1e-2, checkpoints=[1, 2, 40], cell_polarizability=1e-4),
+    # a molecule network (MasterOfNetworks.run_loop) stepped with the ions
+    'net_r50_s21': dict(radius=50e-6, seed=21, is_ecm=False, grid_size=20,
+                        dt=1e-2, checkpoints=[1, 2, 50, 300], network=NETWORK),
     # a handful of cells: boundary-dominated edge case
     'noecm_r20_s2': dict(radius=20e-6, seed=2, is_ecm=False, grid_size=12,
                          dt=1e-2, checkpoints=[1, 20]),

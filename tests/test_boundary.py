@@ -127,12 +127,17 @@ def test_ctypes_layouts_match_c_compiler(tmp_path):
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "bx.h"\n'
                    'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\\n",'
                    'sizeof(bx_geom), sizeof(bx_params), sizeof(bx_state), sizeof(bx_outputs),'
-                   'sizeof(bx_step_status), offsetof(bx_params, zs), offsetof(bx_geom, gj_len));return 0;}\n')
+                   'sizeof(bx_step_status), offsetof(bx_params, zs), offsetof(bx_geom, gj_len));'
+                   'printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(bx_net_term), sizeof(bx_net_substance),'
+                   'sizeof(bx_net_reaction), sizeof(bx_net_spec), offsetof(bx_net_substance, growth_mod),'
+                   'offsetof(bx_net_reaction, keq));return 0;}\n')
     exe = tmp_path / 'probe'
     subprocess.run([cc, '-I', os.path.join(ROOT, 'include'), str(src), '-o', str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
                                           check=True).stdout.split()]
     want = [ct.sizeof(_lib.BxGeom), ct.sizeof(_lib.BxParams), ct.sizeof(_lib.BxState),
             ct.sizeof(_lib.BxOutputs), ct.sizeof(_lib.BxStepStatus),
-            _lib.BxParams.zs.offset, _lib.BxGeom.gj_len.offset]
+            _lib.BxParams.zs.offset, _lib.BxGeom.gj_len.offset,
+            ct.sizeof(_lib.BxNetTerm), ct.sizeof(_lib.BxNetSubstance), ct.sizeof(_lib.BxNetReaction),
+            ct.sizeof(_lib.BxNetSpec), _lib.BxNetSubstance.growth_mod.offset, _lib.BxNetReaction.keq.offset]
     assert got == want

@@ -154,3 +154,32 @@ def test_resident_barrier_timeout_is_reported_and_harmless():
     for k in ('cc_cells', 'cc_env'):
         assert gi.rel_err(got[k], ref[k]) < 1e-9, k
     assert gi.rel_err(got['cc_at_mem'], ref['cc_at_mem']) < 2.5e-7
+
+
+def test_pipelined_equals_factored_bit_for_bit():
+    """The persistent pipelined factored kernel computes k_split_fact's
+    arithmetic on staged copies of the same data: the same state, bit for
+    bit, on a golden cluster, ragged cells and a batch of clusters."""
+    from betse_gb300.engine import BatchEngine
+    for d in (gi.load('noecm_r80_s1'), synthetic.ragged_fixture()):
+        res = []
+        for kernel in ('factored', 'pipelined'):
+            with _engine(d, kernel) as e:
+                e.step(45)
+                e.check_stable()
+                res.append(e.download())
+        for k in res[0]:
+            assert np.array_equal(res[0][k], res[1][k]), k
+    ds = [synthetic.ragged_fixture(), gi.load('noecm_r50_s7'), gi.load('noecm_r80_s1')]
+    ins = [gi.engine_inputs(d) for d in ds]
+    got = []
+    for kernel in ('factored', 'pipelined'):
+        with BatchEngine([x[0] for x in ins], [x[1] for x in ins], 'split') as b:
+            b.set_membrane_diffusivity([x[2] for x in ins])
+            b.upload_states([x[3] for x in ins])
+            b.set_launch_config(256, kernel)
+            b.step(70)
+            got.append(b.download_states())
+    for a, c in zip(*got):
+        for k in a:
+            assert np.array_equal(a[k], c[k]), k
