@@ -266,7 +266,7 @@ def cpu_baseline_sweep(gs, ps, Dms, sts, budget_s=12.0):
                       f'C restatement of the step (oracle/c), {threads} OpenMP threads'}
 
 
-def init_time_to_steady(n_clusters=16, n_cells=5000):
+def init_time_to_steady(n_clusters=256, n_cells=5000):
     """The learned warm start against the plain init on fresh clusters."""
     from betse_gb300 import warmstart as ws
     r = ws.evaluate(ws.WarmStart(), n_clusters=n_clusters, n_cells=n_cells, seed=9001, max_steps=1_500_000,

@@ -2452,7 +2452,7 @@ struct bx_network {
   bx::NetTables* d_tab = nullptr;
   double *d_gamma = nullptr, *d_Rr = nullptr, *d_gmod = nullptr, *d_cc = nullptr, *d_cm = nullptr,
          *d_cmid = nullptr, *d_cmmid = nullptr, *d_env = nullptr, *d_part = nullptr, *d_fmem = nullptr,
-         *d_fgj = nullptr;
+         *d_fgj = nullptr, *d_rates = nullptr;
   uint8_t* d_gmask = nullptr;
   unsigned long long* d_neg = nullptr;
   cudaGraphExec_t graph = nullptr;   // kGraphChunk coupled steps from ion parity 0
@@ -2464,7 +2464,7 @@ namespace {
 
 void net_free(bx_network* n) {
   void* ptrs[] = {n->d_tab, n->d_gamma, n->d_Rr, n->d_gmod, n->d_cc, n->d_cm, n->d_cmid, n->d_cmmid,
-                  n->d_env, n->d_part, n->d_fmem, n->d_fgj, n->d_gmask, n->d_neg};
+                  n->d_env, n->d_part, n->d_fmem, n->d_fgj, n->d_rates, n->d_gmask, n->d_neg};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (n->graph) cudaGraphExecDestroy(n->graph);
@@ -2505,7 +2505,8 @@ bx::NetArgs net_args(bx_network* n, int vm_parity) {
   a.vm = h->d_vm[vm_parity];
   a.tab = n->d_tab; a.gamma = n->d_gamma; a.R_rads = n->d_Rr; a.gmod = n->d_gmod; a.gmask = n->d_gmask;
   a.c_cells = n->d_cc; a.cmem = n->d_cm; a.c_mid = n->d_cmid; a.cmem_mid = n->d_cmmid; a.env = n->d_env;
-  a.env_part = n->d_part; a.f_mem = n->d_fmem; a.f_gj = n->d_fgj; a.neg = n->d_neg; a.nblk = n->nblk;
+  a.env_part = n->d_part; a.f_mem = n->d_fmem; a.f_gj = n->d_fgj; a.rates = n->d_rates; a.neg = n->d_neg;
+  a.nblk = n->nblk;
   return a;
 }
 
@@ -2640,12 +2641,14 @@ int bx_network_create(bx_handle h, const bx_net_spec* sp, bx_network_handle* out
       dalloc(&n->d_cm, (size_t)S * M) != cudaSuccess || dalloc(&n->d_cmid, (size_t)S * C) != cudaSuccess ||
       dalloc(&n->d_cmmid, (size_t)S * M) != cudaSuccess || dalloc(&n->d_env, (size_t)S) != cudaSuccess ||
       dalloc(&n->d_part, (size_t)n->nblk * S) != cudaSuccess || dalloc(&n->d_fmem, (size_t)S * M) != cudaSuccess ||
-      dalloc(&n->d_fgj, (size_t)S * M) != cudaSuccess || dalloc(&n->d_neg, 1) != cudaSuccess)
+      dalloc(&n->d_fgj, (size_t)S * M) != cudaSuccess || dalloc(&n->d_neg, 1) != cudaSuccess ||
+      dalloc(&n->d_rates, (size_t)std::max(R, 1) * C) != cudaSuccess)
     return fail(BX_ENOMEM, "network allocation");
   BX_CU(cudaMemcpy(n->d_tab, tb.get(), sizeof(bx::NetTables), cudaMemcpyHostToDevice));
   BX_CU(cudaMemset(n->d_neg, 0, sizeof(unsigned long long)));
   BX_CU(cudaMemset(n->d_fmem, 0, (size_t)S * M * sizeof(double)));
   BX_CU(cudaMemset(n->d_fgj, 0, (size_t)S * M * sizeof(double)));
+  BX_CU(cudaMemset(n->d_rates, 0, (size_t)std::max(R, 1) * C * sizeof(double)));
   if (any_ui) {
     std::vector<double> msa(M);
     BX_CU(cudaMemcpy(msa.data(), h->d_mem_sa, (size_t)M * sizeof(double), cudaMemcpyDeviceToHost));
@@ -2705,13 +2708,15 @@ int bx_network_download(bx_network_handle n, double* c_cells, double* cc_at_mem,
   return BX_OK;
 }
 
-int bx_network_fluxes(bx_network_handle n, double* f_mem, double* f_gj) {
+int bx_network_fluxes(bx_network_handle n, double* f_mem, double* f_gj, double* rates) {
   if (!n) return fail(BX_EINVAL, "null handle");
   if (!n->have_fluxes) return fail(BX_ESTATE, "no network step with want_outputs yet");
   const size_t bytes = (size_t)n->S * n->h->M * sizeof(double);
   cudaStream_t s = n->h->stream;
   if (f_mem) BX_CU(cudaMemcpyAsync(f_mem, n->d_fmem, bytes, cudaMemcpyDefault, s));
   if (f_gj) BX_CU(cudaMemcpyAsync(f_gj, n->d_fgj, bytes, cudaMemcpyDefault, s));
+  if (rates && n->R)
+    BX_CU(cudaMemcpyAsync(rates, n->d_rates, (size_t)n->R * n->h->C * sizeof(double), cudaMemcpyDefault, s));
   BX_CU(cudaStreamSynchronize(s));
   return BX_OK;
 }

@@ -23,7 +23,8 @@
 // the gap-junction flux reads the partner cell after its membrane step.
 //
 // Data layout in HBM (row = substance): c_cells [S][C], cc_at_mem [S][M] and
-// their "mid" copies, the last step's fluxes f_mem/f_gj [S][M], growth
+// their "mid" copies, the last step's fluxes f_mem/f_gj [S][M] and reaction
+// rates [R][C], growth
 // modulation [S][C] and target masks [S][C] only for the substances that have
 // them, env [S], env partials [nblk][S]; the tables (substances, terms,
 // reactions, stoichiometry) are one small block in global memory that every
@@ -98,6 +99,7 @@ struct NetArgs {
   double* env_part;          // [nblk][S]
   double* f_mem;             // [S][M] (OUT)
   double* f_gj;              // [S][M] (OUT)
+  double* rates;             // [R][C] (OUT) cell-zone reaction rates (MasterOfNetworks.reaction_rates)
   unsigned long long* neg;   // negative concentrations seen
   int nblk;
 };
@@ -231,6 +233,7 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
         }
         rate = rx.vmax * al * (1.0 - (num / den) / rx.keq);
       }
+      if (OUT) a.rates[(size_t)j * a.C + c] = rate;
       for (int k = 0; k < S; ++k) delta[k] += tb.rm[k][j] * rate;
     }
     const double inv_vol = 1.0 / a.cell_vol[c];

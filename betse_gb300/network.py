@@ -414,10 +414,14 @@ class Network:
                    'bx_network_step')
 
     def fluxes(self):
+        """The last output step's ``f_mem``, ``f_gj`` [S][M] and the cell-zone
+        ``reaction_rates`` [R][C]."""
         fm = np.empty((self.S, self.M))
         fg = np.empty((self.S, self.M))
-        _lib.check(self.lib.bx_network_fluxes(self.h, fm.ctypes.data, fg.ctypes.data), 'bx_network_fluxes')
-        return {'f_mem': fm, 'f_gj': fg}
+        rr = np.empty((len(self.spec.reactions), self.C))
+        _lib.check(self.lib.bx_network_fluxes(self.h, fm.ctypes.data, fg.ctypes.data,
+                                              rr.ctypes.data if rr.size else None), 'bx_network_fluxes')
+        return {'f_mem': fm, 'f_gj': fg, 'reaction_rates': rr}
 
     def negative_count(self):
         v = ct.c_int64()

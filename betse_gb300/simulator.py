@@ -14,10 +14,19 @@ the device under BETSE's names, then -- as the reference loop does --
 hold the last step, so ``run_sim_core``'s pickling and the plotting pipeline
 see what the reference would leave.
 
-Features of the reference loop outside the electrodiffusion step (endoplasmic
-reticulum calcium dynamics, molecules/GRN networks, pressures, flow, deformation, polarizability in the
-split form, scheduled events of the SIM phase, dynamic protein
-noise) are refused with ``NotImplementedError`` naming them, before any work.
+A general network (``p.molecules_enabled``) or a gene regulatory network
+(``p.grn_enabled``) steps with the ions in the plain FP64 form
+(``betse_gb300.network``; ``sim.py:1290-1319``): its substances are uploaded
+from the ``Molecule`` objects, and at each sampled step their concentrations,
+fluxes and the reaction rates are written back before ``write2storage`` (whose
+``core.write_data`` reads them).
+
+Features of the reference loop outside the step (endoplasmic reticulum
+calcium dynamics, pressures, flow, deformation, polarizability in the split
+form, networks in the split form or both networks at once, the network
+features ``NetworkSpec.from_betse`` names, scheduled events of the SIM phase,
+dynamic protein noise) are refused with ``NotImplementedError`` naming them,
+before any work.
 
 ``install()`` patches the method on BETSE's ``Simulator`` class.
 """
@@ -29,6 +38,7 @@ import numpy as np
 
 from .cluster import ClusterGeometry, StepParams
 from .engine import ClusterEngine
+from .network import Network, NetworkSpec
 
 
 def unsupported_features(sim, phase, assume_no_events=False, precision='fp64'):
@@ -41,9 +51,20 @@ def unsupported_features(sim, phase, assume_no_events=False, precision='fp64'):
     ions = getattr(p, 'ions_dict', {}) or {}
     if ions.get('Ca', 0) == 1 and bool(getattr(p, 'Ca_dyn', False)):
         reasons.append('endoplasmic reticulum calcium dynamics (Ca_dyn, sim.py:2157-2159)')
-    for flag, what in (('molecules_enabled', 'molecules network'),
-                       ('grn_enabled', 'gene regulatory network'),
-                       ('deform_osmo', 'osmotic pressure'),
+    nets = [f for f in ('molecules_enabled', 'grn_enabled') if bool(getattr(p, f, False))]
+    if len(nets) == 2:
+        reasons.append('a general network and a gene regulatory network at once '
+                       '(molecules_enabled and grn_enabled)')
+    if nets and precision != 'fp64':
+        reasons.append('networks in the split form (the plain form, precision="fp64", steps them)')
+    if nets and bool(getattr(p, 'is_ecm', False)):
+        reasons.append('networks with extracellular spaces (is_ecm)')
+    for flag, holder in (('molecules_enabled', 'molecules'), ('grn_enabled', 'grn')):
+        h = getattr(sim, holder, None) if flag in nets else None
+        for what in ('transporters', 'channels', 'modulators'):
+            if h is not None and getattr(h, what, False):
+                reasons.append(f'network {what} ({holder})')
+    for flag, what in (('deform_osmo', 'osmotic pressure'),
                        ('fluid_flow', 'fluid flow'),
                        ('deformation', 'deformation')):
         if bool(getattr(p, flag, False)):
@@ -61,6 +82,41 @@ def unsupported_features(sim, phase, assume_no_events=False, precision='fp64'):
         if getattr(p, 'dynamic_noise', 0) == 1 and ions.get('P', 0) == 1:
             reasons.append('dynamic protein noise (dynamic_noise)')
     return reasons
+
+
+def _network_core(sim, p):
+    """The MasterOfNetworks the loop steps (sim.molecules.core or
+    sim.grn.core), or None."""
+    if bool(getattr(p, 'molecules_enabled', False)):
+        return sim.molecules.core
+    if bool(getattr(p, 'grn_enabled', False)):
+        return sim.grn.core
+    return None
+
+
+def _network_upload(net, core, M):
+    mols = list(core.molecules.values())
+    net.upload(np.stack([np.asarray(m.c_cells, np.float64) for m in mols]),
+               np.stack([np.asarray(m.cc_at_mem, np.float64) for m in mols]),
+               np.stack([np.asarray(m.c_env, np.float64) * np.ones(M) for m in mols]))
+
+
+def _network_mirror(sim, core, net, M):
+    """Write the substances back on BETSE's objects (Molecule.c_cells,
+    cc_at_mem, c_env as the uniform length-M vector, f_mem, f_gj;
+    MasterOfNetworks.reaction_rates) and let BETSE's own energy_charge
+    (networks.py:3996-4013) refresh chi from them."""
+    st = net.download()
+    fl = net.fluxes()
+    for k, m in enumerate(core.molecules.values()):
+        m.c_cells = st['c_cells'][k].copy()
+        m.cc_at_mem = st['cc_at_mem'][k].copy()
+        m.c_env = np.full(M, st['c_env'][k])
+        m.f_mem = fl['f_mem'][k].copy()
+        m.f_gj = fl['f_gj'][k].copy()
+    core.reaction_rates = fl['reaction_rates'] if len(core.reactions) else np.asarray([])
+    if hasattr(core, 'energy_charge'):
+        core.energy_charge(sim)
 
 
 def _grid_shape(cells):
@@ -120,6 +176,8 @@ def run_sim_core_loop(sim, phase, time_steps, time_steps_sampled, anim_cells=Non
     n = len(time_steps)
     if n == 0:
         return
+    core = _network_core(sim, p)
+    spec = NetworkSpec.from_betse(core, cells, p, sim) if core is not None else None
     geom = ClusterGeometry.from_cells(cells, sim=sim, p=p)
     params = StepParams.from_betse(p, sim)
     lap = getattr(cells, 'lapENVinv', None) if fields else None
@@ -147,25 +205,40 @@ def run_sim_core_loop(sim, phase, time_steps, time_steps_sampled, anim_cells=Non
             eng.autotune()
         elif launch_config is not None:
             eng.set_launch_config(*launch_config)
+        net = None
+        if spec is not None:
+            net = Network(eng, spec)
+            _network_upload(net, core, eng.M)
         sampled = {k for k, t in enumerate(time_steps) if t in time_steps_sampled}
         # the first step runs alone so the solver-time estimate sees one step
         stops = sorted(sampled | {0, n - 1})
         done = 0
         loop_measure = time.time()
-        for k in stops:
-            eng.step(k + 1 - done, outputs=True)
-            done = k + 1
-            eng.check_stable()  # check_v: BetseSimUnstableException on NaN
-            if k in sampled or k == n - 1:
-                _mirror(sim, cells, eng, lap is not None, D_env_weight)
-            if k in sampled:
-                t = time_steps[k]
-                phase.callbacks.progressed_next()
-                sim.write2storage(t, cells, p)
-                if anim_cells is not None:
-                    anim_cells.plot_frame(time_step=-1)
-            if k == 0 and hasattr(sim, '_log_solver_time_estimate'):
-                sim._log_solver_time_estimate(phase=phase, step_first_time=loop_measure)
+        try:
+            for k in stops:
+                if net is not None:
+                    net.step(k + 1 - done, with_ions=True, outputs=True)
+                else:
+                    eng.step(k + 1 - done, outputs=True)
+                done = k + 1
+                eng.check_stable()  # check_v: BetseSimUnstableException on NaN
+                if net is not None:
+                    net.check_stable()   # negative substance concentrations
+                if k in sampled or k == n - 1:
+                    _mirror(sim, cells, eng, lap is not None, D_env_weight)
+                    if net is not None:
+                        _network_mirror(sim, core, net, eng.M)
+                if k in sampled:
+                    t = time_steps[k]
+                    phase.callbacks.progressed_next()
+                    sim.write2storage(t, cells, p)
+                    if anim_cells is not None:
+                        anim_cells.plot_frame(time_step=-1)
+                if k == 0 and hasattr(sim, '_log_solver_time_estimate'):
+                    sim._log_solver_time_estimate(phase=phase, step_first_time=loop_measure)
+        finally:
+            if net is not None:
+                net.close()
 
 
 def install(simulator_cls=None, **options):

@@ -46,6 +46,10 @@
  *   bx_dense_apply      np.dot(cells.lapENVinv, .) / np.dot(cells.lapGJinv, .)
  *                       (ion_current.py:90,170; sim_toolbox.py:1263,1284;
  *                       physics/pressures.py:59).
+ *   bx_network_*        MasterOfNetworks (chemistry/networks.py): tissue_init
+ *                       / read_reactions tables (:307-657, 814-922) and
+ *                       run_loop (:2805-2983), called from sim.py:1290-1319
+ *                       and gene.py:220-308.
  */
 #ifndef BX_H
 #define BX_H
@@ -505,10 +509,13 @@ int bx_network_download(bx_network_handle n, double* c_cells, double* cc_at_mem,
  * (bx_step) followed by the network step in BETSE's order -- the network
  * reads Vmem from the start of the step and the gap-junction state that
  * step leaves; with_ions = 0: the network alone on the cluster's current
- * Vmem and gap-junction state (gene.py:220-308).  want_fluxes = 1 keeps the
- * last step's membrane and gap-junction fluxes for bx_network_fluxes. */
-int bx_network_step(bx_network_handle n, int n_steps, int with_ions, int want_fluxes);
-int bx_network_fluxes(bx_network_handle n, double* f_mem, double* f_gj);   /* [S][M] each */
+ * Vmem and gap-junction state (gene.py:220-308).  want_outputs = 1: the last
+ * step also computes the ion step's outputs (bx_outputs_download) and keeps
+ * the network's fluxes and reaction rates for bx_network_fluxes. */
+int bx_network_step(bx_network_handle n, int n_steps, int with_ions, int want_outputs);
+/* The last output step's Molecule.f_mem and f_gj ([S][M] each) and
+ * MasterOfNetworks.reaction_rates ([R][C]); any pointer may be NULL. */
+int bx_network_fluxes(bx_network_handle n, double* f_mem, double* f_gj, double* rates);
 /* Negative substance concentrations seen since the upload (BETSE raises
  * BetseSimUnstableException on them, sim_toolbox.py:1132-1151,
  * networks.py:5802-5807). */

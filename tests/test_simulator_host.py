@@ -25,8 +25,7 @@ def test_default_electrodiffusion_config_is_supported():
 
 @pytest.mark.parametrize('opt,frag', [
     (dict(Ca_dyn=True), 'endoplasmic reticulum'),
-    (dict(molecules_enabled=True), 'molecules'),
-    (dict(grn_enabled=True), 'gene regulatory'),
+    (dict(molecules_enabled=True, grn_enabled=True), 'gene regulatory'),
     (dict(deform_osmo=True), 'osmotic'),
     (dict(fluid_flow=True), 'fluid flow'),
     (dict(deformation=True), 'deformation'),
@@ -38,6 +37,21 @@ def test_unsupported_options_are_named(opt, frag):
         setattr(ph.p, k, v)
     reasons = simulator.unsupported_features(None, ph)
     assert len(reasons) == 1 and frag in reasons[0]
+
+
+def test_networks_need_the_plain_form_without_ecm():
+    """A general or gene regulatory network steps with the plain FP64 form;
+    the split form, extracellular spaces and network transporters are named."""
+    sim = SimpleNamespace(molecules=SimpleNamespace(transporters=False, channels=False, modulators=False),
+                          grn=SimpleNamespace(transporters=True, channels=False, modulators=False))
+    for flag in ('molecules_enabled', 'grn_enabled'):
+        ph = _phase(**{flag: True})
+        r = simulator.unsupported_features(sim, ph, precision='fp64')
+        assert r == [] if flag == 'molecules_enabled' else ('network transporters (grn)' in r[0] and len(r) == 1)
+        r = simulator.unsupported_features(sim, ph, precision='split')
+        assert any('split form' in x for x in r)
+        ph.p.is_ecm = True
+        assert any('extracellular' in x for x in simulator.unsupported_features(sim, ph, precision='fp64'))
 
 
 def test_polarizability_needs_the_plain_form():
@@ -71,7 +85,7 @@ def test_install_patches_and_returns_original():
     assert orig(Simulator(), None, None, None, None) == 'cpu'
     assert Simulator._run_sim_core_loop.__wrapped__ is orig
     ph = _phase(grn_enabled=True)
-    with pytest.raises(NotImplementedError, match='gene regulatory'):
+    with pytest.raises(NotImplementedError, match='networks in the split form'):
         Simulator()._run_sim_core_loop(ph, np.arange(2), set(), None)
 
 
