@@ -281,6 +281,119 @@ def init_time_to_steady(n_clusters=256, n_cells=5000):
             'cold': r['cold'], 'warm': w}
 
 
+# A four-substance network in BETSE's configuration format ('general network'
+# -> 'biomolecules', 'reactions'): gene products with Hill activation and
+# inhibition, a charged substance crossing the membrane and gap junctions, a
+# neutral one with intracellular transport, two cell-zone reactions.
+def _bench_substance(name, z, Dm, Dgj, env, cell, gad, ui=False, gj_imp=False):
+    return {'name': name, 'Dm': Dm, 'Do': 1.0e-11, 'Dgj': Dgj, 'z': z, 'env conc': env, 'cell conc': cell,
+            'update intracellular': ui, 'use time dilation': False, 'TJ permeable': False,
+            'GJ impermeable': gj_imp, 'TJ factor': 1.0, 'growth and decay': gad,
+            'plotting': {'plot 2D': False, 'animate': False}}
+
+
+def _bench_gad(prod, decay, acts=None, inhs=None, apply_to='all', mod='None'):
+    a = acts or ([], [], [])
+    i = inhs or ([], [], [])
+    return {'production rate': prod, 'decay rate': decay, 'apply to': apply_to, 'modulator function': mod,
+            'activators': a[0] or 'None', 'Km activators': a[1] or 'None', 'n activators': a[2] or 'None',
+            'inhibitors': i[0] or 'None', 'Km inhibitors': i[1] or 'None', 'n inhibitors': i[2] or 'None'}
+
+
+BENCH_NETWORK = dict(
+    substances=[
+        _bench_substance('g1', 0, 0.0, 1e-15, 0.0, 0.1, _bench_gad(0.5, 0.2, inhs=(['g3'], [0.3], [2.0]),
+                                                                    mod='gradient_x')),
+        _bench_substance('g2', 0, 0.0, 1e-15, 0.0, 0.05, _bench_gad(1.0, 0.5, acts=(['g1', 'g3!'], [0.2, 0.5],
+                                                                                     [2.0, 1.0]),
+                                                                     apply_to=['spot']), gj_imp=True),
+        _bench_substance('g3', -1, 1e-18, 1e-14, 0.5, 0.2, _bench_gad(0.2, 0.1, acts=(['g2'], [0.1], [1.0]))),
+        _bench_substance('g4', 0, 5e-19, 1e-15, 1.0, 0.1, _bench_gad(0.05, 0.05, inhs=(['g3'], [0.4], [1.0])),
+                         ui=True),
+    ],
+    reactions=[
+        {'name': 'r1', 'reaction zone': 'cell', 'reactants': ['g1', 'g3'], 'reactant multipliers': [1, 1],
+         'Km reactants': [0.1, 0.2], 'products': ['g4'], 'product multipliers': [1], 'Km products': [0.5],
+         'max rate': 0.01, 'standard free energy': 'None', 'reaction activators': ['g2'], 'activator Km': [0.1],
+         'activator n': [2.0]},
+        {'name': 'r2', 'reaction zone': 'cell', 'reactants': ['g4'], 'reactant multipliers': [1],
+         'Km reactants': [0.3], 'products': ['g2'], 'product multipliers': [2], 'Km products': [0.4],
+         'max rate': 0.02, 'standard free energy': -5000.0},
+    ])
+
+
+def network_step(g, p, Dm, st, stream, flush, n_steps=200, cpu=True):
+    """The molecule / gene-regulatory-network step (MasterOfNetworks.run_loop)
+    with the plain FP64 ion step on the headline cluster: the network kernels
+    alone and the coupled step, ms per time step (CUDA events), and the
+    network kernels' roofline on their algorithmic bytes."""
+    from betse_gb300.engine import ClusterEngine
+    from betse_gb300.network import Network, NetworkSpec
+    C, M = g.n_cells, g.n_mems
+    rng = np.random.default_rng(17)
+    spot = np.sort(rng.choice(C, size=C // 3, replace=False))
+    gmod = rng.uniform(0.2, 1.2, size=C)
+    R_rads = np.asarray(g.R_rads)
+    mem_vol = 0.5 * R_rads * np.asarray(g.mem_sa)
+    spec = NetworkSpec.from_config(BENCH_NETWORK['substances'], BENCH_NETWORK['reactions'], 1.0, n_cells=C,
+                                   profiles={'spot': spot}, growth_mod={'g1': gmod}, ion_names=p.ion_names,
+                                   mem_vol=mem_vol, R_rads=R_rads)
+    out = {'workload': f'4-substance network (2 cell-zone reactions, Hill activators and inhibitors) on the '
+                       f'{C}-cell / {M}-membrane cluster, plain FP64 ion step',
+           'substances': 4, 'reactions': 2, 'unit': 'ms per time step'}
+    with ClusterEngine(g, p, 'fp64') as eng:
+        eng.set_membrane_diffusivity(Dm)
+        eng.upload(**st)
+        with Network(eng, spec) as net:
+            net.upload_initial()
+            net.step(2 * 32 + 3, with_ions=True)     # warm-up, graphs captured
+            flush.fill_(1)
+            torch_sync()
+            ms_net = net.time_step(n_steps, with_ions=False)
+            flush.fill_(1)
+            torch_sync()
+            ms_both = net.time_step(n_steps, with_ions=True)
+            net.check_stable()
+            eng.check_stable()
+            nbytes = net.algorithmic_bytes()
+    out.update({'ms_network_alone': ms_net, 'ms_with_ion_step': ms_both,
+                'cell_substance_updates_per_s': C * 4 / (ms_net / 1e3),
+                'roofline': roofline_entry(nbytes, ms_net / 1e3, 'k_net_cell + k_net_gj',
+                                           note='algorithmic bytes of one network step (both kernels; '
+                                                'Network.algorithmic_bytes) / its time per step, network alone')})
+    if cpu:
+        out['cpu_baseline'] = cpu_baseline_network(g, p, Dm, st, spec_args=(spot, gmod, mem_vol, R_rads))
+    return out
+
+
+def torch_sync():
+    import torch
+    torch.cuda.synchronize()
+
+
+def cpu_baseline_network(g, p, Dm, st, spec_args, budget_s=8.0):
+    """The network oracle (oracle/network.py, NumPy, one thread) on the same
+    cluster with Vmem frozen, a bounded number of steps."""
+    from oracle.adapt import from_workload
+    from oracle.network import Network as OracleNetwork
+    spot, gmod, mem_vol, R_rads = spec_args
+    og, op, os_ = from_workload(g, p, Dm, st)
+    og.R_rads = R_rads
+    onet = OracleNetwork(BENCH_NETWORK['substances'], BENCH_NETWORK['reactions'], og, op, mem_vol, 1.0,
+                         {'g2': spot}, {'g1': gmod})
+    ost = onet.initial_state()
+    vm = os_.vm
+    vgj = vm[og.nn_i] - vm
+    gjo = op.gj_block * og.gj_weight
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s or n < 2:
+        onet.step(ost, vm, vgj, gjo, op.gj_block)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {'value': 1e3 * dt / n, 'unit': 'ms per time step', 'cores': 1, 'kind': 'port',
+            'sample': f'{n} network-alone steps of the full cluster, oracle/network.py (NumPy, one thread)'}
+
+
 def batch_fields_timing(n_clusters=128):
     """Environment fields of a sweep at a sampled step: one tensor-core GEMM per
     grid shape for all clusters (host wall time of bx_batch_env_fields, the
@@ -530,10 +643,30 @@ def profile_kernel(which):
     """One small launch sequence of a dense-product kernel for ncu captures:
     'gemm' -- k_gemm_bf16x3 on an 8192 x 8192 operator with 1024 right-hand
     sides (two warm-up launches, then the captured one); 'fields' --
-    k_dense_rows2_df on a 12000 x 12000 double-float operator."""
+    k_dense_rows2_df on a 12000 x 12000 double-float operator; 'network' --
+    the four-substance network alone on the 100k-cell cluster (three warm-up
+    steps, then k_net_cell and k_net_gj once each)."""
     from betse_gb300.build import build
     build()
-    if which == 'gemm':
+    if which == 'network':
+        from betse_gb300.engine import ClusterEngine
+        from betse_gb300.network import Network, NetworkSpec
+        w, g, p, Dm, st, _ = build_workload('cluster100k')
+        C = g.n_cells
+        rng = np.random.default_rng(17)
+        R_rads = np.asarray(g.R_rads)
+        spec = NetworkSpec.from_config(BENCH_NETWORK['substances'], BENCH_NETWORK['reactions'], 1.0, n_cells=C,
+                                       profiles={'spot': np.sort(rng.choice(C, size=C // 3, replace=False))},
+                                       growth_mod={'g1': rng.uniform(0.2, 1.2, size=C)}, ion_names=p.ion_names,
+                                       mem_vol=0.5 * R_rads * np.asarray(g.mem_sa), R_rads=R_rads)
+        with ClusterEngine(g, p, 'fp64') as eng:
+            eng.set_membrane_diffusivity(Dm)
+            eng.upload(**st)
+            with Network(eng, spec) as net:
+                net.upload_initial()
+                net.step(4, with_ions=False)
+                net.check_stable()
+    elif which == 'gemm':
         from betse_gb300.dense import DenseOperator
         n = 8192
         A = np.empty((n, n))
@@ -610,7 +743,7 @@ def main():
     ap.add_argument('--launch', default=None,
                     help='with --profile-run: membrane slots per tile, suffix p persistent, f factored, '
                          'r resident kernel (e.g. 192r)')
-    ap.add_argument('--profile-kernel', choices=['gemm', 'fields'],
+    ap.add_argument('--profile-kernel', choices=['gemm', 'fields', 'network'],
                     help='for ncu: run a small case of one dense-product kernel and exit')
     args = ap.parse_args()
     if args.profile_kernel:
@@ -788,6 +921,7 @@ def main():
                    'warm_start': init_time_to_steady()}
         extra = dense_products(stream, flush, others['ecm20k'])
         extra['batch_env_fields'] = batch_fields_timing()
+        extra['network'] = network_step(g, p, Dm, st, stream, flush, cpu=cpu_on)
 
     if rank == 0:
         line = {

@@ -2786,6 +2786,29 @@ int bx_network_step(bx_network_handle n, int n_steps, int with_ions, int want_ou
   return BX_OK;
 }
 
+int bx_network_time_step(bx_network_handle n, int n_steps, int with_ions, double* ms_per_step) {
+  if (!n || !ms_per_step || n_steps <= 0) return fail(BX_EINVAL, "bad argument");
+  cudaStream_t s = n->h->stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  BX_CU(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(BX_ECUDA, "cudaEventCreate");
+  }
+  cudaEventRecord(e0, s);
+  const int rc = bx_network_step(n, n_steps, with_ions, 0);
+  cudaEventRecord(e1, s);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != BX_OK) return rc;
+  if (e != cudaSuccess) return fail(BX_ECUDA, cudaGetErrorString(e));
+  *ms_per_step = (double)ms / n_steps;
+  return BX_OK;
+}
+
 int bx_network_status(bx_network_handle n, int64_t* negative) {
   if (!n || !negative) return fail(BX_EINVAL, "null argument");
   unsigned long long v = 0;

@@ -240,7 +240,7 @@ def make_cluster(radius, seed, d_cell=10e-6, disorder=0.4, cell_height=1e-5,
         mem_sa=mem_sa, mem_nx=nx, mem_ny=ny, gj_weight=np.ones(M), cell_vol=cell_vol,
         cell_sa=cell_sa, diviterm=diviterm, grid_shape=(gny, gnx), delta=delta,
         gj_len=cell_space, smooth_cells=smooth_cells, mem_sa_per_env=msa_env,
-        D_env_weight=np.ones(gnx * gny), cell_nn_ptr=cnn_ptr, cell_nn=dst)
+        D_env_weight=np.ones(gnx * gny), cell_nn_ptr=cnn_ptr, cell_nn=dst, R_rads=R_rads)
     return GeneratedCluster(geom=geom, cell_centres=poly_c, mem_mids=mids,
                             xmin=xmin, xmax=xmax, ymin=ymin, ymax=ymax, world=wsx)
 

@@ -423,6 +423,30 @@ class Network:
                                               rr.ctypes.data if rr.size else None), 'bx_network_fluxes')
         return {'f_mem': fm, 'f_gj': fg, 'reaction_rates': rr}
 
+    def time_step(self, n_steps, with_ions=True):
+        """ms per time step of ``n_steps`` steps, timed with CUDA events on the
+        cluster's stream (the state advances)."""
+        v = ct.c_double()
+        _lib.check(self.lib.bx_network_time_step(self.h, int(n_steps), int(bool(with_ions)), ct.byref(v)),
+                   'bx_network_time_step')
+        return float(v.value)
+
+    def algorithmic_bytes(self):
+        """Bytes one network step (both kernels) moves, each array once at
+        its stored width: per cell the concentrations in and out of both
+        kernels (16 S each), the CSR pointer and volume; per membrane Vmem,
+        mem_sa, the partner maps, boundary flag and gap-junction weight; per
+        membrane and substance the cc_at_mem write, and for 'update
+        intracellular' substances the membrane values in, mid out and in, and
+        gamma / R_rads; growth modulation and target rows per cell."""
+        S, C, M = self.S, self.C, self.M
+        n_ui = sum(r['update_intra'] for r in self.spec.subs)
+        rows = sum(r['growth_mod'] is not None for r in self.spec.subs) * 8 + \
+            sum(r['growth_target'] is not None for r in self.spec.subs)
+        cell = C * (2 * 16 * S + 2 * 12) + C * rows
+        mem = M * (8 + 8 + 4 + 4 + 1 + 8) + M * 8 * S + n_ui * M * (8 + 8 + 8 + 8 + 8)
+        return int(cell + mem)
+
     def negative_count(self):
         v = ct.c_int64()
         _lib.check(self.lib.bx_network_status(self.h, ct.byref(v)), 'bx_network_status')

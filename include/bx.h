@@ -520,6 +520,9 @@ int bx_network_fluxes(bx_network_handle n, double* f_mem, double* f_gj, double* 
  * BetseSimUnstableException on them, sim_toolbox.py:1132-1151,
  * networks.py:5802-5807). */
 int bx_network_status(bx_network_handle n, int64_t* negative);
+/* Runs bx_network_step(n, n_steps, with_ions, 0) between two CUDA events on
+ * the cluster's stream; reports ms per time step (the state advances). */
+int bx_network_time_step(bx_network_handle n, int n_steps, int with_ions, double* ms_per_step);
 int bx_network_destroy(bx_network_handle n);
 
 #ifdef __cplusplus

@@ -108,8 +108,8 @@ def test_network_generated_cluster_matches_oracle():
     rng = np.random.default_rng(7)
     spot = np.sort(rng.choice(C, size=C // 3, replace=False))
     gmod = rng.uniform(0.2, 1.2, size=C)
-    mem_vol = geom.mem_sa * 2.0e-6 / 3.0
-    R_rads = rng.uniform(3e-6, 6e-6, size=M)
+    R_rads = np.asarray(geom.R_rads)
+    mem_vol = 0.5 * R_rads * geom.mem_sa          # cells.py:1382
     spec = NetworkSpec.from_config(cfg['substances'], cfg['reactions'], cfg['time_dilation'], n_cells=C,
                                    profiles={'spot': spot}, growth_mod={'A': gmod}, ion_names=params.ion_names,
                                    mem_vol=mem_vol, R_rads=R_rads)
