@@ -82,7 +82,8 @@ struct bx_cluster {
   int nblk = 0;
   int tpb = kTPB;                  // membrane slots per CTA (autotuned)
   int kind = KIND_TILE;            // split form: tile, persistent, factored or resident kernel (autotuned)
-  int fact_unroll = 4;             // factored kernel: gap junctions loaded per round (2 or 4, autotuned)
+  int fact_unroll = 4;             // factored kernel: gap junctions loaded per round (2 or 4; +10 with the
+                                   // first entries prefetched before the dependency wait), autotuned
   double tune_ms = -1.0;           // ms per step of the configuration the last autotune chose
   int sm_count = 0;
   bool ecm = false;
@@ -539,13 +540,13 @@ cudaError_t launch_persist_t(bx_cluster* h, int parity, cudaStream_t s) {
 
 // the factored step: 8 tiles (warps) per CTA
 constexpr int kFactWarps = 8;
-template <int U>
+template <int U, int PF>
 cudaError_t launch_fact_u(bx_cluster* h, int parity, cudaStream_t s) {
   const unsigned grid = (unsigned)((h->nblk + kFactWarps - 1) / kFactWarps);
   if (is_betse_six_ions(h))
-    return launch_pdl(bx::k_split_fact<kFactWarps, 1, U>, grid, kFactWarps * 32, s, fact_geom(h),
+    return launch_pdl(bx::k_split_fact<kFactWarps, 1, U, PF>, grid, kFactWarps * 32, s, fact_geom(h),
                       split_ptrs(h, parity), make_split_const(h));
-  return launch_pdl(bx::k_split_fact<kFactWarps, 0, U>, grid, kFactWarps * 32, s, fact_geom(h),
+  return launch_pdl(bx::k_split_fact<kFactWarps, 0, U, PF>, grid, kFactWarps * 32, s, fact_geom(h),
                     split_ptrs(h, parity), make_split_const(h));
 }
 
@@ -573,7 +574,14 @@ cudaError_t launch_fact_pipe_t(bx_cluster* h, int parity, cudaStream_t s) {
 cudaError_t launch_fact(bx_cluster* h, int parity, cudaStream_t s) {
   if (h->kind == KIND_FACT_PIPE)
     return is_betse_six_ions(h) ? launch_fact_pipe_t<1>(h, parity, s) : launch_fact_pipe_t<0>(h, parity, s);
-  return h->fact_unroll == 2 ? launch_fact_u<2>(h, parity, s) : launch_fact_u<4>(h, parity, s);
+  // fact_unroll: gap junctions per load round (2, 4); +10 with the first
+  // entries prefetched before the grid dependency wait (6 for 2, 8 for 4)
+  switch (h->fact_unroll) {
+    case 2: return launch_fact_u<2, 0>(h, parity, s);
+    case 12: return launch_fact_u<2, 6>(h, parity, s);
+    case 14: return launch_fact_u<4, 8>(h, parity, s);
+    default: return launch_fact_u<4, 0>(h, parity, s);
+  }
 }
 
 void drop_resident(bx_cluster* h) {
@@ -1860,7 +1868,11 @@ int bx_set_launch_config(bx_handle h, int tpb, int kernel) {
   if (!h) return fail(BX_EINVAL, "null handle");
   const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256) : (tpb == 128 || tpb == 256);
   if (!ok) return fail(BX_EINVAL, "unsupported CTA size for this form");
+  const int variant = (kernel >> 8) & 0xff;
+  kernel &= 0xff;
   if (kernel < KIND_TILE || kernel > KIND_FACT_PIPE) return fail(BX_EINVAL, "kernel must be 0 to 4");
+  if (variant && !(variant == 2 || variant == 4 || variant == 12 || variant == 14))
+    return fail(BX_EINVAL, "factored-kernel variant must be 2, 4, 12 or 14");
   if (kernel != KIND_TILE && h->mode != MODE_SPLIT)
     return fail(BX_EINVAL, "the persistent, factored and resident kernels are the split form's");
   if (kernel != KIND_TILE && h->ecm) return fail(BX_EINVAL, "only the tile kernel has an extracellular-space variant");
@@ -1878,6 +1890,7 @@ int bx_set_launch_config(bx_handle h, int tpb, int kernel) {
   if (had_state && (rc = bx_state_download(h, &sv)) != BX_OK) return rc;
   if ((rc = build_partition(h, tpb)) != BX_OK) return rc;
   h->kind = kernel;
+  if (variant) h->fact_unroll = variant;
   h->graph_valid = false;
   if (had_state && (rc = bx_state_upload(h, &sv)) != BX_OK) return rc;
   return BX_OK;
@@ -1954,6 +1967,7 @@ int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* 
   else if (h->mode == MODE_SPLIT)
     cands = {{256, KIND_TILE, 4},     {192, KIND_TILE, 4},     {256, KIND_PERSIST, 4}, {192, KIND_PERSIST, 4},
              {256, KIND_FACT, 4},     {192, KIND_FACT, 4},     {256, KIND_FACT, 2},    {192, KIND_FACT, 2},
+             {256, KIND_FACT, 12},    {192, KIND_FACT, 12},    {256, KIND_FACT, 14},   {192, KIND_FACT, 14},
              {256, KIND_FACT_PIPE, 4}, {192, KIND_FACT_PIPE, 4},
              {256, KIND_RESIDENT, 4}, {192, KIND_RESIDENT, 4}};
   else cands = {{256, KIND_TILE, 4}, {128, KIND_TILE, 4}};
@@ -2450,7 +2464,7 @@ struct bx_network {
   int S = 0, R = 0, nblk = 0;
   bool any_ui = false, have_state = false, have_fluxes = false;
   bx::NetTables* d_tab = nullptr;
-  double *d_gamma = nullptr, *d_Rr = nullptr, *d_gmod = nullptr, *d_cc = nullptr, *d_cm = nullptr,
+  double *d_gamma = nullptr, *d_Rr = nullptr /* gamma / R_rads */, *d_gmod = nullptr, *d_cc = nullptr, *d_cm = nullptr,
          *d_cmid = nullptr, *d_cmmid = nullptr, *d_env = nullptr, *d_part = nullptr, *d_fmem = nullptr,
          *d_fgj = nullptr, *d_rates = nullptr;
   uint8_t* d_gmask = nullptr;
@@ -2496,14 +2510,14 @@ bx::NetArgs net_args(bx_network* n, int vm_parity) {
   bx_cluster* h = n->h;
   bx::NetArgs a{};
   a.C = h->C; a.M = h->M;
-  a.dt = h->par.dt; a.tm = h->par.tm; a.F_RT = h->par.F / (h->par.R * h->par.T);
-  a.gj_len = h->gj_len; a.gj_block = h->par.gj_block;
+  a.dt = h->par.dt; a.inv_tm = 1.0 / h->par.tm; a.F_RT = h->par.F / (h->par.R * h->par.T);
+  a.inv_gj_len = 1.0 / h->gj_len; a.gj_block = h->par.gj_block;
   a.inv_vol_env_M = 1.0 / (h->par.vol_env * (double)h->M);
   a.cell_ptr = h->d_cell_ptr; a.nn = h->d_nn; a.nn_cell = h->d_nn_cell; a.bflag = h->d_bflag;
   a.mem_sa = h->d_mem_sa; a.cell_vol = h->d_cell_vol; a.gj_w = h->d_gj_w;
   a.gjo = h->vgj ? h->d_gjo : nullptr;
   a.vm = h->d_vm[vm_parity];
-  a.tab = n->d_tab; a.gamma = n->d_gamma; a.R_rads = n->d_Rr; a.gmod = n->d_gmod; a.gmask = n->d_gmask;
+  a.tab = n->d_tab; a.gamma = n->d_gamma; a.g_over_r = n->d_Rr; a.gmod = n->d_gmod; a.gmask = n->d_gmask;
   a.c_cells = n->d_cc; a.cmem = n->d_cm; a.c_mid = n->d_cmid; a.cmem_mid = n->d_cmmid; a.env = n->d_env;
   a.env_part = n->d_part; a.f_mem = n->d_fmem; a.f_gj = n->d_fgj; a.rates = n->d_rates; a.neg = n->d_neg;
   a.nblk = n->nblk;
@@ -2657,7 +2671,7 @@ int bx_network_create(bx_handle h, const bx_net_spec* sp, bx_network_handle* out
       const double mv = sp->mem_vol[m];
       if (!(mv > 0.0) || !(sp->R_rads[m] > 0.0)) return fail(BX_EINVAL, "mem_vol and R_rads must be > 0");
       gam[m] = msa[m] / ((3.0 / 4.0) * mv);
-      rr[m] = sp->R_rads[m];
+      rr[m] = gam[m] / sp->R_rads[m];
     }
     if (dalloc(&n->d_gamma, M) != cudaSuccess || dalloc(&n->d_Rr, M) != cudaSuccess)
       return fail(BX_ENOMEM, "network allocation");

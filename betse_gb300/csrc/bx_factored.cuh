@@ -194,9 +194,13 @@ __device__ __forceinline__ float warp_sum_down(float v) {
 // k_split_env of the previous step; the static data is read before the
 // dependency wait.
 // ---------------------------------------------------------------------------
-template <int NW, int ZP, int U>
+// PF > 0: the first PF gap-junction entries of each cell (static data) are
+// loaded before the grid dependency wait, so after it each round of U
+// junctions waits for the partner records only, not for the entry first.
+template <int NW, int ZP, int U, int PF>
 __global__ void __launch_bounds__(NW * 32)
 k_split_fact(FactGeom fg, SplitPtrs p, SplitConst k) {
+  static_assert(PF % U == 0, "prefetched entries come in whole rounds");
   using IS = IonSet<ZP>;
   constexpr int NI = IS::NI;
   const int I = IS::n(k);
@@ -222,6 +226,9 @@ k_split_fact(FactGeom fg, SplitPtrs p, SplitConst k) {
   }
   const int gcnt = __float_as_int(cs.w);
   const bool live = tile_ok && gcnt >= 0;
+  int2 pf[PF > 0 ? PF : 1];
+#pragma unroll
+  for (int u = 0; u < PF; ++u) pf[u] = (live && u < gcnt) ? fg.gj[gb + u] : make_int2(s, 0);
 
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
   cudaGridDependencySynchronize();
@@ -243,7 +250,21 @@ k_split_fact(FactGeom fg, SplitPtrs p, SplitConst k) {
     const float pc = p.pump_coef[cl];
     const float v1 = own[7] + 1.0e-25f;
     const int2* e = fg.gj + gb;
-    for (int j = 0; j < gcnt; j += U) {
+#pragma unroll
+    for (int j = 0; j < PF; j += U) {
+      if (j >= gcnt) break;
+      float4 r0[U], r1[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float4* r4 = reinterpret_cast<const float4*>(p.rec_in + (size_t)pf[j + u].x * 8);
+        r0[u] = r4[0];
+        r1[u] = r4[1];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (j + u < gcnt) fact_gj_add<ZP, NI>(k, I, v1, cin, r0[u], r1[u], __int_as_float(pf[j + u].y), s2);
+    }
+    for (int j = PF; j < gcnt; j += U) {
       int2 en[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) en[u] = (j + u < gcnt) ? e[j + u] : make_int2(s, 0);

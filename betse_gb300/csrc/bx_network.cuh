@@ -74,7 +74,7 @@ struct NetTables {
 
 struct NetArgs {
   int C, M;
-  double dt, tm, F_RT, gj_len, gj_block, inv_vol_env_M;
+  double dt, inv_tm, F_RT, inv_gj_len, gj_block, inv_vol_env_M;
   // cluster geometry and state (the handle's arrays)
   const int* cell_ptr;
   const int* nn;
@@ -88,7 +88,7 @@ struct NetArgs {
   // network
   const NetTables* tab;
   const double* gamma;       // [M] mem_sa / ((3/4) mem_vol)
-  const double* R_rads;      // [M]
+  const double* g_over_r;    // [M] gamma / R_rads
   const double* gmod;        // [rows][C]
   const uint8_t* gmask;      // [rows][C]
   double* c_cells;           // [S][C]
@@ -104,13 +104,30 @@ struct NetArgs {
   int nblk;
 };
 
-// sim_toolbox.electroflux (sim_toolbox.py:18-69) for a general charge, FP64.
-__device__ __forceinline__ double net_ghk(double cA, double cB, double Dc, double d, double z, double v,
+// sim_toolbox.electroflux (sim_toolbox.py:18-69) for a general charge, FP64,
+// with the FP64 transcendentals only where they carry information (the
+// GPU's FP64 pipe bounds these kernels):
+//   |a| < 1e-17 (every neutral substance: a = 1e-25 v F/RT): exp(-a) rounds
+//     to 1 and expm1(-a) to -a, in FP64 as in NumPy, so the flux is
+//     -(Dc/d)(cB - cA) (a few ulp from BETSE's order of operations);
+//   |a| > 1e-3: -expm1(-a) = 1 - exp(-a) to within 1e-13 relative;
+//   otherwise both functions.
+__device__ __forceinline__ double net_ghk(double cA, double cB, double Dc, double inv_d, double z, double v,
                                           double F_RT) {
   const double a = ((z + kNonce) * (v + kNonce)) * F_RT;
+  const double aa = fabs(a);
+  if (aa < 1.0e-17) return -(Dc * inv_d) * (cB - cA);
   const double ea = exp(-a);
-  const double den = -expm1(-a);
-  return -((Dc * a) / d) * ((cB - cA * ea) / den);
+  const double den = aa > 1.0e-3 ? 1.0 - ea : -expm1(-a);
+  return -((Dc * a) * inv_d) * ((cB - cA * ea) / den);
+}
+
+// (c/Km)^n: BETSE's '**' (C pow); exponents 1 and 2 by multiplication (the
+// same value as a correctly rounded pow), others by pow.
+__device__ __forceinline__ double net_pow(double x, double n) {
+  if (n == 1.0) return x;
+  if (n == 2.0) return x * x;
+  return pow(x, n);
 }
 
 __device__ __forceinline__ double net_conc(const NetTermD& t, const double* cs, const double* env) {
@@ -130,19 +147,19 @@ __device__ double net_factor(const NetTables& tb, int t0, int nt, const double* 
     const double c = net_conc(t, cs, env);
     switch (t.kind) {
       case NT_ACT: {
-        const double x = pow(c / t.km, t.n);
+        const double x = net_pow(c / t.km, t.n);
         const double h = x / (1.0 + x);
         act = any_mult ? act * h : h;
         any_mult = true;
         break;
       }
       case NT_ACT_INDEP: {
-        const double x = pow(c / t.km, t.n);
+        const double x = net_pow(c / t.km, t.n);
         act = act + x / (1.0 + x);
         break;
       }
       case NT_INH: {
-        const double h = 1.0 / (1.0 + pow(c / t.km, t.n));
+        const double h = 1.0 / (1.0 + net_pow(c / t.km, t.n));
         inh = any_inh ? inh * h : h;
         any_inh = true;
         break;
@@ -216,7 +233,7 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
       if (rx.keq == 0.0) {
         double fwd = 1.0;
         for (int q = 0; q < rx.nr; ++q) {
-          const double x = pow(cs[rx.r[q]] / rx.rkm[q], rx.rc[q]);
+          const double x = net_pow(cs[rx.r[q]] / rx.rkm[q], rx.rc[q]);
           fwd = q == 0 ? x / (1.0 + x) : fwd * (x / (1.0 + x));
         }
         rate = rx.vmax * al * fwd;
@@ -224,11 +241,11 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
         // BETSE's quotient applies the power before the 1e-3 (networks.py:1364-1396)
         double num = 1.0, den = 1.0;
         for (int q = 0; q < rx.np; ++q) {
-          const double t = 1.0e-3 * pow(cs[rx.p[q]], rx.pc[q]);
+          const double t = 1.0e-3 * net_pow(cs[rx.p[q]], rx.pc[q]);
           num = q == 0 ? t : num * t;
         }
         for (int q = 0; q < rx.nr; ++q) {
-          const double t = 1.0e-3 * pow(cs[rx.r[q]], rx.rc[q]);
+          const double t = 1.0e-3 * net_pow(cs[rx.r[q]], rx.rc[q]);
           den = q == 0 ? t : den * t;
         }
         rate = rx.vmax * al * (1.0 - (num / den) / rx.keq);
@@ -245,14 +262,14 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
         double cm;
         if (sb.ui) {
           // Molecule.update_intra, implicit Euler toward the cell centre
-          // (neutral substance: no field term)
-          const double g = a.gamma[m], dts = a.dt * sb.tdf, rr = a.R_rads[m];
-          cm = ((g * sb.Do * dts * cs[k]) / rr + a.cmem[(size_t)k * a.M + m]) / (1.0 + (g * sb.Do * dts) / rr);
+          // (neutral substance: no field term); kq = gamma Do dt' / R_rads
+          const double kq = a.g_over_r[m] * (sb.Do * (a.dt * sb.tdf));
+          cm = (kq * cs[k] + a.cmem[(size_t)k * a.M + m]) / (1.0 + kq);
           neg += cm < 0.0;
         } else {
           cm = cs[k];
         }
-        const double f = sb.Dm != 0.0 ? net_ghk(env[k], cm, sb.Dm, a.tm, sb.z, a.vm[m], a.F_RT) : 0.0;
+        const double f = sb.Dm != 0.0 ? net_ghk(env[k], cm, sb.Dm, a.inv_tm, sb.z, a.vm[m], a.F_RT) : 0.0;
         const double fa = f * a.mem_sa[m];
         s += fa;
         if (sb.ui) a.cmem_mid[(size_t)k * a.M + m] = cm + f * a.gamma[m] * a.dt;
@@ -290,7 +307,8 @@ __global__ void __launch_bounds__(kNetTPB) k_net_gj(NetArgs a) {
           const double cB = sb.ui ? a.cmem_mid[(size_t)k * a.M + n] : a.c_mid[(size_t)k * a.C + a.nn_cell[m]];
           const double go = a.gjo ? a.gjo[m] : a.gj_block * a.gj_w[m];
           double f = 0.0;
-          if (!a.bflag[m]) f = net_ghk(cA, cB, sb.Dgj * a.gj_block * go, a.gj_len, sb.z, a.vm[n] - a.vm[m], a.F_RT);
+          if (!a.bflag[m])
+            f = net_ghk(cA, cB, sb.Dgj * a.gj_block * go, a.inv_gj_len, sb.z, a.vm[n] - a.vm[m], a.F_RT);
           s += -f * a.mem_sa[m];
           if (sb.ui) {
             const double cm = cA + (-f) * a.gamma[m] * sb.tdf * a.dt;

@@ -227,12 +227,15 @@ class ClusterEngine:
         _lib.check(self.lib.bx_time_cell_kernel(self.h, int(n), ct.byref(ms)), 'bx_time_cell_kernel')
         return ms.value
 
-    def set_launch_config(self, tpb, kernel=0):
+    def set_launch_config(self, tpb, kernel=0, variant=0):
         """Pin the tile size (membrane slots per tile) and, for the split form,
         the kernel: 0/'tile', 1/'persistent' (True), 2/'factored',
-        3/'resident', 4/'pipelined' (factored, persistent); the state is kept."""
+        3/'resident', 4/'pipelined' (factored, persistent); ``variant`` picks
+        the factored kernel's (2 or 4 junctions per load round, +10 with
+        prefetched entries; 0 keeps it). The state is kept."""
         k = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
-        _lib.check(self.lib.bx_set_launch_config(self.h, int(tpb), k), 'bx_set_launch_config')
+        _lib.check(self.lib.bx_set_launch_config(self.h, int(tpb), k | (int(variant) << 8)),
+                   'bx_set_launch_config')
 
     def launch_config(self):
         """(membrane slots per tile, kernel number) in use."""

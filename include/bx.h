@@ -389,6 +389,8 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
  *   4  factored kernel, persistent and software-pipelined: each warp stages
  *      its next tiles' cell data, gap-junction entries and partner records
  *      in shared memory (cp.async) while it computes (results as kernel 2)
+ * Bits 8-15 of kernel, when nonzero, pick the factored kernel's variant (the
+ * third column of bx_autotune_table: 2, 4, 12 or 14).
  * Kernels 1-4 need no extracellular spaces, no voltage-gated gap junctions
  * and no Ca-ATPase; steps with outputs or a nonzero Phi_b always run the
  * tile kernel.  The state is kept.  bx_autotune picks these by timing. */
@@ -405,16 +407,18 @@ int bx_resident_barrier_check(bx_handle h, int64_t timeout_ns, int* timed_out);
 
 /* Autotuner: times n_steps steps (run as bx_step runs them) for each
  * launch configuration -- tile size and, for the split form, the tile,
- * persistent, factored (at two load depths), pipelined factored and
- * resident kernels -- on the
+ * persistent, factored (at two load depths, with and without prefetched
+ * junction entries), pipelined factored and resident kernels -- on the
  * uploaded state, keeps the fastest, and restores the state so the
  * simulation does not advance.
  * Reports the choice and its ms per step (either pointer may be NULL). */
 int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out);
 /* The same search, reporting every candidate it timed: up to max_rows rows of
- * (membrane slots per tile, kernel, gap junctions loaded per round by the
- * factored kernel, ms per step); *n_rows is set to the rows written.  The
- * fastest candidate is kept, as by bx_autotune. */
+ * (membrane slots per tile, kernel, factored-kernel variant, ms per step);
+ * *n_rows is set to the rows written.  The variant is the number of gap
+ * junctions loaded per round (2 or 4), plus 10 when the first entries of each
+ * cell (6 or 8) are loaded before the grid dependency wait.  The fastest
+ * candidate is kept, as by bx_autotune. */
 int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* tpb, int* kernel, int* unroll,
                       double* ms_per_step);
 
