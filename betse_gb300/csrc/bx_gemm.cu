@@ -91,6 +91,19 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                "l"(src), "r"(bytes), "r"(bar)
                : "memory");
 }
+// the same copy with an L2 cache policy (createpolicy)
+__device__ __forceinline__ void bulk_g2s_hint(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar,
+                                              uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;"
+      ::"r"(dst), "l"(src), "r"(bytes), "r"(bar), "l"(policy)
+      : "memory");
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   // start >> 4 [0,14), leading byte offset >> 4 [16,30), stride byte offset >> 4
   // [32,46), descriptor version 1 [46,48), base offset 0, no swizzle
@@ -166,7 +179,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_bf16x3(GemmArgs g) {
   const uint32_t tmem = tmem_base;
 
   if (warp == 0 && lane == 0) {
-    // ---- producer: four 16 KB tiles per K block
+    // ---- producer: four 16 KB tiles per K block.  The right-hand sides (read
+    // by every row block) are marked evict_last so the operator streaming
+    // through L2 does not push them out between row blocks.
+    const uint64_t keep = policy_evict_last();
     int issued = 0;
     for (int kb = 0; kb < Kt; ++kb) {
       const int s = kb % STAGES;
@@ -181,8 +197,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_gemm_bf16x3(GemmArgs g) {
       mbar_expect_tx(fb, STAGE_BYTES);
       bulk_g2s(dst, g.a_hi + ao, TILE_BYTES, fb);
       bulk_g2s(dst + TILE_BYTES, g.a_lo + ao, TILE_BYTES, fb);
-      bulk_g2s(dst + 2 * TILE_BYTES, g.b_hi + bo, TILE_BYTES, fb);
-      bulk_g2s(dst + 3 * TILE_BYTES, g.b_lo + bo, TILE_BYTES, fb);
+      bulk_g2s_hint(dst + 2 * TILE_BYTES, g.b_hi + bo, TILE_BYTES, fb, keep);
+      bulk_g2s_hint(dst + 3 * TILE_BYTES, g.b_lo + bo, TILE_BYTES, fb, keep);
       issued = kb + 1;
     }
     // drain: the last copies of each stage have landed before the CTA can exit

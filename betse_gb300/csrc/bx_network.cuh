@@ -111,14 +111,23 @@ struct NetArgs {
 //     to 1 and expm1(-a) to -a, in FP64 as in NumPy, so the flux is
 //     -(Dc/d)(cB - cA) (a few ulp from BETSE's order of operations);
 //   |a| > 1e-3: -expm1(-a) = 1 - exp(-a) to within 1e-13 relative;
-//   otherwise both functions.
+//   otherwise (small gap-junction voltages) the Taylor series of expm1(-a)
+//   to the fifth power, whose remainder a^6/720 is below 2e-21 |a|.
 __device__ __forceinline__ double net_ghk(double cA, double cB, double Dc, double inv_d, double z, double v,
                                           double F_RT) {
   const double a = ((z + kNonce) * (v + kNonce)) * F_RT;
   const double aa = fabs(a);
   if (aa < 1.0e-17) return -(Dc * inv_d) * (cB - cA);
-  const double ea = exp(-a);
-  const double den = aa > 1.0e-3 ? 1.0 - ea : -expm1(-a);
+  double ea, den;
+  if (aa > 1.0e-3) {
+    ea = exp(-a);
+    den = 1.0 - ea;
+  } else {
+    const double x = -a;
+    const double em1 = x * (1.0 + x * (0.5 + x * (1.0 / 6.0 + x * (1.0 / 24.0 + x * (1.0 / 120.0)))));
+    ea = 1.0 + em1;
+    den = -em1;
+  }
   return -((Dc * a) * inv_d) * ((cB - cA * ea) / den);
 }
 
