@@ -184,6 +184,7 @@ SIGNATURES = {
     'bx_network_fluxes': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     'bx_network_status': (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int64)]),
     'bx_network_destroy': (ct.c_int, [ct.c_void_p]),
+    'bx_network_info': (ct.c_int, [ct.c_void_p, _ip]),
     'bx_network_time_step': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.POINTER(ct.c_double)]),
     'bx_step_fp64_noalloc': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,

@@ -575,11 +575,14 @@ cudaError_t launch_fact(bx_cluster* h, int parity, cudaStream_t s) {
   if (h->kind == KIND_FACT_PIPE)
     return is_betse_six_ions(h) ? launch_fact_pipe_t<1>(h, parity, s) : launch_fact_pipe_t<0>(h, parity, s);
   // fact_unroll: gap junctions per load round (2, 4); +10 with the first
-  // entries prefetched before the grid dependency wait (6 for 2, 8 for 4)
+  // entries prefetched before the grid dependency wait (2, 3, 6 per round
+  // with 6 prefetched; 4 per round with 8)
   switch (h->fact_unroll) {
     case 2: return launch_fact_u<2, 0>(h, parity, s);
     case 12: return launch_fact_u<2, 6>(h, parity, s);
+    case 13: return launch_fact_u<3, 6>(h, parity, s);
     case 14: return launch_fact_u<4, 8>(h, parity, s);
+    case 16: return launch_fact_u<6, 6>(h, parity, s);
     default: return launch_fact_u<4, 0>(h, parity, s);
   }
 }
@@ -1871,8 +1874,8 @@ int bx_set_launch_config(bx_handle h, int tpb, int kernel) {
   const int variant = (kernel >> 8) & 0xff;
   kernel &= 0xff;
   if (kernel < KIND_TILE || kernel > KIND_FACT_PIPE) return fail(BX_EINVAL, "kernel must be 0 to 4");
-  if (variant && !(variant == 2 || variant == 4 || variant == 12 || variant == 14))
-    return fail(BX_EINVAL, "factored-kernel variant must be 2, 4, 12 or 14");
+  if (variant && !(variant == 2 || variant == 4 || variant == 12 || variant == 13 || variant == 14 || variant == 16))
+    return fail(BX_EINVAL, "factored-kernel variant must be 2, 4, 12, 13, 14 or 16");
   if (kernel != KIND_TILE && h->mode != MODE_SPLIT)
     return fail(BX_EINVAL, "the persistent, factored and resident kernels are the split form's");
   if (kernel != KIND_TILE && h->ecm) return fail(BX_EINVAL, "only the tile kernel has an extracellular-space variant");
@@ -1967,7 +1970,8 @@ int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* 
   else if (h->mode == MODE_SPLIT)
     cands = {{256, KIND_TILE, 4},     {192, KIND_TILE, 4},     {256, KIND_PERSIST, 4}, {192, KIND_PERSIST, 4},
              {256, KIND_FACT, 4},     {192, KIND_FACT, 4},     {256, KIND_FACT, 2},    {192, KIND_FACT, 2},
-             {256, KIND_FACT, 12},    {192, KIND_FACT, 12},    {256, KIND_FACT, 14},   {192, KIND_FACT, 14},
+             {256, KIND_FACT, 12},    {192, KIND_FACT, 12},    {256, KIND_FACT, 13},   {192, KIND_FACT, 13},
+             {256, KIND_FACT, 14},    {192, KIND_FACT, 14},    {256, KIND_FACT, 16},   {192, KIND_FACT, 16},
              {256, KIND_FACT_PIPE, 4}, {192, KIND_FACT_PIPE, 4},
              {256, KIND_RESIDENT, 4}, {192, KIND_RESIDENT, 4}};
   else cands = {{256, KIND_TILE, 4}, {128, KIND_TILE, 4}};
@@ -2600,7 +2604,8 @@ int bx_network_create(bx_handle h, const bx_net_spec* sp, bx_network_handle* out
     const bx_net_substance& u = sp->substances[k];
     bx::NetSubD& d = tb->sub[k];
     d.z = u.z; d.Dm = u.Dm; d.Do = u.Do; d.Dgj = u.Dgj; d.tdf = u.time_factor;
-    d.r_prod = u.r_production; d.r_decay = u.r_decay; d.decay_max = u.decay_max; d.gsf = u.gad_scale_factor;
+    d.r_prod = u.r_production; d.r_decay = u.r_decay; d.decay_max = u.decay_max;
+    d.inv_gsf = u.gad_scale_factor != 0.0 ? 1.0 / u.gad_scale_factor : 0.0;
     d.growth = u.growth ? 1 : 0; d.ui = u.update_intra ? 1 : 0; d.gj_imp = u.gj_impermeable ? 1 : 0;
     d.gt0 = u.growth_term0; d.gnt = u.growth_nterm; d.dt0 = u.decay_term0; d.dnt = u.decay_nterm;
     d.mod_row = (u.growth && u.growth_mod) ? mod_rows++ : -1;
@@ -2626,11 +2631,13 @@ int bx_network_create(bx_handle h, const bx_net_spec* sp, bx_network_handle* out
       return fail(BX_EINVAL, "reaction " + std::to_string(j) + ": 1..4 reactants and 0..4 products");
     if (r.keq != 0.0 && r.n_products < 1)
       return fail(BX_EINVAL, "reaction " + std::to_string(j) + ": a standard free energy needs products");
-    d.nr = r.n_reactants; d.np = r.n_products; d.vmax = r.vmax; d.keq = r.keq; d.t0 = r.term0; d.nt = r.nterm;
+    if (r.keq < 0.0 || !std::isfinite(r.keq)) return fail(BX_EINVAL, "reaction keq must be >= 0 and finite");
+    d.nr = r.n_reactants; d.np = r.n_products; d.vmax = r.vmax; d.inv_keq = r.keq > 0.0 ? 1.0 / r.keq : 0.0;
+    d.t0 = r.term0; d.nt = r.nterm;
     for (int q = 0; q < r.n_reactants; ++q) {
       if (r.reactant[q] < 0 || r.reactant[q] >= S) return fail(BX_EINVAL, "reactant names no substance");
       if (!(r.reactant_Km[q] > 0.0)) return fail(BX_EINVAL, "reactant Km must be > 0");
-      d.r[q] = r.reactant[q]; d.rc[q] = r.reactant_coeff[q]; d.rkm[q] = r.reactant_Km[q];
+      d.r[q] = r.reactant[q]; d.rc[q] = r.reactant_coeff[q]; d.inv_rkm[q] = 1.0 / r.reactant_Km[q];
       tb->rm[r.reactant[q]][j] += -r.reactant_coeff[q];
     }
     for (int q = 0; q < r.n_products; ++q) {
@@ -2642,7 +2649,8 @@ int bx_network_create(bx_handle h, const bx_net_spec* sp, bx_network_handle* out
   }
   for (int q = 0; q < sp->n_terms; ++q) {
     const bx_net_term& t = sp->terms[q];
-    tb->term[q] = bx::NetTermD{t.kind, t.substance, t.env_zone ? 1 : 0, 0, t.Km, t.n};
+    tb->term[q] = bx::NetTermD{t.kind, t.substance, t.env_zone ? 1 : 0, 0,
+                               (t.kind == BX_TERM_DIRECT_POS || t.kind == BX_TERM_DIRECT_NEG) ? 0.0 : 1.0 / t.Km, t.n};
   }
   std::unique_ptr<bx_network> n(new bx_network());
   struct Guard {
@@ -2829,6 +2837,12 @@ int bx_network_status(bx_network_handle n, int64_t* negative) {
   BX_CU(cudaStreamSynchronize(n->h->stream));
   BX_CU(cudaMemcpy(&v, n->d_neg, sizeof(v), cudaMemcpyDeviceToHost));
   *negative = (int64_t)v;
+  return BX_OK;
+}
+
+int bx_network_info(bx_network_handle n, int32_t* info) {
+  if (!n || !info) return fail(BX_EINVAL, "null argument");
+  info[0] = n->S; info[1] = n->R; info[2] = n->h->C; info[3] = n->h->M;
   return BX_OK;
 }
 

@@ -48,18 +48,18 @@ enum NetTermKind { NT_ACT = 0, NT_ACT_INDEP = 1, NT_INH = 2, NT_DIRECT_POS = 3, 
 
 struct NetTermD {
   int kind, sub, env, pad;
-  double km, n;
+  double inv_km, n;        // 1 / Km (the host divides once)
 };
 
 struct NetSubD {
-  double z, Dm, Do, Dgj, tdf, r_prod, r_decay, decay_max, gsf;
+  double z, Dm, Do, Dgj, tdf, r_prod, r_decay, decay_max, inv_gsf;
   int growth, ui, gj_imp, gt0, gnt, dt0, dnt, mod_row, mask_row, pad;
 };
 
 struct NetReactD {
   int nr, np, r[kNetStoich], p[kNetStoich];
-  double rc[kNetStoich], rkm[kNetStoich], pc[kNetStoich];
-  double vmax, keq;
+  double rc[kNetStoich], inv_rkm[kNetStoich], pc[kNetStoich];
+  double vmax, inv_keq;    // inv_keq 0: no standard free energy
   int t0, nt;
 };
 
@@ -105,19 +105,22 @@ struct NetArgs {
 };
 
 // sim_toolbox.electroflux (sim_toolbox.py:18-69) for a general charge, FP64,
-// with the FP64 transcendentals only where they carry information (the
-// GPU's FP64 pipe bounds these kernels):
+// with Dk = Dc / d and zF = (z + 1e-25) F / (R T) hoisted out of the
+// membrane loops, and the FP64 transcendentals only where they carry
+// information (the GPU's FP64 pipe bounds these kernels):
 //   |a| < 1e-17 (every neutral substance: a = 1e-25 v F/RT): exp(-a) rounds
 //     to 1 and expm1(-a) to -a, in FP64 as in NumPy, so the flux is
-//     -(Dc/d)(cB - cA) (a few ulp from BETSE's order of operations);
+//     -Dk (cB - cA) (a few ulp from BETSE's order of operations);
 //   |a| > 1e-3: -expm1(-a) = 1 - exp(-a) to within 1e-13 relative;
 //   otherwise (small gap-junction voltages) the Taylor series of expm1(-a)
 //   to the fifth power, whose remainder a^6/720 is below 2e-21 |a|.
-__device__ __forceinline__ double net_ghk(double cA, double cB, double Dc, double inv_d, double z, double v,
-                                          double F_RT) {
-  const double a = ((z + kNonce) * (v + kNonce)) * F_RT;
+__device__ __forceinline__ bool net_neutral(double zF) { return fabs(zF) < 1.0e-20; }
+
+__device__ __forceinline__ double net_ghk(double cA, double cB, double Dk, double zF, bool neutral, double v) {
+  if (neutral) return -Dk * (cB - cA);
+  const double a = zF * (v + kNonce);
   const double aa = fabs(a);
-  if (aa < 1.0e-17) return -(Dc * inv_d) * (cB - cA);
+  if (aa < 1.0e-17) return -Dk * (cB - cA);
   double ea, den;
   if (aa > 1.0e-3) {
     ea = exp(-a);
@@ -128,7 +131,7 @@ __device__ __forceinline__ double net_ghk(double cA, double cB, double Dc, doubl
     ea = 1.0 + em1;
     den = -em1;
   }
-  return -((Dc * a) * inv_d) * ((cB - cA * ea) / den);
+  return -(Dk * a) * ((cB - cA * ea) / den);
 }
 
 // (c/Km)^n: BETSE's '**' (C pow); exponents 1 and 2 by multiplication (the
@@ -156,19 +159,19 @@ __device__ double net_factor(const NetTables& tb, int t0, int nt, const double* 
     const double c = net_conc(t, cs, env);
     switch (t.kind) {
       case NT_ACT: {
-        const double x = net_pow(c / t.km, t.n);
+        const double x = net_pow(c * t.inv_km, t.n);
         const double h = x / (1.0 + x);
         act = any_mult ? act * h : h;
         any_mult = true;
         break;
       }
       case NT_ACT_INDEP: {
-        const double x = net_pow(c / t.km, t.n);
+        const double x = net_pow(c * t.inv_km, t.n);
         act = act + x / (1.0 + x);
         break;
       }
       case NT_INH: {
-        const double h = 1.0 / (1.0 + net_pow(c / t.km, t.n));
+        const double h = 1.0 / (1.0 + net_pow(c * t.inv_km, t.n));
         inh = any_inh ? inh * h : h;
         any_inh = true;
         break;
@@ -228,7 +231,7 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
       const bool target = sb.mask_row < 0 || a.gmask[(size_t)sb.mask_row * a.C + c];
       if (sb.growth && target) {
         const double mod = sb.mod_row < 0 ? 1.0 : a.gmod[(size_t)sb.mod_row * a.C + c];
-        const double cc = cs[k] / sb.gsf;
+        const double cc = cs[k] * sb.inv_gsf;
         const double ga = net_factor(tb, sb.gt0, sb.gnt, cs, env);
         const double da = net_factor(tb, sb.dt0, sb.dnt, cs, env);
         r = mod * (sb.r_prod * sb.tdf) * ga - (sb.r_decay * sb.tdf) * cc - (sb.decay_max * sb.tdf) * da * cc;
@@ -239,10 +242,10 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
       const NetReactD& rx = tb.react[j];
       const double al = net_factor(tb, rx.t0, rx.nt, cs, env);
       double rate;
-      if (rx.keq == 0.0) {
+      if (rx.inv_keq == 0.0) {
         double fwd = 1.0;
         for (int q = 0; q < rx.nr; ++q) {
-          const double x = net_pow(cs[rx.r[q]] / rx.rkm[q], rx.rc[q]);
+          const double x = net_pow(cs[rx.r[q]] * rx.inv_rkm[q], rx.rc[q]);
           fwd = q == 0 ? x / (1.0 + x) : fwd * (x / (1.0 + x));
         }
         rate = rx.vmax * al * fwd;
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
           const double t = 1.0e-3 * net_pow(cs[rx.r[q]], rx.rc[q]);
           den = q == 0 ? t : den * t;
         }
-        rate = rx.vmax * al * (1.0 - (num / den) / rx.keq);
+        rate = rx.vmax * al * (1.0 - (num / den) * rx.inv_keq);
       }
       if (OUT) a.rates[(size_t)j * a.C + c] = rate;
       for (int k = 0; k < S; ++k) delta[k] += tb.rm[k][j] * rate;
@@ -266,6 +269,8 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
     for (int k = 0; k < S; ++k) {
       const NetSubD& sb = tb.sub[k];
       const double c1 = cs[k] + delta[k] * a.dt;
+      const double zF = (sb.z + kNonce) * a.F_RT, Dk = sb.Dm * a.inv_tm;
+      const bool neutral = net_neutral(zF);
       double s = 0.0;
       for (int m = m0; m < m1; ++m) {
         double cm;
@@ -278,7 +283,7 @@ __global__ void __launch_bounds__(kNetTPB) k_net_cell(NetArgs a) {
         } else {
           cm = cs[k];
         }
-        const double f = sb.Dm != 0.0 ? net_ghk(env[k], cm, sb.Dm, a.inv_tm, sb.z, a.vm[m], a.F_RT) : 0.0;
+        const double f = sb.Dm != 0.0 ? net_ghk(env[k], cm, Dk, zF, neutral, a.vm[m]) : 0.0;
         const double fa = f * a.mem_sa[m];
         s += fa;
         if (sb.ui) a.cmem_mid[(size_t)k * a.M + m] = cm + f * a.gamma[m] * a.dt;
@@ -309,6 +314,8 @@ __global__ void __launch_bounds__(kNetTPB) k_net_gj(NetArgs a) {
       const double c2 = a.c_mid[(size_t)k * a.C + c];
       double c3 = c2;
       if (!sb.gj_imp) {
+        const double zF = (sb.z + kNonce) * a.F_RT, Dk = sb.Dgj * a.gj_block * a.inv_gj_len;
+        const bool neutral = net_neutral(zF);
         double s = 0.0;
         for (int m = m0; m < m1; ++m) {
           const int n = a.nn[m];
@@ -316,8 +323,7 @@ __global__ void __launch_bounds__(kNetTPB) k_net_gj(NetArgs a) {
           const double cB = sb.ui ? a.cmem_mid[(size_t)k * a.M + n] : a.c_mid[(size_t)k * a.C + a.nn_cell[m]];
           const double go = a.gjo ? a.gjo[m] : a.gj_block * a.gj_w[m];
           double f = 0.0;
-          if (!a.bflag[m])
-            f = net_ghk(cA, cB, sb.Dgj * a.gj_block * go, a.inv_gj_len, sb.z, a.vm[n] - a.vm[m], a.F_RT);
+          if (!a.bflag[m]) f = net_ghk(cA, cB, Dk * go, zF, neutral, a.vm[n] - a.vm[m]);
           s += -f * a.mem_sa[m];
           if (sb.ui) {
             const double cm = cA + (-f) * a.gamma[m] * sb.tdf * a.dt;

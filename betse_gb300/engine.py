@@ -231,8 +231,9 @@ class ClusterEngine:
         """Pin the tile size (membrane slots per tile) and, for the split form,
         the kernel: 0/'tile', 1/'persistent' (True), 2/'factored',
         3/'resident', 4/'pipelined' (factored, persistent); ``variant`` picks
-        the factored kernel's (2 or 4 junctions per load round, +10 with
-        prefetched entries; 0 keeps it). The state is kept."""
+        the factored kernel's (2, 3, 4 or 6 junctions per load round, +10
+        with prefetched entries: 2, 4, 12, 13, 14, 16; 0 keeps it). The state
+        is kept."""
         k = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
         _lib.check(self.lib.bx_set_launch_config(self.h, int(tpb), k | (int(variant) << 8)),
                    'bx_set_launch_config')

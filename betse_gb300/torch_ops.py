@@ -207,6 +207,79 @@ def set_lap_env_inv(h: int, lap_env_inv: Tensor) -> None:
 
 
 
+# ---- molecule / gene regulatory networks (bx_network_*) ----------------------
+def _net_info(n: int):
+    """(substances, reactions, n_cells, n_mems)."""
+    v = np.zeros(4, np.int32)
+    _lib.check(_lib.load().bx_network_info(ct.c_void_p(n), _lib.iptr(v)), 'bx_network_info')
+    return [int(x) for x in v]
+
+
+@torch.library.custom_op('bx::network_upload', mutates_args=())
+def network_upload(n: int, c_cells: Tensor, cc_at_mem: Tensor, c_env: Tensor) -> None:
+    """Molecule.c_cells [S, C], cc_at_mem [S, M], c_env [S] (CUDA or CPU
+    float64). Work queued on the current stream is finished first."""
+    S, _, C, M = _net_info(n)
+    ts = [_f64(c_cells).reshape(S, C), _f64(cc_at_mem).reshape(S, M), _f64(c_env).reshape(S)]
+    if any(t.is_cuda for t in ts):
+        torch.cuda.current_stream().synchronize()
+    _lib.check(_lib.load().bx_network_upload(ct.c_void_p(n), *(_p(t) for t in ts)), 'bx::network_upload')
+
+
+@torch.library.custom_op('bx::network_step', mutates_args=())
+def network_step(n: int, n_steps: int, with_ions: bool = True, outputs: bool = False) -> None:
+    """bx_network_step: the ion step then the network (or the network alone),
+    on the cluster's stream after the current stream's queued work."""
+    torch.cuda.current_stream().synchronize()
+    _lib.check(_lib.load().bx_network_step(ct.c_void_p(n), int(n_steps), int(bool(with_ions)), int(bool(outputs))),
+               'bx::network_step')
+
+
+@torch.library.custom_op('bx::network_download', mutates_args=())
+def network_download(n: int) -> Tuple[Tensor, Tensor, Tensor]:
+    """(c_cells [S, C], cc_at_mem [S, M], c_env [S]) as new CUDA float64 tensors."""
+    S, _, C, M = _net_info(n)
+    dev = torch.device('cuda', torch.cuda.current_device())
+    out = (torch.empty((S, C), dtype=torch.float64, device=dev), torch.empty((S, M), dtype=torch.float64, device=dev),
+           torch.empty(S, dtype=torch.float64, device=dev))
+    torch.cuda.current_stream().synchronize()
+    _lib.check(_lib.load().bx_network_download(ct.c_void_p(n), *(_p(t) for t in out)), 'bx::network_download')
+    return out
+
+
+@torch.library.custom_op('bx::network_status', mutates_args=())
+def network_status(n: int) -> Tensor:
+    """int64 [1]: negative substance concentrations seen since the upload."""
+    v = ct.c_int64()
+    _lib.check(_lib.load().bx_network_status(ct.c_void_p(n), ct.byref(v)), 'bx::network_status')
+    return torch.tensor([v.value], dtype=torch.int64)
+
+
+@torch.library.custom_op('bx::network_destroy', mutates_args=())
+def network_destroy(n: int) -> None:
+    _lib.load().bx_network_destroy(ct.c_void_p(n))
+
+
+def create_network(h: int, spec, params) -> int:
+    """bx_network_create on cluster handle ``h`` (plain FP64) from a
+    ``NetworkSpec`` (``betse_gb300.network``) and the cluster's
+    ``StepParams`` (R and T give each reaction's equilibrium constant);
+    returns the network's integer handle, released by ``bx::network_destroy``."""
+    c = spec.to_c(params.R, params.T)
+    out = ct.c_void_p()
+    _lib.check(_lib.load().bx_network_create(ct.c_void_p(h), ct.byref(c), ct.byref(out)), 'bx_network_create')
+    return int(out.value)
+
+
+def check_network_stable(n: int) -> Tensor:
+    """Raise BetseSimUnstableException on a negative substance concentration
+    (sim_toolbox.py:1132-1151)."""
+    st = torch.ops.bx.network_status(n)
+    if int(st[0]):
+        raise BetseSimUnstableException('Network concentration below zero! Your simulation has become unstable.')
+    return st
+
+
 def params_tensor(params) -> Tensor:
     """The bytes of a bx_params (from a ``StepParams``) as a uint8 tensor."""
     p = params.to_c()

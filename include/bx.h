@@ -390,7 +390,7 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
  *      its next tiles' cell data, gap-junction entries and partner records
  *      in shared memory (cp.async) while it computes (results as kernel 2)
  * Bits 8-15 of kernel, when nonzero, pick the factored kernel's variant (the
- * third column of bx_autotune_table: 2, 4, 12 or 14).
+ * third column of bx_autotune_table: 2, 4, 12, 13, 14 or 16).
  * Kernels 1-4 need no extracellular spaces, no voltage-gated gap junctions
  * and no Ca-ATPase; steps with outputs or a nonzero Phi_b always run the
  * tile kernel.  The state is kept.  bx_autotune picks these by timing. */
@@ -416,9 +416,10 @@ int bx_autotune(bx_handle h, int n_steps, int* tpb_out, double* ms_per_step_out)
 /* The same search, reporting every candidate it timed: up to max_rows rows of
  * (membrane slots per tile, kernel, factored-kernel variant, ms per step);
  * *n_rows is set to the rows written.  The variant is the number of gap
- * junctions loaded per round (2 or 4), plus 10 when the first entries of each
- * cell (6 or 8) are loaded before the grid dependency wait.  The fastest
- * candidate is kept, as by bx_autotune. */
+ * junctions loaded per round (2, 3, 4 or 6), plus 10 when the first entries
+ * of each cell (6, or 8 with 4 per round) are loaded before the grid
+ * dependency wait: 2, 4, 12, 13, 14, 16.  The fastest candidate is kept, as
+ * by bx_autotune. */
 int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* tpb, int* kernel, int* unroll,
                       double* ms_per_step);
 
@@ -527,6 +528,8 @@ int bx_network_status(bx_network_handle n, int64_t* negative);
 /* Runs bx_network_step(n, n_steps, with_ions, 0) between two CUDA events on
  * the cluster's stream; reports ms per time step (the state advances). */
 int bx_network_time_step(bx_network_handle n, int n_steps, int with_ions, double* ms_per_step);
+/* info[4] = {substances, reactions, n_cells, n_mems}. */
+int bx_network_info(bx_network_handle n, int32_t* info);
 int bx_network_destroy(bx_network_handle n);
 
 #ifdef __cplusplus

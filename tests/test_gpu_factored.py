@@ -185,7 +185,7 @@ def test_pipelined_equals_factored_bit_for_bit():
             assert np.array_equal(a[k], c[k]), k
 
 
-@pytest.mark.parametrize('variant', [2, 12, 14])
+@pytest.mark.parametrize('variant', [2, 12, 13, 14, 16])
 def test_factored_variants_equal_bit_for_bit(variant):
     """The factored kernel's variants (junctions per load round; entries
     prefetched before the dependency wait) order the same arithmetic the same
