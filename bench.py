@@ -360,7 +360,9 @@ def network_step(g, p, Dm, st, stream, flush, n_steps=200, cpu=True):
                 'cell_substance_updates_per_s': C * 4 / (ms_net / 1e3),
                 'roofline': roofline_entry(nbytes, ms_net / 1e3, 'k_net_cell + k_net_gj',
                                            note='algorithmic bytes of one network step (both kernels; '
-                                                'Network.algorithmic_bytes) / its time per step, network alone')})
+                                                'Network.algorithmic_bytes) / its time per step, network alone. '
+                                                'The plain FP64 network is bound by the FP64 pipe (about 80% '
+                                                'of active cycles under ncu), not by HBM')})
     if cpu:
         out['cpu_baseline'] = cpu_baseline_network(g, p, Dm, st, spec_args=(spot, gmod, mem_vol, R_rads))
     return out
