@@ -700,9 +700,13 @@ LAUNCH_SUFFIX = {'': 0, 'p': 1, 'f': 2, 'r': 3, 'q': 4}
 
 def parse_launch(text):
     """'192' tile kernel, '192p' persistent, '192f' factored, '256r' resident,
-    '256q' pipelined factored."""
-    suffix = text.lstrip('0123456789')
-    return int(text[:len(text) - len(suffix)]), LAUNCH_SUFFIX[suffix]
+    '256q' pipelined factored; a number after 'f' picks the factored kernel's
+    variant ('256f12': two junctions per round, entries prefetched)."""
+    head = text.lstrip('0123456789')
+    tpb = int(text[:len(text) - len(head)])
+    suffix = head.rstrip('0123456789')
+    variant = head[len(suffix):]
+    return tpb, LAUNCH_SUFFIX[suffix], int(variant) if variant else 0
 
 
 def profile_run(args):
@@ -743,8 +747,8 @@ def main():
                     help='for ncu: build the workload, upload it, run 4 steps (or --time-steps), exit')
     ap.add_argument('--precision', default='split', choices=['split', 'fp64'])
     ap.add_argument('--launch', default=None,
-                    help='with --profile-run: membrane slots per tile, suffix p persistent, f factored, '
-                         'r resident kernel (e.g. 192r)')
+                    help='with --profile-run: membrane slots per tile, suffix p persistent, f factored '
+                         '(optionally followed by its variant, e.g. 256f12), r resident, q pipelined (e.g. 192r)')
     ap.add_argument('--profile-kernel', choices=['gemm', 'fields', 'network'],
                     help='for ncu: run a small case of one dense-product kernel and exit')
     args = ap.parse_args()
