@@ -789,10 +789,18 @@ cudaError_t enqueue_env(bx_cluster* h, bool out, cudaStream_t s) {
                                                             h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
     h->launches += 3;
   } else {
+    // the common configuration: flux, then update + charge fused, then the
+    // fields in one tiled launch (4 launches per step with the cell kernel)
     bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
-    bx::k_env_update<true><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, nullptr, h->d_fx, h->d_fy, h->d_env_ptr,
-                                                 h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
-    h->launches += 2;
+    const unsigned gc = (unsigned)(((size_t)h->G * 8 + 255) / 256);
+    bx::k_env_update_charge<<<gc, 256, 0, s>>>(h->d_cenv, h->d_fx, h->d_fy, h->d_env_ptr, h->d_env_mem,
+                                               h->d_mem_flux_sa, h->M, h->d_touched, h->d_vsrc,
+                                               out ? h->d_rho_env : nullptr, ec);
+    const dim3 gt((unsigned)((h->nx + bx::kEnvTX - 1) / bx::kEnvTX), (unsigned)((h->ny + bx::kEnvTY - 1) / bx::kEnvTY));
+    bx::k_env_fields_tile<<<gt, bx::kEnvTX * bx::kEnvTY, 0, s>>>(h->d_vsrc, h->phib_nonzero ? h->d_phib : nullptr,
+                                                                h->d_venv, ec.screen, h->d_Ex, h->d_Ey, ec);
+    h->launches += 3;
+    return cudaGetLastError();
   }
   bx::k_env_charge<<<gg, kEnvTPB, 0, s>>>(h->d_cenv, h->d_touched, h->d_vsrc, out ? h->d_rho_env : nullptr, ec);
   h->launches += 1;
@@ -858,7 +866,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
 int launches_per_step(const bx_cluster* h) {
   if (!h->ecm) return 2;
   if (h->ca) return h->par.sharpness < 1.0 ? 9 : 8;
-  return h->par.sharpness < 1.0 ? 8 : 7;
+  return h->par.sharpness < 1.0 ? 8 : 4;
 }
 
 int upload_fact_cst(bx_cluster* h);

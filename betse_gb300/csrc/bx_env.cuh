@@ -230,6 +230,114 @@ __global__ void k_env_neg_grad(const double* __restrict__ F, double scale, doubl
 }
 
 // ---------------------------------------------------------------------------
+// Fused forms of the sequences above, for the common configuration (no
+// Ca-ATPase, sharpness >= 1): fewer launches on a grid that is small against
+// the GPU, the same arithmetic term by term.
+// ---------------------------------------------------------------------------
+
+// k_env_update<true> and k_env_charge in one launch.  Eight lanes per grid
+// cell (lane = ion, I <= 8): each lane advances its ion's concentration in
+// place (it reads only fluxes and its own cell's value), then the cell's
+// group sums F z_i c_i over the ions in order through shuffles.
+__global__ void __launch_bounds__(256) k_env_update_charge(double* cenv, const double* __restrict__ fx,
+                                                           const double* __restrict__ fy,
+                                                           const int* __restrict__ env_ptr,
+                                                           const int* __restrict__ env_mem,
+                                                           const double* __restrict__ mem_flux_sa, int M,
+                                                           const uint8_t* __restrict__ touched, double* vsrc,
+                                                           double* rho_env, EnvConst e) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = t >> 3, ion = t & 7;
+  const bool live = k < e.G && ion < e.I;
+  double zc = 0.0;
+  if (live) {
+    const int i = k / e.nx, j = k - i * e.nx;
+    const double* fxi = fx + (size_t)ion * e.G;
+    const double* fyi = fy + (size_t)ion * e.G;
+    const double div = ddx_neg(fxi, e, i, j) + ddy_neg(fyi, e, i, j);
+    double c = cb_at(cenv, e, ion, i, j) + div * e.dt;
+    double s = 0.0;
+    for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
+    c = c + (s * e.inv_h_d2) * e.dt;
+    cenv[(size_t)ion * e.G + k] = c;
+    zc = e.zF[ion] * c;
+  }
+  // the group of cell k: lanes 8 (k mod 4) .. +7 of this warp
+  const int base = threadIdx.x & 24;
+  double rho = 0.0;
+  for (int q = 0; q < e.I; ++q) {
+    const double v = __shfl_sync(0xffffffffu, zc, base + q);
+    rho += v;
+  }
+  if (live && ion == 0) env_charge_out(k, rho, touched, vsrc, rho_env, e);
+}
+
+// k_env_gauss_y, k_env_gauss_x (+ Phi_b) and k_env_neg_grad in one launch:
+// each CTA computes a kEnvTX x kEnvTY tile of E_env (and v_env) from the
+// potential source in shared memory, with the halos the two Gaussian passes
+// (4 cells) and the gradient (1 cell) need.
+constexpr int kEnvTX = 32, kEnvTY = 16;
+constexpr int kEnvVX = kEnvTX + 2, kEnvVY = kEnvTY + 2;        // v_env tile (gradient halo)
+constexpr int kEnvSX = kEnvVX + 8, kEnvSY = kEnvVY + 8;        // source tile (Gaussian halo)
+__global__ void __launch_bounds__(kEnvTX * kEnvTY) k_env_fields_tile(const double* __restrict__ vsrc,
+                                                                     const double* __restrict__ phib,
+                                                                     double* venv, double scale, double* Ex,
+                                                                     double* Ey, EnvConst e) {
+  __shared__ double src[kEnvSY][kEnvSX];
+  __shared__ double gy[kEnvVY][kEnvSX];
+  __shared__ double v[kEnvVY][kEnvVX];
+  const int i0 = blockIdx.y * kEnvTY - 1 - 4, j0 = blockIdx.x * kEnvTX - 1 - 4;   // src tile origin
+  const int nt = blockDim.x;
+  for (int q = threadIdx.x; q < kEnvSY * kEnvSX; q += nt) {
+    const int a = q / kEnvSX, b = q - a * kEnvSX, i = i0 + a, j = j0 + b;
+    src[a][b] = (i >= 0 && i < e.ny && j >= 0 && j < e.nx) ? vsrc[i * e.nx + j] : 0.0;
+  }
+  __syncthreads();
+  // axis-0 pass (zero padding: taps outside the grid are skipped, as k_env_gauss_y does)
+  for (int q = threadIdx.x; q < kEnvVY * kEnvSX; q += nt) {
+    const int a = q / kEnvSX, b = q - a * kEnvSX, i = i0 + 4 + a;
+    double acc = 0.0;
+#pragma unroll
+    for (int w = -4; w <= 4; ++w) {
+      const int ii = i + w;
+      if (ii < 0 || ii >= e.ny) continue;
+      acc += e.gw[w + 4] * src[a + 4 + w][b];
+    }
+    gy[a][b] = acc;
+  }
+  __syncthreads();
+  // axis-1 pass + Phi_b -> v_env on the tile and its one-cell halo
+  for (int q = threadIdx.x; q < kEnvVY * kEnvVX; q += nt) {
+    const int a = q / kEnvVX, b = q - a * kEnvVX, i = i0 + 4 + a, j = j0 + 4 + b;
+    double acc = 0.0;
+    for (int w = -4; w <= 4; ++w) {
+      const int jj = j + w;
+      if (jj < 0 || jj >= e.nx) continue;
+      acc += e.gw[w + 4] * gy[a][b + 4 + w];
+    }
+    const bool in = i >= 0 && i < e.ny && j >= 0 && j < e.nx;
+    v[a][b] = in ? acc + (phib ? phib[i * e.nx + j] : 0.0) : 0.0;
+  }
+  __syncthreads();
+  // E = -gradient(scale * v_env), one-sided on the grid edges
+  const int a = threadIdx.x / kEnvTX + 1, b = threadIdx.x % kEnvTX + 1;
+  const int i = blockIdx.y * kEnvTY + a - 1, j = blockIdx.x * kEnvTX + b - 1;
+  if (i >= e.ny || j >= e.nx) return;
+  const int k = i * e.nx + j;
+  venv[k] = v[a][b];
+  auto f = [&](int da, int db) { return scale * v[a + da][b + db]; };
+  double gx, gyy;
+  if (j == 0) gx = (f(0, 1) - f(0, 0)) * e.inv_delta;
+  else if (j == e.nx - 1) gx = (f(0, 0) - f(0, -1)) * e.inv_delta;
+  else gx = -(f(0, -1) - f(0, 1)) * e.inv_2delta;
+  if (i == 0) gyy = (f(1, 0) - f(0, 0)) * e.inv_delta;
+  else if (i == e.ny - 1) gyy = (f(0, 0) - f(-1, 0)) * e.inv_delta;
+  else gyy = -(f(-1, 0) - f(1, 0)) * e.inv_2delta;
+  Ex[k] = -gx;
+  Ey[k] = -gyy;
+}
+
+// ---------------------------------------------------------------------------
 // Dense FP64 products Y[n x R] = A[n x n] X[n x R], R <= 4 (row-major).
 // One warp per row; the row streams from HBM with 16-byte loads, X is
 // L2-resident.  The HBM-bound form of np.dot(lapENVinv, .).
