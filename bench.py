@@ -765,7 +765,7 @@ def main():
     w, g, p, Dm, st, D_env = build_workload(args.workload)
     sweep = bool(w.get('sweep'))
     full = rank == 0 and world == 1 and args.workload == 'cluster100k' and not args.no_secondary
-    # the other configurations' workloads, built before the GPU is touched
+    # the other configurations' workloads (generated on the GPU), built first
     others = {n: build_workload(n) for n in ('plain250', 'ecm20k', 'sweep512')} if full else {}
     import torch
     dist = None

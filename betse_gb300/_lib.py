@@ -115,6 +115,28 @@ class BxStepStatus(ct.Structure):
                 ('unstable', ct.c_int32), ('precision', ct.c_int32)]
 
 
+class BxGraphLevel(ct.Structure):
+    _fields_ = [('n', ct.c_int32), ('nnz', ct.c_int32), ('row_ptr', _ip), ('col', _ip), ('val', _dp)]
+
+
+class BxGenSpec(ct.Structure):
+    _fields_ = [('seed', ct.c_uint32), ('grid_size', ct.c_int32), ('nbx', ct.c_int32),
+                ('nby', ct.c_int32), ('nrx', ct.c_int32), ('nry', ct.c_int32)] + \
+        [(n, ct.c_double) for n in ('bx0', 'bx1', 'by0', 'by1', 'rx0', 'rx1', 'ry0', 'ry1', 'jitter',
+                                    'radius', 'd_cell', 'cell_radius', 'scale_cell', 'cell_height')]
+
+
+GEN_ARRAYS = [('cell_mem_ptr', 'i'), ('nn_i', 'i'), ('map_mem2ecm', 'i'), ('mem_sa', 'd'),
+              ('mem_nx', 'd'), ('mem_ny', 'd'), ('R_rads', 'd'), ('mem_mid_x', 'd'),
+              ('mem_mid_y', 'd'), ('cell_vol', 'd'), ('cell_sa', 'd'), ('diviterm', 'd'),
+              ('cell_centre_x', 'd'), ('cell_centre_y', 'd'), ('mem_sa_per_env', 'd'),
+              ('cell_nn_ptr', 'i'), ('cell_nn', 'i'), ('lattice_x', 'd'), ('lattice_y', 'd')]
+
+
+class BxGenArrays(ct.Structure):
+    _fields_ = [(n, _ip if t == 'i' else _dp) for n, t in GEN_ARRAYS]
+
+
 # every symbol include/bx.h declares: name -> (restype, argtypes)
 SIGNATURES = {
     'bx_cluster_create': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_int,
@@ -147,6 +169,17 @@ SIGNATURES = {
     'bx_dense_op_time': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_int,
                                     ct.POINTER(ct.c_double)]),
     'bx_dense_op_destroy': (ct.c_int, [ct.c_void_p]),
+    'bx_dense_op_create_empty': (ct.c_int, [ct.c_int, ct.POINTER(ct.c_void_p)]),
+    'bx_dense_op_set_columns': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    'bx_graph_create': (ct.c_int, [ct.c_int, ct.POINTER(BxGraphLevel), _dp, ct.POINTER(BxGraphLevel), _dp,
+                                   ct.c_int, ct.POINTER(ct.c_void_p)]),
+    'bx_graph_solve': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_double, ct.c_int,
+                                  ct.POINTER(ct.c_int), ct.POINTER(ct.c_double), ct.c_void_p]),
+    'bx_lap_gj_apply': (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_double, ct.c_int,
+                                   ct.POINTER(ct.c_int), ct.POINTER(ct.c_double), ct.c_void_p]),
+    'bx_lap_gj_dense': (ct.c_int, [ct.c_void_p, ct.c_double, ct.c_int, ct.POINTER(ct.c_int),
+                                   ct.POINTER(ct.c_double), ct.c_void_p, ct.POINTER(ct.c_void_p)]),
+    'bx_graph_destroy': (ct.c_int, [ct.c_void_p]),
     'bx_gnn_create': (ct.c_int, [ct.POINTER(ct.c_void_p)]),
     'bx_gnn_n_params': (ct.c_int, []),
     'bx_gnn_set_params': (ct.c_int, [ct.c_void_p, _fp]),
@@ -189,6 +222,10 @@ SIGNATURES = {
     'bx_step_fp64_noalloc': (ct.c_int, [ct.POINTER(BxGeom), ct.POINTER(BxParams), ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                         ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p]),
+    'bx_generate_cluster': (ct.c_int, [ct.POINTER(BxGenSpec), ct.c_void_p, ct.POINTER(ct.c_void_p)]),
+    'bx_generated_info': (ct.c_int, [ct.c_void_p, _ip, _dp]),
+    'bx_generated_download': (ct.c_int, [ct.c_void_p, ct.POINTER(BxGenArrays)]),
+    'bx_generated_destroy': (ct.c_int, [ct.c_void_p]),
 }
 
 _lib = None

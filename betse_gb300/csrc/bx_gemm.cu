@@ -281,6 +281,28 @@ __global__ void k_pack_split(const double* __restrict__ src, int rows, int cols,
   }
 }
 
+// Split columns [col0, col0 + ncols) of an n x n operator, given as
+// src[row * ncols + (col - col0)], into the hi/lo tiles of 64-column tile
+// columns kt0 .. kt0 + nkt - 1 (col0 = kt0 * 64); zero outside the block.
+__global__ void k_pack_cols(const double* __restrict__ src, int n, int col0, int ncols, int Mt, int Kt, int kt0,
+                            int nkt, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+  const long long n_el = (long long)Mt * nkt * TILE;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n_el;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long tl = e / TILE;
+    const int w = (int)(e - tl * TILE);
+    const int mt = (int)(tl / nkt), kt = kt0 + (int)(tl % nkt);
+    const int core = w >> 6, in = w & 63;
+    const int r = ((core >> 3) << 3) + (in >> 3), k = ((core & 7) << 3) + (in & 7);
+    const int row = mt * BM + r, col = kt * BK + k;
+    const double a = (row < n && col < n && col - col0 < ncols) ? src[(long long)row * ncols + (col - col0)] : 0.0;
+    const long long d = ((long long)mt * Kt + kt) * TILE + w;
+    const __nv_bfloat16 h = __double2bfloat16(a);
+    hi[d] = h;
+    lo[d] = __double2bfloat16(a - (double)__bfloat162float(h));
+  }
+}
+
 // R = X - L Y for a CSR operator L, all [n][nrhs] row-major
 __global__ void k_csr_residual(int n, int nrhs, const int* __restrict__ ptr, const int* __restrict__ col,
                                const double* __restrict__ val, const double* __restrict__ X,
@@ -405,6 +427,43 @@ int bx_dense_op_create(const double* A, int n, bx_dense_op_handle* out) {
     return rc;
   }
   *out = op;
+  return BX_OK;
+}
+
+int bx_dense_op_create_empty(int n, bx_dense_op_handle* out) {
+  if (!out || n <= 0) return gfail(BX_EINVAL, "bx_dense_op_create_empty: bad arguments");
+  *out = nullptr;
+  GX(cudaFuncSetAttribute(bxg::k_gemm_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, bxg::SMEM_BYTES));
+  bx_dense_op* op = new bx_dense_op();
+  op->n = n;
+  op->Mt = (n + bxg::BM - 1) / bxg::BM;
+  op->Kt = (n + bxg::BK - 1) / bxg::BK;
+  const size_t el = (size_t)op->Mt * op->Kt * bxg::TILE;
+  if (cudaMalloc(&op->a_hi, el * 2) != cudaSuccess || cudaMalloc(&op->a_lo, el * 2) != cudaSuccess ||
+      cudaMalloc(&op->err, sizeof(unsigned int)) != cudaSuccess) {
+    cudaGetLastError();
+    bx_dense_op_destroy(op);
+    return gfail(BX_ENOMEM, "cudaMalloc dense operator");
+  }
+  if (cudaMemset(op->a_hi, 0, el * 2) != cudaSuccess || cudaMemset(op->a_lo, 0, el * 2) != cudaSuccess ||
+      cudaMemset(op->err, 0, sizeof(unsigned int)) != cudaSuccess) {
+    bx_dense_op_destroy(op);
+    return gfail(BX_ECUDA, "cudaMemset dense operator");
+  }
+  *out = op;
+  return BX_OK;
+}
+
+int bx_dense_op_set_columns(bx_dense_op_handle op, int col0, int ncols, const double* cols, void* stream) {
+  if (!op || !cols || col0 < 0 || ncols <= 0 || col0 + ncols > op->n || col0 % bxg::BK ||
+      (ncols % bxg::BK && col0 + ncols != op->n))
+    return gfail(BX_EINVAL, "bx_dense_op_set_columns: the block must start on a 64-column boundary and hold "
+                            "whole 64-column tiles (or end at n)");
+  const int kt0 = col0 / bxg::BK, nkt = (ncols + bxg::BK - 1) / bxg::BK;
+  const long long n_el = (long long)op->Mt * nkt * bxg::TILE;
+  bxg::k_pack_cols<<<grid_for(n_el), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      cols, op->n, col0, ncols, op->Mt, op->Kt, kt0, nkt, op->a_hi, op->a_lo);
+  GX(cudaGetLastError());
   return BX_OK;
 }
 

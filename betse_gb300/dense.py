@@ -9,6 +9,11 @@ computes one column at a time with ``np.dot(cells.lapGJinv, rhs)``
 ``A`` inverts (``set_forward``), ``apply(X, refine=True)`` adds one FP64
 refinement step ``Y += A (X - L Y)``.
 
+``LapGJ`` applies ``cells.lapGJinv`` at any cluster size without forming it:
+``-L+ Lw L+ A X`` with ``L+`` by multigrid-preconditioned conjugate gradients
+on the GPU (``bx_graph_*``, ``csrc/bx_graph.cu``), and builds the dense
+operator for the tensor cores column block by column block from it.
+
 Device memory for X and Y comes from PyTorch (CUDA tensors); numpy inputs are
 copied to the current device and the result is returned as numpy.
 """
@@ -56,7 +61,60 @@ def lap_gj_operators(tri_edges, tri_edge_len, vor_edge_len, vor_sa):
     return lap_inv, lap
 
 
+def _incidence(tri_edges, n):
+    import scipy.sparse as sp
+    e = np.asarray(tri_edges, np.int64)
+    m = len(e)
+    rows = np.repeat(np.arange(m), 2)
+    return sp.csr_matrix((np.tile([-1.0, 1.0], m), (rows, e.ravel())), shape=(m, n))
+
+
+def graph_levels(L, coarse_max=64):
+    """The multigrid hierarchy of a graph Laplacian ``L`` (scipy sparse): the
+    Galerkin operators ``P^T A P`` of aggregates of 4 consecutive nodes
+    (node ``i`` -> ``i // 4``), level by level down to ``coarse_max`` nodes or
+    fewer, and the pseudo-inverse of the coarsest.  Consecutive nodes should
+    be neighbours (cells along a Z curve)."""
+    import scipy.sparse as sp
+    levels = [sp.csr_matrix(L)]
+    while levels[-1].shape[0] > coarse_max:
+        A = levels[-1]
+        n = A.shape[0]
+        P = sp.csr_matrix((np.ones(n), (np.arange(n), np.arange(n) // 4)), shape=(n, (n + 3) // 4))
+        levels.append(sp.csr_matrix(P.T @ A @ P))
+    for A in levels:
+        A.sum_duplicates()
+        A.sort_indices()
+    return levels, np.linalg.pinv(levels[-1].toarray())
+
+
+def lap_gj_inputs(geom, cell_centres, cell_height=1e-5, scale_cell=0.99):
+    """``graphLaplacian``'s inputs for a generated cluster: one triangulation
+    edge per pair of cells sharing a membrane (lower cell first), its length
+    the distance between the cell centres, the dual (Voronoi) edge the shared
+    membrane's unscaled length, and the cell areas unscaled from the volumes
+    (membranes are scaled by ``scale_cell`` about the centre)."""
+    m2c = np.asarray(geom.mem_to_cells, np.int64)
+    nn = np.asarray(geom.nn_i, np.int64)
+    c, d = m2c, m2c[nn]
+    sel = c < d
+    edges = np.column_stack((c[sel], d[sel]))
+    cc = np.asarray(cell_centres, np.float64)
+    tri_len = np.hypot(*(cc[edges[:, 0]] - cc[edges[:, 1]]).T)
+    vor_len = np.asarray(geom.mem_sa)[sel] / (cell_height * scale_cell)
+    vor_sa = np.asarray(geom.cell_vol) / (cell_height * scale_cell ** 2)
+    return edges, tri_len, vor_len, vor_sa
+
+
 class DenseOperator:
+    @classmethod
+    def _wrap(cls, handle, n):
+        op = cls.__new__(cls)
+        op.lib = _lib.load()
+        op.n = int(n)
+        op.h = handle
+        return op
+
     def __init__(self, A, forward=None):
         A = np.ascontiguousarray(np.asarray(A, np.float64))
         if A.ndim != 2 or A.shape[0] != A.shape[1]:
@@ -130,6 +188,121 @@ class DenseOperator:
     def close(self):
         if getattr(self, 'h', None) is not None and self.h.value:
             self.lib.bx_dense_op_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class LapGJ:
+    """``cells.lapGJinv`` (``Cells.graphLaplacian``, ``cells.py:1845-1894``)
+    on the GPU at any size, from the DEC mesh's ``tri_edges``,
+    ``tri_edge_len``, ``vor_edge_len`` and ``vor_sa``, as
+    ``lap_gj_operators`` takes them.
+
+    ``apply(X)`` = ``lapGJinv @ X`` = ``-L+ Lw L+ (vor_sa * X)`` in FP64 (two
+    multigrid-preconditioned CG solves per block of right-hand sides, each
+    column to ``tol`` relative residual); ``solve(B)`` = ``L+ B``;
+    ``dense()`` the operator as BF16x3 tensor-core tiles (``DenseOperator``),
+    built from ``apply`` on identity columns.  The hierarchy groups 4
+    consecutive cells, so cells ordered along a Z curve (the generator's
+    order) converge fastest."""
+
+    def __init__(self, tri_edges, tri_edge_len, vor_edge_len, vor_sa, max_rhs=64, coarse_max=64):
+        import scipy.sparse as sp
+        vor_sa = np.ascontiguousarray(vor_sa, np.float64)
+        self.n = n = len(vor_sa)
+        D = _incidence(tri_edges, n)
+        w = np.asarray(tri_edge_len, np.float64) / np.asarray(vor_edge_len, np.float64)
+        L = D.T @ D
+        Lw = sp.csr_matrix(D.T @ sp.diags(w) @ D)
+        Lw.sum_duplicates()
+        Lw.sort_indices()
+        levels, pinv = graph_levels(L, coarse_max)
+        self.n_levels = len(levels)
+        self.level_sizes = [A.shape[0] for A in levels]
+        keep = []
+
+        def lvl(A):
+            ptr = np.ascontiguousarray(A.indptr, np.int32)
+            col = np.ascontiguousarray(A.indices, np.int32)
+            val = np.ascontiguousarray(A.data, np.float64)
+            keep.extend([ptr, col, val])
+            return _lib.BxGraphLevel(n=A.shape[0], nnz=len(val), row_ptr=_lib.iptr(ptr), col=_lib.iptr(col),
+                                     val=_lib.dptr(val))
+
+        arr = (_lib.BxGraphLevel * len(levels))(*[lvl(A) for A in levels])
+        wl = lvl(Lw)
+        pinv = np.ascontiguousarray(pinv, np.float64)
+        self.lib = _lib.load()
+        self.max_rhs = int(max_rhs)
+        h = ct.c_void_p()
+        _lib.check(self.lib.bx_graph_create(len(levels), arr, _lib.dptr(pinv), ct.byref(wl), _lib.dptr(vor_sa),
+                                            self.max_rhs, ct.byref(h)), 'bx_graph_create')
+        self.h = h
+        self.last_iters = 0
+        self.last_rel_res = 0.0
+
+    def _run(self, fn, X, tol, max_iter, stream):
+        import torch
+        as_numpy = not isinstance(X, torch.Tensor)
+        Xt = torch.as_tensor(np.asarray(X, np.float64) if as_numpy else X, dtype=torch.float64,
+                             device='cuda')
+        squeeze = Xt.ndim == 1
+        if squeeze:
+            Xt = Xt[:, None]
+        if Xt.shape[0] != self.n:
+            raise ValueError('X must have n rows')
+        st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
+        outs, worst_it, worst_res = [], 0, 0.0
+        for j0 in range(0, Xt.shape[1], self.max_rhs):
+            xb = Xt[:, j0:j0 + self.max_rhs].contiguous()
+            yb = torch.empty_like(xb)
+            it, res = ct.c_int(), ct.c_double()
+            _lib.check(fn(self.h, ct.c_void_p(xb.data_ptr()), ct.c_void_p(yb.data_ptr()), int(xb.shape[1]),
+                          float(tol), int(max_iter), ct.byref(it), ct.byref(res), ct.c_void_p(st)), fn.__name__)
+            worst_it, worst_res = max(worst_it, it.value), max(worst_res, res.value)
+            outs.append(yb)
+        self.last_iters, self.last_rel_res = worst_it, worst_res
+        if worst_res > tol:
+            raise RuntimeError(f'graph Laplacian solve did not reach {tol:g} in {max_iter} iterations '
+                               f'(relative residual {worst_res:.2e})')
+        Y = torch.cat(outs, dim=1)
+        if squeeze:
+            Y = Y[:, 0]
+        return Y.cpu().numpy() if as_numpy else Y
+
+    def solve(self, B, tol=1e-12, max_iter=1000, stream=None):
+        return self._run(self.lib.bx_graph_solve, B, tol, max_iter, stream)
+
+    def apply(self, X, tol=1e-12, max_iter=1000, stream=None):
+        return self._run(self.lib.bx_lap_gj_apply, X, tol, max_iter, stream)
+
+    def dense(self, tol=1e-10, max_iter=1000, stream=None):
+        import torch
+        st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
+        h = ct.c_void_p()
+        it, res = ct.c_int(), ct.c_double()
+        _lib.check(self.lib.bx_lap_gj_dense(self.h, float(tol), int(max_iter), ct.byref(it), ct.byref(res),
+                                            ct.c_void_p(st), ct.byref(h)), 'bx_lap_gj_dense')
+        self.last_iters, self.last_rel_res = it.value, res.value
+        if res.value > tol:
+            self.lib.bx_dense_op_destroy(h)
+            raise RuntimeError(f'lapGJinv build did not reach {tol:g} (relative residual {res.value:.2e})')
+        return DenseOperator._wrap(h, self.n)
+
+    def close(self):
+        if getattr(self, 'h', None) is not None and self.h.value:
+            self.lib.bx_graph_destroy(self.h)
             self.h = None
 
     def __del__(self):

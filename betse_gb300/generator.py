@@ -1,38 +1,36 @@
-"""Synthetic cell clusters with BETSE's conventions, at any size.
+"""Synthetic cell clusters with BETSE's conventions, generated on the GPU.
 
 BETSE seeds a cluster with ``Cells.make_world`` (``betse/science/cells.py:414``):
 a jittered hexagonal lattice (``_make_cell_lattice``, cells.py:742-801), a DEC
 mesh whose Voronoi vertices are triangle centroids (``DECMesh(use_centroids=
-True)``, math/mesh.py:86) clipped to the tissue shape, then per-cell membranes
+True)``, math/mesh.py:86) clipped to the tissue shape in two passes
+(``clip_and_refine``, math/mesh.py:189, 2290-2372), then per-cell membranes
 (``cellVerts``, cells.py:978-1175), volumes (``cell_vols``, :1358-1390), gap
 junction pairs (``mem_processing``/``near_neigh``, :1392-1573) and the
 environment grid maps (``makeECM``/``environment``, :1576-1843). Its O(N^2)
 Python loops and dense ``pinv`` limit it to a few thousand cells.
 
-This module builds the same data in vectorised NumPy/SciPy:
+``make_cluster`` runs the same construction as CUDA kernels
+(``bx_generate_cluster``, ``csrc/bx_generator.cu``): BETSE's seed lattice bit
+for bit (numpy's linspace rows and legacy ``RandomState`` jitter), per-point
+Voronoi cells clipped against the neighbouring buckets' bisectors (Delaunay
+stars without a global triangulation), two-pass seeding, Z-ordered cells,
+membranes, gap-junction pairs across shared Delaunay edges, the environment
+grid map and the cell adjacency.  Clip-edge refinement of the reference mesh
+is not reproduced: boundary cells are whole Voronoi cells and the open outer
+ring of the second pass is left out.
 
-* the lattice recipe is BETSE's (linspace rows, legacy ``np.random`` jitter
-  ``disorder * d_cell * (rand - 0.5)``);
-* cells are the Delaunay duals with centroid vertices of every seed whose
-  distance to the lattice centre is below ``radius`` and whose triangle fan is
-  closed; membranes are the polygon edges scaled in by ``scale_cell`` about the
-  centroid, listed counter-clockwise per cell exactly as ``cellVerts`` does;
-* gap-junction partners come from the shared Delaunay edge (BETSE finds the
-  same pairs by a radius search on membrane midpoints); a membrane with no
-  partner in the cluster is a boundary membrane, paired with itself;
-* cells are ordered along a Z-order curve so that gap-junction partners sit
-  close in memory.
-
-The result is a ``ClusterGeometry`` plus the initial-state helpers the step
-needs; clip-edge refinement of the reference mesh is not reproduced (boundary
-cells are whole Voronoi cells).
+``workload`` adds the step parameters, diffusivities and initial state of
+the seeded synthetic workloads; ``sweep_workload`` a batch of them.
 """
 from __future__ import annotations
 
+import ctypes as ct
 from dataclasses import dataclass
 
 import numpy as np
 
+from . import _lib
 from .cluster import ClusterGeometry, StepParams
 
 ION_NAMES = ['Na', 'K', 'Cl', 'Ca', 'P', 'M']
@@ -41,35 +39,6 @@ CELL_CONC = {'Na': 8.0, 'K': 125.0, 'Cl': 10.0, 'Ca': 1e-4, 'P': 100.0}
 ENV_CONC = {'Na': 145.0, 'K': 5.0, 'Cl': 105.0, 'Ca': 1.0, 'P': 10.0}
 Z = {'Na': 1, 'K': 1, 'Cl': -1, 'Ca': 2, 'P': -1, 'M': -1}
 D_FREE = {'Na': 1.33e-9, 'K': 1.96e-9, 'Cl': 2.03e-9, 'Ca': 1.0e-10, 'P': 0.0, 'M': 1.0e-9}
-
-
-def hex_lattice(wsx, wsy, d_cell, disorder, rs):
-    """BETSE's hexagonal seed lattice (cells.py:742-801) with jitter from ``rs``."""
-    r = d_cell / 2
-    a_hex = np.sqrt(3) * r
-    b_hex = 3 * r
-    bx = np.linspace(0, wsy, int(wsy / b_hex))
-    by = np.linspace(a_hex / 2, wsx - a_hex / 2, int((wsx - a_hex) / a_hex))
-    rx = np.linspace(b_hex / 2, wsy - b_hex / 2, int((wsy - b_hex) / b_hex))
-    ry = np.linspace(0, wsx, int(wsx / a_hex))
-    xb, yb = np.meshgrid(bx, by)
-    xr, yr = np.meshgrid(rx, ry)
-    x = np.hstack((xb.ravel(), xr.ravel()))
-    y = np.hstack((yb.ravel(), yr.ravel()))
-    x = x + disorder * d_cell * (rs.rand(len(x)) - 0.5)
-    y = y + disorder * d_cell * (rs.rand(len(y)) - 0.5)
-    return np.column_stack((x, y))
-
-
-def _zorder(xy, bits=16):
-    lo = xy.min(axis=0)
-    span = np.maximum(xy.max(axis=0) - lo, 1e-30)
-    q = ((xy - lo) / span * (2 ** bits - 1)).astype(np.uint64)
-    key = np.zeros(len(xy), np.uint64)
-    for b in range(bits):
-        key |= ((q[:, 0] >> np.uint64(b)) & np.uint64(1)) << np.uint64(2 * b)
-        key |= ((q[:, 1] >> np.uint64(b)) & np.uint64(1)) << np.uint64(2 * b + 1)
-    return key
 
 
 @dataclass
@@ -83,39 +52,93 @@ class GeneratedCluster:
     ymax: float
     world: float       # side of the square world (p.wsx after the disorder margin)
 
+def world_size(radius, d_cell=10e-6, disorder=0.4):
+    """(world, wsx): the side of BETSE's square world for a disc of
+    ``radius`` (world_len = 2 R + 20 um) and the lattice's side with the
+    disorder margin."""
+    world = 2 * radius + 20e-6
+    return world, world + 5 * disorder * d_cell
 
-def poly_centroid(P):
-    """Area centroid of a polygon (vertices in order), as DECMesh.poly_centroid."""
-    Q = np.roll(P, -1, axis=0)
-    a = P[:, 0] * Q[:, 1] - Q[:, 0] * P[:, 1]
-    A = a.sum() / 2
-    return np.array([((P[:, 0] + Q[:, 0]) * a).sum(), ((P[:, 1] + Q[:, 1]) * a).sum()]) / (6 * A)
+
+def lattice_rows(wsx, wsy, d_cell):
+    """The four linspace rows of ``_make_cell_lattice`` (cells.py:742-801):
+    ((start, stop, count) of bx, by, rx, ry)."""
+    r = d_cell / 2
+    a_hex = np.sqrt(3) * r
+    b_hex = 3 * r
+    return ((0.0, wsy, int(wsy / b_hex)),
+            (a_hex / 2, wsx - a_hex / 2, int((wsx - a_hex) / a_hex)),
+            (b_hex / 2, wsy - b_hex / 2, int((wsy - b_hex) / b_hex)),
+            (0.0, wsx, int(wsx / a_hex)))
 
 
-def _centroid_voronoi(pts):
-    """Delaunay triangulation of ``pts`` and, per point, its triangles in
-    counter-clockwise order; the Voronoi vertices are triangle centroids
-    (DECMesh(use_centroids=True)).  Returns (simplices, triangle centroids,
-    fan triangle ids, fan pointer, hull mask)."""
-    from scipy.spatial import Delaunay
-    tri = Delaunay(pts)
-    simp = tri.simplices
-    tcent = pts[simp].mean(axis=1)
-    n = len(pts)
-    owner = simp.ravel()
-    tid = np.repeat(np.arange(len(simp)), 3)
-    ang = np.arctan2(tcent[tid, 1] - pts[owner, 1], tcent[tid, 0] - pts[owner, 0])
-    order = np.lexsort((ang, owner))
-    owner, tid = owner[order], tid[order]
-    fan_ptr = np.concatenate([[0], np.cumsum(np.bincount(owner, minlength=n))])
-    hull = np.zeros(n, bool)
-    hull[np.unique(tri.convex_hull.ravel())] = True
-    return simp, tcent, tid, fan_ptr, hull
+def gen_spec(radius, seed, d_cell=10e-6, disorder=0.4, cell_height=1e-5, scale_cell=0.99, grid_size=20):
+    wsx = world_size(radius, d_cell, disorder)[1]
+    (bx0, bx1, nbx), (by0, by1, nby), (rx0, rx1, nrx), (ry0, ry1, nry) = lattice_rows(wsx, wsx, d_cell)
+    return _lib.BxGenSpec(seed=int(seed), grid_size=int(grid_size), nbx=nbx, nby=nby, nrx=nrx, nry=nry,
+                          bx0=bx0, bx1=bx1, by0=by0, by1=by1, rx0=rx0, rx1=rx1, ry0=ry0, ry1=ry1,
+                          jitter=disorder * d_cell, radius=radius, d_cell=d_cell, cell_radius=d_cell / 2,
+                          scale_cell=scale_cell, cell_height=cell_height)
+
+
+class _Generated:
+    """A ``bx_generate_cluster`` result on the device."""
+
+    def __init__(self, spec, stream=None):
+        self.lib = _lib.load()
+        h = ct.c_void_p()
+        _lib.check(self.lib.bx_generate_cluster(ct.byref(spec), stream, ct.byref(h)), 'bx_generate_cluster')
+        self.h = h
+        sizes = np.zeros(6, np.int32)
+        box = np.zeros(5, np.float64)
+        _lib.check(self.lib.bx_generated_info(self.h, _lib.iptr(sizes), _lib.dptr(box)), 'bx_generated_info')
+        self.C, self.M, self.gny, self.gnx, self.E, self.L = (int(v) for v in sizes)
+        self.box = box
+
+    def download(self, lattice=False):
+        n = {'C': self.C, 'M': self.M, 'G': self.gny * self.gnx, 'E': self.E, 'L': self.L}
+        shapes = {'cell_mem_ptr': n['C'] + 1, 'cell_nn_ptr': n['C'] + 1, 'cell_nn': n['E'],
+                  'mem_sa_per_env': n['G'], 'lattice_x': n['L'], 'lattice_y': n['L']}
+        cells = {'cell_vol', 'cell_sa', 'diviterm', 'cell_centre_x', 'cell_centre_y'}
+        out, ptrs = {}, {}
+        for name, t in _lib.GEN_ARRAYS:
+            if name.startswith('lattice') and not lattice:
+                continue
+            size = shapes.get(name, n['C'] if name in cells else n['M'])
+            a = np.zeros(size, np.int32 if t == 'i' else np.float64)
+            out[name] = a
+            ptrs[name] = _lib.iptr(a) if t == 'i' else _lib.dptr(a)
+        arr = _lib.BxGenArrays(**ptrs)
+        _lib.check(self.lib.bx_generated_download(self.h, ct.byref(arr)), 'bx_generated_download')
+        return out
+
+    def close(self):
+        if getattr(self, 'h', None) is not None and self.h.value:
+            self.lib.bx_generated_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def seed_lattice(radius, seed, d_cell=10e-6, disorder=0.4):
+    """BETSE's jittered seed lattice for a disc of ``radius``, made on the GPU
+    (the ``lattice_x``/``lattice_y`` of ``bx_generate_cluster``)."""
+    g = _Generated(gen_spec(radius, seed, d_cell, disorder))
+    try:
+        d = g.download(lattice=True)
+    finally:
+        g.close()
+    return np.column_stack((d['lattice_x'], d['lattice_y']))
 
 
 def make_cluster(radius, seed, d_cell=10e-6, disorder=0.4, cell_height=1e-5,
-                 cell_space=26e-9, scale_cell=0.99, grid_size=20, smooth_cells=2.0):
-    """A jittered-hex Voronoi cluster clipped to a disc of ``radius`` (m).
+                 cell_space=26e-9, scale_cell=0.99, grid_size=20, smooth_cells=2.0, stream=None):
+    """A jittered-hex Voronoi cluster clipped to a disc of ``radius`` (m),
+    generated on the current CUDA device.
 
     BETSE's seeding (Cells.make_world -> DECMesh.clip_and_refine,
     math/mesh.py:189, 2290-2372) in two passes: the centroid-Voronoi cells of
@@ -128,121 +151,27 @@ def make_cluster(radius, seed, d_cell=10e-6, disorder=0.4, cell_height=1e-5,
     outer cells of the second along the cut; here the first-pass cells are
     whole and the outer ring of the second pass (open Voronoi fans) is left
     out, so the interior is BETSE's and the boundary ring differs."""
-    cell_radius = d_cell / 2
-    world = 2 * radius + 20e-6
-    # the world of BETSE's configuration: world_len plus the disorder margin
-    wsx = wsy = world + 5 * disorder * d_cell
-    rs = np.random.RandomState(seed)
-    lat = hex_lattice(wsx, wsy, d_cell, disorder, rs)
-    centre = lat.mean(axis=0)
-    lo, hi = lat.min(axis=0), lat.max(axis=0)
-    xmin, ymin = lo - cell_radius
-    xmax, ymax = hi + cell_radius
-    # first pass: the lattice and its bounding-box corners
-    corners = np.array([[lo[0], lo[1]], [hi[0], lo[1]], [hi[0], hi[1]], [lo[0], hi[1]]])
-    allp = np.vstack([lat, corners])
-    simp0, tcent0, tid0, fan0, hull0 = _centroid_voronoi(allp)
-    first = [s for s in range(len(lat)) if not hull0[s] and fan0[s + 1] - fan0[s] >= 3]
-    c0 = np.array([poly_centroid(tcent0[tid0[fan0[s]:fan0[s + 1]]]) for s in first])
-    pts = c0[np.hypot(c0[:, 0] - centre[0], c0[:, 1] - centre[1]) < radius]
-
-    # second pass: the cells of the rebuilt mesh
-    simp, tcent, tid, fan_ptr, hull = _centroid_voronoi(pts)
-    n = len(pts)
-    keep = (~hull) & (np.diff(fan_ptr) >= 3)
-    seeds = np.nonzero(keep)[0]
-    # polygon of each kept seed, then cell order along a Z curve of the centroid
-    polys = [tcent[tid[fan_ptr[s]:fan_ptr[s + 1]]] for s in seeds]
-    cents = np.array([poly_centroid(p) for p in polys])
-    zo = np.argsort(_zorder(cents), kind='stable')
-    seeds = seeds[zo]
-    polys = [polys[i] for i in zo]
-    C = len(seeds)
-    seed_to_cell = -np.ones(n, np.int64)
-    seed_to_cell[seeds] = np.arange(C)
-
-    counts = np.array([len(p) for p in polys])
-    M = int(counts.sum())
-    ptr = np.concatenate([[0], np.cumsum(counts)])
-    m2c = np.repeat(np.arange(C), counts)
-    # vertices scaled toward the cell centre, the area centroid (cellVerts: p.scale_cell)
-    poly_c = cents[zo]
-    V = np.concatenate(polys)
-    V = scale_cell * (V - poly_c[m2c]) + poly_c[m2c]
-    # membrane k of a cell joins vertex k-1 and vertex k (cellVerts' loop)
-    prev = np.arange(M) - 1
-    prev[ptr[:-1]] = ptr[1:] - 1
-    p1, p2 = V[prev], V[np.arange(M)]
-    mids = (p1 + p2) / 2
-    tang = p2 - p1
-    length = np.hypot(tang[:, 0], tang[:, 1])
-    tang = tang / length[:, None]
-    nx, ny = tang[:, 1], -tang[:, 0]
-    mem_sa = length * cell_height
-    # cell centre: BETSE's cell_centres are polygon centroids of the unscaled cells
-    rad = mids - poly_c[m2c]
-    R_rads = np.hypot(rad[:, 0], rad[:, 1])
-    mem_vol = 0.5 * R_rads * mem_sa
-    cell_vol = np.bincount(m2c, weights=mem_vol, minlength=C)
-    cell_sa = np.bincount(m2c, weights=mem_sa, minlength=C)
-    diviterm = cell_vol / cell_sa
-
-    # gap junction partners: the edge between triangles (t_prev, t) around seed s is
-    # the Voronoi edge dual to the Delaunay edge (s, other); pair by that edge.
-    t_prev = tid[np.concatenate([fan_ptr[s] + (np.arange(c) - 1) % c for s, c in
-                                 zip(seeds, counts)])] if C else np.zeros(0, np.int64)
-    t_cur = tid[np.concatenate([fan_ptr[s] + np.arange(c) for s, c in zip(seeds, counts)])]
-    own_seed = seeds[m2c]
-    a, b = simp[t_prev], simp[t_cur]
-    # the shared vertex of the two triangles that is not the owner seed
-    other = np.full(M, -1, np.int64)
-    for ka in range(3):
-        for kb in range(3):
-            same = (a[:, ka] == b[:, kb]) & (a[:, ka] != own_seed)
-            other = np.where(same & (other < 0), a[:, ka], other)
-    key_lo = np.minimum(own_seed, other)
-    key_hi = np.maximum(own_seed, other)
-    nn = np.arange(M)
-    valid = (other >= 0) & (seed_to_cell[np.maximum(other, 0)] >= 0)
-    idx = np.nonzero(valid)[0]
-    keys = key_lo[idx] * (n + 1) + key_hi[idx]
-    o = np.argsort(keys, kind='stable')
-    ks, ix = keys[o], idx[o]
-    pair = np.nonzero(ks[1:] == ks[:-1])[0]
-    nn[ix[pair]] = ix[pair + 1]
-    nn[ix[pair + 1]] = ix[pair]
-    bflags = np.nonzero(nn == np.arange(M))[0]
-
-    # environment grid (makeECM / FiniteDiffSolver.cell_grid, environment)
-    delta = (xmax - xmin) / grid_size
-    gnx = int((xmax - xmin) / delta)
-    gny = int((ymax - ymin) / delta)
-    xv = np.linspace(xmin, xmax, gnx + 1)
-    yv = np.linspace(ymin, ymax, gny + 1)
-    cx = (xv[:-1] + xv[1:]) / 2
-    cy = (yv[:-1] + yv[1:]) / 2
-    jx = np.clip(np.searchsorted(cx, mids[:, 0]), 1, gnx - 1)
-    jx = np.where(np.abs(cx[jx - 1] - mids[:, 0]) <= np.abs(cx[jx] - mids[:, 0]), jx - 1, jx)
-    iy = np.clip(np.searchsorted(cy, mids[:, 1]), 1, gny - 1)
-    iy = np.where(np.abs(cy[iy - 1] - mids[:, 1]) <= np.abs(cy[iy] - mids[:, 1]), iy - 1, iy)
-    map_env = iy * gnx + jx
-    msa_env = np.bincount(map_env, weights=mem_sa, minlength=gnx * gny)
-
-    # cell adjacency (near_neigh's cell_nn) for the warm-start network
-    part = nn != np.arange(M)
-    src, dst = m2c[part], m2c[nn[part]]
-    oo = np.lexsort((dst, src))
-    src, dst = src[oo], dst[oo]
-    cnn_ptr = np.concatenate([[0], np.cumsum(np.bincount(src, minlength=C))])
-
+    world = world_size(radius, d_cell, disorder)[1]
+    g = _Generated(gen_spec(radius, seed, d_cell, disorder, cell_height, scale_cell, grid_size), stream)
+    try:
+        d = g.download()
+    finally:
+        g.close()
+    xmin, xmax, ymin, ymax, delta = (float(v) for v in g.box)
+    ptr = d['cell_mem_ptr']
+    C, M = g.C, g.M
+    m2c = np.repeat(np.arange(C), np.diff(ptr))
+    nn = d['nn_i'].astype(np.int64)
     geom = ClusterGeometry.from_arrays(
-        mem_to_cells=m2c, nn_i=nn, bflags_mems=bflags, map_mem2ecm=map_env,
-        mem_sa=mem_sa, mem_nx=nx, mem_ny=ny, gj_weight=np.ones(M), cell_vol=cell_vol,
-        cell_sa=cell_sa, diviterm=diviterm, grid_shape=(gny, gnx), delta=delta,
-        gj_len=cell_space, smooth_cells=smooth_cells, mem_sa_per_env=msa_env,
-        D_env_weight=np.ones(gnx * gny), cell_nn_ptr=cnn_ptr, cell_nn=dst, R_rads=R_rads)
-    return GeneratedCluster(geom=geom, cell_centres=poly_c, mem_mids=mids,
-                            xmin=xmin, xmax=xmax, ymin=ymin, ymax=ymax, world=wsx)
+        mem_to_cells=m2c, nn_i=nn, bflags_mems=np.nonzero(nn == np.arange(M))[0],
+        map_mem2ecm=d['map_mem2ecm'], mem_sa=d['mem_sa'], mem_nx=d['mem_nx'], mem_ny=d['mem_ny'],
+        gj_weight=np.ones(M), cell_vol=d['cell_vol'], cell_sa=d['cell_sa'], diviterm=d['diviterm'],
+        grid_shape=(g.gny, g.gnx), delta=delta, gj_len=cell_space, smooth_cells=smooth_cells,
+        mem_sa_per_env=d['mem_sa_per_env'], D_env_weight=np.ones(g.gny * g.gnx),
+        cell_nn_ptr=d['cell_nn_ptr'], cell_nn=d['cell_nn'], R_rads=d['R_rads'])
+    return GeneratedCluster(geom=geom, cell_centres=np.column_stack((d['cell_centre_x'], d['cell_centre_y'])),
+                            mem_mids=np.column_stack((d['mem_mid_x'], d['mem_mid_y'])),
+                            xmin=xmin, xmax=xmax, ymin=ymin, ymax=ymax, world=world)
 
 
 def charge_balanced(conc):
@@ -255,15 +184,18 @@ def charge_balanced(conc):
 
 def workload(radius, seed, is_ecm=False, dt=1e-2, dm_range=(1e-19, 1e-17),
              grid_size=20, cell_space=26e-9, alpha_NaK=5e-8, gj_range=(0.5, 1.0),
-             na_k_dm_mult=1.0, pump_mult=1.0):
+             na_k_dm_mult=1.0, pump_mult=1.0, cluster=None):
     """Cluster + parameters + initial state of the seeded synthetic workload.
 
     Returns (geom, params, Dm, state dict, D_env). Diffusivities are
     log-uniform in ``dm_range`` per membrane and ion (Dm_P = 0), gap-junction
     weights uniform in ``gj_range`` per membrane pair; draws come from
     ``np.random.default_rng(seed + 1)``, the lattice from ``RandomState(seed)``.
+    ``cluster`` (a ``GeneratedCluster`` of the same radius and seed) skips
+    the generation.
     """
-    gc = make_cluster(radius, seed, grid_size=grid_size, cell_space=cell_space)
+    gc = cluster if cluster is not None else make_cluster(radius, seed, grid_size=grid_size,
+                                                          cell_space=cell_space)
     g = gc.geom
     M, C, G = g.n_mems, g.n_cells, g.n_grid
     rng = np.random.default_rng(seed + 1)
@@ -309,24 +241,13 @@ def cell_conc_vec(cell):
     return np.array([cell[k] for k in ION_NAMES], np.float64)
 
 
-def _sweep_member(args):
-    k, n_cells, seed, na_k_mult, pump_mult, dt, dm_range = args
-    R = np.sqrt(n_cells / 0.0456) * 1e-6       # cells ~ 0.0456 (R / 1 um)^2 for this lattice
-    g, p, Dm, st, _ = workload(R, seed, dt=dt, dm_range=dm_range, na_k_dm_mult=na_k_mult,
-                               pump_mult=pump_mult)
-    return k, g, p, Dm, st
-
-
 def sweep_workload(n_clusters=512, seed=7, cells_range=(200, 5000), mult_range=(0.1, 10.0),
-                   dt=5e-3, dm_range=(1e-19, 1e-17), workers=None, pump_range=None):
+                   dt=5e-3, dm_range=(1e-19, 1e-17), pump_range=None):
     """A parameter sweep: ``n_clusters`` independent clusters with cell counts
     log-uniform in ``cells_range`` and per-cluster Na/K diffusivity and pump
     multipliers log-uniform in ``mult_range`` (the pump's in ``pump_range`` when
-    given). Clusters are generated in a
-    spawn-started process pool. Returns lists (geoms, params, Dms, states)."""
-    import concurrent.futures as cf
-    import multiprocessing as mp
-    import os
+    given), each generated on the GPU in turn. Returns lists (geoms, params,
+    Dms, states)."""
     rng = np.random.default_rng(seed)
     lo, hi = np.log(cells_range[0]), np.log(cells_range[1])
     counts = np.exp(rng.uniform(lo, hi, n_clusters))
@@ -334,16 +255,11 @@ def sweep_workload(n_clusters=512, seed=7, cells_range=(200, 5000), mult_range=(
     pr = mult_range if pump_range is None else pump_range
     dmm = np.exp(rng.uniform(ml, mh, n_clusters))
     pmm = np.exp(rng.uniform(np.log(pr[0]), np.log(pr[1]), n_clusters))
-    jobs = [(k, float(counts[k]), seed * 1000 + k, float(dmm[k]), float(pmm[k]), dt, dm_range)
-            for k in range(n_clusters)]
-    workers = workers or min(16, os.cpu_count() or 1)
-    out = [None] * n_clusters
-    if workers > 1:
-        with cf.ProcessPoolExecutor(workers, mp_context=mp.get_context('spawn')) as ex:
-            for k, g, p, Dm, st in ex.map(_sweep_member, jobs, chunksize=8):
-                out[k] = (g, p, Dm, st)
-    else:
-        for j in jobs:
-            k, g, p, Dm, st = _sweep_member(j)
-            out[k] = (g, p, Dm, st)
-    return ([o[0] for o in out], [o[1] for o in out], [o[2] for o in out], [o[3] for o in out])
+    out = ([], [], [], [])
+    for k in range(n_clusters):
+        R = np.sqrt(float(counts[k]) / 0.0456) * 1e-6   # cells ~ 0.0456 (R / 1 um)^2 for this lattice
+        g, p, Dm, st, _ = workload(R, seed * 1000 + k, dt=dt, dm_range=dm_range,
+                                   na_k_dm_mult=float(dmm[k]), pump_mult=float(pmm[k]))
+        for lst, v in zip(out, (g, p, Dm, st)):
+            lst.append(v)
+    return out

@@ -311,6 +311,51 @@ int bx_dense_op_status(bx_dense_op_handle op, int* timed_out);
 int bx_dense_op_time(bx_dense_op_handle op, const double* X, double* Y, int nrhs,
                      int n_iter, double* ms);
 int bx_dense_op_destroy(bx_dense_op_handle op);
+/* An operator built on the device: zero planes, then column blocks (device
+ * src [n x ncols] row-major, col0 a multiple of 64, ncols a multiple of 64
+ * unless the block ends at n), asynchronous on `stream`. */
+int bx_dense_op_create_empty(int n, bx_dense_op_handle* out);
+int bx_dense_op_set_columns(bx_dense_op_handle op, int col0, int ncols, const double* src, void* stream);
+
+/* Cells.graphLaplacian at any cluster size (cells.py:1845-1894):
+ *   lapGJinv = pinv(D) diag(tri_len/vor_len) (-pinv(D)^T) diag(vor_sa)
+ *            = -L+ Lw L+ A
+ * with L = D^T D the graph Laplacian of the triangulation's edges D, L+ its
+ * pseudo-inverse, Lw = D^T diag(tri_len/vor_len) D and A = diag(vor_sa);
+ * np.dot(cells.lapGJinv, .) at physics/pressures.py:59.  L+ is applied by
+ * FP64 conjugate gradients per right-hand side, preconditioned by an
+ * aggregation multigrid V-cycle.  levels[0] is L (n nodes); level l+1 is
+ * the Galerkin operator of level l's aggregates of 4 consecutive nodes
+ * (node i -> i / 4), down to the coarsest level, whose pseudo-inverse
+ * [nc x nc] row-major is coarse_pinv; host CSR arrays, copied.  `weighted`
+ * is Lw, vor_sa [n] the cell areas.  max_rhs bounds nrhs (the workspace is
+ * 12 n max_rhs doubles).  Right-hand sides and results are DEVICE arrays
+ * [n x nrhs] row-major; a solve stops when every column's residual is below
+ * tol relative to its right-hand side (checked every 4 iterations) or after
+ * max_iter iterations; iters and rel_res report the worst column. */
+typedef struct bx_graph_level {
+    int32_t n, nnz;
+    const int32_t* row_ptr;
+    const int32_t* col;
+    const double* val;
+} bx_graph_level;
+typedef struct bx_graph_solver* bx_graph_handle;
+int bx_graph_create(int n_levels, const bx_graph_level* levels, const double* coarse_pinv,
+                    const bx_graph_level* weighted, const double* vor_sa, int max_rhs,
+                    bx_graph_handle* out);
+/* X = L+ B (B's component along the constants is removed first) */
+int bx_graph_solve(bx_graph_handle h, const double* B, double* X, int nrhs, double tol, int max_iter,
+                   int* iters, double* rel_res, void* stream);
+/* Y = lapGJinv X, FP64, two solves */
+int bx_lap_gj_apply(bx_graph_handle h, const double* X, double* Y, int nrhs, double tol, int max_iter,
+                    int* iters, double* rel_res, void* stream);
+/* the dense lapGJinv as a BF16x3 tensor-core operator (bx_dense_op_*), built
+ * column block by column block (max_rhs rounded down to 64 columns per
+ * block) from bx_lap_gj_apply on scaled identity columns; no n x n FP64
+ * matrix is formed */
+int bx_lap_gj_dense(bx_graph_handle h, double tol, int max_iter, int* iters, double* rel_res,
+                    void* stream, bx_dense_op_handle* out);
+int bx_graph_destroy(bx_graph_handle h);
 
 /* Warm-start graph network (no reference counterpart: BETSE's init phase
  * always starts from the uniform profile).  A 3-layer, 64-wide message-passing
@@ -531,6 +576,58 @@ int bx_network_time_step(bx_network_handle n, int n_steps, int with_ions, double
 /* info[4] = {substances, reactions, n_cells, n_mems}. */
 int bx_network_info(bx_network_handle n, int32_t* info);
 int bx_network_destroy(bx_network_handle n);
+
+/* ---- synthetic clusters on the GPU (Cells.make_world's seeding,
+ * cells.py:414-961; _make_cell_lattice :742-801; DECMesh.clip_and_refine's
+ * two passes, math/mesh.py:189,2290-2372; cellVerts :978-1175; cell_vols
+ * :1358-1390; near_neigh :1477-1573; makeECM/environment :1576-1843).
+ *
+ * The lattice is BETSE's bit for bit: numpy.linspace rows (the caller passes
+ * each row's start, stop and count, computed as _make_cell_lattice does) and
+ * the jitter jitter * (rand - 0.5), x draws then y draws, from MT19937 seeded
+ * as numpy.random.RandomState(seed).  Pass one: the centroid-Voronoi cell of
+ * each lattice point (with the lattice's bounding-box corners added) and its
+ * area centroid; the centroids inside the disc of `radius` about the
+ * lattice's mean are the points of pass two, whose closed cells are the
+ * cluster, ordered along a Z curve of their area centroids.  Membranes are
+ * each cell's polygon edges scaled by scale_cell about its centre, listed as
+ * cellVerts lists them; gap-junction partners are the membranes across each
+ * shared Delaunay edge (a membrane without one is paired with itself); the
+ * grid is the lattice box widened by cell_radius, grid_size cells wide. */
+typedef struct bx_gen_spec {
+    uint32_t seed;          /* numpy.random.RandomState seed of the jitter */
+    int32_t grid_size;      /* p.grid_size */
+    int32_t nbx, nby, nrx, nry;                 /* linspace counts of the four rows */
+    double bx0, bx1, by0, by1, rx0, rx1, ry0, ry1;   /* their starts and stops */
+    double jitter;          /* p.cell_lattice_disorder * d_cell */
+    double radius;          /* disc radius (m) */
+    double d_cell;          /* lattice spacing (m) */
+    double cell_radius;     /* d_cell / 2 */
+    double scale_cell;      /* p.scale_cell */
+    double cell_height;     /* p.cell_height */
+} bx_gen_spec;
+
+typedef struct bx_gen_arrays {      /* destinations, host or device; NULL skips */
+    int32_t* cell_mem_ptr;          /* [C+1] */
+    int32_t* nn_i;                  /* [M] */
+    int32_t* map_mem2ecm;           /* [M] */
+    double *mem_sa, *mem_nx, *mem_ny, *R_rads, *mem_mid_x, *mem_mid_y;   /* [M] */
+    double *cell_vol, *cell_sa, *diviterm, *cell_centre_x, *cell_centre_y;  /* [C] */
+    double* mem_sa_per_env;         /* [grid_ny * grid_nx] */
+    int32_t* cell_nn_ptr;           /* [C+1] */
+    int32_t* cell_nn;               /* [n_cell_nn]: each cell's neighbours, ascending */
+    double *lattice_x, *lattice_y;  /* [n_lattice] the jittered seed lattice */
+} bx_gen_arrays;
+
+typedef struct bx_generated* bx_gen_handle;
+/* Runs the whole generation on `stream` (allocates; returns when done).
+ * BX_EINVAL on a bad specification or a degenerate point set. */
+int bx_generate_cluster(const bx_gen_spec* spec, void* stream, bx_gen_handle* out);
+/* sizes[6] = {C, M, grid_ny, grid_nx, n_cell_nn, n_lattice};
+ * box[5] = {xmin, xmax, ymin, ymax, delta} of the environment grid. */
+int bx_generated_info(bx_gen_handle g, int32_t* sizes, double* box);
+int bx_generated_download(bx_gen_handle g, const bx_gen_arrays* a);
+int bx_generated_destroy(bx_gen_handle g);
 
 #ifdef __cplusplus
 }

@@ -1,4 +1,5 @@
-"""The synthetic cluster generator against BETSE's own Cells at the same seed
+"""The NumPy restatement of the cluster generator (oracle/generator.py, the
+checker of the GPU generator) against BETSE's own Cells at the same seed
 and radius (tests/golden/cells_lattice.npz, written by make_golden.py from
 BETSE's _make_cell_lattice, DECMesh.clip_and_refine and Cells methods).
 
@@ -30,7 +31,7 @@ def fx():
 
 @pytest.mark.parametrize('key', sorted(CASES))
 def test_lattice_is_betse_bit_for_bit(fx, key):
-    from betse_gb300.generator import hex_lattice
+    from oracle.generator import hex_lattice
     radius, seed = CASES[key]
     wsx = float(fx[f'{key}_wsx'])
     assert np.isclose(wsx, 2 * radius + 20e-6 + 5 * 0.4 * 10e-6)   # world_len + the disorder margin
@@ -53,7 +54,7 @@ def test_interior_cells_match_betse(fx, key):
     away; an exact cell whose neighbours are exact too has BETSE's membrane
     count, gap-junction neighbours, membrane areas and volume (1e-9)."""
     from scipy.spatial import cKDTree
-    from betse_gb300.generator import make_cluster
+    from oracle.generator import make_cluster
     radius, seed = CASES[key]
     gc = make_cluster(radius, seed)
     g = gc.geom
@@ -92,7 +93,7 @@ def test_boundary_ring_deviation_is_bounded(fx, key):
     the open outer ring of its second pass.  Cell counts agree within 25 %
     and every generated cell is within 0.3 d_cell of a BETSE cell."""
     from scipy.spatial import cKDTree
-    from betse_gb300.generator import make_cluster
+    from oracle.generator import make_cluster
     radius, seed = CASES[key]
     gc = make_cluster(radius, seed)
     Cb = len(fx[f'{key}_cell_centres'])

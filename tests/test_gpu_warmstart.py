@@ -27,7 +27,7 @@ def test_prediction_is_a_consistent_state():
     from betse_gb300 import warmstart as ws
     w = ws.WarmStart()
     gs, ps, Dms, sts = gen.sweep_workload(4, 777, cells_range=(800, 1200), dt=ws.DT,
-                                          mult_range=ws.MULT_RANGE, pump_range=ws.PUMP_RANGE, workers=1)
+                                          mult_range=ws.MULT_RANGE, pump_range=ws.PUMP_RANGE)
     pred, _ = w.predict(gs, ps, Dms)
     for g, p, s, y in zip(gs, ps, sts, pred):
         assert y.shape == (g.n_cells, ws.N_OUT) and np.all(np.isfinite(y))

@@ -3,10 +3,13 @@ import numpy as np
 
 from betse_gb300 import generator as gen
 from betse_gb300 import warmstart as ws
+from oracle import generator as ogen
 
 
 def _cluster():
-    return gen.workload(np.sqrt(300 / 0.0456) * 1e-6, 21, dt=1e-2)
+    # the NumPy restatement of the generator stands in for the GPU one here
+    R = np.sqrt(300 / 0.0456) * 1e-6
+    return gen.workload(R, 21, dt=1e-2, cluster=ogen.make_cluster(R, 21))
 
 
 def test_identity_prediction_reproduces_initial_state():
