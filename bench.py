@@ -608,6 +608,62 @@ def dense_products(stream, flush, wl_ecm):
     return out
 
 
+def lap_gj_timing(wl_full, wl_ecm, dense_full=False):
+    """cells.lapGJinv (Cells.graphLaplacian) of the generated clusters:
+    the matrix-free FP64 product (two multigrid-preconditioned CG solves,
+    bx_lap_gj_apply) at 100k cells for one right-hand side (pressures.py:59
+    applies it to one vector per step) and for a block of 32; the dense
+    operator built on the GPU from it and applied as a BF16x3 tcgen05 GEMM,
+    with its error against the FP64 product, at 20k cells (and at 100k cells
+    with dense_full: a build of several minutes)."""
+    import torch
+    from betse_gb300.dense import LapGJ, lap_gj_inputs
+
+    def sync():
+        torch.cuda.synchronize()
+
+    out = {}
+    g = wl_full[1]
+    gen = torch.Generator('cuda').manual_seed(11)
+    with LapGJ(*lap_gj_inputs(g, g.extra['cell_centres']), max_rhs=32) as op:
+        res = {'cells': g.n_cells, 'levels': op.level_sizes, 'tol': 1e-10}
+        for K in (1, 32):
+            X = torch.randn(g.n_cells, K, dtype=torch.float64, device='cuda', generator=gen)
+            op.apply(X, tol=1e-10)
+            sync()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                op.apply(X, tol=1e-10)
+            sync()
+            res[f'ms_apply_{K}_rhs'] = (time.perf_counter() - t0) / 3 * 1e3
+            res[f'cg_iterations_{K}_rhs'] = op.last_iters
+        out['matrix_free_fp64'] = res
+    cases = [wl_ecm] + ([wl_full] if dense_full else [])
+    for wl in cases:
+        g = wl[1]
+        with LapGJ(*lap_gj_inputs(g, g.extra['cell_centres']), max_rhs=1024) as op:
+            sync()
+            t0 = time.perf_counter()
+            dense = op.dense(tol=1e-10)
+            sync()
+            build_s = time.perf_counter() - t0
+            try:
+                X = torch.randn(g.n_cells, 256, dtype=torch.float64, device='cuda', generator=gen)
+                ref = op.apply(X, tol=1e-13)
+                Y = dense.apply(X)
+                err = float((Y - ref).abs().max() / ref.abs().max())
+                ms = dense.time(256, 5)
+            finally:
+                dense.close()
+        n = g.n_cells
+        tf = 3 * 2.0 * n * n * 256 / (ms / 1e3) / 1e12
+        out[f'dense_bf16x3_{n}_cells'] = {
+            'build_s': build_s, 'build': 'bx_lap_gj_dense: FP64 CG on blocks of 1024 identity columns, '
+                                          'split into BF16 hi/lo tiles; no n x n FP64 matrix',
+            'gemm_ms_256_rhs': ms, 'tflops': tf, 'rel_err_vs_fp64': err}
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU restatement of BETSE's step on the host cores
     (the C restatement on every OpenMP thread without extracellular spaces,
@@ -746,6 +802,8 @@ def main():
     ap.add_argument('--profile-run', action='store_true',
                     help='for ncu: build the workload, upload it, run 4 steps (or --time-steps), exit')
     ap.add_argument('--precision', default='split', choices=['split', 'fp64'])
+    ap.add_argument('--lapgj-dense-full', action='store_true',
+                    help='also build the dense lapGJinv of the 100k-cell cluster (several minutes)')
     ap.add_argument('--launch', default=None,
                     help='with --profile-run: membrane slots per tile, suffix p persistent, f factored '
                          '(optionally followed by its variant, e.g. 256f12), r resident, q pipelined (e.g. 192r)')
@@ -928,6 +986,8 @@ def main():
         extra = dense_products(stream, flush, others['ecm20k'])
         extra['batch_env_fields'] = batch_fields_timing()
         extra['network'] = network_step(g, p, Dm, st, stream, flush, cpu=cpu_on)
+        extra['lap_gj'] = lap_gj_timing((w, g, p, Dm, st, D_env), others['ecm20k'],
+                                        dense_full=args.lapgj_dense_full)
 
     if rank == 0:
         line = {

@@ -835,7 +835,7 @@ __device__ int nearest_centre(const double* c, int n, double v) {
   return j;
 }
 
-__global__ void k_env_map(int M, const double* __restrict__ mx, const double* __restrict__ my,
+__global__ void k_grid_map(int M, const double* __restrict__ mx, const double* __restrict__ my,
                           const double* __restrict__ cx, int gnx, const double* __restrict__ cy, int gny,
                           int* __restrict__ map, uint32_t* __restrict__ key, int* __restrict__ val) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -847,7 +847,7 @@ __global__ void k_env_map(int M, const double* __restrict__ mx, const double* __
 }
 
 // membrane area per grid cell, summed in membrane order (np.bincount)
-__global__ void k_env_sum(int M, const uint32_t* __restrict__ key, const int* __restrict__ mem,
+__global__ void k_grid_area(int M, const uint32_t* __restrict__ key, const int* __restrict__ mem,
                           const double* __restrict__ sa, double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M || (i > 0 && key[i - 1] == key[i])) return;
@@ -1081,13 +1081,13 @@ void generate(const bx_gen_spec& sp, cudaStream_t s, bx_generated* G) {
   k_grid_centres<<<nblocks(gny, 256), 256, 0, s>>>(ymin, ymax, gny, gcy);
   uint32_t* gk = need<uint32_t>(tmp, M, "grid");
   int* gm = need<int>(tmp, M, "grid");
-  k_env_map<<<nblocks(M, 256), 256, 0, s>>>(M, G->mx, G->my, gcx, gnx, gcy, gny, G->map, gk, gm);
+  k_grid_map<<<nblocks(M, 256), 256, 0, s>>>(M, G->mx, G->my, gcx, gnx, gcy, gny, G->map, gk, gm);
   int gbits = 1;
   while ((1ll << gbits) < (int64_t)gnx * gny) ++gbits;
   radix_sort(tmp, gk, gm, M, gbits, s);
   G->msa_env = need<double>(keep, (size_t)gnx * gny, "grid");
   GEN_CHECK(cudaMemsetAsync(G->msa_env, 0, (size_t)gnx * gny * 8, s), "grid");
-  k_env_sum<<<nblocks(M, 256), 256, 0, s>>>(M, gk, gm, G->sa, G->msa_env);
+  k_grid_area<<<nblocks(M, 256), 256, 0, s>>>(M, gk, gm, G->sa, G->msa_env);
 
   // 6. cell adjacency (near_neigh's cell_nn)
   int* ncnt = need<int>(tmp, C, "adjacency");

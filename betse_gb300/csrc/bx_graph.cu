@@ -57,36 +57,87 @@ int gfail(int code, const std::string& msg) {
     if (e_ != cudaSuccess) return gfail(BX_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-unsigned grid_for(long long n_el) { return (unsigned)std::max<long long>(1, std::min<long long>((n_el + 255) / 256, 152LL * 16)); }
+// Kernels over [rows][K] blocks: a CTA covers kt columns (a power of two up
+// to 256, so that wide blocks read long runs of each row) times 256 / kt
+// rows, and strides over the rows.
+struct Shape {
+  dim3 grid, block;
+};
 
-#define FOR_EL(tot) for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < (tot); t += (long long)gridDim.x * blockDim.x)
+Shape shape_for(int rows, int K) {
+  int kt = 1;
+  while (kt < K && kt < 256) kt <<= 1;
+  const int rpb = 256 / kt;
+  const int gx = (K + kt - 1) / kt;
+  // about 16 CTAs per SM in all, each striding over rows: short-lived CTAs
+  // of one row each cost more to schedule than their work
+  const int gy = std::max(1, std::min((rows + rpb - 1) / rpb, std::max(1, 152 * 16 / gx)));
+  return {dim3((unsigned)gx, (unsigned)gy), dim3((unsigned)kt, (unsigned)rpb)};
+}
+
+#define FOR_RC(rows, K)                                       \
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;        \
+  if (k >= (K)) return;                                       \
+  for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < (rows); i += gridDim.y * blockDim.y)
+
+#define LAUNCH(kern, rows, K, s, ...)                          \
+  do {                                                        \
+    const Shape sh_ = shape_for((rows), (K));                 \
+    kern<<<sh_.grid, sh_.block, 0, (s)>>>(__VA_ARGS__);       \
+  } while (0)
+
+// sum over row i's entries p of val[p] * xv(col[p]), in entry order
+template <class F>
+__device__ __forceinline__ double row_dot(const int* __restrict__ ptr, const int* __restrict__ col,
+                                          const double* __restrict__ val, int i, F xv) {
+  double sum = 0.0;
+  for (int p = ptr[i]; p < ptr[i + 1]; ++p) sum += val[p] * xv(col[p]);
+  return sum;
+}
 
 // out = L in (CSR, rows of K values)
 __global__ void k_spmv(int n, int K, const int* __restrict__ ptr, const int* __restrict__ col,
                        const double* __restrict__ val, const double* __restrict__ in, double* __restrict__ out) {
-  FOR_EL((long long)n * K) {
-    const int i = (int)(t / K), k = (int)(t - (long long)i * K);
-    double s = 0.0;
-    for (int p = ptr[i]; p < ptr[i + 1]; ++p) s += val[p] * in[(long long)col[p] * K + k];
-    out[t] = s;
+  FOR_RC(n, K) {
+    out[(long long)i * K + k] = row_dot(ptr, col, val, i, [&](int j) { return in[(long long)j * K + k]; });
   }
 }
 
-// x = omega D^-1 b (the first Jacobi sweep from x = 0)
-__global__ void k_jacobi0(long long tot, int K, const double* __restrict__ dinv, const double* __restrict__ b,
-                          double* __restrict__ x) {
-  FOR_EL(tot) x[t] = kOmega * dinv[t / K] * b[t];
+// two damped Jacobi sweeps from x = 0: x1 = w D^-1 b, x = x1 + w D^-1 (b - L x1)
+__global__ void k_smooth_pre(int n, int K, const int* __restrict__ ptr, const int* __restrict__ col,
+                             const double* __restrict__ val, const double* __restrict__ dinv,
+                             const double* __restrict__ b, double* __restrict__ x) {
+  FOR_RC(n, K) {
+    const double sum =
+        row_dot(ptr, col, val, i, [&](int j) { return kOmega * dinv[j] * b[(long long)j * K + k]; });
+    const double bi = b[(long long)i * K + k];
+    x[(long long)i * K + k] = kOmega * dinv[i] * bi + kOmega * dinv[i] * (bi - sum);
+  }
 }
 
-// x_out = x_in + omega D^-1 (b - L x_in)
+// the coarse correction and one sweep: xp = x + w_c xc[aggregate],
+// out = xp + w D^-1 (b - L xp)
+__global__ void k_smooth_post(int n, int K, const int* __restrict__ ptr, const int* __restrict__ col,
+                              const double* __restrict__ val, const double* __restrict__ dinv,
+                              const double* __restrict__ b, const double* __restrict__ x,
+                              const double* __restrict__ xc, double* __restrict__ out) {
+  FOR_RC(n, K) {
+    const double sum = row_dot(ptr, col, val, i, [&](int j) {
+      return x[(long long)j * K + k] + kCoarseWeight * xc[(long long)(j / kAgg) * K + k];
+    });
+    const double xi = x[(long long)i * K + k] + kCoarseWeight * xc[(long long)(i / kAgg) * K + k];
+    out[(long long)i * K + k] = xi + kOmega * dinv[i] * (b[(long long)i * K + k] - sum);
+  }
+}
+
+// x_out = x_in + w D^-1 (b - L x_in)
 __global__ void k_jacobi(int n, int K, const int* __restrict__ ptr, const int* __restrict__ col,
                          const double* __restrict__ val, const double* __restrict__ dinv,
                          const double* __restrict__ b, const double* __restrict__ xin, double* __restrict__ xout) {
-  FOR_EL((long long)n * K) {
-    const int i = (int)(t / K), k = (int)(t - (long long)i * K);
-    double s = 0.0;
-    for (int p = ptr[i]; p < ptr[i + 1]; ++p) s += val[p] * xin[(long long)col[p] * K + k];
-    xout[t] = xin[t] + kOmega * dinv[i] * (b[t] - s);
+  FOR_RC(n, K) {
+    const double sum = row_dot(ptr, col, val, i, [&](int j) { return xin[(long long)j * K + k]; });
+    const long long t = (long long)i * K + k;
+    xout[t] = xin[t] + kOmega * dinv[i] * (b[t] - sum);
   }
 }
 
@@ -94,102 +145,111 @@ __global__ void k_jacobi(int n, int K, const int* __restrict__ ptr, const int* _
 __global__ void k_restrict(int n, int nc, int K, const int* __restrict__ ptr, const int* __restrict__ col,
                            const double* __restrict__ val, const double* __restrict__ b,
                            const double* __restrict__ x, double* __restrict__ bc) {
-  FOR_EL((long long)nc * K) {
-    const int a = (int)(t / K), k = (int)(t - (long long)a * K);
+  FOR_RC(nc, K) {
     double r = 0.0;
-    for (int i = a * kAgg; i < min(a * kAgg + kAgg, n); ++i) {
-      double s = 0.0;
-      for (int p = ptr[i]; p < ptr[i + 1]; ++p) s += val[p] * x[(long long)col[p] * K + k];
-      r += b[(long long)i * K + k] - s;
+    for (int m = i * kAgg; m < min(i * kAgg + kAgg, n); ++m) {
+      const double sum = row_dot(ptr, col, val, m, [&](int j) { return x[(long long)j * K + k]; });
+      r += b[(long long)m * K + k] - sum;
     }
-    bc[t] = r;
-  }
-}
-
-// x += w xc[aggregate]
-__global__ void k_prolong(long long tot, int K, const double* __restrict__ xc, double* __restrict__ x) {
-  FOR_EL(tot) {
-    const long long i = t / K;
-    x[t] += kCoarseWeight * xc[(i / kAgg) * K + (t - i * K)];
+    bc[(long long)i * K + k] = r;
   }
 }
 
 // x = Pinv b on the coarsest level
 __global__ void k_coarse(int nc, int K, const double* __restrict__ pinv, const double* __restrict__ b,
                          double* __restrict__ x) {
-  FOR_EL((long long)nc * K) {
-    const int i = (int)(t / K), k = (int)(t - (long long)i * K);
-    double s = 0.0;
-    for (int j = 0; j < nc; ++j) s += pinv[(long long)i * nc + j] * b[(long long)j * K + k];
-    x[t] = s;
+  FOR_RC(nc, K) {
+    double sum = 0.0;
+    for (int j = 0; j < nc; ++j) sum += pinv[(long long)i * nc + j] * b[(long long)j * K + k];
+    x[(long long)i * K + k] = sum;
   }
 }
 
-// per-column partial sums of a*b (or of a when b is null) over row blocks
+// per-column partial sums of a*b (or of a when b is null) over gridDim.y
+// row partitions (blocks shaped as shape_for's; smem: one double a thread)
 __global__ void k_colsum(int n, int K, const double* __restrict__ a, const double* __restrict__ b,
                          double* __restrict__ part) {
-  __shared__ double sh[8][33];
-  const int k = blockIdx.x * 32 + threadIdx.x;
-  double s = 0.0;
-  if (k < K)
-    for (int i = blockIdx.y * 8 + threadIdx.y; i < n; i += gridDim.y * 8) {
+  extern __shared__ double sh[];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double sum = 0.0;
+  if (k < K) {
+#pragma unroll 4
+    for (int i = blockIdx.y * blockDim.y + threadIdx.y; i < n; i += gridDim.y * blockDim.y) {
       const double v = a[(long long)i * K + k];
-      s += b ? v * b[(long long)i * K + k] : v;
+      sum += b ? v * b[(long long)i * K + k] : v;
     }
-  sh[threadIdx.y][threadIdx.x] = s;
+  }
+  sh[threadIdx.y * blockDim.x + threadIdx.x] = sum;
   __syncthreads();
   if (threadIdx.y == 0 && k < K) {
     double r = 0.0;
-    for (int j = 0; j < 8; ++j) r += sh[j][threadIdx.x];
+    for (int j = 0; j < (int)blockDim.y; ++j) r += sh[j * blockDim.x + threadIdx.x];
     part[(long long)blockIdx.y * K + k] = r;
   }
 }
 
+// out[k] = scale * sum of the nparts partials of column k: 8 lanes per
+// column take every 8th partial, then add up in lane order (fixed order)
 __global__ void k_colfinish(int K, int nparts, const double* __restrict__ part, double scale, double* __restrict__ out) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= K) return;
+  __shared__ double sh[8][33];
+  const int k = blockIdx.x * 32 + threadIdx.x;
   double r = 0.0;
-  for (int j = 0; j < nparts; ++j) r += part[(long long)j * K + k];
-  out[k] = scale * r;
+  if (k < K) {
+#pragma unroll 8
+    for (int j = threadIdx.y; j < nparts; j += 8) r += part[(long long)j * K + k];
+  }
+  sh[threadIdx.y][threadIdx.x] = r;
+  __syncthreads();
+  if (threadIdx.y == 0 && k < K) {
+    double t = 0.0;
+    for (int j = 0; j < 8; ++j) t += sh[j][threadIdx.x];
+    out[k] = scale * t;
+  }
 }
 
-// dst = src - mean (per column)
-__global__ void k_sub_mean(long long tot, int K, const double* __restrict__ mean, const double* __restrict__ src,
-                           double* __restrict__ dst) {
-  FOR_EL(tot) dst[t] = src[t] - mean[t % K];
+// dst = src - mean (per column; src may be dst)
+__global__ void k_sub_mean(int n, int K, const double* __restrict__ mean, const double* src, double* dst) {
+  FOR_RC(n, K) dst[(long long)i * K + k] = src[(long long)i * K + k] - mean[k];
 }
 
-// alpha = rz / pq (0 where pq or rz vanish: a converged column stops moving)
-__global__ void k_ratio(int K, const double* __restrict__ num, const double* __restrict__ den, double* __restrict__ out) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < K) out[k] = (den[k] != 0.0 && num[k] != 0.0) ? num[k] / den[k] : 0.0;
+// num / den, 0 where either vanishes (a converged column stops moving)
+__device__ __forceinline__ double guarded_ratio(double num, double den) {
+  return (den != 0.0 && num != 0.0) ? num / den : 0.0;
 }
 
-__global__ void k_xr_update(long long tot, int K, const double* __restrict__ alpha, const double* __restrict__ P,
-                            const double* __restrict__ Q, double* __restrict__ X, double* __restrict__ R) {
-  FOR_EL(tot) {
-    const double a = alpha[t % K];
+// X += alpha P, R -= alpha Q with alpha = rz / pq
+__global__ void k_xr_update(int n, int K, const double* __restrict__ rz, const double* __restrict__ pq,
+                            const double* __restrict__ P, const double* __restrict__ Q, double* __restrict__ X,
+                            double* __restrict__ R) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  const double a = kk < K ? guarded_ratio(rz[kk], pq[kk]) : 0.0;
+  FOR_RC(n, K) {
+    const long long t = (long long)i * K + k;
     X[t] += a * P[t];
     R[t] -= a * Q[t];
   }
 }
 
-__global__ void k_p_update(long long tot, int K, const double* __restrict__ beta, const double* __restrict__ Z,
-                           double* __restrict__ P) {
-  FOR_EL(tot) P[t] = Z[t] + beta[t % K] * P[t];
+// P = Z + beta P with beta = rz_new / rz_old
+__global__ void k_p_update(int n, int K, const double* __restrict__ rz_new, const double* __restrict__ rz_old,
+                           const double* __restrict__ Z, double* __restrict__ P) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  const double be = kk < K ? guarded_ratio(rz_new[kk], rz_old[kk]) : 0.0;
+  FOR_RC(n, K) {
+    const long long t = (long long)i * K + k;
+    P[t] = Z[t] + be * P[t];
+  }
 }
 
-__global__ void k_row_scale(long long tot, int K, const double* __restrict__ s, const double* __restrict__ X,
+// Y = sign * diag(s) X (s null: 1)
+__global__ void k_row_scale(int n, int K, const double* __restrict__ s, const double* __restrict__ X,
                             double* __restrict__ Y, double sign) {
-  FOR_EL(tot) Y[t] = sign * (s ? s[t / K] : 1.0) * X[t];
+  FOR_RC(n, K) Y[(long long)i * K + k] = sign * (s ? s[i] : 1.0) * X[(long long)i * K + k];
 }
 
 // the scaled identity columns col0 .. col0+K-1: E[i][k] = s_i where i == col0 + k
 __global__ void k_scaled_identity(int n, int K, int col0, const double* __restrict__ s, double* __restrict__ E) {
-  FOR_EL((long long)n * K) {
-    const int i = (int)(t / K), k = (int)(t - (long long)i * K);
-    E[t] = (i == col0 + k) ? s[i] : 0.0;
-  }
+  FOR_RC(n, K) E[(long long)i * K + k] = (i == col0 + k) ? s[i] : 0.0;
 }
 
 struct Level {
@@ -208,8 +268,8 @@ struct bx_graph_solver {
   int *w_ptr = nullptr, *w_col = nullptr;
   double *w_val = nullptr, *area = nullptr;
   double *R = nullptr, *Z = nullptr, *P = nullptr, *Q = nullptr, *T0 = nullptr, *T1 = nullptr, *T2 = nullptr;
-  double *part = nullptr, *alpha = nullptr, *beta = nullptr, *rz = nullptr, *rz2 = nullptr, *rr = nullptr,
-         *bb = nullptr, *pq = nullptr, *mean = nullptr;
+  double *part = nullptr, *rz = nullptr, *rz2 = nullptr, *rr = nullptr, *bb = nullptr, *pq = nullptr,
+         *mean = nullptr;
   std::vector<void*> owned;
   ~bx_graph_solver() {
     for (void* p : owned) cudaFree(p);
@@ -227,8 +287,10 @@ namespace {
 
 int colsum(bx_graph_solver* h, int n, int K, const double* a, const double* b, double scale, double* out,
            cudaStream_t s) {
-  k_colsum<<<dim3((unsigned)((K + 31) / 32), kRedRows), dim3(32, 8), 0, s>>>(n, K, a, b, h->part);
-  k_colfinish<<<(K + 127) / 128, 128, 0, s>>>(K, kRedRows, h->part, scale, out);
+  Shape sh = shape_for(n, K);
+  sh.grid.y = kRedRows;
+  k_colsum<<<sh.grid, sh.block, 256 * sizeof(double), s>>>(n, K, a, b, h->part);
+  k_colfinish<<<(K + 31) / 32, dim3(32, 8), 0, s>>>(K, kRedRows, h->part, scale, out);
   GCK(cudaGetLastError());
   return BX_OK;
 }
@@ -236,22 +298,17 @@ int colsum(bx_graph_solver* h, int n, int K, const double* a, const double* b, d
 // x = V-cycle(b) on level l; returns the buffer holding x (x or t of the level)
 double* vcycle(bx_graph_solver* h, int l, const double* b, double* x, double* t, int K, cudaStream_t s) {
   const Level& L = h->lv[l];
-  const long long tot = (long long)L.n * K;
   if (l + 1 == (int)h->lv.size()) {
-    k_coarse<<<grid_for(tot), 256, 0, s>>>(L.n, K, h->pinv, b, x);
+    LAUNCH(k_coarse, L.n, K, s, L.n, K, h->pinv, b, x);
     return x;
   }
-  k_jacobi0<<<grid_for(tot), 256, 0, s>>>(tot, K, L.dinv, b, x);
-  k_jacobi<<<grid_for(tot), 256, 0, s>>>(L.n, K, L.ptr, L.col, L.val, L.dinv, b, x, t);
-  std::swap(x, t);
+  LAUNCH(k_smooth_pre, L.n, K, s, L.n, K, L.ptr, L.col, L.val, L.dinv, b, x);
   const Level& C = h->lv[l + 1];
-  k_restrict<<<grid_for((long long)C.n * K), 256, 0, s>>>(L.n, C.n, K, L.ptr, L.col, L.val, b, x, C.b);
+  LAUNCH(k_restrict, C.n, K, s, L.n, C.n, K, L.ptr, L.col, L.val, b, x, C.b);
   const double* xc = vcycle(h, l + 1, C.b, C.x, C.t, K, s);
-  k_prolong<<<grid_for(tot), 256, 0, s>>>(tot, K, xc, x);
-  k_jacobi<<<grid_for(tot), 256, 0, s>>>(L.n, K, L.ptr, L.col, L.val, L.dinv, b, x, t);
-  std::swap(x, t);
-  k_jacobi<<<grid_for(tot), 256, 0, s>>>(L.n, K, L.ptr, L.col, L.val, L.dinv, b, x, t);
-  return t;
+  LAUNCH(k_smooth_post, L.n, K, s, L.n, K, L.ptr, L.col, L.val, L.dinv, b, x, xc, t);
+  LAUNCH(k_jacobi, L.n, K, s, L.n, K, L.ptr, L.col, L.val, L.dinv, b, t, x);
+  return x;
 }
 
 // X = L+ B for K columns (B and X device [n][K], distinct from the workspace)
@@ -262,28 +319,28 @@ int solve(bx_graph_solver* h, const double* B, double* X, int K, double tol, int
   const Level& L0 = h->lv[0];
   int rc = colsum(h, n, K, B, nullptr, 1.0 / n, h->mean, s);
   if (rc != BX_OK) return rc;
-  k_sub_mean<<<grid_for(tot), 256, 0, s>>>(tot, K, h->mean, B, h->R);
+  LAUNCH(k_sub_mean, n, K, s, n, K, h->mean, B, h->R);
   GCK(cudaMemsetAsync(X, 0, (size_t)tot * sizeof(double), s));
   if ((rc = colsum(h, n, K, h->R, h->R, 1.0, h->bb, s)) != BX_OK) return rc;
+  // Z = M(R) projected orthogonal to the constants; rz2 = R . Z
   auto precondition = [&]() -> int {
     double* z = vcycle(h, 0, h->R, h->Z, h->T0, K, s);
     int r = colsum(h, n, K, z, nullptr, 1.0 / n, h->mean, s);
     if (r != BX_OK) return r;
-    k_sub_mean<<<grid_for(tot), 256, 0, s>>>(tot, K, h->mean, z, h->Z);
+    LAUNCH(k_sub_mean, n, K, s, n, K, h->mean, z, h->Z);
     return colsum(h, n, K, h->R, h->Z, 1.0, h->rz2, s);
   };
   if ((rc = precondition()) != BX_OK) return rc;
   GCK(cudaMemcpyAsync(h->P, h->Z, (size_t)tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  GCK(cudaMemcpyAsync(h->rz, h->rz2, (size_t)K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  std::swap(h->rz, h->rz2);
   std::vector<double> hrr(K), hbb(K);
   GCK(cudaMemcpyAsync(hbb.data(), h->bb, (size_t)K * sizeof(double), cudaMemcpyDeviceToHost, s));
   double worst = 0.0;
   int it = 0;
   for (it = 1; it <= max_iter; ++it) {
-    k_spmv<<<grid_for(tot), 256, 0, s>>>(n, K, L0.ptr, L0.col, L0.val, h->P, h->Q);
+    LAUNCH(k_spmv, n, K, s, n, K, L0.ptr, L0.col, L0.val, h->P, h->Q);
     if ((rc = colsum(h, n, K, h->P, h->Q, 1.0, h->pq, s)) != BX_OK) return rc;
-    k_ratio<<<(K + 127) / 128, 128, 0, s>>>(K, h->rz, h->pq, h->alpha);
-    k_xr_update<<<grid_for(tot), 256, 0, s>>>(tot, K, h->alpha, h->P, h->Q, X, h->R);
+    LAUNCH(k_xr_update, n, K, s, n, K, h->rz, h->pq, h->P, h->Q, X, h->R);
     if (it % 4 == 0 || it == max_iter) {
       if ((rc = colsum(h, n, K, h->R, h->R, 1.0, h->rr, s)) != BX_OK) return rc;
       GCK(cudaMemcpyAsync(hrr.data(), h->rr, (size_t)K * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -295,9 +352,8 @@ int solve(bx_graph_solver* h, const double* B, double* X, int K, double tol, int
       if (worst <= tol) break;
     }
     if ((rc = precondition()) != BX_OK) return rc;
-    k_ratio<<<(K + 127) / 128, 128, 0, s>>>(K, h->rz2, h->rz, h->beta);
-    GCK(cudaMemcpyAsync(h->rz, h->rz2, (size_t)K * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    k_p_update<<<grid_for(tot), 256, 0, s>>>(tot, K, h->beta, h->Z, h->P);
+    LAUNCH(k_p_update, n, K, s, n, K, h->rz2, h->rz, h->Z, h->P);
+    std::swap(h->rz, h->rz2);
     GCK(cudaGetLastError());
   }
   if (iters) *iters = std::min(it, max_iter);
@@ -309,18 +365,17 @@ int solve(bx_graph_solver* h, const double* B, double* X, int K, double tol, int
 int lap_gj(bx_graph_solver* h, const double* X, double* Y, int K, double tol, int max_iter, int* iters,
            double* rel_res, cudaStream_t s, bool identity_cols = false, int col0 = 0) {
   const int n = h->n;
-  const long long tot = (long long)n * K;
   if (identity_cols)
-    k_scaled_identity<<<grid_for(tot), 256, 0, s>>>(n, K, col0, h->area, h->T1);
+    LAUNCH(k_scaled_identity, n, K, s, n, K, col0, h->area, h->T1);
   else
-    k_row_scale<<<grid_for(tot), 256, 0, s>>>(tot, K, h->area, X, h->T1, 1.0);
+    LAUNCH(k_row_scale, n, K, s, n, K, h->area, X, h->T1, 1.0);
   int i1 = 0, i2 = 0;
   double r1 = 0.0, r2 = 0.0;
   int rc = solve(h, h->T1, h->T2, K, tol, max_iter, &i1, &r1, s);
   if (rc != BX_OK) return rc;
-  k_spmv<<<grid_for(tot), 256, 0, s>>>(n, K, h->w_ptr, h->w_col, h->w_val, h->T2, h->T1);
+  LAUNCH(k_spmv, n, K, s, n, K, h->w_ptr, h->w_col, h->w_val, h->T2, h->T1);
   if ((rc = solve(h, h->T1, h->T2, K, tol, max_iter, &i2, &r2, s)) != BX_OK) return rc;
-  k_row_scale<<<grid_for(tot), 256, 0, s>>>(tot, K, nullptr, h->T2, Y, -1.0);
+  LAUNCH(k_row_scale, n, K, s, n, K, nullptr, h->T2, Y, -1.0);
   GCK(cudaGetLastError());
   if (iters) *iters = std::max(i1, i2);
   if (rel_res) *rel_res = std::max(r1, r2);
@@ -400,10 +455,10 @@ extern "C" int bx_graph_create(int n_levels, const bx_graph_level* levels, const
     h->area = h->alloc<double>(n);
     for (double** v : {&h->R, &h->Z, &h->P, &h->Q, &h->T0, &h->T1, &h->T2}) *v = h->alloc<double>(big);
     h->part = h->alloc<double>((size_t)kRedRows * max_rhs);
-    for (double** v : {&h->alpha, &h->beta, &h->rz, &h->rz2, &h->rr, &h->bb, &h->pq, &h->mean})
+    for (double** v : {&h->rz, &h->rz2, &h->rr, &h->bb, &h->pq, &h->mean})
       *v = h->alloc<double>(max_rhs);
     ok = h->pinv && h->w_ptr && h->w_col && h->w_val && h->area && h->R && h->Z && h->P && h->Q && h->T0 &&
-         h->T1 && h->T2 && h->part && h->alpha && h->beta && h->rz && h->rz2 && h->rr && h->bb && h->pq && h->mean;
+         h->T1 && h->T2 && h->part && h->rz && h->rz2 && h->rr && h->bb && h->pq && h->mean;
     ok = ok && cudaMemcpy(h->pinv, coarse_pinv, (size_t)nc * nc * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(h->w_ptr, weighted->row_ptr, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(h->w_col, weighted->col, (size_t)weighted->nnz * 4, cudaMemcpyHostToDevice) == cudaSuccess &&

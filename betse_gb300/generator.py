@@ -197,6 +197,7 @@ def workload(radius, seed, is_ecm=False, dt=1e-2, dm_range=(1e-19, 1e-17),
     gc = cluster if cluster is not None else make_cluster(radius, seed, grid_size=grid_size,
                                                           cell_space=cell_space)
     g = gc.geom
+    g.extra['cell_centres'] = gc.cell_centres
     M, C, G = g.n_mems, g.n_cells, g.n_grid
     rng = np.random.default_rng(seed + 1)
     Dm = np.exp(rng.uniform(np.log(dm_range[0]), np.log(dm_range[1]), size=(6, M)))
