@@ -608,6 +608,34 @@ def dense_products(stream, flush, wl_ecm):
     return out
 
 
+def generator_timing(radius=1450e-6, seed=3, cpu=True):
+    """Cluster generation (Cells.make_world's seeding): bx_generate_cluster on
+    the GPU, the whole make_cluster call (generation, download, host
+    assembly), against its NumPy/SciPy restatement on one host thread."""
+    import torch
+    from betse_gb300 import generator as gen
+    gen.make_cluster(radius, seed)              # module load, first allocations
+    ts = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gc = gen.make_cluster(radius, seed)
+        ts.append(time.perf_counter() - t0)
+    out = {'cells': gc.geom.n_cells, 'membranes': gc.geom.n_mems, 'gpu_ms': min(ts) * 1e3,
+           'note': 'lattice (MT19937), two Voronoi passes, Z order, membranes, pairs, grid map, adjacency; '
+                   'includes the download and ClusterGeometry assembly on the host'}
+    if cpu:
+        from oracle.generator import make_cluster as make_ref
+        t0 = time.perf_counter()
+        ref = make_ref(radius, seed)
+        dt = time.perf_counter() - t0
+        out['cpu_baseline'] = {'value': dt * 1e3, 'unit': 'ms', 'cores': 1, 'kind': 'port',
+                               'sample': f'oracle/generator.py (NumPy/SciPy Delaunay) on the same radius and seed, '
+                                         f'{ref.geom.n_cells} cells'}
+        out['speedup'] = dt * 1e3 / out['gpu_ms']
+    return out
+
+
 def lap_gj_timing(wl_full, wl_ecm, dense_full=False):
     """cells.lapGJinv (Cells.graphLaplacian) of the generated clusters:
     the matrix-free FP64 product (two multigrid-preconditioned CG solves,
@@ -986,6 +1014,7 @@ def main():
         extra = dense_products(stream, flush, others['ecm20k'])
         extra['batch_env_fields'] = batch_fields_timing()
         extra['network'] = network_step(g, p, Dm, st, stream, flush, cpu=cpu_on)
+        extra['generator'] = generator_timing(cpu=cpu_on)
         extra['lap_gj'] = lap_gj_timing((w, g, p, Dm, st, D_env), others['ecm20k'],
                                         dense_full=args.lapgj_dense_full)
 

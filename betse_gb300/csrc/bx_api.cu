@@ -747,8 +747,12 @@ cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   bx::DevGeom g = dev_geom(h);
   bx::StepConst k = make_step_const(h);
   bx::StepPtrs p = step_ptrs(h, parity);
-  return h->tpb == 128 ? bx::launch_cell_step<double, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k)
-                       : bx::launch_cell_step<double, 256>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+  switch (h->tpb) {
+    case 32: return bx::launch_cell_step<double, 32>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+    case 64: return bx::launch_cell_step<double, 64>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+    case 128: return bx::launch_cell_step<double, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+    default: return bx::launch_cell_step<double, 256>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
+  }
 }
 
 // The extracellular grid of one step (update_ecm, update_Co's ECM term, get_current's E_env).
@@ -1877,7 +1881,8 @@ int bx_get_launch_config(bx_handle h, int* tpb, int* kernel) {
 
 int bx_set_launch_config(bx_handle h, int tpb, int kernel) {
   if (!h) return fail(BX_EINVAL, "null handle");
-  const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256) : (tpb == 128 || tpb == 256);
+  const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256)
+                                           : (tpb == 32 || tpb == 64 || tpb == 128 || tpb == 256);
   if (!ok) return fail(BX_EINVAL, "unsupported CTA size for this form");
   const int variant = (kernel >> 8) & 0xff;
   kernel &= 0xff;
@@ -1982,7 +1987,8 @@ int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* 
              {256, KIND_FACT, 14},    {192, KIND_FACT, 14},    {256, KIND_FACT, 16},   {192, KIND_FACT, 16},
              {256, KIND_FACT_PIPE, 4}, {192, KIND_FACT_PIPE, 4},
              {256, KIND_RESIDENT, 4}, {192, KIND_RESIDENT, 4}};
-  else cands = {{256, KIND_TILE, 4}, {128, KIND_TILE, 4}};
+  // plain form: small CTAs spread a small cluster's FP64 work over more SMs
+  else cands = {{256, KIND_TILE, 4}, {128, KIND_TILE, 4}, {64, KIND_TILE, 4}, {32, KIND_TILE, 4}};
   double best = 1e300;
   int best_tpb = h->tpb, best_kind = h->kind, best_unroll = h->fact_unroll;
   cudaEvent_t e0, e1;

@@ -1,0 +1,7 @@
+// Plain FP64 form of the fused cell step, small CTAs (instantiations; a
+// unit of its own so that it compiles in parallel with the larger ones).
+#include "bx_launch.cuh"
+namespace bx {
+BX_DEFINE_CELL_STEP_LAUNCHER(double, 32)
+BX_DEFINE_CELL_STEP_LAUNCHER(double, 64)
+}  // namespace bx

@@ -420,7 +420,8 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
                          double* vm_work, double* cc_cells, double* cc_mem, double* cc_mem_work,
                          double* cc_env, int n_steps, void* stream);
 
-/* Launch configuration: CTA size (plain form 128 or 256; split form 192 or
+/* Launch configuration: CTA size (plain form 32, 64, 128 or 256 membrane
+ * slots per CTA -- the small ones spread a small cluster over more SMs; split form 192 or
  * 256 membrane slots per tile, which sets how cells are grouped into tiles)
  * and, for the split form, the kernel:
  *   0  tile kernel (one tile per CTA, one launch per step; every variant)

@@ -175,15 +175,37 @@ def test_autotune_keeps_state_and_results(precision):
     d = gi.load('noecm_r80_s1')
     with _engine(d, precision) as a, _engine(d, precision) as b:
         tpb, ms = a.autotune(5)
-        assert tpb in (128, 192, 256) and ms > 0
+        assert tpb in (32, 64, 128, 192, 256) and ms > 0
         s0 = a.download()
         assert np.array_equal(s0['vm'], b.download()['vm'])
         a.step(40)
         b.step(40)
         sa, sb = a.download(), b.download()
-    tol = 0.0 if precision == 'fp64' else 1e-12
+    # the well-mixed environment adds the CTAs' partial sums in partition
+    # order, so a different CTA size rounds differently (FP64: ~1e-16)
+    tol = 1e-13 if precision == 'fp64' else 1e-12
     for k in sa:
         assert gi.rel_err(sa[k], sb[k]) <= tol, k
+
+
+@pytest.mark.parametrize('tpb', [32, 64, 128, 256])
+def test_fp64_cta_sizes_match_betse(tpb):
+    """Every CTA size of the plain FP64 kernel (the small ones spread a small
+    cluster over more SMs) reproduces BETSE's state at every checkpoint."""
+    d = gi.load('noecm_r80_s1')
+    with _engine(d, 'fp64') as eng:
+        eng.set_launch_config(tpb, 0)
+        done = 0
+        for cp in d['meta_checkpoints']:
+            eng.step(int(cp - done))
+            done = int(cp)
+            eng.check_stable()
+            s = eng.download()
+            ok, e_vm, bound = gi.vm_err_ok(d, s['vm'], d[f's{cp}_vm'], d[f's{cp}_cc_cells'])
+            assert ok, (tpb, cp, e_vm, bound)
+            assert gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells']) < TOL_FP64, (tpb, cp)
+            assert _cmp_env(s['cc_env'], d[f's{cp}_cc_env'], False) < TOL_FP64, (tpb, cp)
+        assert eng.launch_config()[0] == tpb
 
 
 @pytest.mark.parametrize('tpb', [192, 256])
@@ -224,9 +246,31 @@ def test_voltage_gated_gj_state_round_trip_and_autotune(precision):
         if precision == 'split':
             with pytest.raises(Exception):
                 a.set_launch_config(256, True)
-    tol = 0.0 if precision == 'fp64' else 1e-12
+    # the well-mixed environment adds the CTAs' partial sums in partition
+    # order, so a different CTA size rounds differently (FP64: ~1e-16)
+    tol = 1e-13 if precision == 'fp64' else 1e-12
     for k in sa:
         assert gi.rel_err(sa[k], sb[k]) <= tol, k
+
+
+@pytest.mark.parametrize('tpb', [32, 64, 128, 256])
+def test_fp64_cta_sizes_match_betse(tpb):
+    """Every CTA size of the plain FP64 kernel (the small ones spread a small
+    cluster over more SMs) reproduces BETSE's state at every checkpoint."""
+    d = gi.load('noecm_r80_s1')
+    with _engine(d, 'fp64') as eng:
+        eng.set_launch_config(tpb, 0)
+        done = 0
+        for cp in d['meta_checkpoints']:
+            eng.step(int(cp - done))
+            done = int(cp)
+            eng.check_stable()
+            s = eng.download()
+            ok, e_vm, bound = gi.vm_err_ok(d, s['vm'], d[f's{cp}_vm'], d[f's{cp}_cc_cells'])
+            assert ok, (tpb, cp, e_vm, bound)
+            assert gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells']) < TOL_FP64, (tpb, cp)
+            assert _cmp_env(s['cc_env'], d[f's{cp}_cc_env'], False) < TOL_FP64, (tpb, cp)
+        assert eng.launch_config()[0] == tpb
 
 
 @pytest.mark.parametrize('precision', ['fp64', 'split'])
