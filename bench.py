@@ -479,7 +479,8 @@ def config_plain250(wl, stream, flush, cpu=True):
     with ClusterEngine(g, p, 'fp64') as e:
         e.set_membrane_diffusivity(Dm)
         e.upload(**st)
-        e.autotune(3)
+        table = e.autotune_table(20)
+        launch = e.launch_config()
         ms = timed_run_ms(e, T, stream, flush)
         e.upload(**st)
         kms = e.time_cell_kernel(200)
@@ -487,10 +488,14 @@ def config_plain250(wl, stream, flush, cpu=True):
     out = {'workload': w['desc'], 'cells': g.n_cells, 'membranes': g.n_mems, 'time_steps_per_run': T,
            'form': 'plain FP64', 'value': g.n_mems * T / (ms / 1e3), 'unit': UNIT, 'ms_per_run': ms,
            'roofline': roofline_entry(kb, kms / 1e3, 'k_cell_step<double>',
-                                      note='a 1.4k-membrane cluster fills a few CTAs: launch- and '
-                                           'latency-bound, the roofline is far away by construction',
+                                      note='a 1.4k-membrane cluster fills a few dozen CTAs: bound by '
+                                           'the dependent FP64 instruction chain of a lane, not by HBM',
                                       survey=survey_bytes('fp64', g.n_cells, g.n_mems)),
-           'kernel_launches_per_step': 2}
+           'kernel_launches_per_step': 2,
+           'autotuned_launch': {'cta_slots': launch[0], 'kernel': 'k_cell_step_ion' if launch[1] == 5
+                                else 'k_cell_step<double>'},
+           'autotune_table': table}
+    out['roofline']['kernel'] = out['autotuned_launch']['kernel']
     if cpu:
         out['cpu_baseline'] = cpu_baseline(g, p, Dm, st, budget_s=6.0)
     return out
@@ -776,15 +781,16 @@ def profile_kernel(which):
     print('profile kernel done:', which)
 
 
-# kernels of the split form, by the number bx_set_launch_config takes
+# kernels, by the number bx_set_launch_config takes (5: the plain form's)
 KERNEL_NAMES = {0: 'k_split_step', 1: 'k_split_persist', 2: 'k_split_fact', 3: 'k_split_resident',
-                4: 'k_split_fact_pipe'}
-LAUNCH_SUFFIX = {'': 0, 'p': 1, 'f': 2, 'r': 3, 'q': 4}
+                4: 'k_split_fact_pipe', 5: 'k_cell_step_ion'}
+LAUNCH_SUFFIX = {'': 0, 'p': 1, 'f': 2, 'r': 3, 'q': 4, 'i': 5}
 
 
 def parse_launch(text):
     """'192' tile kernel, '192p' persistent, '192f' factored, '256r' resident,
-    '256q' pipelined factored; a number after 'f' picks the factored kernel's
+    '256q' pipelined factored, '32i' the plain form's one-lane-per-ion
+    kernel; a number after 'f' picks the factored kernel's
     variant ('256f12': two junctions per round, entries prefetched)."""
     head = text.lstrip('0123456789')
     tpb = int(text[:len(text) - len(head)])

@@ -67,7 +67,7 @@ constexpr int kRec = 8;          // floats per cell record of the split form (<=
 
 enum Mode { MODE_PLAIN = 0, MODE_SPLIT = 1 };
 // kernels of the split form (bx_set_launch_config's `kernel`)
-enum Kind { KIND_TILE = 0, KIND_PERSIST = 1, KIND_FACT = 2, KIND_RESIDENT = 3, KIND_FACT_PIPE = 4 };
+enum Kind { KIND_TILE = 0, KIND_PERSIST = 1, KIND_FACT = 2, KIND_RESIDENT = 3, KIND_FACT_PIPE = 4, KIND_ION = 5 };
 constexpr long long kResTimeoutNs = 2000000000LL;   // grid-barrier wait limit of k_split_resident
 
 }  // namespace
@@ -143,6 +143,7 @@ struct bx_cluster {
   double *d_Denv = nullptr, *d_Ex = nullptr, *d_Ey = nullptr, *d_fx = nullptr, *d_fy = nullptr,
          *d_tmp = nullptr, *d_tmp2 = nullptr, *d_venv = nullptr, *d_rho_env = nullptr, *d_vsrc = nullptr;
   unsigned long long* d_status = nullptr;
+  unsigned* d_env_ticket = nullptr;   // [ncl] k_cell_step_ion's last-CTA counters (zero between steps)
   // ---- outputs
   double *o_fmem = nullptr, *o_fgj = nullptr, *o_rate = nullptr, *o_rho = nullptr, *o_Jn = nullptr,
          *o_Imem = nullptr, *o_Jcx = nullptr, *o_Jcy = nullptr, *o_Jc = nullptr, *o_vmave = nullptr,
@@ -215,7 +216,7 @@ void free_all(bx_cluster* h) {
       h->t_gw, h->t_dtv, h->t_dvc, h->t_rng,
       h->s_cenv_f, h->s_pump, h->s_part, h->s_phib, h->d_cenv, h->d_phib, h->d_env_part,
       h->d_mem_flux_sa, h->d_pump, h->d_env_scale, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy,
-      h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_vsrc, h->d_status, h->o_fmem, h->o_fgj, h->o_rate,
+      h->d_tmp, h->d_tmp2, h->d_venv, h->d_rho_env, h->d_vsrc, h->d_status, h->d_env_ticket, h->o_fmem, h->o_fgj, h->o_rate,
       h->o_rho, h->o_Jn, h->o_Imem, h->o_Jcx, h->o_Jcy, h->o_Jc, h->o_vmave, h->o_dvm, h->o_Ecx,
       h->o_Ecy, h->o_Emc, h->o_Egjx, h->o_Egjy, h->o_gjopen, h->o_sigma, h->o_vmc, h->o_vm_mem,
       h->o_drho, h->f_lap, h->f_X, h->f_buf, h->f_last, h->d_cl_mem, h->d_resid,
@@ -431,6 +432,13 @@ bx::FactGeom fact_geom(const bx_cluster* h) {
 // Ca-ATPase (which reads the cell concentration per membrane), no outputs.
 bool fact_eligible(const bx_cluster* h, bool out) {
   return h->mode == MODE_SPLIT && !out && !h->phib_nonzero && !h->ecm && !h->vgj && !h->ca;
+}
+
+// The plain form's one-lane-per-ion kernel covers the same configuration
+// without polarizability, on CTAs of 8 to 64 membrane slots.
+bool ion_eligible(const bx_cluster* h, bool out) {
+  return h->mode != MODE_SPLIT && !out && !h->phib_nonzero && !h->ecm && !h->vgj && !h->ca && !h->polar &&
+         (h->tpb == 8 || h->tpb == 16 || h->tpb == 32 || h->tpb == 64);
 }
 
 bool is_betse_six_ions(const bx_cluster* h) {
@@ -747,7 +755,19 @@ cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   bx::DevGeom g = dev_geom(h);
   bx::StepConst k = make_step_const(h);
   bx::StepPtrs p = step_ptrs(h, parity);
+  if (h->kind == KIND_ION && ion_eligible(h, out)) {
+    const bx::EnvMix em{h->d_cenv, h->d_cl_blk, h->d_env_scale, h->d_env_ticket};
+    switch (h->tpb) {
+      case 8: return bx::launch_cell_step_ion<8>(h->nblk, s, g, p, k, em);
+      case 16: return bx::launch_cell_step_ion<16>(h->nblk, s, g, p, k, em);
+      case 32: return bx::launch_cell_step_ion<32>(h->nblk, s, g, p, k, em);
+      default: return bx::launch_cell_step_ion<64>(h->nblk, s, g, p, k, em);
+    }
+  }
+  // partitions of 8 or 16 membrane slots run on 32-thread CTAs
   switch (h->tpb) {
+    case 8:
+    case 16:
     case 32: return bx::launch_cell_step<double, 32>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
     case 64: return bx::launch_cell_step<double, 64>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
     case 128: return bx::launch_cell_step<double, 128>(h->ecm, out, h->phib_nonzero, h->nblk, s, g, p, k);
@@ -859,6 +879,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
   e = launch_cell(h, parity, out, s);
   if (e != cudaSuccess) return e;
   h->launches++;
+  if (h->kind == KIND_ION && ion_eligible(h, out)) return cudaSuccess;   // it mixed the environment
   if (!h->ecm) {
     bx::k_env_mix<<<h->ncl, 256, 0, s>>>(h->d_env_part, h->d_cl_blk, h->I, h->d_cenv, h->d_env_scale);
     h->launches++;
@@ -868,6 +889,7 @@ cudaError_t enqueue_step(bx_cluster* h, int parity, bool out, cudaStream_t s) {
 }
 
 int launches_per_step(const bx_cluster* h) {
+  if (h->kind == KIND_ION && ion_eligible(h, false)) return 1;
   if (!h->ecm) return 2;
   if (h->ca) return h->par.sharpness < 1.0 ? 9 : 8;
   return h->par.sharpness < 1.0 ? 8 : 4;
@@ -1318,7 +1340,9 @@ int create_impl(const bx_geom* gs, const bx_params* ps, int ncl, int precision, 
   ALLOC(h->d_pump, ncl); ALLOC(h->d_env_scale, ncl);
   ALLOC(h->d_phib, G);
   ALLOC(h->d_status, 4);
+  ALLOC(h->d_env_ticket, ncl);
   if (cudaMemset(h->d_status, 0, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(h->d_env_ticket, 0, (size_t)ncl * sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(h->d_phib, 0, (size_t)G * sizeof(double)) != cudaSuccess)
     return bail(BX_ECUDA, "cudaMemset");
   if (h->mode == MODE_SPLIT) {
@@ -1882,14 +1906,19 @@ int bx_get_launch_config(bx_handle h, int* tpb, int* kernel) {
 int bx_set_launch_config(bx_handle h, int tpb, int kernel) {
   if (!h) return fail(BX_EINVAL, "null handle");
   const bool ok = (h->mode == MODE_SPLIT) ? (tpb == 192 || tpb == 256)
-                                           : (tpb == 32 || tpb == 64 || tpb == 128 || tpb == 256);
+                                           : (tpb == 8 || tpb == 16 || tpb == 32 || tpb == 64 || tpb == 128 ||
+                                              tpb == 256);
   if (!ok) return fail(BX_EINVAL, "unsupported CTA size for this form");
   const int variant = (kernel >> 8) & 0xff;
   kernel &= 0xff;
-  if (kernel < KIND_TILE || kernel > KIND_FACT_PIPE) return fail(BX_EINVAL, "kernel must be 0 to 4");
+  if (kernel < KIND_TILE || kernel > KIND_ION) return fail(BX_EINVAL, "kernel must be 0 to 5");
   if (variant && !(variant == 2 || variant == 4 || variant == 12 || variant == 13 || variant == 14 || variant == 16))
     return fail(BX_EINVAL, "factored-kernel variant must be 2, 4, 12, 13, 14 or 16");
-  if (kernel != KIND_TILE && h->mode != MODE_SPLIT)
+  if (kernel == KIND_ION && h->mode == MODE_SPLIT)
+    return fail(BX_EINVAL, "the one-lane-per-ion kernel is the plain form's");
+  if (kernel == KIND_ION && (h->polar))
+    return fail(BX_EINVAL, "the one-lane-per-ion kernel has no polarizability variant");
+  if (kernel != KIND_TILE && kernel != KIND_ION && h->mode != MODE_SPLIT)
     return fail(BX_EINVAL, "the persistent, factored and resident kernels are the split form's");
   if (kernel != KIND_TILE && h->ecm) return fail(BX_EINVAL, "only the tile kernel has an extracellular-space variant");
   if (kernel != KIND_TILE && h->vgj)
@@ -1988,7 +2017,12 @@ int bx_autotune_table(bx_handle h, int n_steps, int max_rows, int* n_rows, int* 
              {256, KIND_FACT_PIPE, 4}, {192, KIND_FACT_PIPE, 4},
              {256, KIND_RESIDENT, 4}, {192, KIND_RESIDENT, 4}};
   // plain form: small CTAs spread a small cluster's FP64 work over more SMs
-  else cands = {{256, KIND_TILE, 4}, {128, KIND_TILE, 4}, {64, KIND_TILE, 4}, {32, KIND_TILE, 4}};
+  else {
+    cands = {{256, KIND_TILE, 4}, {128, KIND_TILE, 4}, {64, KIND_TILE, 4}, {32, KIND_TILE, 4},
+             {16, KIND_TILE, 4},  {8, KIND_TILE, 4}};
+    if (!h->phib_nonzero && !h->ecm && !h->vgj && !h->ca && !h->polar)
+      for (int mb : {64, 32, 16, 8}) cands.push_back({mb, KIND_ION, 4});
+  }
   double best = 1e300;
   int best_tpb = h->tpb, best_kind = h->kind, best_unroll = h->fact_unroll;
   cudaEvent_t e0, e1;

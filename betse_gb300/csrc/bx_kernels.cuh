@@ -483,6 +483,182 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
   }
 }
 
+// The well-mixed environment folded into the step: the last CTA of a
+// cluster to finish (a ticket counter, reset by that CTA) adds the cluster's
+// CTA partials in CTA order and updates its environment, as k_env_mix does.
+struct EnvMix {
+  double* cenv;               // [ncl][I]
+  const int* cl_blk;          // [ncl + 1] first CTA of each cluster
+  const double* env_scale;    // [ncl] dt / (vol_env M)
+  unsigned* ticket;           // [ncl] zero between steps
+};
+
+// The plain FP64 step for small clusters.  On a 1.4k-membrane cluster
+// k_cell_step spends ~3200 FP64-heavy instructions per thread on a few
+// dozen SMs, and an FP64 warp instruction costs the same whatever the
+// number of lanes it uses; here the work is spread and no lane idles:
+//   A. one lane per membrane: the shared exponentials of the membrane and
+//      gap-junction voltages and the Na/K-ATPase rate, into shared memory;
+//   B. eight lanes per membrane slot, lane i = ion i: the transmembrane and
+//      gap-junction GHK fluxes of that ion;
+//   C. eight lanes per cell, lane i = ion i: the concentration update, and
+//      the charge sum gathered in ion order by shuffles; then Vmem.
+// The arithmetic of every flux and every (cell, ion) update is
+// k_cell_step<double>'s in the same order; the environment partials add in
+// slot order.  The configuration without extracellular spaces, outputs,
+// Phi_b, gating, Ca-ATPase and polarizability; MB membrane slots per CTA,
+// MB * 8 threads.
+template <int MB>
+__global__ void __launch_bounds__(MB * 8)
+k_cell_step_ion(DevGeom g, StepPtrs p, StepConst k, EnvMix em) {
+  __shared__ double sA[kMaxIons][MB];   // f_mem*sa
+  __shared__ double sB[kMaxIons][MB];   // -f_gj*sa
+  __shared__ double sV[MB];             // per-cell Vmem (by local cell)
+  __shared__ double sh_m[5][MB], sh_g[5][MB];   // GhkShared {a1, em1, e1, r, q2} of vm and vgj
+  __shared__ double sh_v1[MB], sh_vg1[MB], sh_na[MB], sh_sa[MB], sh_gw[MB];
+  __shared__ int sh_c[MB], sh_cn[MB], sh_bnd[MB];
+  __shared__ int s_last;
+  const int I = k.I;
+  const int b = blockIdx.x;
+  const int c0 = g.blk_cell[b], c1 = g.blk_cell[b + 1];
+  const int cl = g.blk_cluster[b];
+  const double* cenv_cl = p.cenv + (size_t)cl * I;
+  const int m0 = g.cell_ptr[c0], m1 = g.cell_ptr[c1];
+  const int nmem = m1 - m0;
+  const int t = threadIdx.x;
+
+  // ---- A: per membrane
+  if (t < nmem) {
+    const int m = m0 + t;
+    const double v = p.vm_in[m];
+    const int c = g.m2c[m];
+    const double vn = p.vm_in[g.nn[m]];
+    const double v1 = v + kNonce;
+    const double vgj = (vn + kNonce) - v1;       // update_gj, sim.py:2166
+    const double vgj1 = vgj + kNonce;
+    GhkShared<double> sm, sg;
+    sm.init(v1, k.F_RT);
+    sg.init(vgj1, k.F_RT);
+    sh_m[0][t] = sm.a1; sh_m[1][t] = sm.em1; sh_m[2][t] = sm.e1; sh_m[3][t] = sm.r; sh_m[4][t] = sm.q2;
+    sh_g[0][t] = sg.a1; sh_g[1][t] = sg.em1; sh_g[2][t] = sg.e1; sh_g[3][t] = sg.r; sh_g[4][t] = sg.q2;
+    sh_v1[t] = v1;
+    sh_vg1[t] = vgj1;
+    double fNa = 0.0;
+    const double pcoef = p.pump_coef[cl];
+    if (pcoef != 0.0)                            // Na/K-ATPase (sim.py:1196-1234)
+      fNa = pump_fna<double>(k, pcoef, sm.e1, p.ccm_in[k.iNa * g.C + c], cenv_cl[k.iNa],
+                             p.ccm_in[k.iK * g.C + c], cenv_cl[k.iK]);
+    sh_na[t] = fNa;
+    sh_sa[t] = g.mem_sa[m];
+    sh_gw[t] = g.gj_w[m];
+    sh_c[t] = c;
+    sh_cn[t] = g.nn_cell[m];
+    sh_bnd[t] = g.bflag[m] != 0;
+  }
+  __syncthreads();
+
+  // ---- B: lane i of slot s, ion i of membrane m0 + s
+  const int slot = t >> 3, i = t & 7;
+  if (slot < nmem && i < I) {
+    const int m = m0 + slot;
+    GhkShared<double> sm, sg;
+    sm.a1 = sh_m[0][slot]; sm.em1 = sh_m[1][slot]; sm.e1 = sh_m[2][slot]; sm.r = sh_m[3][slot];
+    sm.q2 = sh_m[4][slot];
+    sg.a1 = sh_g[0][slot]; sg.em1 = sh_g[1][slot]; sg.e1 = sh_g[2][slot]; sg.r = sh_g[3][slot];
+    sg.q2 = sh_g[4][slot];
+    const int c = sh_c[slot], cn = sh_cn[slot];
+    const double msa = sh_sa[slot];
+    const double fNa = sh_na[slot];
+    const double cin = p.ccm_in[i * g.C + c];
+    const double cout = cenv_cl[i];
+    const double dm = p.Dm[(size_t)i * g.M + m];
+    double f = ghk_flux<double>(sm, k.zcode[i], k.z[i], sh_v1[slot], k.F_RT, cout, cin, dm, 1.0 / k.tm);
+    if (i == k.iNa) f = fNa + f;
+    else if (i == k.iK) f = -(2.0 / 3.0) * fNa + f;
+    const double cn_i = p.ccm_in[i * g.C + cn];
+    const double dgj = k.dgj_gs[i] * (sh_gw[slot] * k.gj_block);
+    double fg = ghk_flux<double>(sg, k.zcode[i], k.z[i], sh_vg1[slot], k.F_RT, cin, cn_i, dgj, 1.0 / k.gj_len);
+    if (sh_bnd[slot]) fg = 0.0;
+    sA[i][slot] = f * msa;
+    sB[i][slot] = -fg * msa;
+  }
+  __syncthreads();
+
+  // ---- the CTA's environment partial of ion t, in slot order
+  if (t < I) {
+    double sum = 0.0;
+    for (int j = 0; j < nmem; ++j) sum += sA[t][j];
+    p.env_part[(size_t)b * I + t] = sum;
+  }
+
+  // ---- C: lane i of group c, ion i of cell c0 + c
+  const int ncell = c1 - c0;
+  const int lc = t >> 3;
+  double x = 0.0;
+  if (lc < ncell && i < I) {
+    const int cc = c0 + lc;
+    const int a0 = g.cell_ptr[cc] - m0, a1 = g.cell_ptr[cc + 1] - m0;
+    const double inv_vol = 1.0 / g.cell_vol[cc];
+    double s1 = 0.0, s2 = 0.0;
+    for (int j = a0; j < a1; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
+    x = p.cc[i * g.C + cc] + (s1 * inv_vol) * k.dt;   // update_Co, sim_toolbox.py:1182-1183
+    p.ccm_out[i * g.C + cc] = x;
+    x = x + k.dt * (s2 * inv_vol);                    // gap-junction term, sim.py:2105-2108
+    const bool bad = x != x;
+    const bool neg = x < 0.0;
+    if (neg) x = 0.0;                                 // no_negs
+    p.cc[i * g.C + cc] = x;
+    if (bad) atomicAdd(&p.status[1], 1ull);
+    if (neg) atomicAdd(&p.status[2], 1ull);
+  }
+  // rho_cells (ion_current.py:19): the group's ions in ion order
+  const int base = (t & 31) & ~7;
+  double rho = 0.0;
+  for (int j = 0; j < I; ++j) rho += k.zF[j] * __shfl_sync(0xffffffffu, x, base + j);
+  if (lc < ncell && i == 0) sV[lc] = k.inv_cm * (rho * g.diviterm[c0 + lc]);   // sim.py:2027-2029
+  __syncthreads();
+
+  // ---- new Vmem, one lane per membrane
+  if (t < nmem) {
+    const double vnew = sV[sh_c[t] - c0];
+    p.vm_out[m0 + t] = vnew;
+    if (vnew != vnew) atomicAdd(&p.status[0], 1ull);
+  }
+
+  // ---- the last CTA of the cluster mixes the environment (sim_toolbox.py:1196-1205)
+  if (t == 0) {
+    __threadfence();
+    const unsigned n_cl = (unsigned)(em.cl_blk[cl + 1] - em.cl_blk[cl]);
+    s_last = atomicAdd(&em.ticket[cl], 1u) == n_cl - 1u;
+  }
+  __syncthreads();
+  if (s_last) {
+    // every thread adds a stride of CTA rows (all ions at once), then warps
+    // reduce by shuffles and thread i adds the warps' sums of ion i in order
+    __shared__ double s_w[kMaxIons][MB * 8 / 32];
+    __threadfence();
+    double acc[kMaxIons];
+#pragma unroll
+    for (int q = 0; q < kMaxIons; ++q) acc[q] = 0.0;
+    for (int bb = em.cl_blk[cl] + t; bb < em.cl_blk[cl + 1]; bb += MB * 8)
+#pragma unroll
+      for (int q = 0; q < kMaxIons; ++q)
+        if (q < I) acc[q] += __ldcg(p.env_part + (size_t)bb * I + q);
+#pragma unroll
+    for (int q = 0; q < kMaxIons; ++q) {
+      const double w = warp_sum(acc[q]);
+      if ((t & 31) == 0) s_w[q][t >> 5] = w;
+    }
+    __syncthreads();
+    if (t < I) {
+      double tot = 0.0;
+      for (int w = 0; w < MB * 8 / 32; ++w) tot += s_w[t][w];
+      em.cenv[(size_t)cl * I + t] = em.cenv[(size_t)cl * I + t] - tot * em.env_scale[cl];
+    }
+    if (t == 0) em.ticket[cl] = 0u;
+  }
+}
+
 // No-ECM environment: the well-mixed value per cluster and ion
 // (sim_toolbox.py:1196-1205) c_env <- mean_m(c_env - f_m sa_m / vol_env * dt);
 // one CTA per cluster reduces its CTAs' partial sums in a fixed order.

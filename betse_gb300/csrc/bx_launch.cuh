@@ -36,4 +36,18 @@ cudaError_t launch_cell_step(bool ecm, bool out, bool phib, int nblk, cudaStream
     return cudaGetLastError();                                                                  \
   }
 
+// the plain step for small clusters (k_cell_step_ion), MB membrane slots; it
+// also mixes the well-mixed environment
+template <int MB>
+cudaError_t launch_cell_step_ion(int nblk, cudaStream_t s, const DevGeom& g, const StepPtrs& p, const StepConst& k,
+                                 const EnvMix& em);
+
+#define BX_DEFINE_CELL_STEP_ION_LAUNCHER(MB)                                                       \
+  template <>                                                                                      \
+  cudaError_t launch_cell_step_ion<MB>(int nblk, cudaStream_t s, const DevGeom& g, const StepPtrs& p, \
+                                       const StepConst& k, const EnvMix& em) {                     \
+    k_cell_step_ion<MB><<<nblk, MB * 8, 0, s>>>(g, p, k, em);                                      \
+    return cudaGetLastError();                                                                     \
+  }
+
 }  // namespace bx

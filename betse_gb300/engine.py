@@ -18,8 +18,9 @@ from .exceptions import BetseSimUnstableException
 
 PRECISIONS = {'fp64': _lib.PLAIN_FP64, 'plain': _lib.PLAIN_FP64,
               'split': _lib.SPLIT_FP32, 'fp32': _lib.SPLIT_FP32}
-# kernels of the split form (bx_set_launch_config)
-KERNELS = {'tile': 0, 'persistent': 1, 'factored': 2, 'resident': 3, 'pipelined': 4}
+# kernels (bx_set_launch_config): the split form's, and 'ion' (the plain
+# form's one-lane-per-ion kernel)
+KERNELS = {'tile': 0, 'persistent': 1, 'factored': 2, 'resident': 3, 'pipelined': 4, 'ion': 5}
 KERNEL_NAMES = {v: k for k, v in KERNELS.items()}
 
 

@@ -420,8 +420,9 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
                          double* vm_work, double* cc_cells, double* cc_mem, double* cc_mem_work,
                          double* cc_env, int n_steps, void* stream);
 
-/* Launch configuration: CTA size (plain form 32, 64, 128 or 256 membrane
- * slots per CTA -- the small ones spread a small cluster over more SMs; split form 192 or
+/* Launch configuration: CTA size (plain form 8, 16, 32, 64, 128 or 256
+ * membrane slots per CTA -- the small ones spread a small cluster over more
+ * SMs, 8 and 16 on 32-thread CTAs; split form 192 or
  * 256 membrane slots per tile, which sets how cells are grouped into tiles)
  * and, for the split form, the kernel:
  *   0  tile kernel (one tile per CTA, one launch per step; every variant)
@@ -435,6 +436,12 @@ int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const double* Dm,
  *   4  factored kernel, persistent and software-pipelined: each warp stages
  *      its next tiles' cell data, gap-junction entries and partner records
  *      in shared memory (cp.async) while it computes (results as kernel 2)
+ *   5  (plain form, 8, 16, 32 or 64 slots) the small-cluster FP64 step: one
+ *      lane per membrane for the shared exponentials and the pump, one lane
+ *      per (membrane, ion) for the fluxes and per (cell, ion) for the update,
+ *      the environment mixed by the last CTA (one launch per step); no
+ *      outputs, Phi_b, extracellular spaces, gating, Ca-ATPase or
+ *      polarizability (else the tile kernel runs)
  * Bits 8-15 of kernel, when nonzero, pick the factored kernel's variant (the
  * third column of bx_autotune_table: 2, 4, 12, 13, 14 or 16).
  * Kernels 1-4 need no extracellular spaces, no voltage-gated gap junctions

@@ -175,7 +175,7 @@ def test_autotune_keeps_state_and_results(precision):
     d = gi.load('noecm_r80_s1')
     with _engine(d, precision) as a, _engine(d, precision) as b:
         tpb, ms = a.autotune(5)
-        assert tpb in (32, 64, 128, 192, 256) and ms > 0
+        assert tpb in (8, 16, 32, 64, 128, 192, 256) and ms > 0
         s0 = a.download()
         assert np.array_equal(s0['vm'], b.download()['vm'])
         a.step(40)
@@ -188,13 +188,15 @@ def test_autotune_keeps_state_and_results(precision):
         assert gi.rel_err(sa[k], sb[k]) <= tol, k
 
 
-@pytest.mark.parametrize('tpb', [32, 64, 128, 256])
-def test_fp64_cta_sizes_match_betse(tpb):
-    """Every CTA size of the plain FP64 kernel (the small ones spread a small
-    cluster over more SMs) reproduces BETSE's state at every checkpoint."""
+@pytest.mark.parametrize('tpb,kernel', [(16, 0), (32, 0), (64, 0), (128, 0), (256, 0), (16, 5), (32, 5),
+                                        (64, 5)])
+def test_fp64_cta_sizes_match_betse(tpb, kernel):
+    """Every CTA size of the plain FP64 kernel, and the small-cluster kernel
+    (5: lanes per ion, the environment mixed by the last CTA), reproduces
+    BETSE's state at every checkpoint."""
     d = gi.load('noecm_r80_s1')
     with _engine(d, 'fp64') as eng:
-        eng.set_launch_config(tpb, 0)
+        eng.set_launch_config(tpb, kernel)
         done = 0
         for cp in d['meta_checkpoints']:
             eng.step(int(cp - done))
@@ -205,7 +207,7 @@ def test_fp64_cta_sizes_match_betse(tpb):
             assert ok, (tpb, cp, e_vm, bound)
             assert gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells']) < TOL_FP64, (tpb, cp)
             assert _cmp_env(s['cc_env'], d[f's{cp}_cc_env'], False) < TOL_FP64, (tpb, cp)
-        assert eng.launch_config()[0] == tpb
+        assert eng.launch_config() == (tpb, kernel)
 
 
 @pytest.mark.parametrize('tpb', [192, 256])
@@ -253,13 +255,15 @@ def test_voltage_gated_gj_state_round_trip_and_autotune(precision):
         assert gi.rel_err(sa[k], sb[k]) <= tol, k
 
 
-@pytest.mark.parametrize('tpb', [32, 64, 128, 256])
-def test_fp64_cta_sizes_match_betse(tpb):
-    """Every CTA size of the plain FP64 kernel (the small ones spread a small
-    cluster over more SMs) reproduces BETSE's state at every checkpoint."""
+@pytest.mark.parametrize('tpb,kernel', [(16, 0), (32, 0), (64, 0), (128, 0), (256, 0), (16, 5), (32, 5),
+                                        (64, 5)])
+def test_fp64_cta_sizes_match_betse(tpb, kernel):
+    """Every CTA size of the plain FP64 kernel, and the small-cluster kernel
+    (5: lanes per ion, the environment mixed by the last CTA), reproduces
+    BETSE's state at every checkpoint."""
     d = gi.load('noecm_r80_s1')
     with _engine(d, 'fp64') as eng:
-        eng.set_launch_config(tpb, 0)
+        eng.set_launch_config(tpb, kernel)
         done = 0
         for cp in d['meta_checkpoints']:
             eng.step(int(cp - done))
@@ -270,7 +274,7 @@ def test_fp64_cta_sizes_match_betse(tpb):
             assert ok, (tpb, cp, e_vm, bound)
             assert gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells']) < TOL_FP64, (tpb, cp)
             assert _cmp_env(s['cc_env'], d[f's{cp}_cc_env'], False) < TOL_FP64, (tpb, cp)
-        assert eng.launch_config()[0] == tpb
+        assert eng.launch_config() == (tpb, kernel)
 
 
 @pytest.mark.parametrize('precision', ['fp64', 'split'])
@@ -308,3 +312,20 @@ def test_upload_checks_and_download_into_given_arrays(precision):
         for k in ref:
             assert got[k] is out[k]
             assert np.array_equal(out[k], ref[k]), k
+
+
+@pytest.mark.parametrize('name', ['noecm_r80_s1', 'noecm_r50_s7'])
+def test_ion_lane_kernel_equals_tile_kernel(name):
+    """The small-cluster kernel does k_cell_step's arithmetic per ion and per
+    (cell, ion) in the same order; only the environment's partial sums add
+    in another order, so the two agree to rounding after 300 steps."""
+    d = gi.load(name)
+    with _engine(d, 'fp64') as a, _engine(d, 'fp64') as b:
+        a.set_launch_config(32, 0)
+        b.set_launch_config(32, 5)
+        a.step(300)
+        b.step(300)
+        b.check_stable()
+        sa, sb = a.download(), b.download()
+    for k in sa:
+        assert gi.rel_err(sb[k], sa[k]) < 1e-13, k
