@@ -36,6 +36,7 @@
 // ulp or two of libm's).
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <string>
@@ -407,15 +408,6 @@ __device__ int clip_cell(double* vx, double* vy, int* lab, int n, double dx, dou
   return m;
 }
 
-// does the bisector with a point at offset (dx, dy) cut the cell by more
-// than rel * |d|^2 / 2 (a margin above the rounding of computed vertices)?
-__device__ bool cuts_cell(const double* vx, const double* vy, int n, double dx, double dy, double d2, double rel) {
-  const double c = 0.5 * d2;
-  for (int a = 0; a < n; ++a)
-    if (vx[a] * dx + vy[a] * dy - c > rel * c) return true;
-  return false;
-}
-
 // The Delaunay neighbours of point query[q] (or q), counter-clockwise, as
 // the labels of its cell's edges (-1: an unbounded cell, the point is on the
 // convex hull).  The buckets are visited ring by ring, up to ring kRings; a
@@ -503,8 +495,8 @@ __global__ void __launch_bounds__(kTpb) k_star(Grid g, const int* __restrict__ q
 
 // One CTA per cell handed over by k_star: every point of the set is tested
 // against the cell in parallel; those whose bisector cuts it (a superset of
-// the missing neighbours: the cell only shrinks) are collected and clipped
-// in order of distance by one thread.
+// the missing neighbours: the cell only shrinks) are collected, then clipped
+// nearest first in rounds.
 constexpr int kScanThreads = 256, kScanCand = 2048;
 
 __global__ void __launch_bounds__(kScanThreads) k_star_scan(const double* __restrict__ X, const double* __restrict__ Y,
@@ -512,6 +504,7 @@ __global__ void __launch_bounds__(kScanThreads) k_star_scan(const double* __rest
                                                             int* __restrict__ nbr, int* __restrict__ nnb,
                                                             int* __restrict__ flags) {
   __shared__ double svx[kMaxV], svy[kMaxV];
+  __shared__ float fvx[kMaxV], fvy[kMaxV];
   __shared__ int slab[kMaxV];
   __shared__ int cand[kScanCand];
   __shared__ double cd2[kScanCand];
@@ -523,57 +516,112 @@ __global__ void __launch_bounds__(kScanThreads) k_star_scan(const double* __rest
   for (int a = threadIdx.x; a < n0; a += blockDim.x) {
     svx[a] = slow.vx[(int64_t)q * kMaxV + a];
     svy[a] = slow.vy[(int64_t)q * kMaxV + a];
+    fvx[a] = (float)svx[a];
+    fvy[a] = (float)svy[a];
     slab[a] = slow.lab[(int64_t)q * kMaxV + a];
   }
   if (threadIdx.x == 0) ncand = 0;
   __syncthreads();
   for (int i = threadIdx.x; i < npts; i += blockDim.x) {
     if (i == ip) continue;
+    const double dx = X[i] - px, dy = Y[i] - py;
+    const double d2 = dx * dx + dy * dy;
+    if (d2 == 0.0) continue;
+    // the cut test in FP32 first: with g = v.d - c, |g32 - g| stays below
+    // 1e-6 (|vx dx| + |vy dy| + c) (conversions and products round to 2^-24
+    // each), so only a vertex within that margin of the threshold needs FP64
+    const double c = 0.5 * d2;
+    const float fdx = (float)dx, fdy = (float)dy, fc = (float)c;
+    const float thr = fc * 1e-12f;
+    bool cut = false;
+    for (int a = 0; a < n0 && !cut; ++a) {
+      const float gx = fvx[a] * fdx, gy = fvy[a] * fdy;
+      const float g = gx + gy - fc;
+      const float err = (fabsf(gx) + fabsf(gy) + fc) * 1e-6f;
+      if (g > thr + err) cut = true;
+      else if (g >= -err) cut = svx[a] * dx + svy[a] * dy - c > 1e-12 * c;
+    }
+    if (!cut) continue;
     bool known = false;                 // already a neighbour: its bisector holds an edge
     for (int a = 0; a < n0; ++a) known |= slab[a] == i;
     if (known) continue;
-    const double dx = X[i] - px, dy = Y[i] - py;
-    const double d2 = dx * dx + dy * dy;
-    if (d2 == 0.0 || !cuts_cell(svx, svy, n0, dx, dy, d2, 1e-12)) continue;
     const int at = atomicAdd(&ncand, 1);
     if (at < kScanCand) { cand[at] = i; cd2[at] = d2; }
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
   const int nc = ncand;
   if (nc > kScanCand) {
-    atomicAdd(flags + kPolyOverflow, 1);
-    nnb[q] = 0;
+    if (threadIdx.x == 0) {
+      atomicAdd(flags + kPolyOverflow, 1);
+      nnb[q] = 0;
+    }
     return;
   }
-  // nearest first (ties by index, so the order is fixed)
-  for (int a = 1; a < nc; ++a) {
-    const int ci = cand[a];
-    const double cv = cd2[a];
-    int b = a - 1;
-    while (b >= 0 && (cd2[b] > cv || (cd2[b] == cv && cand[b] > ci))) {
-      cand[b + 1] = cand[b]; cd2[b + 1] = cd2[b]; --b;
+  // Rounds: every thread finds, among its candidates, the nearest one (ties
+  // by index) whose bisector still cuts the cell; the block's nearest is
+  // clipped by thread 0.  The cell only shrinks, so a candidate that stops
+  // cutting never cuts again; the rounds end when none cuts (about as many
+  // rounds as the cell has edges).
+  __shared__ int sn;
+  __shared__ double sr2;
+  __shared__ double bd2[kScanThreads / 32];
+  __shared__ int bix[kScanThreads / 32];
+  if (threadIdx.x == 0) {
+    sn = n0;
+    double r2 = 0.0;
+    for (int a = 0; a < n0; ++a) r2 = fmax(r2, svx[a] * svx[a] + svy[a] * svy[a]);
+    sr2 = r2;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int round = 0; round <= nc; ++round) {
+    const int n = sn;
+    const double r2max = sr2;
+    double best = INFINITY;
+    int bi = INT_MAX;
+    for (int j = threadIdx.x; j < nc; j += blockDim.x) {
+      const double d2 = cd2[j];
+      if (0.25 * d2 >= r2max || cand[j] < 0) continue;
+      const double dx = X[cand[j]] - px, dy = Y[cand[j]] - py;
+      const double c = 0.5 * d2;
+      bool cut = false;
+      for (int a = 0; a < n && !cut; ++a) cut = svx[a] * dx + svy[a] * dy - c > 0.0;
+      if (!cut) { cand[j] = -1; continue; }       // never cuts again
+      if (d2 < best || (d2 == best && cand[j] < bi)) { best = d2; bi = cand[j]; }
     }
-    cand[b + 1] = ci; cd2[b + 1] = cv;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) { bd2[wid] = best; bix[wid] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+        if (bd2[w] < best || (bd2[w] == best && bix[w] < bi)) { best = bd2[w]; bi = bix[w]; }
+      if (bi == INT_MAX) {
+        sn = -sn - 1;                                  // done (the count, encoded)
+      } else {
+        double r2 = r2max;
+        const int m = clip_cell(svx, svy, slab, n, X[bi] - px, Y[bi] - py, best, bi, &r2);
+        sn = m;
+        sr2 = r2;
+        for (int j = 0; j < nc; ++j)
+          if (cand[j] == bi) { cand[j] = -1; break; }
+      }
+    }
+    __syncthreads();
+    if (sn <= 0) break;
   }
-  double vx[kMaxV], vy[kMaxV];
-  int lab[kMaxV];
-  int n = n0;
-  for (int a = 0; a < n; ++a) { vx[a] = svx[a]; vy[a] = svy[a]; lab[a] = slab[a]; }
-  double r2max = 0.0;
-  for (int a = 0; a < n; ++a) r2max = fmax(r2max, vx[a] * vx[a] + vy[a] * vy[a]);
-  for (int c = 0; c < nc && n > 0; ++c) {
-    const int iq = cand[c];
-    if (0.25 * cd2[c] >= r2max) continue;
-    n = clip_cell(vx, vy, lab, n, X[iq] - px, Y[iq] - py, cd2[c], iq, &r2max);
-  }
-  if (n <= 0) {
+  if (threadIdx.x != 0) return;
+  const int n = sn < 0 ? -sn - 1 : sn;
+  if (sn == 0 || n <= 0) {
     atomicAdd(flags + kPolyOverflow, 1);
     nnb[q] = 0;
     return;
   }
   nnb[q] = n;
-  for (int a = 0; a < n; ++a) nbr[(int64_t)q * kMaxV + a] = lab[a];
+  for (int a = 0; a < n; ++a) nbr[(int64_t)q * kMaxV + a] = slab[a];
 }
 
 // numpy's float64 sum of a short contiguous array (pairwise_sum: a plain
