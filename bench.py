@@ -440,13 +440,19 @@ def survey_bytes(form, C, M, G=0, ecm=False):
 
 
 def roofline_entry(bytes_per_step, s_per_step, kernel, note=None, survey=None):
+    """achieved = algorithmic bytes per time step / time per step.  With
+    `survey` (the per-membrane count of survey_bytes, the step's algorithmic
+    bytes by definition) that count is the one `achieved` and `frac` use;
+    the bytes the chosen kernel's own layout reads and writes stand beside
+    it (kernel_bytes_per_step, frac_on_kernel_bytes)."""
     hbm, src = peaks()
-    a = bytes_per_step / s_per_step / 1e9
+    algo = bytes_per_step if survey is None else survey
+    a = algo / s_per_step / 1e9
     r = {'bound': 'hbm', 'achieved': a, 'peak': hbm, 'unit': 'GB/s', 'frac': a / hbm,
-         'algorithmic_bytes_per_step': int(bytes_per_step), 'kernel': kernel, 'peak_source': src}
+         'algorithmic_bytes_per_step': int(algo), 'kernel': kernel, 'peak_source': src}
     if survey is not None:
-        r['survey_bytes_per_step'] = int(survey)
-        r['frac_on_survey_bytes'] = survey / s_per_step / 1e9 / hbm
+        r['kernel_bytes_per_step'] = int(bytes_per_step)
+        r['frac_on_kernel_bytes'] = bytes_per_step / s_per_step / 1e9 / hbm
     if note:
         r['note'] = note
     return r
@@ -522,7 +528,7 @@ def config_ecm20k(wl, stream, flush, cpu=True):
                      'ms_per_time_step': ms / T,
                      'roofline': roofline_entry(sv, ms / 1e3 / T, 'whole step (cell kernel + grid stencils)',
                                                 note='bytes by the per-array count with the grid terms; the '
-                                                     'per-kernel shares are in profiles/launch_list_ecm20k.md')}
+                                                     'per-kernel shares are in profiles/ecm_step_kernels_ecm20k.md')}
     out['value'] = out['fp64']['value']
     out['unit'] = UNIT
     out['form'] = 'plain FP64 (split form beside it)'
@@ -549,9 +555,9 @@ def config_sweep512(wl, stream, flush, cpu=True):
            'form': 'split', 'value': M * T / (ms / 1e3), 'unit': UNIT, 'ms_per_run': ms,
            'autotuned': {'tpb': tpb, 'kernel': kname}, 'autotune_table': table,
            'roofline': roofline_entry(kb, kms / 1e3, kname, survey=survey_bytes('split', C, M),
-                                      note='algorithmic bytes of the kernel that runs (the factored form '
-                                           'reads one sum of Dm*mem_sa per cell instead of Dm per membrane); '
-                                           'frac_on_survey_bytes counts the per-membrane arrays instead')}
+                                      note='algorithmic bytes of the split step (64 B per membrane + 112 B per '
+                                           'cell); kernel_bytes_per_step is what the factored layout moves (one '
+                                           'sum of Dm*mem_sa per cell instead of Dm per membrane)')}
     S.close()
     if cpu:
         out['cpu_baseline'] = cpu_baseline_sweep(gs, ps, Dms, sts, budget_s=8.0)
@@ -958,11 +964,12 @@ def main():
         tj = json.load(open(tp))
         traffic = int(tj.get('dram_bytes_per_step', tj.get('dram_bytes_per_launch')) * n_mems / tj['membranes'])
     roof = roofline_entry(kbytes, kern_ms / 1e3, kname, survey=survey_bytes('split', n_cells, n_mems),
-                          note='achieved = the chosen kernel\'s algorithmic bytes per time step (each array once '
-                               'at its stored width; the factored kernels read one sum of Dm*mem_sa per cell '
-                               'where the per-membrane form reads Dm per membrane) / its time per step; the '
-                               'resident kernel keeps that data in shared memory across steps, so HBM does '
-                               'not bound it; frac_on_survey_bytes counts the per-membrane arrays')
+                          note='achieved = the split step\'s algorithmic bytes per time step (64 B per membrane '
+                               '+ 112 B per cell: each per-membrane and per-cell array once at its stored width) '
+                               '/ the chosen kernel\'s time per step; kernel_bytes_per_step is what the factored '
+                               'layout itself moves (one sum of Dm*mem_sa per cell instead of Dm per membrane); '
+                               'the resident kernel keeps its data in shared memory across steps, so HBM does '
+                               'not bound it')
     roof['traffic'] = traffic
     roof['ms_per_step'] = kern_ms
 
