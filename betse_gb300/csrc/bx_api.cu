@@ -784,7 +784,7 @@ cudaError_t launch_cell(bx_cluster* h, int parity, bool out, cudaStream_t s) {
 cudaError_t enqueue_env_pre(bx_cluster* h, cudaStream_t s) {
   bx::EnvConst ec = make_env_const(h);
   const int gi = env_grid(h->G * h->I);
-  bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
+  bx::k_env_np_flux<double><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
   bx::k_env_update<false><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_fx, h->d_fy, h->d_env_ptr,
                                                 h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
   h->launches += 2;
@@ -806,7 +806,7 @@ cudaError_t enqueue_env(bx_cluster* h, bool out, cudaStream_t s) {
                                                 h->d_mem_flux_sa, h->M, ec);
     h->launches += 1;
   } else if (h->par.sharpness < 1.0) {
-    bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
+    bx::k_env_np_flux<double><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
     bx::k_env_update<false><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_fx, h->d_fy, h->d_env_ptr,
                                                   h->d_env_mem, h->d_mem_flux_sa, h->M, ec);
     bx::k_env_integrate_scatter<true><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_tmp2, h->d_env_ptr,
@@ -814,15 +814,25 @@ cudaError_t enqueue_env(bx_cluster* h, bool out, cudaStream_t s) {
     h->launches += 3;
   } else {
     // the common configuration: flux, then update + charge fused, then the
-    // fields in one tiled launch (4 launches per step with the cell kernel)
-    bx::k_env_np_flux<<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
+    // fields in one tiled launch (4 launches per step with the cell kernel);
+    // the split form runs these stencils in FP32 around FP64 state
     const unsigned gc = (unsigned)(((size_t)h->G * 8 + 255) / 256);
-    bx::k_env_update_charge<<<gc, 256, 0, s>>>(h->d_cenv, h->d_fx, h->d_fy, h->d_env_ptr, h->d_env_mem,
-                                               h->d_mem_flux_sa, h->M, h->d_touched, h->d_vsrc,
-                                               out ? h->d_rho_env : nullptr, ec);
     const dim3 gt((unsigned)((h->nx + bx::kEnvTX - 1) / bx::kEnvTX), (unsigned)((h->ny + bx::kEnvTY - 1) / bx::kEnvTY));
-    bx::k_env_fields_tile<<<gt, bx::kEnvTX * bx::kEnvTY, 0, s>>>(h->d_vsrc, h->phib_nonzero ? h->d_phib : nullptr,
-                                                                h->d_venv, ec.screen, h->d_Ex, h->d_Ey, ec);
+    const double* phib = h->phib_nonzero ? h->d_phib : nullptr;
+    double* rho = out ? h->d_rho_env : nullptr;
+    if (h->mode == MODE_SPLIT) {
+      bx::k_env_np_flux<float><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
+      bx::k_env_update_charge<float><<<gc, 256, 0, s>>>(h->d_cenv, h->d_fx, h->d_fy, h->d_env_ptr, h->d_env_mem,
+                                                        h->d_mem_flux_sa, h->M, h->d_touched, h->d_vsrc, rho, ec);
+      bx::k_env_fields_tile<float><<<gt, bx::kEnvTX * bx::kEnvTY, 0, s>>>(h->d_vsrc, phib, h->d_venv, ec.screen,
+                                                                         h->d_Ex, h->d_Ey, ec);
+    } else {
+      bx::k_env_np_flux<double><<<gi, kEnvTPB, 0, s>>>(h->d_cenv, h->d_Denv, h->d_Ex, h->d_Ey, h->d_fx, h->d_fy, ec);
+      bx::k_env_update_charge<double><<<gc, 256, 0, s>>>(h->d_cenv, h->d_fx, h->d_fy, h->d_env_ptr, h->d_env_mem,
+                                                         h->d_mem_flux_sa, h->M, h->d_touched, h->d_vsrc, rho, ec);
+      bx::k_env_fields_tile<double><<<gt, bx::kEnvTX * bx::kEnvTY, 0, s>>>(h->d_vsrc, phib, h->d_venv, ec.screen,
+                                                                          h->d_Ex, h->d_Ey, ec);
+    }
     h->launches += 3;
     return cudaGetLastError();
   }

@@ -37,7 +37,10 @@ __device__ __forceinline__ double cb_at(const double* c, const EnvConst& e, int 
 // The grid kernels multiply by 1/delta and 1/(2 delta) where the reference
 // divides (a difference of at most one rounding): an FP64 division costs
 // GB300 several FP64-pipe operations, and the stencils are otherwise cheap.
+// R = float is the split form's stencil: the concentration differences are
+// taken in FP64 (the state) and scaled, with the drift term, in FP32.
 // One thread per (ion, grid cell): t = ion*G + k.
+template <typename R>
 __global__ void k_env_np_flux(const double* __restrict__ cenv, const double* __restrict__ Denv,
                               const double* __restrict__ Ex, const double* __restrict__ Ey,
                               double* fx, double* fy, EnvConst e) {
@@ -47,35 +50,40 @@ __global__ void k_env_np_flux(const double* __restrict__ cenv, const double* __r
   const int i = k / e.nx, j = k - i * e.nx;
   {
     const double c0 = cb_at(cenv, e, ion, i, j);
-    double gcx, gcy;
-    if (j == 0) gcx = (cb_at(cenv, e, ion, i, 1) - c0) * e.inv_delta;
-    else if (j == e.nx - 1) gcx = (c0 - cb_at(cenv, e, ion, i, j - 1)) * e.inv_delta;
-    else gcx = -(cb_at(cenv, e, ion, i, j - 1) - cb_at(cenv, e, ion, i, j + 1)) * e.inv_2delta;
-    if (i == 0) gcy = (cb_at(cenv, e, ion, 1, j) - c0) * e.inv_delta;
-    else if (i == e.ny - 1) gcy = (c0 - cb_at(cenv, e, ion, i - 1, j)) * e.inv_delta;
-    else gcy = -(cb_at(cenv, e, ion, i - 1, j) - cb_at(cenv, e, ion, i + 1, j)) * e.inv_2delta;
-    const double D = Denv[(size_t)ion * e.G + k];
-    const double alpha = D * e.np_alpha[ion];
-    const double gvx = -Ex[k], gvy = -Ey[k];
-    fx[(size_t)ion * e.G + k] = -D * gcx - alpha * gvx * c0;
-    fy[(size_t)ion * e.G + k] = -D * gcy - alpha * gvy * c0;
+    const R inv_d = (R)e.inv_delta, inv_2d = (R)e.inv_2delta;
+    R gcx, gcy;
+    if (j == 0) gcx = (R)(cb_at(cenv, e, ion, i, 1) - c0) * inv_d;
+    else if (j == e.nx - 1) gcx = (R)(c0 - cb_at(cenv, e, ion, i, j - 1)) * inv_d;
+    else gcx = -(R)(cb_at(cenv, e, ion, i, j - 1) - cb_at(cenv, e, ion, i, j + 1)) * inv_2d;
+    if (i == 0) gcy = (R)(cb_at(cenv, e, ion, 1, j) - c0) * inv_d;
+    else if (i == e.ny - 1) gcy = (R)(c0 - cb_at(cenv, e, ion, i - 1, j)) * inv_d;
+    else gcy = -(R)(cb_at(cenv, e, ion, i - 1, j) - cb_at(cenv, e, ion, i + 1, j)) * inv_2d;
+    const R D = (R)Denv[(size_t)ion * e.G + k];
+    const R alpha = D * (R)e.np_alpha[ion];
+    const R gvx = -(R)Ex[k], gvy = -(R)Ey[k];
+    fx[(size_t)ion * e.G + k] = (double)(-D * gcx - alpha * gvx * (R)c0);
+    fy[(size_t)ion * e.G + k] = (double)(-D * gcy - alpha * gvy * (R)c0);
   }
 }
 
 // fd.diff with the reference's flipped one-sided edge signs (finitediff.py:1268-1303)
-__device__ __forceinline__ double ddx_neg(const double* f, const EnvConst& e, int i, int j) {
+template <typename R = double>
+__device__ __forceinline__ R ddx_neg(const double* f, const EnvConst& e, int i, int j) {
   // diff(-f, axis=0)
   const double* r = f + i * e.nx;
-  if (j == 0) return ((-r[0]) - (-r[1])) * e.inv_delta;
-  if (j == e.nx - 1) return ((-r[j - 1]) - (-r[j])) * e.inv_delta;
-  return -((-r[j - 1]) - (-r[j + 1])) * e.inv_2delta;
+  const R inv_d = (R)e.inv_delta, inv_2d = (R)e.inv_2delta;
+  if (j == 0) return ((-(R)r[0]) - (-(R)r[1])) * inv_d;
+  if (j == e.nx - 1) return ((-(R)r[j - 1]) - (-(R)r[j])) * inv_d;
+  return -((-(R)r[j - 1]) - (-(R)r[j + 1])) * inv_2d;
 }
-__device__ __forceinline__ double ddy_neg(const double* f, const EnvConst& e, int i, int j) {
+template <typename R = double>
+__device__ __forceinline__ R ddy_neg(const double* f, const EnvConst& e, int i, int j) {
   // diff(-f, axis=1)
   const int nx = e.nx;
-  if (i == 0) return -((-f[nx + j]) - (-f[j])) * e.inv_delta;
-  if (i == e.ny - 1) return -((-f[i * nx + j]) - (-f[(i - 1) * nx + j])) * e.inv_delta;
-  return -((-f[(i - 1) * nx + j]) - (-f[(i + 1) * nx + j])) * e.inv_2delta;
+  const R inv_d = (R)e.inv_delta, inv_2d = (R)e.inv_2delta;
+  if (i == 0) return -((-(R)f[nx + j]) - (-(R)f[j])) * inv_d;
+  if (i == e.ny - 1) return -((-(R)f[i * nx + j]) - (-(R)f[(i - 1) * nx + j])) * inv_d;
+  return -((-(R)f[(i - 1) * nx + j]) - (-(R)f[(i + 1) * nx + j])) * inv_2d;
 }
 
 // Environment charge of grid cell k from its new concentrations, for
@@ -239,6 +247,9 @@ __global__ void k_env_neg_grad(const double* __restrict__ F, double scale, doubl
 // cell (lane = ion, I <= 8): each lane advances its ion's concentration in
 // place (it reads only fluxes and its own cell's value), then the cell's
 // group sums F z_i c_i over the ions in order through shuffles.
+// R = float (split form): the divergence of the FP32 fluxes in FP32; the
+// concentration, the membrane exchange and the charge stay FP64.
+template <typename R>
 __global__ void __launch_bounds__(256) k_env_update_charge(double* cenv, const double* __restrict__ fx,
                                                            const double* __restrict__ fy,
                                                            const int* __restrict__ env_ptr,
@@ -254,8 +265,8 @@ __global__ void __launch_bounds__(256) k_env_update_charge(double* cenv, const d
     const int i = k / e.nx, j = k - i * e.nx;
     const double* fxi = fx + (size_t)ion * e.G;
     const double* fyi = fy + (size_t)ion * e.G;
-    const double div = ddx_neg(fxi, e, i, j) + ddy_neg(fyi, e, i, j);
-    double c = cb_at(cenv, e, ion, i, j) + div * e.dt;
+    const R div = ddx_neg<R>(fxi, e, i, j) + ddy_neg<R>(fyi, e, i, j);
+    double c = cb_at(cenv, e, ion, i, j) + (double)(div * (R)e.dt);
     double s = 0.0;
     for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
     c = c + (s * e.inv_h_d2) * e.dt;
@@ -279,29 +290,31 @@ __global__ void __launch_bounds__(256) k_env_update_charge(double* cenv, const d
 constexpr int kEnvTX = 32, kEnvTY = 16;
 constexpr int kEnvVX = kEnvTX + 2, kEnvVY = kEnvTY + 2;        // v_env tile (gradient halo)
 constexpr int kEnvSX = kEnvVX + 8, kEnvSY = kEnvVY + 8;        // source tile (Gaussian halo)
+// R = float (split form): both passes and the gradient in FP32.
+template <typename R>
 __global__ void __launch_bounds__(kEnvTX * kEnvTY) k_env_fields_tile(const double* __restrict__ vsrc,
                                                                      const double* __restrict__ phib,
                                                                      double* venv, double scale, double* Ex,
                                                                      double* Ey, EnvConst e) {
-  __shared__ double src[kEnvSY][kEnvSX];
-  __shared__ double gy[kEnvVY][kEnvSX];
-  __shared__ double v[kEnvVY][kEnvVX];
+  __shared__ R src[kEnvSY][kEnvSX];
+  __shared__ R gy[kEnvVY][kEnvSX];
+  __shared__ R v[kEnvVY][kEnvVX];
   const int i0 = blockIdx.y * kEnvTY - 1 - 4, j0 = blockIdx.x * kEnvTX - 1 - 4;   // src tile origin
   const int nt = blockDim.x;
   for (int q = threadIdx.x; q < kEnvSY * kEnvSX; q += nt) {
     const int a = q / kEnvSX, b = q - a * kEnvSX, i = i0 + a, j = j0 + b;
-    src[a][b] = (i >= 0 && i < e.ny && j >= 0 && j < e.nx) ? vsrc[i * e.nx + j] : 0.0;
+    src[a][b] = (i >= 0 && i < e.ny && j >= 0 && j < e.nx) ? (R)vsrc[i * e.nx + j] : (R)0;
   }
   __syncthreads();
   // axis-0 pass (zero padding: taps outside the grid are skipped, as k_env_gauss_y does)
   for (int q = threadIdx.x; q < kEnvVY * kEnvSX; q += nt) {
     const int a = q / kEnvSX, b = q - a * kEnvSX, i = i0 + 4 + a;
-    double acc = 0.0;
+    R acc = 0;
 #pragma unroll
     for (int w = -4; w <= 4; ++w) {
       const int ii = i + w;
       if (ii < 0 || ii >= e.ny) continue;
-      acc += e.gw[w + 4] * src[a + 4 + w][b];
+      acc += (R)e.gw[w + 4] * src[a + 4 + w][b];
     }
     gy[a][b] = acc;
   }
@@ -309,14 +322,14 @@ __global__ void __launch_bounds__(kEnvTX * kEnvTY) k_env_fields_tile(const doubl
   // axis-1 pass + Phi_b -> v_env on the tile and its one-cell halo
   for (int q = threadIdx.x; q < kEnvVY * kEnvVX; q += nt) {
     const int a = q / kEnvVX, b = q - a * kEnvVX, i = i0 + 4 + a, j = j0 + 4 + b;
-    double acc = 0.0;
+    R acc = 0;
     for (int w = -4; w <= 4; ++w) {
       const int jj = j + w;
       if (jj < 0 || jj >= e.nx) continue;
-      acc += e.gw[w + 4] * gy[a][b + 4 + w];
+      acc += (R)e.gw[w + 4] * gy[a][b + 4 + w];
     }
     const bool in = i >= 0 && i < e.ny && j >= 0 && j < e.nx;
-    v[a][b] = in ? acc + (phib ? phib[i * e.nx + j] : 0.0) : 0.0;
+    v[a][b] = in ? acc + (phib ? (R)phib[i * e.nx + j] : (R)0) : (R)0;
   }
   __syncthreads();
   // E = -gradient(scale * v_env), one-sided on the grid edges
@@ -324,17 +337,18 @@ __global__ void __launch_bounds__(kEnvTX * kEnvTY) k_env_fields_tile(const doubl
   const int i = blockIdx.y * kEnvTY + a - 1, j = blockIdx.x * kEnvTX + b - 1;
   if (i >= e.ny || j >= e.nx) return;
   const int k = i * e.nx + j;
-  venv[k] = v[a][b];
-  auto f = [&](int da, int db) { return scale * v[a + da][b + db]; };
-  double gx, gyy;
-  if (j == 0) gx = (f(0, 1) - f(0, 0)) * e.inv_delta;
-  else if (j == e.nx - 1) gx = (f(0, 0) - f(0, -1)) * e.inv_delta;
-  else gx = -(f(0, -1) - f(0, 1)) * e.inv_2delta;
-  if (i == 0) gyy = (f(1, 0) - f(0, 0)) * e.inv_delta;
-  else if (i == e.ny - 1) gyy = (f(0, 0) - f(-1, 0)) * e.inv_delta;
-  else gyy = -(f(-1, 0) - f(1, 0)) * e.inv_2delta;
-  Ex[k] = -gx;
-  Ey[k] = -gyy;
+  venv[k] = (double)v[a][b];
+  const R sc = (R)scale, inv_d = (R)e.inv_delta, inv_2d = (R)e.inv_2delta;
+  auto f = [&](int da, int db) { return sc * v[a + da][b + db]; };
+  R gx, gyy;
+  if (j == 0) gx = (f(0, 1) - f(0, 0)) * inv_d;
+  else if (j == e.nx - 1) gx = (f(0, 0) - f(0, -1)) * inv_d;
+  else gx = -(f(0, -1) - f(0, 1)) * inv_2d;
+  if (i == 0) gyy = (f(1, 0) - f(0, 0)) * inv_d;
+  else if (i == e.ny - 1) gyy = (f(0, 0) - f(-1, 0)) * inv_d;
+  else gyy = -(f(-1, 0) - f(1, 0)) * inv_2d;
+  Ex[k] = (double)(-gx);
+  Ey[k] = (double)(-gyy);
 }
 
 // ---------------------------------------------------------------------------
