@@ -14,12 +14,16 @@
 //   Yhat = H3 Wd^T + bd
 // Training is BF16 with FP32 master weights: products read BF16 copies of the
 // weights and BF16 activations and accumulate in FP32; gradients and Adam
-// moments are FP32.  The products are 64 x 64 per node, far below tensor-core
-// tile sizes per node and bound by the activation traffic, so each layer is
-// one fused kernel: a warp per node, the two 64 x 64 weight matrices in shared
-// memory, the node's input row broadcast by warp shuffles.  Weight gradients
-// are per-block partial sums reduced in a fixed order (deterministic, no
-// floating-point atomics).
+// moments are FP32.  A forward layer is a tall product [nodes x 64] [64 x 64]
+// (two of them for a message layer): it runs on the tensor cores, one CTA per
+// 128 nodes, the activation tile and the weights staged in shared memory in
+// the canonical K-major core-matrix layout, tcgen05.mma (BF16 x BF16 -> FP32
+// in TMEM, M = 128, N = 64, K = 16 per instruction) issued by one thread, and
+// four warps reading the accumulator back for the bias, activation and
+// residual epilogue.  The backward products take FP32 gradients and stay on
+// the FMA pipe: a warp per node, the weights in shared memory.  Weight
+// gradients are per-block partial sums reduced in a fixed order
+// (deterministic, no floating-point atomics).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -29,6 +33,7 @@
 #include <vector>
 
 #include "../../include/bx.h"
+#include "bx_tc.cuh"
 
 // error text for bx_last_error (defined with the other entry points)
 void bx_record_error(const char* msg);
@@ -57,61 +62,130 @@ __global__ void k_pack_x(int rows, int n_in, const float* __restrict__ x, bf16* 
   X[t] = __float2bfloat16_rn(f < n_in ? x[(size_t)i * n_in + f] : 0.0f);
 }
 
+// ---- forward layers on the tensor cores
+constexpr int kTcRows = 128;                         // nodes per CTA (the MMA's M)
+constexpr int kTcThreads = 128;                      // four warps: TMEM lanes 32 w .. 32 w + 31
+constexpr int kActTile = kTcRows * W * 2;            // 16 KB of BF16
+constexpr int kWTile = W * W * 2;                    // 8 KB
+constexpr int kTcSmem = 2 * (kActTile + kWTile) + 1024;
+// kind::f16: FP32 accumulator, BF16 A and B, both K-major, N = 64, M = 128
+constexpr uint32_t kIdescFwd = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(W >> 3) << 17) |
+                               ((uint32_t)(kTcRows >> 4) << 24);
+
+// Rows [0, rows) of a row-major [*][64] BF16 array into a tile in the
+// canonical no-swizzle K-major layout: 8 x 16-byte core matrices, the 8
+// K-adjacent cores of an 8-row group contiguous (128 B apart), 8-row groups
+// 1024 B apart; rows at or past `valid` are zero.
+__device__ __forceinline__ void stage_tile(uint8_t* tile, const bf16* __restrict__ src, int rows, int valid) {
+  for (int e = threadIdx.x; e < rows * 8; e += blockDim.x) {
+    const int r = e >> 3, c = e & 7;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (r < valid) v = reinterpret_cast<const uint4*>(src + (size_t)r * W)[c];
+    *reinterpret_cast<uint4*>(tile + ((r >> 3) * 8 + c) * 128 + (r & 7) * 16) = v;
+  }
+}
+
 // MODE 0: encoder  H = relu(in1 W1^T + b)
 // MODE 1: message  R = relu(in1 W1^T + in2 W2^T + b), H = in1 + R
 // MODE 2: decoder  Y = in1 W1^T + b (FP32, first n_out columns)
+// A wait that runs out (about two seconds) raises *err and leaves the rows
+// unwritten; the TMEM is freed either way.
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_fwd(int n, const bf16* __restrict__ in1, const bf16* __restrict__ in2,
-                                                  const bf16* __restrict__ wb, int off_w1, int off_w2,
-                                                  const float* __restrict__ master, int off_b,
-                                                  bf16* __restrict__ outR, bf16* __restrict__ outH,
-                                                  float* __restrict__ outY, int n_out) {
-  __shared__ float w1t[W * W];
-  __shared__ float w2t[MODE == 1 ? W * W : 1];
-  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-    const int f = e / W, k = e - f * W;  // W[f][k]
-    w1t[k * W + f] = __bfloat162float(wb[off_w1 + e]);
-    if (MODE == 1) w2t[k * W + f] = __bfloat162float(wb[off_w2 + e]);
+__global__ void __launch_bounds__(kTcThreads) k_fwd_tc(int n, const bf16* __restrict__ in1, const bf16* __restrict__ in2,
+                                                       const bf16* __restrict__ wb, int off_w1, int off_w2,
+                                                       const float* __restrict__ master, int off_b,
+                                                       bf16* __restrict__ outR, bf16* __restrict__ outH,
+                                                       float* __restrict__ outY, int n_out, unsigned* err) {
+  using namespace bxtc;
+  extern __shared__ uint8_t tc_smem_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* a1 = sm;
+  uint8_t* b1 = a1 + kActTile;
+  uint8_t* a2 = b1 + kWTile;
+  uint8_t* b2 = a2 + kActTile;
+  __shared__ __align__(8) uint64_t done;
+  __shared__ uint32_t tmem_base;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r0 = blockIdx.x * kTcRows;
+  const int valid = min(kTcRows, n - r0);
+
+  stage_tile(a1, in1 + (size_t)r0 * W, kTcRows, valid);
+  stage_tile(b1, wb + off_w1, W, W);
+  if (MODE == 1) {
+    stage_tile(a2, in2 + (size_t)r0 * W, kTcRows, valid);
+    stage_tile(b2, wb + off_w2, W, W);
   }
+  // the tensor core reads shared memory through the async proxy
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(W));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  const float bias0 = master[off_b + lane], bias1 = master[off_b + lane + 32];
-  for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n; i += nw) {
-    const float2 x1 = ld_bf2(in1 + (size_t)i * W, lane);
-    float2 x2 = make_float2(0.f, 0.f);
-    if (MODE == 1) x2 = ld_bf2(in2 + (size_t)i * W, lane);
-    float a0 = bias0, a1 = bias1;
-#pragma unroll 8
-    for (int src = 0; src < 32; ++src) {
-      const int k = 2 * src;
-      const float u0 = __shfl_sync(FULL, x1.x, src), u1 = __shfl_sync(FULL, x1.y, src);
-      a0 = fmaf(w1t[k * W + lane], u0, a0);
-      a0 = fmaf(w1t[(k + 1) * W + lane], u1, a0);
-      a1 = fmaf(w1t[k * W + lane + 32], u0, a1);
-      a1 = fmaf(w1t[(k + 1) * W + lane + 32], u1, a1);
-      if (MODE == 1) {
-        const float v0 = __shfl_sync(FULL, x2.x, src), v1 = __shfl_sync(FULL, x2.y, src);
-        a0 = fmaf(w2t[k * W + lane], v0, a0);
-        a0 = fmaf(w2t[(k + 1) * W + lane], v1, a0);
-        a1 = fmaf(w2t[k * W + lane + 32], v0, a1);
-        a1 = fmaf(w2t[(k + 1) * W + lane + 32], v1, a1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int kk = 0; kk < W / 16; ++kk) {     // two K-adjacent core matrices per MMA (K = 16)
+      const uint32_t o = (uint32_t)kk * 256u;
+      mma_f16(tmem, smem_desc(smem_u32(a1) + o, 128, 1024), smem_desc(smem_u32(b1) + o, 128, 1024), kIdescFwd,
+              kk > 0 ? 1u : 0u);
+    }
+    if (MODE == 1)
+#pragma unroll
+      for (int kk = 0; kk < W / 16; ++kk) {
+        const uint32_t o = (uint32_t)kk * 256u;
+        mma_f16(tmem, smem_desc(smem_u32(a2) + o, 128, 1024), smem_desc(smem_u32(b2) + o, 128, 1024), kIdescFwd,
+                1u);
+      }
+    mma_commit(smem_u32(&done));
+  }
+  __syncwarp();
+  const bool ok = __all_sync(FULL, mbar_wait(smem_u32(&done), 0u));
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    float v[W];
+#pragma unroll
+    for (int c0 = 0; c0 < W; c0 += 16) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v + c0);
+    const int r = r0 + warp * 32 + lane;
+    if (r < n) {
+      const size_t o = (size_t)r * W;
+#pragma unroll
+      for (int f = 0; f < W; ++f) v[f] += master[off_b + f];
+      if (MODE == 2) {
+        for (int f = 0; f < n_out; ++f) outY[(size_t)r * n_out + f] = v[f];
+      } else {
+#pragma unroll
+        for (int f8 = 0; f8 < W; f8 += 8) {
+          __align__(16) bf16 rr[8], hh[8];
+          const uint4 x = reinterpret_cast<const uint4*>(in1 + o)[f8 / 8];
+          const bf16* xb = reinterpret_cast<const bf16*>(&x);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            rr[q] = __float2bfloat16_rn(fmaxf(v[f8 + q], 0.f));
+            hh[q] = MODE == 1 ? __float2bfloat16_rn(__bfloat162float(xb[q]) + __bfloat162float(rr[q])) : rr[q];
+          }
+          if (MODE == 1) reinterpret_cast<uint4*>(outR + o)[f8 / 8] = *reinterpret_cast<const uint4*>(rr);
+          reinterpret_cast<uint4*>(outH + o)[f8 / 8] = *reinterpret_cast<const uint4*>(hh);
+        }
       }
     }
-    const size_t o = (size_t)i * W;
-    if (MODE == 0) {
-      outH[o + lane] = __float2bfloat16_rn(fmaxf(a0, 0.f));
-      outH[o + lane + 32] = __float2bfloat16_rn(fmaxf(a1, 0.f));
-    } else if (MODE == 1) {
-      const bf16 r0 = __float2bfloat16_rn(fmaxf(a0, 0.f)), r1 = __float2bfloat16_rn(fmaxf(a1, 0.f));
-      outR[o + lane] = r0;
-      outR[o + lane + 32] = r1;
-      outH[o + lane] = __float2bfloat16_rn(__bfloat162float(in1[o + lane]) + __bfloat162float(r0));
-      outH[o + lane + 32] = __float2bfloat16_rn(__bfloat162float(in1[o + lane + 32]) + __bfloat162float(r1));
-    } else {
-      if (lane < n_out) outY[(size_t)i * n_out + lane] = a0;
-      if (lane + 32 < n_out) outY[(size_t)i * n_out + lane + 32] = a1;
-    }
+  } else if (lane == 0) {
+    atomicOr(err, 1u);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(W));
   }
 }
 
@@ -322,6 +396,7 @@ struct bx_gnn {
   __nv_bfloat16* act = nullptr;             // N_PLANES x [cap][W]
   float *yhat = nullptr, *dY = nullptr, *dHa = nullptr, *dHb = nullptr, *dZ = nullptr, *G = nullptr;
   float *part = nullptr, *loss_part = nullptr, *loss = nullptr;
+  unsigned* err = nullptr;                  // a tensor-core wait ran out (k_fwd_tc)
   int nblk_wg = 0, nblk_loss = 0;
   int step = 0;
   cudaStream_t stream = nullptr;
@@ -371,6 +446,14 @@ int ensure_cap(bx_gnn* h, int rows) {
 
 __nv_bfloat16* plane(bx_gnn* h, int p) { return h->act + (size_t)p * h->cap * W; }
 
+// after a synchronisation: did a tensor-core wait run out?
+int check_tc(bx_gnn* h) {
+  unsigned e = 0;
+  NX(cudaMemcpy(&e, h->err, 4, cudaMemcpyDeviceToHost));
+  if (e) return nfail(BX_ECUDA, "network: a tensor-core wait timed out");
+  return BX_OK;
+}
+
 int check_range(bx_gnn* h, int lo, int hi) {
   if (!h->ptr) return nfail(BX_ESTATE, "network: bx_gnn_set_graph first");
   if (lo < 0 || hi <= lo || hi > h->n_graph) return nfail(BX_EINVAL, "network: node range outside the graph");
@@ -392,16 +475,18 @@ int forward(bx_gnn* h, int lo, int hi, const float* x, int n_in, int n_out) {
   const long long tot = (long long)n * W;
   k_pack_x<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, n_in, x, plane(h, P_X));
   const unsigned g = node_grid(n);
-  k_fwd<0><<<g, kThreads, 0, s>>>(n, plane(h, P_X), nullptr, h->wb, OFF_W0, 0, h->master, OFF_B0, nullptr,
-                                  plane(h, P_H0), nullptr, 0);
+  const unsigned gt = (unsigned)((n + kTcRows - 1) / kTcRows);
+  k_fwd_tc<0><<<gt, kTcThreads, kTcSmem, s>>>(n, plane(h, P_X), nullptr, h->wb, OFF_W0, 0, h->master, OFF_B0,
+                                              nullptr, plane(h, P_H0), nullptr, 0, h->err);
   for (int l = 0; l < NMP; ++l) {
     const int o = OFF_MP + l * MP_STRIDE;
     k_agg<<<g, kThreads, 0, s>>>(n, lo, h->ptr, h->nbr, plane(h, P_H0 + l), plane(h, P_A1 + l));
-    k_fwd<1><<<g, kThreads, 0, s>>>(n, plane(h, P_H0 + l), plane(h, P_A1 + l), h->wb, o, o + W * W, h->master,
-                                    o + 2 * W * W, plane(h, P_R1 + l), plane(h, P_H1 + l), nullptr, 0);
+    k_fwd_tc<1><<<gt, kTcThreads, kTcSmem, s>>>(n, plane(h, P_H0 + l), plane(h, P_A1 + l), h->wb, o, o + W * W,
+                                                h->master, o + 2 * W * W, plane(h, P_R1 + l), plane(h, P_H1 + l),
+                                                nullptr, 0, h->err);
   }
-  k_fwd<2><<<g, kThreads, 0, s>>>(n, plane(h, P_H3), nullptr, h->wb, OFF_WD, 0, h->master, OFF_BD, nullptr,
-                                  nullptr, h->yhat, n_out);
+  k_fwd_tc<2><<<gt, kTcThreads, kTcSmem, s>>>(n, plane(h, P_H3), nullptr, h->wb, OFF_WD, 0, h->master, OFF_BD,
+                                              nullptr, nullptr, h->yhat, n_out, h->err);
   NX(cudaGetLastError());
   return BX_OK;
 }
@@ -450,11 +535,23 @@ int bx_gnn_create(bx_gnn_handle* out) {
       cudaMalloc(&h->wb, P * 2) != cudaSuccess ||
       cudaMalloc(&h->part, (size_t)h->nblk_wg * (W * W + W) * 4) != cudaSuccess ||
       cudaMalloc(&h->loss_part, (size_t)h->nblk_loss * 4) != cudaSuccess ||
-      cudaMalloc(&h->loss, 4) != cudaSuccess || cudaStreamCreate(&h->stream) != cudaSuccess) {
+      cudaMalloc(&h->loss, 4) != cudaSuccess || cudaMalloc(&h->err, 4) != cudaSuccess ||
+      cudaStreamCreate(&h->stream) != cudaSuccess) {
     cudaGetLastError();
     bx_gnn_destroy(h);
     return nfail(BX_ENOMEM, "cudaMalloc network parameters");
   }
+  if (cudaFuncSetAttribute(bxn::k_fwd_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bxn::kTcSmem) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(bxn::k_fwd_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bxn::kTcSmem) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(bxn::k_fwd_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bxn::kTcSmem) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    bx_gnn_destroy(h);
+    return nfail(BX_ECUDA, "network: shared memory attribute of the tensor-core layers");
+  }
+  cudaMemset(h->err, 0, 4);
   cudaMemset(h->master, 0, P * 4);
   cudaMemset(h->m, 0, P * 4);
   cudaMemset(h->v, 0, P * 4);
@@ -536,7 +633,7 @@ int bx_gnn_forward(bx_gnn_handle h, int lo, int hi, const float* x, int n_in, fl
   if (rc != BX_OK) return rc;
   NX(cudaMemcpyAsync(y, h->yhat, (size_t)(hi - lo) * n_out * 4, cudaMemcpyDeviceToDevice, h->stream));
   NX(cudaStreamSynchronize(h->stream));
-  return BX_OK;
+  return check_tc(h);
 }
 
 int bx_gnn_gradients(bx_gnn_handle h, int lo, int hi, const float* x, int n_in, const float* y, int n_out,
@@ -550,7 +647,7 @@ int bx_gnn_gradients(bx_gnn_handle h, int lo, int hi, const float* x, int n_in, 
   NX(cudaStreamSynchronize(h->stream));
   NX(cudaMemcpy(grad_host, h->grad, bxn::NP * 4, cudaMemcpyDeviceToHost));
   if (loss_host) NX(cudaMemcpy(loss_host, h->loss, 4, cudaMemcpyDeviceToHost));
-  return BX_OK;
+  return check_tc(h);
 }
 
 int bx_gnn_train_step(bx_gnn_handle h, int lo, int hi, const float* x, int n_in, const float* y, int n_out, float lr,
@@ -570,6 +667,7 @@ int bx_gnn_train_step(bx_gnn_handle h, int lo, int hi, const float* x, int n_in,
   if (loss_host) {
     NX(cudaMemcpyAsync(loss_host, h->loss, 4, cudaMemcpyDeviceToHost, h->stream));
     NX(cudaStreamSynchronize(h->stream));
+    return check_tc(h);
   }
   return BX_OK;
 }
@@ -577,7 +675,7 @@ int bx_gnn_train_step(bx_gnn_handle h, int lo, int hi, const float* x, int n_in,
 int bx_gnn_destroy(bx_gnn_handle h) {
   if (!h) return BX_OK;
   void* ptrs[] = {h->master, h->m, h->v, h->grad, h->wb, h->ptr, h->nbr, h->ptrT, h->nbrT, h->inv_deg,
-                  h->act, h->yhat, h->dY, h->dHa, h->dHb, h->dZ, h->G, h->part, h->loss_part, h->loss};
+                  h->act, h->yhat, h->dY, h->dHa, h->dHb, h->dZ, h->G, h->part, h->loss_part, h->loss, h->err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
