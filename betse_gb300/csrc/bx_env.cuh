@@ -267,8 +267,22 @@ __global__ void __launch_bounds__(256) k_env_update_charge(double* cenv, const d
     const double* fyi = fy + (size_t)ion * e.G;
     const R div = ddx_neg<R>(fxi, e, i, j) + ddy_neg<R>(fyi, e, i, j);
     double c = cb_at(cenv, e, ion, i, j) + (double)(div * (R)e.dt);
+    // the membrane exchange: indices, then values, four at a time (the
+    // loads of a batch are independent), added in list order
     double s = 0.0;
-    for (int q = env_ptr[k]; q < env_ptr[k + 1]; ++q) s += -mem_flux_sa[(size_t)ion * M + env_mem[q]];
+    const int q1 = env_ptr[k + 1];
+    const double* mf = mem_flux_sa + (size_t)ion * M;
+    for (int q0 = env_ptr[k]; q0 < q1; q0 += 4) {
+      int mm[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) mm[u] = q0 + u < q1 ? env_mem[q0 + u] : -1;
+      double fv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) fv[u] = mm[u] >= 0 ? mf[mm[u]] : 0.0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (mm[u] >= 0) s += -fv[u];
+    }
     c = c + (s * e.inv_h_d2) * e.dt;
     cenv[(size_t)ion * e.G + k] = c;
     zc = e.zF[ion] * c;
