@@ -497,7 +497,7 @@ def config_plain250(wl, stream, flush, cpu=True):
                                       note='a 1.4k-membrane cluster fills a few dozen CTAs: bound by '
                                            'the dependent FP64 instruction chain of a lane, not by HBM',
                                       survey=survey_bytes('fp64', g.n_cells, g.n_mems)),
-           'kernel_launches_per_step': 2,
+           'kernel_launches_per_step': 1 if launch[1] == 5 else 2,   # the ion kernel mixes the environment
            'autotuned_launch': {'cta_slots': launch[0], 'kernel': 'k_cell_step_ion' if launch[1] == 5
                                 else 'k_cell_step<double>'},
            'autotune_table': table}

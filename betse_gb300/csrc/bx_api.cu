@@ -269,6 +269,8 @@ bx::StepConst make_step_const(const bx_cluster* h) {
   k.inv_cm = 1.0 / p.cm;
   k.tm = p.tm;
   k.gj_len = h->gj_len;
+  k.inv_tm = 1.0 / p.tm;
+  k.inv_gj_len = 1.0 / h->gj_len;
   k.gj_block = p.gj_block;
   k.vgj = h->vgj ? 1 : 0;
   k.gj_vth = p.gj_vthresh;

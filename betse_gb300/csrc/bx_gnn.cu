@@ -67,21 +67,35 @@ constexpr int kTcRows = 128;                         // nodes per CTA (the MMA's
 constexpr int kTcThreads = 128;                      // four warps: TMEM lanes 32 w .. 32 w + 31
 constexpr int kActTile = kTcRows * W * 2;            // 16 KB of BF16
 constexpr int kWTile = W * W * 2;                    // 8 KB
-constexpr int kTcSmem = 2 * (kActTile + kWTile) + 1024;
+constexpr int kTcSmem = 2 * (kActTile + kWTile) + 1024;   // two inputs (MODE 1)
+constexpr int kTcSmem1 = kActTile + kWTile + 1024;        // one input (MODE 0, 2)
 // kind::f16: FP32 accumulator, BF16 A and B, both K-major, N = 64, M = 128
 constexpr uint32_t kIdescFwd = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(W >> 3) << 17) |
                                ((uint32_t)(kTcRows >> 4) << 24);
 
-// Rows [0, rows) of a row-major [*][64] BF16 array into a tile in the
-// canonical no-swizzle K-major layout: 8 x 16-byte core matrices, the 8
-// K-adjacent cores of an 8-row group contiguous (128 B apart), 8-row groups
-// 1024 B apart; rows at or past `valid` are zero.
-__device__ __forceinline__ void stage_tile(uint8_t* tile, const bf16* __restrict__ src, int rows, int valid) {
-  for (int e = threadIdx.x; e < rows * 8; e += blockDim.x) {
-    const int r = e >> 3, c = e & 7;
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (r < valid) v = reinterpret_cast<const uint4*>(src + (size_t)r * W)[c];
-    *reinterpret_cast<uint4*>(tile + ((r >> 3) * 8 + c) * 128 + (r & 7) * 16) = v;
+// A tile of ROWS rows of a row-major [*][64] BF16 array is ROWS * 8 pieces of
+// 16 bytes; thread t holds pieces t, t + 128, ...  All of a thread's loads
+// are issued before any store, so a tile costs one memory round trip.
+template <int ROWS>
+__device__ __forceinline__ void load_rows(uint4 (&v)[ROWS * 8 / kTcThreads], const bf16* __restrict__ src,
+                                          int valid) {
+  static_assert(ROWS * 8 % kTcThreads == 0, "whole pieces per thread");
+#pragma unroll
+  for (int j = 0; j < ROWS * 8 / kTcThreads; ++j) {
+    const int e = (int)threadIdx.x + j * kTcThreads, r = e >> 3, c = e & 7;
+    v[j] = r < valid ? reinterpret_cast<const uint4*>(src + (size_t)r * W)[c] : make_uint4(0u, 0u, 0u, 0u);
+  }
+}
+
+// The pieces into the canonical no-swizzle K-major layout: 8 x 16-byte core
+// matrices, the 8 K-adjacent cores of an 8-row group contiguous (128 B
+// apart), 8-row groups 1024 B apart; rows at or past `valid` are zero.
+template <int ROWS>
+__device__ __forceinline__ void store_rows(uint8_t* tile, const uint4 (&v)[ROWS * 8 / kTcThreads]) {
+#pragma unroll
+  for (int j = 0; j < ROWS * 8 / kTcThreads; ++j) {
+    const int e = (int)threadIdx.x + j * kTcThreads, r = e >> 3, c = e & 7;
+    *reinterpret_cast<uint4*>(tile + ((r >> 3) * 8 + c) * 128 + (r & 7) * 16) = v[j];
   }
 }
 
@@ -109,11 +123,24 @@ __global__ void __launch_bounds__(kTcThreads) k_fwd_tc(int n, const bf16* __rest
   const int r0 = blockIdx.x * kTcRows;
   const int valid = min(kTcRows, n - r0);
 
-  stage_tile(a1, in1 + (size_t)r0 * W, kTcRows, valid);
-  stage_tile(b1, wb + off_w1, W, W);
   if (MODE == 1) {
-    stage_tile(a2, in2 + (size_t)r0 * W, kTcRows, valid);
-    stage_tile(b2, wb + off_w2, W, W);
+    // both activation tiles in one round trip, then both weight tiles (L2-resident)
+    uint4 va[kTcRows * 8 / kTcThreads], vb[kTcRows * 8 / kTcThreads];
+    load_rows<kTcRows>(va, in1 + (size_t)r0 * W, valid);
+    load_rows<kTcRows>(vb, in2 + (size_t)r0 * W, valid);
+    store_rows<kTcRows>(a1, va);
+    store_rows<kTcRows>(a2, vb);
+    uint4 w1[W * 8 / kTcThreads], w2[W * 8 / kTcThreads];
+    load_rows<W>(w1, wb + off_w1, W);
+    load_rows<W>(w2, wb + off_w2, W);
+    store_rows<W>(b1, w1);
+    store_rows<W>(b2, w2);
+  } else {
+    uint4 va[kTcRows * 8 / kTcThreads], w1[W * 8 / kTcThreads];
+    load_rows<kTcRows>(va, in1 + (size_t)r0 * W, valid);
+    load_rows<W>(w1, wb + off_w1, W);
+    store_rows<kTcRows>(a1, va);
+    store_rows<W>(b1, w1);
   }
   // the tensor core reads shared memory through the async proxy
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -160,7 +187,9 @@ __global__ void __launch_bounds__(kTcThreads) k_fwd_tc(int n, const bf16* __rest
 #pragma unroll
       for (int f = 0; f < W; ++f) v[f] += master[off_b + f];
       if (MODE == 2) {
-        for (int f = 0; f < n_out; ++f) outY[(size_t)r * n_out + f] = v[f];
+#pragma unroll
+        for (int f = 0; f < W; ++f)           // constant indices keep v in registers
+          if (f < n_out) outY[(size_t)r * n_out + f] = v[f];
       } else {
 #pragma unroll
         for (int f8 = 0; f8 < W; f8 += 8) {
@@ -476,7 +505,7 @@ int forward(bx_gnn* h, int lo, int hi, const float* x, int n_in, int n_out) {
   k_pack_x<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, n_in, x, plane(h, P_X));
   const unsigned g = node_grid(n);
   const unsigned gt = (unsigned)((n + kTcRows - 1) / kTcRows);
-  k_fwd_tc<0><<<gt, kTcThreads, kTcSmem, s>>>(n, plane(h, P_X), nullptr, h->wb, OFF_W0, 0, h->master, OFF_B0,
+  k_fwd_tc<0><<<gt, kTcThreads, kTcSmem1, s>>>(n, plane(h, P_X), nullptr, h->wb, OFF_W0, 0, h->master, OFF_B0,
                                               nullptr, plane(h, P_H0), nullptr, 0, h->err);
   for (int l = 0; l < NMP; ++l) {
     const int o = OFF_MP + l * MP_STRIDE;
@@ -485,7 +514,7 @@ int forward(bx_gnn* h, int lo, int hi, const float* x, int n_in, int n_out) {
                                                 h->master, o + 2 * W * W, plane(h, P_R1 + l), plane(h, P_H1 + l),
                                                 nullptr, 0, h->err);
   }
-  k_fwd_tc<2><<<gt, kTcThreads, kTcSmem, s>>>(n, plane(h, P_H3), nullptr, h->wb, OFF_WD, 0, h->master, OFF_BD,
+  k_fwd_tc<2><<<gt, kTcThreads, kTcSmem1, s>>>(n, plane(h, P_H3), nullptr, h->wb, OFF_WD, 0, h->master, OFF_BD,
                                               nullptr, nullptr, h->yhat, n_out, h->err);
   NX(cudaGetLastError());
   return BX_OK;

@@ -58,6 +58,7 @@ struct StepConst {
   double dgj_gs[kMaxIons]; // D_gj * gj_surface
   double F_RT;             // F / (R T)
   double dt, inv_cm, tm, gj_len;
+  double inv_tm, inv_gj_len;  // 1/tm, 1/gj_len (IEEE divisions on the host: the bits a device division gives)
   double gj_block;
   double inv_KmNa, inv_KmK, atp_term; // 1/Km, (cATP/KmATP)
   double atp_den;          // 1 + cATP/KmATP
@@ -221,8 +222,8 @@ k_cell_step(DevGeom g, StepPtrs p, StepConst k) {
   const int t = threadIdx.x;
   const int m = m0 + t;
   const bool active = m < m1;
-  const T inv_tm = (T)(1.0 / k.tm);
-  const T inv_gjl = (T)(1.0 / k.gj_len);
+  const T inv_tm = (T)k.inv_tm;
+  const T inv_gjl = (T)k.inv_gj_len;
 
   double env_acc[kMaxIons];
 #pragma unroll
@@ -497,8 +498,11 @@ struct EnvMix {
 // k_cell_step spends ~3200 FP64-heavy instructions per thread on a few
 // dozen SMs, and an FP64 warp instruction costs the same whatever the
 // number of lanes it uses; here the work is spread and no lane idles:
-//   A. one lane per membrane: the shared exponentials of the membrane and
-//      gap-junction voltages and the Na/K-ATPase rate, into shared memory;
+//   A. four jobs per membrane, each in its own warp where the CTA has
+//      four: the shared exponentials of the membrane voltage; those of the
+//      gap-junction voltage; the Na/K-ATPase rate (with its own copy of
+//      exp(-alpha1), the same bits); the geometry loads and 1/cell_vol of
+//      the CTA's cells;
 //   B. eight lanes per membrane slot, lane i = ion i: the transmembrane and
 //      gap-junction GHK fluxes of that ion;
 //   C. eight lanes per cell, lane i = ion i: the concentration update, and
@@ -516,6 +520,7 @@ k_cell_step_ion(DevGeom g, StepPtrs p, StepConst k, EnvMix em) {
   __shared__ double sV[MB];             // per-cell Vmem (by local cell)
   __shared__ double sh_m[5][MB], sh_g[5][MB];   // GhkShared {a1, em1, e1, r, q2} of vm and vgj
   __shared__ double sh_v1[MB], sh_vg1[MB], sh_na[MB], sh_sa[MB], sh_gw[MB];
+  __shared__ double sh_ivol[MB];        // 1/cell_vol by local cell
   __shared__ int sh_c[MB], sh_cn[MB], sh_bnd[MB];
   __shared__ int s_last;
   const int I = k.I;
@@ -527,33 +532,49 @@ k_cell_step_ion(DevGeom g, StepPtrs p, StepConst k, EnvMix em) {
   const int nmem = m1 - m0;
   const int t = threadIdx.x;
 
-  // ---- A: per membrane
-  if (t < nmem) {
-    const int m = m0 + t;
-    const double v = p.vm_in[m];
-    const int c = g.m2c[m];
-    const double vn = p.vm_in[g.nn[m]];
-    const double v1 = v + kNonce;
-    const double vgj = (vn + kNonce) - v1;       // update_gj, sim.py:2166
-    const double vgj1 = vgj + kNonce;
-    GhkShared<double> sm, sg;
-    sm.init(v1, k.F_RT);
-    sg.init(vgj1, k.F_RT);
-    sh_m[0][t] = sm.a1; sh_m[1][t] = sm.em1; sh_m[2][t] = sm.e1; sh_m[3][t] = sm.r; sh_m[4][t] = sm.q2;
-    sh_g[0][t] = sg.a1; sh_g[1][t] = sg.em1; sh_g[2][t] = sg.e1; sh_g[3][t] = sg.r; sh_g[4][t] = sg.q2;
-    sh_v1[t] = v1;
-    sh_vg1[t] = vgj1;
-    double fNa = 0.0;
-    const double pcoef = p.pump_coef[cl];
-    if (pcoef != 0.0)                            // Na/K-ATPase (sim.py:1196-1234)
-      fNa = pump_fna<double>(k, pcoef, sm.e1, p.ccm_in[k.iNa * g.C + c], cenv_cl[k.iNa],
-                             p.ccm_in[k.iK * g.C + c], cenv_cl[k.iK]);
-    sh_na[t] = fNa;
-    sh_sa[t] = g.mem_sa[m];
-    sh_gw[t] = g.gj_w[m];
-    sh_c[t] = c;
-    sh_cn[t] = g.nn_cell[m];
-    sh_bnd[t] = g.bflag[m] != 0;
+  // ---- A: job q of membrane slot e, q = entry / MP (one warp per job when MB <= 32)
+  constexpr int MP = (MB + 31) / 32 * 32;
+  const int ncell = c1 - c0;
+  for (int entry = t; entry < 4 * MP; entry += MB * 8) {
+    const int q = entry / MP, e = entry - q * MP;
+    const int m = m0 + e;
+    if (q < 3 && e >= nmem) continue;
+    if (q == 0) {
+      const double v1 = p.vm_in[m] + kNonce;
+      GhkShared<double> sm;
+      sm.init(v1, k.F_RT);
+      sh_m[0][e] = sm.a1; sh_m[1][e] = sm.em1; sh_m[2][e] = sm.e1; sh_m[3][e] = sm.r; sh_m[4][e] = sm.q2;
+      sh_v1[e] = v1;
+    } else if (q == 1) {
+      const double v1 = p.vm_in[m] + kNonce;
+      const double vn = p.vm_in[g.nn[m]];
+      const double vgj = (vn + kNonce) - v1;     // update_gj, sim.py:2166
+      const double vgj1 = vgj + kNonce;
+      GhkShared<double> sg;
+      sg.init(vgj1, k.F_RT);
+      sh_g[0][e] = sg.a1; sh_g[1][e] = sg.em1; sh_g[2][e] = sg.e1; sh_g[3][e] = sg.r; sh_g[4][e] = sg.q2;
+      sh_vg1[e] = vgj1;
+    } else if (q == 2) {
+      double fNa = 0.0;
+      const double pcoef = p.pump_coef[cl];
+      if (pcoef != 0.0) {                        // Na/K-ATPase (sim.py:1196-1234)
+        const int c = g.m2c[m];
+        const double a1 = (p.vm_in[m] + kNonce) * k.F_RT;   // GhkShared::init's e1
+        const double e1 = 1.0 + bx_expm1<double>(-a1);
+        fNa = pump_fna<double>(k, pcoef, e1, p.ccm_in[k.iNa * g.C + c], cenv_cl[k.iNa],
+                               p.ccm_in[k.iK * g.C + c], cenv_cl[k.iK]);
+      }
+      sh_na[e] = fNa;
+    } else {
+      if (e < nmem) {
+        sh_sa[e] = g.mem_sa[m];
+        sh_gw[e] = g.gj_w[m];
+        sh_c[e] = g.m2c[m];
+        sh_cn[e] = g.nn_cell[m];
+        sh_bnd[e] = g.bflag[m] != 0;
+      }
+      if (e < ncell) sh_ivol[e] = 1.0 / g.cell_vol[c0 + e];
+    }
   }
   __syncthreads();
 
@@ -572,12 +593,12 @@ k_cell_step_ion(DevGeom g, StepPtrs p, StepConst k, EnvMix em) {
     const double cin = p.ccm_in[i * g.C + c];
     const double cout = cenv_cl[i];
     const double dm = p.Dm[(size_t)i * g.M + m];
-    double f = ghk_flux<double>(sm, k.zcode[i], k.z[i], sh_v1[slot], k.F_RT, cout, cin, dm, 1.0 / k.tm);
+    double f = ghk_flux<double>(sm, k.zcode[i], k.z[i], sh_v1[slot], k.F_RT, cout, cin, dm, k.inv_tm);
     if (i == k.iNa) f = fNa + f;
     else if (i == k.iK) f = -(2.0 / 3.0) * fNa + f;
     const double cn_i = p.ccm_in[i * g.C + cn];
     const double dgj = k.dgj_gs[i] * (sh_gw[slot] * k.gj_block);
-    double fg = ghk_flux<double>(sg, k.zcode[i], k.z[i], sh_vg1[slot], k.F_RT, cin, cn_i, dgj, 1.0 / k.gj_len);
+    double fg = ghk_flux<double>(sg, k.zcode[i], k.z[i], sh_vg1[slot], k.F_RT, cin, cn_i, dgj, k.inv_gj_len);
     if (sh_bnd[slot]) fg = 0.0;
     sA[i][slot] = f * msa;
     sB[i][slot] = -fg * msa;
@@ -592,13 +613,12 @@ k_cell_step_ion(DevGeom g, StepPtrs p, StepConst k, EnvMix em) {
   }
 
   // ---- C: lane i of group c, ion i of cell c0 + c
-  const int ncell = c1 - c0;
   const int lc = t >> 3;
   double x = 0.0;
   if (lc < ncell && i < I) {
     const int cc = c0 + lc;
     const int a0 = g.cell_ptr[cc] - m0, a1 = g.cell_ptr[cc + 1] - m0;
-    const double inv_vol = 1.0 / g.cell_vol[cc];
+    const double inv_vol = sh_ivol[lc];
     double s1 = 0.0, s2 = 0.0;
     for (int j = a0; j < a1; ++j) { s1 += sA[i][j]; s2 += sB[i][j]; }
     x = p.cc[i * g.C + cc] + (s1 * inv_vol) * k.dt;   // update_Co, sim_toolbox.py:1182-1183

@@ -255,6 +255,7 @@ extern "C" int bx_step_fp64_noalloc(const bx_geom* g, const bx_params* p, const 
     k.dgj_gs[i] = p->D_gj[i] * p->gj_surface;
   }
   k.F_RT = p->F / RT; k.dt = p->dt; k.inv_cm = 1.0 / p->cm; k.tm = p->tm; k.gj_len = g->gj_len;
+  k.inv_tm = 1.0 / p->tm; k.inv_gj_len = 1.0 / g->gj_len;
   k.gj_block = p->gj_block; k.inv_KmNa = 1.0 / p->KmNK_Na; k.inv_KmK = 1.0 / p->KmNK_K;
   k.atp_term = p->cATP / p->KmNK_ATP; k.atp_den = 1.0 + p->cATP / p->KmNK_ATP;
   k.qnum_c = (p->cADP * 1e-3) * (p->cPi * 1e-3); k.qden_c = p->cATP * 1e-3;

@@ -255,28 +255,6 @@ def test_voltage_gated_gj_state_round_trip_and_autotune(precision):
         assert gi.rel_err(sa[k], sb[k]) <= tol, k
 
 
-@pytest.mark.parametrize('tpb,kernel', [(16, 0), (32, 0), (64, 0), (128, 0), (256, 0), (16, 5), (32, 5),
-                                        (64, 5)])
-def test_fp64_cta_sizes_match_betse(tpb, kernel):
-    """Every CTA size of the plain FP64 kernel, and the small-cluster kernel
-    (5: lanes per ion, the environment mixed by the last CTA), reproduces
-    BETSE's state at every checkpoint."""
-    d = gi.load('noecm_r80_s1')
-    with _engine(d, 'fp64') as eng:
-        eng.set_launch_config(tpb, kernel)
-        done = 0
-        for cp in d['meta_checkpoints']:
-            eng.step(int(cp - done))
-            done = int(cp)
-            eng.check_stable()
-            s = eng.download()
-            ok, e_vm, bound = gi.vm_err_ok(d, s['vm'], d[f's{cp}_vm'], d[f's{cp}_cc_cells'])
-            assert ok, (tpb, cp, e_vm, bound)
-            assert gi.rel_err(s['cc_cells'], d[f's{cp}_cc_cells']) < TOL_FP64, (tpb, cp)
-            assert _cmp_env(s['cc_env'], d[f's{cp}_cc_env'], False) < TOL_FP64, (tpb, cp)
-        assert eng.launch_config() == (tpb, kernel)
-
-
 @pytest.mark.parametrize('precision', ['fp64', 'split'])
 def test_upload_checks_and_download_into_given_arrays(precision):
     """The device-side upload checks refuse what BETSE's layouts cannot hold
