@@ -458,6 +458,81 @@ def roofline_entry(bytes_per_step, s_per_step, kernel, note=None, survey=None):
     return r
 
 
+_FP64_PEAK = {}
+
+
+def fp64_peak(stream, best_of=5):
+    """The FP64 pipe's measured peak on this GPU: the probe kernel
+    (bx_fp64_fma_probe: 8 CTAs of 256 threads per SM, 8 independent FMA
+    chains per thread) timed with CUDA events on `stream`, best of `best_of`
+    launches after two warm-ups.  Cached per process."""
+    if 'peak' in _FP64_PEAK:
+        return _FP64_PEAK['peak']
+    import ctypes as ct
+    import torch
+    from betse_gb300 import _lib
+    lib = _lib.load()
+    n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    n_blocks, iters = 8 * n_sm, 2048
+    out = torch.empty(n_blocks * 256, dtype=torch.float64, device='cuda')
+
+    def run():
+        rc = lib.bx_fp64_fma_probe(n_blocks, iters, 1.0, 1.0, ct.c_void_p(out.data_ptr()),
+                                   ct.c_void_p(stream.cuda_stream))
+        if rc != _lib.BX_OK:
+            raise RuntimeError('bx_fp64_fma_probe: ' + lib.bx_last_error().decode())
+    for _ in range(2):
+        run()
+    best = float('inf')
+    for _ in range(best_of):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        run()
+        b.record(stream)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    warp_fma = n_blocks * 64 * iters
+    _FP64_PEAK['peak'] = {'warp_inst_per_s': warp_fma / (best / 1e3),
+                          'fma_tflops': warp_fma * 32 * 2 / (best / 1e3) / 1e12, 'ms': best,
+                          'launch': f'{n_blocks} CTAs x 256 threads, 8 FMA chains x {iters} per thread'}
+    return _FP64_PEAK['peak']
+
+
+def fp64_roofline(kernel_ms, n_mems, peak, kernel, workload):
+    """The FP64-pipe roofline of a plain-form kernel: its FP64 warp
+    instructions per launch (ncu's sm__inst_executed_pipe_fp64.sum, from the
+    committed capture in profiles/fp64_counts.json, per membrane, scaled to
+    this workload's membranes) over its measured time per launch, against
+    the probe's FP64 warp-instruction rate.  An FP64 warp instruction holds
+    the pipe the same whatever the number of active lanes, so `frac` is the
+    share of the kernel's time its FP64 work needs at the pipe's peak."""
+    r = {'bound': 'fp64', 'unit': 'G FP64 warp-instructions/s', 'peak': peak['warp_inst_per_s'] / 1e9,
+         'peak_fma_tflops': peak['fma_tflops'], 'peak_source': 'measured: ' + peak['launch'],
+         'kernel': kernel, 'ms_per_launch': kernel_ms}
+    path = os.path.join(ROOT, 'profiles', 'fp64_counts.json')
+    counts = json.load(open(path)).get('kernels', {}).get(workload, {}) if os.path.exists(path) else {}
+    entry, counted = counts.get(kernel), kernel
+    if entry is None and kernel.startswith('k_cell_step<double>'):
+        # another tile size of the same kernel: every thread runs the same
+        # code per membrane slot, so its count per membrane stands in
+        for name, e in counts.items():
+            if name.startswith('k_cell_step<double>'):
+                entry, counted = e, name
+                break
+    if entry is None:
+        r.update(achieved=None, frac=None, note='no FP64 instruction count captured for this kernel')
+        return r
+    per_mem = entry['fp64_warp_inst_per_launch'] / entry['membranes']
+    inst = per_mem * n_mems
+    a = inst / (kernel_ms / 1e3) / 1e9
+    r.update(achieved=a, frac=a / r['peak'], fp64_warp_inst_per_launch=int(inst),
+             fp64_warp_inst_per_membrane=per_mem, count_source='profiles/fp64_counts.json')
+    if counted != kernel:
+        r['count_of'] = counted + ' (per membrane)'
+    return r
+
+
 def timed_run_ms(eng, T, stream, flush, reps=3):
     """Best of `reps` runs of T time steps on `stream` (CUDA events), the L2
     flushed before each; one untimed run first."""
@@ -502,6 +577,8 @@ def config_plain250(wl, stream, flush, cpu=True):
                                 else 'k_cell_step<double>'},
            'autotune_table': table}
     out['roofline']['kernel'] = out['autotuned_launch']['kernel']
+    kname = f"k_cell_step_ion<{launch[0]}>" if launch[1] == 5 else f"k_cell_step<double> ({launch[0]} slots)"
+    out['roofline_fp64'] = fp64_roofline(kms, g.n_mems, fp64_peak(stream), kname, 'plain250')
     if cpu:
         out['cpu_baseline'] = cpu_baseline(g, p, Dm, st, budget_s=6.0)
     return out
@@ -742,10 +819,16 @@ def profile_kernel(which):
     sides (two warm-up launches, then the captured one); 'fields' --
     k_dense_rows2_df on a 12000 x 12000 double-float operator; 'network' --
     the four-substance network alone on the 100k-cell cluster (three warm-up
-    steps, then k_net_cell and k_net_gj once each)."""
+    steps, then k_net_cell and k_net_gj once each); 'fp64' -- the FP64 probe
+    kernel as fp64_peak launches it (two warm-ups, five timed)."""
     from betse_gb300.build import build
     build()
-    if which == 'network':
+    if which == 'fp64':
+        import torch
+        s = torch.cuda.Stream()
+        pk = fp64_peak(s)
+        print(f"FP64 probe: {pk['fma_tflops']:.3f} TFLOP/s ({pk['launch']}, {pk['ms']:.3f} ms)")
+    elif which == 'network':
         from betse_gb300.engine import ClusterEngine
         from betse_gb300.network import Network, NetworkSpec
         w, g, p, Dm, st, _ = build_workload('cluster100k')
@@ -847,7 +930,7 @@ def main():
     ap.add_argument('--launch', default=None,
                     help='with --profile-run: membrane slots per tile, suffix p persistent, f factored '
                          '(optionally followed by its variant, e.g. 256f12), r resident, q pipelined (e.g. 192r)')
-    ap.add_argument('--profile-kernel', choices=['gemm', 'fields', 'network'],
+    ap.add_argument('--profile-kernel', choices=['gemm', 'fields', 'network', 'fp64'],
                     help='for ncu: run a small case of one dense-product kernel and exit')
     args = ap.parse_args()
     if args.profile_kernel:
@@ -935,6 +1018,8 @@ def main():
     ms_plain, _ = timed_runs(plain, 1, 1)
     split.check_stable()
     plain.check_stable()
+    # the plain kernel alone, for its FP64 roofline (the state is re-uploaded below)
+    kms_plain = None if sweep else plain.time_cell_kernel(10)
 
     t_max, value = job_throughput(sum(ms_split) / 1e3, n_mems * T * args.steps, world, dist, dev)
     plain_value = n_mems * T * len(ms_plain) / (sum(ms_plain) / 1e3)
@@ -1049,7 +1134,10 @@ def main():
                            'ms_per_step': sum(ms_plain) / len(ms_plain),
                            'speedup_split_vs_plain': value / world / plain_value,
                            'vm_max_abs_err_V': vm_err, 'vm_err_after_steps': T,
-                           'vm_err_curve_V': curve},
+                           'vm_err_curve_V': curve,
+                           'roofline_fp64': None if kms_plain is None else fp64_roofline(
+                               kms_plain, n_mems, fp64_peak(stream),
+                               f'k_cell_step<double> ({tune_plain[0]} slots)', args.workload)},
             'roofline': roof,
             'cpu_baseline': cpu,
             'e2e': {'value': e2e_val, 'unit': UNIT, 'h2d_bytes_per_step': int(h2d),

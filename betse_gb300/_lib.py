@@ -203,6 +203,7 @@ SIGNATURES = {
     'bx_cluster_info': (ct.c_int, [ct.c_void_p, _ip]),
     'bx_time_cell_kernel': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_double)]),
     'bx_cell_kernel_bytes': (ct.c_int64, [ct.c_void_p]),
+    'bx_fp64_fma_probe': (ct.c_int, [ct.c_int, ct.c_int, ct.c_double, ct.c_double, ct.c_void_p, ct.c_void_p]),
     'bx_set_launch_config': (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int]),
     'bx_get_launch_config': (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int)]),
     'bx_autotune': (ct.c_int, [ct.c_void_p, ct.c_int, ct.POINTER(ct.c_int), ct.POINTER(ct.c_double)]),

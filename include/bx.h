@@ -389,6 +389,15 @@ int bx_time_cell_kernel(bx_handle h, int n, double* ms_per_launch);
  * counted once at its stored width; reads plus writes). */
 int64_t bx_cell_kernel_bytes(bx_handle h);
 
+/* FP64 throughput probe (no counterpart in the reference: it measures the
+ * FP64 pipe that bounds the plain form's step).  Launches n_blocks CTAs of
+ * 256 threads on `stream`; each thread runs 8 independent chains of `iters`
+ * FMAs a = fma(a, b, c) from a = thread index + chain index and writes the
+ * sum of its chains to out[thread index] (out: n_blocks * 256 doubles on
+ * the device).  The launch issues n_blocks * 64 * iters FP64 warp FMAs;
+ * the caller times it.  Asynchronous; BX_EINVAL on bad arguments. */
+int bx_fp64_fma_probe(int n_blocks, int iters, double b, double c, double* out, void* stream);
+
 /* No-allocation step.  No counterpart in the reference (BETSE has no device
  * memory); it serves callers that cannot allocate GPU memory while they step,
  * e.g. a host framework that owns every device buffer through its own pool,

@@ -93,6 +93,14 @@ def test_create_rejects_bad_geometry(lib):
     assert 'iNa' in _expect_einval(lib, cg, sp2)
 
 
+def test_fp64_probe_rejects_bad_arguments(lib):
+    from betse_gb300 import _lib
+    assert lib.bx_fp64_fma_probe(0, 10, 1.0, 1.0, ct.c_void_p(16), None) == _lib.BX_EINVAL
+    assert lib.bx_fp64_fma_probe(4, 0, 1.0, 1.0, ct.c_void_p(16), None) == _lib.BX_EINVAL
+    assert lib.bx_fp64_fma_probe(4, 10, 1.0, 1.0, None, None) == _lib.BX_EINVAL
+    assert b'bad arguments' in lib.bx_last_error()
+
+
 def test_geometry_rejects_noncontiguous_cells():
     from betse_gb300.cluster import ClusterGeometry
     d = gi.load('noecm_r20_s2')
