@@ -427,7 +427,7 @@ def batch_fields_timing(n_clusters=128):
                     'BF16x3 tcgen05 GEMM with a per-column delta^2 and one FP64 refinement'}
 
 
-def survey_bytes(form, C, M, G=0, ecm=False):
+def step_bytes(form, C, M, G=0, ecm=False):
     """Algorithmic bytes of one time step by the per-array count BETSE's step
     implies (each array once at its stored width, reads plus writes): plain
     FP64 104 B per membrane + 124 B per cell; split form 64 + 112; with
@@ -439,18 +439,18 @@ def survey_bytes(form, C, M, G=0, ecm=False):
     return b
 
 
-def roofline_entry(bytes_per_step, s_per_step, kernel, note=None, survey=None):
+def roofline_entry(bytes_per_step, s_per_step, kernel, note=None, step=None):
     """achieved = algorithmic bytes per time step / time per step.  With
-    `survey` (the per-membrane count of survey_bytes, the step's algorithmic
+    `step` (the per-membrane count of step_bytes, the step's algorithmic
     bytes by definition) that count is the one `achieved` and `frac` use;
     the bytes the chosen kernel's own layout reads and writes stand beside
     it (kernel_bytes_per_step, frac_on_kernel_bytes)."""
     hbm, src = peaks()
-    algo = bytes_per_step if survey is None else survey
+    algo = bytes_per_step if step is None else step
     a = algo / s_per_step / 1e9
     r = {'bound': 'hbm', 'achieved': a, 'peak': hbm, 'unit': 'GB/s', 'frac': a / hbm,
          'algorithmic_bytes_per_step': int(algo), 'kernel': kernel, 'peak_source': src}
-    if survey is not None:
+    if step is not None:
         r['kernel_bytes_per_step'] = int(bytes_per_step)
         r['frac_on_kernel_bytes'] = bytes_per_step / s_per_step / 1e9 / hbm
     if note:
@@ -571,7 +571,7 @@ def config_plain250(wl, stream, flush, cpu=True):
            'roofline': roofline_entry(kb, kms / 1e3, 'k_cell_step<double>',
                                       note='a 1.4k-membrane cluster fills a few dozen CTAs: bound by '
                                            'the dependent FP64 instruction chain of a lane, not by HBM',
-                                      survey=survey_bytes('fp64', g.n_cells, g.n_mems)),
+                                      step=step_bytes('fp64', g.n_cells, g.n_mems)),
            'kernel_launches_per_step': 1 if launch[1] == 5 else 2,   # the ion kernel mixes the environment
            'autotuned_launch': {'cta_slots': launch[0], 'kernel': 'k_cell_step_ion' if launch[1] == 5
                                 else 'k_cell_step<double>'},
@@ -600,7 +600,7 @@ def config_ecm20k(wl, stream, flush, cpu=True):
             e.upload(**st)
             e.autotune(5)
             ms = timed_run_ms(e, T, stream, flush)
-        sv = survey_bytes(prec, g.n_cells, g.n_mems, G, ecm=True)
+        sv = step_bytes(prec, g.n_cells, g.n_mems, G, ecm=True)
         out[prec] = {'value': g.n_mems * T / (ms / 1e3), 'unit': UNIT, 'ms_per_run': ms,
                      'ms_per_time_step': ms / T,
                      'roofline': roofline_entry(sv, ms / 1e3 / T, 'whole step (cell kernel + grid stencils)',
@@ -631,7 +631,7 @@ def config_sweep512(wl, stream, flush, cpu=True):
     out = {'workload': w['desc'], 'clusters': len(gs), 'cells': C, 'membranes': M, 'time_steps_per_run': T,
            'form': 'split', 'value': M * T / (ms / 1e3), 'unit': UNIT, 'ms_per_run': ms,
            'autotuned': {'tpb': tpb, 'kernel': kname}, 'autotune_table': table,
-           'roofline': roofline_entry(kb, kms / 1e3, kname, survey=survey_bytes('split', C, M),
+           'roofline': roofline_entry(kb, kms / 1e3, kname, step=step_bytes('split', C, M),
                                       note='algorithmic bytes of the split step (64 B per membrane + 112 B per '
                                            'cell); kernel_bytes_per_step is what the factored layout moves (one '
                                            'sum of Dm*mem_sa per cell instead of Dm per membrane)')}
@@ -1048,7 +1048,7 @@ def main():
     if os.path.exists(tp):
         tj = json.load(open(tp))
         traffic = int(tj.get('dram_bytes_per_step', tj.get('dram_bytes_per_launch')) * n_mems / tj['membranes'])
-    roof = roofline_entry(kbytes, kern_ms / 1e3, kname, survey=survey_bytes('split', n_cells, n_mems),
+    roof = roofline_entry(kbytes, kern_ms / 1e3, kname, step=step_bytes('split', n_cells, n_mems),
                           note='achieved = the split step\'s algorithmic bytes per time step (64 B per membrane '
                                '+ 112 B per cell: each per-membrane and per-cell array once at its stored width) '
                                '/ the chosen kernel\'s time per step; kernel_bytes_per_step is what the factored '
