@@ -38,7 +38,8 @@ __global__ void __launch_bounds__(kThreads) k_fp64_fma(int iters, double b, doub
 }  // namespace
 
 extern "C" int bx_fp64_fma_probe(int n_blocks, int iters, double b, double c, double* out, void* stream) {
-  if (n_blocks <= 0 || iters <= 0 || !out) {
+  // thread indices are int: at most 2^22 CTAs of 256 threads
+  if (n_blocks <= 0 || n_blocks > (1 << 22) || iters <= 0 || !out) {
     bx_record_error("bx_fp64_fma_probe: bad arguments");
     return BX_EINVAL;
   }

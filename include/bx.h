@@ -395,7 +395,8 @@ int64_t bx_cell_kernel_bytes(bx_handle h);
  * FMAs a = fma(a, b, c) from a = thread index + chain index and writes the
  * sum of its chains to out[thread index] (out: n_blocks * 256 doubles on
  * the device).  The launch issues n_blocks * 64 * iters FP64 warp FMAs;
- * the caller times it.  Asynchronous; BX_EINVAL on bad arguments. */
+ * the caller times it.  Asynchronous; BX_EINVAL on bad arguments
+ * (n_blocks outside [1, 2^22], iters < 1, out NULL). */
 int bx_fp64_fma_probe(int n_blocks, int iters, double b, double c, double* out, void* stream);
 
 /* No-allocation step.  No counterpart in the reference (BETSE has no device

@@ -98,6 +98,7 @@ def test_fp64_probe_rejects_bad_arguments(lib):
     assert lib.bx_fp64_fma_probe(0, 10, 1.0, 1.0, ct.c_void_p(16), None) == _lib.BX_EINVAL
     assert lib.bx_fp64_fma_probe(4, 0, 1.0, 1.0, ct.c_void_p(16), None) == _lib.BX_EINVAL
     assert lib.bx_fp64_fma_probe(4, 10, 1.0, 1.0, None, None) == _lib.BX_EINVAL
+    assert lib.bx_fp64_fma_probe((1 << 22) + 1, 10, 1.0, 1.0, ct.c_void_p(16), None) == _lib.BX_EINVAL
     assert b'bad arguments' in lib.bx_last_error()
 
 
